@@ -1,0 +1,77 @@
+"""Minimal FITS primary-HDU image reader/writer (numpy only).
+
+Imfit reads and writes FITS images through CFITSIO (reference
+core/image_io.cpp:241-375).  This module covers what the model-image path
+needs: a 2-D primary (or first image-extension) HDU with BITPIX 8/16/32/-32/-64,
+BSCALE/BZERO, returned as a float64 array indexed [row, column] with rows
+counted from the bottom of the image (the order Imfit's pixel vectors use).
+"""
+import numpy as np
+
+_BLOCK = 2880
+_DT = {8: ">u1", 16: ">i2", 32: ">i4", 64: ">i8", -32: ">f4", -64: ">f8"}
+
+
+def _parse_header(raw, pos):
+    cards = {}
+    while True:
+        block = raw[pos:pos + _BLOCK]
+        if len(block) < _BLOCK:
+            raise ValueError("truncated FITS header")
+        pos += _BLOCK
+        done = False
+        for i in range(0, _BLOCK, 80):
+            card = block[i:i + 80].decode("ascii", errors="replace")
+            key = card[:8].strip()
+            if key == "END":
+                done = True
+                break
+            if card[8:10] == "= ":
+                val = card[10:].split("/")[0].strip()
+                if val.startswith("'"):
+                    val = val.strip("'").strip()
+                else:
+                    try:
+                        val = int(val)
+                    except ValueError:
+                        try:
+                            val = float(val.replace("D", "E"))
+                        except ValueError:
+                            pass
+                cards[key] = val
+        if done:
+            return cards, pos
+
+
+def read_image(path):
+    """Return (float64 array [nrows, ncols], header dict) of the first 2-D image HDU."""
+    with open(path, "rb") as f:
+        raw = f.read()
+    pos = 0
+    while pos < len(raw):
+        hdr, pos = _parse_header(raw, pos)
+        naxis = int(hdr.get("NAXIS", 0))
+        bitpix = int(hdr["BITPIX"])
+        dims = [int(hdr.get(f"NAXIS{i + 1}", 0)) for i in range(naxis)]
+        nbytes = abs(bitpix) // 8 * (int(np.prod(dims)) if naxis else 0)
+        if naxis >= 2 and nbytes > 0 and hdr.get("XTENSION", "IMAGE") in ("IMAGE", None):
+            data = np.frombuffer(raw, dtype=_DT[bitpix], count=int(np.prod(dims)), offset=pos)
+            arr = data.astype(np.float64).reshape(dims[1], dims[0])
+            arr = arr * float(hdr.get("BSCALE", 1.0)) + float(hdr.get("BZERO", 0.0))
+            return arr, hdr
+        pos += ((nbytes + _BLOCK - 1) // _BLOCK) * _BLOCK
+    raise ValueError(f"no 2-D image HDU in {path}")
+
+
+def write_image(path, arr, bitpix=-32):
+    """Write a 2-D array as a primary-HDU FITS image (float32 by default)."""
+    arr = np.asarray(arr)
+    nrows, ncols = arr.shape
+    cards = [("SIMPLE", "T"), ("BITPIX", str(bitpix)), ("NAXIS", "2"), ("NAXIS1", str(ncols)),
+             ("NAXIS2", str(nrows))]
+    hdr = "".join(f"{k:<8}= {v:>20}".ljust(80) for k, v in cards) + "END".ljust(80)
+    hdr = hdr.ljust(((len(hdr) + _BLOCK - 1) // _BLOCK) * _BLOCK)
+    body = np.ascontiguousarray(arr, dtype=_DT[bitpix]).tobytes()
+    body += b"\0" * ((-len(body)) % _BLOCK)
+    with open(path, "wb") as f:
+        f.write(hdr.encode("ascii") + body)
