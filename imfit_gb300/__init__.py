@@ -1,0 +1,345 @@
+"""GB300 model-image / fit-statistic library: Python mirror of ModelObject.
+
+The compute path is the CUDA library ``_build/libimfit_gb300.so`` (built by
+``imfit_gb300.build``) reached through its C ABI (include/imfit_gb300.h).
+There is no CPU fallback: if the library cannot be loaded, or no GPU is
+present, calls raise.
+
+``ModelObject`` keeps the reference's method order and semantics
+(core/model_object.h); method names are the reference's, in snake case.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+WEIGHTS_ARE_SIGMAS, WEIGHTS_ARE_VARIANCES, WEIGHTS_ARE_WEIGHTS = 100, 110, 120
+MASK_ZERO_IS_GOOD, MASK_ZERO_IS_BAD = 10, 20
+
+_lib = None
+
+_D = ctypes.c_double
+_I = ctypes.c_int
+_L = ctypes.c_long
+_P = ctypes.c_void_p
+_DP = ctypes.POINTER(ctypes.c_double)
+
+# (name, restype, argtypes) of every C-ABI entry point
+_SIGS = [
+    ("imfit_ModelObject_new", _I, [_I, ctypes.POINTER(_P)]),
+    ("imfit_ModelObject_delete", _I, [_P]),
+    ("imfit_LastError", ctypes.c_char_p, [_P]),
+    ("imfit_Version", ctypes.c_char_p, []),
+    ("imfit_AddFunction", _I, [_P, ctypes.c_char_p]),
+    ("imfit_SetSubsampling", _I, [_P, _I, _I]),
+    ("imfit_DefineFunctionSets", _I, [_P, ctypes.POINTER(_I), _I]),
+    ("imfit_PopulateParameterNames", _I, [_P]),
+    ("imfit_GetParameterName", _I, [_P, _I, ctypes.c_char_p, _I]),
+    ("imfit_AddPSFVector", _I, [_P, _L, _I, _I, _DP, _I]),
+    ("imfit_SetupModelImage", _I, [_P, _I, _I]),
+    ("imfit_AddImageDataVector", _I, [_P, _DP, _I, _I]),
+    ("imfit_AddImageCharacteristics", _I, [_P, _D, _D, _D, _I, _D]),
+    ("imfit_AddOversampledPsfInfo", _I, [_P, _DP, _I, _I, _I, _I, _I, _I, _I, _I]),
+    ("imfit_AddErrorVector", _I, [_P, _L, _I, _I, _DP, _I]),
+    ("imfit_AddMaskVector", _I, [_P, _L, _I, _I, _DP, _I]),
+    ("imfit_UseCashStatistic", _I, [_P]),
+    ("imfit_UsePoissonMLR", _I, [_P]),
+    ("imfit_UseModelErrors", _I, [_P]),
+    ("imfit_FinalSetupForFitting", _I, [_P]),
+    ("imfit_SetMaxThreads", _I, [_P, _I]),
+    ("imfit_SetOMPChunkSize", _I, [_P, _I]),
+    ("imfit_GetNParams", _I, [_P]),
+    ("imfit_GetNDataValues", _L, [_P]),
+    ("imfit_GetNValidPixels", _L, [_P]),
+    ("imfit_GetNFunctions", _I, [_P]),
+    ("imfit_WhichFitStatistic", _I, [_P, _I]),
+    ("imfit_GetModelImageSize", _I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I)]),
+    ("imfit_CreateModelImage", _I, [_P, _DP]),
+    ("imfit_ComputeModelImage", _I, [_P, _DP]),
+    ("imfit_ComputeDeviates", _I, [_P, _DP, _DP]),
+    ("imfit_GetFitStatistic", _I, [_P, _DP, _DP]),
+    ("imfit_ChiSquared", _I, [_P, _DP, _DP]),
+    ("imfit_CashStatistic", _I, [_P, _DP, _DP]),
+    ("imfit_GetModelImageVector", _I, [_P, _DP]),
+    ("imfit_GetExpandedModelImageVector", _I, [_P, _DP]),
+    ("imfit_GetResidualImageVector", _I, [_P, _DP]),
+    ("imfit_GetWeightImageVector", _I, [_P, _DP]),
+    ("imfit_GetDataVector", _I, [_P, _DP]),
+    ("imfit_UseBootstrap", _I, [_P, ctypes.c_ulong]),
+    ("imfit_MakeBootstrapSample", _I, [_P]),
+    ("imfit_GetFitStatisticAndGradientFD", _I, [_P, _DP, _DP, _DP]),
+    ("imfit_GetFitStatisticAndGradient", _I, [_P, _DP, _DP, _DP]),
+    ("imfit_GetFitStatisticFast", _I, [_P, _DP, _DP]),
+    ("imfit_BatchFitStatisticAndGradient", _I, [_P, _I, _DP, _DP, _DP]),
+    ("imfit_BatchFitStatisticAndGradientDevice", _I, [_P, _I, _P, _P, _P]),
+    ("imfit_Synchronize", _I, [_P]),
+    ("imfit_SetUseGraphs", _I, [_P, _I]),
+    ("imfit_GetFastModelImageVector", _I, [_P, _DP, _DP]),
+]
+
+
+class ImfitError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"imfit_gb300 error {code}: {msg}")
+        self.code = code
+
+
+def library_path():
+    return _build.LIB
+
+
+def load_library(build_if_missing=True):
+    """Load the CUDA library (building it first if needed)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError(f"{path} missing: run python -m imfit_gb300.build")
+        _build.build()
+    lib = ctypes.CDLL(path)
+    for name, res, args in _SIGS:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def exported_symbols():
+    return [s[0] for s in _SIGS]
+
+
+def _dp(a):
+    return a.ctypes.data_as(_DP)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class ModelObject:
+    """One model + data image on one GPU (the reference's ModelObject)."""
+
+    def __init__(self, device=0):
+        self.lib = load_library()
+        h = _P()
+        st = self.lib.imfit_ModelObject_new(device, ctypes.byref(h))
+        if st != 0:
+            raise ImfitError(st, self.lib.imfit_LastError(None).decode())
+        self.h = h
+        self.ncols = self.nrows = 0
+        self._funcs = []
+        self._set_starts = []
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            self.lib.imfit_ModelObject_delete(h)
+            self.h = None
+
+    def _ck(self, st, allow_negative=False):
+        if st != 0 and not allow_negative:
+            raise ImfitError(st, self.lib.imfit_LastError(self.h).decode())
+        return st
+
+    @property
+    def last_error(self):
+        return self.lib.imfit_LastError(self.h).decode()
+
+    # --- functions ---
+    def add_function(self, name, new_set=False, subsampling=True):
+        self._ck(self.lib.imfit_AddFunction(self.h, name.encode()))
+        idx = len(self._funcs)
+        self._funcs.append(name)
+        if new_set or idx == 0:
+            self._set_starts.append(idx)
+        self._ck(self.lib.imfit_SetSubsampling(self.h, idx, int(subsampling)))
+
+    def set_subsampling(self, index, flag):
+        self._ck(self.lib.imfit_SetSubsampling(self.h, index, int(flag)))
+
+    def define_function_sets(self, starts):
+        arr = (ctypes.c_int * len(starts))(*starts)
+        self._ck(self.lib.imfit_DefineFunctionSets(self.h, arr, len(starts)))
+
+    def finish_functions(self):
+        self.define_function_sets(self._set_starts)
+        self._ck(self.lib.imfit_PopulateParameterNames(self.h))
+
+    def parameter_names(self):
+        buf = ctypes.create_string_buffer(64)
+        out = []
+        for i in range(self.n_params):
+            self.lib.imfit_GetParameterName(self.h, i, buf, 64)
+            out.append(buf.value.decode())
+        return out
+
+    # --- image setup ---
+    def add_psf(self, psf, normalize=True):
+        psf = _f64(psf)
+        return self._ck(self.lib.imfit_AddPSFVector(self.h, psf.size, psf.shape[1], psf.shape[0], _dp(psf),
+                                                    int(normalize)))
+
+    def setup_model_image(self, ncols, nrows):
+        self.ncols, self.nrows = ncols, nrows
+        return self._ck(self.lib.imfit_SetupModelImage(self.h, ncols, nrows))
+
+    def add_image_data(self, img):
+        img = _f64(img)
+        self.nrows, self.ncols = img.shape
+        return self._ck(self.lib.imfit_AddImageDataVector(self.h, _dp(img), img.shape[1], img.shape[0]))
+
+    def add_image_characteristics(self, gain=1.0, read_noise=0.0, exp_time=1.0, n_combined=1,
+                                  original_sky=0.0):
+        return self._ck(self.lib.imfit_AddImageCharacteristics(self.h, gain, read_noise, exp_time,
+                                                               n_combined, original_sky))
+
+    def add_oversampled_psf(self, psf, scale, region, normalize=True):
+        psf = _f64(psf)
+        x1, x2, y1, y2 = region
+        return self._ck(self.lib.imfit_AddOversampledPsfInfo(self.h, _dp(psf), psf.shape[1], psf.shape[0],
+                                                             scale, x1, x2, y1, y2, int(normalize)))
+
+    def add_error_vector(self, err, input_type=WEIGHTS_ARE_SIGMAS):
+        err = _f64(err)
+        return self._ck(self.lib.imfit_AddErrorVector(self.h, err.size, err.shape[1], err.shape[0], _dp(err),
+                                                      input_type))
+
+    def add_mask_vector(self, mask, input_type=MASK_ZERO_IS_GOOD):
+        mask = _f64(mask)
+        return self._ck(self.lib.imfit_AddMaskVector(self.h, mask.size, mask.shape[1], mask.shape[0],
+                                                     _dp(mask), input_type))
+
+    def use_cash(self):
+        return self._ck(self.lib.imfit_UseCashStatistic(self.h))
+
+    def use_pmlr(self):
+        return self._ck(self.lib.imfit_UsePoissonMLR(self.h))
+
+    def use_model_errors(self):
+        return self._ck(self.lib.imfit_UseModelErrors(self.h))
+
+    def final_setup(self):
+        """Returns FinalSetupForFitting's status (0, -1, -2, -3) like the reference."""
+        return self.lib.imfit_FinalSetupForFitting(self.h)
+
+    # --- queries ---
+    @property
+    def n_params(self):
+        return self.lib.imfit_GetNParams(self.h)
+
+    @property
+    def n_data(self):
+        return self.lib.imfit_GetNDataValues(self.h)
+
+    @property
+    def n_valid(self):
+        return self.lib.imfit_GetNValidPixels(self.h)
+
+    def which_statistic(self, verbose=True):
+        return self.lib.imfit_WhichFitStatistic(self.h, int(verbose))
+
+    def model_size(self):
+        a, b = _I(), _I()
+        self.lib.imfit_GetModelImageSize(self.h, ctypes.byref(a), ctypes.byref(b))
+        return a.value, b.value
+
+    # --- plain FP64 path ---
+    def create_model_image(self, params):
+        p = _f64(params)
+        self._ck(self.lib.imfit_CreateModelImage(self.h, _dp(p)))
+
+    def get_model_image(self):
+        out = np.empty((self.nrows, self.ncols))
+        self._ck(self.lib.imfit_GetModelImageVector(self.h, _dp(out)))
+        return out
+
+    def get_expanded_model_image(self):
+        nc, nr = self.model_size()
+        out = np.empty((nr, nc))
+        self._ck(self.lib.imfit_GetExpandedModelImageVector(self.h, _dp(out)))
+        return out
+
+    def get_residual_image(self):
+        out = np.empty((self.nrows, self.ncols))
+        self._ck(self.lib.imfit_GetResidualImageVector(self.h, _dp(out)))
+        return out
+
+    def get_weights(self):
+        out = np.empty((self.nrows, self.ncols))
+        self._ck(self.lib.imfit_GetWeightImageVector(self.h, _dp(out)))
+        return out
+
+    def get_data(self):
+        out = np.empty((self.nrows, self.ncols))
+        self._ck(self.lib.imfit_GetDataVector(self.h, _dp(out)))
+        return out
+
+    def compute_deviates(self, params, n=None):
+        p = _f64(params)
+        out = np.empty(n if n is not None else self.n_data)
+        self._ck(self.lib.imfit_ComputeDeviates(self.h, _dp(out), _dp(p)))
+        return out
+
+    def get_fit_statistic(self, params):
+        p = _f64(params)
+        s = _D()
+        self._ck(self.lib.imfit_GetFitStatistic(self.h, _dp(p), ctypes.byref(s)))
+        return s.value
+
+    def use_bootstrap(self, seed):
+        return self._ck(self.lib.imfit_UseBootstrap(self.h, seed))
+
+    def make_bootstrap_sample(self):
+        return self._ck(self.lib.imfit_MakeBootstrapSample(self.h))
+
+    # --- gradients ---
+    def statistic_and_gradient_fd(self, params):
+        p = _f64(params)
+        s = _D()
+        g = np.empty(self.n_params)
+        self._ck(self.lib.imfit_GetFitStatisticAndGradientFD(self.h, _dp(p), ctypes.byref(s), _dp(g)))
+        return s.value, g
+
+    def statistic_and_gradient(self, params):
+        p = _f64(params)
+        s = _D()
+        g = np.empty(self.n_params)
+        self._ck(self.lib.imfit_GetFitStatisticAndGradient(self.h, _dp(p), ctypes.byref(s), _dp(g)))
+        return s.value, g
+
+    def fit_statistic_fast(self, params):
+        p = _f64(params)
+        s = _D()
+        self._ck(self.lib.imfit_GetFitStatisticFast(self.h, _dp(p), ctypes.byref(s)))
+        return s.value
+
+    def batch_statistic_and_gradient(self, params, want_grad=True):
+        p = _f64(np.atleast_2d(params))
+        B = p.shape[0]
+        s = np.empty(B)
+        g = np.empty((B, self.n_params)) if want_grad else None
+        self._ck(self.lib.imfit_BatchFitStatisticAndGradient(self.h, B, _dp(p), _dp(s),
+                                                             _dp(g) if want_grad else None))
+        return (s, g) if want_grad else s
+
+    def batch_device(self, n_batch, d_params, d_stats, d_grads):
+        """Device-pointer batch call (ints: raw device addresses); enqueues only."""
+        return self._ck(self.lib.imfit_BatchFitStatisticAndGradientDevice(self.h, n_batch, d_params, d_stats,
+                                                                          d_grads))
+
+    def synchronize(self):
+        return self._ck(self.lib.imfit_Synchronize(self.h))
+
+    def set_use_graphs(self, flag):
+        return self._ck(self.lib.imfit_SetUseGraphs(self.h, int(flag)))
+
+    def get_fast_model_image(self, params):
+        p = _f64(params)
+        out = np.empty((self.nrows, self.ncols))
+        self._ck(self.lib.imfit_GetFastModelImageVector(self.h, _dp(p), _dp(out)))
+        return out

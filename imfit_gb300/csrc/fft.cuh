@@ -1,0 +1,253 @@
+// fft.cuh -- shared-memory mixed-radix Stockham FFT for the PSF convolution.
+//
+// Replaces the reference's FFTW r2c/c2r convolution (core/convolver.cpp:340-414).
+// A CTA transforms several independent lines (rows of the model window, or
+// columns of the half spectrum) held in shared memory.  Each pass of radix R
+// with span Ns reads src[j + r*n/R], multiplies by exp(s*2*pi*i*r*(j mod Ns)/(Ns*R)),
+// performs a length-R DFT in registers and writes dst[(j/Ns)*Ns*R + (j mod Ns) + t*Ns]
+// (the self-sorting Stockham formulation), so no bit reversal is needed and
+// the output is in natural order after the last pass.  Lengths are products
+// of 2, 3, 4, 5, 7 and 8; padded sizes are always chosen from that set.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace imfit {
+
+template <typename T>
+struct cplx {
+  T x, y;
+};
+
+template <typename T>
+__device__ __forceinline__ cplx<T> cmul(cplx<T> a, cplx<T> b) {
+  return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+}
+template <typename T>
+__device__ __forceinline__ cplx<T> cadd(cplx<T> a, cplx<T> b) { return {a.x + b.x, a.y + b.y}; }
+template <typename T>
+__device__ __forceinline__ cplx<T> csub(cplx<T> a, cplx<T> b) { return {a.x - b.x, a.y - b.y}; }
+// multiply by s*i (s = +1 or -1)
+template <typename T>
+__device__ __forceinline__ cplx<T> mul_si(cplx<T> a, int s) { return s > 0 ? cplx<T>{-a.y, a.x} : cplx<T>{a.y, -a.x}; }
+
+constexpr int kMaxRadixPasses = 16;
+
+// Plan of one transform length: radices applied in order, plus the twiddle
+// table tw[k] = exp(-2*pi*i*k/n), k in [0,n).
+template <typename T>
+struct FFTPlan {
+  int n;
+  int npass;
+  int radix[kMaxRadixPasses];
+  const cplx<T> *tw;
+};
+
+// length-R DFT in registers, sign s (-1 forward, +1 inverse)
+template <typename T>
+__device__ __forceinline__ void dft2(cplx<T> *v) {
+  cplx<T> a = v[0], b = v[1];
+  v[0] = cadd(a, b);
+  v[1] = csub(a, b);
+}
+
+template <typename T>
+__device__ __forceinline__ void dft3(cplx<T> *v, int s) {
+  const T h = (T)0.86602540378443864676;
+  cplx<T> t1 = cadd(v[1], v[2]);
+  cplx<T> t2 = {v[0].x - (T)0.5 * t1.x, v[0].y - (T)0.5 * t1.y};
+  cplx<T> d = csub(v[1], v[2]);
+  cplx<T> t3 = mul_si(cplx<T>{h * d.x, h * d.y}, s);
+  v[0] = cadd(v[0], t1);
+  v[1] = cadd(t2, t3);
+  v[2] = csub(t2, t3);
+}
+
+template <typename T>
+__device__ __forceinline__ void dft4(cplx<T> *v, int s) {
+  cplx<T> a0 = cadd(v[0], v[2]), a1 = csub(v[0], v[2]);
+  cplx<T> a2 = cadd(v[1], v[3]), d = csub(v[1], v[3]);
+  cplx<T> e = mul_si(d, s);
+  v[0] = cadd(a0, a2);
+  v[2] = csub(a0, a2);
+  v[1] = cadd(a1, e);
+  v[3] = csub(a1, e);
+}
+
+template <typename T>
+__device__ __forceinline__ void dft5(cplx<T> *v, int s) {
+  const T c1 = (T)0.30901699437494742410, c2 = (T)-0.80901699437494742410;
+  const T s1 = (T)0.95105651629515357212, s2 = (T)0.58778525229247312917;
+  cplx<T> a1 = cadd(v[1], v[4]), b1 = csub(v[1], v[4]);
+  cplx<T> a2 = cadd(v[2], v[3]), b2 = csub(v[2], v[3]);
+  cplx<T> r1 = {v[0].x + c1 * a1.x + c2 * a2.x, v[0].y + c1 * a1.y + c2 * a2.y};
+  cplx<T> r2 = {v[0].x + c2 * a1.x + c1 * a2.x, v[0].y + c2 * a1.y + c1 * a2.y};
+  cplx<T> i1 = mul_si(cplx<T>{s1 * b1.x + s2 * b2.x, s1 * b1.y + s2 * b2.y}, s);
+  cplx<T> i2 = mul_si(cplx<T>{s2 * b1.x - s1 * b2.x, s2 * b1.y - s1 * b2.y}, s);
+  v[0] = {v[0].x + a1.x + a2.x, v[0].y + a1.y + a2.y};
+  v[1] = cadd(r1, i1);
+  v[4] = csub(r1, i1);
+  v[2] = cadd(r2, i2);
+  v[3] = csub(r2, i2);
+}
+
+template <typename T>
+__device__ __forceinline__ void dft7(cplx<T> *v, int s) {
+  const T C[3] = {(T)0.62348980185873353053, (T)-0.22252093395631440429, (T)-0.90096886790241912624};
+  const T S[3] = {(T)0.78183148246802980871, (T)0.97492791218182360702, (T)0.43388373911755812048};
+  cplx<T> a[3], b[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    a[k] = cadd(v[k + 1], v[6 - k]);
+    b[k] = csub(v[k + 1], v[6 - k]);
+  }
+  cplx<T> v0 = v[0];
+  v[0] = {v0.x + a[0].x + a[1].x + a[2].x, v0.y + a[0].y + a[1].y + a[2].y};
+#pragma unroll
+  for (int t = 1; t <= 3; t++) {
+    cplx<T> re = v0, im = {0, 0};
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const int m = ((k + 1) * t) % 7;  // angle index (k+1)*t mod 7
+      const T c = (m <= 3) ? C[m - 1] : C[7 - m - 1];
+      const T sn = (m <= 3) ? S[m - 1] : -S[7 - m - 1];
+      re.x += c * a[k].x;
+      re.y += c * a[k].y;
+      im.x += sn * b[k].x;
+      im.y += sn * b[k].y;
+    }
+    cplx<T> ii = mul_si(im, s);
+    v[t] = cadd(re, ii);
+    v[7 - t] = csub(re, ii);
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void dft8(cplx<T> *v, int s) {
+  const T r = (T)0.70710678118654752440;
+  cplx<T> e[4] = {v[0], v[2], v[4], v[6]};
+  cplx<T> o[4] = {v[1], v[3], v[5], v[7]};
+  dft4(e, s);
+  dft4(o, s);
+  // twiddles W8^k = exp(s*2*pi*i*k/8)
+  cplx<T> o1 = {r * (o[1].x - s * o[1].y), r * (o[1].y + s * o[1].x)};
+  cplx<T> o2 = mul_si(o[2], s);
+  cplx<T> o3 = {r * (-o[3].x - s * o[3].y), r * (-o[3].y + s * o[3].x)};
+  v[0] = cadd(e[0], o[0]);
+  v[4] = csub(e[0], o[0]);
+  v[1] = cadd(e[1], o1);
+  v[5] = csub(e[1], o1);
+  v[2] = cadd(e[2], o2);
+  v[6] = csub(e[2], o2);
+  v[3] = cadd(e[3], o3);
+  v[7] = csub(e[3], o3);
+}
+
+// Twiddle exp(s*2*pi*i*idx/n) from the forward table.
+template <typename T>
+__device__ __forceinline__ cplx<T> twiddle(const cplx<T> *tw, int idx, int s) {
+  cplx<T> w = tw[idx];
+  if (s > 0) w.y = -w.y;
+  return w;
+}
+
+// One radix-R Stockham pass over 'nl' lines of length n.
+// Element t of line l lives at buf[l*ls + t*es].
+template <typename T, int R>
+__device__ __forceinline__ void stockham_pass(const cplx<T> *__restrict__ src, cplx<T> *__restrict__ dst,
+                                              int n, int Ns, int nl, int ls, int es,
+                                              const cplx<T> *__restrict__ tw, int s, bool lineFastest) {
+  const int m = n / R;
+  const int total = m * nl;
+  const int twStep = n / (Ns * R);
+  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+    int l, j;
+    if (lineFastest) {
+      l = idx % nl;
+      j = idx / nl;
+    } else {
+      j = idx % m;
+      l = idx / m;
+    }
+    const int k = j % Ns;
+    const cplx<T> *in = src + l * ls;
+    cplx<T> v[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) v[r] = in[(j + r * m) * es];
+    if (k != 0) {
+#pragma unroll
+      for (int r = 1; r < R; r++) v[r] = cmul(v[r], twiddle(tw, r * k * twStep, s));
+    }
+    if (R == 2) dft2(v);
+    if (R == 3) dft3(v, s);
+    if (R == 4) dft4(v, s);
+    if (R == 5) dft5(v, s);
+    if (R == 7) dft7(v, s);
+    if (R == 8) dft8(v, s);
+    cplx<T> *out = dst + l * ls;
+    const int base = (j - k) * R + k;
+#pragma unroll
+    for (int t = 0; t < R; t++) out[(base + t * Ns) * es] = v[t];
+  }
+}
+
+// Full transform of nl lines; ping-pongs between a and b.  Returns the buffer
+// that holds the result.  Must be called by all threads of the CTA.
+template <typename T>
+__device__ cplx<T> *block_fft(cplx<T> *a, cplx<T> *b, const FFTPlan<T> &p, int nl, int ls, int es,
+                              int s, bool lineFastest) {
+  int Ns = 1;
+  cplx<T> *src = a, *dst = b;
+  for (int ps = 0; ps < p.npass; ps++) {
+    const int R = p.radix[ps];
+    switch (R) {
+      case 2: stockham_pass<T, 2>(src, dst, p.n, Ns, nl, ls, es, p.tw, s, lineFastest); break;
+      case 3: stockham_pass<T, 3>(src, dst, p.n, Ns, nl, ls, es, p.tw, s, lineFastest); break;
+      case 4: stockham_pass<T, 4>(src, dst, p.n, Ns, nl, ls, es, p.tw, s, lineFastest); break;
+      case 5: stockham_pass<T, 5>(src, dst, p.n, Ns, nl, ls, es, p.tw, s, lineFastest); break;
+      case 7: stockham_pass<T, 7>(src, dst, p.n, Ns, nl, ls, es, p.tw, s, lineFastest); break;
+      default: stockham_pass<T, 8>(src, dst, p.n, Ns, nl, ls, es, p.tw, s, lineFastest); break;
+    }
+    __syncthreads();
+    Ns *= R;
+    cplx<T> *t = src;
+    src = dst;
+    dst = t;
+  }
+  return src;
+}
+
+// ---------------------------------------------------------------------------
+// Real <-> half-complex helpers for a real line of even length L = 2M packed
+// as z[k] = x[2k] + i x[2k+1] (M-point complex FFT).
+//   forward:  X[k] = E[k] + W^k O[k],  E = (Z[k] + conj Z[M-k])/2,
+//             O = (Z[k] - conj Z[M-k])/(2i),  W = exp(-2 pi i / L),  k = 0..M
+//   inverse:  Z[k] = (X[k] + conj X[M-k]) + i W^-k (X[k] - conj X[M-k]),
+//             k = 0..M-1; an M-point inverse FFT then yields L*(x[2k] + i x[2k+1]).
+// twL[k] = exp(-2*pi*i*k/L) for k in [0, M].
+
+template <typename T>
+__device__ __forceinline__ cplx<T> r2c_post(const cplx<T> *Z, int k, int M, const cplx<T> *twL) {
+  cplx<T> zk = Z[k == M ? 0 : k];
+  cplx<T> zc = Z[k == 0 ? 0 : M - k];
+  zc.y = -zc.y;  // conj Z[M-k]
+  cplx<T> E = {(T)0.5 * (zk.x + zc.x), (T)0.5 * (zk.y + zc.y)};
+  // O = (zk - zc) / (2i) = ( (zk-zc).y/2 , -(zk-zc).x/2 )
+  cplx<T> d = csub(zk, zc);
+  cplx<T> O = {(T)0.5 * d.y, (T)-0.5 * d.x};
+  return cadd(E, cmul(twL[k], O));
+}
+
+template <typename T>
+__device__ __forceinline__ cplx<T> c2r_pre(const cplx<T> *X, int k, int M, const cplx<T> *twL) {
+  cplx<T> xk = X[k];
+  cplx<T> xc = X[M - k];
+  if (k == 0) { xk.y = 0; xc.y = 0; }  // c2r ignores imag parts of DC / Nyquist
+  xc.y = -xc.y;
+  cplx<T> E = cadd(xk, xc);
+  cplx<T> w = twL[k];
+  w.y = -w.y;  // W^-k
+  cplx<T> O = cmul(w, csub(xk, xc));
+  return {E.x - O.y, E.y + O.x};  // E + i O
+}
+
+}  // namespace imfit

@@ -1,0 +1,332 @@
+// k_fft.cu -- 2-D real convolution kernels (FP64 plain path and FP32 helpers).
+//
+// The reference convolves the zero-padded model with the PSF by FFTW r2c,
+// complex multiply, c2r and a 1/N rescale (core/convolver.cpp:340-414).  Here
+// the 2-D transform is split into
+//   1. k_rows_r2c   : each row -> half spectrum (real row packed as M = L/2
+//                     complex points, M-point FFT, split), rows beyond the
+//                     image are implicit zeros and never read;
+//   2. k_cols       : each group of half-spectrum columns -> column FFT,
+//                     multiply by the cached PSF spectrum (or its conjugate
+//                     for the adjoint), inverse column FFT, all in shared
+//                     memory with a single read and write of the spectrum;
+//   3. k_rows_c2r   : each needed row -> real row, rescaled.
+// Padded lengths are 7-smooth, at least as large as the reference's
+// (N + P - 1); linear convolution is unchanged by extra zero padding.
+#include "kernels.h"
+#include "fft.cuh"
+
+namespace imfit {
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_rows_r2c(const T *__restrict__ in, long inPitch, long inBatch,
+                                                  int inCols, int nRows, cplx<T> *__restrict__ out,
+                                                  long outPitch, long outBatch, FFTPlan<T> plan,
+                                                  const cplx<T> *__restrict__ twL, int rpb) {
+  extern __shared__ unsigned char smem_raw[];
+  cplx<T> *bufA = reinterpret_cast<cplx<T> *>(smem_raw);
+  const int M = plan.n;
+  const int ls = M + 1;
+  cplx<T> *bufB = bufA + rpb * ls;
+  const int row0 = blockIdx.x * rpb;
+  const int b = blockIdx.y;
+  const int nl = min(rpb, nRows - row0);
+  if (nl <= 0) return;
+  in += b * inBatch;
+  out += b * outBatch;
+  for (int idx = threadIdx.x; idx < nl * M; idx += blockDim.x) {
+    const int l = idx / M, k = idx % M;
+    const T *src = in + (long)(row0 + l) * inPitch;
+    const int c0 = 2 * k, c1 = 2 * k + 1;
+    cplx<T> z;
+    z.x = (c0 < inCols) ? src[c0] : (T)0;
+    z.y = (c1 < inCols) ? src[c1] : (T)0;
+    bufA[l * ls + k] = z;
+  }
+  __syncthreads();
+  cplx<T> *Z = block_fft(bufA, bufB, plan, nl, ls, 1, -1, false);
+  for (int idx = threadIdx.x; idx < nl * (M + 1); idx += blockDim.x) {
+    const int l = idx / (M + 1), k = idx % (M + 1);
+    out[(long)(row0 + l) * outPitch + k] = r2c_post(Z + l * ls, k, M, twL);
+  }
+}
+
+template <typename T, int MODE>
+__global__ void __launch_bounds__(256) k_cols(cplx<T> *__restrict__ spec, long pitch, long batch, int nColsC,
+                                              int nRowsIn, int nRowsOut, const cplx<T> *__restrict__ H,
+                                              long hPitch, FFTPlan<T> plan, T scale, int cpb) {
+  extern __shared__ unsigned char smem_raw[];
+  cplx<T> *bufA = reinterpret_cast<cplx<T> *>(smem_raw);
+  const int Ly = plan.n;
+  cplx<T> *bufB = bufA + Ly * cpb;
+  const int c0 = blockIdx.x * cpb;
+  const int nl = min(cpb, nColsC - c0);
+  if (nl <= 0) return;
+  spec += blockIdx.y * batch;
+  for (int idx = threadIdx.x; idx < Ly * cpb; idx += blockDim.x) {
+    const int t = idx / cpb, f = idx % cpb;
+    cplx<T> v = {(T)0, (T)0};
+    if (t < nRowsIn && f < nl) v = spec[(long)t * pitch + c0 + f];
+    bufA[t * cpb + f] = v;
+  }
+  __syncthreads();
+  cplx<T> *X = block_fft(bufA, bufB, plan, cpb, 1, cpb, -1, true);
+  if constexpr (MODE == 0) {
+    for (int idx = threadIdx.x; idx < Ly * cpb; idx += blockDim.x) {
+      const int t = idx / cpb, f = idx % cpb;
+      if (f < nl) spec[(long)t * pitch + c0 + f] = X[t * cpb + f];
+    }
+  } else {
+  for (int idx = threadIdx.x; idx < Ly * cpb; idx += blockDim.x) {
+    const int t = idx / cpb, f = idx % cpb;
+    if (f < nl) {
+      cplx<T> h = H[(long)t * hPitch + c0 + f];
+      if (MODE == 2) h.y = -h.y;
+      cplx<T> v = cmul(X[t * cpb + f], h);
+      v.x *= scale;
+      v.y *= scale;
+      X[t * cpb + f] = v;
+    }
+  }
+  __syncthreads();
+  cplx<T> *other = (X == bufA) ? bufB : bufA;
+  cplx<T> *Y = block_fft(X, other, plan, cpb, 1, cpb, +1, true);
+  for (int idx = threadIdx.x; idx < nRowsOut * cpb; idx += blockDim.x) {
+    const int t = idx / cpb, f = idx % cpb;
+    if (f < nl) spec[(long)t * pitch + c0 + f] = Y[t * cpb + f];
+  }
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_rows_c2r(const cplx<T> *__restrict__ in, long inPitch, long inBatch,
+                                                  int nRows, T *__restrict__ out, long outPitch,
+                                                  long outBatch, int outCols, T scale, FFTPlan<T> plan,
+                                                  const cplx<T> *__restrict__ twL, int rpb) {
+  extern __shared__ unsigned char smem_raw[];
+  const int M = plan.n;
+  const int ls = M + 1;
+  cplx<T> *bufX = reinterpret_cast<cplx<T> *>(smem_raw);
+  cplx<T> *bufA = bufX + rpb * ls;
+  cplx<T> *bufB = bufA + rpb * ls;
+  const int row0 = blockIdx.x * rpb;
+  const int nl = min(rpb, nRows - row0);
+  if (nl <= 0) return;
+  in += blockIdx.y * inBatch;
+  out += blockIdx.y * outBatch;
+  for (int idx = threadIdx.x; idx < nl * (M + 1); idx += blockDim.x) {
+    const int l = idx / (M + 1), k = idx % (M + 1);
+    bufX[l * ls + k] = in[(long)(row0 + l) * inPitch + k];
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < nl * M; idx += blockDim.x) {
+    const int l = idx / M, k = idx % M;
+    bufA[l * ls + k] = c2r_pre(bufX + l * ls, k, M, twL);
+  }
+  __syncthreads();
+  cplx<T> *Z = block_fft(bufA, bufB, plan, nl, ls, 1, +1, false);
+  for (int idx = threadIdx.x; idx < nl * outCols; idx += blockDim.x) {
+    const int l = idx / outCols, c = idx % outCols;
+    const cplx<T> z = Z[l * ls + (c >> 1)];
+    out[(long)(row0 + l) * outPitch + c] = scale * ((c & 1) ? z.y : z.x);
+  }
+}
+
+// ------------------------------------------------------------------ launchers
+template <typename T>
+static FFTPlan<T> plan_of(const FFTLen &L, bool half) {
+  FFTPlan<T> p;
+  const FFTTable &t = half ? L.half : L.full;
+  p.n = t.n;
+  p.npass = t.npass;
+  for (int i = 0; i < kMaxRadixPasses; i++) p.radix[i] = t.radix[i];
+  p.tw = reinterpret_cast<const cplx<T> *>(sizeof(T) == 8 ? (const void *)t.tw64 : (const void *)t.tw32);
+  return p;
+}
+
+template <typename T>
+static const cplx<T> *twl_of(const FFTLen &L) {
+  return reinterpret_cast<const cplx<T> *>(sizeof(T) == 8 ? (const void *)L.twL64 : (const void *)L.twL32);
+}
+
+int rows_per_block(int M, int elemBytes, int nbuf) {
+  // keep shared memory per CTA at or below ~48 KB, 1..8 lines
+  int bytes = (M + 1) * elemBytes * 2 * nbuf;
+  int r = (48 * 1024) / (bytes > 0 ? bytes : 1);
+  if (r < 1) r = 1;
+  if (r > 8) r = 8;
+  return r;
+}
+
+template <typename T>
+cudaError_t launch_rows_r2c(const T *in, long inPitch, long inBatch, int inCols, int nRows, void *out,
+                            long outPitch, long outBatch, const FFTLen &Lx, int nBatch, cudaStream_t st) {
+  const int M = Lx.half.n;
+  const int rpb = rows_per_block(M, sizeof(T), 2);
+  const size_t sm = sizeof(cplx<T>) * 2 * (size_t)rpb * (M + 1);
+  auto kern = k_rows_r2c<T>;
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  dim3 grid((nRows + rpb - 1) / rpb, nBatch);
+  kern<<<grid, 256, sm, st>>>(in, inPitch, inBatch, inCols, nRows, reinterpret_cast<cplx<T> *>(out), outPitch,
+                              outBatch, plan_of<T>(Lx, true), twl_of<T>(Lx), rpb);
+  return cudaGetLastError();
+}
+
+int cols_per_block(int Ly, int elemBytes, int nColsC) {
+  // two ping-pong buffers of Ly x cpb complex; aim for >= 1 CTA per SM
+  int cpb = 8;
+  while (cpb > 1 && (size_t)2 * Ly * cpb * 2 * elemBytes > 200 * 1024) cpb >>= 1;
+  while (cpb > 1 && (nColsC + cpb - 1) / cpb < 152) cpb >>= 1;
+  return cpb;
+}
+
+template <typename T>
+cudaError_t launch_cols(void *spec, long pitch, long batch, int nColsC, int nRowsIn, int nRowsOut,
+                        const void *H, long hPitch, const FFTLen &Ly, T scale, int mode, int nBatch,
+                        cudaStream_t st) {
+  const int L = Ly.full.n;
+  const int cpb = cols_per_block(L, sizeof(T), nColsC);
+  const size_t sm = sizeof(cplx<T>) * 2 * (size_t)L * cpb;
+  dim3 grid((nColsC + cpb - 1) / cpb, nBatch);
+  auto p = plan_of<T>(Ly, false);
+  cplx<T> *s = reinterpret_cast<cplx<T> *>(spec);
+  const cplx<T> *h = reinterpret_cast<const cplx<T> *>(H);
+  if (mode == 0) {
+    cudaFuncSetAttribute(k_cols<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_cols<T, 0><<<grid, 256, sm, st>>>(s, pitch, batch, nColsC, nRowsIn, nRowsOut, h, hPitch, p, scale, cpb);
+  } else if (mode == 1) {
+    cudaFuncSetAttribute(k_cols<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_cols<T, 1><<<grid, 256, sm, st>>>(s, pitch, batch, nColsC, nRowsIn, nRowsOut, h, hPitch, p, scale, cpb);
+  } else {
+    cudaFuncSetAttribute(k_cols<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_cols<T, 2><<<grid, 256, sm, st>>>(s, pitch, batch, nColsC, nRowsIn, nRowsOut, h, hPitch, p, scale, cpb);
+  }
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_rows_c2r(const void *in, long inPitch, long inBatch, int nRows, T *out, long outPitch,
+                            long outBatch, int outCols, T scale, const FFTLen &Lx, int nBatch,
+                            cudaStream_t st) {
+  const int M = Lx.half.n;
+  const int rpb = rows_per_block(M, sizeof(T), 3);
+  const size_t sm = sizeof(cplx<T>) * 3 * (size_t)rpb * (M + 1);
+  auto kern = k_rows_c2r<T>;
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  dim3 grid((nRows + rpb - 1) / rpb, nBatch);
+  kern<<<grid, 256, sm, st>>>(reinterpret_cast<const cplx<T> *>(in), inPitch, inBatch, nRows, out, outPitch,
+                              outBatch, outCols, scale, plan_of<T>(Lx, true), twl_of<T>(Lx), rpb);
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_rows_r2c<double>(const double *, long, long, int, int, void *, long, long,
+                                             const FFTLen &, int, cudaStream_t);
+template cudaError_t launch_rows_r2c<float>(const float *, long, long, int, int, void *, long, long,
+                                            const FFTLen &, int, cudaStream_t);
+template cudaError_t launch_cols<double>(void *, long, long, int, int, int, const void *, long,
+                                         const FFTLen &, double, int, int, cudaStream_t);
+template cudaError_t launch_cols<float>(void *, long, long, int, int, int, const void *, long,
+                                        const FFTLen &, float, int, int, cudaStream_t);
+template cudaError_t launch_rows_c2r<double>(const void *, long, long, int, double *, long, long, int,
+                                             double, const FFTLen &, int, cudaStream_t);
+template cudaError_t launch_rows_c2r<float>(const void *, long, long, int, float *, long, long, int, float,
+                                            const FFTLen &, int, cudaStream_t);
+
+}  // namespace imfit
+
+// ------------------------------------------------------------ FFT tables
+#include <cmath>
+#include <vector>
+
+namespace imfit {
+
+static bool is_smooth(int n) {
+  for (int p : {2, 3, 5, 7})
+    while (n % p == 0) n /= p;
+  return n == 1;
+}
+
+int smooth_size(int n, bool even) {
+  if (n < 2) n = 2;
+  for (int m = n;; m++) {
+    if (even && (m & 1)) continue;
+    if (is_smooth(m)) return m;
+  }
+}
+
+int radix_schedule(int n, int *radix) {
+  int np = 0;
+  while (n % 8 == 0 && np < kMaxRadixPasses) { radix[np++] = 8; n /= 8; }
+  while (n % 4 == 0 && np < kMaxRadixPasses) { radix[np++] = 4; n /= 4; }
+  while (n % 2 == 0 && np < kMaxRadixPasses) { radix[np++] = 2; n /= 2; }
+  for (int p : {3, 5, 7})
+    while (n % p == 0 && np < kMaxRadixPasses) { radix[np++] = p; n /= p; }
+  return (n == 1) ? np : -1;
+}
+
+static cudaError_t table_create(FFTTable &t, int n) {
+  t.n = n;
+  t.npass = radix_schedule(n, t.radix);
+  if (t.npass < 0) return cudaErrorInvalidValue;
+  std::vector<double> w64(2 * (size_t)n);
+  std::vector<float> w32(2 * (size_t)n);
+  for (int k = 0; k < n; k++) {
+    // angle reduced to [0, pi/2]-symmetric evaluation for accuracy
+    const double a = 2.0 * M_PI * (double)k / (double)n;
+    w64[2 * k] = cos(a);
+    w64[2 * k + 1] = -sin(a);
+    w32[2 * k] = (float)w64[2 * k];
+    w32[2 * k + 1] = (float)w64[2 * k + 1];
+  }
+  cudaError_t e = cudaMalloc(&t.tw64, sizeof(double) * 2 * (size_t)n);
+  if (e) return e;
+  e = cudaMalloc(&t.tw32, sizeof(float) * 2 * (size_t)n);
+  if (e) return e;
+  e = cudaMemcpy(t.tw64, w64.data(), sizeof(double) * 2 * (size_t)n, cudaMemcpyHostToDevice);
+  if (e) return e;
+  return cudaMemcpy(t.tw32, w32.data(), sizeof(float) * 2 * (size_t)n, cudaMemcpyHostToDevice);
+}
+
+cudaError_t fftlen_create(FFTLen &L, int len) {
+  L.L = len;
+  cudaError_t e = table_create(L.full, len);
+  if (e) return e;
+  if (len % 2 == 0) {
+    e = table_create(L.half, len / 2);
+    if (e) return e;
+    const int M = len / 2;
+    std::vector<double> w64(2 * (size_t)(M + 1));
+    std::vector<float> w32(2 * (size_t)(M + 1));
+    for (int k = 0; k <= M; k++) {
+      const double a = 2.0 * M_PI * (double)k / (double)len;
+      w64[2 * k] = cos(a);
+      w64[2 * k + 1] = -sin(a);
+      w32[2 * k] = (float)w64[2 * k];
+      w32[2 * k + 1] = (float)w64[2 * k + 1];
+    }
+    e = cudaMalloc(&L.twL64, sizeof(double) * 2 * (size_t)(M + 1));
+    if (e) return e;
+    e = cudaMalloc(&L.twL32, sizeof(float) * 2 * (size_t)(M + 1));
+    if (e) return e;
+    e = cudaMemcpy(L.twL64, w64.data(), sizeof(double) * 2 * (size_t)(M + 1), cudaMemcpyHostToDevice);
+    if (e) return e;
+    e = cudaMemcpy(L.twL32, w32.data(), sizeof(float) * 2 * (size_t)(M + 1), cudaMemcpyHostToDevice);
+  }
+  return e;
+}
+
+static void table_destroy(FFTTable &t) {
+  if (t.tw64) cudaFree(t.tw64);
+  if (t.tw32) cudaFree(t.tw32);
+  t.tw64 = t.tw32 = nullptr;
+}
+
+void fftlen_destroy(FFTLen &L) {
+  table_destroy(L.full);
+  table_destroy(L.half);
+  if (L.twL64) cudaFree(L.twL64);
+  if (L.twL32) cudaFree(L.twL32);
+  L.twL64 = L.twL32 = nullptr;
+}
+
+}  // namespace imfit

@@ -1,0 +1,369 @@
+// k_plain.cu -- the plain FP64 path: the drop-in for ModelObject's
+// CreateModelImage / ComputeDeviates / GetFitStatistic.
+//
+// Compiled with --fmad=false: every expression is evaluated in the same order
+// and with the same rounding as the reference's (non-FMA) x86 build, so the
+// per-pixel model matches ModelObject::CreateModelImage to a few ulp (the
+// transcendental functions are CUDA's, not glibc's).
+#include "kernels.h"
+
+namespace imfit {
+
+// CreateModelImage pixel loop: core/model_object.cpp:1144-1175 (main grid),
+// OversampledRegion::ComputeRegionAndDownsample core/oversampled_region.cpp:301-327
+// (region grid).  One thread per model pixel; Kahan sum over components.
+__global__ void __launch_bounds__(256) k_eval64(const CompF64 *__restrict__ comps, int nComp,
+                                                double *__restrict__ model, long pitch, Grid64 g) {
+  __shared__ CompF64 sc[kMaxComponents];
+  for (int i = threadIdx.x; i < nComp; i += blockDim.x) sc[i] = comps[i];
+  __syncthreads();
+  const long n = (long)g.nCols * g.nRows;
+  const long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const long j = k % g.nCols, i = k / g.nCols;
+  double x, y;
+  if (!g.isRegion) {
+    y = (double)(i - g.pr + 1);
+    x = (double)(j - g.pc + 1);
+  } else {
+    y = g.y1 + g.off + (i - g.pr) * g.frac;
+    x = g.x1 + g.off + (j - g.pc) * g.frac;
+  }
+  double s = 0.0, err = 0.0;
+  for (int c = 0; c < nComp; c++) {
+    const double v = comp_value64_2d(sc[c], x, y);
+    const double adj = v - err;
+    const double tmp = s + adj;
+    err = (tmp - s) - adj;
+    s = tmp;
+  }
+  model[i * pitch + j] = s;
+}
+
+cudaError_t launch_eval64(const CompF64 *comps, int nComp, double *model, long pitch, Grid64 g,
+                          cudaStream_t st) {
+  const long n = (long)g.nCols * g.nRows;
+  if (n == 0) return cudaSuccess;
+  k_eval64<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(comps, nComp, model, pitch, g);
+  return cudaGetLastError();
+}
+
+// DownsampleAndReplace: core/downsample.cpp:54-109.  nRows_subregion uses the
+// column count (core/downsample.cpp:79); the caller has checked the reads stay
+// inside the region model.
+__global__ void k_downsample64(const double *__restrict__ os, int nOC, int osPsfCols, int osPsfRows,
+                               double *__restrict__ mainImg, int nMainCols, int i1, int j1, int nColsSub,
+                               int nRowsSub, int scale) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nColsSub * nRowsSub) return;
+  const int i_sub = t / nColsSub, j_sub = t % nColsSub;
+  const int jj1 = j_sub * scale + osPsfCols;
+  const int ii1 = i_sub * scale + osPsfRows;
+  double b = 0.0;
+  for (int ii = ii1; ii < ii1 + scale; ii++)
+    for (int jj = jj1; jj < jj1 + scale; jj++) b += os[(long)ii * nOC + jj];
+  const double area = scale * scale;
+  mainImg[(long)(i1 + i_sub) * nMainCols + (j1 + j_sub)] = b / area;
+}
+
+cudaError_t launch_downsample64(const double *region, int nOC, int nOR, int osPsfCols, int osPsfRows,
+                                double *mainImg, int nMainCols, int nMainRows, int mainPsfCols,
+                                int mainPsfRows, int x1, int y1, int scale, cudaStream_t st) {
+  (void)nOR;
+  (void)nMainRows;
+  const int j1 = x1 - 1 + mainPsfCols;
+  const int i1 = y1 - 1 + mainPsfRows;
+  const int nColsSub = (nOC - 2 * osPsfCols) / scale;
+  const int nRowsSub = (nOC - 2 * osPsfRows) / scale;
+  const int n = nColsSub * nRowsSub;
+  if (n <= 0) return cudaSuccess;
+  k_downsample64<<<(n + 127) / 128, 128, 0, st>>>(region, nOC, osPsfCols, osPsfRows, mainImg, nMainCols, i1, j1,
+                                                  nColsSub, nRowsSub, scale);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------- statistics
+#define LOG_SMALL_VALUE 1.0e-25  // core/model_object.cpp:86
+
+struct Term {
+  double w, d, m, extra;
+  long b;
+};
+
+__device__ __forceinline__ long model_index(const StatArgs64 &a, long b) {
+  const long row = b / a.nDataCols;
+  const long col = b - row * a.nDataCols;
+  return (long)a.modelCols * (a.offR + row) + a.offC + col;
+}
+
+// weight for term b; UpdateWeightVector (core/model_object.cpp:1345-1381)
+// when model-based errors are in use
+__device__ __forceinline__ double term_weight(const StatArgs64 &a, long b, double m) {
+  if (a.modelErrors && a.mask[b] > 0) {
+    const double tf = m + a.sky;
+    const double ns = tf / a.effGain + a.rnTerm;
+    return 1.0 / sqrt(ns);
+  }
+  return a.weight[b];
+}
+
+// ComputeDeviates (core/model_object.cpp:1413-1496) and
+// ComputePoissonMLRDeviate (core/model_object.cpp:1386-1401)
+__global__ void k_deviates64(StatArgs64 a, double *__restrict__ dev, double *__restrict__ wOut) {
+  const long z = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (z >= a.nz) return;
+  const long b = a.boot ? a.boot[z] : z;
+  const double m = a.model[model_index(a, b)];
+  const double w = term_weight(a, b, m);
+  if (wOut && a.modelErrors && !a.boot) wOut[b] = w;
+  double r;
+  if (a.kind == 2) {
+    const double mv = a.effGain * (m + a.sky);
+    const double dv = a.effGain * (a.data[b] + a.sky);
+    const double lm = (mv <= 0) ? LOG_SMALL_VALUE : log(mv);
+    r = sqrt(2.0 * w * fabs(mv - dv * lm + a.extra[b]));
+  } else {
+    r = w * (a.data[b] - m);
+  }
+  dev[z] = r;
+}
+
+cudaError_t launch_deviates64(const StatArgs64 &a, double *dev, double *wOut, cudaStream_t st) {
+  if (a.nz <= 0) return cudaSuccess;
+  k_deviates64<<<(unsigned)((a.nz + 255) / 256), 256, 0, st>>>(a, dev, wOut);
+  return cudaGetLastError();
+}
+
+// MINPACK enorm (core/mp_enorm.cpp:51-122) as a mergeable state: sums of
+// squares of large / intermediate / small magnitudes, the first and last
+// kept scaled by their running maxima.
+struct Enorm {
+  double s1, x1, s2, s3, x3;
+};
+
+__device__ __forceinline__ void enorm_add(Enorm &e, double v, double agiant) {
+  const double rdwarf = 3.834e-20;
+  const double xabs = fabs(v);
+  if (xabs > rdwarf && xabs < agiant) {
+    e.s2 += xabs * xabs;
+  } else if (xabs > rdwarf) {
+    if (xabs > e.x1) {
+      const double t = e.x1 / xabs;
+      e.s1 = 1.0 + e.s1 * t * t;
+      e.x1 = xabs;
+    } else {
+      const double t = xabs / e.x1;
+      e.s1 += t * t;
+    }
+  } else if (xabs > e.x3) {
+    const double t = e.x3 / xabs;
+    e.s3 = 1.0 + e.s3 * t * t;
+    e.x3 = xabs;
+  } else if (xabs != 0.0) {
+    const double t = xabs / e.x3;
+    e.s3 += t * t;
+  }
+}
+
+__device__ __forceinline__ void scaled_merge(double &s, double &x, double s2, double x2) {
+  if (x2 > x) {
+    const double t = x / x2;
+    s = s2 + s * t * t;
+    x = x2;
+  } else if (x2 > 0.0) {
+    const double t = x2 / x;
+    s += s2 * t * t;
+  }
+}
+
+__device__ __forceinline__ void enorm_merge(Enorm &a, const Enorm &b) {
+  scaled_merge(a.s1, a.x1, b.s1, b.x1);
+  a.s2 += b.s2;
+  scaled_merge(a.s3, a.x3, b.s3, b.x3);
+}
+
+__device__ __forceinline__ double enorm_final(const Enorm &e) {
+  if (e.s1 != 0.0) return e.x1 * sqrt(e.s1 + (e.s2 / e.x1) / e.x1);
+  if (e.s2 != 0.0) {
+    double temp;
+    if (e.s2 >= e.x3)
+      temp = e.s2 * (1.0 + (e.x3 / e.s2) * (e.x3 * e.s3));
+    else
+      temp = e.x3 * ((e.s2 / e.x3) + (e.x3 * e.s3));
+    return sqrt(temp);
+  }
+  return e.x3 * sqrt(e.s3);
+}
+
+__device__ __forceinline__ Enorm enorm_shfl(const Enorm &e, int off) {
+  Enorm o;
+  o.s1 = __shfl_down_sync(0xffffffffu, e.s1, off);
+  o.x1 = __shfl_down_sync(0xffffffffu, e.x1, off);
+  o.s2 = __shfl_down_sync(0xffffffffu, e.s2, off);
+  o.s3 = __shfl_down_sync(0xffffffffu, e.s3, off);
+  o.x3 = __shfl_down_sync(0xffffffffu, e.x3, off);
+  return o;
+}
+
+__device__ __forceinline__ Enorm block_enorm(Enorm e) {
+  __shared__ Enorm sh[32];
+  for (int off = 16; off > 0; off >>= 1) {
+    Enorm o = enorm_shfl(e, off);
+    enorm_merge(e, o);
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) sh[wid] = e;
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = blockDim.x >> 5;
+    e = (lane < nw) ? sh[lane] : Enorm{0, 0, 0, 0, 0};
+    for (int off = 16; off > 0; off >>= 1) {
+      Enorm o = enorm_shfl(e, off);
+      enorm_merge(e, o);
+    }
+  }
+  return e;
+}
+
+__device__ __forceinline__ double block_sum(double v) {
+  __shared__ double sh[32];
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = blockDim.x >> 5;
+    v = (lane < nw) ? sh[lane] : 0.0;
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+  }
+  return v;
+}
+
+// ChiSquared (core/model_object.cpp:1633-1689) and CashStatistic (:1703-1775),
+// first level: fixed grid, grid-stride terms, per-block partial state.
+__global__ void __launch_bounds__(256) k_stat64_partial(StatArgs64 a, double *__restrict__ partials) {
+  const long stride = (long)gridDim.x * blockDim.x;
+  if (a.kind == 0) {
+    Enorm e = {0, 0, 0, 0, 0};
+    const double agiant = 1.304e19 / (double)(int)a.nz;
+    for (long z = blockIdx.x * (long)blockDim.x + threadIdx.x; z < a.nz; z += stride) {
+      const long b = a.boot ? a.boot[z] : z;
+      const double m = a.model[model_index(a, b)];
+      const double w = term_weight(a, b, m);
+      enorm_add(e, w * (a.data[b] - m), agiant);
+    }
+    e = block_enorm(e);
+    if (threadIdx.x == 0) {
+      double *p = partials + blockIdx.x * 5;
+      p[0] = e.s1; p[1] = e.x1; p[2] = e.s2; p[3] = e.s3; p[4] = e.x3;
+    }
+  } else {
+    double s = 0.0;
+    for (long z = blockIdx.x * (long)blockDim.x + threadIdx.x; z < a.nz; z += stride) {
+      const long b = a.boot ? a.boot[z] : z;
+      const double mv = a.effGain * (a.model[model_index(a, b)] + a.sky);
+      const double dv = a.effGain * (a.data[b] + a.sky);
+      const double lm = (mv <= 0) ? LOG_SMALL_VALUE : log(mv);
+      s += a.weight[b] * (mv - dv * lm + a.extra[b]);
+    }
+    s = block_sum(s);
+    if (threadIdx.x == 0) partials[blockIdx.x * 5] = s;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_stat64_final(const double *__restrict__ partials, int nPart, int kind,
+                                                      double *__restrict__ result) {
+  if (kind == 0) {
+    Enorm e = {0, 0, 0, 0, 0};
+    for (int i = threadIdx.x; i < nPart; i += blockDim.x) {
+      const double *p = partials + i * 5;
+      Enorm o = {p[0], p[1], p[2], p[3], p[4]};
+      enorm_merge(e, o);
+    }
+    e = block_enorm(e);
+    if (threadIdx.x == 0) {
+      const double chi = enorm_final(e);
+      *result = chi * chi;
+    }
+  } else {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < nPart; i += blockDim.x) s += partials[i * 5];
+    s = block_sum(s);
+    if (threadIdx.x == 0) *result = 2.0 * s;
+  }
+}
+
+cudaError_t launch_statistic64(const StatArgs64 &a, double *partials, double *result, cudaStream_t st) {
+  k_stat64_partial<<<kStatBlocks, 256, 0, st>>>(a, partials);
+  k_stat64_final<<<1, 256, 0, st>>>(partials, kStatBlocks, a.kind == 0 ? 0 : 1, result);
+  return cudaGetLastError();
+}
+
+__global__ void __launch_bounds__(256) k_fd_dot_partial(const double *__restrict__ d0,
+                                                        const double *__restrict__ d1, long n, double invh,
+                                                        double *__restrict__ partials) {
+  const long stride = (long)gridDim.x * blockDim.x;
+  double s = 0.0;
+  for (long z = blockIdx.x * (long)blockDim.x + threadIdx.x; z < n; z += stride)
+    s += d0[z] * ((d1[z] - d0[z]) * invh);
+  s = block_sum(s);
+  if (threadIdx.x == 0) partials[blockIdx.x * 5] = s;
+}
+
+cudaError_t launch_fd_dot64(const double *dev0, const double *dev1, long n, double invh, double *partials,
+                            double *result, cudaStream_t st) {
+  k_fd_dot_partial<<<kStatBlocks, 256, 0, st>>>(dev0, dev1, n, invh, partials);
+  k_stat64_final<<<1, 256, 0, st>>>(partials, kStatBlocks, 1, result);  // returns 2*sum
+  return cudaGetLastError();
+}
+
+__global__ void k_crop64(const double *__restrict__ model, int modelCols, int offR, int offC, int nCols,
+                         int nRows, double *__restrict__ out) {
+  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (t >= (long)nCols * nRows) return;
+  const long r = t / nCols, c = t % nCols;
+  out[t] = model[(long)modelCols * (offR + r) + offC + c];
+}
+
+cudaError_t launch_crop64(const double *model, int modelCols, int offR, int offC, int nCols, int nRows,
+                          double *out, cudaStream_t st) {
+  const long n = (long)nCols * nRows;
+  if (n == 0) return cudaSuccess;
+  k_crop64<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(model, modelCols, offR, offC, nCols, nRows, out);
+  return cudaGetLastError();
+}
+
+// UpdateWeightVector (core/model_object.cpp:1345-1381): model-based weights
+// for unmasked pixels, recomputed after every model image.
+__global__ void k_update_weights64(const double *__restrict__ model, const double *__restrict__ mask,
+                                   double *__restrict__ weight, long nData, int nDataCols, int modelCols,
+                                   int offR, int offC, double effGain, double sky, double rnTerm) {
+  const long z = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (z >= nData || !(mask[z] > 0)) return;
+  const long row = z / nDataCols, col = z - row * nDataCols;
+  const double tf = model[(long)modelCols * (offR + row) + offC + col] + sky;
+  const double ns = tf / effGain + rnTerm;
+  weight[z] = 1.0 / sqrt(ns);
+}
+
+cudaError_t launch_update_weights64(const double *model, const double *mask, double *weight, long nData,
+                                    int nDataCols, int modelCols, int offR, int offC, double effGain, double sky,
+                                    double rnTerm, cudaStream_t st) {
+  if (nData <= 0) return cudaSuccess;
+  k_update_weights64<<<(unsigned)((nData + 255) / 256), 256, 0, st>>>(model, mask, weight, nData, nDataCols,
+                                                                        modelCols, offR, offC, effGain, sky, rnTerm);
+  return cudaGetLastError();
+}
+
+__global__ void k_f64_to_f32(const double *__restrict__ in, float *__restrict__ out, long n) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (float)in[i];
+}
+
+cudaError_t launch_f64_to_f32(const double *in, float *out, long n, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  k_f64_to_f32<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(in, out, n);
+  return cudaGetLastError();
+}
+
+}  // namespace imfit

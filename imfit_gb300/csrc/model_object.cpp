@@ -1,0 +1,1354 @@
+// model_object.cpp -- host facade of the GB300 library: a C++ restatement of
+// the reference's ModelObject state machine (core/model_object.cpp) whose
+// compute calls go to the kernels in k_plain.cu / k_fft.cu / k_fast.cu, and
+// the C ABI declared in include/imfit_gb300.h.
+//
+// Weight / mask / extra-term preparation stays on the host in FP64 with the
+// reference's expressions (bit-identical by construction); the results are
+// uploaded once at FinalSetupForFitting.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/imfit_gb300.h"
+#include "kernels.h"
+
+namespace imfit {
+cudaError_t launch_update_weights64(const double *model, const double *mask, double *weight, long nData,
+                                    int nDataCols, int modelCols, int offR, int offC, double effGain, double sky,
+                                    double rnTerm, cudaStream_t st);
+cudaError_t launch_f64_to_f32(const double *in, float *out, long n, cudaStream_t st);
+}  // namespace imfit
+
+using namespace imfit;
+
+namespace {
+
+const char *kVersion = "imfit-gb300 0.1 (sm_103a)";
+
+struct FuncInfo {
+  std::string name;
+  int type;
+  int nParams;
+  int subsample;
+  std::vector<std::string> paramNames;
+};
+
+bool lookup_function(const std::string &n, FuncInfo &f) {
+  // core/add_functions.cpp:170-248 (config names) and each class's PARAM_LABELS
+  static const std::map<std::string, std::pair<int, std::vector<std::string>>> reg = {
+      {"Sersic", {F_SERSIC, {"PA", "ell", "n", "I_e", "r_e"}}},
+      {"Exponential", {F_EXP, {"PA", "ell", "I_0", "h"}}},
+      {"FlatSky", {F_FLATSKY, {"I_sky"}}},
+      {"GaussianRing", {F_GRING, {"PA", "ell", "A", "R_ring", "sigma_r"}}},
+      {"Moffat", {F_MOFFAT, {"PA", "ell", "I_0", "fwhm", "beta"}}},
+      {"Gaussian", {F_GAUSS, {"PA", "ell", "I_0", "sigma"}}},
+      {"ExponentialDisk3D", {F_EXPDISK3D, {"PA", "inc", "J_0", "h", "n", "z_0"}}},
+      {"FerrersBar3D", {F_FERRERS3D, {"PA", "inc", "barPA", "J_0", "R_bar", "q", "q_z", "n"}}},
+  };
+  auto it = reg.find(n);
+  if (it == reg.end()) return false;
+  f.name = n;
+  f.type = it->second.first;
+  f.paramNames = it->second.second;
+  f.nParams = (int)f.paramNames.size();
+  f.subsample = (f.type == F_EXPDISK3D || f.type == F_FERRERS3D) ? 0 : 1;
+  return true;
+}
+
+// Kahan-summed normalisation (core/convolver.cpp:296-311, core/model_object.cpp:2581-2594)
+double kahan_sum(const double *v, long n) {
+  double s = 0.0, err = 0.0, adj, tmp;
+  for (long k = 0; k < n; k++) {
+    adj = v[k] - err;
+    tmp = s + adj;
+    err = (tmp - s) - adj;
+    s = tmp;
+  }
+  return s;
+}
+
+// MT19937 (Matsumoto & Nishimura 1998) as used by the reference's bootstrap
+// (core/mersenne_twister.cpp:60-166).
+struct MT19937 {
+  unsigned long mt[624];
+  int mti = 625;
+  void seed(unsigned long s) {
+    mt[0] = s & 0xffffffffUL;
+    for (int i = 1; i < 624; i++) mt[i] = (1812433253UL * (mt[i - 1] ^ (mt[i - 1] >> 30)) + i) & 0xffffffffUL;
+    mti = 624;
+  }
+  unsigned long next() {
+    static const unsigned long mag01[2] = {0x0UL, 0x9908b0dfUL};
+    unsigned long y;
+    if (mti >= 624) {
+      if (mti == 625) seed(5489UL);
+      int kk;
+      for (kk = 0; kk < 227; kk++) {
+        y = (mt[kk] & 0x80000000UL) | (mt[kk + 1] & 0x7fffffffUL);
+        mt[kk] = mt[kk + 397] ^ (y >> 1) ^ mag01[y & 1UL];
+      }
+      for (; kk < 623; kk++) {
+        y = (mt[kk] & 0x80000000UL) | (mt[kk + 1] & 0x7fffffffUL);
+        mt[kk] = mt[kk - 227] ^ (y >> 1) ^ mag01[y & 1UL];
+      }
+      y = (mt[623] & 0x80000000UL) | (mt[0] & 0x7fffffffUL);
+      mt[623] = mt[396] ^ (y >> 1) ^ mag01[y & 1UL];
+      mti = 0;
+    }
+    y = mt[mti++];
+    y ^= (y >> 11);
+    y ^= (y << 7) & 0x9d2c5680UL;
+    y ^= (y << 15) & 0xefc60000UL;
+    y ^= (y >> 18);
+    return y & 0xffffffffUL;
+  }
+  double real2() { return (double)next() * (1.0 / 4294967296.0); }
+};
+
+template <typename T>
+struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  cudaError_t reserve(size_t count) {
+    if (count <= n && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    cudaError_t e = cudaMalloc(&p, sizeof(T) * (count ? count : 1));
+    if (e == cudaSuccess) n = count;
+    return e;
+  }
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+};
+
+struct Region {
+  int x1, y1, nBaseCols, nBaseRows, scale;
+  int nPsfCols, nPsfRows;
+  std::vector<double> psf;  // normalised as the region's Convolver does
+  double psfSum = 1.0;
+  int nModelCols, nModelRows;
+  long nModelVals;
+  FFTLen Lx, Ly;
+  DevBuf<double> model;
+  DevBuf<double> spec;   // complex, Ly x (Lx/2+1)
+  DevBuf<double> H;      // complex
+  int nColsSub, nRowsSub;
+};
+
+struct Captured {
+  int nBatch = -1;
+  const void *p = nullptr, *s = nullptr, *g = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+}  // namespace
+
+struct imfit_model_s {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string lastError;
+
+  // functions
+  std::vector<FuncInfo> funcs;
+  std::vector<int> setStart;
+  bool setsDefined = false;
+  int nParamsTot = 0;
+  std::vector<int> paramOffset, x0Index;
+  std::vector<std::string> paramNames;
+
+  // PSF / model grid
+  bool doConv = false;
+  int nPsfCols = 0, nPsfRows = 0;
+  std::vector<double> psf;  // normalised (Convolver) copy
+  bool psfNormalize = true;
+  double psfSum = 1.0;
+  bool modelSetupDone = false, modelComputed = false;
+  int nDataCols = 0, nDataRows = 0, nModelCols = 0, nModelRows = 0;
+  long nDataVals = 0, nValid = 0, nModelVals = 0;
+
+  // data & statistic state (host, FP64, reference semantics)
+  std::vector<double> data, weight, mask, extra;
+  bool dataValsSet = false, weightValsSet = false, maskExists = false;
+  bool dataErrors = true, modelErrors = false, externalErrors = false;
+  bool useCash = false, pmlr = false, doBootstrap = false, finalSetupDone = false;
+  double gain = 1.0, readNoise = 0.0, expTime = 1.0, sky = 0.0, effGain = 1.0, rnAduSq = 0.0;
+  int nCombined = 1;
+  std::vector<long> bootIdx;
+  MT19937 rng;
+
+  std::vector<Region *> regions;
+
+  // plain FP64 device state
+  FFTLen Lx, Ly;
+  DevBuf<double> dModel, dSpec, dH, dData, dWeight, dMask, dExtra, dDev, dDev2, dPart, dRes;
+  DevBuf<long> dBoot;
+  DevBuf<CompF64> dComps;
+  std::vector<CompF64> hComps;
+  double *hPinned = nullptr;  // pinned scratch for small transfers
+  size_t hPinnedN = 0;
+
+  // fast FP32 device state
+  bool fastReady = false;
+  FastGeom fg{};
+  FFTLen Fx, Fy, FRx, FRy;
+  DevBuf<float> dH32, dHr32, dData32, dW32, dExtra32, dCount32, dBg, dRegModel, dRegG, dModelOut;
+  DevBuf<float> dSpec32, dRSpec32;  // complex
+  DevBuf<CompDesc> dDesc;
+  DevBuf<CompF32> dComps32;
+  DevBuf<double> dParams, dStatPart, dGradPart, dStat, dGrad;
+  int fastCap = 0;
+  bool useGraphs = true;
+  Captured graph;
+
+  ~imfit_model_s() {
+    for (Region *r : regions) {
+      fftlen_destroy(r->Lx);
+      fftlen_destroy(r->Ly);
+      delete r;
+    }
+    fftlen_destroy(Lx);
+    fftlen_destroy(Ly);
+    fftlen_destroy(Fx);
+    fftlen_destroy(Fy);
+    fftlen_destroy(FRx);
+    fftlen_destroy(FRy);
+    if (graph.exec) cudaGraphExecDestroy(graph.exec);
+    if (hPinned) cudaFreeHost(hPinned);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  int fail(int code, const std::string &msg) {
+    lastError = msg;
+    return code;
+  }
+  int cuda_fail(cudaError_t e, const char *where) {
+    lastError = std::string(where) + ": " + cudaGetErrorString(e);
+    return (e == cudaErrorMemoryAllocation) ? IMFIT_E_NOMEM : IMFIT_E_CUDA;
+  }
+  double *pinned(size_t n) {
+    if (n > hPinnedN) {
+      if (hPinned) cudaFreeHost(hPinned);
+      hPinned = nullptr;
+      if (cudaMallocHost(&hPinned, sizeof(double) * n) != cudaSuccess) {
+        hPinnedN = 0;
+        return nullptr;
+      }
+      hPinnedN = n;
+    }
+    return hPinned;
+  }
+
+  long modelIndex(long z) const {
+    if (!doConv) return z;
+    long row = z / nDataCols, col = z - row * nDataCols;
+    return (long)nModelCols * (nPsfRows + row) + nPsfCols + col;
+  }
+
+  // -------------------------------------------------------------- setup
+  int defineSets(const int *starts, int n) {
+    if (funcs.empty()) return fail(IMFIT_E_STATE, "DefineFunctionSets: no functions added");
+    setStart.assign(funcs.size(), 0);
+    setStart[0] = 1;
+    for (int i = 0; i < n; i++) {
+      if (starts[i] < 0 || starts[i] >= (int)funcs.size()) return fail(IMFIT_E_ARG, "bad function-set index");
+      setStart[starts[i]] = 1;
+    }
+    paramOffset.assign(funcs.size(), 0);
+    x0Index.assign(funcs.size(), 0);
+    int off = 0, xi = 0;
+    for (size_t f = 0; f < funcs.size(); f++) {
+      if (setStart[f]) {
+        xi = off;
+        off += 2;
+      }
+      x0Index[f] = xi;
+      paramOffset[f] = off;
+      off += funcs[f].nParams;
+    }
+    nParamsTot = off;
+    if (nParamsTot > kMaxParams) return fail(IMFIT_E_UNSUPPORTED, "too many parameters");
+    setsDefined = true;
+    fastReady = false;
+    return 0;
+  }
+
+  void populateNames() {
+    paramNames.clear();
+    for (size_t f = 0; f < funcs.size(); f++) {
+      if (setStart[f]) {
+        paramNames.push_back("X0");
+        paramNames.push_back("Y0");
+      }
+      for (auto &s : funcs[f].paramNames) paramNames.push_back(s);
+    }
+  }
+
+  // FP64 spectrum of a real Ly x Lx array (host) via the device FFT kernels
+  int spectrum64(const std::vector<double> &padded, const FFTLen &fx, const FFTLen &fy, DevBuf<double> &H) {
+    const int nc = fx.L / 2 + 1;
+    DevBuf<double> tmp;
+    cudaError_t e = tmp.reserve(padded.size());
+    if (!e) e = H.reserve(2 * (size_t)fy.L * nc);
+    if (!e) e = cudaMemcpyAsync(tmp.p, padded.data(), sizeof(double) * padded.size(), cudaMemcpyHostToDevice, stream);
+    if (!e) e = launch_rows_r2c<double>(tmp.p, fx.L, 0, fx.L, fy.L, H.p, nc, 0, fx, 1, stream);
+    if (!e) e = launch_cols<double>(H.p, nc, 0, nc, fy.L, fy.L, nullptr, 0, fy, 1.0, 0, 1, stream);
+    if (!e) e = cudaStreamSynchronize(stream);
+    if (e) return cuda_fail(e, "PSF spectrum");
+    return 0;
+  }
+
+  // padded PSF with the centre pixel (P/2) wrapped to (0,0): ShiftAndWrapPSF
+  // (core/convolver.cpp:421-441)
+  static std::vector<double> wrap_psf(const std::vector<double> &p, int pc, int pr, int Lx, int Ly) {
+    std::vector<double> out((size_t)Lx * Ly, 0.0);
+    const int cx = pc / 2, cy = pr / 2;
+    for (int i = 0; i < pr; i++)
+      for (int j = 0; j < pc; j++) {
+        const int dc = (Lx - cx + j) % Lx, dr = (Ly - cy + i) % Ly;
+        out[(size_t)dr * Lx + dc] = p[(size_t)i * pc + j];
+      }
+    return out;
+  }
+
+  int setupModelImage(int nc, int nr) {
+    if (nc < 1 || nr < 1) return fail(IMFIT_E_ARG, "SetupModelImage: bad size");
+    nDataCols = nc;
+    nDataRows = nr;
+    nDataVals = (long)nc * nr;
+    if (doConv) {
+      nModelCols = nc + 2 * nPsfCols;
+      nModelRows = nr + 2 * nPsfRows;
+      // reference padding N_model + P - 1 (core/convolver.cpp:217-219), rounded up to a 7-smooth size
+      int e1 = fftlen_create(Lx, smooth_size(nModelCols + nPsfCols - 1, true));
+      int e2 = fftlen_create(Ly, smooth_size(nModelRows + nPsfRows - 1, true));
+      if (e1 || e2) return fail(IMFIT_E_CUDA, "FFT tables");
+      int st = spectrum64(wrap_psf(psf, nPsfCols, nPsfRows, Lx.L, Ly.L), Lx, Ly, dH);
+      if (st) return st;
+      cudaError_t e = dSpec.reserve(2 * (size_t)Ly.L * (Lx.L / 2 + 1));
+      if (e) return cuda_fail(e, "spectrum buffer");
+    } else {
+      nModelCols = nc;
+      nModelRows = nr;
+    }
+    nModelVals = (long)nModelCols * nModelRows;
+    cudaError_t e = dModel.reserve(nModelVals);
+    if (e) return cuda_fail(e, "model buffer");
+    modelSetupDone = true;
+    fastReady = false;
+    return 0;
+  }
+
+  int addRegion(const double *p, int pc, int pr, int scale, int x1, int x2, int y1, int y2, int normalize) {
+    if (!modelSetupDone) return fail(IMFIT_E_STATE, "AddOversampledPsfInfo: SetupModelImage not called");
+    if (pc < 1 || pr < 1 || scale < 1 || x1 >= x2 || y1 >= y2) return fail(IMFIT_E_ARG, "bad oversampled region");
+    for (long i = 0; i < (long)pc * pr; i++)
+      if (!std::isfinite(p[i])) return fail(IMFIT_E_ARG, "Oversampled PSF image has non-finite values");
+    if (x1 < 1) x1 = 1;
+    if (y1 < 1) y1 = 1;
+    if (x2 > nDataCols) x2 = nDataCols;
+    if (y2 > nDataRows) y2 = nDataRows;
+    Region *r = new Region();
+    r->x1 = x1;
+    r->y1 = y1;
+    r->nBaseCols = x2 - x1 + 1;
+    r->nBaseRows = y2 - y1 + 1;
+    r->scale = scale;
+    r->nPsfCols = pc;
+    r->nPsfRows = pr;
+    r->psf.assign(p, p + (size_t)pc * pr);
+    if (normalize) {
+      const double s = kahan_sum(r->psf.data(), (long)r->psf.size());
+      for (auto &v : r->psf) v = v / s;
+    }
+    r->psfSum = 0.0;
+    for (double v : r->psf) r->psfSum += v;
+    r->nModelCols = r->nBaseCols * scale + 2 * pc;
+    r->nModelRows = r->nBaseRows * scale + 2 * pr;
+    r->nModelVals = (long)r->nModelCols * r->nModelRows;
+    r->nColsSub = (r->nModelCols - 2 * pc) / scale;
+    r->nRowsSub = (r->nModelCols - 2 * pr) / scale;  // core/downsample.cpp:79 uses the column count
+    // the reference reads region-model rows up to (nRowsSub)*k + pr - 1 and
+    // writes main pixels up to row y1-1+P+nRowsSub-1: both must stay in range
+    const int lastRow = (r->nRowsSub - 1) * scale + pr + scale - 1;
+    const int pcm = doConv ? nPsfCols : 0, prm = doConv ? nPsfRows : 0;
+    if (r->nRowsSub < 1 || lastRow >= r->nModelRows || (y1 - 1 + prm + r->nRowsSub) > nModelRows ||
+        (x1 - 1 + pcm + r->nColsSub) > nModelCols) {
+      delete r;
+      return fail(IMFIT_E_UNSUPPORTED,
+                  "oversampled region shape would make DownsampleAndReplace read/write outside its images");
+    }
+    int e1 = fftlen_create(r->Lx, smooth_size(r->nModelCols + pc - 1, true));
+    int e2 = fftlen_create(r->Ly, smooth_size(r->nModelRows + pr - 1, true));
+    if (e1 || e2) {
+      delete r;
+      return fail(IMFIT_E_CUDA, "FFT tables");
+    }
+    int st = spectrum64(wrap_psf(r->psf, pc, pr, r->Lx.L, r->Ly.L), r->Lx, r->Ly, r->H);
+    if (st) {
+      delete r;
+      return st;
+    }
+    cudaError_t e = r->model.reserve(r->nModelVals);
+    if (!e) e = r->spec.reserve(2 * (size_t)r->Ly.L * (r->Lx.L / 2 + 1));
+    if (e) {
+      delete r;
+      return cuda_fail(e, "region buffers");
+    }
+    regions.push_back(r);
+    fastReady = false;
+    return 0;
+  }
+
+  // GenerateErrorVector (core/model_object.cpp:642-673)
+  void generateErrorVector() {
+    weight.assign(nDataVals, 0.0);
+    for (long z = 0; z < nDataVals; z++) {
+      double tf = data[z] + sky;
+      if (tf < 0.0) tf = 0.0;
+      const double ns = tf / effGain + nCombined * rnAduSq;
+      weight[z] = 1.0 / sqrt(ns);
+    }
+    weightValsSet = true;
+  }
+
+  // FinalSetupForFitting (core/model_object.cpp:967-1079)
+  int finalSetup() {
+    if (!dataValsSet) return fail(IMFIT_E_STATE, "FinalSetupForFitting: no image data");
+    int ret = 0;
+    const long n = nDataVals;
+    if (!maskExists) {
+      mask.assign(n, 1.0);
+      maskExists = true;
+    }
+    for (long z = 0; z < n; z++)
+      if (mask[z] > 0.0 && !std::isfinite(data[z])) {
+        mask[z] = 0.0;
+        nValid--;
+      }
+    if (!useCash && dataErrors && !externalErrors) generateErrorVector();
+    if (useCash && pmlr) {
+      // GenerateExtraCashTerms (core/model_object.cpp:695-709)
+      for (long z = 0; z < n; z++) {
+        const double dv = effGain * (data[z] + sky);
+        extra[z] = (dv <= 0.0) ? 0.0 : dv * log(dv) - dv;
+      }
+    }
+    if (externalErrors) {
+      for (long z = 0; z < n; z++)
+        if (mask[z] > 0.0 && !std::isfinite(weight[z])) {
+          mask[z] = 0.0;
+          weight[z] = 0.0;
+          nValid--;
+        }
+    }
+    // ApplyMask (core/model_object.cpp:794-816)
+    if (weightValsSet && maskExists) {
+      for (long z = 0; z < n; z++) {
+        double nv = mask[z] * weight[z];
+        if (!std::isfinite(nv) && mask[z] == 0.0) nv = 0.0;
+        weight[z] = nv;
+      }
+    }
+    // CheckWeightVector (core/model_object.cpp:2508-2550)
+    bool nonfinite = false, negative = false;
+    for (long z = 0; z < n; z++)
+      if (mask[z] > 0.0) {
+        if (!std::isfinite(weight[z])) nonfinite = true;
+        else if (weight[z] < 0.0) negative = true;
+      }
+    if (nonfinite || negative) ret = -1;
+    // VetDataVector (core/model_object.cpp:2496-2506)
+    bool bad = false;
+    for (long z = 0; z < n; z++)
+      if (!std::isfinite(data[z])) {
+        if (mask[z] > 0.0) bad = true;
+        else data[z] = 0.0;
+      }
+    if (bad) ret = -2;
+    if (nValid < 1) ret = -3;
+    // upload
+    cudaError_t e = dData.reserve(n);
+    if (!e) e = dWeight.reserve(n);
+    if (!e) e = dMask.reserve(n);
+    if (!e) e = dExtra.reserve(n);
+    if (!e) e = dDev.reserve(n);
+    if (!e) e = dDev2.reserve(n);
+    if (!e) e = dPart.reserve(kStatBlocks * 8);
+    if (!e) e = dRes.reserve(kMaxParams + 8);
+    if (!e) e = cudaMemcpy(dData.p, data.data(), sizeof(double) * n, cudaMemcpyHostToDevice);
+    if (!e) e = cudaMemcpy(dWeight.p, weight.data(), sizeof(double) * n, cudaMemcpyHostToDevice);
+    if (!e) e = cudaMemcpy(dMask.p, mask.data(), sizeof(double) * n, cudaMemcpyHostToDevice);
+    if (!e && !extra.empty()) e = cudaMemcpy(dExtra.p, extra.data(), sizeof(double) * n, cudaMemcpyHostToDevice);
+    if (!e && extra.empty()) e = cudaMemset(dExtra.p, 0, sizeof(double) * n);
+    if (e) return cuda_fail(e, "FinalSetupForFitting upload");
+    finalSetupDone = true;
+    fastReady = false;
+    if (ret == -1) lastError = "bad values detected in weight vector";
+    if (ret == -2) lastError = "bad (non-masked) data values";
+    if (ret == -3) lastError = "not enough valid data values available for fitting";
+    return ret;
+  }
+
+  // -------------------------------------------------------- plain path
+  int checkEval() {
+    if (!setsDefined) return fail(IMFIT_E_STATE, "DefineFunctionSets not called");
+    if (!modelSetupDone) return fail(IMFIT_E_STATE, "SetupModelImage not called");
+    for (auto &f : funcs)
+      if (f.type == F_EXPDISK3D || f.type == F_FERRERS3D)
+        return fail(IMFIT_E_UNSUPPORTED, "3-D line-of-sight functions are not available on the plain path");
+    return 0;
+  }
+
+  void setupComps(const double *params, CompF64 *out) {
+    double x0 = 0.0, y0 = 0.0;
+    for (size_t f = 0; f < funcs.size(); f++) {
+      if (setStart[f]) {
+        x0 = params[x0Index[f]];
+        y0 = params[x0Index[f] + 1];
+      }
+      comp_setup64(out[f], funcs[f].type, funcs[f].subsample, params + paramOffset[f], x0, y0);
+    }
+  }
+
+  cudaError_t conv64(double *img, int nCols, int nRows, const FFTLen &fx, const FFTLen &fy, const double *H,
+                     double *spec) {
+    const int nc = fx.L / 2 + 1;
+    cudaError_t e = launch_rows_r2c<double>(img, nCols, 0, nCols, nRows, spec, nc, 0, fx, 1, stream);
+    if (!e) e = launch_cols<double>(spec, nc, 0, nc, nRows, nRows, H, nc, fy, 1.0 / ((double)fx.L * fy.L), 1, 1, stream);
+    if (!e) e = launch_rows_c2r<double>(spec, nc, 0, nRows, img, nCols, 0, nCols, 1.0, fx, 1, stream);
+    return e;
+  }
+
+  // CreateModelImage (core/model_object.cpp:1103-1229) with comps already on the device
+  cudaError_t enqueueModel(const CompF64 *dC) {
+    const int nC = (int)funcs.size();
+    Grid64 g{};
+    g.nCols = nModelCols;
+    g.nRows = nModelRows;
+    g.pc = doConv ? nPsfCols : 0;
+    g.pr = doConv ? nPsfRows : 0;
+    cudaError_t e = launch_eval64(dC, nC, dModel.p, nModelCols, g, stream);
+    if (!e && doConv) e = conv64(dModel.p, nModelCols, nModelRows, Lx, Ly, dH.p, dSpec.p);
+    for (Region *r : regions) {
+      if (e) break;
+      Grid64 rg{};
+      rg.nCols = r->nModelCols;
+      rg.nRows = r->nModelRows;
+      rg.pc = r->nPsfCols;
+      rg.pr = r->nPsfRows;
+      rg.isRegion = 1;
+      rg.x1 = r->x1;
+      rg.y1 = r->y1;
+      rg.frac = 1.0 / r->scale;
+      rg.off = 0.5 * rg.frac - 0.5;
+      e = launch_eval64(dC, nC, r->model.p, r->nModelCols, rg, stream);
+      if (!e) e = conv64(r->model.p, r->nModelCols, r->nModelRows, r->Lx, r->Ly, r->H.p, r->spec.p);
+      if (!e)
+        e = launch_downsample64(r->model.p, r->nModelCols, r->nModelRows, r->nPsfCols, r->nPsfRows, dModel.p,
+                                nModelCols, nModelRows, doConv ? nPsfCols : 0, doConv ? nPsfRows : 0, r->x1, r->y1,
+                                r->scale, stream);
+    }
+    if (!e && modelErrors && finalSetupDone)
+      e = launch_update_weights64(dModel.p, dMask.p, dWeight.p, nDataVals, nDataCols, nModelCols,
+                                  doConv ? nPsfRows : 0, doConv ? nPsfCols : 0, effGain, sky, nCombined * rnAduSq,
+                                  stream);
+    return e;
+  }
+
+  int createModelImage(const double *params) {
+    int st = checkEval();
+    if (st) return st;
+    const int nC = (int)funcs.size();
+    hComps.resize(nC);
+    setupComps(params, hComps.data());
+    cudaError_t e = dComps.reserve(nC);
+    if (!e) e = cudaMemcpyAsync(dComps.p, hComps.data(), sizeof(CompF64) * nC, cudaMemcpyHostToDevice, stream);
+    if (!e) e = enqueueModel(dComps.p);
+    if (!e) e = cudaStreamSynchronize(stream);  // hComps is pageable and reused
+    if (e) return cuda_fail(e, "CreateModelImage");
+    modelComputed = true;
+    return 0;
+  }
+
+  StatArgs64 statArgs(int kind) {
+    StatArgs64 a{};
+    a.model = dModel.p;
+    a.data = dData.p;
+    a.weight = dWeight.p;
+    a.extra = dExtra.p;
+    a.mask = dMask.p;
+    a.boot = doBootstrap ? dBoot.p : nullptr;
+    a.nz = doBootstrap ? nValid : nDataVals;
+    a.nDataCols = nDataCols;
+    a.modelCols = nModelCols;
+    a.offR = doConv ? nPsfRows : 0;
+    a.offC = doConv ? nPsfCols : 0;
+    a.effGain = effGain;
+    a.sky = sky;
+    a.rnTerm = nCombined * rnAduSq;
+    a.modelErrors = 0;  // weights are updated in place after each model
+    a.kind = kind;
+    return a;
+  }
+
+  int statKind() const { return useCash ? (pmlr ? 2 : 1) : 0; }
+
+  int getFitStatistic(const double *params, double *out, int forceKind = -1) {
+    if (!finalSetupDone) return fail(IMFIT_E_STATE, "FinalSetupForFitting not called");
+    int st = createModelImage(params);
+    if (st) return st;
+    int kind = forceKind >= 0 ? forceKind : statKind();
+    if (kind == 2) kind = 1;  // GetFitStatistic -> CashStatistic for PMLR (core/model_object.cpp:1620-1626)
+    cudaError_t e = launch_statistic64(statArgs(kind), dPart.p, dRes.p, stream);
+    double *h = pinned(8);
+    if (!e) e = cudaMemcpyAsync(h, dRes.p, sizeof(double), cudaMemcpyDeviceToHost, stream);
+    if (!e) e = cudaStreamSynchronize(stream);
+    if (e) return cuda_fail(e, "GetFitStatistic");
+    *out = h[0];
+    return 0;
+  }
+
+  int computeDeviates(double *y, const double *params) {
+    if (!finalSetupDone) return fail(IMFIT_E_STATE, "FinalSetupForFitting not called");
+    int st = createModelImage(params);
+    if (st) return st;
+    StatArgs64 a = statArgs(pmlr ? 2 : 0);
+    cudaError_t e = launch_deviates64(a, dDev.p, nullptr, stream);
+    if (!e) e = cudaMemcpyAsync(y, dDev.p, sizeof(double) * a.nz, cudaMemcpyDeviceToHost, stream);
+    if (!e) e = cudaStreamSynchronize(stream);
+    if (e) return cuda_fail(e, "ComputeDeviates");
+    return 0;
+  }
+
+  // statistic + FD gradient (1 + nParams plain evaluations)
+  int fdGradient(const double *params, double *stat, double *grad) {
+    if (!finalSetupDone) return fail(IMFIT_E_STATE, "FinalSetupForFitting not called");
+    int st = checkEval();
+    if (st) return st;
+    const int nP = nParamsTot, nC = (int)funcs.size();
+    const double eps = sqrt(2.2204460e-16);  // MP_MACHEP0 (solvers/mpfit.h)
+    std::vector<CompF64> all((size_t)(nP + 1) * nC);
+    std::vector<double> x(params, params + nP), h(nP);
+    setupComps(x.data(), all.data());
+    for (int j = 0; j < nP; j++) {
+      const double t = x[j];
+      double hh = eps * fabs(t);
+      if (hh == 0.0) hh = eps;
+      h[j] = hh;
+      x[j] = t + hh;
+      setupComps(x.data(), all.data() + (size_t)(j + 1) * nC);
+      x[j] = t;
+    }
+    cudaError_t e = dComps.reserve(all.size());
+    if (!e) e = cudaMemcpyAsync(dComps.p, all.data(), sizeof(CompF64) * all.size(), cudaMemcpyHostToDevice, stream);
+    const bool chi = !useCash;
+    StatArgs64 a = statArgs(chi ? 0 : 1);
+    if (!e) e = enqueueModel(dComps.p);
+    if (!e) e = launch_statistic64(a, dPart.p, dRes.p, stream);
+    if (chi && !e) e = launch_deviates64(statArgs(0), dDev.p, nullptr, stream);
+    for (int j = 0; j < nP && !e; j++) {
+      e = enqueueModel(dComps.p + (size_t)(j + 1) * nC);
+      if (e) break;
+      if (chi) {
+        e = launch_deviates64(statArgs(0), dDev2.p, nullptr, stream);
+        if (!e) e = launch_fd_dot64(dDev.p, dDev2.p, a.nz, 1.0 / h[j], dPart.p, dRes.p + 1 + j, stream);
+      } else {
+        e = launch_statistic64(a, dPart.p, dRes.p + 1 + j, stream);
+      }
+    }
+    double *hb = pinned(nP + 1);
+    if (!e) e = cudaMemcpyAsync(hb, dRes.p, sizeof(double) * (nP + 1), cudaMemcpyDeviceToHost, stream);
+    if (!e) e = cudaStreamSynchronize(stream);
+    if (e) return cuda_fail(e, "FD gradient");
+    *stat = hb[0];
+    for (int j = 0; j < nP; j++) grad[j] = chi ? hb[1 + j] : (hb[1 + j] - hb[0]) / h[j];
+    modelComputed = true;
+    return 0;
+  }
+
+  // --------------------------------------------------------- fast path
+  int prepareFast() {
+    if (fastReady) return 0;
+    if (!finalSetupDone) return fail(IMFIT_E_STATE, "FinalSetupForFitting not called");
+    if (!setsDefined) return fail(IMFIT_E_STATE, "DefineFunctionSets not called");
+    for (auto &f : funcs)
+      if (f.type == F_EXPDISK3D || f.type == F_FERRERS3D)
+        return fail(IMFIT_E_UNSUPPORTED, "3-D line-of-sight functions are not available on the fast path");
+    if (regions.size() > 1) return fail(IMFIT_E_UNSUPPORTED, "fast path supports at most one oversampled region");
+    if ((int)funcs.size() > kMaxComponents) return fail(IMFIT_E_UNSUPPORTED, "too many components");
+    const int pc = doConv ? nPsfCols : 1, pr = doConv ? nPsfRows : 1;
+    std::vector<double> kp = doConv ? psf : std::vector<double>{1.0};
+    FastGeom &g = fg;
+    g = FastGeom{};
+    g.nDataCols = nDataCols;
+    g.nDataRows = nDataRows;
+    g.winCols = nDataCols + pc - 1;
+    g.winRows = nDataRows + pr - 1;
+    g.xOrig = 2 - pc + pc / 2;
+    g.yOrig = 2 - pr + pr / 2;
+    fftlen_destroy(Fx);
+    fftlen_destroy(Fy);
+    if (fftlen_create(Fx, smooth_size(g.winCols, true)) || fftlen_create(Fy, smooth_size(g.winRows, true)))
+      return fail(IMFIT_E_CUDA, "FFT tables");
+    if (Fx.L / 2 > 4096 || Fy.L > 4096) return fail(IMFIT_E_UNSUPPORTED, "image too large for the fast path");
+    g.specPitch = Fx.L / 2 + 1;
+    g.specBatch = (long)Fy.L * g.specPitch;
+    // PSF placed so that circular output (r,c) is the data pixel (r,c)
+    int st = shiftedSpectrum32(kp, pc, pr, Fx, Fy, dH32);
+    if (st) return st;
+    double ps = 0.0;
+    for (double v : kp) ps += v;
+    psfSumFast = ps;
+    psfSumOsFast = 1.0;
+    if (!regions.empty()) {
+      Region *r = regions[0];
+      const int k = r->scale;
+      g.hasRegion = 1;
+      g.rx0 = r->x1 - 1;
+      g.ry0 = r->y1 - 1;
+      g.rCols = r->nColsSub;
+      g.rRows = r->nRowsSub;
+      if (g.rRows > r->nBaseRows || g.rCols > r->nBaseCols || g.ry0 + g.rRows > nDataRows ||
+          g.rx0 + g.rCols > nDataCols)
+        return fail(IMFIT_E_UNSUPPORTED, "fast path needs the replaced region inside the region model and the image");
+      g.rScale = k;
+      g.rSubCols = g.rCols * k;
+      g.rSubRows = g.rRows * k;
+      g.rWinCols = g.rSubCols + r->nPsfCols - 1;
+      g.rWinRows = g.rSubRows + r->nPsfRows - 1;
+      g.rXBase = r->x1;
+      g.rYBase = r->y1;
+      g.rWinOffX = 1 + r->nPsfCols / 2 - r->nPsfCols;
+      g.rWinOffY = 1 + r->nPsfRows / 2 - r->nPsfRows;
+      const double frac = 1.0 / k;
+      g.rFrac = (float)frac;
+      g.rStartOff = (float)(0.5 * frac - 0.5);
+      fftlen_destroy(FRx);
+      fftlen_destroy(FRy);
+      if (fftlen_create(FRx, smooth_size(g.rWinCols, true)) || fftlen_create(FRy, smooth_size(g.rWinRows, true)))
+        return fail(IMFIT_E_CUDA, "FFT tables");
+      if (FRx.L / 2 > 4096 || FRy.L > 4096) return fail(IMFIT_E_UNSUPPORTED, "region too large for the fast path");
+      g.rSpecPitch = FRx.L / 2 + 1;
+      g.rSpecBatch = (long)FRy.L * g.rSpecPitch;
+      st = shiftedSpectrum32(r->psf, r->nPsfCols, r->nPsfRows, FRx, FRy, dHr32);
+      if (st) return st;
+      psfSumOsFast = r->psfSum;
+    }
+    // FP32 statistic inputs
+    const long n = nDataVals;
+    std::vector<float> f32(n);
+    cudaError_t e = dData32.reserve(n);
+    if (!e) e = dW32.reserve(n);
+    if (!e) e = dExtra32.reserve(n);
+    if (!e) e = dCount32.reserve(n);
+    if (e) return cuda_fail(e, "fast buffers");
+    for (long z = 0; z < n; z++) f32[z] = (float)data[z];
+    e = cudaMemcpy(dData32.p, f32.data(), sizeof(float) * n, cudaMemcpyHostToDevice);
+    for (long z = 0; z < n; z++) f32[z] = (float)weight[z];
+    if (!e) e = cudaMemcpy(dW32.p, f32.data(), sizeof(float) * n, cudaMemcpyHostToDevice);
+    for (long z = 0; z < n; z++) f32[z] = extra.empty() ? 0.f : (float)extra[z];
+    if (!e) e = cudaMemcpy(dExtra32.p, f32.data(), sizeof(float) * n, cudaMemcpyHostToDevice);
+    if (!e) e = uploadCounts();
+    // component descriptors
+    std::vector<CompDesc> desc(funcs.size());
+    for (size_t f = 0; f < funcs.size(); f++) {
+      CompDesc &d = desc[f];
+      d = CompDesc{};
+      d.type = funcs[f].type;
+      d.subsample = funcs[f].subsample;
+      d.paramOffset = paramOffset[f];
+      d.x0Index = x0Index[f];
+      d.nParams = funcs[f].nParams;
+      d.background = (funcs[f].type == F_FLATSKY) ? 1 : 0;
+    }
+    if (!e) e = dDesc.reserve(desc.size());
+    if (!e) e = cudaMemcpy(dDesc.p, desc.data(), sizeof(CompDesc) * desc.size(), cudaMemcpyHostToDevice);
+    if (e) return cuda_fail(e, "fast setup upload");
+    fastCap = 0;
+    if (graph.exec) {
+      cudaGraphExecDestroy(graph.exec);
+      graph = Captured{};
+    }
+    fastReady = true;
+    return 0;
+  }
+  double psfSumFast = 1.0, psfSumOsFast = 1.0;
+
+  cudaError_t uploadCounts() {
+    if (!doBootstrap) return cudaSuccess;
+    std::vector<float> cnt(nDataVals, 0.f);
+    for (long i = 0; i < nValid; i++) cnt[bootIdx[i]] += 1.f;
+    return cudaMemcpy(dCount32.p, cnt.data(), sizeof(float) * nDataVals, cudaMemcpyHostToDevice);
+  }
+
+  int shiftedSpectrum32(const std::vector<double> &p, int pc, int pr, const FFTLen &fx, const FFTLen &fy,
+                        DevBuf<float> &H32) {
+    std::vector<double> pad((size_t)fx.L * fy.L, 0.0);
+    for (int k = 0; k < pr; k++)
+      for (int l = 0; l < pc; l++) {
+        const int rr = ((k - pr + 1) % fy.L + fy.L) % fy.L;
+        const int cc = ((l - pc + 1) % fx.L + fx.L) % fx.L;
+        pad[(size_t)rr * fx.L + cc] = p[(size_t)k * pc + l];
+      }
+    DevBuf<double> H64;
+    int st = spectrum64(pad, fx, fy, H64);
+    if (st) return st;
+    const size_t nc = 2 * (size_t)fy.L * (fx.L / 2 + 1);
+    cudaError_t e = H32.reserve(nc);
+    if (!e) e = launch_f64_to_f32(H64.p, H32.p, (long)nc, stream);
+    if (!e) e = cudaStreamSynchronize(stream);
+    if (e) return cuda_fail(e, "FP32 PSF spectrum");
+    return 0;
+  }
+
+  int ensureFastCap(int B) {
+    if (B <= fastCap) return 0;
+    const FastGeom &g = fg;
+    const int nP = nParamsTot, nC = (int)funcs.size();
+    const int nStat = fast_stat_blocks(g);
+    const int nGrad = fast_grad_blocks(g) + fast_reg_grad_blocks(g);
+    cudaError_t e = dParams.reserve((size_t)B * nP);
+    if (!e) e = dComps32.reserve((size_t)B * nC);
+    if (!e) e = dBg.reserve((size_t)B * 2);
+    if (!e) e = dSpec32.reserve(2 * (size_t)B * g.specBatch);
+    if (!e && g.hasRegion) e = dRSpec32.reserve(2 * (size_t)B * g.rSpecBatch);
+    if (!e && g.hasRegion) e = dRegModel.reserve((size_t)B * g.rRows * g.rCols);
+    if (!e && g.hasRegion) e = dRegG.reserve((size_t)B * g.rRows * g.rCols);
+    if (!e) e = dStatPart.reserve((size_t)B * nStat * 2);
+    if (!e) e = dGradPart.reserve((size_t)B * nGrad * nP);
+    if (!e) e = dStat.reserve(B);
+    if (!e) e = dGrad.reserve((size_t)B * nP);
+    if (e) return cuda_fail(e, "fast batch buffers");
+    fastCap = B;
+    if (graph.exec) {
+      cudaGraphExecDestroy(graph.exec);
+      graph = Captured{};
+    }
+    return 0;
+  }
+
+  FastArgs fastArgs(const double *dP, double *dS, double *dG, float *modelOut) {
+    FastArgs a{};
+    a.desc = dDesc.p;
+    a.nComp = (int)funcs.size();
+    a.nParams = nParamsTot;
+    a.params = dP;
+    a.comps = dComps32.p;
+    a.bgLevel = dBg.p;
+    a.data = dData32.p;
+    a.weight = dW32.p;
+    a.extra = (useCash && pmlr) ? dExtra32.p : nullptr;
+    a.count = doBootstrap ? dCount32.p : nullptr;
+    a.kind = useCash ? 1 : 0;
+    a.modelErrors = modelErrors ? 1 : 0;
+    a.effGain = (float)effGain;
+    a.sky = (float)sky;
+    a.rnTerm = (float)(nCombined * rnAduSq);
+    a.psfSum = (float)psfSumFast;
+    a.psfSumOs = (float)psfSumOsFast;
+    a.spec = dSpec32.p;
+    a.rspec = dRSpec32.p;
+    a.regModel = dRegModel.p;
+    a.regG = dRegG.p;
+    a.statPart = dStatPart.p;
+    a.gradPart = dGradPart.p;
+    a.nStatBlocks = fast_stat_blocks(fg);
+    a.nGradBlocks = fast_grad_blocks(fg);
+    a.nRegGradBlocks = fast_reg_grad_blocks(fg);
+    a.stat = dS;
+    a.grad = dG;
+    a.modelOut = modelOut;
+    return a;
+  }
+
+  FastPlan fastPlan() {
+    FastPlan p{};
+    p.g = fg;
+    p.Lx = &Fx;
+    p.Ly = &Fy;
+    p.Rx = &FRx;
+    p.Ry = &FRy;
+    p.H = dH32.p;
+    p.Hr = dHr32.p;
+    p.hPitch = Fx.L / 2 + 1;
+    p.hrPitch = FRx.L / 2 + 1;
+    return p;
+  }
+
+  // enqueue the fast evaluation for nBatch vectors already on the device
+  int enqueueFast(int B, const double *dP, double *dS, double *dG, float *modelOut = nullptr) {
+    int st = prepareFast();
+    if (st) return st;
+    st = ensureFastCap(B);
+    if (st) return st;
+    const bool wantGrad = dG != nullptr;
+    FastArgs a = fastArgs(dP, dS, dG ? dG : dGrad.p, modelOut);
+    FastPlan p = fastPlan();
+    if (useGraphs && !modelOut) {
+      if (!(graph.exec && graph.nBatch == B && graph.p == dP && graph.s == dS && graph.g == dG)) {
+        if (graph.exec) cudaGraphExecDestroy(graph.exec);
+        graph = Captured{};
+        cudaGraph_t gr;
+        cudaError_t e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
+        if (e) return cuda_fail(e, "graph capture");
+        cudaError_t e2 = fast_forward(p, a, B, wantGrad, stream);
+        e = cudaStreamEndCapture(stream, &gr);
+        if (e2) return cuda_fail(e2, "fast path launch");
+        if (e) return cuda_fail(e, "graph capture");
+        e = cudaGraphInstantiate(&graph.exec, gr, 0);
+        cudaGraphDestroy(gr);
+        if (e) return cuda_fail(e, "graph instantiate");
+        graph.nBatch = B;
+        graph.p = dP;
+        graph.s = dS;
+        graph.g = dG;
+      }
+      cudaError_t e = cudaGraphLaunch(graph.exec, stream);
+      if (e) return cuda_fail(e, "graph launch");
+      return 0;
+    }
+    cudaError_t e = fast_forward(p, a, B, wantGrad, stream);
+    if (e) return cuda_fail(e, "fast path launch");
+    return 0;
+  }
+
+  int fastHost(int B, const double *params, double *stats, double *grads) {
+    int st = prepareFast();
+    if (st) return st;
+    st = ensureFastCap(B);
+    if (st) return st;
+    const int nP = nParamsTot;
+    cudaError_t e = cudaMemcpyAsync(dParams.p, params, sizeof(double) * (size_t)B * nP, cudaMemcpyHostToDevice, stream);
+    if (e) return cuda_fail(e, "params upload");
+    st = enqueueFast(B, dParams.p, dStat.p, grads ? dGrad.p : nullptr);
+    if (st) return st;
+    e = cudaMemcpyAsync(stats, dStat.p, sizeof(double) * B, cudaMemcpyDeviceToHost, stream);
+    if (!e && grads) e = cudaMemcpyAsync(grads, dGrad.p, sizeof(double) * (size_t)B * nP, cudaMemcpyDeviceToHost, stream);
+    if (!e) e = cudaStreamSynchronize(stream);
+    if (e) return cuda_fail(e, "fast results");
+    return 0;
+  }
+
+  int makeBootstrapSample() {
+    if (!finalSetupDone) return fail(IMFIT_E_STATE, "FinalSetupForFitting not called");
+    bootIdx.assign(nValid, 0);
+    for (long i = 0; i < nValid; i++) {
+      long n;
+      do {
+        n = (long)floor(rng.real2() * nDataVals);
+      } while (!(weight[n] > 0.0));
+      bootIdx[i] = n;
+    }
+    cudaError_t e = dBoot.reserve(nValid);
+    if (!e) e = cudaMemcpy(dBoot.p, bootIdx.data(), sizeof(long) * nValid, cudaMemcpyHostToDevice);
+    if (!e && fastReady) e = uploadCounts();
+    if (e) return cuda_fail(e, "bootstrap indices");
+    return 0;
+  }
+};
+
+static thread_local std::string g_createError;
+
+#define GET(m)                                                     \
+  if (!(m)) return IMFIT_E_ARG;                                    \
+  if (cudaSetDevice((m)->device) != cudaSuccess) return IMFIT_E_CUDA;
+
+extern "C" {
+
+const char *imfit_Version(void) { return kVersion; }
+
+int imfit_ModelObject_new(int device, imfit_model_t *out) {
+  if (!out) return IMFIT_E_ARG;
+  *out = nullptr;
+  cudaError_t e = cudaSetDevice(device);
+  if (e) {
+    g_createError = std::string("cudaSetDevice: ") + cudaGetErrorString(e);
+    return IMFIT_E_CUDA;
+  }
+  auto *m = new imfit_model_s();
+  m->device = device;
+  e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
+  if (e) {
+    g_createError = std::string("cudaStreamCreate: ") + cudaGetErrorString(e);
+    delete m;
+    return IMFIT_E_CUDA;
+  }
+  *out = m;
+  return 0;
+}
+
+int imfit_ModelObject_delete(imfit_model_t m) {
+  if (!m) return 0;
+  cudaSetDevice(m->device);
+  cudaStreamSynchronize(m->stream);
+  delete m;
+  return 0;
+}
+
+const char *imfit_LastError(imfit_model_t m) { return m ? m->lastError.c_str() : g_createError.c_str(); }
+
+int imfit_AddFunction(imfit_model_t m, const char *name) {
+  GET(m);
+  if (!name) return m->fail(IMFIT_E_ARG, "null function name");
+  FuncInfo f;
+  if (!lookup_function(name, f)) return m->fail(IMFIT_E_UNSUPPORTED, std::string("unknown or unsupported function: ") + name);
+  if (m->funcs.size() >= (size_t)kMaxComponents) return m->fail(IMFIT_E_UNSUPPORTED, "too many functions");
+  m->funcs.push_back(f);
+  m->setsDefined = false;
+  return 0;
+}
+
+int imfit_SetSubsampling(imfit_model_t m, int i, int s) {
+  GET(m);
+  if (i < 0 || i >= (int)m->funcs.size()) return m->fail(IMFIT_E_ARG, "bad function index");
+  m->funcs[i].subsample = s ? 1 : 0;
+  m->fastReady = false;
+  return 0;
+}
+
+int imfit_DefineFunctionSets(imfit_model_t m, const int *starts, int n) {
+  GET(m);
+  if (n < 0 || (n > 0 && !starts)) return m->fail(IMFIT_E_ARG, "bad function-set list");
+  return m->defineSets(starts, n);
+}
+
+int imfit_PopulateParameterNames(imfit_model_t m) {
+  GET(m);
+  if (!m->setsDefined) return m->fail(IMFIT_E_STATE, "DefineFunctionSets not called");
+  m->populateNames();
+  return 0;
+}
+
+int imfit_GetParameterName(imfit_model_t m, int i, char *buf, int len) {
+  GET(m);
+  if (!buf || len < 1) return IMFIT_E_ARG;
+  const char *s = (i >= 0 && i < (int)m->paramNames.size()) ? m->paramNames[i].c_str() : "<undefined>";
+  snprintf(buf, len, "%s", s);
+  return 0;
+}
+
+int imfit_AddPSFVector(imfit_model_t m, long nPix, int nc, int nr, const double *psf, int normalize) {
+  GET(m);
+  if (!psf || nc < 1 || nr < 1 || nPix != (long)nc * nr) return m->fail(IMFIT_E_ARG, "bad PSF arguments");
+  double s = 0.0;
+  for (long i = 0; i < nPix; i++) {
+    if (!std::isfinite(psf[i])) return m->fail(-1, "PSF image has one or more non-finite values");
+    s += psf[i];
+  }
+  if (normalize && s <= 0.0) return m->fail(-1, "Sum of PSF pixel values is <= 0 -- PSF cannot be normalized");
+  m->psf.assign(psf, psf + nPix);
+  if (normalize) {
+    const double ks = kahan_sum(m->psf.data(), nPix);
+    for (auto &v : m->psf) v = v / ks;
+  }
+  m->psfSum = 0.0;
+  for (double v : m->psf) m->psfSum += v;
+  m->nPsfCols = nc;
+  m->nPsfRows = nr;
+  m->doConv = true;
+  m->psfNormalize = normalize != 0;
+  if (m->modelSetupDone) return m->fail(-1, "PSF was added after SetupModelImage() was already called");
+  return 0;
+}
+
+int imfit_SetupModelImage(imfit_model_t m, int nc, int nr) {
+  GET(m);
+  return m->setupModelImage(nc, nr);
+}
+
+int imfit_AddImageDataVector(imfit_model_t m, const double *pix, int nc, int nr) {
+  GET(m);
+  if (!pix || nc < 1 || nr < 1) return m->fail(IMFIT_E_ARG, "bad image");
+  m->data.assign(pix, pix + (size_t)nc * nr);
+  m->nDataVals = m->nValid = (long)nc * nr;
+  m->dataValsSet = true;
+  int st = m->setupModelImage(nc, nr);
+  return st ? -1 : 0;
+}
+
+int imfit_AddImageCharacteristics(imfit_model_t m, double gain, double rn, double texp, int ncomb, double sky) {
+  GET(m);
+  if (!(gain > 0.0) || rn < 0.0 || !(texp > 0.0) || ncomb < 1 || sky < 0.0)
+    return m->fail(IMFIT_E_ARG, "bad image characteristics");
+  m->gain = gain;
+  m->readNoise = rn;
+  m->expTime = texp;
+  m->nCombined = ncomb;
+  m->sky = sky;
+  m->effGain = gain * texp * ncomb;
+  m->rnAduSq = rn * rn / (m->effGain * m->effGain);
+  return 0;
+}
+
+int imfit_AddOversampledPsfInfo(imfit_model_t m, const double *psf, int nc, int nr, int scale, int x1, int x2,
+                                int y1, int y2, int normalize) {
+  GET(m);
+  if (!psf) return m->fail(IMFIT_E_ARG, "null PSF");
+  return m->addRegion(psf, nc, nr, scale, x1, x2, y1, y2, normalize);
+}
+
+int imfit_AddErrorVector(imfit_model_t m, long n, int nc, int nr, const double *pix, int type) {
+  GET(m);
+  if (!pix || n != m->nDataVals || nc != m->nDataCols || nr != m->nDataRows)
+    return m->fail(IMFIT_E_ARG, "error image size does not match the data");
+  std::vector<double> w(pix, pix + n);
+  switch (type) {  // core/model_object.cpp:595-617
+    case IMFIT_WEIGHTS_ARE_SIGMAS: for (auto &v : w) v = 1.0 / v; break;
+    case IMFIT_WEIGHTS_ARE_VARIANCES: for (auto &v : w) v = 1.0 / sqrt(v); break;
+    case IMFIT_WEIGHTS_ARE_WEIGHTS: for (auto &v : w) v = sqrt(v); break;
+    default: m->weightValsSet = false; return m->fail(IMFIT_E_ARG, "incorrect input-type specification");
+  }
+  m->weight = w;
+  m->weightValsSet = true;
+  m->externalErrors = true;
+  return 0;
+}
+
+int imfit_AddMaskVector(imfit_model_t m, long n, int nc, int nr, const double *pix, int type) {
+  GET(m);
+  if (!pix || n != m->nDataVals || nc != m->nDataCols || nr != m->nDataRows)
+    return m->fail(IMFIT_E_ARG, "mask size does not match the data");
+  std::vector<double> mk(pix, pix + n);
+  long valid = 0;
+  if (type == IMFIT_MASK_ZERO_IS_GOOD) {
+    for (auto &v : mk) {
+      if (!std::isfinite(v) || v > 0.0) v = 0.0;
+      else { v = 1.0; valid++; }
+    }
+  } else if (type == IMFIT_MASK_ZERO_IS_BAD) {
+    for (auto &v : mk) {
+      if (!std::isfinite(v) || v < 1.0) v = 0.0;
+      else { v = 1.0; valid++; }
+    }
+  } else {
+    m->maskExists = false;
+    return m->fail(-1, "unknown mask inputType");
+  }
+  m->mask = mk;
+  m->nValid = valid;
+  m->maskExists = true;
+  return 0;
+}
+
+int imfit_UseCashStatistic(imfit_model_t m) {
+  GET(m);
+  if (!m->dataValsSet && m->nDataVals == 0) return m->fail(IMFIT_E_STATE, "no image size yet");
+  m->useCash = true;
+  m->weight.assign(m->nDataVals, 1.0);
+  if (m->extra.empty()) m->extra.assign(m->nDataVals, 0.0);
+  m->weightValsSet = true;
+  return 0;
+}
+
+int imfit_UsePoissonMLR(imfit_model_t m) {
+  GET(m);
+  m->pmlr = true;
+  return imfit_UseCashStatistic(m);
+}
+
+int imfit_UseModelErrors(imfit_model_t m) {
+  GET(m);
+  m->modelErrors = true;
+  m->dataErrors = false;
+  m->weight.assign(m->nDataVals, 1.0);
+  m->weightValsSet = true;
+  return 0;
+}
+
+int imfit_FinalSetupForFitting(imfit_model_t m) {
+  GET(m);
+  return m->finalSetup();
+}
+
+int imfit_SetMaxThreads(imfit_model_t m, int) { GET(m); return 0; }
+int imfit_SetOMPChunkSize(imfit_model_t m, int) { GET(m); return 0; }
+
+int imfit_GetNParams(imfit_model_t m) { return m ? m->nParamsTot : IMFIT_E_ARG; }
+long imfit_GetNDataValues(imfit_model_t m) { return m ? m->nDataVals : IMFIT_E_ARG; }
+long imfit_GetNValidPixels(imfit_model_t m) { return m ? m->nValid : IMFIT_E_ARG; }
+int imfit_GetNFunctions(imfit_model_t m) { return m ? (int)m->funcs.size() : IMFIT_E_ARG; }
+
+int imfit_WhichFitStatistic(imfit_model_t m, int verbose) {
+  if (!m) return IMFIT_E_ARG;
+  if (m->useCash) return m->pmlr ? IMFIT_FITSTAT_POISSON_MLR : IMFIT_FITSTAT_CASH;
+  if (!verbose) return IMFIT_FITSTAT_CHISQUARE;
+  if (m->modelErrors) return IMFIT_FITSTAT_CHISQUARE_MODEL;
+  if (m->externalErrors) return IMFIT_FITSTAT_CHISQUARE_USER;
+  return IMFIT_FITSTAT_CHISQUARE_DATA;
+}
+
+int imfit_GetModelImageSize(imfit_model_t m, int *nc, int *nr) {
+  if (!m || !nc || !nr) return IMFIT_E_ARG;
+  *nc = m->nModelCols;
+  *nr = m->nModelRows;
+  return 0;
+}
+
+int imfit_CreateModelImage(imfit_model_t m, const double *params) {
+  GET(m);
+  if (!params) return m->fail(IMFIT_E_ARG, "null parameter vector");
+  return m->createModelImage(params);
+}
+
+int imfit_ComputeModelImage(imfit_model_t m, const double *params) { return imfit_CreateModelImage(m, params); }
+
+int imfit_ComputeDeviates(imfit_model_t m, double *y, const double *params) {
+  GET(m);
+  if (!y || !params) return m->fail(IMFIT_E_ARG, "null argument");
+  return m->computeDeviates(y, params);
+}
+
+int imfit_GetFitStatistic(imfit_model_t m, const double *params, double *s) {
+  GET(m);
+  if (!s || !params) return m->fail(IMFIT_E_ARG, "null argument");
+  return m->getFitStatistic(params, s);
+}
+
+int imfit_ChiSquared(imfit_model_t m, const double *params, double *s) {
+  GET(m);
+  if (!s || !params) return m->fail(IMFIT_E_ARG, "null argument");
+  return m->getFitStatistic(params, s, 0);
+}
+
+int imfit_CashStatistic(imfit_model_t m, const double *params, double *s) {
+  GET(m);
+  if (!s || !params) return m->fail(IMFIT_E_ARG, "null argument");
+  if (!m->useCash) return m->fail(IMFIT_E_STATE, "Cash statistic needs UseCashStatistic");
+  return m->getFitStatistic(params, s, 1);
+}
+
+int imfit_GetModelImageVector(imfit_model_t m, double *out) {
+  GET(m);
+  if (!out) return IMFIT_E_ARG;
+  if (!m->modelComputed) return m->fail(IMFIT_E_STATE, "Model image has not yet been computed");
+  DevBuf<double> tmp;
+  cudaError_t e = tmp.reserve(m->nDataVals);
+  if (!e)
+    e = launch_crop64(m->dModel.p, m->nModelCols, m->doConv ? m->nPsfRows : 0, m->doConv ? m->nPsfCols : 0,
+                      m->nDataCols, m->nDataRows, tmp.p, m->stream);
+  if (!e) e = cudaMemcpyAsync(out, tmp.p, sizeof(double) * m->nDataVals, cudaMemcpyDeviceToHost, m->stream);
+  if (!e) e = cudaStreamSynchronize(m->stream);
+  return e ? m->cuda_fail(e, "GetModelImageVector") : 0;
+}
+
+int imfit_GetExpandedModelImageVector(imfit_model_t m, double *out) {
+  GET(m);
+  if (!out) return IMFIT_E_ARG;
+  if (!m->modelComputed) return m->fail(IMFIT_E_STATE, "Model image has not yet been computed");
+  cudaError_t e = cudaMemcpyAsync(out, m->dModel.p, sizeof(double) * m->nModelVals, cudaMemcpyDeviceToHost, m->stream);
+  if (!e) e = cudaStreamSynchronize(m->stream);
+  return e ? m->cuda_fail(e, "GetExpandedModelImageVector") : 0;
+}
+
+int imfit_GetResidualImageVector(imfit_model_t m, double *out) {
+  GET(m);
+  int st = imfit_GetModelImageVector(m, out);
+  if (st) return st;
+  for (long z = 0; z < m->nDataVals; z++) out[z] = m->data[z] - out[z];
+  return 0;
+}
+
+int imfit_GetWeightImageVector(imfit_model_t m, double *out) {
+  GET(m);
+  if (!out) return IMFIT_E_ARG;
+  if (!m->weightValsSet) return m->fail(IMFIT_E_STATE, "Weight image has not yet been computed");
+  std::vector<double> w = m->weight;
+  if (m->modelErrors && m->finalSetupDone) {
+    cudaError_t e = cudaMemcpy(w.data(), m->dWeight.p, sizeof(double) * m->nDataVals, cudaMemcpyDeviceToHost);
+    if (e) return m->cuda_fail(e, "GetWeightImageVector");
+  }
+  for (long z = 0; z < m->nDataVals; z++) out[z] = w[z] * w[z];
+  return 0;
+}
+
+int imfit_GetDataVector(imfit_model_t m, double *out) {
+  GET(m);
+  if (!out || !m->dataValsSet) return m->fail(IMFIT_E_STATE, "Image data values have not yet been supplied");
+  memcpy(out, m->data.data(), sizeof(double) * m->nDataVals);
+  return 0;
+}
+
+int imfit_UseBootstrap(imfit_model_t m, unsigned long seed) {
+  GET(m);
+  m->rng.seed(seed);
+  m->doBootstrap = true;
+  return m->makeBootstrapSample();
+}
+
+int imfit_MakeBootstrapSample(imfit_model_t m) {
+  GET(m);
+  if (!m->doBootstrap) return m->fail(IMFIT_E_STATE, "UseBootstrap not called");
+  return m->makeBootstrapSample();
+}
+
+int imfit_GetFitStatisticAndGradientFD(imfit_model_t m, const double *params, double *s, double *g) {
+  GET(m);
+  if (!params || !s || !g) return m->fail(IMFIT_E_ARG, "null argument");
+  return m->fdGradient(params, s, g);
+}
+
+int imfit_GetFitStatisticAndGradient(imfit_model_t m, const double *params, double *s, double *g) {
+  GET(m);
+  if (!params || !s || !g) return m->fail(IMFIT_E_ARG, "null argument");
+  return m->fastHost(1, params, s, g);
+}
+
+int imfit_GetFitStatisticFast(imfit_model_t m, const double *params, double *s) {
+  GET(m);
+  if (!params || !s) return m->fail(IMFIT_E_ARG, "null argument");
+  return m->fastHost(1, params, s, nullptr);
+}
+
+int imfit_BatchFitStatisticAndGradient(imfit_model_t m, int B, const double *params, double *stats, double *grads) {
+  GET(m);
+  if (B < 1 || !params || !stats) return m->fail(IMFIT_E_ARG, "bad batch arguments");
+  return m->fastHost(B, params, stats, grads);
+}
+
+int imfit_BatchFitStatisticAndGradientDevice(imfit_model_t m, int B, const double *dP, double *dS, double *dG) {
+  GET(m);
+  if (B < 1 || !dP || !dS) return m->fail(IMFIT_E_ARG, "bad batch arguments");
+  return m->enqueueFast(B, dP, dS, dG);
+}
+
+int imfit_Synchronize(imfit_model_t m) {
+  GET(m);
+  cudaError_t e = cudaStreamSynchronize(m->stream);
+  return e ? m->cuda_fail(e, "synchronize") : 0;
+}
+
+int imfit_SetUseGraphs(imfit_model_t m, int enable) {
+  GET(m);
+  m->useGraphs = enable != 0;
+  return 0;
+}
+
+int imfit_GetFastModelImageVector(imfit_model_t m, const double *params, double *out) {
+  GET(m);
+  if (!params || !out) return m->fail(IMFIT_E_ARG, "null argument");
+  int st = m->prepareFast();
+  if (st) return st;
+  st = m->ensureFastCap(1);
+  if (st) return st;
+  DevBuf<float> mo;
+  cudaError_t e = mo.reserve(m->nDataVals);
+  if (!e) e = cudaMemcpyAsync(m->dParams.p, params, sizeof(double) * m->nParamsTot, cudaMemcpyHostToDevice, m->stream);
+  if (e) return m->cuda_fail(e, "fast model");
+  st = m->enqueueFast(1, m->dParams.p, m->dStat.p, nullptr, mo.p);
+  if (st) return st;
+  std::vector<float> h(m->nDataVals);
+  e = cudaMemcpyAsync(h.data(), mo.p, sizeof(float) * m->nDataVals, cudaMemcpyDeviceToHost, m->stream);
+  if (!e) e = cudaStreamSynchronize(m->stream);
+  if (e) return m->cuda_fail(e, "fast model");
+  for (long z = 0; z < m->nDataVals; z++) out[z] = h[z];
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,180 @@
+/* imfit_gb300.h -- C ABI of the GB300 model-image / fit-statistic library.
+ *
+ * The entry points mirror the reference's ModelObject methods one for one
+ * (core/model_object.h:38-347, core/model_object.cpp) so that a thin C++
+ * subclass of ModelObject, or any FFI, can route the solvers' calls here.
+ * Each declaration names the reference method it replaces.
+ *
+ * Conventions
+ *  - Every call returns an int status: 0 on success, a negative IMFIT_E_*
+ *    code on failure (imfit_LastError gives the message).  Nothing aborts.
+ *  - Images are row-major double arrays, x (column) fastest, row 0 first --
+ *    the reference's pixel-vector layout.
+ *  - Host arrays passed in are copied; nothing is borrowed after the call
+ *    returns (the reference borrows data/mask/error arrays and rewrites them
+ *    in place; here the converted weights/mask can be read back with the
+ *    Get* calls).
+ *  - One handle is used by one host thread at a time, like a ModelObject.
+ */
+#ifndef IMFIT_GB300_H
+#define IMFIT_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct imfit_model_s *imfit_model_t;
+
+#define IMFIT_OK 0
+#define IMFIT_E_ARG (-1)        /* invalid argument or call order */
+#define IMFIT_E_CUDA (-2)       /* CUDA runtime error */
+#define IMFIT_E_NOMEM (-3)      /* device allocation failed */
+#define IMFIT_E_UNSUPPORTED (-4) /* valid for the reference, not supported on this path */
+#define IMFIT_E_STATE (-5)      /* required setup step missing */
+
+/* error-weight and mask input types (core/definitions.h) */
+#define IMFIT_WEIGHTS_ARE_SIGMAS 100
+#define IMFIT_WEIGHTS_ARE_VARIANCES 110
+#define IMFIT_WEIGHTS_ARE_WEIGHTS 120
+#define IMFIT_MASK_ZERO_IS_GOOD 10
+#define IMFIT_MASK_ZERO_IS_BAD 20
+
+/* fit-statistic codes (core/definitions.h) */
+#define IMFIT_FITSTAT_CHISQUARE 1
+#define IMFIT_FITSTAT_CASH 2
+#define IMFIT_FITSTAT_POISSON_MLR 3
+#define IMFIT_FITSTAT_CHISQUARE_DATA 10
+#define IMFIT_FITSTAT_CHISQUARE_MODEL 11
+#define IMFIT_FITSTAT_CHISQUARE_USER 12
+
+/* ---- lifetime ------------------------------------------------------------- */
+/* ModelObject::ModelObject (core/model_object.cpp:108); device = CUDA ordinal */
+int imfit_ModelObject_new(int device, imfit_model_t *out);
+/* ModelObject::~ModelObject (core/model_object.cpp:181) */
+int imfit_ModelObject_delete(imfit_model_t m);
+/* message of the last failing call on this handle (or the last creation error) */
+const char *imfit_LastError(imfit_model_t m);
+/* version string of the library */
+const char *imfit_Version(void);
+
+/* ---- functions (FunctionObject plug-ins, by config-file name) --------------- */
+/* ModelObject::AddFunction (core/model_object.cpp:279) with the factory of
+ * core/add_functions.cpp:389-461: name is the config-file FUNCTION name
+ * ("Sersic", "Exponential", "FlatSky", "GaussianRing", "Moffat", "Gaussian",
+ * "ExponentialDisk3D", "FerrersBar3D"). */
+int imfit_AddFunction(imfit_model_t m, const char *name);
+/* FunctionObject::SetSubsampling (function_objects/function_object.cpp:78) */
+int imfit_SetSubsampling(imfit_model_t m, int functionIndex, int subsample);
+/* ModelObject::DefineFunctionSets (core/model_object.cpp:387) */
+int imfit_DefineFunctionSets(imfit_model_t m, const int *startIndices, int nSets);
+/* ModelObject::PopulateParameterNames (core/model_object.cpp:2169) */
+int imfit_PopulateParameterNames(imfit_model_t m);
+/* ModelObject::GetParameterName (core/model_object.cpp:2186); copies into buf */
+int imfit_GetParameterName(imfit_model_t m, int i, char *buf, int bufLen);
+
+/* ---- image setup ------------------------------------------------------------ */
+/* ModelObject::AddPSFVector (core/model_object.cpp:827); must precede SetupModelImage */
+int imfit_AddPSFVector(imfit_model_t m, long nPixels, int nColumns, int nRows, const double *psf,
+                       int normalize);
+/* ModelObject::SetupModelImage (core/model_object.cpp:488) */
+int imfit_SetupModelImage(imfit_model_t m, int nColumns, int nRows);
+/* ModelObject::AddImageDataVector (core/model_object.cpp:462) */
+int imfit_AddImageDataVector(imfit_model_t m, const double *pixels, int nColumns, int nRows);
+/* ModelObject::AddImageCharacteristics (core/model_object.cpp:532) */
+int imfit_AddImageCharacteristics(imfit_model_t m, double gain, double readNoise, double expTime,
+                                  int nCombined, double originalSky);
+/* ModelObject::AddOversampledPsfInfo (core/model_object.cpp:881), with the
+ * PsfOversamplingInfo fields flattened: region x1:x2,y1:y2 in 1-based pixels */
+int imfit_AddOversampledPsfInfo(imfit_model_t m, const double *psf, int nColumns, int nRows,
+                                int scale, int x1, int x2, int y1, int y2, int normalize);
+/* ModelObject::AddErrorVector (core/model_object.cpp:573) */
+int imfit_AddErrorVector(imfit_model_t m, long nDataValues, int nColumns, int nRows,
+                         const double *pixels, int inputType);
+/* ModelObject::AddMaskVector (core/model_object.cpp:721) */
+int imfit_AddMaskVector(imfit_model_t m, long nDataValues, int nColumns, int nRows,
+                        const double *pixels, int inputType);
+/* ModelObject::UseCashStatistic (core/model_object.cpp:1541) */
+int imfit_UseCashStatistic(imfit_model_t m);
+/* ModelObject::UsePoissonMLR (core/model_object.cpp:1583) */
+int imfit_UsePoissonMLR(imfit_model_t m);
+/* ModelObject::UseModelErrors (core/model_object.cpp:1501) */
+int imfit_UseModelErrors(imfit_model_t m);
+/* ModelObject::FinalSetupForFitting (core/model_object.cpp:967); returns 0, -1, -2, -3 */
+int imfit_FinalSetupForFitting(imfit_model_t m);
+/* ModelObject::SetMaxThreads / SetOMPChunkSize (core/model_object.cpp:248, 260):
+ * accepted and ignored (the GPU decides its own parallelism) */
+int imfit_SetMaxThreads(imfit_model_t m, int n);
+int imfit_SetOMPChunkSize(imfit_model_t m, int n);
+
+/* ---- queries ---------------------------------------------------------------- */
+int imfit_GetNParams(imfit_model_t m);           /* core/model_object.cpp:2207 */
+long imfit_GetNDataValues(imfit_model_t m);      /* core/model_object.cpp:2215 */
+long imfit_GetNValidPixels(imfit_model_t m);     /* core/model_object.cpp:2223 */
+int imfit_GetNFunctions(imfit_model_t m);        /* core/model_object.cpp:2199 */
+int imfit_WhichFitStatistic(imfit_model_t m, int verbose); /* core/model_object.cpp:1592 */
+/* size of the expanded (PSF-padded) model image of GetExpandedModelImageVector */
+int imfit_GetModelImageSize(imfit_model_t m, int *nColumns, int *nRows);
+
+/* ---- the plain FP64 path (drop-in) ------------------------------------------ */
+/* ModelObject::CreateModelImage (core/model_object.cpp:1103) */
+int imfit_CreateModelImage(imfit_model_t m, const double *params);
+/* alias of imfit_CreateModelImage under the name used in some documentation */
+int imfit_ComputeModelImage(imfit_model_t m, const double *params);
+/* ModelObject::ComputeDeviates (core/model_object.cpp:1413); yResults holds
+ * GetNDataValues() doubles, or GetNValidPixels() in bootstrap mode */
+int imfit_ComputeDeviates(imfit_model_t m, double *yResults, const double *params);
+/* ModelObject::GetFitStatistic (core/model_object.cpp:1620) */
+int imfit_GetFitStatistic(imfit_model_t m, const double *params, double *statistic);
+/* ModelObject::ChiSquared (core/model_object.cpp:1633) */
+int imfit_ChiSquared(imfit_model_t m, const double *params, double *statistic);
+/* ModelObject::CashStatistic (core/model_object.cpp:1703) */
+int imfit_CashStatistic(imfit_model_t m, const double *params, double *statistic);
+/* ModelObject::GetModelImageVector (core/model_object.cpp:2257): data-sized crop */
+int imfit_GetModelImageVector(imfit_model_t m, double *out);
+/* ModelObject::GetExpandedModelImageVector (core/model_object.cpp:2296) */
+int imfit_GetExpandedModelImageVector(imfit_model_t m, double *out);
+/* ModelObject::GetResidualImageVector (core/model_object.cpp:2312) */
+int imfit_GetResidualImageVector(imfit_model_t m, double *out);
+/* ModelObject::GetWeightImageVector (core/model_object.cpp:2359): 1/sigma^2 */
+int imfit_GetWeightImageVector(imfit_model_t m, double *out);
+/* ModelObject::GetDataVector (core/model_object.cpp:2383) */
+int imfit_GetDataVector(imfit_model_t m, double *out);
+/* ModelObject::UseBootstrap (core/model_object.cpp:2042), seeding MT19937 like
+ * core/bootstrap_errors.cpp:176 */
+int imfit_UseBootstrap(imfit_model_t m, unsigned long seed);
+/* ModelObject::MakeBootstrapSample (core/model_object.cpp:2061) */
+int imfit_MakeBootstrapSample(imfit_model_t m);
+
+/* ---- gradients (no counterpart in the reference) ---------------------------- */
+/* Statistic and its gradient w.r.t. all GetNParams() parameters by the plain
+ * FP64 model and a one-sided finite difference per parameter, with mpfit's
+ * step rule h = sqrt(eps)*|x| (solvers/mpfit.cpp:1194, 1254-1258):
+ * 1 + nParams model evaluations.  For chi^2 the gradient is 2 J^T dev with J
+ * the forward-difference Jacobian of the deviates, as mpfit forms it. */
+int imfit_GetFitStatisticAndGradientFD(imfit_model_t m, const double *params, double *statistic,
+                                       double *gradient);
+/* Statistic and gradient by the fast path: FP32 model evaluation and FFTs,
+ * FP64 geometry setup and reductions, adjoint (reverse-mode) gradient. */
+int imfit_GetFitStatisticAndGradient(imfit_model_t m, const double *params, double *statistic,
+                                     double *gradient);
+/* Fast-path statistic only (FP32 evaluation, FP64 reduction) */
+int imfit_GetFitStatisticFast(imfit_model_t m, const double *params, double *statistic);
+/* Batched fast path over nBatch parameter vectors (params: nBatch x nParams,
+ * row-major).  Host buffers; gradients may be NULL for statistics only. */
+int imfit_BatchFitStatisticAndGradient(imfit_model_t m, int nBatch, const double *params,
+                                       double *statistics, double *gradients);
+/* Same with DEVICE pointers on the handle's stream (no host copies); the
+ * call returns once the work is enqueued.  imfit_Synchronize waits. */
+int imfit_BatchFitStatisticAndGradientDevice(imfit_model_t m, int nBatch, const double *d_params,
+                                             double *d_statistics, double *d_gradients);
+int imfit_Synchronize(imfit_model_t m);
+/* Record the fast batched evaluation for nBatch vectors as a CUDA graph and
+ * replay it on later calls with the same nBatch and device pointers. */
+int imfit_SetUseGraphs(imfit_model_t m, int enable);
+/* FP32 model image of the fast path (data-sized), for diagnostics */
+int imfit_GetFastModelImageVector(imfit_model_t m, const double *params, double *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IMFIT_GB300_H */

@@ -97,7 +97,8 @@ int ref_finish_functions(void *h) {
   RefModel *r = static_cast<RefModel *>(h);
   r->mo->DefineFunctionSets(r->setStarts);
   r->mo->PopulateParameterNames();
-  r->mo->FinalModelSetup();
+  // (FinalModelSetup is multimfit-only: imfit never calls it, and it reads
+  // ModelObject::nGlobalFunctions, which the constructor leaves unset)
   return 0;
 }
 

@@ -1,0 +1,114 @@
+"""Generate the committed golden fixtures from the reference.
+
+Run in a checkout that has the reference at /root/reference (or
+IMFIT_REFERENCE_DIR):  python tests/golden/make_golden.py
+
+Outputs (all small .npz files next to this script):
+  n3073.npz          the reference regression inputs tests/n3073rss_small.fits,
+                     tests/n3073rss_small_mask.fits, tests/psf_moffat_35_n4699z.fits
+                     (float32 / int, exactly as stored), the printed goldens of
+                     tests/imfit_reference/imfit_textout4c:24 and imfit_textout4d,
+                     the full-precision values from the reference's own code
+                     compiled here (oracle/_ref), and its mpfit LM fit.
+  makeimage.npz      reference makeimage outputs tests/sersic+exp_orig.fits
+                     (central 128x128 crop and four 16x16 corners) and
+                     tests/oversampled_orig.fits (whole image) with their PSFs
+                     (do_makeimage_tests:51, 68-72).
+  small_case.npz     the reference's own outputs (oracle/_ref) for
+                     imfit_gb300.workloads.small_case: model images, deviates and
+                     statistics for chi^2 / Cash / PMLR.
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import oracle  # noqa: E402
+from imfit_gb300 import fits, workloads  # noqa: E402
+
+REF = oracle.REFERENCE_DIR
+
+
+def n3073():
+    t = os.path.join(REF, "tests")
+    data, _ = fits.read_image(os.path.join(t, "n3073rss_small.fits"))
+    mask, _ = fits.read_image(os.path.join(t, "n3073rss_small_mask.fits"))
+    psf, _ = fits.read_image(os.path.join(t, "psf_moffat_35_n4699z.fits"))
+    # tests/imfit_reference/imfit_config_n3073.dat
+    params = np.array([101.0, 97.0, 110.0, 0.2, 1.5, 150.0, 15.0, 55.0, 0.2, 70.0, 45.0])
+    lo = np.array([90, 90, 0, 0, 0, 0, 0, 0, 0, 0, 0], dtype=float)
+    hi = np.array([110, 110, 180, 1, 5, 500, 100, 90, 1, 600, 1000], dtype=float)
+    out = {}
+    for stat in ("chi2", "cash"):
+        m = oracle.RefModel()
+        m.add_function("Sersic", True)
+        m.add_function("Exponential")
+        m.finish_functions()
+        m.add_psf(psf)
+        m.add_image_data(data)
+        m.add_image_characteristics(4.725, 4.3, 1.0, 1, 154.33)
+        m.add_mask_vector(mask)
+        if stat == "cash":
+            m.use_cash()
+        assert m.final_setup() == 0
+        out[f"{stat}_ref"] = m.get_fit_statistic(params)
+        if stat == "chi2":
+            out["deviates_ref"] = m.compute_deviates(params)
+            fit = m.lm_fit(params, lo=lo, hi=hi, ftol=1e-8, maxiter=10000)
+            out["lm_params"] = fit["params"]
+            out["lm_chi2"] = fit["chi2"]
+            out["lm_niter"] = fit["niter"]
+            out["lm_nfev"] = fit["nfev"]
+    np.savez_compressed(os.path.join(HERE, "n3073.npz"), data=data.astype(np.float32),
+                        mask=mask.astype(np.int16), psf=psf.astype(np.float32), params=params, lo=lo, hi=hi,
+                        gain=4.725, read_noise=4.3, original_sky=154.33,
+                        chi2_printed=235606.146670, cash_printed=-305659765.743167,
+                        lm_chi2_printed=36828.577653, **out)
+
+
+def makeimage():
+    t = os.path.join(REF, "tests")
+    se, _ = fits.read_image(os.path.join(t, "sersic+exp_orig.fits"))
+    ov, _ = fits.read_image(os.path.join(t, "oversampled_orig.fits"))
+    psf_std, _ = fits.read_image(os.path.join(t, "psf_standard.fits"))
+    psf_os, _ = fits.read_image(os.path.join(t, "psf_oversamp.fits"))
+    np.savez_compressed(
+        os.path.join(HERE, "makeimage.npz"),
+        # tests/makeimage_reference/config_makeimage_sersic+exp512.dat
+        se_params=np.array([256.0, 256.0, 30.0, 0.5, 2.5, 100.0, 50.0, 30.0, 0.75, 10.0, 150.0]),
+        se_center=se[192:320, 192:320].astype(np.float32),
+        se_corners=np.stack([se[:16, :16], se[:16, -16:], se[-16:, :16], se[-16:, -16:]]).astype(np.float32),
+        # tests/makeimage_reference/config_makeimage_gauss-oversample.dat
+        ov_params=np.array([105.2377, 105.4582, 0.0, 0.0, 99.8787, 1.20062]),
+        ov_image=ov.astype(np.float32), psf_standard=psf_std.astype(np.float32),
+        psf_oversamp=psf_os.astype(np.float32), ov_region=np.array([100, 110, 100, 110]), ov_scale=3)
+
+
+def small_case():
+    out = {}
+    for stat in ("chi2", "cash", "pmlr"):
+        wl = workloads.small_case(stat=stat)
+        workloads.synthesize(wl, oracle.RefModel)
+        m = workloads.configure(oracle.RefModel(), wl)
+        out[f"{stat}_data"] = wl.data
+        for tag, p in (("truth", wl.truth), ("start", wl.start)):
+            out[f"{stat}_{tag}_stat"] = m.get_fit_statistic(p)
+            out[f"{stat}_{tag}_dev"] = m.compute_deviates(p)
+            out[f"{stat}_{tag}_model"] = m.get_model_image()
+    np.savez_compressed(os.path.join(HERE, "small_case.npz"), **out)
+
+
+if __name__ == "__main__":
+    if not os.path.isdir(os.path.join(REF, "core")):
+        sys.exit(f"reference checkout not found at {REF}")
+    oracle.build_reference()
+    n3073()
+    makeimage()
+    small_case()
+    for f in sorted(os.listdir(HERE)):
+        if f.endswith(".npz"):
+            print(f, os.path.getsize(os.path.join(HERE, f)))
