@@ -1,0 +1,384 @@
+"""Benchmark: statistic + gradient evaluations per second on the C2 workload.
+
+Workload (synthetic, seeded): 1024x1024 Sersic + Exponential + FlatSky, 63x63
+Moffat PSF, central 40x40 region oversampled 5x with a 315x315 PSF, 10% random
+mask, Poisson noise, chi^2 with data-based errors, 12 free parameters.  One
+"step" = one fit statistic plus its full gradient for one parameter vector
+(what one Levenberg-Marquardt iteration needs).
+
+Arms
+  gb300 (default):
+    value  -- fast path (FP32 evaluation and FFTs, FP64 setup and reductions,
+              adjoint gradient), parameter vector already in device memory,
+              one CUDA-graph launch per step, timed with CUDA events on the
+              library's stream; L2 is flushed (256 MiB write) before each step.
+    e2e    -- the same through the host C-ABI call imfit_GetFitStatisticAndGradient
+              with pinned host buffers: parameters copied in, statistic and
+              gradient copied out, every step.
+    plain_fp64_fd -- the drop-in FP64 path with a forward-difference gradient
+              (1 + 12 model evaluations per step, mpfit's step rule), same GPU.
+    cpu_baseline -- the CPU port of the reference path (oracle/), all host cores.
+  reference (--impl reference):
+    the reference's algorithm on the host CPU (the oracle port; the reference's
+    own build needs its checkout, which the GPU host does not have), same metric.
+Multi-GPU (torchrun): independent replicas, one per GPU, no collective on the data
+path; value = sum over ranks (weak scaling).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "statistic+gradient evals/s vs plain FP64 + FD Jacobian, same GPU, <=1e-5 rel err"
+UNIT = "evals/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--plain-steps", type=int, default=20)
+    ap.add_argument("--cpu-units", type=int, default=3, help="statistic+gradient units in the CPU sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--config", default="C2", choices=["C1", "C2", "C4"])
+    return ap.parse_args()
+
+
+def dist_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+
+
+def workload(name):
+    from imfit_gb300 import workloads
+    return {"C1": workloads.c1, "C2": workloads.c2, "C4": workloads.c4}[name]()
+
+
+def config_block(wl, extra=None):
+    cfg = {"workload": f"{wl.name}: {wl.ncols}x{wl.nrows}, " + "+".join(f for f, _ in wl.functions)
+           + (f", PSF {wl.psf.shape[1]}x{wl.psf.shape[0]}" if wl.psf is not None else "")
+           + "".join(f", region {r[2]} x{r[1]} PSF {r[0].shape[0]}" for r in wl.regions)
+           + f", {wl.stat}", "n_params": wl.n_params, "batch_per_step": 1,
+           "l2": "flushed (256 MiB write) before every timed step"}
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+# ------------------------------------------------------------------ CPU arm
+def cpu_time(wl, units):
+    """Time `units` statistic+gradient units (1 + n_params evaluations each) of
+    the CPU port with all host threads; returns (evals/s, threads)."""
+    import oracle
+    oracle.build_restatement()
+    m = oracle.OracleModel()
+    m.set_fft_smooth(True)
+    threads = os.cpu_count() or 1
+    m.set_max_threads(threads)
+    from imfit_gb300 import workloads
+    workloads.configure(m, wl)
+    p = np.array(wl.start, dtype=float)
+    m.get_fit_statistic(p)  # warm
+    eps = np.sqrt(2.2204460e-16)
+    t0 = time.perf_counter()
+    for _ in range(units):
+        m.get_fit_statistic(p)
+        for j in range(len(p)):
+            q = p.copy()
+            q[j] += eps * abs(q[j]) if q[j] != 0 else eps
+            m.get_fit_statistic(q)
+    dt = time.perf_counter() - t0
+    return units / dt, threads
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    wl = workload(args.config)
+    import oracle
+    from imfit_gb300 import workloads
+    workloads.synthesize(wl, oracle.OracleModel)
+    for _ in range(args.warmup and 1):
+        cpu_time(wl, 1)
+    rates = []
+    threads = 1
+    for _ in range(max(1, min(args.steps, 3))):
+        r, threads = cpu_time(wl, 1)
+        rates.append(r)
+    v = float(np.mean(rates))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": len(rates), "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": config_block(wl, {"parallelism": "host OpenMP"}),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{len(rates)} statistic+gradient units of {wl.name} "
+                                       f"({wl.n_params + 1} FP64 model evaluations each), FFTs padded to "
+                                       f"7-smooth sizes"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ GPU arm
+class Clocks:
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            out = self.proc.communicate(timeout=5)[0]
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out = self.proc.communicate()[0]
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in out.strip().splitlines():
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax = float(f[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def algorithmic_bytes(model, wl):
+    """HBM bytes each fast-path kernel must move per launch (one parameter vector)."""
+    from imfit_gb300 import build  # noqa: F401
+    # spectrum geometry mirrors the library's choice of 7-smooth padded sizes
+    def smooth(n, even):
+        m = n
+        while True:
+            if not (even and m % 2):
+                k = m
+                for p in (2, 3, 5, 7):
+                    while k % p == 0:
+                        k //= p
+                if k == 1:
+                    return m
+            m += 1
+    P = wl.psf.shape
+    N = (wl.nrows, wl.ncols)
+    W = (N[0] + P[0] - 1, N[1] + P[1] - 1)
+    Lx, Ly = smooth(W[1], True), smooth(W[0], True)
+    pitch = Lx // 2 + 1
+    c8 = 8  # complex64
+    out = {
+        "eval_r2c": W[0] * pitch * c8,
+        "cols_conv": (W[0] + Ly + N[0]) * pitch * c8,
+        "stat_rows": 2 * N[0] * pitch * c8 + N[0] * N[1] * 8,
+        "cols_adjoint": (N[0] + Ly + W[0]) * pitch * c8,
+        "grad_rows": W[0] * pitch * c8,
+    }
+    if wl.regions:
+        psf, k, (x1, x2, y1, y2) = wl.regions[0]
+        n = x2 - x1 + 1
+        sub = n * k
+        rw = sub + psf.shape[0] - 1
+        rl = smooth(rw, True)
+        rp = rl // 2 + 1
+        out.update({"region_eval_r2c": rw * rp * c8, "region_cols_conv": (rw + rl + sub) * rp * c8,
+                    "region_down": sub * rp * c8, "region_g_r2c": sub * rp * c8,
+                    "region_cols_adjoint": (sub + rl + rw) * rp * c8, "region_grad_rows": rw * rp * c8})
+    return out
+
+
+def run_gpu(args, rank, local_rank, world):
+    import torch
+
+    import imfit_gb300
+    from imfit_gb300 import build, workloads
+    build.build()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    wl = workload(args.config)
+    workloads.synthesize(wl, lambda: imfit_gb300.ModelObject(local_rank))
+    m = workloads.configure(imfit_gb300.ModelObject(local_rank), wl)
+    nP = wl.n_params
+    stream = torch.cuda.ExternalStream(m.stream(), device=dev)
+    p0 = np.array(wl.start, dtype=np.float64)
+
+    # accuracy against the FP64 path on the same inputs
+    s64 = m.get_fit_statistic(p0)
+    s_fast, g_fast = m.statistic_and_gradient(p0)
+    s_fd, g_fd = m.statistic_and_gradient_fd(p0)
+    stat_rel = abs(s_fast - s64) / abs(s64)
+    gscale = np.abs(g_fd) + 1e-3 * np.max(np.abs(g_fd))
+    grad_rel_median = float(np.median(np.abs(g_fast - g_fd) / gscale))
+
+    d_params = torch.tensor(p0, dtype=torch.float64, device=dev)
+    d_stat = torch.zeros(1, dtype=torch.float64, device=dev)
+    d_grad = torch.zeros(nP, dtype=torch.float64, device=dev)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MiB > 129 MB L2
+    m.set_use_graphs(True)
+    m.set_kernel_timing(True)
+
+    def step():
+        m.batch_device(1, d_params.data_ptr(), d_stat.data_ptr(), d_grad.data_ptr())
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            flush.fill_(1.0)
+            step()
+    torch.cuda.synchronize()
+    per_kernel = {}
+    times = []
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(local_rank)
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            ev[i][0].record(stream)
+            step()
+            ev[i][1].record(stream)
+            kt = m.kernel_times()  # synchronizes the library stream
+            for name, ms in kt:
+                per_kernel.setdefault(name, []).append(ms)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    for a, b in ev:
+        times.append(a.elapsed_time(b))
+    t_ms = float(np.sum(times))
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([t_ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_ms = float(t.item())
+    value = world * args.steps / (t_ms / 1e3)
+    kernels_per_step = len(per_kernel)
+    m.set_kernel_timing(False)
+
+    # end-to-end through the host C ABI, pinned buffers
+    import ctypes
+    lib = imfit_gb300.load_library()
+    hp = ctypes.c_void_p()
+    lib.imfit_HostAlloc(8 * (2 * nP + 1), ctypes.byref(hp))
+    hbuf = np.ctypeslib.as_array((ctypes.c_double * (2 * nP + 1)).from_address(hp.value))
+    hbuf[:nP] = p0
+    pp = hbuf[:nP].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    ps = hbuf[nP:nP + 1].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    pg = hbuf[nP + 1:].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    for _ in range(args.warmup):
+        lib.imfit_GetFitStatisticAndGradient(m.h, pp, ps, pg)
+    e2e_t = 0.0
+    for i in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(i))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st = lib.imfit_GetFitStatisticAndGradient(m.h, pp, ps, pg)
+        e2e_t += time.perf_counter() - t0
+        assert st == 0
+    e2e = world * args.steps / e2e_t
+    lib.imfit_HostFree(hp)
+
+    # plain FP64 + finite-difference gradient (the drop-in), same GPU
+    for _ in range(min(2, args.warmup)):
+        m.statistic_and_gradient_fd(p0)
+    pt = 0.0
+    for i in range(args.plain_steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(i))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        m.statistic_and_gradient_fd(p0)
+        pt += time.perf_counter() - t0
+    plain = args.plain_steps / pt
+
+    # roofline of the dominant kernel
+    import json as _json
+    peaks = {}
+    try:
+        peaks = _json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    avg = {k: float(np.mean(v)) for k, v in per_kernel.items()}
+    total = sum(avg.values())
+    dom = max(avg, key=avg.get)
+    ab = algorithmic_bytes(m, wl)
+    kernel_table = {k: {"ms": round(v, 5), "share": round(v / total, 4),
+                        "GBps": round(ab[k] / (v * 1e-3) / 1e9, 1) if k in ab and v > 0 else None}
+                    for k, v in sorted(avg.items(), key=lambda kv: -kv[1])}
+    achieved = ab.get(dom, 0) / (avg[dom] * 1e-3) / 1e9
+    roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
+            "frac": round(achieved / hbm_peak, 4), "peak_source": peak_src,
+            "algorithmic_bytes_per_launch": ab.get(dom), "traffic": None}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        rate, threads = cpu_time(wl, args.cpu_units)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{args.cpu_units} statistic+gradient units of {wl.name} "
+                         f"({nP + 1} FP64 model evaluations each, forward differences)"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32 eval / f64 setup+reductions",
+                "data": "synthetic (seeded), model-generated with Poisson + read noise",
+                "config": config_block(wl, {"parallelism": f"replicas x{world}" if world > 1 else "single GPU"}),
+                "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 8 * nP, "d2h_bytes_per_step": 8 * (nP + 1)},
+                "plain_fp64_fd": {"value": plain * world, "unit": UNIT, "steps": args.plain_steps,
+                                  "evals_per_step": nP + 1},
+                "speedup_vs_plain_fp64_fd": {"device": value / (plain * world), "e2e": e2e / (plain * world)},
+                "accuracy": {"stat_rel_err_vs_fp64": stat_rel, "grad_rel_err_median_vs_fd": grad_rel_median},
+                "roofline": roof, "kernels": kernel_table, "gpu_launches": kernels_per_step * args.steps,
+                "clocks": clk, "cpu_baseline": cpu}
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, local_rank, world = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+        if args.impl == "reference":
+            dist.init_process_group("gloo")
+        else:
+            import torch
+            torch.cuda.set_device(local_rank)
+            dist.init_process_group("gloo")
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_gpu(args, rank, local_rank, world)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -75,8 +75,13 @@ _SIGS = [
     ("imfit_BatchFitStatisticAndGradient", _I, [_P, _I, _DP, _DP, _DP]),
     ("imfit_BatchFitStatisticAndGradientDevice", _I, [_P, _I, _P, _P, _P]),
     ("imfit_Synchronize", _I, [_P]),
+    ("imfit_GetStream", _I, [_P, ctypes.POINTER(_P)]),
     ("imfit_SetUseGraphs", _I, [_P, _I]),
     ("imfit_GetFastModelImageVector", _I, [_P, _DP, _DP]),
+    ("imfit_SetKernelTiming", _I, [_P, _I]),
+    ("imfit_GetKernelTimes", _I, [_P, _DP, ctypes.c_char_p, _I, _I]),
+    ("imfit_HostAlloc", _I, [ctypes.c_ulong, ctypes.POINTER(_P)]),
+    ("imfit_HostFree", _I, [_P]),
 ]
 
 
@@ -335,8 +340,27 @@ class ModelObject:
     def synchronize(self):
         return self._ck(self.lib.imfit_Synchronize(self.h))
 
+    def stream(self):
+        """Raw cudaStream_t (int) of this handle."""
+        s = _P()
+        self._ck(self.lib.imfit_GetStream(self.h, ctypes.byref(s)))
+        return s.value
+
     def set_use_graphs(self, flag):
         return self._ck(self.lib.imfit_SetUseGraphs(self.h, int(flag)))
+
+    def set_kernel_timing(self, flag):
+        return self._ck(self.lib.imfit_SetKernelTiming(self.h, int(flag)))
+
+    def kernel_times(self):
+        """[(kernel name, ms)] of the most recent fast evaluation."""
+        ms = np.zeros(64)
+        buf = ctypes.create_string_buffer(4096)
+        n = self.lib.imfit_GetKernelTimes(self.h, _dp(ms), buf, 4096, 64)
+        if n < 0:
+            raise ImfitError(n, self.last_error)
+        names = buf.value.decode().split(",") if n else []
+        return list(zip(names, ms[:n].tolist()))
 
     def get_fast_model_image(self, params):
         p = _f64(params)

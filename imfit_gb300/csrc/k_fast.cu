@@ -640,24 +640,40 @@ static cudaError_t launch_grad(const FastArgs &a, const WinDesc &w, const FFTLen
   return cudaGetLastError();
 }
 
+static void mark(const FastPlan &p, const char *name, cudaStream_t st) {
+  StageTimer *t = p.timer;
+  if (!t || t->n >= StageTimer::kMax) return;
+  // External: becomes an event-record node when the launches are captured into a graph
+  cudaEventRecordWithFlags(t->ev[t->n], st, cudaEventRecordExternal);
+  t->names[t->n] = name;
+  t->n++;
+}
+
 cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool wantGrad, cudaStream_t st) {
   const FastGeom &g = p.g;
+  if (p.timer) p.timer->n = 0;
+  mark(p, "start", st);
   cudaError_t e = fast_setup(a, nBatch, st);
   if (e) return e;
+  mark(p, "setup", st);
   // main window -> spectrum
   e = launch_eval(a, main_win(g, a.spec), *p.Lx, nBatch, st);
   if (e) return e;
+  mark(p, "eval_r2c", st);
   const float scale = 1.f / ((float)p.Lx->L * (float)p.Ly->L);
   e = launch_cols<float>(a.spec, g.specPitch, g.specBatch, p.Lx->L / 2 + 1, g.winRows, g.nDataRows, p.H, p.hPitch,
                          *p.Ly, scale, 1, nBatch, st);
   if (e) return e;
+  mark(p, "cols_conv", st);
   if (g.hasRegion) {
     e = launch_eval(a, region_win(g, a.rspec), *p.Rx, nBatch, st);
     if (e) return e;
+    mark(p, "region_eval_r2c", st);
     const float rscale = 1.f / ((float)p.Rx->L * (float)p.Ry->L);
     e = launch_cols<float>(a.rspec, g.rSpecPitch, g.rSpecBatch, p.Rx->L / 2 + 1, g.rWinRows, g.rSubRows, p.Hr,
                            p.hrPitch, *p.Ry, rscale, 1, nBatch, st);
     if (e) return e;
+    mark(p, "region_cols_conv", st);
     const int M = p.Rx->half.n;
     const size_t sm = sizeof(cplx<float>) * 3 * g.rScale * (M + 1);
     ensure_smem(k_fast_region_down, sm);
@@ -666,6 +682,7 @@ cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool 
                                                                reinterpret_cast<const cplx<float> *>(p.Rx->twL32));
     e = cudaGetLastError();
     if (e) return e;
+    mark(p, "region_down", st);
   }
   {
     const int M = p.Lx->half.n;
@@ -677,10 +694,13 @@ cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool 
                                             reinterpret_cast<const cplx<float> *>(p.Lx->twL32), rpb, wantGrad ? 1 : 0);
     e = cudaGetLastError();
     if (e) return e;
+    mark(p, "stat_rows", st);
   }
   if (!wantGrad) {
     k_fast_reduce<<<nBatch, 256, 0, st>>>(a, 0, 0);
-    return cudaGetLastError();
+    e = cudaGetLastError();
+    mark(p, "reduce", st);
+    return e;
   }
   return fast_adjoint(p, a, nBatch, st);
 }
@@ -692,10 +712,12 @@ cudaError_t fast_adjoint(const FastPlan &p, const FastArgs &a, int nBatch, cudaS
   e = launch_cols<float>(a.spec, g.specPitch, g.specBatch, p.Lx->L / 2 + 1, g.nDataRows, g.winRows, p.H, p.hPitch,
                          *p.Ly, scale, 2, nBatch, st);
   if (e) return e;
+  mark(p, "cols_adjoint", st);
   const int nMain = fast_grad_blocks(g), nReg = fast_reg_grad_blocks(g);
   const int nTot = nMain + nReg;
   e = launch_grad(a, main_win(g, a.spec), *p.Lx, nBatch, nTot, 0, st);
   if (e) return e;
+  mark(p, "grad_rows", st);
   if (g.hasRegion) {
     const int M = p.Rx->half.n;
     const size_t sm = sizeof(cplx<float>) * 2 * (M + 1);
@@ -704,15 +726,20 @@ cudaError_t fast_adjoint(const FastPlan &p, const FastArgs &a, int nBatch, cudaS
         reinterpret_cast<const cplx<float> *>(p.Rx->twL32));
     e = cudaGetLastError();
     if (e) return e;
+    mark(p, "region_g_r2c", st);
     const float rscale = 1.f / ((float)p.Rx->L * (float)p.Ry->L);
     e = launch_cols<float>(a.rspec, g.rSpecPitch, g.rSpecBatch, p.Rx->L / 2 + 1, g.rSubRows, g.rWinRows, p.Hr,
                            p.hrPitch, *p.Ry, rscale, 2, nBatch, st);
     if (e) return e;
+    mark(p, "region_cols_adjoint", st);
     e = launch_grad(a, region_win(g, a.rspec), *p.Rx, nBatch, nTot, nMain, st);
     if (e) return e;
+    mark(p, "region_grad_rows", st);
   }
   k_fast_reduce<<<nBatch, 256, 0, st>>>(a, nTot, 1);
-  return cudaGetLastError();
+  e = cudaGetLastError();
+  mark(p, "reduce", st);
+  return e;
 }
 
 }  // namespace imfit

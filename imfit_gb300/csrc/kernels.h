@@ -141,7 +141,17 @@ struct FastArgs {
   float *modelOut;       // optional: [B][N] model image (FP32) for inspection
 };
 
+// Optional per-stage CUDA events: an event is recorded on the launch stream
+// after every kernel of the fast path (recorded into the graph when captured).
+struct StageTimer {
+  static constexpr int kMax = 48;
+  cudaEvent_t ev[kMax];
+  const char *names[kMax];
+  int n = 0;
+};
+
 struct FastPlan {
+  StageTimer *timer = nullptr;
   FastGeom g;
   const FFTLen *Lx, *Ly, *Rx, *Ry;  // main and region lengths
   const void *H, *Hr;               // FP32 PSF spectra (main, region)

@@ -206,6 +206,8 @@ struct imfit_model_s {
   int fastCap = 0;
   bool useGraphs = true;
   Captured graph;
+  StageTimer timer;
+  bool timing = false;
 
   ~imfit_model_s() {
     for (Region *r : regions) {
@@ -220,6 +222,8 @@ struct imfit_model_s {
     fftlen_destroy(FRx);
     fftlen_destroy(FRy);
     if (graph.exec) cudaGraphExecDestroy(graph.exec);
+    if (timing)
+      for (int i = 0; i < StageTimer::kMax; i++) cudaEventDestroy(timer.ev[i]);
     if (hPinned) cudaFreeHost(hPinned);
     if (stream) cudaStreamDestroy(stream);
   }
@@ -870,6 +874,7 @@ struct imfit_model_s {
 
   FastPlan fastPlan() {
     FastPlan p{};
+    p.timer = timing ? &timer : nullptr;
     p.g = fg;
     p.Lx = &Fx;
     p.Ly = &Fy;
@@ -1324,9 +1329,70 @@ int imfit_Synchronize(imfit_model_t m) {
   return e ? m->cuda_fail(e, "synchronize") : 0;
 }
 
+int imfit_GetStream(imfit_model_t m, void **stream) {
+  GET(m);
+  if (!stream) return IMFIT_E_ARG;
+  *stream = (void *)m->stream;
+  return 0;
+}
+
 int imfit_SetUseGraphs(imfit_model_t m, int enable) {
   GET(m);
   m->useGraphs = enable != 0;
+  return 0;
+}
+
+int imfit_SetKernelTiming(imfit_model_t m, int enable) {
+  GET(m);
+  const bool on = enable != 0;
+  if (on == m->timing) return 0;
+  cudaStreamSynchronize(m->stream);
+  if (on) {
+    for (int i = 0; i < StageTimer::kMax; i++)
+      if (cudaEventCreate(&m->timer.ev[i]) != cudaSuccess) return m->fail(IMFIT_E_CUDA, "cudaEventCreate");
+  } else {
+    for (int i = 0; i < StageTimer::kMax; i++) cudaEventDestroy(m->timer.ev[i]);
+  }
+  m->timer.n = 0;
+  m->timing = on;
+  if (m->graph.exec) {
+    cudaGraphExecDestroy(m->graph.exec);
+    m->graph = Captured{};
+  }
+  return 0;
+}
+
+int imfit_GetKernelTimes(imfit_model_t m, double *ms, char *names, int namesLen, int maxN) {
+  GET(m);
+  if (!m->timing) return m->fail(IMFIT_E_STATE, "kernel timing is not enabled");
+  cudaError_t e = cudaStreamSynchronize(m->stream);
+  if (e) return m->cuda_fail(e, "GetKernelTimes");
+  std::string joined;
+  int k = 0;
+  for (int i = 1; i < m->timer.n && k < maxN; i++, k++) {
+    float t = 0.f;
+    e = cudaEventElapsedTime(&t, m->timer.ev[i - 1], m->timer.ev[i]);
+    if (e) return m->cuda_fail(e, "cudaEventElapsedTime");
+    if (ms) ms[k] = t;
+    if (!joined.empty()) joined += ",";
+    joined += m->timer.names[i];
+  }
+  if (names && namesLen > 0) snprintf(names, namesLen, "%s", joined.c_str());
+  return k;
+}
+
+int imfit_HostAlloc(unsigned long bytes, void **ptr) {
+  if (!ptr) return IMFIT_E_ARG;
+  cudaError_t e = cudaMallocHost(ptr, bytes ? bytes : 1);
+  if (e) {
+    g_createError = std::string("cudaMallocHost: ") + cudaGetErrorString(e);
+    return IMFIT_E_NOMEM;
+  }
+  return 0;
+}
+
+int imfit_HostFree(void *ptr) {
+  if (ptr) cudaFreeHost(ptr);
   return 0;
 }
 

@@ -168,11 +168,23 @@ int imfit_BatchFitStatisticAndGradient(imfit_model_t m, int nBatch, const double
 int imfit_BatchFitStatisticAndGradientDevice(imfit_model_t m, int nBatch, const double *d_params,
                                              double *d_statistics, double *d_gradients);
 int imfit_Synchronize(imfit_model_t m);
+/* The CUDA stream (cudaStream_t) all work of this handle is enqueued on. */
+int imfit_GetStream(imfit_model_t m, void **stream);
 /* Record the fast batched evaluation for nBatch vectors as a CUDA graph and
  * replay it on later calls with the same nBatch and device pointers. */
 int imfit_SetUseGraphs(imfit_model_t m, int enable);
 /* FP32 model image of the fast path (data-sized), for diagnostics */
 int imfit_GetFastModelImageVector(imfit_model_t m, const double *params, double *out);
+/* Per-kernel timing of the fast path with CUDA events recorded on the
+ * handle's stream after every kernel (also inside captured graphs).
+ * GetKernelTimes synchronizes, writes the elapsed milliseconds of each kernel
+ * of the most recent fast evaluation and their comma-separated names, and
+ * returns the number of kernels. */
+int imfit_SetKernelTiming(imfit_model_t m, int enable);
+int imfit_GetKernelTimes(imfit_model_t m, double *ms, char *names, int namesLen, int maxN);
+/* Page-locked host memory for the host-buffer entry points (cudaMallocHost). */
+int imfit_HostAlloc(unsigned long bytes, void **ptr);
+int imfit_HostFree(void *ptr);
 
 #ifdef __cplusplus
 }

@@ -107,6 +107,8 @@ def _bind(lib, prefix):
         lib.orc_function_qags_nsub.argtypes = [_S, _DP, _D, _D, _D, _D]
         lib.orc_function_nparams.restype = _I
         lib.orc_function_nparams.argtypes = [_S]
+        lib.orc_set_fft_smooth.restype = None
+        lib.orc_set_fft_smooth.argtypes = [_P, _I]
     else:
         lib.ref_add_oversampled_psf.restype = _I
         lib.ref_add_oversampled_psf.argtypes = [_P, _I, _I, _DP, _I, _S, _I]
@@ -276,6 +278,9 @@ class _CModel:
 
 class OracleModel(_CModel):
     prefix = "orc"
+
+    def set_fft_smooth(self, flag=True):
+        self.lib.orc_set_fft_smooth(self.h, int(flag))
 
     def add_oversampled_psf(self, psf, scale, region, normalize=True):
         psf = _f64(psf)

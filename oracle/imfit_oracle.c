@@ -338,7 +338,21 @@ static double kahan_sum(const double *v, long n) {
   return sum;
 }
 
-static int conv_setup(oconv *c, const double *psf, int ncp, int nrp, int normalize, int nci, int nri) {
+/* smallest 2,3,5,7-smooth integer >= n (optional padding for speed only:
+ * linear convolution is unchanged by extra zero padding) */
+static int smooth_at_least(int n) {
+  for (int m = n;; m++) {
+    int k = m;
+    while (k % 2 == 0) k /= 2;
+    while (k % 3 == 0) k /= 3;
+    while (k % 5 == 0) k /= 5;
+    while (k % 7 == 0) k /= 7;
+    if (k == 1) return m;
+  }
+}
+
+static int conv_setup(oconv *c, const double *psf, int ncp, int nrp, int normalize, int nci, int nri,
+                      int smooth) {
   memset(c, 0, sizeof(*c));
   c->nColsPsf = ncp;
   c->nRowsPsf = nrp;
@@ -346,6 +360,10 @@ static int conv_setup(oconv *c, const double *psf, int ncp, int nrp, int normali
   c->nRowsImg = nri;
   c->nColsPad = nci + ncp - 1;
   c->nRowsPad = nri + nrp - 1;
+  if (smooth) {
+    c->nColsPad = smooth_at_least(c->nColsPad);
+    c->nRowsPad = smooth_at_least(c->nRowsPad);
+  }
   c->nPad = (long)c->nColsPad * c->nRowsPad;
   c->rescale = 1.0 / c->nPad;
   c->nPadC = (long)c->nRowsPad * (c->nColsPad / 2 + 1);
@@ -428,6 +446,7 @@ struct orc_model {
   int nRegions;
   oregion reg[MAXREGIONS];
   int maxThreads;
+  int fftSmooth;
 };
 
 orc_model *orc_create(void) {
@@ -457,6 +476,8 @@ void orc_destroy(orc_model *m) {
   }
   free(m);
 }
+
+void orc_set_fft_smooth(orc_model *m, int flag) { m->fftSmooth = flag ? 1 : 0; }
 
 void orc_set_max_threads(orc_model *m, int n) {
   m->maxThreads = n;
@@ -525,7 +546,7 @@ int orc_setup_model_image(orc_model *m, int ncols, int nrows) {
     m->nModelRows = nrows + 2 * m->nPsfRows;
     double *psf = m->conv.psf;
     int normalize = m->conv.nColsPsf;
-    conv_setup(&m->conv, psf, m->nPsfCols, m->nPsfRows, normalize, m->nModelCols, m->nModelRows);
+    conv_setup(&m->conv, psf, m->nPsfCols, m->nPsfRows, normalize, m->nModelCols, m->nModelRows, m->fftSmooth);
     free(psf);
   } else {
     m->nModelCols = ncols;
@@ -744,7 +765,7 @@ int orc_add_oversampled_psf(orc_model *m, int ncols, int nrows, const double *ps
   r->nModelCols = nrc + 2 * ncols;
   r->nModelRows = nrr + 2 * nrows;
   r->nModelVals = (long)r->nModelCols * r->nModelRows;
-  conv_setup(&r->conv, psf, ncols, nrows, normalize, r->nModelCols, r->nModelRows);
+  conv_setup(&r->conv, psf, ncols, nrows, normalize, r->nModelCols, r->nModelRows, m->fftSmooth);
   r->model = (double *)calloc((size_t)r->nModelVals, sizeof(double));
   m->nRegions++;
   return 0;

@@ -21,6 +21,9 @@ typedef struct orc_model orc_model;
 orc_model *orc_create(void);
 void orc_destroy(orc_model *m);
 void orc_set_max_threads(orc_model *m, int n);
+/* pad FFTs to 2,3,5,7-smooth sizes (>= the reference's N+P-1): same
+ * convolution up to rounding, faster transforms; call before the image size */
+void orc_set_fft_smooth(orc_model *m, int flag);
 
 /* name = config-file function name; newSet = 1 starts a new function set
  * (its own X0,Y0).  Returns 0, or -1 for an unknown name. */

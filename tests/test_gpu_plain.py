@@ -98,7 +98,9 @@ def test_n3073_golden(gpu):
         assert m.final_setup() == 0
         assert m.n_valid == 28754
         s = m.get_fit_statistic(d["params"])
-        assert abs(s - float(d[f"{key}_printed"])) < 5e-7
+        # printed to 6 decimals; a 3e8 Cash value also carries ~1e-15 relative summation-order noise
+        printed = float(d[f"{key}_printed"])
+        assert abs(s - printed) <= max(5e-7, 1e-14 * abs(printed))
         assert relerr(s, float(d[f"{key}_ref"])) < 1e-10
         if stat == "chi2":
             assert normwise(m.compute_deviates(d["params"]), d["deviates_ref"]) < 1e-10
