@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--cpu-units", type=int, default=3, help="statistic+gradient units in the CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--config", default="C2", choices=["C1", "C2", "C4"])
+    ap.add_argument("--no-graphs", action="store_true", help="launch kernels one by one (for profilers)")
     return ap.parse_args()
 
 
@@ -237,7 +238,7 @@ def run_gpu(args, rank, local_rank, world):
     d_stat = torch.zeros(1, dtype=torch.float64, device=dev)
     d_grad = torch.zeros(nP, dtype=torch.float64, device=dev)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MiB > 129 MB L2
-    m.set_use_graphs(True)
+    m.set_use_graphs(not args.no_graphs)
     m.set_kernel_timing(True)
 
     def step():

@@ -643,8 +643,14 @@ static cudaError_t launch_grad(const FastArgs &a, const WinDesc &w, const FFTLen
 static void mark(const FastPlan &p, const char *name, cudaStream_t st) {
   StageTimer *t = p.timer;
   if (!t || t->n >= StageTimer::kMax) return;
-  // External: becomes an event-record node when the launches are captured into a graph
-  cudaEventRecordWithFlags(t->ev[t->n], st, cudaEventRecordExternal);
+  // while the stream is being captured the record must be External to become an
+  // event-record node of the graph; outside capture that flag is not allowed
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(st, &cs);
+  if (cs == cudaStreamCaptureStatusActive)
+    cudaEventRecordWithFlags(t->ev[t->n], st, cudaEventRecordExternal);
+  else
+    cudaEventRecord(t->ev[t->n], st);
   t->names[t->n] = name;
   t->n++;
 }
