@@ -82,6 +82,7 @@ _SIGS = [
     ("imfit_GetKernelTimes", _I, [_P, _DP, ctypes.c_char_p, _I, _I]),
     ("imfit_HostAlloc", _I, [ctypes.c_ulong, ctypes.POINTER(_P)]),
     ("imfit_HostFree", _I, [_P]),
+    ("imfit_ChiSquaredDeviceNoAlloc", _I, [_P, _P, _P, _L, _P, _P]),
 ]
 
 

@@ -23,6 +23,7 @@ UNITS = [
     ("k_fft.cu", []),
     ("k_fast.cu", []),
     ("model_object.cpp", ["-x", "cu"]),
+    ("k_noalloc.cu", ["--fmad=false"]),
 ]
 
 

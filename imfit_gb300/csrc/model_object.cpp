@@ -961,6 +961,11 @@ struct imfit_model_s {
 
 static thread_local std::string g_createError;
 
+namespace imfit {
+// message for imfit_LastError(NULL) from entry points that take no handle
+void set_global_error(const char *msg) { g_createError = msg ? msg : ""; }
+}  // namespace imfit
+
 #define GET(m)                                                     \
   if (!(m)) return IMFIT_E_ARG;                                    \
   if (cudaSetDevice((m)->device) != cudaSuccess) return IMFIT_E_CUDA;

@@ -186,6 +186,31 @@ int imfit_GetKernelTimes(imfit_model_t m, double *ms, char *names, int namesLen,
 int imfit_HostAlloc(unsigned long bytes, void **ptr);
 int imfit_HostFree(void *ptr);
 
+/* ---- allocation-free statistic (no counterpart in the reference) ----------- */
+/* chi^2 = sum over pixels of (weight * (data - model))^2, summed with the
+ * same MINPACK-enorm reduction as imfit_ChiSquared, for callers that must not
+ * allocate device memory when they ask for it: plug-ins of host frameworks
+ * that reserve all device memory up front, deployments with a fixed device
+ * budget, and solver loops that cannot afford the allocator's locking or the
+ * synchronisation cudaFree implies.
+ *   d_model, d_data, d_weight : nPixels device doubles each (the model already
+ *                               cropped to the data; weights are 1/sigma, 0 where masked)
+ *   d_result                  : one device double receiving chi^2
+ *   stream                    : cudaStream_t to run on (NULL = legacy default stream)
+ * Nothing is allocated: the per-block partial sums live in one fixed
+ * file-scope device array of IMFIT_NOALLOC_MAX_BLOCKS * 5 doubles (160 KiB)
+ * that every GPU using the library keeps until the process exits.  Inputs
+ * larger than IMFIT_NOALLOC_MAX_PIXELS are rejected with IMFIT_E_ARG (see
+ * imfit_LastError(NULL)).  The first call on each device looks up the array's
+ * device address (with that device current); make that first call before any
+ * stream capture.  All calls share the one array, so calls that overlap on
+ * the GPU (different streams, or different host threads, on one device)
+ * race; serialise them.  The call only enqueues work on `stream`. */
+#define IMFIT_NOALLOC_MAX_BLOCKS 4096
+#define IMFIT_NOALLOC_MAX_PIXELS (IMFIT_NOALLOC_MAX_BLOCKS * 2048L)
+int imfit_ChiSquaredDeviceNoAlloc(const double *d_model, const double *d_data, const double *d_weight,
+                                  long nPixels, double *d_result, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
