@@ -80,6 +80,10 @@ _SIGS = [
     ("imfit_GetFastModelImageVector", _I, [_P, _DP, _DP]),
     ("imfit_SetKernelTiming", _I, [_P, _I]),
     ("imfit_GetKernelTimes", _I, [_P, _DP, ctypes.c_char_p, _I, _I]),
+    ("imfit_SetKernelTimingStage", _I, [_P, ctypes.c_char_p]),
+    ("imfit_SetConcurrentRegions", _I, [_P, _I]),
+    ("imfit_SetAutotune", _I, [_P, _I]),
+    ("imfit_GetLaunchShape", _I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     ("imfit_HostAlloc", _I, [ctypes.c_ulong, ctypes.POINTER(_P)]),
     ("imfit_HostFree", _I, [_P]),
     ("imfit_ChiSquaredDeviceNoAlloc", _I, [_P, _P, _P, _L, _P, _P]),
@@ -352,6 +356,20 @@ class ModelObject:
 
     def set_kernel_timing(self, flag):
         return self._ck(self.lib.imfit_SetKernelTiming(self.h, int(flag)))
+
+    def set_kernel_timing_stage(self, name=None):
+        return self._ck(self.lib.imfit_SetKernelTimingStage(self.h, name.encode() if name else None))
+
+    def set_concurrent_regions(self, flag):
+        return self._ck(self.lib.imfit_SetConcurrentRegions(self.h, int(flag)))
+
+    def set_autotune(self, flag):
+        return self._ck(self.lib.imfit_SetAutotune(self.h, int(flag)))
+
+    def launch_shape(self):
+        a, b, c = _I(), _I(), _I()
+        self._ck(self.lib.imfit_GetLaunchShape(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return {"rows_per_cta": a.value, "row_threads": b.value, "cols_per_cta": c.value}
 
     def kernel_times(self):
         """[(kernel name, ms)] of the most recent fast evaluation."""

@@ -270,14 +270,39 @@ __host__ __device__ inline double comp_value64_2d(const CompF64 &c, double x, do
 // The "E" factor below is the profile divided by its amplitude, so the
 // amplitude derivative is E itself and zero amplitudes need no special case.
 
-__device__ inline void comp_setup32(CompF32 &o, const CompDesc &d, const double *params) {
+// FP64 transcendentals of a component's Setup, computed by separate warps
+// (FP64 is a narrow pipe on this GPU: one long serial chain per component
+// would dominate the set-up time).
+struct SetupFP64 {
+  double cosPA, sinPA;  // orientation (PA + 90 deg)
+  double bn, dbn;       // Sersic b_n and db_n/dn
+  double log2re;        // Sersic log2(r_e)
+  double t;             // Moffat 2^(1/beta)
+};
+
+// b_n written in powers of 1/n (one division), same coefficients as
+// function_objects/helper_funcs.cpp:14-29
+__device__ inline void sersic_bn_horner(double n, double &bn, double &dbn) {
+  if (n > 0.36) {
+    const double v = 1.0 / n;
+    const double c1 = 0.009876543209876543, c2 = 0.0018028610621203215;
+    const double c3 = 0.00011409410586365319, c4 = -7.1510122958919723e-05;
+    bn = 2.0 * n - 0.333333333333333 + v * (c1 + v * (c2 + v * (c3 + v * c4)));
+    dbn = 2.0 - v * v * (c1 + v * (2.0 * c2 + v * (3.0 * c3 + v * 4.0 * c4)));
+  } else {
+    bn = sersic_bn(n);
+    dbn = sersic_dbn_dn(n);
+  }
+}
+
+__device__ inline void comp_setup32(CompF32 &o, const CompDesc &d, const double *params, const SetupFP64 &q) {
   const double *p = params + d.paramOffset;
   const double x0 = params[d.x0Index], y0 = params[d.x0Index + 1];
   o.type = d.type;
   o.subsample = d.subsample;
   o.paramOffset = d.paramOffset;
   o.x0Index = d.x0Index;
-  double xr = rint(x0), yr = rint(y0);
+  const double xr = rint(x0), yr = rint(y0);
   o.x0i = (int)xr;
   o.y0i = (int)yr;
   o.x0r = (float)(x0 - xr);
@@ -286,29 +311,27 @@ __device__ inline void comp_setup32(CompF32 &o, const CompDesc &d, const double 
   o.s0 = o.s1 = o.s2 = o.s3 = o.s4 = o.s5 = o.s6 = o.s7 = 0.f;
   o.subScale = 1.f; o.subInner = 3.f; o.subSmallK = 20.f;
   if (d.type != F_FLATSKY) {
-    double s, c;
-    sincos((p[0] + 90.0) * kDeg2Rad, &s, &c);
-    o.cosPA = (float)c;
-    o.sinPA = (float)s;
+    o.cosPA = (float)q.cosPA;
+    o.sinPA = (float)q.sinPA;
   }
   switch (d.type) {
     case F_SERSIC: {
-      double q = 1.0 - p[1], n = p[2], bn = sersic_bn(n);
-      o.q = (float)q; o.invq = (float)(1.0 / q);
+      const double qq = 1.0 - p[1], n = p[2];
+      o.q = (float)qq; o.invq = (float)(1.0 / qq);
       o.s0 = (float)p[3];
-      o.s1 = (float)(bn * kLog2e);
-      o.s2 = (float)log2(p[4]);
+      o.s1 = (float)(q.bn * kLog2e);
+      o.s2 = (float)q.log2re;
       o.s3 = (float)(1.0 / n);
-      o.s4 = (float)bn;
-      o.s5 = (float)sersic_dbn_dn(n);
+      o.s4 = (float)q.bn;
+      o.s5 = (float)q.dbn;
       o.s6 = (float)n;
       o.s7 = (float)p[4];
       o.subScale = (float)p[4]; o.subInner = 4.f; o.subSmallK = 20.f;
       break;
     }
     case F_EXP: {
-      double q = 1.0 - p[1];
-      o.q = (float)q; o.invq = (float)(1.0 / q);
+      const double qq = 1.0 - p[1];
+      o.q = (float)qq; o.invq = (float)(1.0 / qq);
       o.s0 = (float)p[2];
       o.s1 = (float)(kLog2e / p[3]);
       o.s2 = (float)p[3];
@@ -319,8 +342,8 @@ __device__ inline void comp_setup32(CompF32 &o, const CompDesc &d, const double 
       o.s0 = (float)p[0];
       break;
     case F_GRING: {
-      double q = 1.0 - p[1];
-      o.q = (float)q; o.invq = (float)(1.0 / q);
+      const double qq = 1.0 - p[1];
+      o.q = (float)qq; o.invq = (float)(1.0 / qq);
       o.s0 = (float)p[2];
       o.s1 = (float)p[3];
       o.s2 = (float)(kLog2e / (2.0 * p[4] * p[4]));
@@ -328,11 +351,10 @@ __device__ inline void comp_setup32(CompF32 &o, const CompDesc &d, const double 
       break;
     }
     case F_MOFFAT: {
-      double q = 1.0 - p[1];
-      double beta = p[4], fwhm = p[3];
-      double t = pow(2.0, 1.0 / beta);
-      double alpha = 0.5 * fwhm / sqrt(t - 1.0);
-      o.q = (float)q; o.invq = (float)(1.0 / q);
+      const double qq = 1.0 - p[1];
+      const double beta = p[4], fwhm = p[3], t = q.t;
+      const double alpha = 0.5 * fwhm / sqrt(t - 1.0);
+      o.q = (float)qq; o.invq = (float)(1.0 / qq);
       o.s0 = (float)p[2];
       o.s1 = (float)(1.0 / (alpha * alpha));
       o.s2 = (float)beta;
@@ -343,8 +365,8 @@ __device__ inline void comp_setup32(CompF32 &o, const CompDesc &d, const double 
       break;
     }
     case F_GAUSS: {
-      double q = 1.0 - p[1];
-      o.q = (float)q; o.invq = (float)(1.0 / q);
+      const double qq = 1.0 - p[1];
+      o.q = (float)qq; o.invq = (float)(1.0 / qq);
       o.s0 = (float)p[2];
       o.s1 = (float)(kLog2e / (2.0 * p[3] * p[3]));
       o.s2 = (float)p[3];

@@ -21,6 +21,8 @@
 // plus N + 3P - 1 padding) is exactly the set of model pixels the data
 // crop depends on; constant backgrounds (FlatSky) are added after the
 // convolution as I_sky * sum(PSF), which is what convolving a constant gives.
+#include <cstring>
+
 #include "kernels.h"
 #include "fft.cuh"
 
@@ -79,47 +81,154 @@ __device__ __forceinline__ int sub_count(const CompF32 &c, const Geo &g) {
 }
 
 // --------------------------------------------------------------- setup
-__global__ void k_fast_setup(FastArgs a) {
-  const int b = blockIdx.x;
-  const double *p = a.params + (long)b * a.nParams;
-  for (int c = threadIdx.x; c < a.nComp; c += blockDim.x) comp_setup32(a.comps[b * a.nComp + c], a.desc[c], p);
-  if (threadIdx.x == 0) {
-    double bg = 0.0;
-    for (int c = 0; c < a.nComp; c++)
-      if (a.desc[c].background) bg += p[a.desc[c].paramOffset];
-    a.bgLevel[2 * b] = (float)(bg * a.psfSum);
-    a.bgLevel[2 * b + 1] = (float)(bg * a.psfSumOs);
+// One CTA per (component, parameter vector); warp w computes the w-th group
+// of FP64 transcendentals, thread 0 assembles the FP32 component record.
+__global__ void __launch_bounds__(128) k_fast_setup(FastArgs a) {
+  const int c = blockIdx.x, b = blockIdx.y;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __shared__ SetupFP64 q;
+  const CompDesc d = a.desc[c];
+  const double *P = a.params + (long)b * a.nParams;
+  const double *p = P + d.paramOffset;
+  if (lane == 0) {
+    if (w == 0) {
+      if (d.type != F_FLATSKY) {
+        double sn, cs;
+        sincospi((p[0] + 90.0) / 180.0, &sn, &cs);
+        q.cosPA = cs;
+        q.sinPA = sn;
+      }
+    } else if (w == 1) {
+      if (d.type == F_SERSIC) sersic_bn_horner(p[2], q.bn, q.dbn);
+      if (d.type == F_MOFFAT) q.t = exp2(1.0 / p[4]);
+    } else if (w == 2) {
+      if (d.type == F_SERSIC) q.log2re = log2(p[4]);
+    } else if (w == 3 && c == 0) {
+      double bg = 0.0;
+      for (int k = 0; k < a.nComp; k++)
+        if (a.desc[k].background) bg += P[a.desc[k].paramOffset];
+      a.bgLevel[2 * b] = (float)(bg * a.psfSum);
+      a.bgLevel[2 * b + 1] = (float)(bg * a.psfSumOs);
+    }
   }
+  __syncthreads();
+  if (threadIdx.x == 0) comp_setup32(a.comps[b * a.nComp + c], d, P, q);
 }
 
 cudaError_t fast_setup(const FastArgs &a, int nBatch, cudaStream_t st) {
-  k_fast_setup<<<nBatch, 32, 0, st>>>(a);
+  k_fast_setup<<<dim3(a.nComp, nBatch), 128, 0, st>>>(a);
   return cudaGetLastError();
 }
 
+// ------------------------------------------- subsampled pixels (precomputed)
+// Offset of the table slot of (batch b, component c, window w).
+__device__ __forceinline__ long sub_base(const FastArgs &a, int b, int c, int w) {
+  const long areaM = (long)a.boxMain * a.boxMain, areaR = (long)a.boxReg * a.boxReg;
+  return (((long)b * a.nComp + c) * (areaM + areaR) + (w ? areaM : 0)) * 8;
+}
+
+__device__ __forceinline__ bool subsampling_type(int t) {
+  return t == F_SERSIC || t == F_EXP || t == F_MOFFAT || t == F_GAUSS;
+}
+
+// Box origin (window col, row) around a component centre.  Every pixel whose
+// centre is within radius 10 of the component centre (the only ones the
+// subsampling rule can touch) lies inside the box.
+__device__ __forceinline__ void box_origin(const WinDesc &w, const CompF32 &c, int side, int &col0, int &row0) {
+  if (!w.isRegion) {
+    col0 = c.x0i - w.xOrig - (side / 2 - 1);
+    row0 = c.y0i - w.yOrig - (side / 2 - 1);
+  } else {
+    const float tcx = ((float)(c.x0i - w.x1) + c.x0r - w.startOff) * (float)w.scale;
+    const float tcy = ((float)(c.y0i - w.y1) + c.y0r - w.startOff) * (float)w.scale;
+    col0 = (int)floorf(tcx) - w.offX - side / 2;
+    row0 = (int)floorf(tcy) - w.offY - side / 2;
+  }
+}
+
+// One warp per box pixel: the average over the pixel's ns x ns subsamples of
+// the profile and of its 7 derivatives (X0, Y0, then the function parameters).
+__global__ void __launch_bounds__(256) k_fast_subsample(FastArgs a, WinDesc w, int win) {
+  const int b = blockIdx.z, c = blockIdx.y;
+  const CompF32 cc = a.comps[b * a.nComp + c];
+  if (!cc.subsample || !subsampling_type(cc.type)) return;
+  const int side = win ? a.boxReg : a.boxMain;
+  int col0, row0;
+  box_origin(w, cc, side, col0, row0);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    int *o = a.subBox + (((long)b * a.nComp + c) * 2 + win) * 2;
+    o[0] = col0;
+    o[1] = row0;
+  }
+  const int lane = threadIdx.x & 31;
+  const int p = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (p >= side * side) return;
+  const int row = row0 + p / side, col = col0 + p % side;
+  if (row < 0 || row >= w.rows || col < 0 || col >= w.cols) return;
+  float dx, dy;
+  win_offsets(w, cc, row, col, dx, dy);
+  const Geo g = geo32(cc, dx, dy);
+  const int ns = sub_count(cc, g);
+  if (ns <= 1) return;
+  const float d = 1.f / ns;
+  const float xs = dx - 0.5f + 0.5f * d, ys = dy - 0.5f + 0.5f * d;
+  float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  float o[7];
+  for (int t = lane; t < ns * ns; t += 32) {
+    const int ii = t / ns, jj = t - ii * ns;
+    const Geo gs = geo32(cc, xs + ii * d, ys + jj * d);
+    acc[0] += radial32(cc, gs.r2);
+    const int np = radial_grad32(cc, gs, 1.f, o);
+#pragma unroll
+    for (int q = 0; q < 7; q++)
+      if (q < 2 + np) acc[1 + q] += o[q];
+  }
+#pragma unroll
+  for (int q = 0; q < 8; q++) acc[q] = warp_sum(acc[q]);
+  if (lane == 0) {
+    float *dst = a.subTab + sub_base(a, b, c, win) + (long)p * 8;
+    const float dd = d * d;
+#pragma unroll
+    for (int q = 0; q < 8; q++) dst[q] = acc[q] * dd;
+  }
+}
+
+// Subsampled value of component c at window pixel (row, col): table lookup,
+// or (outside the box, which the radius bound rules out) a direct sum.
+__device__ __forceinline__ float sub_value(const FastArgs &a, const int *box, int b, int c, int win,
+                                           const CompF32 &cc, int row, int col, float dx, float dy) {
+  const int side = win ? a.boxReg : a.boxMain;
+  const int br = row - box[1], bc = col - box[0];
+  if (br >= 0 && br < side && bc >= 0 && bc < side) return a.subTab[sub_base(a, b, c, win) + ((long)br * side + bc) * 8];
+  return comp_value32(cc, dx, dy, nullptr);
+}
+
 // ------------------------------------------------------ eval + row r2c
-__global__ void __launch_bounds__(256) k_fast_eval_r2c(FastArgs a, WinDesc w, FFTPlan<float> plan,
-                                                       const cplx<float> *__restrict__ twL, int rpb) {
+__global__ void __launch_bounds__(1024) k_fast_eval_r2c(FastArgs a, WinDesc w, FFTPlan<float> plan,
+                                                       const cplx<float> *__restrict__ twL, int rpb, int win) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int b = blockIdx.y;
   const int M = plan.n, ls = M + 1;
   CompF32 *sc = reinterpret_cast<CompF32 *>(smem);
-  cplx<float> *bufA = reinterpret_cast<cplx<float> *>(sc + kMaxComponents);
+  int *boxes = reinterpret_cast<int *>(sc + kMaxComponents);
+  cplx<float> *bufA = reinterpret_cast<cplx<float> *>(boxes + 2 * kMaxComponents);
   cplx<float> *bufB = bufA + rpb * ls;
-  unsigned char *flags = reinterpret_cast<unsigned char *>(bufB + rpb * ls);
   const int nC = a.nComp;
-  for (int i = threadIdx.x; i < nC; i += blockDim.x) sc[i] = a.comps[b * nC + i];
+  for (int i = threadIdx.x; i < nC; i += blockDim.x) {
+    sc[i] = a.comps[b * nC + i];
+    const int *o = a.subBox + (((long)b * nC + i) * 2 + win) * 2;
+    boxes[2 * i] = o[0];
+    boxes[2 * i + 1] = o[1];
+  }
   const int row0 = blockIdx.x * rpb;
   const int nl = min(rpb, w.rows - row0);
   __syncthreads();
   if (nl <= 0) return;
-  const int twoM = 2 * M;
-  // pass 1: one thread per complex point (two pixels)
+  // one thread per complex point (two pixels)
   for (int idx = threadIdx.x; idx < nl * M; idx += blockDim.x) {
     const int l = idx / M, k = idx - l * M;
     const int row = row0 + l;
     float v[2] = {0.f, 0.f};
-    unsigned char f[2] = {0, 0};
 #pragma unroll
     for (int e = 0; e < 2; e++) {
       const int col = 2 * k + e;
@@ -130,55 +239,14 @@ __global__ void __launch_bounds__(256) k_fast_eval_r2c(FastArgs a, WinDesc w, FF
           float dx, dy;
           win_offsets(w, cc, row, col, dx, dy);
           const Geo g = geo32(cc, dx, dy);
-          if (sub_count(cc, g) > 1) {
-            f[e] = 1;
-            continue;
-          }
-          v[e] += radial32(cc, g.r2);
+          if (sub_count(cc, g) > 1)
+            v[e] += sub_value(a, boxes + 2 * c, b, c, win, cc, row, col, dx, dy);
+          else
+            v[e] += radial32(cc, g.r2);
         }
       }
     }
     bufA[l * ls + k] = {v[0], v[1]};
-    flags[l * twoM + 2 * k] = f[0];
-    flags[l * twoM + 2 * k + 1] = f[1];
-  }
-  __syncthreads();
-  // pass 2: subsampled pixels, one warp per pixel
-  {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const int cpr = (twoM + 31) >> 5;
-    for (int ch = wid; ch < nl * cpr; ch += nw) {
-      const int l = ch / cpr, p0 = (ch - l * cpr) << 5;
-      const int p = p0 + lane;
-      unsigned mask = __ballot_sync(0xffffffffu, (p < twoM) && flags[l * twoM + p]);
-      while (mask) {
-        const int q = p0 + __ffs(mask) - 1;
-        mask &= mask - 1;
-        float tot = 0.f;
-        for (int c = 0; c < nC; c++) {
-          const CompF32 &cc = sc[c];
-          if (cc.type == F_FLATSKY) continue;
-          float dx, dy;
-          win_offsets(w, cc, row0 + l, q, dx, dy);
-          const Geo g = geo32(cc, dx, dy);
-          const int ns = sub_count(cc, g);
-          if (ns <= 1) continue;
-          const float d = 1.f / ns;
-          const float xs = dx - 0.5f + 0.5f * d, ys = dy - 0.5f + 0.5f * d;
-          float s = 0.f;
-          for (int t = lane; t < ns * ns; t += 32) {
-            const int ii = t / ns, jj = t - ii * ns;
-            const Geo gs = geo32(cc, xs + ii * d, ys + jj * d);
-            s += radial32(cc, gs.r2);
-          }
-          tot += warp_sum(s) * (d * d);
-        }
-        if (lane == 0) {
-          cplx<float> &z = bufA[l * ls + (q >> 1)];
-          if (q & 1) z.y += tot; else z.x += tot;
-        }
-      }
-    }
   }
   __syncthreads();
   cplx<float> *Z = block_fft(bufA, bufB, plan, nl, ls, 1, -1, false);
@@ -190,7 +258,7 @@ __global__ void __launch_bounds__(256) k_fast_eval_r2c(FastArgs a, WinDesc w, FF
 }
 
 // ---------------------------------------- region: c2r + block average
-__global__ void __launch_bounds__(256) k_fast_region_down(FastArgs a, FastGeom g, const cplx<float> *__restrict__ rspec,
+__global__ void __launch_bounds__(1024) k_fast_region_down(FastArgs a, FastGeom g, const cplx<float> *__restrict__ rspec,
                                                           FFTPlan<float> plan, const cplx<float> *__restrict__ twL) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int b = blockIdx.y, s = blockIdx.x;  // replaced data row within the region
@@ -226,7 +294,12 @@ __global__ void __launch_bounds__(256) k_fast_region_down(FastArgs a, FastGeom g
 }
 
 // -------------------------- stat rows: c2r + statistic + g + g row r2c
-__device__ __forceinline__ void stat_term(const FastArgs &a, long z, float m, double &S, float &gout) {
+// Per-pixel statistic term (FP32, accumulated per thread in FP32 over a few
+// pixels; the block and final reductions are FP64) and its derivative
+// g = dS/dM.  chi^2: (w (d - M))^2; with model-based errors
+// (d - M)^2 / V(M), V = (M + sky)/g_eff + n_comb rn^2; Cash: 2 w (m' - d' ln m' + extra)
+// with m' = g_eff (M + sky), ln m' replaced by 1e-25 when m' <= 0 (core/model_object.cpp:1703-1775).
+__device__ __forceinline__ void stat_term(const FastArgs &a, long z, float m, float &S, float &gout) {
   const float cnt = a.count ? a.count[z] : 1.f;
   const float w = a.weight[z];
   if (cnt == 0.f || (w == 0.f && !a.modelErrors)) {
@@ -242,38 +315,36 @@ __device__ __forceinline__ void stat_term(const FastArgs &a, long z, float m, do
       }
       const float V = (m + a.sky) / a.effGain + a.rnTerm;
       const float r = d - m;
-      S += (double)cnt * (double)r * (double)r / (double)V;
+      S += cnt * r * r / V;
       gout = cnt * (-2.f * r / V - r * r / (V * V * a.effGain));
     } else {
       const float dev = w * (d - m);
-      S += (double)cnt * (double)dev * (double)dev;
+      S += cnt * dev * dev;
       gout = -2.f * cnt * w * dev;
     }
   } else {
     const float mv = a.effGain * (m + a.sky);
     const float dv = a.effGain * (d + a.sky);
     const float ex = a.extra ? a.extra[z] : 0.f;
-    double term;
-    float dterm;
+    float term, dterm;
     if (mv > 0.f) {
       if (ex != 0.f && dv > 0.f) {
         // (mv - dv ln mv) + (dv ln dv - dv) written without cancellation
-        const float del = (mv - dv) / dv;
-        term = (double)(mv - dv) - (double)dv * (double)log1pf(del);
+        term = (mv - dv) - dv * log1pf((mv - dv) / dv);
       } else {
-        term = (double)mv - (double)dv * (double)logf(mv) + (double)ex;
+        term = mv - dv * logf(mv) + ex;
       }
       dterm = a.effGain * (1.f - dv / mv);
     } else {
-      term = (double)mv - (double)dv * 1.0e-25 + (double)ex;
+      term = mv - dv * 1.0e-25f + ex;
       dterm = a.effGain;
     }
-    S += 2.0 * (double)cnt * (double)w * term;
+    S += 2.f * cnt * w * term;
     gout = 2.f * cnt * w * dterm;
   }
 }
 
-__global__ void __launch_bounds__(256) k_fast_stat_rows(FastArgs a, FastGeom g, FFTPlan<float> plan,
+__global__ void __launch_bounds__(1024) k_fast_stat_rows(FastArgs a, FastGeom g, FFTPlan<float> plan,
                                                         const cplx<float> *__restrict__ twL, int rpb, int wantGrad) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int b = blockIdx.y;
@@ -281,11 +352,11 @@ __global__ void __launch_bounds__(256) k_fast_stat_rows(FastArgs a, FastGeom g, 
   cplx<float> *bufX = reinterpret_cast<cplx<float> *>(smem);
   cplx<float> *bufA = bufX + rpb * ls;
   cplx<float> *bufB = bufA + rpb * ls;
-  __shared__ double red[2][32];
+  __shared__ float red[2][32];
   const int row0 = blockIdx.x * rpb;
   const int nl = min(rpb, g.nDataRows - row0);
   cplx<float> *spec = reinterpret_cast<cplx<float> *>(a.spec) + (long)b * g.specBatch;
-  double S = 0.0, SG = 0.0;
+  float S = 0.f, SG = 0.f;
   if (nl > 0) {
     for (int idx = threadIdx.x; idx < nl * (M + 1); idx += blockDim.x) {
       const int l = idx / (M + 1), k = idx - l * (M + 1);
@@ -325,7 +396,7 @@ __global__ void __launch_bounds__(256) k_fast_stat_rows(FastArgs a, FastGeom g, 
         if (a.modelOut) a.modelOut[(long)b * g.nDataRows * g.nDataCols + zi] = m;
         float gz;
         stat_term(a, zi, m, S, gz);
-        SG += (double)gz * (double)(inReg ? a.psfSumOs : a.psfSum);
+        SG += gz * (inReg ? a.psfSumOs : a.psfSum);
         if (inReg) {
           if (wantGrad) a.regG[ri] = gz;
           gz = 0.f;
@@ -344,29 +415,31 @@ __global__ void __launch_bounds__(256) k_fast_stat_rows(FastArgs a, FastGeom g, 
       }
     }
   }
-  // block reduction of (S, SG)
+  // CTA partial sums of (S, SG): FP32 tree over this CTA's pixels
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  S = warp_sum_d(S);
-  SG = warp_sum_d(SG);
+  S = warp_sum(S);
+  SG = warp_sum(SG);
   if (lane == 0) {
     red[0][wid] = S;
     red[1][wid] = SG;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    double s0 = 0.0, s1 = 0.0;
-    for (int i = 0; i < (int)(blockDim.x >> 5); i++) {
-      s0 += red[0][i];
-      s1 += red[1][i];
+  if (wid == 0) {
+    const int nw = blockDim.x >> 5;
+    float v0 = lane < nw ? red[0][lane] : 0.f;
+    float v1 = lane < nw ? red[1][lane] : 0.f;
+    v0 = warp_sum(v0);
+    v1 = warp_sum(v1);
+    if (lane == 0) {
+      float *p = a.statPart + (long)b * 2 * a.partStride + blockIdx.x;
+      p[0] = v0;
+      p[a.partStride] = v1;
     }
-    double *p = a.statPart + ((long)b * a.nStatBlocks + blockIdx.x) * 2;
-    p[0] = s0;
-    p[1] = s1;
   }
 }
 
 // --------------------------- region adjoint seed: g/k^2 on subpixels, r2c
-__global__ void __launch_bounds__(256) k_fast_region_g_r2c(FastArgs a, FastGeom g, cplx<float> *__restrict__ rspec,
+__global__ void __launch_bounds__(1024) k_fast_region_g_r2c(FastArgs a, FastGeom g, cplx<float> *__restrict__ rspec,
                                                            FFTPlan<float> plan, const cplx<float> *__restrict__ twL) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int b = blockIdx.y, u = blockIdx.x;  // subpixel row
@@ -390,23 +463,27 @@ __global__ void __launch_bounds__(256) k_fast_region_g_r2c(FastArgs a, FastGeom 
 }
 
 // ---------------------------------------- gradient pass over the window
-__global__ void __launch_bounds__(256) k_fast_grad_rows(FastArgs a, WinDesc w, FFTPlan<float> plan,
+__global__ void __launch_bounds__(1024) k_fast_grad_rows(FastArgs a, WinDesc w, FFTPlan<float> plan,
                                                         const cplx<float> *__restrict__ twL, int rpb,
-                                                        double *__restrict__ gradPart, int nBlocksTotal,
-                                                        int blockBase) {
+                                                        float *__restrict__ gradPart, int blockBase, int win) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int b = blockIdx.y;
   const int M = plan.n, ls = M + 1;
   CompF32 *sc = reinterpret_cast<CompF32 *>(smem);
-  double *gsm = reinterpret_cast<double *>(sc + kMaxComponents);
+  int *boxes = reinterpret_cast<int *>(sc + kMaxComponents);
+  float *gsm = reinterpret_cast<float *>(boxes + 2 * kMaxComponents);
   cplx<float> *bufX = reinterpret_cast<cplx<float> *>(gsm + kMaxParams);
   cplx<float> *bufA = bufX + rpb * ls;
   cplx<float> *bufB = bufA + rpb * ls;
-  unsigned char *flags = reinterpret_cast<unsigned char *>(bufB + rpb * ls);
-  __shared__ float red[8][8];
+  __shared__ float red[32][8];
   const int nC = a.nComp, nP = a.nParams;
-  for (int i = threadIdx.x; i < nC; i += blockDim.x) sc[i] = a.comps[b * nC + i];
-  for (int i = threadIdx.x; i < nP; i += blockDim.x) gsm[i] = 0.0;
+  for (int i = threadIdx.x; i < nC; i += blockDim.x) {
+    sc[i] = a.comps[b * nC + i];
+    const int *o = a.subBox + (((long)b * nC + i) * 2 + win) * 2;
+    boxes[2 * i] = o[0];
+    boxes[2 * i + 1] = o[1];
+  }
+  for (int i = threadIdx.x; i < nP; i += blockDim.x) gsm[i] = 0.f;
   const int row0 = blockIdx.x * rpb;
   const int nl = min(rpb, w.rows - row0);
   const cplx<float> *spec = w.spec + (long)b * w.specBatch;
@@ -423,58 +500,51 @@ __global__ void __launch_bounds__(256) k_fast_grad_rows(FastArgs a, WinDesc w, F
     __syncthreads();
     cplx<float> *Z = block_fft(bufA, bufB, plan, nl, ls, 1, +1, false);
     const float *rt = reinterpret_cast<const float *>(Z);  // r~ of (l, col) at rt[2*(l*ls) + col]
-    const int twoM = 2 * M;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int npix = nl * w.cols;
     for (int c = 0; c < nC; c++) {
       const CompF32 &cc = sc[c];
       if (cc.type == F_FLATSKY) continue;
+      const int side = win ? a.boxReg : a.boxMain;
+      const float *tab = a.subTab + sub_base(a, b, c, win);
       float acc[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
       float o[7];
-      for (int idx = threadIdx.x; idx < nl * twoM; idx += blockDim.x) {
-        const int l = idx / twoM, col = idx - l * twoM;
-        unsigned char f = 0;
-        if (col < w.cols) {
-          const float r = rt[2 * l * ls + col];
-          float dx, dy;
-          win_offsets(w, cc, row0 + l, col, dx, dy);
-          const Geo g = geo32(cc, dx, dy);
-          if (sub_count(cc, g) > 1) {
-            f = 1;
-          } else if (r != 0.f) {
-            const int np = radial_grad32(cc, g, r, o);
+      for (int idx = threadIdx.x; idx < npix; idx += blockDim.x) {
+        const int l = idx / w.cols, col = idx - l * w.cols;
+        const int row = row0 + l;
+        const float r = rt[2 * l * ls + col];
+        float dx, dy;
+        win_offsets(w, cc, row, col, dx, dy);
+        const Geo g = geo32(cc, dx, dy);
+        int np;
+        if (sub_count(cc, g) > 1) {
+          const int br = row - boxes[2 * c + 1], bc = col - boxes[2 * c];
+          if (br >= 0 && br < side && bc >= 0 && bc < side) {
+            const float *t = tab + ((long)br * side + bc) * 8 + 1;
 #pragma unroll
-            for (int q = 0; q < 7; q++)
-              if (q < 2 + np) acc[q] += o[q];
-          }
-        }
-        flags[l * twoM + col] = f;
-      }
-      __syncthreads();
-      const int cprr = (twoM + 31) >> 5;
-      for (int ch = wid; ch < nl * cprr; ch += nw) {
-        const int l = ch / cprr, p0 = (ch - l * cprr) << 5;
-        const int p = p0 + lane;
-        unsigned mask = __ballot_sync(0xffffffffu, (p < twoM) && flags[l * twoM + p]);
-        while (mask) {
-          const int q = p0 + __ffs(mask) - 1;
-          mask &= mask - 1;
-          const float r = rt[2 * l * ls + q];
-          float dx, dy;
-          win_offsets(w, cc, row0 + l, q, dx, dy);
-          const Geo g = geo32(cc, dx, dy);
-          const int ns = sub_count(cc, g);
-          const float d = 1.f / ns;
-          const float scale = r * d * d;
-          const float xs = dx - 0.5f + 0.5f * d, ys = dy - 0.5f + 0.5f * d;
-          for (int t = lane; t < ns * ns; t += 32) {
-            const int ii = t / ns, jj = t - ii * ns;
-            const Geo gs = geo32(cc, xs + ii * d, ys + jj * d);
-            const int np = radial_grad32(cc, gs, scale, o);
+            for (int q = 0; q < 7; q++) o[q] = r * t[q];
+            np = 5;  // unused slots of the table are zero
+          } else {
+            // outside the precomputed box (not reached for radius < 10): direct average
+            const int ns = sub_count(cc, g);
+            const float d = 1.f / ns;
+            float s7[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            for (int t = 0; t < ns * ns; t++) {
+              const Geo gs = geo32(cc, dx - 0.5f + (t / ns + 0.5f) * d, dy - 0.5f + (t % ns + 0.5f) * d);
+              const int n2 = radial_grad32(cc, gs, r * d * d, o);
+              for (int q = 0; q < 2 + n2; q++) s7[q] += o[q];
+            }
 #pragma unroll
-            for (int qq = 0; qq < 7; qq++)
-              if (qq < 2 + np) acc[qq] += o[qq];
+            for (int q = 0; q < 7; q++) o[q] = s7[q];
+            np = 5;
           }
+        } else {
+          if (r == 0.f) continue;
+          np = radial_grad32(cc, g, r, o);
         }
+#pragma unroll
+        for (int q = 0; q < 7; q++)
+          if (q < 2 + np) acc[q] += o[q];
       }
       // block reduction of acc[0..6]
 #pragma unroll
@@ -484,64 +554,63 @@ __global__ void __launch_bounds__(256) k_fast_grad_rows(FastArgs a, WinDesc w, F
         for (int q = 0; q < 7; q++) red[wid][q] = acc[q];
       }
       __syncthreads();
-      if (threadIdx.x == 0) {
-        double t[7] = {0, 0, 0, 0, 0, 0, 0};
-        for (int i = 0; i < nw; i++)
-          for (int q = 0; q < 7; q++) t[q] += (double)red[i][q];
-        gsm[cc.x0Index] += t[0];
-        gsm[cc.x0Index + 1] += t[1];
+      if (threadIdx.x < 7) {
+        float t = 0.f;
+        for (int i = 0; i < nw; i++) t += red[i][threadIdx.x];
+        const int q = threadIdx.x;
         const int npf = a.desc[c].nParams;
-        for (int q = 0; q < npf && q < 5; q++) gsm[cc.paramOffset + q] += t[2 + q];
+        if (q == 0) gsm[cc.x0Index] += t;
+        else if (q == 1) gsm[cc.x0Index + 1] += t;
+        else if (q - 2 < npf) gsm[cc.paramOffset + q - 2] += t;
       }
       __syncthreads();
     }
   }
   __syncthreads();
-  double *out = gradPart + ((long)b * nBlocksTotal + blockBase + blockIdx.x) * nP;
-  for (int i = threadIdx.x; i < nP; i += blockDim.x) out[i] = gsm[i];
+  float *out = gradPart + (long)b * nP * a.partStride + blockBase + blockIdx.x;
+  for (int i = threadIdx.x; i < nP; i += blockDim.x) out[(long)i * a.partStride] = gsm[i];
 }
 
 // ------------------------------------------------------------- reduce
-__global__ void __launch_bounds__(256) k_fast_reduce(FastArgs a, int nGradBlocks, int wantGrad) {
-  const int b = blockIdx.x;
+// One CTA per output quantity (statistic, background term, each gradient
+// entry): FP64 sum of the per-CTA FP32 partials in a fixed order.
+__device__ __forceinline__ double block_sum_d(double v) {
   __shared__ double sh[32];
-  // statistic
-  double s = 0.0, sg = 0.0;
-  for (int i = threadIdx.x; i < a.nStatBlocks; i += blockDim.x) {
-    const double *p = a.statPart + ((long)b * a.nStatBlocks + i) * 2;
-    s += p[0];
-    sg += p[1];
-  }
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  s = warp_sum_d(s);
-  sg = warp_sum_d(sg);
-  if (lane == 0) sh[wid] = s;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  v = warp_sum_d(v);
+  if (lane == 0) sh[wid] = v;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int i = 0; i < nw; i++) t += sh[i];
+  if (wid == 0) {
+    const int nw = blockDim.x >> 5;
+    v = lane < nw ? sh[lane] : 0.0;
+    v = warp_sum_d(v);
+  }
+  return v;
+}
+
+__global__ void __launch_bounds__(256) k_fast_reduce(FastArgs a, int nGradBlocks) {
+  const int j = blockIdx.x, b = blockIdx.y;
+  double t = 0.0;
+  if (j < 2) {
+    const float *p = a.statPart + ((long)b * 2 + j) * a.partStride;
+    for (int i = threadIdx.x; i < a.nStatBlocks; i += blockDim.x) t += (double)p[i];
+  } else {
+    const float *p = a.gradPart + ((long)b * a.nParams + (j - 2)) * a.partStride;
+    for (int i = threadIdx.x; i < nGradBlocks; i += blockDim.x) t += (double)p[i];
+  }
+  t = block_sum_d(t);
+  if (threadIdx.x != 0) return;
+  if (j == 0) {
     a.stat[b] = t;
-  }
-  __syncthreads();
-  if (lane == 0) sh[wid] = sg;
-  __syncthreads();
-  double sgt = 0.0;
-  if (threadIdx.x == 0)
-    for (int i = 0; i < nw; i++) sgt += sh[i];
-  __syncthreads();
-  if (threadIdx.x == 0) sh[0] = sgt;
-  __syncthreads();
-  sgt = sh[0];
-  if (!wantGrad) return;
-  for (int j = threadIdx.x; j < a.nParams; j += blockDim.x) {
-    double t = 0.0;
-    for (int i = 0; i < nGradBlocks; i++) t += a.gradPart[((long)b * nGradBlocks + i) * a.nParams + j];
-    a.grad[(long)b * a.nParams + j] = t;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
+  } else if (j == 1) {
+    if (nGradBlocks > 0)
+      for (int c = 0; c < a.nComp; c++)
+        if (a.desc[c].background) a.grad[(long)b * a.nParams + a.desc[c].paramOffset] = t;
+  } else {
+    bool bgParam = false;
     for (int c = 0; c < a.nComp; c++)
-      if (a.desc[c].background) a.grad[(long)b * a.nParams + a.desc[c].paramOffset] = sgt;
+      if (a.desc[c].background && a.desc[c].paramOffset == j - 2) bgParam = true;
+    if (!bgParam) a.grad[(long)b * a.nParams + (j - 2)] = t;
   }
 }
 
@@ -556,18 +625,9 @@ static FFTPlan<float> plan32(const FFTLen &L, bool half) {
   return p;
 }
 
-static int fast_rpb(int M) {
-  // ~40 KB of complex line buffers per CTA
-  int r = (40 * 1024) / (3 * (M + 1) * 8);
-  if (r < 1) r = 1;
-  if (r > 4) r = 4;
-  return r;
-}
 
-int fast_stat_blocks(const FastGeom &g) {
-  const int M = (g.specPitch - 1);
-  const int rpb = fast_rpb(M);
-  return (g.nDataRows + rpb - 1) / rpb;
+int fast_stat_blocks(const FastGeom &g, const FastTune &t) {
+  return (g.nDataRows + t.rowRpb - 1) / t.rowRpb;
 }
 
 static WinDesc main_win(const FastGeom &g, void *spec) {
@@ -601,151 +661,214 @@ static WinDesc region_win(const FastGeom &g, void *rspec) {
   return w;
 }
 
-int fast_grad_blocks(const FastGeom &g) {
-  const int rpb = fast_rpb(g.specPitch - 1);
-  return (g.winRows + rpb - 1) / rpb;
+int fast_grad_blocks(const FastGeom &g, const FastTune &t) {
+  return (g.winRows + t.rowRpb - 1) / t.rowRpb;
 }
 
-int fast_reg_grad_blocks(const FastGeom &g) {
+int fast_reg_grad_blocks(const FastGeom &g, const FastTune &t) {
   if (!g.hasRegion) return 0;
-  const int rpb = fast_rpb(g.rSpecPitch - 1);
-  return (g.rWinRows + rpb - 1) / rpb;
+  return (g.rWinRows + t.rowRpb - 1) / t.rowRpb;
 }
 
 template <typename K>
 static void ensure_smem(K kern, size_t bytes) {
-  if (bytes > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  (void)bytes;
+  allow_max_smem((const void *)kern);
 }
 
-static cudaError_t launch_eval(const FastArgs &a, const WinDesc &w, const FFTLen &L, int nBatch, cudaStream_t st) {
+static cudaError_t launch_subsample(const FastArgs &a, const WinDesc &w, int win, int nBatch, cudaStream_t st) {
+  const int side = win ? a.boxReg : a.boxMain;
+  dim3 grid((side * side + 7) / 8, a.nComp, nBatch);
+  k_fast_subsample<<<grid, 256, 0, st>>>(a, w, win);
+  return cudaGetLastError();
+}
+
+static cudaError_t launch_eval(const FastArgs &a, const WinDesc &w, const FFTLen &L, int nBatch, int win,
+                               const FastTune &tu, cudaStream_t st) {
   const int M = L.half.n;
-  const int rpb = fast_rpb(M);
-  const size_t sm = sizeof(CompF32) * kMaxComponents + sizeof(cplx<float>) * 2 * rpb * (M + 1) + (size_t)rpb * 2 * M + 16;
+  const int rpb = tu.rowRpb;
+  const size_t sm = sizeof(CompF32) * kMaxComponents + sizeof(int) * 2 * kMaxComponents +
+                    sizeof(cplx<float>) * 2 * rpb * (M + 1) + 16;
   ensure_smem(k_fast_eval_r2c, sm);
   dim3 grid((w.rows + rpb - 1) / rpb, nBatch);
-  k_fast_eval_r2c<<<grid, 256, sm, st>>>(a, w, plan32(L, true), reinterpret_cast<const cplx<float> *>(L.twL32), rpb);
+  k_fast_eval_r2c<<<grid, tu.rowThreads, sm, st>>>(a, w, plan32(L, true), reinterpret_cast<const cplx<float> *>(L.twL32), rpb,
+                                         win);
   return cudaGetLastError();
 }
 
-static cudaError_t launch_grad(const FastArgs &a, const WinDesc &w, const FFTLen &L, int nBatch, int nBlocksTotal,
-                               int blockBase, cudaStream_t st) {
+static cudaError_t launch_grad(const FastArgs &a, const WinDesc &w, const FFTLen &L, int nBatch, int blockBase,
+                               int win, const FastTune &tu, cudaStream_t st) {
   const int M = L.half.n;
-  const int rpb = fast_rpb(M);
-  const size_t sm = sizeof(CompF32) * kMaxComponents + sizeof(double) * kMaxParams +
-                    sizeof(cplx<float>) * 3 * rpb * (M + 1) + (size_t)rpb * 2 * M + 16;
+  const int rpb = tu.rowRpb;
+  const size_t sm = sizeof(CompF32) * kMaxComponents + sizeof(int) * 2 * kMaxComponents +
+                    sizeof(float) * kMaxParams + sizeof(cplx<float>) * 3 * rpb * (M + 1) + 16;
   ensure_smem(k_fast_grad_rows, sm);
   dim3 grid((w.rows + rpb - 1) / rpb, nBatch);
-  k_fast_grad_rows<<<grid, 256, sm, st>>>(a, w, plan32(L, true), reinterpret_cast<const cplx<float> *>(L.twL32), rpb,
-                                          a.gradPart, nBlocksTotal, blockBase);
+  k_fast_grad_rows<<<grid, tu.rowThreads, sm, st>>>(a, w, plan32(L, true), reinterpret_cast<const cplx<float> *>(L.twL32), rpb,
+                                                   a.gradPart, blockBase, win);
   return cudaGetLastError();
 }
 
-static void mark(const FastPlan &p, const char *name, cudaStream_t st) {
-  StageTimer *t = p.timer;
-  if (!t || t->n >= StageTimer::kMax) return;
+static void record(cudaEvent_t ev, cudaStream_t st) {
   // while the stream is being captured the record must be External to become an
   // event-record node of the graph; outside capture that flag is not allowed
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   cudaStreamIsCapturing(st, &cs);
   if (cs == cudaStreamCaptureStatusActive)
-    cudaEventRecordWithFlags(t->ev[t->n], st, cudaEventRecordExternal);
+    cudaEventRecordWithFlags(ev, st, cudaEventRecordExternal);
   else
-    cudaEventRecord(t->ev[t->n], st);
+    cudaEventRecord(ev, st);
+}
+
+// called before a kernel of the given stage is launched
+static void stage_begin(const FastPlan &p, const char *name, cudaStream_t st) {
+  StageTimer *t = p.timer;
+  if (t && t->only && strcmp(t->only, name) == 0) {
+    record(t->ev[0], st);
+    t->names[0] = "start";
+  }
+}
+
+// called after the kernel of the stage has been launched
+static void stage_end(const FastPlan &p, const char *name, cudaStream_t st) {
+  StageTimer *t = p.timer;
+  if (!t) return;
+  if (t->only) {
+    if (strcmp(t->only, name) == 0) {
+      record(t->ev[1], st);
+      t->names[1] = name;
+      t->n = 2;
+    }
+    return;
+  }
+  if (t->n >= StageTimer::kMax) return;
+  record(t->ev[t->n], st);
   t->names[t->n] = name;
   t->n++;
 }
 
+#define STAGE(name, stream, call)        \
+  do {                                   \
+    stage_begin(p, name, stream);        \
+    cudaError_t e_ = (call);             \
+    if (e_) return e_;                   \
+    stage_end(p, name, stream);          \
+  } while (0)
+
+static cudaError_t launch_region_down(const FastPlan &p, const FastArgs &a, int nBatch, cudaStream_t st) {
+  const FastGeom &g = p.g;
+  const int M = p.Rx->half.n;
+  const size_t sm = sizeof(cplx<float>) * 3 * g.rScale * (M + 1);
+  ensure_smem(k_fast_region_down, sm);
+  k_fast_region_down<<<dim3(g.rRows, nBatch), line_threads(M * g.rScale / 2), sm, st>>>(a, g, reinterpret_cast<const cplx<float> *>(a.rspec),
+                                                             plan32(*p.Rx, true),
+                                                             reinterpret_cast<const cplx<float> *>(p.Rx->twL32));
+  return cudaGetLastError();
+}
+
+static cudaError_t launch_stat(const FastPlan &p, const FastArgs &a, int nBatch, bool wantGrad, cudaStream_t st) {
+  const FastGeom &g = p.g;
+  const int M = p.Lx->half.n;
+  const int rpb = p.tune.rowRpb;
+  const size_t sm = sizeof(cplx<float>) * 3 * rpb * (M + 1);
+  ensure_smem(k_fast_stat_rows, sm);
+  dim3 grid((g.nDataRows + rpb - 1) / rpb, nBatch);
+  k_fast_stat_rows<<<grid, p.tune.rowThreads, sm, st>>>(a, g, plan32(*p.Lx, true),
+                                          reinterpret_cast<const cplx<float> *>(p.Lx->twL32), rpb, wantGrad ? 1 : 0);
+  return cudaGetLastError();
+}
+
+static cudaError_t launch_region_g(const FastPlan &p, const FastArgs &a, int nBatch, cudaStream_t st) {
+  const FastGeom &g = p.g;
+  const int M = p.Rx->half.n;
+  const size_t sm = sizeof(cplx<float>) * 2 * (M + 1);
+  k_fast_region_g_r2c<<<dim3(g.rSubRows, nBatch), line_threads(M), sm, st>>>(
+      a, g, reinterpret_cast<cplx<float> *>(a.rspec), plan32(*p.Rx, true),
+      reinterpret_cast<const cplx<float> *>(p.Rx->twL32));
+  return cudaGetLastError();
+}
+
+static cudaError_t launch_reduce(const FastArgs &a, int nBatch, int nGrad, int wantGrad, cudaStream_t st) {
+  k_fast_reduce<<<dim3(2 + (wantGrad ? a.nParams : 0), nBatch), 256, 0, st>>>(a, wantGrad ? nGrad : 0);
+  return cudaGetLastError();
+}
+
+// The whole statistic (+ gradient) evaluation.  With p.side set, the
+// oversampled-region pipeline runs on the side stream, forked after the
+// main-window subsample table and joined before the statistic (forward) and
+// before the final reduction (adjoint).
 cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool wantGrad, cudaStream_t st) {
   const FastGeom &g = p.g;
   if (p.timer) p.timer->n = 0;
-  mark(p, "start", st);
-  cudaError_t e = fast_setup(a, nBatch, st);
-  if (e) return e;
-  mark(p, "setup", st);
-  // main window -> spectrum
-  e = launch_eval(a, main_win(g, a.spec), *p.Lx, nBatch, st);
-  if (e) return e;
-  mark(p, "eval_r2c", st);
+  if (p.timer && !p.timer->only) stage_end(p, "start", st);
+  const bool fork = g.hasRegion && p.side;
+  cudaStream_t rs = fork ? p.side : st;
   const float scale = 1.f / ((float)p.Lx->L * (float)p.Ly->L);
-  e = launch_cols<float>(a.spec, g.specPitch, g.specBatch, p.Lx->L / 2 + 1, g.winRows, g.nDataRows, p.H, p.hPitch,
-                         *p.Ly, scale, 1, nBatch, st);
-  if (e) return e;
-  mark(p, "cols_conv", st);
+  const float rscale = g.hasRegion ? 1.f / ((float)p.Rx->L * (float)p.Ry->L) : 0.f;
+  const FastTune &tu = p.tune;
+  const int nMain = fast_grad_blocks(g, tu), nReg = fast_reg_grad_blocks(g, tu);
+  const int nTot = nMain + nReg;
+
+  STAGE("setup", st, fast_setup(a, nBatch, st));
+  if (fork) {
+    cudaError_t e = cudaEventRecord(p.fork0, st);
+    if (!e) e = cudaStreamWaitEvent(rs, p.fork0, 0);
+    if (e) return e;
+  }
   if (g.hasRegion) {
-    e = launch_eval(a, region_win(g, a.rspec), *p.Rx, nBatch, st);
-    if (e) return e;
-    mark(p, "region_eval_r2c", st);
-    const float rscale = 1.f / ((float)p.Rx->L * (float)p.Ry->L);
-    e = launch_cols<float>(a.rspec, g.rSpecPitch, g.rSpecBatch, p.Rx->L / 2 + 1, g.rWinRows, g.rSubRows, p.Hr,
-                           p.hrPitch, *p.Ry, rscale, 1, nBatch, st);
-    if (e) return e;
-    mark(p, "region_cols_conv", st);
-    const int M = p.Rx->half.n;
-    const size_t sm = sizeof(cplx<float>) * 3 * g.rScale * (M + 1);
-    ensure_smem(k_fast_region_down, sm);
-    k_fast_region_down<<<dim3(g.rRows, nBatch), 256, sm, st>>>(a, g, reinterpret_cast<const cplx<float> *>(a.rspec),
-                                                               plan32(*p.Rx, true),
-                                                               reinterpret_cast<const cplx<float> *>(p.Rx->twL32));
-    e = cudaGetLastError();
-    if (e) return e;
-    mark(p, "region_down", st);
+    STAGE("region_subsample", rs, launch_subsample(a, region_win(g, a.rspec), 1, nBatch, rs));
+    STAGE("region_eval_r2c", rs, launch_eval(a, region_win(g, a.rspec), *p.Rx, nBatch, 1, tu, rs));
+    STAGE("region_cols_conv", rs,
+          launch_cols<float>(a.rspec, g.rSpecPitch, g.rSpecBatch, p.Rx->L / 2 + 1, g.rWinRows, g.rSubRows, p.Hr,
+                             p.hrPitch, *p.Ry, rscale, 1, nBatch, rs, tu.colCpb));
+    STAGE("region_down", rs, launch_region_down(p, a, nBatch, rs));
   }
-  {
-    const int M = p.Lx->half.n;
-    const int rpb = fast_rpb(M);
-    const size_t sm = sizeof(cplx<float>) * 3 * rpb * (M + 1);
-    ensure_smem(k_fast_stat_rows, sm);
-    dim3 grid((g.nDataRows + rpb - 1) / rpb, nBatch);
-    k_fast_stat_rows<<<grid, 256, sm, st>>>(a, g, plan32(*p.Lx, true),
-                                            reinterpret_cast<const cplx<float> *>(p.Lx->twL32), rpb, wantGrad ? 1 : 0);
-    e = cudaGetLastError();
+  STAGE("subsample", st, launch_subsample(a, main_win(g, a.spec), 0, nBatch, st));
+  STAGE("eval_r2c", st, launch_eval(a, main_win(g, a.spec), *p.Lx, nBatch, 0, tu, st));
+  STAGE("cols_conv", st,
+        launch_cols<float>(a.spec, g.specPitch, g.specBatch, p.Lx->L / 2 + 1, g.winRows, g.nDataRows, p.H, p.hPitch,
+                           *p.Ly, scale, 1, nBatch, st, tu.colCpb));
+  if (fork) {
+    cudaError_t e = cudaEventRecord(p.join0, rs);
+    if (!e) e = cudaStreamWaitEvent(st, p.join0, 0);
     if (e) return e;
-    mark(p, "stat_rows", st);
   }
+  STAGE("stat_rows", st, launch_stat(p, a, nBatch, wantGrad, st));
   if (!wantGrad) {
-    k_fast_reduce<<<nBatch, 256, 0, st>>>(a, 0, 0);
-    e = cudaGetLastError();
-    mark(p, "reduce", st);
-    return e;
+    STAGE("reduce", st, launch_reduce(a, nBatch, 0, 0, st));
+    return cudaSuccess;
   }
-  return fast_adjoint(p, a, nBatch, st);
+  if (fork) {
+    cudaError_t e = cudaEventRecord(p.fork1, st);
+    if (!e) e = cudaStreamWaitEvent(rs, p.fork1, 0);
+    if (e) return e;
+  }
+  if (g.hasRegion) {
+    STAGE("region_g_r2c", rs, launch_region_g(p, a, nBatch, rs));
+    STAGE("region_cols_adjoint", rs,
+          launch_cols<float>(a.rspec, g.rSpecPitch, g.rSpecBatch, p.Rx->L / 2 + 1, g.rSubRows, g.rWinRows, p.Hr,
+                             p.hrPitch, *p.Ry, rscale, 2, nBatch, rs, tu.colCpb));
+    STAGE("region_grad_rows", rs, launch_grad(a, region_win(g, a.rspec), *p.Rx, nBatch, nMain, 1, tu, rs));
+  }
+  STAGE("cols_adjoint", st,
+        launch_cols<float>(a.spec, g.specPitch, g.specBatch, p.Lx->L / 2 + 1, g.nDataRows, g.winRows, p.H, p.hPitch,
+                           *p.Ly, scale, 2, nBatch, st, tu.colCpb));
+  STAGE("grad_rows", st, launch_grad(a, main_win(g, a.spec), *p.Lx, nBatch, 0, 0, tu, st));
+  if (fork) {
+    cudaError_t e = cudaEventRecord(p.join1, rs);
+    if (!e) e = cudaStreamWaitEvent(st, p.join1, 0);
+    if (e) return e;
+  }
+  STAGE("reduce", st, launch_reduce(a, nBatch, nTot, 1, st));
+  return cudaSuccess;
 }
 
-cudaError_t fast_adjoint(const FastPlan &p, const FastArgs &a, int nBatch, cudaStream_t st) {
-  const FastGeom &g = p.g;
-  cudaError_t e;
-  const float scale = 1.f / ((float)p.Lx->L * (float)p.Ly->L);
-  e = launch_cols<float>(a.spec, g.specPitch, g.specBatch, p.Lx->L / 2 + 1, g.nDataRows, g.winRows, p.H, p.hPitch,
-                         *p.Ly, scale, 2, nBatch, st);
-  if (e) return e;
-  mark(p, "cols_adjoint", st);
-  const int nMain = fast_grad_blocks(g), nReg = fast_reg_grad_blocks(g);
-  const int nTot = nMain + nReg;
-  e = launch_grad(a, main_win(g, a.spec), *p.Lx, nBatch, nTot, 0, st);
-  if (e) return e;
-  mark(p, "grad_rows", st);
-  if (g.hasRegion) {
-    const int M = p.Rx->half.n;
-    const size_t sm = sizeof(cplx<float>) * 2 * (M + 1);
-    k_fast_region_g_r2c<<<dim3(g.rSubRows, nBatch), 256, sm, st>>>(
-        a, g, reinterpret_cast<cplx<float> *>(a.rspec), plan32(*p.Rx, true),
-        reinterpret_cast<const cplx<float> *>(p.Rx->twL32));
-    e = cudaGetLastError();
-    if (e) return e;
-    mark(p, "region_g_r2c", st);
-    const float rscale = 1.f / ((float)p.Rx->L * (float)p.Ry->L);
-    e = launch_cols<float>(a.rspec, g.rSpecPitch, g.rSpecBatch, p.Rx->L / 2 + 1, g.rSubRows, g.rWinRows, p.Hr,
-                           p.hrPitch, *p.Ry, rscale, 2, nBatch, st);
-    if (e) return e;
-    mark(p, "region_cols_adjoint", st);
-    e = launch_grad(a, region_win(g, a.rspec), *p.Rx, nBatch, nTot, nMain, st);
-    if (e) return e;
-    mark(p, "region_grad_rows", st);
-  }
-  k_fast_reduce<<<nBatch, 256, 0, st>>>(a, nTot, 1);
-  e = cudaGetLastError();
-  mark(p, "reduce", st);
-  return e;
+void fast_prepare_kernels() {
+  allow_max_smem((const void *)k_fast_eval_r2c);
+  allow_max_smem((const void *)k_fast_grad_rows);
+  allow_max_smem((const void *)k_fast_stat_rows);
+  allow_max_smem((const void *)k_fast_region_down);
+  allow_max_smem((const void *)k_fast_region_g_r2c);
 }
 
 }  // namespace imfit

@@ -19,7 +19,7 @@
 namespace imfit {
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_rows_r2c(const T *__restrict__ in, long inPitch, long inBatch,
+__global__ void __launch_bounds__(1024) k_rows_r2c(const T *__restrict__ in, long inPitch, long inBatch,
                                                   int inCols, int nRows, cplx<T> *__restrict__ out,
                                                   long outPitch, long outBatch, FFTPlan<T> plan,
                                                   const cplx<T> *__restrict__ twL, int rpb) {
@@ -52,7 +52,7 @@ __global__ void __launch_bounds__(256) k_rows_r2c(const T *__restrict__ in, long
 }
 
 template <typename T, int MODE>
-__global__ void __launch_bounds__(256) k_cols(cplx<T> *__restrict__ spec, long pitch, long batch, int nColsC,
+__global__ void __launch_bounds__(1024) k_cols(cplx<T> *__restrict__ spec, long pitch, long batch, int nColsC,
                                               int nRowsIn, int nRowsOut, const cplx<T> *__restrict__ H,
                                               long hPitch, FFTPlan<T> plan, T scale, int cpb) {
   extern __shared__ unsigned char smem_raw[];
@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(256) k_cols(cplx<T> *__restrict__ spec, long p
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_rows_c2r(const cplx<T> *__restrict__ in, long inPitch, long inBatch,
+__global__ void __launch_bounds__(1024) k_rows_c2r(const cplx<T> *__restrict__ in, long inPitch, long inBatch,
                                                   int nRows, T *__restrict__ out, long outPitch,
                                                   long outBatch, int outCols, T scale, FFTPlan<T> plan,
                                                   const cplx<T> *__restrict__ twL, int rpb) {
@@ -149,13 +149,21 @@ static const cplx<T> *twl_of(const FFTLen &L) {
   return reinterpret_cast<const cplx<T> *>(sizeof(T) == 8 ? (const void *)L.twL64 : (const void *)L.twL32);
 }
 
+// One line per CTA and about one thread per complex point: the FFT passes of a
+// line then have one butterfly per thread, and many small CTAs keep the SMs
+// occupied even for a single image.
 int rows_per_block(int M, int elemBytes, int nbuf) {
-  // keep shared memory per CTA at or below ~48 KB, 1..8 lines
-  int bytes = (M + 1) * elemBytes * 2 * nbuf;
-  int r = (48 * 1024) / (bytes > 0 ? bytes : 1);
-  if (r < 1) r = 1;
-  if (r > 8) r = 8;
-  return r;
+  (void)M;
+  (void)elemBytes;
+  (void)nbuf;
+  return 1;
+}
+
+int line_threads(int points) {
+  int t = (points + 31) / 32 * 32;
+  if (t < 64) t = 64;
+  if (t > 1024) t = 1024;
+  return t;
 }
 
 template <typename T>
@@ -165,41 +173,43 @@ cudaError_t launch_rows_r2c(const T *in, long inPitch, long inBatch, int inCols,
   const int rpb = rows_per_block(M, sizeof(T), 2);
   const size_t sm = sizeof(cplx<T>) * 2 * (size_t)rpb * (M + 1);
   auto kern = k_rows_r2c<T>;
-  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  allow_max_smem((const void *)kern);
   dim3 grid((nRows + rpb - 1) / rpb, nBatch);
-  kern<<<grid, 256, sm, st>>>(in, inPitch, inBatch, inCols, nRows, reinterpret_cast<cplx<T> *>(out), outPitch,
+  kern<<<grid, line_threads(M * rpb), sm, st>>>(in, inPitch, inBatch, inCols, nRows, reinterpret_cast<cplx<T> *>(out), outPitch,
                               outBatch, plan_of<T>(Lx, true), twl_of<T>(Lx), rpb);
   return cudaGetLastError();
 }
 
 int cols_per_block(int Ly, int elemBytes, int nColsC) {
-  // two ping-pong buffers of Ly x cpb complex; aim for >= 1 CTA per SM
-  int cpb = 8;
+  // two ping-pong buffers of Ly x cpb complex per CTA; one or two columns per
+  // CTA, two only when that still leaves several CTAs per SM
+  int cpb = (nColsC >= 600) ? 2 : 1;
   while (cpb > 1 && (size_t)2 * Ly * cpb * 2 * elemBytes > 200 * 1024) cpb >>= 1;
-  while (cpb > 1 && (nColsC + cpb - 1) / cpb < 152) cpb >>= 1;
   return cpb;
 }
 
 template <typename T>
 cudaError_t launch_cols(void *spec, long pitch, long batch, int nColsC, int nRowsIn, int nRowsOut,
                         const void *H, long hPitch, const FFTLen &Ly, T scale, int mode, int nBatch,
-                        cudaStream_t st) {
+                        cudaStream_t st, int cpbOverride) {
   const int L = Ly.full.n;
-  const int cpb = cols_per_block(L, sizeof(T), nColsC);
+  int cpb = cpbOverride > 0 ? cpbOverride : cols_per_block(L, sizeof(T), nColsC);
+  while (cpb > 1 && (size_t)2 * L * cpb * 2 * sizeof(T) > 200 * 1024) cpb >>= 1;
   const size_t sm = sizeof(cplx<T>) * 2 * (size_t)L * cpb;
   dim3 grid((nColsC + cpb - 1) / cpb, nBatch);
+  const int nt = line_threads(L * cpb / 2);
   auto p = plan_of<T>(Ly, false);
   cplx<T> *s = reinterpret_cast<cplx<T> *>(spec);
   const cplx<T> *h = reinterpret_cast<const cplx<T> *>(H);
   if (mode == 0) {
-    cudaFuncSetAttribute(k_cols<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_cols<T, 0><<<grid, 256, sm, st>>>(s, pitch, batch, nColsC, nRowsIn, nRowsOut, h, hPitch, p, scale, cpb);
+    allow_max_smem((const void *)k_cols<T, 0>);
+    k_cols<T, 0><<<grid, nt, sm, st>>>(s, pitch, batch, nColsC, nRowsIn, nRowsOut, h, hPitch, p, scale, cpb);
   } else if (mode == 1) {
-    cudaFuncSetAttribute(k_cols<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_cols<T, 1><<<grid, 256, sm, st>>>(s, pitch, batch, nColsC, nRowsIn, nRowsOut, h, hPitch, p, scale, cpb);
+    allow_max_smem((const void *)k_cols<T, 1>);
+    k_cols<T, 1><<<grid, nt, sm, st>>>(s, pitch, batch, nColsC, nRowsIn, nRowsOut, h, hPitch, p, scale, cpb);
   } else {
-    cudaFuncSetAttribute(k_cols<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_cols<T, 2><<<grid, 256, sm, st>>>(s, pitch, batch, nColsC, nRowsIn, nRowsOut, h, hPitch, p, scale, cpb);
+    allow_max_smem((const void *)k_cols<T, 2>);
+    k_cols<T, 2><<<grid, nt, sm, st>>>(s, pitch, batch, nColsC, nRowsIn, nRowsOut, h, hPitch, p, scale, cpb);
   }
   return cudaGetLastError();
 }
@@ -212,9 +222,9 @@ cudaError_t launch_rows_c2r(const void *in, long inPitch, long inBatch, int nRow
   const int rpb = rows_per_block(M, sizeof(T), 3);
   const size_t sm = sizeof(cplx<T>) * 3 * (size_t)rpb * (M + 1);
   auto kern = k_rows_c2r<T>;
-  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  allow_max_smem((const void *)kern);
   dim3 grid((nRows + rpb - 1) / rpb, nBatch);
-  kern<<<grid, 256, sm, st>>>(reinterpret_cast<const cplx<T> *>(in), inPitch, inBatch, nRows, out, outPitch,
+  kern<<<grid, line_threads(M * rpb), sm, st>>>(reinterpret_cast<const cplx<T> *>(in), inPitch, inBatch, nRows, out, outPitch,
                               outBatch, outCols, scale, plan_of<T>(Lx, true), twl_of<T>(Lx), rpb);
   return cudaGetLastError();
 }
@@ -224,9 +234,9 @@ template cudaError_t launch_rows_r2c<double>(const double *, long, long, int, in
 template cudaError_t launch_rows_r2c<float>(const float *, long, long, int, int, void *, long, long,
                                             const FFTLen &, int, cudaStream_t);
 template cudaError_t launch_cols<double>(void *, long, long, int, int, int, const void *, long,
-                                         const FFTLen &, double, int, int, cudaStream_t);
+                                         const FFTLen &, double, int, int, cudaStream_t, int);
 template cudaError_t launch_cols<float>(void *, long, long, int, int, int, const void *, long,
-                                        const FFTLen &, float, int, int, cudaStream_t);
+                                        const FFTLen &, float, int, int, cudaStream_t, int);
 template cudaError_t launch_rows_c2r<double>(const void *, long, long, int, double *, long, long, int,
                                              double, const FFTLen &, int, cudaStream_t);
 template cudaError_t launch_rows_c2r<float>(const void *, long, long, int, float *, long, long, int, float,
@@ -236,9 +246,39 @@ template cudaError_t launch_rows_c2r<float>(const void *, long, long, int, float
 
 // ------------------------------------------------------------ FFT tables
 #include <cmath>
+#include <mutex>
+#include <set>
+#include <utility>
 #include <vector>
 
 namespace imfit {
+
+void fft_prepare_kernels() {
+  allow_max_smem((const void *)k_rows_r2c<float>);
+  allow_max_smem((const void *)k_rows_r2c<double>);
+  allow_max_smem((const void *)k_rows_c2r<float>);
+  allow_max_smem((const void *)k_rows_c2r<double>);
+  allow_max_smem((const void *)k_cols<float, 0>);
+  allow_max_smem((const void *)k_cols<float, 1>);
+  allow_max_smem((const void *)k_cols<float, 2>);
+  allow_max_smem((const void *)k_cols<double, 0>);
+  allow_max_smem((const void *)k_cols<double, 1>);
+  allow_max_smem((const void *)k_cols<double, 2>);
+}
+
+void allow_max_smem(const void *kernel) {
+  static std::mutex lock;
+  static std::set<std::pair<int, const void *>> done;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return;
+  std::lock_guard<std::mutex> g(lock);
+  if (!done.insert({dev, kernel}).second) return;
+  int optin = 0;
+  if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return;
+  cudaFuncAttributes fa;
+  if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess) return;
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+}
 
 static bool is_smooth(int n) {
   for (int p : {2, 3, 5, 7})

@@ -7,6 +7,12 @@
 
 namespace imfit {
 
+// Raise a kernel's dynamic shared-memory limit to the device's opt-in maximum,
+// once per (device, kernel).  The limit is never lowered, so launches of one
+// kernel with different shared-memory sizes (possibly captured in one graph)
+// are all valid.
+void allow_max_smem(const void *kernel);
+
 // One FFT length with its radix schedule and device twiddle tables.
 struct FFTTable {
   int n = 0;
@@ -27,6 +33,8 @@ struct FFTLen {
   void *twL32 = nullptr;
 };
 
+// threads of a CTA that transforms lines totalling `points` complex values
+int line_threads(int points);
 // smallest 7-smooth (2,3,5,7) integer >= n, optionally even
 int smooth_size(int n, bool even);
 // radix schedule (8,4,2,3,5,7 preference); returns number of passes or -1
@@ -41,7 +49,7 @@ cudaError_t launch_rows_r2c(const T *in, long inPitch, long inBatch, int inCols,
 template <typename T>
 cudaError_t launch_cols(void *spec, long pitch, long batch, int nColsC, int nRowsIn, int nRowsOut,
                         const void *H, long hPitch, const FFTLen &Ly, T scale, int mode, int nBatch,
-                        cudaStream_t st);
+                        cudaStream_t st, int cpbOverride = 0);
 template <typename T>
 cudaError_t launch_rows_c2r(const void *in, long inPitch, long inBatch, int nRows, T *out, long outPitch,
                             long outBatch, int outCols, T scale, const FFTLen &Lx, int nBatch,
@@ -133,12 +141,22 @@ struct FastArgs {
   void *rspec;           // region half spectrum
   float *regModel;       // [B][rRows][rCols] downsampled region model
   float *regG;           // [B][rRows][rCols] dS/dM for region pixels
-  double *statPart;      // [B][nStatBlocks][2]   (S, sum g)
-  double *gradPart;      // [B][nGradBlocks][nParams]
+  // per-CTA partial sums (FP32 over one CTA's pixels); the final reduction
+  // over CTAs is FP64.  Layouts [B][quantity][partStride].
+  float *statPart;       // quantities: S, sum of g * sum(PSF)
+  float *gradPart;       // quantities: the nParams gradient entries
+  int partStride;        // >= number of CTAs of any launch shape
   int nStatBlocks, nGradBlocks, nRegGradBlocks;
   double *stat;          // [B]
   double *grad;          // [B][nParams]
   float *modelOut;       // optional: [B][N] model image (FP32) for inspection
+  // subsampled pixels, precomputed warp-per-pixel over the whole GPU: for each
+  // (batch, component, window) a square box of window pixels around the
+  // component centre holds [value, 7 derivatives] averaged over the pixel's
+  // subsamples (only pixels that subsample are written or read)
+  float *subTab;         // [B][nComp][2 windows][boxArea(w)][8]
+  int *subBox;           // [B][nComp][2][2]  box origin (col, row) in window coordinates
+  int boxMain, boxReg;   // box sides (pixels)
 };
 
 // Optional per-stage CUDA events: an event is recorded on the launch stream
@@ -148,10 +166,25 @@ struct StageTimer {
   cudaEvent_t ev[kMax];
   const char *names[kMax];
   int n = 0;
+  // when set, only this stage is bracketed (ev[0] before it, ev[1] after), so
+  // the timed graph carries two event nodes instead of one per kernel
+  const char *only = nullptr;
+};
+
+// Launch shape of the fast-path kernels (chosen by the autotuner).
+struct FastTune {
+  int rowRpb = 3;        // window rows per CTA (eval, statistic, gradient kernels)
+  int rowThreads = 256;  // threads per row CTA
+  int colCpb = 0;        // half-spectrum columns per CTA (0: automatic)
 };
 
 struct FastPlan {
+  FastTune tune;
   StageTimer *timer = nullptr;
+  // second stream for the oversampled-region pipeline (null: run serially)
+  // and the events that fork it from / join it back to the main stream
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork0 = nullptr, join0 = nullptr, fork1 = nullptr, join1 = nullptr;
   FastGeom g;
   const FFTLen *Lx, *Ly, *Rx, *Ry;  // main and region lengths
   const void *H, *Hr;               // FP32 PSF spectra (main, region)
@@ -160,9 +193,11 @@ struct FastPlan {
 
 cudaError_t fast_setup(const FastArgs &a, int nBatch, cudaStream_t st);
 cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool wantGrad, cudaStream_t st);
-cudaError_t fast_adjoint(const FastPlan &p, const FastArgs &a, int nBatch, cudaStream_t st);
-int fast_stat_blocks(const FastGeom &g);
-int fast_grad_blocks(const FastGeom &g);
-int fast_reg_grad_blocks(const FastGeom &g);
+// one-time kernel attribute set-up (call before any stream capture)
+void fast_prepare_kernels();
+void fft_prepare_kernels();
+int fast_stat_blocks(const FastGeom &g, const FastTune &t);
+int fast_grad_blocks(const FastGeom &g, const FastTune &t);
+int fast_reg_grad_blocks(const FastGeom &g, const FastTune &t);
 
 }  // namespace imfit

@@ -6,6 +6,7 @@
 // Weight / mask / extra-term preparation stays on the host in FP64 with the
 // reference's expressions (bit-identical by construction); the results are
 // uploaded once at FinalSetupForFitting.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -202,12 +203,22 @@ struct imfit_model_s {
   DevBuf<float> dSpec32, dRSpec32;  // complex
   DevBuf<CompDesc> dDesc;
   DevBuf<CompF32> dComps32;
-  DevBuf<double> dParams, dStatPart, dGradPart, dStat, dGrad;
+  DevBuf<float> dSubTab;
+  DevBuf<int> dSubBox;
+  DevBuf<double> dParams, dStat, dGrad;
+  DevBuf<float> dStatPart, dGradPart;
+  FastTune tune;
+  std::map<int, FastTune> tuned;  // per batch size
+  bool autotune = true;
   int fastCap = 0;
   bool useGraphs = true;
   Captured graph;
   StageTimer timer;
   bool timing = false;
+  std::string timingStage;           // empty: time every kernel (serially)
+  cudaStream_t side = nullptr;       // oversampled-region pipeline
+  cudaEvent_t forkEv[2] = {nullptr, nullptr}, joinEv[2] = {nullptr, nullptr};
+  bool concurrent = true;
 
   ~imfit_model_s() {
     for (Region *r : regions) {
@@ -225,6 +236,11 @@ struct imfit_model_s {
     if (timing)
       for (int i = 0; i < StageTimer::kMax; i++) cudaEventDestroy(timer.ev[i]);
     if (hPinned) cudaFreeHost(hPinned);
+    for (int i = 0; i < 2; i++) {
+      if (forkEv[i]) cudaEventDestroy(forkEv[i]);
+      if (joinEv[i]) cudaEventDestroy(joinEv[i]);
+    }
+    if (side) cudaStreamDestroy(side);
     if (stream) cudaStreamDestroy(stream);
   }
 
@@ -776,6 +792,7 @@ struct imfit_model_s {
     if (!e) e = cudaMemcpy(dDesc.p, desc.data(), sizeof(CompDesc) * desc.size(), cudaMemcpyHostToDevice);
     if (e) return cuda_fail(e, "fast setup upload");
     fastCap = 0;
+    tuned.clear();
     if (graph.exec) {
       cudaGraphExecDestroy(graph.exec);
       graph = Captured{};
@@ -816,8 +833,7 @@ struct imfit_model_s {
     if (B <= fastCap) return 0;
     const FastGeom &g = fg;
     const int nP = nParamsTot, nC = (int)funcs.size();
-    const int nStat = fast_stat_blocks(g);
-    const int nGrad = fast_grad_blocks(g) + fast_reg_grad_blocks(g);
+    const int stride = partStride();
     cudaError_t e = dParams.reserve((size_t)B * nP);
     if (!e) e = dComps32.reserve((size_t)B * nC);
     if (!e) e = dBg.reserve((size_t)B * 2);
@@ -825,10 +841,13 @@ struct imfit_model_s {
     if (!e && g.hasRegion) e = dRSpec32.reserve(2 * (size_t)B * g.rSpecBatch);
     if (!e && g.hasRegion) e = dRegModel.reserve((size_t)B * g.rRows * g.rCols);
     if (!e && g.hasRegion) e = dRegG.reserve((size_t)B * g.rRows * g.rCols);
-    if (!e) e = dStatPart.reserve((size_t)B * nStat * 2);
-    if (!e) e = dGradPart.reserve((size_t)B * nGrad * nP);
+    if (!e) e = dStatPart.reserve((size_t)B * 2 * stride);
+    if (!e) e = dGradPart.reserve((size_t)B * nP * stride);
     if (!e) e = dStat.reserve(B);
     if (!e) e = dGrad.reserve((size_t)B * nP);
+    const long area = (long)kBoxMain * kBoxMain + (long)boxReg() * boxReg();
+    if (!e) e = dSubTab.reserve((size_t)B * nC * area * 8);
+    if (!e) e = dSubBox.reserve((size_t)B * nC * 4);
     if (e) return cuda_fail(e, "fast batch buffers");
     fastCap = B;
     if (graph.exec) {
@@ -838,8 +857,17 @@ struct imfit_model_s {
     return 0;
   }
 
+  static constexpr int kBoxMain = 24;  // covers radius 10 around a centre, main grid
+  // CTA count of the finest launch shape (one row per CTA): bounds every shape
+  int partStride() const { return std::max(fg.nDataRows, fg.winRows + (fg.hasRegion ? fg.rWinRows : 0)); }
+  int boxReg() const { return fg.hasRegion ? 20 * fg.rScale + 5 : 0; }
+
   FastArgs fastArgs(const double *dP, double *dS, double *dG, float *modelOut) {
     FastArgs a{};
+    a.subTab = dSubTab.p;
+    a.subBox = dSubBox.p;
+    a.boxMain = kBoxMain;
+    a.boxReg = boxReg();
     a.desc = dDesc.p;
     a.nComp = (int)funcs.size();
     a.nParams = nParamsTot;
@@ -863,9 +891,10 @@ struct imfit_model_s {
     a.regG = dRegG.p;
     a.statPart = dStatPart.p;
     a.gradPart = dGradPart.p;
-    a.nStatBlocks = fast_stat_blocks(fg);
-    a.nGradBlocks = fast_grad_blocks(fg);
-    a.nRegGradBlocks = fast_reg_grad_blocks(fg);
+    a.partStride = partStride();
+    a.nStatBlocks = fast_stat_blocks(fg, tune);
+    a.nGradBlocks = fast_grad_blocks(fg, tune);
+    a.nRegGradBlocks = fast_reg_grad_blocks(fg, tune);
     a.stat = dS;
     a.grad = dG;
     a.modelOut = modelOut;
@@ -874,7 +903,17 @@ struct imfit_model_s {
 
   FastPlan fastPlan() {
     FastPlan p{};
+    p.tune = tune;
     p.timer = timing ? &timer : nullptr;
+    timer.only = timingStage.empty() ? nullptr : timingStage.c_str();
+    // per-kernel timing of every stage needs them in one stream order
+    if (concurrent && !(timing && timingStage.empty())) {
+      p.side = side;
+      p.fork0 = forkEv[0];
+      p.fork1 = forkEv[1];
+      p.join0 = joinEv[0];
+      p.join1 = joinEv[1];
+    }
     p.g = fg;
     p.Lx = &Fx;
     p.Ly = &Fy;
@@ -887,12 +926,81 @@ struct imfit_model_s {
     return p;
   }
 
+  // Autotuner: time a few launch shapes of the row and column kernels on the
+  // actual workload (the caller's parameter vectors) and keep the fastest.
+  // Row shapes are tried with the automatic column shape, then column shapes
+  // with the best row shape.  Runs outside any graph capture.
+  int autotuneFast(int B, const double *dP, double *dS, double *dG) {
+    auto it = tuned.find(B);
+    if (it != tuned.end()) {
+      tune = it->second;
+      return 0;
+    }
+    if (!autotune) {
+      tune = FastTune{};
+      tuned[B] = tune;
+      return 0;
+    }
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) || cudaEventCreate(&e1)) return fail(IMFIT_E_CUDA, "autotune events");
+    const bool timingWas = timing;
+    timing = false;
+    auto measure = [&](const FastTune &t, float &best) -> cudaError_t {
+      tune = t;
+      FastArgs a = fastArgs(dP, dS, dG ? dG : dGrad.p, nullptr);
+      FastPlan p = fastPlan();
+      cudaError_t e = fast_forward(p, a, B, dG != nullptr, stream);  // warm
+      if (e) return e;
+      e = cudaEventRecord(e0, stream);
+      for (int r = 0; r < 3 && !e; r++) e = fast_forward(p, a, B, dG != nullptr, stream);
+      if (!e) e = cudaEventRecord(e1, stream);
+      if (!e) e = cudaEventSynchronize(e1);
+      float ms = 0.f;
+      if (!e) e = cudaEventElapsedTime(&ms, e0, e1);
+      best = ms;
+      return e;
+    };
+    const int rowShapes[][2] = {{1, 128}, {1, 256}, {2, 256}, {3, 256}, {4, 256}, {2, 512}, {4, 512}};
+    FastTune bestT{};
+    float bestMs = 1e30f;
+    cudaError_t e = cudaSuccess;
+    for (auto &rs : rowShapes) {
+      FastTune t{};
+      t.rowRpb = rs[0];
+      t.rowThreads = rs[1];
+      float ms;
+      e = measure(t, ms);
+      if (e) break;
+      if (ms < bestMs) { bestMs = ms; bestT = t; }
+    }
+    for (int cpb : {1, 2, 4}) {
+      if (e) break;
+      FastTune t = bestT;
+      t.colCpb = cpb;
+      float ms;
+      e = measure(t, ms);
+      if (e) break;
+      if (ms < bestMs) { bestMs = ms; bestT = t; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    timing = timingWas;
+    if (e) return cuda_fail(e, "autotune");
+    tune = bestT;
+    tuned[B] = tune;
+    return 0;
+  }
+
   // enqueue the fast evaluation for nBatch vectors already on the device
   int enqueueFast(int B, const double *dP, double *dS, double *dG, float *modelOut = nullptr) {
     int st = prepareFast();
     if (st) return st;
     st = ensureFastCap(B);
     if (st) return st;
+    if (tuned.find(B) == tuned.end() || !(graph.exec && graph.nBatch == B)) {
+      st = autotuneFast(B, dP, dS, dG);
+      if (st) return st;
+    }
     const bool wantGrad = dG != nullptr;
     FastArgs a = fastArgs(dP, dS, dG ? dG : dGrad.p, modelOut);
     FastPlan p = fastPlan();
@@ -985,11 +1093,19 @@ int imfit_ModelObject_new(int device, imfit_model_t *out) {
   auto *m = new imfit_model_s();
   m->device = device;
   e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
+  if (!e) e = cudaStreamCreateWithFlags(&m->side, cudaStreamNonBlocking);
+  for (int i = 0; i < 2 && !e; i++) {
+    e = cudaEventCreateWithFlags(&m->forkEv[i], cudaEventDisableTiming);
+    if (!e) e = cudaEventCreateWithFlags(&m->joinEv[i], cudaEventDisableTiming);
+  }
   if (e) {
-    g_createError = std::string("cudaStreamCreate: ") + cudaGetErrorString(e);
+    g_createError = std::string("stream/event creation: ") + cudaGetErrorString(e);
     delete m;
     return IMFIT_E_CUDA;
   }
+  // kernel attributes are set once here, before any stream capture can begin
+  fast_prepare_kernels();
+  fft_prepare_kernels();
   *out = m;
   return 0;
 }
@@ -1360,6 +1476,45 @@ int imfit_SetKernelTiming(imfit_model_t m, int enable) {
   }
   m->timer.n = 0;
   m->timing = on;
+  if (m->graph.exec) {
+    cudaGraphExecDestroy(m->graph.exec);
+    m->graph = Captured{};
+  }
+  return 0;
+}
+
+int imfit_SetKernelTimingStage(imfit_model_t m, const char *stage) {
+  GET(m);
+  m->timingStage = stage ? stage : "";
+  if (m->graph.exec) {
+    cudaGraphExecDestroy(m->graph.exec);
+    m->graph = Captured{};
+  }
+  return 0;
+}
+
+int imfit_SetAutotune(imfit_model_t m, int enable) {
+  GET(m);
+  m->autotune = enable != 0;
+  m->tuned.clear();
+  if (m->graph.exec) {
+    cudaGraphExecDestroy(m->graph.exec);
+    m->graph = Captured{};
+  }
+  return 0;
+}
+
+int imfit_GetLaunchShape(imfit_model_t m, int *rowRpb, int *rowThreads, int *colCpb) {
+  GET(m);
+  if (rowRpb) *rowRpb = m->tune.rowRpb;
+  if (rowThreads) *rowThreads = m->tune.rowThreads;
+  if (colCpb) *colCpb = m->tune.colCpb;
+  return 0;
+}
+
+int imfit_SetConcurrentRegions(imfit_model_t m, int enable) {
+  GET(m);
+  m->concurrent = enable != 0;
   if (m->graph.exec) {
     cudaGraphExecDestroy(m->graph.exec);
     m->graph = Captured{};

@@ -182,6 +182,17 @@ int imfit_GetFastModelImageVector(imfit_model_t m, const double *params, double 
  * returns the number of kernels. */
 int imfit_SetKernelTiming(imfit_model_t m, int enable);
 int imfit_GetKernelTimes(imfit_model_t m, double *ms, char *names, int namesLen, int maxN);
+/* Restrict the timing to one named stage (two events around that kernel
+ * only), or pass NULL to time every stage (then the stages run serially). */
+int imfit_SetKernelTimingStage(imfit_model_t m, const char *stage);
+/* Run the oversampled-region pipeline on a second stream concurrently with
+ * the main-window pipeline (default on). */
+int imfit_SetConcurrentRegions(imfit_model_t m, int enable);
+/* Autotuning of the fast path's launch shapes (default on): the first fast
+ * call for each batch size times a few row/column CTA shapes on that call's
+ * parameters and keeps the fastest.  GetLaunchShape reports the choice. */
+int imfit_SetAutotune(imfit_model_t m, int enable);
+int imfit_GetLaunchShape(imfit_model_t m, int *rowsPerCta, int *rowThreads, int *colsPerCta);
 /* Page-locked host memory for the host-buffer entry points (cudaMallocHost). */
 int imfit_HostAlloc(unsigned long bytes, void **ptr);
 int imfit_HostFree(void *ptr);

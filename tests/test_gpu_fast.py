@@ -7,7 +7,9 @@ Tolerances:
   * gradient: against FP64 central finite differences of the oracle's
     statistic, with subsampling off (the subsample count switches make the
     model only piecewise smooth): |g - g_fd| <= 2e-3 * (|g_fd| + 1e-3 max|g_fd|);
-  * batched evaluation reproduces single-vector calls exactly.
+  * repeated calls are bit-identical; batched evaluation matches single-vector
+    calls to 2e-6 relative (the autotuner may pick different CTA shapes for
+    different batch sizes, which changes the FP32 per-CTA partial sums).
 """
 import numpy as np
 import pytest
@@ -116,10 +118,13 @@ def test_batch_equals_single_calls(gpu, oracle_mod):
     P = np.array([wl.start * (1 + 0.02 * rng.standard_normal(len(wl.start))) for _ in range(5)])
     P[:, 3] = np.clip(P[:, 3], 0.05, 0.8)
     S, G = g.batch_statistic_and_gradient(P)
+    S2, G2 = g.batch_statistic_and_gradient(P)
+    assert np.array_equal(S, S2) and np.array_equal(G, G2)
     for b in range(len(P)):
         s1, g1 = g.statistic_and_gradient(P[b])
-        assert s1 == S[b]
-        assert np.array_equal(g1, G[b])
+        assert relerr(s1, S[b]) < 2e-6
+        scale = np.abs(G[b]) + 1e-3 * np.max(np.abs(G[b]))
+        assert np.all(np.abs(g1 - G[b]) / scale < 1e-4)
 
 
 def test_graph_replay_equals_direct_launch(gpu, oracle_mod):
