@@ -68,7 +68,8 @@ def config_block(wl, extra=None):
     cfg = {"workload": f"{wl.name}: {wl.ncols}x{wl.nrows}, " + "+".join(f for f, _ in wl.functions)
            + (f", PSF {wl.psf.shape[1]}x{wl.psf.shape[0]}" if wl.psf is not None else "")
            + "".join(f", region {r[2]} x{r[1]} PSF {r[0].shape[0]}" for r in wl.regions)
-           + f", {wl.stat}", "n_params": wl.n_params, "batch_per_step": 1,
+           + f", {wl.stat}", "n_params": wl.n_params,
+           "batch_per_step": 1 if wl.batch is None else len(wl.batch),
            "l2": "flushed (256 MiB write) before every timed step"}
     if extra:
         cfg.update(extra)
@@ -225,6 +226,8 @@ def run_gpu(args, rank, local_rank, world):
     nP = wl.n_params
     stream = torch.cuda.ExternalStream(m.stream(), device=dev)
     p0 = np.array(wl.start, dtype=np.float64)
+    P = np.array(wl.batch if wl.batch is not None else [wl.start], dtype=np.float64)
+    B = P.shape[0]
 
     # accuracy against the FP64 path on the same inputs
     s64 = m.get_fit_statistic(p0)
@@ -234,14 +237,14 @@ def run_gpu(args, rank, local_rank, world):
     gscale = np.abs(g_fd) + 1e-3 * np.max(np.abs(g_fd))
     grad_rel_median = float(np.median(np.abs(g_fast - g_fd) / gscale))
 
-    d_params = torch.tensor(p0, dtype=torch.float64, device=dev)
-    d_stat = torch.zeros(1, dtype=torch.float64, device=dev)
-    d_grad = torch.zeros(nP, dtype=torch.float64, device=dev)
+    d_params = torch.tensor(P.ravel(), dtype=torch.float64, device=dev)
+    d_stat = torch.zeros(B, dtype=torch.float64, device=dev)
+    d_grad = torch.zeros(B * nP, dtype=torch.float64, device=dev)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MiB > 129 MB L2
     m.set_use_graphs(not args.no_graphs)
 
     def step():
-        m.batch_device(1, d_params.data_ptr(), d_stat.data_ptr(), d_grad.data_ptr())
+        m.batch_device(B, d_params.data_ptr(), d_stat.data_ptr(), d_grad.data_ptr())
 
     # calibration (not timed): every kernel bracketed by events, stages serial
     m.set_kernel_timing(True)
@@ -291,31 +294,33 @@ def run_gpu(args, rank, local_rank, world):
         t = torch.tensor([t_ms], dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         t_ms = float(t.item())
-    value = world * args.steps / (t_ms / 1e3)
+    value = world * B * args.steps / (t_ms / 1e3)
     m.set_kernel_timing(False)
 
     # end-to-end through the host C ABI, pinned buffers
     import ctypes
     lib = imfit_gb300.load_library()
     hp = ctypes.c_void_p()
-    lib.imfit_HostAlloc(8 * (2 * nP + 1), ctypes.byref(hp))
-    hbuf = np.ctypeslib.as_array((ctypes.c_double * (2 * nP + 1)).from_address(hp.value))
-    hbuf[:nP] = p0
-    pp = hbuf[:nP].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
-    ps = hbuf[nP:nP + 1].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
-    pg = hbuf[nP + 1:].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    nin, nout = B * nP, B + B * nP
+    lib.imfit_HostAlloc(8 * (nin + nout), ctypes.byref(hp))
+    hbuf = np.ctypeslib.as_array((ctypes.c_double * (nin + nout)).from_address(hp.value))
+    hbuf[:nin] = P.ravel()
+    DP = ctypes.POINTER(ctypes.c_double)
+    pp = hbuf[:nin].ctypes.data_as(DP)
+    ps = hbuf[nin:nin + B].ctypes.data_as(DP)
+    pg = hbuf[nin + B:].ctypes.data_as(DP)
     for _ in range(args.warmup):
-        lib.imfit_GetFitStatisticAndGradient(m.h, pp, ps, pg)
+        lib.imfit_BatchFitStatisticAndGradient(m.h, B, pp, ps, pg)
     e2e_t = 0.0
     for i in range(args.steps):
         with torch.cuda.stream(stream):
             flush.fill_(float(i))
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        st = lib.imfit_GetFitStatisticAndGradient(m.h, pp, ps, pg)
+        st = lib.imfit_BatchFitStatisticAndGradient(m.h, B, pp, ps, pg)
         e2e_t += time.perf_counter() - t0
         assert st == 0
-    e2e = world * args.steps / e2e_t
+    e2e = world * B * args.steps / e2e_t
     lib.imfit_HostFree(hp)
 
     # plain FP64 + finite-difference gradient (the drop-in), same GPU
@@ -343,13 +348,13 @@ def run_gpu(args, rank, local_rank, world):
     total = sum(cal.values())
     ab = algorithmic_bytes(m, wl)
     kernel_table = {k: {"ms": round(v, 5), "share": round(v / total, 4),
-                        "GBps": round(ab[k] / (v * 1e-3) / 1e9, 1) if k in ab and v > 0 else None}
+                        "GBps": round(B * ab[k] / (v * 1e-3) / 1e9, 1) if k in ab and v > 0 else None}
                     for k, v in sorted(cal.items(), key=lambda kv: -kv[1])}
     dom_avg = float(np.mean(dom_ms)) if dom_ms else cal[dom]
-    achieved = ab.get(dom, 0) / (dom_avg * 1e-3) / 1e9
+    achieved = B * ab.get(dom, 0) / (dom_avg * 1e-3) / 1e9
     roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
             "frac": round(achieved / hbm_peak, 4), "peak_source": peak_src,
-            "algorithmic_bytes_per_launch": ab.get(dom), "kernel_ms_in_timed_region": round(dom_avg, 5),
+            "algorithmic_bytes_per_launch": B * ab.get(dom, 0), "kernel_ms_in_timed_region": round(dom_avg, 5),
             "traffic": None}
 
     cpu = None
@@ -365,12 +370,12 @@ def run_gpu(args, rank, local_rank, world):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32 eval / f64 setup+reductions",
                 "data": "synthetic (seeded), model-generated with Poisson + read noise",
                 "config": config_block(wl, {"parallelism": f"replicas x{world}" if world > 1 else "single GPU"}),
-                "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 8 * nP, "d2h_bytes_per_step": 8 * (nP + 1)},
+                "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 8 * nin, "d2h_bytes_per_step": 8 * nout},
                 "plain_fp64_fd": {"value": plain * world, "unit": UNIT, "steps": args.plain_steps,
                                   "evals_per_step": nP + 1},
                 "speedup_vs_plain_fp64_fd": {"device": value / (plain * world), "e2e": e2e / (plain * world)},
                 "accuracy": {"stat_rel_err_vs_fp64": stat_rel, "grad_rel_err_median_vs_fd": grad_rel_median},
-                "roofline": roof, "kernels_serial_calibration": kernel_table, "gpu_launches": kernels_per_step * args.steps,
+                "roofline": roof, "launch_shape": m.launch_shape(), "kernels_serial_calibration": kernel_table, "gpu_launches": kernels_per_step * args.steps,
                 "clocks": clk, "cpu_baseline": cpu}
         print(json.dumps(line), flush=True)
 
