@@ -74,6 +74,10 @@ _SIGS = [
     ("imfit_GetFitStatisticFast", _I, [_P, _DP, _DP]),
     ("imfit_BatchFitStatisticAndGradient", _I, [_P, _I, _DP, _DP, _DP]),
     ("imfit_BatchFitStatisticAndGradientDevice", _I, [_P, _I, _P, _P, _P]),
+    ("imfit_GetJtWJ", _I, [_P, _DP, _DP, _DP, _DP]),
+    ("imfit_BatchJtWJDevice", _I, [_P, _I, _P, _P, _P, _P]),
+    ("imfit_FitLM", _I, [_P, _DP, ctypes.POINTER(_I), _DP, _DP, _D, _I, _DP, ctypes.POINTER(_I),
+                         ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     ("imfit_Synchronize", _I, [_P]),
     ("imfit_GetStream", _I, [_P, ctypes.POINTER(_P)]),
     ("imfit_SetUseGraphs", _I, [_P, _I]),
@@ -341,6 +345,35 @@ class ModelObject:
         """Device-pointer batch call (ints: raw device addresses); enqueues only."""
         return self._ck(self.lib.imfit_BatchFitStatisticAndGradientDevice(self.h, n_batch, d_params, d_stats,
                                                                           d_grads))
+
+    def jtwj(self, params):
+        """(statistic, J^T J, J^T dev) of the deviates by the forward-mode fast path."""
+        p = _f64(params)
+        n = self.n_params
+        s = _D()
+        a = np.empty((n, n))
+        b = np.empty(n)
+        self._ck(self.lib.imfit_GetJtWJ(self.h, _dp(p), ctypes.byref(s), _dp(a), _dp(b)))
+        return s.value, a, b
+
+    def batch_jtwj_device(self, n_batch, d_params, d_stats, d_jtj, d_jtdev):
+        """Device-pointer batched JtWJ (ints: raw device addresses); enqueues only."""
+        return self._ck(self.lib.imfit_BatchJtWJDevice(self.h, n_batch, d_params, d_stats, d_jtj, d_jtdev))
+
+    def fit_lm(self, params, fixed=None, lower=None, upper=None, ftol=1e-8, max_iter=0):
+        """Levenberg-Marquardt fit on the normal equations (FP64 host solve,
+        JtWJ from the GPU).  Returns a dict with the fitted parameters, the
+        fast-path statistic, iteration and evaluation counts and the status."""
+        p = _f64(params).copy()
+        n = p.size
+        fx = (_I * n)(*([0] * n if fixed is None else [int(v) for v in fixed]))
+        lo = _f64(lower) if lower is not None else None
+        hi = _f64(upper) if upper is not None else None
+        s, it, ne, st = _D(), _I(), _I(), _I()
+        self._ck(self.lib.imfit_FitLM(self.h, _dp(p), fx, _dp(lo) if lo is not None else None,
+                                      _dp(hi) if hi is not None else None, ftol, int(max_iter),
+                                      ctypes.byref(s), ctypes.byref(it), ctypes.byref(ne), ctypes.byref(st)))
+        return dict(params=p, statistic=s.value, niter=it.value, nev=ne.value, status=st.value)
 
     def synchronize(self):
         return self._ck(self.lib.imfit_Synchronize(self.h))

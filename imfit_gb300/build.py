@@ -24,6 +24,7 @@ UNITS = [
     ("k_fast.cu", []),
     ("model_object.cpp", ["-x", "cu"]),
     ("k_noalloc.cu", ["--fmad=false"]),
+    ("lm.cpp", []),
 ]
 
 

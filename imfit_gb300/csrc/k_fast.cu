@@ -21,6 +21,7 @@
 // plus N + 3P - 1 padding) is exactly the set of model pixels the data
 // crop depends on; constant backgrounds (FlatSky) are added after the
 // convolution as I_sky * sum(PSF), which is what convolving a constant gives.
+#include <algorithm>
 #include <cstring>
 
 #include "kernels.h"
@@ -258,8 +259,12 @@ __global__ void __launch_bounds__(1024) k_fast_eval_r2c(FastArgs a, WinDesc w, F
 }
 
 // ---------------------------------------- region: c2r + block average
+// (also used for the derivative images of the JtWJ pass: batch index b then
+// runs over (parameter vector, parameter) pairs, no background is added and
+// the output goes to a different buffer)
 __global__ void __launch_bounds__(1024) k_fast_region_down(FastArgs a, FastGeom g, const cplx<float> *__restrict__ rspec,
-                                                          FFTPlan<float> plan, const cplx<float> *__restrict__ twL) {
+                                                          FFTPlan<float> plan, const cplx<float> *__restrict__ twL,
+                                                          float *__restrict__ out, int addBackground) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int b = blockIdx.y, s = blockIdx.x;  // replaced data row within the region
   const int k = g.rScale;
@@ -280,7 +285,7 @@ __global__ void __launch_bounds__(1024) k_fast_region_down(FastArgs a, FastGeom 
   __syncthreads();
   cplx<float> *Z = block_fft(bufA, bufB, plan, k, ls, 1, +1, false);
   const float inv = 1.f / (float)(k * k);
-  const float bg = a.bgLevel[2 * b + 1];
+  const float bg = addBackground ? a.bgLevel[2 * b + 1] : 0.f;
   for (int t = threadIdx.x; t < g.rCols; t += blockDim.x) {
     float acc = 0.f;
     for (int u = 0; u < k; u++)
@@ -289,7 +294,7 @@ __global__ void __launch_bounds__(1024) k_fast_region_down(FastArgs a, FastGeom 
         const cplx<float> z = Z[u * ls + (col >> 1)];
         acc += (col & 1) ? z.y : z.x;
       }
-    a.regModel[((long)b * g.rRows + s) * g.rCols + t] = acc * inv + bg;
+    out[((long)b * g.rRows + s) * g.rCols + t] = acc * inv + bg;
   }
 }
 
@@ -614,6 +619,260 @@ __global__ void __launch_bounds__(256) k_fast_reduce(FastArgs a, int nGradBlocks
   }
 }
 
+// ------------------------------------ forward-mode derivative images (JtWJ)
+// One CTA per (window row, parameter vector): dm/dtheta_j of every
+// non-background parameter at every pixel of the row -- analytic, subsampled
+// pixels from the precomputed table -- accumulated into nD real lines in
+// shared memory (a pixel belongs to one thread, so no atomics), then the nD
+// row FFTs.  Derivative spectra of parameter vector b are the nD consecutive
+// entries b*nD .. b*nD+nD-1 of the spectrum batch.
+__global__ void __launch_bounds__(1024) k_fast_deriv_r2c(FastArgs a, WinDesc w, FFTPlan<float> plan,
+                                                        const cplx<float> *__restrict__ twL,
+                                                        const int *__restrict__ slot, int nD, int win) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int b = blockIdx.y, row = blockIdx.x;
+  const int M = plan.n, ls = M + 1;
+  CompF32 *sc = reinterpret_cast<CompF32 *>(smem);
+  int *boxes = reinterpret_cast<int *>(sc + kMaxComponents);
+  int *npar = boxes + 2 * kMaxComponents;
+  int *ss = npar + kMaxComponents;
+  cplx<float> *bufA = reinterpret_cast<cplx<float> *>(ss + kMaxParams);
+  cplx<float> *bufB = bufA + nD * ls;
+  const int nC = a.nComp;
+  for (int i = threadIdx.x; i < nC; i += blockDim.x) {
+    sc[i] = a.comps[b * nC + i];
+    const int *o = a.subBox + (((long)b * nC + i) * 2 + win) * 2;
+    boxes[2 * i] = o[0];
+    boxes[2 * i + 1] = o[1];
+    npar[i] = a.desc[i].nParams;
+  }
+  for (int i = threadIdx.x; i < a.nParams; i += blockDim.x) ss[i] = slot[i];
+  for (int i = threadIdx.x; i < nD * ls; i += blockDim.x) bufA[i] = {0.f, 0.f};
+  __syncthreads();
+  float *lines = reinterpret_cast<float *>(bufA);  // real line j: lines[2 * j * ls + col]
+  const int side = win ? a.boxReg : a.boxMain;
+  for (int col = threadIdx.x; col < w.cols; col += blockDim.x) {
+    for (int c = 0; c < nC; c++) {
+      const CompF32 &cc = sc[c];
+      if (cc.type == F_FLATSKY) continue;
+      float dx, dy;
+      win_offsets(w, cc, row, col, dx, dy);
+      const Geo g = geo32(cc, dx, dy);
+      float o[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      int np;
+      const int ns = sub_count(cc, g);
+      if (ns > 1) {
+        const int br = row - boxes[2 * c + 1], bc = col - boxes[2 * c];
+        if (br >= 0 && br < side && bc >= 0 && bc < side) {
+          const float *t = a.subTab + sub_base(a, b, c, win) + ((long)br * side + bc) * 8 + 1;
+#pragma unroll
+          for (int q = 0; q < 7; q++) o[q] = t[q];
+        } else {
+          // outside the precomputed box (not reached for radius < 10): direct average
+          const float d = 1.f / ns;
+          float t7[7];
+          for (int t = 0; t < ns * ns; t++) {
+            const Geo gs = geo32(cc, dx - 0.5f + (t / ns + 0.5f) * d, dy - 0.5f + (t % ns + 0.5f) * d);
+            const int n2 = radial_grad32(cc, gs, d * d, t7);
+#pragma unroll
+            for (int q = 0; q < 7; q++)
+              if (q < 2 + n2) o[q] += t7[q];
+          }
+        }
+        np = 5;  // unused slots are zero
+      } else {
+        np = radial_grad32(cc, g, 1.f, o);
+      }
+      np = min(np, npar[c]);
+      int s = ss[cc.x0Index];
+      if (s >= 0) lines[2 * s * ls + col] += o[0];
+      s = ss[cc.x0Index + 1];
+      if (s >= 0) lines[2 * s * ls + col] += o[1];
+#pragma unroll
+      for (int q = 0; q < 5; q++) {
+        if (q >= np) break;
+        s = ss[cc.paramOffset + q];
+        if (s >= 0) lines[2 * s * ls + col] += o[2 + q];
+      }
+    }
+  }
+  __syncthreads();
+  cplx<float> *Z = block_fft(bufA, bufB, plan, nD, ls, 1, -1, false);
+  cplx<float> *out = w.spec + (long)b * nD * w.specBatch + (long)row * w.specPitch;
+  for (int idx = threadIdx.x; idx < nD * (M + 1); idx += blockDim.x) {
+    const int j = idx / (M + 1), k = idx - j * (M + 1);
+    out[(long)j * w.specBatch + k] = r2c_post(Z + j * ls, k, M, twL);
+  }
+}
+
+// Deviate of pixel z at model value m and its slope q = d(deviate)/dM, so the
+// Levenberg-Marquardt Jacobian is J_zj = q_z dM_z/dtheta_j.
+//   chi^2, data/external errors: dev = w (d - M)               (model_object.cpp:1480-1490)
+//   chi^2, model errors:         dev = (d - M) / sqrt(V(M))    (model_object.cpp:1345-1381)
+//   Poisson-MLR:                 dev = sqrt(2 w |m' - d' ln m' + extra|)  (model_object.cpp:1386-1401)
+__device__ __forceinline__ void deviate_slope(const FastArgs &a, long z, float m, float &dev, float &q) {
+  const float w = a.weight[z];
+  dev = 0.f;
+  q = 0.f;
+  if (a.kind == 0) {
+    if (a.modelErrors) {
+      if (w <= 0.f) return;
+      const float V = (m + a.sky) / a.effGain + a.rnTerm;
+      const float iv = 1.f / sqrtf(V);
+      const float r = a.data[z] - m;
+      dev = r * iv;
+      q = -iv - 0.5f * r * iv / (V * a.effGain);
+    } else {
+      dev = w * (a.data[z] - m);
+      q = -w;
+    }
+    return;
+  }
+  if (w == 0.f) return;
+  const float mv = a.effGain * (m + a.sky), dv = a.effGain * (a.data[z] + a.sky);
+  const float ex = a.extra ? a.extra[z] : 0.f;
+  float T, dT;
+  if (mv > 0.f) {
+    T = (ex != 0.f && dv > 0.f) ? (mv - dv) - dv * log1pf((mv - dv) / dv) : mv - dv * logf(mv) + ex;
+    dT = a.effGain * (1.f - dv / mv);
+  } else {
+    T = mv - dv * 1.0e-25f + ex;
+    dT = a.effGain;
+  }
+  dev = sqrtf(2.f * w * fabsf(T));
+  q = (dev > 0.f) ? ((T < 0.f) ? -1.f : 1.f) * w * dT / dev : 0.f;
+}
+
+// One CTA per (data row, parameter vector): inverse row FFT of the nD
+// convolved derivative rows, the per-pixel Jacobian rows u_j = q dM/dtheta_j
+// (region pixels from the downsampled region derivatives, background
+// parameters from sum(PSF)), then the row's partial sums of
+//   alpha_jk = sum c u_j u_k (j <= k),  beta_j = sum c u_j dev,  S = sum c dev^2
+// (c = bootstrap multiplicity) in FP32, one partial per quantity per CTA.
+__global__ void __launch_bounds__(1024) k_fast_jtwj_rows(FastArgs a, FastGeom g, FFTPlan<float> plan,
+                                                        const cplx<float> *__restrict__ twL,
+                                                        const cplx<float> *__restrict__ dspec,
+                                                        const float *__restrict__ regDeriv,
+                                                        const int *__restrict__ slot, int nD,
+                                                        float *__restrict__ part) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int b = blockIdx.y, row = blockIdx.x;
+  const int M = plan.n, ls = M + 1, nP = a.nParams, nc = g.nDataCols;
+  int *ss = reinterpret_cast<int *>(smem);
+  cplx<float> *bufA = reinterpret_cast<cplx<float> *>(ss + kMaxParams);
+  cplx<float> *bufB = bufA + nD * ls;
+  float *U = reinterpret_cast<float *>(bufB + nD * ls);  // nD + 4 rows of nc floats
+  float *red = U + (long)(nD + 4) * nc;                  // blockDim.x floats
+  for (int i = threadIdx.x; i < nP; i += blockDim.x) ss[i] = slot[i];
+  const cplx<float> *src = dspec + (long)b * nD * g.specBatch + (long)row * g.specPitch;
+  for (int idx = threadIdx.x; idx < nD * M; idx += blockDim.x) {
+    const int j = idx / M, k = idx - j * M;
+    bufA[j * ls + k] = c2r_pre(src + (long)j * g.specBatch, k, M, twL);
+  }
+  __syncthreads();
+  const cplx<float> *Z = block_fft(bufA, bufB, plan, nD, ls, 1, +1, false);
+  const float *Zr = reinterpret_cast<const float *>(Z);
+  float *qb = U + (long)nD * nc, *cw = qb + nc, *cd = cw + nc, *dv = cd + nc;
+  const long nPix = (long)g.nDataRows * nc;
+  for (int col = threadIdx.x; col < nc; col += blockDim.x) {
+    const long zi = (long)row * nc + col;
+    const float m = a.modelOut[(long)b * nPix + zi];
+    float dev, q;
+    deviate_slope(a, zi, m, dev, q);
+    const float cnt = a.count ? a.count[zi] : 1.f;
+    bool inReg = false;
+    long ri = 0;
+    if (g.hasRegion) {
+      const int rr = row - g.ry0, rc = col - g.rx0;
+      if (rr >= 0 && rr < g.rRows && rc >= 0 && rc < g.rCols) {
+        inReg = true;
+        ri = (long)rr * g.rCols + rc;
+      }
+    }
+    const long rStride = (long)g.rRows * g.rCols;
+    for (int j = 0; j < nD; j++)
+      U[(long)j * nc + col] = q * (inReg ? regDeriv[((long)b * nD + j) * rStride + ri] : Zr[2 * j * ls + col]);
+    qb[col] = q * (inReg ? a.psfSumOs : a.psfSum);
+    cw[col] = cnt;
+    cd[col] = cnt * dev;
+    dv[col] = dev;
+  }
+  __syncthreads();
+  const int nPair = nP * (nP + 1) / 2, Q = nPair + nP + 1;
+  const int T = blockDim.x;
+  int nseg = T / Q;
+  nseg = nseg < 1 ? 1 : (nseg > 32 ? 32 : nseg);
+  const int perRound = T / nseg;
+  const int myQ = threadIdx.x / nseg, seg = threadIdx.x - myQ * nseg;
+  for (int q0 = 0; q0 < Q; q0 += perRound) {
+    const int qi = q0 + myQ;
+    float acc = 0.f;
+    if (myQ < perRound && qi < Q) {
+      const float *X, *Y, *C;
+      if (qi < nPair) {
+        int j = 0, r = qi;
+        while (r >= nP - j) {
+          r -= nP - j;
+          j++;
+        }
+        const int k = j + r;
+        X = ss[j] >= 0 ? U + (long)ss[j] * nc : qb;
+        Y = ss[k] >= 0 ? U + (long)ss[k] * nc : qb;
+        C = cw;
+      } else if (qi < nPair + nP) {
+        const int j = qi - nPair;
+        X = ss[j] >= 0 ? U + (long)ss[j] * nc : qb;
+        Y = cd;
+        C = nullptr;
+      } else {
+        X = cd;
+        Y = dv;
+        C = nullptr;
+      }
+      if (C) {
+        for (int col = seg; col < nc; col += nseg) acc += C[col] * X[col] * Y[col];
+      } else {
+        for (int col = seg; col < nc; col += nseg) acc += X[col] * Y[col];
+      }
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    if (threadIdx.x < perRound && q0 + threadIdx.x < Q) {
+      float t = 0.f;
+      for (int i = 0; i < nseg; i++) t += red[threadIdx.x * nseg + i];
+      part[((long)b * Q + q0 + threadIdx.x) * a.partStride + blockIdx.x] = t;
+    }
+    __syncthreads();
+  }
+}
+
+// FP64 sums of the per-row partials: grid (quantity, parameter vector).
+__global__ void __launch_bounds__(256) k_fast_jtwj_reduce(FastArgs a, const float *__restrict__ part, int nRows,
+                                                         double *__restrict__ alpha, double *__restrict__ beta,
+                                                         double *__restrict__ stat) {
+  const int qi = blockIdx.x, b = blockIdx.y, nP = a.nParams;
+  const int nPair = nP * (nP + 1) / 2, Q = nPair + nP + 1;
+  const float *p = part + ((long)b * Q + qi) * a.partStride;
+  double t = 0.0;
+  for (int i = threadIdx.x; i < nRows; i += blockDim.x) t += (double)p[i];
+  t = block_sum_d(t);
+  if (threadIdx.x != 0) return;
+  if (qi < nPair) {
+    int j = 0, r = qi;
+    while (r >= nP - j) {
+      r -= nP - j;
+      j++;
+    }
+    const int k = j + r;
+    alpha[((long)b * nP + j) * nP + k] = t;
+    alpha[((long)b * nP + k) * nP + j] = t;
+  } else if (qi < nPair + nP) {
+    beta[(long)b * nP + (qi - nPair)] = t;
+  } else {
+    stat[b] = t;
+  }
+}
+
 // ------------------------------------------------------------ launchers
 static FFTPlan<float> plan32(const FFTLen &L, bool half) {
   FFTPlan<float> p;
@@ -760,9 +1019,9 @@ static cudaError_t launch_region_down(const FastPlan &p, const FastArgs &a, int 
   const int M = p.Rx->half.n;
   const size_t sm = sizeof(cplx<float>) * 3 * g.rScale * (M + 1);
   ensure_smem(k_fast_region_down, sm);
-  k_fast_region_down<<<dim3(g.rRows, nBatch), line_threads(M * g.rScale / 2), sm, st>>>(a, g, reinterpret_cast<const cplx<float> *>(a.rspec),
-                                                             plan32(*p.Rx, true),
-                                                             reinterpret_cast<const cplx<float> *>(p.Rx->twL32));
+  k_fast_region_down<<<dim3(g.rRows, nBatch), line_threads(M * g.rScale / 2), sm, st>>>(
+      a, g, reinterpret_cast<const cplx<float> *>(a.rspec), plan32(*p.Rx, true),
+      reinterpret_cast<const cplx<float> *>(p.Rx->twL32), a.regModel, 1);
   return cudaGetLastError();
 }
 
@@ -863,12 +1122,92 @@ cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool 
   return cudaSuccess;
 }
 
+// ----------------------------------------------------- JtWJ (forward mode)
+static size_t deriv_smem(int M, int nD) {
+  return sizeof(CompF32) * kMaxComponents + sizeof(int) * (3 * kMaxComponents + kMaxParams) +
+         sizeof(cplx<float>) * 2 * (size_t)nD * (M + 1) + 16;
+}
+
+static size_t jtwj_rows_smem(int M, int nD, int nCols, int threads) {
+  return sizeof(int) * kMaxParams + sizeof(cplx<float>) * 2 * (size_t)nD * (M + 1) +
+         sizeof(float) * ((size_t)(nD + 4) * nCols + threads) + 16;
+}
+
+static constexpr int kJtwjThreads = 512;
+
+size_t fast_jtwj_smem(const FastPlan &p, int nD) {
+  size_t s = deriv_smem(p.Lx->half.n, nD);
+  s = std::max(s, jtwj_rows_smem(p.Lx->half.n, nD, p.g.nDataCols, kJtwjThreads));
+  if (p.g.hasRegion) s = std::max(s, deriv_smem(p.Rx->half.n, nD));
+  return s;
+}
+
+static cudaError_t launch_deriv(const FastArgs &a, const WinDesc &w, const FFTLen &L, int nBatch, int win,
+                                const JtwjArgs &J, cudaStream_t st) {
+  const int M = L.half.n;
+  const size_t sm = deriv_smem(M, J.nD);
+  k_fast_deriv_r2c<<<dim3(w.rows, nBatch), kJtwjThreads, sm, st>>>(
+      a, w, plan32(L, true), reinterpret_cast<const cplx<float> *>(L.twL32), J.slot, J.nD, win);
+  return cudaGetLastError();
+}
+
+// Statistic, JtJ and Jt dev of the deviates for nBatch parameter vectors:
+// the forward pass (which leaves the FP32 model image in a.modelOut), the
+// derivative images of every non-background parameter convolved with the PSF
+// (region derivatives through the oversampled pipeline and the block
+// average), then the per-row products and their FP64 sums.
+cudaError_t fast_jtwj(const FastPlan &p, const FastArgs &a, const JtwjArgs &J, int nBatch, cudaStream_t st) {
+  const FastGeom &g = p.g;
+  cudaError_t e = fast_forward(p, a, nBatch, false, st);
+  if (e) return e;
+  const int nD = J.nD, nB = nBatch * nD;
+  const FastTune &tu = p.tune;
+  if (nD > 0) {
+    if (g.hasRegion) {
+      const float rscale = 1.f / ((float)p.Rx->L * (float)p.Ry->L);
+      STAGE("jtwj_region_deriv_r2c", st, launch_deriv(a, region_win(g, J.drspec), *p.Rx, nBatch, 1, J, st));
+      STAGE("jtwj_region_cols", st,
+            launch_cols<float>(J.drspec, g.rSpecPitch, g.rSpecBatch, p.Rx->L / 2 + 1, g.rWinRows, g.rSubRows, p.Hr,
+                               p.hrPitch, *p.Ry, rscale, 1, nB, st, tu.colCpb));
+      const int M = p.Rx->half.n;
+      const size_t sm = sizeof(cplx<float>) * 3 * g.rScale * (M + 1);
+      stage_begin(p, "jtwj_region_down", st);
+      k_fast_region_down<<<dim3(g.rRows, nB), line_threads(M * g.rScale / 2), sm, st>>>(
+          a, g, reinterpret_cast<const cplx<float> *>(J.drspec), plan32(*p.Rx, true),
+          reinterpret_cast<const cplx<float> *>(p.Rx->twL32), J.regDeriv, 0);
+      if ((e = cudaGetLastError())) return e;
+      stage_end(p, "jtwj_region_down", st);
+    }
+    const float scale = 1.f / ((float)p.Lx->L * (float)p.Ly->L);
+    STAGE("jtwj_deriv_r2c", st, launch_deriv(a, main_win(g, J.dspec), *p.Lx, nBatch, 0, J, st));
+    STAGE("jtwj_cols", st,
+          launch_cols<float>(J.dspec, g.specPitch, g.specBatch, p.Lx->L / 2 + 1, g.winRows, g.nDataRows, p.H,
+                             p.hPitch, *p.Ly, scale, 1, nB, st, tu.colCpb));
+  }
+  const int M = p.Lx->half.n;
+  const size_t sm = jtwj_rows_smem(M, nD, g.nDataCols, kJtwjThreads);
+  stage_begin(p, "jtwj_rows", st);
+  k_fast_jtwj_rows<<<dim3(g.nDataRows, nBatch), kJtwjThreads, sm, st>>>(
+      a, g, plan32(*p.Lx, true), reinterpret_cast<const cplx<float> *>(p.Lx->twL32),
+      reinterpret_cast<const cplx<float> *>(J.dspec), J.regDeriv, J.slot, nD, J.part);
+  if ((e = cudaGetLastError())) return e;
+  stage_end(p, "jtwj_rows", st);
+  const int nP = a.nParams, Q = nP * (nP + 1) / 2 + nP + 1;
+  stage_begin(p, "jtwj_reduce", st);
+  k_fast_jtwj_reduce<<<dim3(Q, nBatch), 256, 0, st>>>(a, J.part, g.nDataRows, J.alpha, J.beta, J.stat);
+  if ((e = cudaGetLastError())) return e;
+  stage_end(p, "jtwj_reduce", st);
+  return cudaSuccess;
+}
+
 void fast_prepare_kernels() {
   allow_max_smem((const void *)k_fast_eval_r2c);
   allow_max_smem((const void *)k_fast_grad_rows);
   allow_max_smem((const void *)k_fast_stat_rows);
   allow_max_smem((const void *)k_fast_region_down);
   allow_max_smem((const void *)k_fast_region_g_r2c);
+  allow_max_smem((const void *)k_fast_deriv_r2c);
+  allow_max_smem((const void *)k_fast_jtwj_rows);
 }
 
 }  // namespace imfit

@@ -191,7 +191,23 @@ struct FastPlan {
   long hPitch, hrPitch;
 };
 
+// Forward-mode JtWJ buffers.  Parameters with slot[j] >= 0 get a derivative
+// image; background parameters (slot -1) have dM/dtheta = sum(PSF).
+struct JtwjArgs {
+  void *dspec;       // [B*nD] main derivative spectra (complex float, specBatch each)
+  void *drspec;      // [B*nD] region derivative spectra (rSpecBatch each)
+  float *regDeriv;   // [B*nD][rRows][rCols] downsampled region derivatives
+  const int *slot;   // [nParams]
+  int nD;
+  float *part;       // [B][Q][partStride] per-row partials, Q = nP(nP+1)/2 + nP + 1
+  double *alpha;     // [B][nP][nP]  J^T J
+  double *beta;      // [B][nP]      J^T dev
+  double *stat;      // [B]          sum dev^2 (the fit statistic)
+};
+
 cudaError_t fast_setup(const FastArgs &a, int nBatch, cudaStream_t st);
+cudaError_t fast_jtwj(const FastPlan &p, const FastArgs &a, const JtwjArgs &J, int nBatch, cudaStream_t st);
+size_t fast_jtwj_smem(const FastPlan &p, int nD);
 cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool wantGrad, cudaStream_t st);
 // one-time kernel attribute set-up (call before any stream capture)
 void fast_prepare_kernels();

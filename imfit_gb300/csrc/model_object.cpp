@@ -17,6 +17,7 @@
 
 #include "../../include/imfit_gb300.h"
 #include "kernels.h"
+#include "lm.h"
 
 namespace imfit {
 cudaError_t launch_update_weights64(const double *model, const double *mask, double *weight, long nData,
@@ -207,6 +208,12 @@ struct imfit_model_s {
   DevBuf<int> dSubBox;
   DevBuf<double> dParams, dStat, dGrad;
   DevBuf<float> dStatPart, dGradPart;
+  // forward-mode JtWJ state: derivative slot per parameter (-1: background)
+  std::vector<int> hSlot;
+  int nDeriv = 0, jtwjCap = 0;
+  DevBuf<int> dSlot;
+  DevBuf<float> dDSpec32, dDRSpec32, dRegDeriv, dJPart;
+  DevBuf<double> dAlpha, dBeta;
   FastTune tune;
   std::map<int, FastTune> tuned;  // per batch size
   bool autotune = true;
@@ -790,7 +797,17 @@ struct imfit_model_s {
     }
     if (!e) e = dDesc.reserve(desc.size());
     if (!e) e = cudaMemcpy(dDesc.p, desc.data(), sizeof(CompDesc) * desc.size(), cudaMemcpyHostToDevice);
+    // derivative images for every parameter except constant backgrounds
+    hSlot.assign(nParamsTot, 0);
+    for (auto &d : desc)
+      if (d.background) hSlot[d.paramOffset] = -1;
+    nDeriv = 0;
+    for (int j = 0; j < nParamsTot; j++)
+      if (hSlot[j] >= 0) hSlot[j] = nDeriv++;
+    if (!e) e = dSlot.reserve(std::max(nParamsTot, 1));
+    if (!e) e = cudaMemcpy(dSlot.p, hSlot.data(), sizeof(int) * nParamsTot, cudaMemcpyHostToDevice);
     if (e) return cuda_fail(e, "fast setup upload");
+    jtwjCap = 0;
     fastCap = 0;
     tuned.clear();
     if (graph.exec) {
@@ -1046,6 +1063,77 @@ struct imfit_model_s {
     if (!e && grads) e = cudaMemcpyAsync(grads, dGrad.p, sizeof(double) * (size_t)B * nP, cudaMemcpyDeviceToHost, stream);
     if (!e) e = cudaStreamSynchronize(stream);
     if (e) return cuda_fail(e, "fast results");
+    return 0;
+  }
+
+  // ------------------------------------------------- JtWJ (forward mode)
+  int ensureJtwjCap(int B) {
+    if (B <= jtwjCap) return 0;
+    const FastGeom &g = fg;
+    const int nP = nParamsTot, Q = nP * (nP + 1) / 2 + nP + 1;
+    cudaError_t e = dModelOut.reserve((size_t)B * nDataVals);
+    if (!e && nDeriv) e = dDSpec32.reserve(2 * (size_t)B * nDeriv * g.specBatch);
+    if (!e && nDeriv && g.hasRegion) e = dDRSpec32.reserve(2 * (size_t)B * nDeriv * g.rSpecBatch);
+    if (!e && nDeriv && g.hasRegion) e = dRegDeriv.reserve((size_t)B * nDeriv * g.rRows * g.rCols);
+    if (!e) e = dJPart.reserve((size_t)B * Q * partStride());
+    if (!e) e = dAlpha.reserve((size_t)B * nP * nP);
+    if (!e) e = dBeta.reserve((size_t)B * nP);
+    if (e) return cuda_fail(e, "JtWJ buffers");
+    jtwjCap = B;
+    return 0;
+  }
+
+  // statistic, J^T J and J^T dev for B parameter vectors on the device
+  int enqueueJtwj(int B, const double *dP, double *dS, double *dA, double *dBt) {
+    int st = prepareFast();
+    if (st) return st;
+    if (useCash && !pmlr)
+      return fail(IMFIT_E_UNSUPPORTED, "J^T J needs per-pixel deviates: chi^2 or Poisson-MLR, not the Cash statistic");
+    st = ensureFastCap(B);
+    if (!st) st = ensureJtwjCap(B);
+    if (st) return st;
+    if (!dP || !dS || !dA || !dBt) return fail(IMFIT_E_ARG, "JtWJ: null device buffer");
+    if (tuned.find(B) == tuned.end()) {
+      st = autotuneFast(B, dP, dS, nullptr);
+      if (st) return st;
+    }
+    FastArgs a = fastArgs(dP, dS, dGrad.p, dModelOut.p);
+    FastPlan p = fastPlan();
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    if (fast_jtwj_smem(p, nDeriv) > (size_t)optin)
+      return fail(IMFIT_E_UNSUPPORTED, "J^T J: too many parameters for this image width (shared memory)");
+    JtwjArgs J{};
+    J.dspec = dDSpec32.p;
+    J.drspec = dDRSpec32.p;
+    J.regDeriv = dRegDeriv.p;
+    J.slot = dSlot.p;
+    J.nD = nDeriv;
+    J.part = dJPart.p;
+    J.alpha = dA;
+    J.beta = dBt;
+    J.stat = dS;
+    cudaError_t e = fast_jtwj(p, a, J, B, stream);
+    if (e) return cuda_fail(e, "JtWJ launch");
+    return 0;
+  }
+
+  int jtwjHost(int B, const double *params, double *stats, double *alpha, double *beta) {
+    int st = prepareFast();
+    if (!st) st = ensureFastCap(B);
+    // the output buffers must exist before their addresses are taken below
+    if (!st) st = ensureJtwjCap(B);
+    if (st) return st;
+    const int nP = nParamsTot;
+    cudaError_t e = cudaMemcpyAsync(dParams.p, params, sizeof(double) * (size_t)B * nP, cudaMemcpyHostToDevice, stream);
+    if (e) return cuda_fail(e, "params upload");
+    st = enqueueJtwj(B, dParams.p, dStat.p, dAlpha.p, dBeta.p);
+    if (st) return st;
+    e = cudaMemcpyAsync(stats, dStat.p, sizeof(double) * B, cudaMemcpyDeviceToHost, stream);
+    if (!e && alpha) e = cudaMemcpyAsync(alpha, dAlpha.p, sizeof(double) * (size_t)B * nP * nP, cudaMemcpyDeviceToHost, stream);
+    if (!e && beta) e = cudaMemcpyAsync(beta, dBeta.p, sizeof(double) * (size_t)B * nP, cudaMemcpyDeviceToHost, stream);
+    if (!e) e = cudaStreamSynchronize(stream);
+    if (e) return cuda_fail(e, "JtWJ results");
     return 0;
   }
 
@@ -1442,6 +1530,40 @@ int imfit_BatchFitStatisticAndGradientDevice(imfit_model_t m, int B, const doubl
   GET(m);
   if (B < 1 || !dP || !dS) return m->fail(IMFIT_E_ARG, "bad batch arguments");
   return m->enqueueFast(B, dP, dS, dG);
+}
+
+int imfit_GetJtWJ(imfit_model_t m, const double *params, double *s, double *jtj, double *jtdev) {
+  GET(m);
+  if (!params || !s) return m->fail(IMFIT_E_ARG, "null argument");
+  return m->jtwjHost(1, params, s, jtj, jtdev);
+}
+
+int imfit_BatchJtWJDevice(imfit_model_t m, int B, const double *dP, double *dS, double *dA, double *dB) {
+  GET(m);
+  if (B < 1 || !dP || !dS || !dA || !dB) return m->fail(IMFIT_E_ARG, "bad batch arguments");
+  return m->enqueueJtwj(B, dP, dS, dA, dB);
+}
+
+int imfit_FitLM(imfit_model_t m, double *params, const int *fixed, const double *lower, const double *upper,
+                double ftol, int maxIter, double *stat, int *nIter, int *nEval, int *status) {
+  GET(m);
+  if (!params) return m->fail(IMFIT_E_ARG, "null argument");
+  if (!(ftol > 0.0)) return m->fail(IMFIT_E_ARG, "ftol must be positive");
+  LMSettings set;
+  set.ftol = ftol;
+  if (maxIter > 0) set.maxIter = maxIter;
+  const int n = m->nParamsTot;
+  LMResult res;
+  JtwjEval ev = [m, n](const double *x, double *S, double *A, double *b) {
+    (void)n;
+    return m->jtwjHost(1, x, S, A, b);
+  };
+  int st = lm_minimize(n, params, fixed, lower, upper, set, ev, res);
+  if (stat) *stat = res.stat;
+  if (nIter) *nIter = res.nIter;
+  if (nEval) *nEval = res.nEval;
+  if (status) *status = res.status;
+  return st < 0 ? st : 0;
 }
 
 int imfit_Synchronize(imfit_model_t m) {

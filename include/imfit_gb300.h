@@ -167,6 +167,30 @@ int imfit_BatchFitStatisticAndGradient(imfit_model_t m, int nBatch, const double
  * call returns once the work is enqueued.  imfit_Synchronize waits. */
 int imfit_BatchFitStatisticAndGradientDevice(imfit_model_t m, int nBatch, const double *d_params,
                                              double *d_statistics, double *d_gradients);
+/* Gauss-Newton normal equations of the deviates by the fast path, forward
+ * mode: the PSF-convolved derivative image of every parameter (one batched
+ * FFT convolution), then jtj = J^T J (nParams x nParams, row-major),
+ * jtdev = J^T dev and statistic = sum dev^2, with J = d dev / d params the
+ * analytic Jacobian mpfit approximates by finite differences
+ * (solvers/mpfit.cpp:1102-1356).  The gradient of the statistic is 2 jtdev.
+ * chi^2 (data, external or model-based errors) and Poisson-MLR; the Cash
+ * statistic has no deviates and returns IMFIT_E_UNSUPPORTED. */
+int imfit_GetJtWJ(imfit_model_t m, const double *params, double *statistic, double *jtj, double *jtdev);
+/* Batched form on DEVICE pointers (nBatch x nParams in, nBatch, nBatch x
+ * nParams^2 and nBatch x nParams out), enqueued on the handle's stream. */
+int imfit_BatchJtWJDevice(imfit_model_t m, int nBatch, const double *d_params, double *d_statistics,
+                          double *d_jtj, double *d_jtdev);
+/* Levenberg-Marquardt fit (FP64 normal-equation solve on the host, JtWJ from
+ * imfit_GetJtWJ).  params: start values in, fitted values out.  fixed (may be
+ * NULL): nonzero = held fixed.  lower/upper (may be NULL): limits, used where
+ * lower < upper.  ftol: relative-reduction tolerance (the reference's default
+ * is 1e-8, core/definitions.h:61); maxIter <= 0 selects 1000
+ * (solvers/levmar_fit.cpp:38).  Outputs (each may be NULL): the fast-path
+ * statistic at the result, iterations, JtWJ evaluations, and a status
+ * (1 ftol, 2 xtol, 3 no further reduction at FP32 precision, 5 iteration
+ * limit).  Returns 0 or a negative IMFIT_E_* code. */
+int imfit_FitLM(imfit_model_t m, double *params, const int *fixed, const double *lower, const double *upper,
+                double ftol, int maxIter, double *statistic, int *nIter, int *nEval, int *status);
 int imfit_Synchronize(imfit_model_t m);
 /* The CUDA stream (cudaStream_t) all work of this handle is enqueued on. */
 int imfit_GetStream(imfit_model_t m, void **stream);
