@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--plain-steps", type=int, default=20)
     ap.add_argument("--cpu-units", type=int, default=3, help="statistic+gradient units in the CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--config", default="C2", choices=["C1", "C2", "C4"])
+    ap.add_argument("--config", default="C2", choices=["C1", "C2", "C3", "C4"])
     ap.add_argument("--no-graphs", action="store_true", help="launch kernels one by one (for profilers)")
     return ap.parse_args()
 
@@ -61,7 +61,7 @@ def dist_info():
 
 def workload(name):
     from imfit_gb300 import workloads
-    return {"C1": workloads.c1, "C2": workloads.c2, "C4": workloads.c4}[name]()
+    return {"C1": workloads.c1, "C2": workloads.c2, "C3": workloads.c3, "C4": workloads.c4}[name]()
 
 
 def config_block(wl, extra=None):

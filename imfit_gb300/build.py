@@ -25,6 +25,7 @@ UNITS = [
     ("model_object.cpp", ["-x", "cu"]),
     ("k_noalloc.cu", ["--fmad=false"]),
     ("lm.cpp", []),
+    ("k_los.cu", ["--fmad=false"]),
 ]
 
 

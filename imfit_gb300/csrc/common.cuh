@@ -267,6 +267,10 @@ __host__ __device__ inline double comp_value64_2d(const CompF64 &c, double x, do
 //   Moffat:   s0=I_0 s1=1/alpha^2 s2=beta s3=alpha s4=fwhm s5=d(alpha)/d(beta)
 //   Gaussian: s0=I_0 s1=log2(e)/(2 sigma^2) s2=sigma
 //   FlatSky:  s0=I_sky
+//   ExpDisk3D:    s0=J_0 s1=1/h s2=h s3=cos(inc) s4=sin(inc) s5=alpha=2/n
+//                 s6=1/(alpha z_0) s7=z_0 subScale=n subInner=20h (half-range)
+//   FerrersBar3D: s0=J_0 s1=R_bar s2=q s3=cos(inc) s4=sin(inc) s5,s6=cos,sin(barPA+90)
+//                 s7=n subScale=1/a^2 subInner=1/b^2 subSmallK=1/c^2 pad=q_z q=half-range
 // The "E" factor below is the profile divided by its amplitude, so the
 // amplitude derivative is E itself and zero amplitudes need no special case.
 
@@ -371,6 +375,43 @@ __device__ inline void comp_setup32(CompF32 &o, const CompDesc &d, const double 
       o.s1 = (float)(kLog2e / (2.0 * p[3] * p[3]));
       o.s2 = (float)p[3];
       o.subScale = (float)p[3]; o.subInner = 3.f; o.subSmallK = 40.f;
+      break;
+    }
+    case F_EXPDISK3D: {  // PA, inc, J_0, h, n, z_0 (func_expdisk3d.cpp:149-171)
+      double si, ci;
+      sincospi(p[1] / 180.0, &si, &ci);
+      const double alpha = 2.0 / p[4];
+      o.s0 = (float)p[2];                     // J_0
+      o.s1 = (float)(1.0 / p[3]);             // 1/h
+      o.s2 = (float)p[3];                     // h
+      o.s3 = (float)ci;                       // cos(inc)
+      o.s4 = (float)si;                       // sin(inc)
+      o.s5 = (float)alpha;                    // 2/n
+      o.s6 = (float)(1.0 / (alpha * p[5]));   // 1/(alpha z_0)
+      o.s7 = (float)p[5];                     // z_0
+      o.subScale = (float)p[4];               // n
+      o.subInner = (float)(20.0 * p[3]);      // integration half-range 20 h
+      break;
+    }
+    case F_FERRERS3D: {  // PA, inc, barPA, J_0, R_bar, q, q_z, n (func_ferrersbar3d.cpp:125-165)
+      double si, ci, sb, cb;
+      sincospi(p[1] / 180.0, &si, &ci);
+      sincospi((p[2] + 90.0) / 180.0, &sb, &cb);
+      const double a2 = p[4] * p[4], b2 = p[5] * p[5] * a2, c2 = p[6] * p[6] * a2;
+      o.s0 = (float)p[3];                     // J_0
+      o.s1 = (float)p[4];                     // R_bar
+      o.s2 = (float)p[5];                     // q
+      o.s3 = (float)ci;
+      o.s4 = (float)si;
+      o.s5 = (float)cb;                       // cos(barPA + 90)
+      o.s6 = (float)sb;                       // sin(barPA + 90)
+      o.s7 = (float)p[7];                     // n
+      o.subScale = (float)(1.0 / a2);
+      o.subInner = (float)(1.0 / b2);
+      o.subSmallK = (float)(1.0 / c2);
+      o.pad = (float)p[6];                    // q_z
+      const double t = sqrt(b2) * si;
+      o.q = (float)(1.01 * ((t < p[4]) ? p[4] : t));  // integration half-range
       break;
     }
     default:

@@ -26,6 +26,7 @@
 
 #include "kernels.h"
 #include "fft.cuh"
+#include "los_fast.cuh"
 
 namespace imfit {
 
@@ -38,6 +39,9 @@ struct WinDesc {
   int specPitch;
   long specBatch;
   cplx<float> *spec;
+  // 3-D components: their summed line-of-sight values per window pixel
+  // (forward) and the adjoint r~ per window pixel (gradient); null without them
+  float *losVal, *losRt;
 };
 
 __device__ __forceinline__ int floordiv(int a, int b) {
@@ -236,7 +240,7 @@ __global__ void __launch_bounds__(1024) k_fast_eval_r2c(FastArgs a, WinDesc w, F
       if (col < w.cols) {
         for (int c = 0; c < nC; c++) {
           const CompF32 &cc = sc[c];
-          if (cc.type == F_FLATSKY) continue;
+          if (cc.type == F_FLATSKY || cc.type >= F_EXPDISK3D) continue;
           float dx, dy;
           win_offsets(w, cc, row, col, dx, dy);
           const Geo g = geo32(cc, dx, dy);
@@ -245,6 +249,7 @@ __global__ void __launch_bounds__(1024) k_fast_eval_r2c(FastArgs a, WinDesc w, F
           else
             v[e] += radial32(cc, g.r2);
         }
+        if (w.losVal) v[e] += w.losVal[((long)b * w.rows + row) * w.cols + col];
       }
     }
     bufA[l * ls + k] = {v[0], v[1]};
@@ -507,9 +512,14 @@ __global__ void __launch_bounds__(1024) k_fast_grad_rows(FastArgs a, WinDesc w, 
     const float *rt = reinterpret_cast<const float *>(Z);  // r~ of (l, col) at rt[2*(l*ls) + col]
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int npix = nl * w.cols;
+    if (w.losRt)
+      for (int idx = threadIdx.x; idx < npix; idx += blockDim.x) {
+        const int l = idx / w.cols, col = idx - l * w.cols;
+        w.losRt[((long)b * w.rows + row0 + l) * w.cols + col] = rt[2 * l * ls + col];
+      }
     for (int c = 0; c < nC; c++) {
       const CompF32 &cc = sc[c];
-      if (cc.type == F_FLATSKY) continue;
+      if (cc.type == F_FLATSKY || cc.type >= F_EXPDISK3D) continue;
       const int side = win ? a.boxReg : a.boxMain;
       const float *tab = a.subTab + sub_base(a, b, c, win);
       float acc[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
@@ -574,6 +584,83 @@ __global__ void __launch_bounds__(1024) k_fast_grad_rows(FastArgs a, WinDesc w, 
   __syncthreads();
   float *out = gradPart + (long)b * nP * a.partStride + blockBase + blockIdx.x;
   for (int i = threadIdx.x; i < nP; i += blockDim.x) out[(long)i * a.partStride] = gsm[i];
+}
+
+// ------------------------------------------------- 3-D line-of-sight terms
+// Rotated-frame coordinates of a window pixel for a component.
+__device__ __forceinline__ void los_pixel(const WinDesc &w, const CompF32 &cc, int row, int col, float &xp,
+                                          float &yp) {
+  float dx, dy;
+  win_offsets(w, cc, row, col, dx, dy);
+  xp = fmaf(dx, cc.cosPA, dy * cc.sinPA);
+  yp = fmaf(-dx, cc.sinPA, dy * cc.cosPA);
+}
+
+// One warp per window pixel (grid-stride): sum of the 3-D components' line of
+// sight integrals, written to w.losVal (added to the model row by eval_r2c).
+__global__ void __launch_bounds__(256) k_fast_los_eval(FastArgs a, WinDesc w) {
+  __shared__ CompF32 sc[kMaxComponents];
+  const int b = blockIdx.y;
+  const int nC = a.nComp;
+  for (int i = threadIdx.x; i < nC; i += blockDim.x) sc[i] = a.comps[b * nC + i];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const long npix = (long)w.rows * w.cols;
+  const long nWarps = (long)gridDim.x * (blockDim.x >> 5);
+  for (long p = blockIdx.x * (long)(blockDim.x >> 5) + (threadIdx.x >> 5); p < npix; p += nWarps) {
+    const int row = (int)(p / w.cols), col = (int)(p - (long)row * w.cols);
+    float v = 0.f;
+    for (int c = 0; c < nC; c++) {
+      const CompF32 &cc = sc[c];
+      if (cc.type < F_EXPDISK3D) continue;
+      float xp, yp;
+      los_pixel(w, cc, row, col, xp, yp);
+      v += los_value_warp(cc, xp, yp);
+    }
+    if (lane == 0) w.losVal[(long)b * npix + p] = v;
+  }
+}
+
+// One warp per window pixel: r~ * d(line-of-sight value)/d(parameters) of
+// every 3-D component, per-warp rows in shared memory (no atomics), then one
+// FP32 partial per parameter for this CTA.
+__global__ void __launch_bounds__(256) k_fast_los_grad(FastArgs a, WinDesc w, float *__restrict__ gradPart,
+                                                      int blockBase) {
+  __shared__ CompF32 sc[kMaxComponents];
+  __shared__ float red[8][kMaxParams];
+  const int b = blockIdx.y;
+  const int nC = a.nComp, nP = a.nParams;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < nC; i += blockDim.x) sc[i] = a.comps[b * nC + i];
+  for (int i = threadIdx.x; i < 8 * kMaxParams; i += blockDim.x) (&red[0][0])[i] = 0.f;
+  __syncthreads();
+  const long npix = (long)w.rows * w.cols;
+  const long nWarps = (long)gridDim.x * (blockDim.x >> 5);
+  for (long p = blockIdx.x * (long)(blockDim.x >> 5) + wid; p < npix; p += nWarps) {
+    const float r = w.losRt[(long)b * npix + p];
+    if (r == 0.f) continue;
+    const int row = (int)(p / w.cols), col = (int)(p - (long)row * w.cols);
+    for (int c = 0; c < nC; c++) {
+      const CompF32 &cc = sc[c];
+      if (cc.type < F_EXPDISK3D) continue;
+      float xp, yp, g[kLosGrad];
+      los_pixel(w, cc, row, col, xp, yp);
+      los_grad_warp(cc, xp, yp, g);
+      if (lane == 0) {
+        red[wid][cc.x0Index] += r * g[0];
+        red[wid][cc.x0Index + 1] += r * g[1];
+        const int npf = los_nparams(cc);
+        for (int q = 0; q < npf; q++) red[wid][cc.paramOffset + q] += r * g[2 + q];
+      }
+    }
+  }
+  __syncthreads();
+  const int nw = blockDim.x >> 5;
+  for (int j = threadIdx.x; j < nP; j += blockDim.x) {
+    float t = 0.f;
+    for (int i = 0; i < nw; i++) t += red[i][j];
+    gradPart[((long)b * nP + j) * a.partStride + blockBase + blockIdx.x] = t;
+  }
 }
 
 // ------------------------------------------------------------- reduce
@@ -654,7 +741,7 @@ __global__ void __launch_bounds__(1024) k_fast_deriv_r2c(FastArgs a, WinDesc w, 
   for (int col = threadIdx.x; col < w.cols; col += blockDim.x) {
     for (int c = 0; c < nC; c++) {
       const CompF32 &cc = sc[c];
-      if (cc.type == F_FLATSKY) continue;
+      if (cc.type == F_FLATSKY || cc.type >= F_EXPDISK3D) continue;
       float dx, dy;
       win_offsets(w, cc, row, col, dx, dy);
       const Geo g = geo32(cc, dx, dy);
@@ -1014,6 +1101,16 @@ static void stage_end(const FastPlan &p, const char *name, cudaStream_t st) {
     stage_end(p, name, stream);          \
   } while (0)
 
+static cudaError_t launch_los_eval(const FastArgs &a, const WinDesc &w, int nBatch, cudaStream_t st) {
+  k_fast_los_eval<<<dim3(kLosCtas, nBatch), 256, 0, st>>>(a, w);
+  return cudaGetLastError();
+}
+
+static cudaError_t launch_los_grad(const FastArgs &a, const WinDesc &w, int nBatch, int blockBase, cudaStream_t st) {
+  k_fast_los_grad<<<dim3(kLosCtas, nBatch), 256, 0, st>>>(a, w, a.gradPart, blockBase);
+  return cudaGetLastError();
+}
+
 static cudaError_t launch_region_down(const FastPlan &p, const FastArgs &a, int nBatch, cudaStream_t st) {
   const FastGeom &g = p.g;
   const int M = p.Rx->half.n;
@@ -1065,8 +1162,15 @@ cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool 
   const float scale = 1.f / ((float)p.Lx->L * (float)p.Ly->L);
   const float rscale = g.hasRegion ? 1.f / ((float)p.Rx->L * (float)p.Ry->L) : 0.f;
   const FastTune &tu = p.tune;
+  const bool los = a.losVal != nullptr;
   const int nMain = fast_grad_blocks(g, tu), nReg = fast_reg_grad_blocks(g, tu);
-  const int nTot = nMain + nReg;
+  const int nLos = los ? kLosCtas * (g.hasRegion ? 2 : 1) : 0;
+  const int nTot = nMain + nReg + nLos;
+  WinDesc mw = main_win(g, a.spec), rw = region_win(g, a.rspec);
+  mw.losVal = a.losVal;
+  mw.losRt = a.losRt;
+  rw.losVal = a.rLosVal;
+  rw.losRt = a.rLosRt;
 
   STAGE("setup", st, fast_setup(a, nBatch, st));
   if (fork) {
@@ -1075,15 +1179,17 @@ cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool 
     if (e) return e;
   }
   if (g.hasRegion) {
-    STAGE("region_subsample", rs, launch_subsample(a, region_win(g, a.rspec), 1, nBatch, rs));
-    STAGE("region_eval_r2c", rs, launch_eval(a, region_win(g, a.rspec), *p.Rx, nBatch, 1, tu, rs));
+    STAGE("region_subsample", rs, launch_subsample(a, rw, 1, nBatch, rs));
+    if (los) STAGE("region_los_eval", rs, launch_los_eval(a, rw, nBatch, rs));
+    STAGE("region_eval_r2c", rs, launch_eval(a, rw, *p.Rx, nBatch, 1, tu, rs));
     STAGE("region_cols_conv", rs,
           launch_cols<float>(a.rspec, g.rSpecPitch, g.rSpecBatch, p.Rx->L / 2 + 1, g.rWinRows, g.rSubRows, p.Hr,
                              p.hrPitch, *p.Ry, rscale, 1, nBatch, rs, tu.colCpb));
     STAGE("region_down", rs, launch_region_down(p, a, nBatch, rs));
   }
-  STAGE("subsample", st, launch_subsample(a, main_win(g, a.spec), 0, nBatch, st));
-  STAGE("eval_r2c", st, launch_eval(a, main_win(g, a.spec), *p.Lx, nBatch, 0, tu, st));
+  STAGE("subsample", st, launch_subsample(a, mw, 0, nBatch, st));
+  if (los) STAGE("los_eval", st, launch_los_eval(a, mw, nBatch, st));
+  STAGE("eval_r2c", st, launch_eval(a, mw, *p.Lx, nBatch, 0, tu, st));
   STAGE("cols_conv", st,
         launch_cols<float>(a.spec, g.specPitch, g.specBatch, p.Lx->L / 2 + 1, g.winRows, g.nDataRows, p.H, p.hPitch,
                            *p.Ly, scale, 1, nBatch, st, tu.colCpb));
@@ -1107,12 +1213,14 @@ cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool 
     STAGE("region_cols_adjoint", rs,
           launch_cols<float>(a.rspec, g.rSpecPitch, g.rSpecBatch, p.Rx->L / 2 + 1, g.rSubRows, g.rWinRows, p.Hr,
                              p.hrPitch, *p.Ry, rscale, 2, nBatch, rs, tu.colCpb));
-    STAGE("region_grad_rows", rs, launch_grad(a, region_win(g, a.rspec), *p.Rx, nBatch, nMain, 1, tu, rs));
+    STAGE("region_grad_rows", rs, launch_grad(a, rw, *p.Rx, nBatch, nMain, 1, tu, rs));
+    if (los) STAGE("region_los_grad", rs, launch_los_grad(a, rw, nBatch, nMain + nReg + kLosCtas, rs));
   }
   STAGE("cols_adjoint", st,
         launch_cols<float>(a.spec, g.specPitch, g.specBatch, p.Lx->L / 2 + 1, g.nDataRows, g.winRows, p.H, p.hPitch,
                            *p.Ly, scale, 2, nBatch, st, tu.colCpb));
-  STAGE("grad_rows", st, launch_grad(a, main_win(g, a.spec), *p.Lx, nBatch, 0, 0, tu, st));
+  STAGE("grad_rows", st, launch_grad(a, mw, *p.Lx, nBatch, 0, 0, tu, st));
+  if (los) STAGE("los_grad", st, launch_los_grad(a, mw, nBatch, nMain + nReg, st));
   if (fork) {
     cudaError_t e = cudaEventRecord(p.join1, rs);
     if (!e) e = cudaStreamWaitEvent(st, p.join1, 0);

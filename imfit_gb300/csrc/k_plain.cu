@@ -14,7 +14,8 @@ namespace imfit {
 // OversampledRegion::ComputeRegionAndDownsample core/oversampled_region.cpp:301-327
 // (region grid).  One thread per model pixel; Kahan sum over components.
 __global__ void __launch_bounds__(256) k_eval64(const CompF64 *__restrict__ comps, int nComp,
-                                                double *__restrict__ model, long pitch, Grid64 g) {
+                                                double *__restrict__ model, long pitch, Grid64 g,
+                                                const double *__restrict__ los) {
   __shared__ CompF64 sc[kMaxComponents];
   for (int i = threadIdx.x; i < nComp; i += blockDim.x) sc[i] = comps[i];
   __syncthreads();
@@ -32,7 +33,9 @@ __global__ void __launch_bounds__(256) k_eval64(const CompF64 *__restrict__ comp
   }
   double s = 0.0, err = 0.0;
   for (int c = 0; c < nComp; c++) {
-    const double v = comp_value64_2d(sc[c], x, y);
+    const int t = sc[c].type;
+    const double v = (t == F_EXPDISK3D || t == F_FERRERS3D) ? los[(long)sc[c].pad0 * n + k]
+                                                              : comp_value64_2d(sc[c], x, y);
     const double adj = v - err;
     const double tmp = s + adj;
     err = (tmp - s) - adj;
@@ -42,10 +45,10 @@ __global__ void __launch_bounds__(256) k_eval64(const CompF64 *__restrict__ comp
 }
 
 cudaError_t launch_eval64(const CompF64 *comps, int nComp, double *model, long pitch, Grid64 g,
-                          cudaStream_t st) {
+                          const double *los, cudaStream_t st) {
   const long n = (long)g.nCols * g.nRows;
   if (n == 0) return cudaSuccess;
-  k_eval64<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(comps, nComp, model, pitch, g);
+  k_eval64<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(comps, nComp, model, pitch, g, los);
   return cudaGetLastError();
 }
 

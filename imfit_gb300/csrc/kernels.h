@@ -67,8 +67,18 @@ struct Grid64 {
   double off, frac;
 };
 
+// 3-D (line-of-sight) components of a model: their indices in the component
+// list; component c's CompF64::pad0 holds its position k3 in this list.
+struct LosList64 {
+  int n;
+  int comp[kMaxComponents];
+};
+// los[k3 * (nCols*nRows) + pixel]: value of the k3-th 3-D component (FP64 QAGS per pixel)
+cudaError_t launch_los64(const CompF64 *comps, const LosList64 &list, double *los, Grid64 g, int *flag,
+                         cudaStream_t st);
+// model pixels; 3-D components are read from 'los' (may be null without them)
 cudaError_t launch_eval64(const CompF64 *comps, int nComp, double *model, long pitch, Grid64 g,
-                          cudaStream_t st);
+                          const double *los, cudaStream_t st);
 cudaError_t launch_downsample64(const double *region, int nOC, int nOR, int osPsfCols, int osPsfRows,
                                 double *mainImg, int nMainCols, int nMainRows, int mainPsfCols,
                                 int mainPsfRows, int x1, int y1, int scale, cudaStream_t st);
@@ -157,7 +167,15 @@ struct FastArgs {
   float *subTab;         // [B][nComp][2 windows][boxArea(w)][8]
   int *subBox;           // [B][nComp][2][2]  box origin (col, row) in window coordinates
   int boxMain, boxReg;   // box sides (pixels)
+  // 3-D (line-of-sight) components, when the model has any: per window
+  // pixel the summed line-of-sight values and the adjoint r~, main window and
+  // region window, [B][rows][cols] each (all null otherwise)
+  float *losVal, *losRt, *rLosVal, *rLosRt;
 };
+
+// CTAs per parameter vector of each line-of-sight kernel (grid-stride, one
+// warp per pixel); the gradient kernel writes one partial per CTA.
+constexpr int kLosCtas = 608;
 
 // Optional per-stage CUDA events: an event is recorded on the launch stream
 // after every kernel of the fast path (recorded into the graph when captured).

@@ -193,6 +193,11 @@ struct imfit_model_s {
   DevBuf<long> dBoot;
   DevBuf<CompF64> dComps;
   std::vector<CompF64> hComps;
+  // 3-D (line-of-sight) components: per-pixel values computed before the pixel sum
+  LosList64 losList{};
+  DevBuf<double> dLos;
+  DevBuf<int> dLosFlag;
+  int *hLosFlag = nullptr;  // pinned copy of the "list too short" flag
   double *hPinned = nullptr;  // pinned scratch for small transfers
   size_t hPinnedN = 0;
 
@@ -208,6 +213,9 @@ struct imfit_model_s {
   DevBuf<int> dSubBox;
   DevBuf<double> dParams, dStat, dGrad;
   DevBuf<float> dStatPart, dGradPart;
+  // 3-D components: per window pixel line-of-sight values and adjoint r~
+  bool hasLos = false;
+  DevBuf<float> dLosVal32, dLosRt32, dRLosVal32, dRLosRt32;
   // forward-mode JtWJ state: derivative slot per parameter (-1: background)
   std::vector<int> hSlot;
   int nDeriv = 0, jtwjCap = 0;
@@ -243,6 +251,7 @@ struct imfit_model_s {
     if (timing)
       for (int i = 0; i < StageTimer::kMax; i++) cudaEventDestroy(timer.ev[i]);
     if (hPinned) cudaFreeHost(hPinned);
+    if (hLosFlag) cudaFreeHost(hLosFlag);
     for (int i = 0; i < 2; i++) {
       if (forkEv[i]) cudaEventDestroy(forkEv[i]);
       if (joinEv[i]) cudaEventDestroy(joinEv[i]);
@@ -527,21 +536,49 @@ struct imfit_model_s {
   int checkEval() {
     if (!setsDefined) return fail(IMFIT_E_STATE, "DefineFunctionSets not called");
     if (!modelSetupDone) return fail(IMFIT_E_STATE, "SetupModelImage not called");
-    for (auto &f : funcs)
-      if (f.type == F_EXPDISK3D || f.type == F_FERRERS3D)
-        return fail(IMFIT_E_UNSUPPORTED, "3-D line-of-sight functions are not available on the plain path");
     return 0;
   }
 
   void setupComps(const double *params, CompF64 *out) {
     double x0 = 0.0, y0 = 0.0;
+    int k3 = 0;
     for (size_t f = 0; f < funcs.size(); f++) {
       if (setStart[f]) {
         x0 = params[x0Index[f]];
         y0 = params[x0Index[f] + 1];
       }
       comp_setup64(out[f], funcs[f].type, funcs[f].subsample, params + paramOffset[f], x0, y0);
+      if (funcs[f].type == F_EXPDISK3D || funcs[f].type == F_FERRERS3D) out[f].pad0 = k3++;
     }
+  }
+
+  // the 3-D components of the model, in component order
+  void buildLosList() {
+    losList.n = 0;
+    for (size_t f = 0; f < funcs.size(); f++)
+      if (funcs[f].type == F_EXPDISK3D || funcs[f].type == F_FERRERS3D) losList.comp[losList.n++] = (int)f;
+  }
+
+  // line-of-sight values of the 3-D components on one model grid, then the pixel sum
+  cudaError_t evalGrid(const CompF64 *dC, double *model, long pitch, const Grid64 &g) {
+    const int nC = (int)funcs.size();
+    if (losList.n == 0) return launch_eval64(dC, nC, model, pitch, g, nullptr, stream);
+    const size_t need = (size_t)losList.n * g.nCols * g.nRows;
+    cudaError_t e = dLos.reserve(need);
+    if (!e) e = launch_los64(dC, losList, dLos.p, g, dLosFlag.p, stream);
+    if (!e) e = launch_eval64(dC, nC, model, pitch, g, dLos.p, stream);
+    return e;
+  }
+
+  // after a synchronize: did a line-of-sight integral run out of subintervals?
+  int losCheck() {
+    if (losList.n && hLosFlag && *hLosFlag) {
+      *hLosFlag = 0;
+      cudaMemset(dLosFlag.p, 0, sizeof(int));
+      return fail(IMFIT_E_UNSUPPORTED, "a line-of-sight integral needed more subintervals than the device "
+                                       "QAGS list holds (64)");
+    }
+    return 0;
   }
 
   cudaError_t conv64(double *img, int nCols, int nRows, const FFTLen &fx, const FFTLen &fy, const double *H,
@@ -555,13 +592,22 @@ struct imfit_model_s {
 
   // CreateModelImage (core/model_object.cpp:1103-1229) with comps already on the device
   cudaError_t enqueueModel(const CompF64 *dC) {
-    const int nC = (int)funcs.size();
+    buildLosList();
+    cudaError_t e = cudaSuccess;
+    if (losList.n && !hLosFlag) {
+      // the flag accumulates over evaluations until losCheck() reads and clears it
+      e = cudaMallocHost(&hLosFlag, sizeof(int));
+      if (!e) e = dLosFlag.reserve(1);
+      if (!e) e = cudaMemsetAsync(dLosFlag.p, 0, sizeof(int), stream);
+      if (e) return e;
+      *hLosFlag = 0;
+    }
     Grid64 g{};
     g.nCols = nModelCols;
     g.nRows = nModelRows;
     g.pc = doConv ? nPsfCols : 0;
     g.pr = doConv ? nPsfRows : 0;
-    cudaError_t e = launch_eval64(dC, nC, dModel.p, nModelCols, g, stream);
+    e = evalGrid(dC, dModel.p, nModelCols, g);
     if (!e && doConv) e = conv64(dModel.p, nModelCols, nModelRows, Lx, Ly, dH.p, dSpec.p);
     for (Region *r : regions) {
       if (e) break;
@@ -575,13 +621,14 @@ struct imfit_model_s {
       rg.y1 = r->y1;
       rg.frac = 1.0 / r->scale;
       rg.off = 0.5 * rg.frac - 0.5;
-      e = launch_eval64(dC, nC, r->model.p, r->nModelCols, rg, stream);
+      e = evalGrid(dC, r->model.p, r->nModelCols, rg);
       if (!e) e = conv64(r->model.p, r->nModelCols, r->nModelRows, r->Lx, r->Ly, r->H.p, r->spec.p);
       if (!e)
         e = launch_downsample64(r->model.p, r->nModelCols, r->nModelRows, r->nPsfCols, r->nPsfRows, dModel.p,
                                 nModelCols, nModelRows, doConv ? nPsfCols : 0, doConv ? nPsfRows : 0, r->x1, r->y1,
                                 r->scale, stream);
     }
+    if (!e && losList.n) e = cudaMemcpyAsync(hLosFlag, dLosFlag.p, sizeof(int), cudaMemcpyDeviceToHost, stream);
     if (!e && modelErrors && finalSetupDone)
       e = launch_update_weights64(dModel.p, dMask.p, dWeight.p, nDataVals, nDataCols, nModelCols,
                                   doConv ? nPsfRows : 0, doConv ? nPsfCols : 0, effGain, sky, nCombined * rnAduSq,
@@ -600,6 +647,8 @@ struct imfit_model_s {
     if (!e) e = enqueueModel(dComps.p);
     if (!e) e = cudaStreamSynchronize(stream);  // hComps is pageable and reused
     if (e) return cuda_fail(e, "CreateModelImage");
+    st = losCheck();
+    if (st) return st;
     modelComputed = true;
     return 0;
   }
@@ -694,6 +743,8 @@ struct imfit_model_s {
     if (!e) e = cudaMemcpyAsync(hb, dRes.p, sizeof(double) * (nP + 1), cudaMemcpyDeviceToHost, stream);
     if (!e) e = cudaStreamSynchronize(stream);
     if (e) return cuda_fail(e, "FD gradient");
+    st = losCheck();
+    if (st) return st;
     *stat = hb[0];
     for (int j = 0; j < nP; j++) grad[j] = chi ? hb[1 + j] : (hb[1 + j] - hb[0]) / h[j];
     modelComputed = true;
@@ -705,9 +756,9 @@ struct imfit_model_s {
     if (fastReady) return 0;
     if (!finalSetupDone) return fail(IMFIT_E_STATE, "FinalSetupForFitting not called");
     if (!setsDefined) return fail(IMFIT_E_STATE, "DefineFunctionSets not called");
+    hasLos = false;
     for (auto &f : funcs)
-      if (f.type == F_EXPDISK3D || f.type == F_FERRERS3D)
-        return fail(IMFIT_E_UNSUPPORTED, "3-D line-of-sight functions are not available on the fast path");
+      if (f.type == F_EXPDISK3D || f.type == F_FERRERS3D) hasLos = true;
     if (regions.size() > 1) return fail(IMFIT_E_UNSUPPORTED, "fast path supports at most one oversampled region");
     if ((int)funcs.size() > kMaxComponents) return fail(IMFIT_E_UNSUPPORTED, "too many components");
     const int pc = doConv ? nPsfCols : 1, pr = doConv ? nPsfRows : 1;
@@ -865,6 +916,13 @@ struct imfit_model_s {
     const long area = (long)kBoxMain * kBoxMain + (long)boxReg() * boxReg();
     if (!e) e = dSubTab.reserve((size_t)B * nC * area * 8);
     if (!e) e = dSubBox.reserve((size_t)B * nC * 4);
+    if (!e && hasLos) {
+      const size_t mw = (size_t)B * g.winRows * g.winCols, rw = (size_t)B * g.rWinRows * g.rWinCols;
+      e = dLosVal32.reserve(mw);
+      if (!e) e = dLosRt32.reserve(mw);
+      if (!e && g.hasRegion) e = dRLosVal32.reserve(rw);
+      if (!e && g.hasRegion) e = dRLosRt32.reserve(rw);
+    }
     if (e) return cuda_fail(e, "fast batch buffers");
     fastCap = B;
     if (graph.exec) {
@@ -876,7 +934,10 @@ struct imfit_model_s {
 
   static constexpr int kBoxMain = 24;  // covers radius 10 around a centre, main grid
   // CTA count of the finest launch shape (one row per CTA): bounds every shape
-  int partStride() const { return std::max(fg.nDataRows, fg.winRows + (fg.hasRegion ? fg.rWinRows : 0)); }
+  int partStride() const {
+    const int los = hasLos ? kLosCtas * (fg.hasRegion ? 2 : 1) : 0;
+    return std::max(fg.nDataRows, fg.winRows + (fg.hasRegion ? fg.rWinRows : 0) + los);
+  }
   int boxReg() const { return fg.hasRegion ? 20 * fg.rScale + 5 : 0; }
 
   FastArgs fastArgs(const double *dP, double *dS, double *dG, float *modelOut) {
@@ -915,6 +976,12 @@ struct imfit_model_s {
     a.stat = dS;
     a.grad = dG;
     a.modelOut = modelOut;
+    if (hasLos) {
+      a.losVal = dLosVal32.p;
+      a.losRt = dLosRt32.p;
+      a.rLosVal = fg.hasRegion ? dRLosVal32.p : nullptr;
+      a.rLosRt = fg.hasRegion ? dRLosRt32.p : nullptr;
+    }
     return a;
   }
 
@@ -1089,6 +1156,9 @@ struct imfit_model_s {
     if (st) return st;
     if (useCash && !pmlr)
       return fail(IMFIT_E_UNSUPPORTED, "J^T J needs per-pixel deviates: chi^2 or Poisson-MLR, not the Cash statistic");
+    if (hasLos)
+      return fail(IMFIT_E_UNSUPPORTED, "J^T J of 3-D line-of-sight components is not available; use the adjoint "
+                                       "gradient (imfit_GetFitStatisticAndGradient)");
     st = ensureFastCap(B);
     if (!st) st = ensureJtwjCap(B);
     if (st) return st;

@@ -12,6 +12,10 @@ any implementation that offers the ModelObject-shaped interface (the GPU
   C2  1024x1024 Sersic + Exponential + FlatSky, 63x63 Moffat (fwhm 4.5, beta 3.5),
       central 40x40 region oversampled 5x with a 315x315 Moffat, 10% random mask,
       Poisson noise, chi^2, 12 parameters.
+  C3  512x512 edge-on ExponentialDisk3D (h 40, n 1, z_0 6, inc U[80,90]) +
+      FerrersBar3D (R_bar 30, q 0.4, q_z 0.2667, n 2, random bar PA), 35x35
+      Gaussian PSF (sigma 1.5), Gaussian noise sigma 5 given as an error image,
+      chi^2, 16 parameters.
   C4  512x512 Poisson counts, Sersic + Exponential + GaussianRing (R 60, sigma 8)
       + FlatSky, 51x51 Moffat, Cash statistic, 256 parameter vectors drawn
       within +-30% boxes around the truth (positions +-3 px), 17 parameters.
@@ -135,7 +139,9 @@ def _perturb(rng, truth, names, frac=0.1, pos=1.0):
 def param_names(functions):
     table = {"Sersic": ["PA", "ell", "n", "I_e", "r_e"], "Exponential": ["PA", "ell", "I_0", "h"],
              "FlatSky": ["I_sky"], "GaussianRing": ["PA", "ell", "A", "R_ring", "sigma_r"],
-             "Moffat": ["PA", "ell", "I_0", "fwhm", "beta"], "Gaussian": ["PA", "ell", "I_0", "sigma"]}
+             "Moffat": ["PA", "ell", "I_0", "fwhm", "beta"], "Gaussian": ["PA", "ell", "I_0", "sigma"],
+             "ExponentialDisk3D": ["PA", "inc", "J_0", "h", "n", "z_0"],
+             "FerrersBar3D": ["PA", "inc", "barPA", "J_0", "R_bar", "q", "q_z", "n"]}
     out = []
     for i, (name, new_set) in enumerate(functions):
         if new_set or i == 0:
@@ -174,6 +180,33 @@ def c2(size=1024, psf_size=63, region=40, scale=5, os_psf_size=315, seed=1002):
                   gain=4.0, read_noise=5.0, seed=seed)
     wl.mask = (rng.random((size, size)) < 0.10).astype(np.float64)
     wl.start = _perturb(rng, truth, param_names(wl.functions))
+    return wl
+
+
+def c3(size=512, psf_size=35, seed=1003):
+    rng = np.random.default_rng(seed)
+    s = size / 512.0
+    c = size / 2 + 0.5
+    pa = rng.uniform(0, 180)
+    inc = rng.uniform(80, 90)
+    truth = np.array([c + rng.uniform(-0.5, 0.5), c + rng.uniform(-0.5, 0.5),
+                      pa, inc, 0.5, 40.0 * s, 1.0, 6.0 * s,
+                      pa, inc, rng.uniform(0, 180), 0.2, 30.0 * s, 0.4, 0.2667, 2.0])
+    wl = Workload("C3", size, size, [("ExponentialDisk3D", True), ("FerrersBar3D", False)], truth,
+                  psf=gaussian_psf(psf_size, 1.5), seed=seed, noise="gaussian", noise_sigma=5.0)
+    wl.errors = np.full((size, size), 5.0)
+    names = param_names(wl.functions)
+    p = truth.copy()
+    for i, nm in enumerate(names):
+        if nm in ("X0", "Y0"):
+            p[i] += rng.uniform(-1, 1)
+        elif nm == "inc":
+            p[i] = min(p[i] + rng.uniform(-2, 2), 90.0)
+        elif nm in ("PA", "barPA"):
+            p[i] += rng.uniform(-3, 3)
+        else:
+            p[i] *= 1.0 + rng.uniform(-0.05, 0.05)
+    wl.start = p
     return wl
 
 

@@ -348,6 +348,15 @@ class RefModel(_CModel):
                     chi2_init=chi2i.value)
 
 
+def set_los_epsrel(epsrel):
+    """Relative tolerance of the oracle restatement's line-of-sight QAGS
+    (the reference's 1e-6 by default; <= 0 restores it)."""
+    lib = _load("orc")
+    lib.orc_set_los_epsrel.restype = None
+    lib.orc_set_los_epsrel.argtypes = [_D]
+    lib.orc_set_los_epsrel(float(epsrel))
+
+
 def function_value(name, params, x0, y0, x, y, subsampling=True, which="orc"):
     lib = _load(which)
     p = _f64(params)

@@ -243,6 +243,12 @@ static double ferrers3d_density(double s, void *pv) {
   return J_0 * pow((1.0 - m2), n);
 }
 
+/* relative tolerance of the line-of-sight QAGS: the reference's 1e-6 unless a
+ * test asks for a tighter "exact" value (orc_set_los_epsrel) */
+static double g_los_epsrel = QAGS_EPSREL;
+
+void orc_set_los_epsrel(double epsrel) { g_los_epsrel = (epsrel > 0.0) ? epsrel : QAGS_EPSREL; }
+
 static double los_integral(const ofunc *f, double x, double y, int *nsub) {
   double x_diff = x - f->x0, y_diff = y - f->y0;
   double xp = x_diff * f->cosPA + y_diff * f->sinPA;
@@ -258,13 +264,13 @@ static double los_integral(const ofunc *f, double x, double y, int *nsub) {
     pp[5] = f->J_0; pp[6] = f->h; pp[7] = f->z_0; pp[8] = f->scaledZ0;
     pp[9] = f->two_to_alpha; pp[10] = f->alpha3;
     lim = EXPDISK_INTEG_MULT * f->h;
-    qags_integrate(expdisk3d_density, pp, -lim, lim, 0, QAGS_EPSREL, QAGS_LIMIT, &result, &abserr,
+    qags_integrate(expdisk3d_density, pp, -lim, lim, 0, g_los_epsrel, QAGS_LIMIT, &result, &abserr,
                    nsub, NULL);
   } else { /* func_ferrersbar3d.cpp:172-210 */
     pp[5] = f->cosBarPA; pp[6] = f->sinBarPA; pp[7] = f->J_0; pp[8] = f->a2; pp[9] = f->b2;
     pp[10] = f->c2; pp[11] = f->nf;
     lim = f->integLimit;
-    qags_integrate(ferrers3d_density, pp, -lim, lim, 0, QAGS_EPSREL, QAGS_LIMIT, &result, &abserr,
+    qags_integrate(ferrers3d_density, pp, -lim, lim, 0, g_los_epsrel, QAGS_LIMIT, &result, &abserr,
                    nsub, NULL);
   }
   return result;

@@ -74,6 +74,9 @@ int orc_fd_jacobian(orc_model *m, const double *params, double *fjac);
 double orc_function_value(const char *name, const double *params, double x0, double y0, double x,
                           double y, int subsampling);
 double orc_function_total_flux(const char *name, const double *params);
+/* QAGS relative tolerance of the 3-D functions' line-of-sight integrals
+ * (default 1e-6 as the reference; a value <= 0 restores it) */
+void orc_set_los_epsrel(double epsrel);
 int orc_function_nparams(const char *name);
 /* number of QAGS subintervals used for one 3-D function pixel (instrumentation) */
 int orc_function_qags_nsub(const char *name, const double *params, double x0, double y0, double x,
