@@ -78,6 +78,9 @@ _SIGS = [
     ("imfit_BatchJtWJDevice", _I, [_P, _I, _P, _P, _P, _P]),
     ("imfit_FitLM", _I, [_P, _DP, ctypes.POINTER(_I), _DP, _DP, _D, _I, _DP, ctypes.POINTER(_I),
                          ctypes.POINTER(_I), ctypes.POINTER(_I)]),
+    ("imfit_FitLMBatch", _I, [_P, _I, _DP, ctypes.POINTER(_I), _DP, _DP, _D, _I, _DP, ctypes.POINTER(_I),
+                              ctypes.POINTER(_I)]),
+    ("imfit_SetupImageStack", _I, [_P, _I, _I, _I, _DP, _DP, _DP, _I, _I]),
     ("imfit_Synchronize", _I, [_P]),
     ("imfit_GetStream", _I, [_P, ctypes.POINTER(_P)]),
     ("imfit_SetUseGraphs", _I, [_P, _I]),
@@ -374,6 +377,30 @@ class ModelObject:
                                       _dp(hi) if hi is not None else None, ftol, int(max_iter),
                                       ctypes.byref(s), ctypes.byref(it), ctypes.byref(ne), ctypes.byref(st)))
         return dict(params=p, statistic=s.value, niter=it.value, nev=ne.value, status=st.value)
+
+    def fit_lm_batch(self, params, fixed=None, lower=None, upper=None, ftol=1e-8, max_iter=0):
+        """Lockstep Levenberg-Marquardt on the rows of params (B x nParams)."""
+        P = _f64(np.atleast_2d(params)).copy()
+        B, n = P.shape
+        fx = (_I * n)(*([0] * n if fixed is None else [int(v) for v in fixed]))
+        lo = _f64(np.broadcast_to(lower, P.shape)).copy() if lower is not None else None
+        hi = _f64(np.broadcast_to(upper, P.shape)).copy() if upper is not None else None
+        S = np.empty(B)
+        it = (_I * B)()
+        st = (_I * B)()
+        self._ck(self.lib.imfit_FitLMBatch(self.h, B, _dp(P), fx, _dp(lo) if lo is not None else None,
+                                           _dp(hi) if hi is not None else None, ftol, int(max_iter), _dp(S),
+                                           it, st))
+        return dict(params=P, statistic=S, niter=np.array(it[:]), status=np.array(st[:]))
+
+    def setup_image_stack(self, images, sigmas, psfs):
+        """images, sigmas: (n, rows, cols); psfs: (n, prows, pcols)."""
+        im = _f64(images)
+        sg = _f64(np.broadcast_to(sigmas, im.shape)).copy()
+        ps = _f64(psfs)
+        n, nr, nc = im.shape
+        return self._ck(self.lib.imfit_SetupImageStack(self.h, n, nc, nr, _dp(im), _dp(sg), _dp(ps),
+                                                       ps.shape[2], ps.shape[1]))
 
     def synchronize(self):
         return self._ck(self.lib.imfit_Synchronize(self.h))

@@ -367,6 +367,11 @@ __global__ void __launch_bounds__(1024) k_fast_stat_rows(FastArgs a, FastGeom g,
   const int nl = min(rpb, g.nDataRows - row0);
   cplx<float> *spec = reinterpret_cast<cplx<float> *>(a.spec) + (long)b * g.specBatch;
   float S = 0.f, SG = 0.f;
+  if (a.dataStride) {  // image stack: this entry's data and weights
+    const long img = a.entry ? a.entry[b] : b;
+    a.data += img * a.dataStride;
+    a.weight += img * a.dataStride;
+  }
   if (nl > 0) {
     for (int idx = threadIdx.x; idx < nl * (M + 1); idx += blockDim.x) {
       const int l = idx / (M + 1), k = idx - l * (M + 1);
@@ -605,6 +610,7 @@ __global__ void __launch_bounds__(256) k_fast_los_eval(FastArgs a, WinDesc w) {
   for (int i = threadIdx.x; i < nC; i += blockDim.x) sc[i] = a.comps[b * nC + i];
   __syncthreads();
   const int lane = threadIdx.x & 31;
+  const GkLane nd = gk21_lane();
   const long npix = (long)w.rows * w.cols;
   const long nWarps = (long)gridDim.x * (blockDim.x >> 5);
   for (long p = blockIdx.x * (long)(blockDim.x >> 5) + (threadIdx.x >> 5); p < npix; p += nWarps) {
@@ -615,7 +621,7 @@ __global__ void __launch_bounds__(256) k_fast_los_eval(FastArgs a, WinDesc w) {
       if (cc.type < F_EXPDISK3D) continue;
       float xp, yp;
       los_pixel(w, cc, row, col, xp, yp);
-      v += los_value_warp(cc, xp, yp);
+      v += los_value_warp(cc, xp, yp, nd);
     }
     if (lane == 0) w.losVal[(long)b * npix + p] = v;
   }
@@ -634,6 +640,7 @@ __global__ void __launch_bounds__(256) k_fast_los_grad(FastArgs a, WinDesc w, fl
   for (int i = threadIdx.x; i < nC; i += blockDim.x) sc[i] = a.comps[b * nC + i];
   for (int i = threadIdx.x; i < 8 * kMaxParams; i += blockDim.x) (&red[0][0])[i] = 0.f;
   __syncthreads();
+  const GkLane nd = gk21_lane();
   const long npix = (long)w.rows * w.cols;
   const long nWarps = (long)gridDim.x * (blockDim.x >> 5);
   for (long p = blockIdx.x * (long)(blockDim.x >> 5) + wid; p < npix; p += nWarps) {
@@ -645,7 +652,7 @@ __global__ void __launch_bounds__(256) k_fast_los_grad(FastArgs a, WinDesc w, fl
       if (cc.type < F_EXPDISK3D) continue;
       float xp, yp, g[kLosGrad];
       los_pixel(w, cc, row, col, xp, yp);
-      los_grad_warp(cc, xp, yp, g);
+      los_grad_warp(cc, xp, yp, nd, g);
       if (lane == 0) {
         red[wid][cc.x0Index] += r * g[0];
         red[wid][cc.x0Index + 1] += r * g[1];
@@ -851,6 +858,11 @@ __global__ void __launch_bounds__(1024) k_fast_jtwj_rows(FastArgs a, FastGeom g,
   float *U = reinterpret_cast<float *>(bufB + nD * ls);  // nD + 4 rows of nc floats
   float *red = U + (long)(nD + 4) * nc;                  // blockDim.x floats
   for (int i = threadIdx.x; i < nP; i += blockDim.x) ss[i] = slot[i];
+  if (a.dataStride) {  // image stack: this entry's data and weights
+    const long img = a.entry ? a.entry[b] : b;
+    a.data += img * a.dataStride;
+    a.weight += img * a.dataStride;
+  }
   const cplx<float> *src = dspec + (long)b * nD * g.specBatch + (long)row * g.specPitch;
   for (int idx = threadIdx.x; idx < nD * M; idx += blockDim.x) {
     const int j = idx / M, k = idx - j * M;
@@ -1192,7 +1204,7 @@ cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool 
   STAGE("eval_r2c", st, launch_eval(a, mw, *p.Lx, nBatch, 0, tu, st));
   STAGE("cols_conv", st,
         launch_cols<float>(a.spec, g.specPitch, g.specBatch, p.Lx->L / 2 + 1, g.winRows, g.nDataRows, p.H, p.hPitch,
-                           *p.Ly, scale, 1, nBatch, st, tu.colCpb));
+                           *p.Ly, scale, 1, nBatch, st, tu.colCpb, p.hBatch, 1, p.hMap));
   if (fork) {
     cudaError_t e = cudaEventRecord(p.join0, rs);
     if (!e) e = cudaStreamWaitEvent(st, p.join0, 0);
@@ -1218,7 +1230,7 @@ cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool 
   }
   STAGE("cols_adjoint", st,
         launch_cols<float>(a.spec, g.specPitch, g.specBatch, p.Lx->L / 2 + 1, g.nDataRows, g.winRows, p.H, p.hPitch,
-                           *p.Ly, scale, 2, nBatch, st, tu.colCpb));
+                           *p.Ly, scale, 2, nBatch, st, tu.colCpb, p.hBatch, 1, p.hMap));
   STAGE("grad_rows", st, launch_grad(a, mw, *p.Lx, nBatch, 0, 0, tu, st));
   if (los) STAGE("los_grad", st, launch_los_grad(a, mw, nBatch, nMain + nReg, st));
   if (fork) {
@@ -1290,7 +1302,7 @@ cudaError_t fast_jtwj(const FastPlan &p, const FastArgs &a, const JtwjArgs &J, i
     STAGE("jtwj_deriv_r2c", st, launch_deriv(a, main_win(g, J.dspec), *p.Lx, nBatch, 0, J, st));
     STAGE("jtwj_cols", st,
           launch_cols<float>(J.dspec, g.specPitch, g.specBatch, p.Lx->L / 2 + 1, g.winRows, g.nDataRows, p.H,
-                             p.hPitch, *p.Ly, scale, 1, nB, st, tu.colCpb));
+                             p.hPitch, *p.Ly, scale, 1, nB, st, tu.colCpb, p.hBatch, nD, p.hMap));
   }
   const int M = p.Lx->half.n;
   const size_t sm = jtwj_rows_smem(M, nD, g.nDataCols, kJtwjThreads);

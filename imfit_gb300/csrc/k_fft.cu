@@ -51,10 +51,13 @@ __global__ void __launch_bounds__(1024) k_rows_r2c(const T *__restrict__ in, lon
   }
 }
 
+// H of batch entry y is H + e * hBatch with e = y / hDiv, or hMap[e] when a map
+// is given (hBatch 0: one PSF for all).
 template <typename T, int MODE>
 __global__ void __launch_bounds__(1024) k_cols(cplx<T> *__restrict__ spec, long pitch, long batch, int nColsC,
                                               int nRowsIn, int nRowsOut, const cplx<T> *__restrict__ H,
-                                              long hPitch, FFTPlan<T> plan, T scale, int cpb) {
+                                              long hPitch, FFTPlan<T> plan, T scale, int cpb, long hBatch,
+                                              int hDiv, const int *__restrict__ hMap) {
   extern __shared__ unsigned char smem_raw[];
   cplx<T> *bufA = reinterpret_cast<cplx<T> *>(smem_raw);
   const int Ly = plan.n;
@@ -63,6 +66,10 @@ __global__ void __launch_bounds__(1024) k_cols(cplx<T> *__restrict__ spec, long 
   const int nl = min(cpb, nColsC - c0);
   if (nl <= 0) return;
   spec += blockIdx.y * batch;
+  if (hBatch) {
+    const int e = blockIdx.y / hDiv;
+    H += (long)(hMap ? hMap[e] : e) * hBatch;
+  }
   for (int idx = threadIdx.x; idx < Ly * cpb; idx += blockDim.x) {
     const int t = idx / cpb, f = idx % cpb;
     cplx<T> v = {(T)0, (T)0};
@@ -191,7 +198,7 @@ int cols_per_block(int Ly, int elemBytes, int nColsC) {
 template <typename T>
 cudaError_t launch_cols(void *spec, long pitch, long batch, int nColsC, int nRowsIn, int nRowsOut,
                         const void *H, long hPitch, const FFTLen &Ly, T scale, int mode, int nBatch,
-                        cudaStream_t st, int cpbOverride) {
+                        cudaStream_t st, int cpbOverride, long hBatch, int hDiv, const int *hMap) {
   const int L = Ly.full.n;
   int cpb = cpbOverride > 0 ? cpbOverride : cols_per_block(L, sizeof(T), nColsC);
   while (cpb > 1 && (size_t)2 * L * cpb * 2 * sizeof(T) > 200 * 1024) cpb >>= 1;
@@ -203,13 +210,13 @@ cudaError_t launch_cols(void *spec, long pitch, long batch, int nColsC, int nRow
   const cplx<T> *h = reinterpret_cast<const cplx<T> *>(H);
   if (mode == 0) {
     allow_max_smem((const void *)k_cols<T, 0>);
-    k_cols<T, 0><<<grid, nt, sm, st>>>(s, pitch, batch, nColsC, nRowsIn, nRowsOut, h, hPitch, p, scale, cpb);
+    k_cols<T, 0><<<grid, nt, sm, st>>>(s, pitch, batch, nColsC, nRowsIn, nRowsOut, h, hPitch, p, scale, cpb, hBatch, hDiv, hMap);
   } else if (mode == 1) {
     allow_max_smem((const void *)k_cols<T, 1>);
-    k_cols<T, 1><<<grid, nt, sm, st>>>(s, pitch, batch, nColsC, nRowsIn, nRowsOut, h, hPitch, p, scale, cpb);
+    k_cols<T, 1><<<grid, nt, sm, st>>>(s, pitch, batch, nColsC, nRowsIn, nRowsOut, h, hPitch, p, scale, cpb, hBatch, hDiv, hMap);
   } else {
     allow_max_smem((const void *)k_cols<T, 2>);
-    k_cols<T, 2><<<grid, nt, sm, st>>>(s, pitch, batch, nColsC, nRowsIn, nRowsOut, h, hPitch, p, scale, cpb);
+    k_cols<T, 2><<<grid, nt, sm, st>>>(s, pitch, batch, nColsC, nRowsIn, nRowsOut, h, hPitch, p, scale, cpb, hBatch, hDiv, hMap);
   }
   return cudaGetLastError();
 }
@@ -234,9 +241,9 @@ template cudaError_t launch_rows_r2c<double>(const double *, long, long, int, in
 template cudaError_t launch_rows_r2c<float>(const float *, long, long, int, int, void *, long, long,
                                             const FFTLen &, int, cudaStream_t);
 template cudaError_t launch_cols<double>(void *, long, long, int, int, int, const void *, long,
-                                         const FFTLen &, double, int, int, cudaStream_t, int);
+                                         const FFTLen &, double, int, int, cudaStream_t, int, long, int, const int *);
 template cudaError_t launch_cols<float>(void *, long, long, int, int, int, const void *, long,
-                                        const FFTLen &, float, int, int, cudaStream_t, int);
+                                        const FFTLen &, float, int, int, cudaStream_t, int, long, int, const int *);
 template cudaError_t launch_rows_c2r<double>(const void *, long, long, int, double *, long, long, int,
                                              double, const FFTLen &, int, cudaStream_t);
 template cudaError_t launch_rows_c2r<float>(const void *, long, long, int, float *, long, long, int, float,

@@ -49,7 +49,8 @@ cudaError_t launch_rows_r2c(const T *in, long inPitch, long inBatch, int inCols,
 template <typename T>
 cudaError_t launch_cols(void *spec, long pitch, long batch, int nColsC, int nRowsIn, int nRowsOut,
                         const void *H, long hPitch, const FFTLen &Ly, T scale, int mode, int nBatch,
-                        cudaStream_t st, int cpbOverride = 0);
+                        cudaStream_t st, int cpbOverride = 0, long hBatch = 0, int hDiv = 1,
+                        const int *hMap = nullptr);
 template <typename T>
 cudaError_t launch_rows_c2r(const void *in, long inPitch, long inBatch, int nRows, T *out, long outPitch,
                             long outBatch, int outCols, T scale, const FFTLen &Lx, int nBatch,
@@ -142,6 +143,8 @@ struct FastArgs {
   const float *weight;   // internal weights (masked), or multiplicity-weighted
   const float *extra;    // Cash extra terms (or null)
   const float *count;    // bootstrap multiplicity per pixel (or null)
+  long dataStride;       // image stacks: data/weight stride between batch entries (0: one image)
+  const int *entry;      // image stacks: image of batch entry b is entry[b] (null: b)
   int kind;              // 0 chi^2, 1 Cash
   int modelErrors;
   float effGain, sky, rnTerm;
@@ -207,6 +210,8 @@ struct FastPlan {
   const FFTLen *Lx, *Ly, *Rx, *Ry;  // main and region lengths
   const void *H, *Hr;               // FP32 PSF spectra (main, region)
   long hPitch, hrPitch;
+  long hBatch = 0;                  // image stacks: spectrum stride between entries (0: one PSF)
+  const int *hMap = nullptr;        // image stacks: PSF spectrum of batch entry b is hMap[b] (null: b)
 };
 
 // Forward-mode JtWJ buffers.  Parameters with slot[j] >= 0 get a derivative

@@ -51,10 +51,10 @@ __device__ __forceinline__ float expdisk_fg(const CompF32 &c, float xp, float yp
   const float yd = fmaf(s, si, yp * ci);
   const float zd = fmaf(-s, ci, yp * si);
   const float R = fast_sqrt(fmaf(xp, xp, yd * yd));
-  const float Rinv = R > 0.f ? 1.f / R : 0.f;
+  const float Rinv = R > 0.f ? __fdividef(1.f, R) : 0.f;
   const float u = fabsf(zd) * c.s6;
   const float e2u = fast_ex2(-2.f * kLog2eF * u);
-  const float th = (1.f - e2u) / (1.f + e2u);  // tanh(u)
+  const float th = __fdividef(1.f - e2u, 1.f + e2u);  // tanh(u)
   const float l1p = fast_lg2(1.f + e2u);
   const float alpha = c.s5;
   const float E = fast_ex2(fmaf(-R * c.s1, kLog2eF, alpha * (1.f - u * kLog2eF - l1p)));
@@ -63,7 +63,8 @@ __device__ __forceinline__ float expdisk_fg(const CompF32 &c, float xp, float yp
   const float fxp = fR * xp * Rinv;
   const float fyd = fR * yd * Rinv;
   const float sgn = zd > 0.f ? 1.f : (zd < 0.f ? -1.f : 0.f);
-  const float fzd = -f * th * sgn / c.s7;
+  const float iz0 = c.s6 * c.s5;  // 1/z_0 = alpha / (alpha z_0)
+  const float fzd = -f * th * sgn * iz0;
   const float gp = fmaf(fyd, ci, fzd * si);
   g[0] = fmaf(-c.cosPA, fxp, c.sinPA * gp);
   g[1] = fmaf(-c.sinPA, fxp, -c.cosPA * gp);
@@ -73,7 +74,7 @@ __device__ __forceinline__ float expdisk_fg(const CompF32 &c, float xp, float yp
   g[5] = f * R * c.s1 * c.s1;
   const float lncosh = (u * kLog2eF + l1p - 1.f) * kLn2F;
   g[6] = f * (-0.5f * alpha * alpha) * fmaf(u, th, -lncosh);
-  g[7] = f * alpha * u * th / c.s7;
+  g[7] = f * alpha * u * th * iz0;
   g[8] = 0.f;
   g[9] = 0.f;
   return f;
@@ -118,9 +119,9 @@ __device__ __forceinline__ float ferrers_fg(const CompF32 &c, float xp, float yp
   g[3] = kDeg2RadF * fmaf(fyd, fmaf(s, ci, -yp * si), fzd * fmaf(yp, ci, s * si));
   g[4] = kDeg2RadF * 2.f * fm * xb * yb * (ib2 - ia2);
   g[5] = P;
-  g[6] = fm * (-2.f * m2 / c.s1);
-  g[7] = fm * (-2.f * xb * xb * ib2 / c.s2);
-  g[8] = fm * (-2.f * zd * zd * ic2 / c.pad);
+  g[6] = fm * (-2.f * m2 * __fdividef(1.f, c.s1));
+  g[7] = fm * (-2.f * xb * xb * ib2 * __fdividef(1.f, c.s2));
+  g[8] = fm * (-2.f * zd * zd * ic2 * __fdividef(1.f, c.pad));
   g[9] = f * lW * kLn2F;
   return f;
 }
@@ -133,26 +134,31 @@ __device__ __forceinline__ float los_f(const CompF32 &c, float xp, float yp, flo
 __device__ __forceinline__ int los_nparams(const CompF32 &c) { return c.type == F_EXPDISK3D ? 6 : 8; }
 
 // ---------------------------------------------------------- warp rule
-// node (on [-1,1]) and Kronrod / Gauss weights evaluated by this lane
-__device__ __forceinline__ void gk21_lane(int lane, float &x, float &wk, float &wg) {
-  if (lane >= 21) {
-    x = 0.f;
-    wk = 0.f;
-    wg = 0.f;
-    return;
+// The node (on [-1,1]) and Kronrod / Gauss weights this lane evaluates:
+// lanes 0..9 the negative abscissae, 10..19 the positive ones, 20 the centre,
+// 21..31 none.  Computed once per kernel (FP64 table -> FP32).
+struct GkLane {
+  float x, wk, wg;
+};
+
+__device__ __forceinline__ GkLane gk21_lane() {
+  const int lane = threadIdx.x & 31;
+  GkLane n{0.f, 0.f, 0.f};
+  if (lane < 21) {
+    const int k = lane < 10 ? lane : (lane < 20 ? lane - 10 : 10);
+    const float xa = (float)GK21_XGK[k];
+    n.x = lane < 10 ? -xa : xa;
+    n.wk = (float)GK21_WGK[k];
+    n.wg = (k & 1) ? (float)GK21_WG[k >> 1] : 0.f;
   }
-  const int k = lane < 10 ? lane : (lane < 20 ? lane - 10 : 10);
-  const float xa = (float)GK21_XGK[k];
-  x = lane < 10 ? -xa : xa;
-  wk = (float)GK21_WGK[k];
-  wg = (k & 1) ? (float)GK21_WG[k >> 1] : 0.f;
+  return n;
 }
 
-__device__ __forceinline__ void los_panel(const CompF32 &c, float xp, float yp, float lo, float hi, float nx,
-                                          float wk, float wg, float &res, float &err) {
+__device__ __forceinline__ void los_panel(const CompF32 &c, float xp, float yp, float lo, float hi,
+                                          const GkLane &nd, float &res, float &err) {
   const float mid = 0.5f * (lo + hi), half = 0.5f * (hi - lo);
-  const float f = (wk != 0.f) ? los_f(c, xp, yp, fmaf(half, nx, mid)) : 0.f;
-  const float K = los_wsum(wk * f), G = los_wsum(wg * f);
+  const float f = (nd.wk != 0.f) ? los_f(c, xp, yp, fmaf(half, nd.x, mid)) : 0.f;
+  const float K = los_wsum(nd.wk * f), G = los_wsum(nd.wg * f);
   res = K * half;
   err = fabsf((K - G) * half);
 }
@@ -161,11 +167,9 @@ __device__ __forceinline__ void los_panel(const CompF32 &c, float xp, float yp, 
 // warp call it with the same arguments).  Lane p < np ends up holding panel
 // p in [lo, hi]; returns np (0 when the integrand is zero everywhere) and the
 // integral in 'total' (same in every lane).
-__device__ __forceinline__ int los_partition(const CompF32 &c, float xp, float yp, float &myLo, float &myHi,
-                                             float &total) {
+__device__ __forceinline__ int los_partition(const CompF32 &c, float xp, float yp, const GkLane &nd,
+                                             float &myLo, float &myHi, float &total) {
   const int lane = threadIdx.x & 31;
-  float nx, wk, wg;
-  gk21_lane(lane, nx, wk, wg);
   float a, b, bp[2];
   int nbp = 0;
   if (c.type == F_EXPDISK3D) {
@@ -228,7 +232,7 @@ __device__ __forceinline__ int los_partition(const CompF32 &c, float xp, float y
   for (int i = 0; i <= nbp; i++) {
     const float hi = (i < nbp) ? bp[i] : b;
     float r, e;
-    los_panel(c, xp, yp, lo, hi, nx, wk, wg, r, e);
+    los_panel(c, xp, yp, lo, hi, nd, r, e);
     if (lane == np) {
       myLo = lo;
       myHi = hi;
@@ -257,8 +261,8 @@ __device__ __forceinline__ int los_partition(const CompF32 &c, float xp, float y
     const float m = 0.5f * (plo + phi);
     if (!(m > plo && m < phi)) break;
     float r1, e1, r2, e2;
-    los_panel(c, xp, yp, plo, m, nx, wk, wg, r1, e1);
-    los_panel(c, xp, yp, m, phi, nx, wk, wg, r2, e2);
+    los_panel(c, xp, yp, plo, m, nd, r1, e1);
+    los_panel(c, xp, yp, m, phi, nd, r2, e2);
     if (lane == id) {
       myHi = m;
       myRes = r1;
@@ -277,34 +281,31 @@ __device__ __forceinline__ int los_partition(const CompF32 &c, float xp, float y
 }
 
 // Value of a 3-D component at a pixel (xp, yp in its rotated frame).
-__device__ __forceinline__ float los_value_warp(const CompF32 &c, float xp, float yp) {
+__device__ __forceinline__ float los_value_warp(const CompF32 &c, float xp, float yp, const GkLane &nd) {
   float lo, hi, total;
-  los_partition(c, xp, yp, lo, hi, total);
+  los_partition(c, xp, yp, nd, lo, hi, total);
   return total;
 }
 
 // d(value)/d(X0, Y0, function parameters) over the same panels; every lane
 // returns the full sums in g[0..kLosGrad).
-__device__ __forceinline__ void los_grad_warp(const CompF32 &c, float xp, float yp, float *g) {
+__device__ __forceinline__ void los_grad_warp(const CompF32 &c, float xp, float yp, const GkLane &nd, float *g) {
   float myLo, myHi, total;
-  const int np = los_partition(c, xp, yp, myLo, myHi, total);
-  const int lane = threadIdx.x & 31;
-  float nx, wk, wg;
-  gk21_lane(lane, nx, wk, wg);
+  const int np = los_partition(c, xp, yp, nd, myLo, myHi, total);
   float acc[kLosGrad];
 #pragma unroll
   for (int q = 0; q < kLosGrad; q++) acc[q] = 0.f;
   for (int p = 0; p < np; p++) {
     const float lo = __shfl_sync(0xffffffffu, myLo, p), hi = __shfl_sync(0xffffffffu, myHi, p);
-    if (wk != 0.f) {
+    if (nd.wk != 0.f) {
       const float mid = 0.5f * (lo + hi), half = 0.5f * (hi - lo);
-      const float s = fmaf(half, nx, mid);
+      const float s = fmaf(half, nd.x, mid);
       float t[kLosGrad];
       if (c.type == F_EXPDISK3D)
         expdisk_fg(c, xp, yp, s, t);
       else
         ferrers_fg(c, xp, yp, s, t);
-      const float w = wk * half;
+      const float w = nd.wk * half;
 #pragma unroll
       for (int q = 0; q < kLosGrad; q++) acc[q] = fmaf(w, t[q], acc[q]);
     }

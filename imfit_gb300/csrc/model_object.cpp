@@ -213,6 +213,15 @@ struct imfit_model_s {
   DevBuf<int> dSubBox;
   DevBuf<double> dParams, dStat, dGrad;
   DevBuf<float> dStatPart, dGradPart;
+  // image stack (fast path only): batch entry b has its own image, weights and PSF
+  struct Stack {
+    int n = 0, pc = 0, pr = 0;
+    std::vector<float> data, weight;  // n x nDataVals
+    std::vector<double> psf;          // n x pc*pr, normalised
+  } stack;
+  // image-stack subset being evaluated: image of batch entry b (device), or null
+  DevBuf<int> dEntry;
+  const int *curEntry = nullptr;
   // 3-D components: per window pixel line-of-sight values and adjoint r~
   bool hasLos = false;
   DevBuf<float> dLosVal32, dLosRt32, dRLosVal32, dRLosRt32;
@@ -534,6 +543,7 @@ struct imfit_model_s {
 
   // -------------------------------------------------------- plain path
   int checkEval() {
+    if (stack.n) return fail(IMFIT_E_UNSUPPORTED, "the plain FP64 path takes one image per ModelObject, not a stack");
     if (!setsDefined) return fail(IMFIT_E_STATE, "DefineFunctionSets not called");
     if (!modelSetupDone) return fail(IMFIT_E_STATE, "SetupModelImage not called");
     return 0;
@@ -761,8 +771,10 @@ struct imfit_model_s {
       if (f.type == F_EXPDISK3D || f.type == F_FERRERS3D) hasLos = true;
     if (regions.size() > 1) return fail(IMFIT_E_UNSUPPORTED, "fast path supports at most one oversampled region");
     if ((int)funcs.size() > kMaxComponents) return fail(IMFIT_E_UNSUPPORTED, "too many components");
-    const int pc = doConv ? nPsfCols : 1, pr = doConv ? nPsfRows : 1;
-    std::vector<double> kp = doConv ? psf : std::vector<double>{1.0};
+    if (stack.n && !regions.empty()) return fail(IMFIT_E_UNSUPPORTED, "image stacks do not take oversampled regions");
+    const int pc = stack.n ? stack.pc : (doConv ? nPsfCols : 1), pr = stack.n ? stack.pr : (doConv ? nPsfRows : 1);
+    std::vector<double> kp = stack.n ? std::vector<double>(stack.psf.begin(), stack.psf.begin() + (size_t)pc * pr)
+                                     : (doConv ? psf : std::vector<double>{1.0});
     FastGeom &g = fg;
     g = FastGeom{};
     g.nDataCols = nDataCols;
@@ -779,7 +791,16 @@ struct imfit_model_s {
     g.specPitch = Fx.L / 2 + 1;
     g.specBatch = (long)Fy.L * g.specPitch;
     // PSF placed so that circular output (r,c) is the data pixel (r,c)
-    int st = shiftedSpectrum32(kp, pc, pr, Fx, Fy, dH32);
+    int st = 0;
+    if (stack.n) {
+      const size_t hb = 2 * (size_t)Fy.L * (Fx.L / 2 + 1);
+      cudaError_t e0 = dH32.reserve(hb * stack.n);
+      if (e0) return cuda_fail(e0, "stack PSF spectra");
+      for (int i = 0; i < stack.n && !st; i++)
+        st = shiftedSpectrum32To(stack.psf.data() + (size_t)i * pc * pr, pc, pr, Fx, Fy, dH32.p + hb * i);
+    } else {
+      st = shiftedSpectrum32(kp, pc, pr, Fx, Fy, dH32);
+    }
     if (st) return st;
     double ps = 0.0;
     for (double v : kp) ps += v;
@@ -822,15 +843,21 @@ struct imfit_model_s {
     // FP32 statistic inputs
     const long n = nDataVals;
     std::vector<float> f32(n);
-    cudaError_t e = dData32.reserve(n);
-    if (!e) e = dW32.reserve(n);
+    const size_t nAll = (size_t)n * (stack.n ? stack.n : 1);
+    cudaError_t e = dData32.reserve(nAll);
+    if (!e) e = dW32.reserve(nAll);
     if (!e) e = dExtra32.reserve(n);
     if (!e) e = dCount32.reserve(n);
     if (e) return cuda_fail(e, "fast buffers");
-    for (long z = 0; z < n; z++) f32[z] = (float)data[z];
-    e = cudaMemcpy(dData32.p, f32.data(), sizeof(float) * n, cudaMemcpyHostToDevice);
-    for (long z = 0; z < n; z++) f32[z] = (float)weight[z];
-    if (!e) e = cudaMemcpy(dW32.p, f32.data(), sizeof(float) * n, cudaMemcpyHostToDevice);
+    if (stack.n) {
+      e = cudaMemcpy(dData32.p, stack.data.data(), sizeof(float) * nAll, cudaMemcpyHostToDevice);
+      if (!e) e = cudaMemcpy(dW32.p, stack.weight.data(), sizeof(float) * nAll, cudaMemcpyHostToDevice);
+    } else {
+      for (long z = 0; z < n; z++) f32[z] = (float)data[z];
+      e = cudaMemcpy(dData32.p, f32.data(), sizeof(float) * n, cudaMemcpyHostToDevice);
+      for (long z = 0; z < n; z++) f32[z] = (float)weight[z];
+      if (!e) e = cudaMemcpy(dW32.p, f32.data(), sizeof(float) * n, cudaMemcpyHostToDevice);
+    }
     for (long z = 0; z < n; z++) f32[z] = extra.empty() ? 0.f : (float)extra[z];
     if (!e) e = cudaMemcpy(dExtra32.p, f32.data(), sizeof(float) * n, cudaMemcpyHostToDevice);
     if (!e) e = uploadCounts();
@@ -879,6 +906,13 @@ struct imfit_model_s {
 
   int shiftedSpectrum32(const std::vector<double> &p, int pc, int pr, const FFTLen &fx, const FFTLen &fy,
                         DevBuf<float> &H32) {
+    cudaError_t e = H32.reserve(2 * (size_t)fy.L * (fx.L / 2 + 1));
+    if (e) return cuda_fail(e, "FP32 PSF spectrum");
+    return shiftedSpectrum32To(p.data(), pc, pr, fx, fy, H32.p);
+  }
+
+  // FP32 spectrum of one PSF (centre wrapped to (0,0)) written to dst
+  int shiftedSpectrum32To(const double *p, int pc, int pr, const FFTLen &fx, const FFTLen &fy, float *dst) {
     std::vector<double> pad((size_t)fx.L * fy.L, 0.0);
     for (int k = 0; k < pr; k++)
       for (int l = 0; l < pc; l++) {
@@ -890,8 +924,7 @@ struct imfit_model_s {
     int st = spectrum64(pad, fx, fy, H64);
     if (st) return st;
     const size_t nc = 2 * (size_t)fy.L * (fx.L / 2 + 1);
-    cudaError_t e = H32.reserve(nc);
-    if (!e) e = launch_f64_to_f32(H64.p, H32.p, (long)nc, stream);
+    cudaError_t e = launch_f64_to_f32(H64.p, dst, (long)nc, stream);
     if (!e) e = cudaStreamSynchronize(stream);
     if (e) return cuda_fail(e, "FP32 PSF spectrum");
     return 0;
@@ -956,6 +989,8 @@ struct imfit_model_s {
     a.weight = dW32.p;
     a.extra = (useCash && pmlr) ? dExtra32.p : nullptr;
     a.count = doBootstrap ? dCount32.p : nullptr;
+    a.dataStride = stack.n ? nDataVals : 0;
+    a.entry = stack.n ? curEntry : nullptr;
     a.kind = useCash ? 1 : 0;
     a.modelErrors = modelErrors ? 1 : 0;
     a.effGain = (float)effGain;
@@ -1007,6 +1042,8 @@ struct imfit_model_s {
     p.Hr = dHr32.p;
     p.hPitch = Fx.L / 2 + 1;
     p.hrPitch = FRx.L / 2 + 1;
+    p.hBatch = stack.n ? (long)Fy.L * (Fx.L / 2 + 1) : 0;
+    p.hMap = stack.n ? curEntry : nullptr;
     return p;
   }
 
@@ -1018,6 +1055,12 @@ struct imfit_model_s {
     auto it = tuned.find(B);
     if (it != tuned.end()) {
       tune = it->second;
+      return 0;
+    }
+    if (stack.n && B != stack.n) {  // a subset of a stack: the whole stack's shape
+      auto full = tuned.find(stack.n);
+      tune = (full != tuned.end()) ? full->second : FastTune{};
+      tuned[B] = tune;
       return 0;
     }
     if (!autotune) {
@@ -1079,6 +1122,7 @@ struct imfit_model_s {
   int enqueueFast(int B, const double *dP, double *dS, double *dG, float *modelOut = nullptr) {
     int st = prepareFast();
     if (st) return st;
+    if (stack.n && B != stack.n) return fail(IMFIT_E_ARG, "an image stack evaluates exactly one parameter vector per image");
     st = ensureFastCap(B);
     if (st) return st;
     if (tuned.find(B) == tuned.end() || !(graph.exec && graph.nBatch == B)) {
@@ -1159,6 +1203,8 @@ struct imfit_model_s {
     if (hasLos)
       return fail(IMFIT_E_UNSUPPORTED, "J^T J of 3-D line-of-sight components is not available; use the adjoint "
                                        "gradient (imfit_GetFitStatisticAndGradient)");
+    if (stack.n && (curEntry ? B > stack.n : B != stack.n))
+      return fail(IMFIT_E_ARG, "an image stack evaluates exactly one parameter vector per image");
     st = ensureFastCap(B);
     if (!st) st = ensureJtwjCap(B);
     if (st) return st;
@@ -1188,16 +1234,28 @@ struct imfit_model_s {
     return 0;
   }
 
-  int jtwjHost(int B, const double *params, double *stats, double *alpha, double *beta) {
+  // imageMap (host, B entries; image stacks only): batch entry b fits image imageMap[b]
+  int jtwjHost(int B, const double *params, double *stats, double *alpha, double *beta,
+               const int *imageMap = nullptr) {
     int st = prepareFast();
     if (!st) st = ensureFastCap(B);
     // the output buffers must exist before their addresses are taken below
     if (!st) st = ensureJtwjCap(B);
     if (st) return st;
+    curEntry = nullptr;
+    if (imageMap && stack.n) {
+      for (int i = 0; i < B; i++)
+        if (imageMap[i] < 0 || imageMap[i] >= stack.n) return fail(IMFIT_E_ARG, "image index out of range");
+      cudaError_t e0 = dEntry.reserve(B);
+      if (!e0) e0 = cudaMemcpyAsync(dEntry.p, imageMap, sizeof(int) * B, cudaMemcpyHostToDevice, stream);
+      if (e0) return cuda_fail(e0, "image map upload");
+      curEntry = dEntry.p;
+    }
     const int nP = nParamsTot;
     cudaError_t e = cudaMemcpyAsync(dParams.p, params, sizeof(double) * (size_t)B * nP, cudaMemcpyHostToDevice, stream);
     if (e) return cuda_fail(e, "params upload");
     st = enqueueJtwj(B, dParams.p, dStat.p, dAlpha.p, dBeta.p);
+    curEntry = nullptr;
     if (st) return st;
     e = cudaMemcpyAsync(stats, dStat.p, sizeof(double) * B, cudaMemcpyDeviceToHost, stream);
     if (!e && alpha) e = cudaMemcpyAsync(alpha, dAlpha.p, sizeof(double) * (size_t)B * nP * nP, cudaMemcpyDeviceToHost, stream);
@@ -1205,6 +1263,96 @@ struct imfit_model_s {
     if (!e) e = cudaStreamSynchronize(stream);
     if (e) return cuda_fail(e, "JtWJ results");
     return 0;
+  }
+
+  // Image stack: nImg images of nc x nr pixels, per-pixel sigmas (internal
+  // weight 1/sigma as AddErrorVector with WEIGHTS_ARE_SIGMAS; sigma <= 0 or
+  // non-finite masks the pixel, as does a non-finite data value) and one PSF
+  // per image, normalised with the Convolver's Kahan sum.  chi^2 statistic.
+  int setupStack(int nImg, int nc, int nr, const double *img, const double *sigma, const double *psfs, int pc,
+                 int pr) {
+    if (!setsDefined) return fail(IMFIT_E_STATE, "DefineFunctionSets not called");
+    if (nImg < 1 || nc < 1 || nr < 1 || pc < 1 || pr < 1 || !img || !sigma || !psfs)
+      return fail(IMFIT_E_ARG, "bad image stack arguments");
+    if (dataValsSet) return fail(IMFIT_E_STATE, "image data already added to this ModelObject");
+    if (useCash || doBootstrap) return fail(IMFIT_E_UNSUPPORTED, "image stacks use the chi^2 statistic");
+    const long n = (long)nc * nr;
+    stack = Stack{};
+    stack.n = nImg;
+    stack.pc = pc;
+    stack.pr = pr;
+    stack.data.resize((size_t)n * nImg);
+    stack.weight.resize((size_t)n * nImg);
+    for (size_t z = 0; z < stack.data.size(); z++) {
+      const double d = img[z], sg = sigma[z];
+      const bool good = std::isfinite(d) && std::isfinite(sg) && sg > 0.0;
+      stack.data[z] = good ? (float)d : 0.f;
+      stack.weight[z] = good ? (float)(1.0 / sg) : 0.f;
+    }
+    const long np = (long)pc * pr;
+    stack.psf.assign(psfs, psfs + np * nImg);
+    for (int i = 0; i < nImg; i++) {
+      double *q = stack.psf.data() + (size_t)i * np;
+      for (long k = 0; k < np; k++)
+        if (!std::isfinite(q[k])) return fail(IMFIT_E_ARG, "PSF image has one or more non-finite values");
+      const double ks = kahan_sum(q, np);
+      if (!(ks > 0.0)) return fail(IMFIT_E_ARG, "Sum of PSF pixel values is <= 0 -- PSF cannot be normalized");
+      for (long k = 0; k < np; k++) q[k] = q[k] / ks;
+    }
+    nDataCols = nc;
+    nDataRows = nr;
+    nDataVals = n;
+    nValid = n;
+    doConv = true;
+    nPsfCols = pc;
+    nPsfRows = pr;
+    finalSetupDone = true;
+    fastReady = false;
+    return 0;
+  }
+
+  int fitLMBatch(int B, double *params, const int *fixed, const double *lower, const double *upper, double ftol,
+                 int maxIter, double *stats, int *nIter, int *status) {
+    const int n = nParamsTot;
+    LMSettings set;
+    set.ftol = ftol;
+    if (maxIter > 0) set.maxIter = maxIter;
+    std::vector<double> hA((size_t)B * n * n), hB((size_t)B * n);
+    // evaluate only the problems still running (compacted; on a stack each
+    // keeps its own image through the image map)
+    std::vector<int> idx;
+    std::vector<double> Xs, Ss, As, Bs;
+    JtwjBatchEval ev = [&, this](const double *X, const unsigned char *act, double *S, double *A, double *b) {
+      idx.clear();
+      for (int i = 0; i < B; i++)
+        if (act[i]) idx.push_back(i);
+      const int k = (int)idx.size();
+      if (k == 0) return 0;
+      if (k == B) return jtwjHost(B, X, S, A, b);
+      Xs.resize((size_t)k * n);
+      Ss.resize(k);
+      As.resize((size_t)k * n * n);
+      Bs.resize((size_t)k * n);
+      for (int r = 0; r < k; r++)
+        std::copy(X + (size_t)idx[r] * n, X + (size_t)(idx[r] + 1) * n, Xs.begin() + (size_t)r * n);
+      int st = jtwjHost(k, Xs.data(), Ss.data(), As.data(), Bs.data(), stack.n ? idx.data() : nullptr);
+      if (st) return st;
+      for (int r = 0; r < k; r++) {
+        const int i = idx[r];
+        S[i] = Ss[r];
+        std::copy(As.begin() + (size_t)r * n * n, As.begin() + (size_t)(r + 1) * n * n, A + (size_t)i * n * n);
+        std::copy(Bs.begin() + (size_t)r * n, Bs.begin() + (size_t)(r + 1) * n, b + (size_t)i * n);
+      }
+      return 0;
+    };
+    std::vector<LMResult> res(B);
+    int st = lm_minimize_batch(B, n, params, fixed, lower, upper, set, ev, res.data());
+    for (int i = 0; i < B; i++) {
+      if (stats) stats[i] = res[i].stat;
+      if (nIter) nIter[i] = res[i].nIter;
+      if (status) status[i] = res[i].status;
+    }
+    return st < 0 ? st : 0;
   }
 
   int makeBootstrapSample() {
@@ -1634,6 +1782,20 @@ int imfit_FitLM(imfit_model_t m, double *params, const int *fixed, const double 
   if (nEval) *nEval = res.nEval;
   if (status) *status = res.status;
   return st < 0 ? st : 0;
+}
+
+int imfit_FitLMBatch(imfit_model_t m, int B, double *params, const int *fixed, const double *lower,
+                     const double *upper, double ftol, int maxIter, double *stats, int *nIter, int *status) {
+  GET(m);
+  if (B < 1 || !params) return m->fail(IMFIT_E_ARG, "bad batch arguments");
+  if (!(ftol > 0.0)) return m->fail(IMFIT_E_ARG, "ftol must be positive");
+  return m->fitLMBatch(B, params, fixed, lower, upper, ftol, maxIter, stats, nIter, status);
+}
+
+int imfit_SetupImageStack(imfit_model_t m, int nImg, int nc, int nr, const double *pix, const double *sig,
+                          const double *psfs, int pc, int pr) {
+  GET(m);
+  return m->setupStack(nImg, nc, nr, pix, sig, psfs, pc, pr);
 }
 
 int imfit_Synchronize(imfit_model_t m) {

@@ -255,3 +255,94 @@ def small_case(seed=7, ncols=64, nrows=48, psf=15, region=True, mask=True, stat=
         wl.mask = m
     wl.start = _perturb(rng, truth, param_names(fns), frac=0.05, pos=0.5)
     return wl
+
+
+def sersic_total_flux(n, I_e, r_e, ell):
+    """Sersic::TotalFlux (function_objects/func_sersic.cpp:246-251)."""
+    import math
+    bn = _sersic_bn(n)
+    return 2.0 * math.pi * n * math.exp(bn) * bn ** (-2.0 * n) * math.gamma(2.0 * n) * (1.0 - ell) * r_e * r_e * I_e
+
+
+def exp_total_flux(I_0, h, ell):
+    """Exponential::TotalFlux (function_objects/func_exp.cpp:210-213)."""
+    import math
+    return 2.0 * math.pi * I_0 * h * h * (1.0 - ell)
+
+
+def _sersic_bn(n):
+    # function_objects/helper_funcs.cpp:14-29
+    n2 = n * n
+    if n > 0.36:
+        return (2 * n - 0.333333333333333 + 0.009876543209876543 / n + 0.0018028610621203215 / n2
+                + 0.00011409410586365319 / (n2 * n) - 7.1510122958919723e-05 / (n2 * n2))
+    return 0.01945 + -0.8902 * n + 10.95 * n2 + -19.67 * n2 * n + 13.43 * n2 * n2
+
+
+C5_FUNCTIONS = [("Sersic", True), ("Exponential", False)]
+
+
+def c5(count=4096, seed=1005, min_side=48, max_side=384):
+    """Uneven batch of cutouts: side log-uniform [min_side, max_side], Sersic
+    (n U[0.5,6], r_e U[2,60] capped by the side, ell U[0,0.7]) + Exponential
+    with B/T U[0,1] through the TotalFlux formulas, per-cutout Moffat PSF
+    (odd 25..63 px, fwhm U[2.5,6], beta U[2.5,4.5]), sky s U[30,70] subtracted
+    and Gaussian noise sigma = sqrt(s).  Returns a dict with the per-cutout
+    geometry, truth, start and limits; the images are made by synthesize_c5."""
+    rng = np.random.default_rng(seed)
+    items = []
+    for k in range(count):
+        side = int(np.floor(np.exp(rng.uniform(np.log(min_side), np.log(max_side)))))
+        side = max(min_side, min(side, max_side))
+        P = int(rng.integers(12, 32)) * 2 + 1  # odd 25..63
+        fwhm = rng.uniform(2.5, 6.0)
+        beta = rng.uniform(2.5, 4.5)
+        c = side / 2 + 0.5
+        x0, y0 = c + rng.uniform(-1, 1), c + rng.uniform(-1, 1)
+        n = rng.uniform(0.5, 6.0)
+        r_e = min(rng.uniform(2.0, 60.0), side / 4)
+        ell_b = rng.uniform(0.0, 0.7)
+        h = min(rng.uniform(3.0, 40.0), side / 5)
+        ell_d = rng.uniform(0.0, 0.7)
+        bt = rng.uniform(0.0, 1.0)
+        flux = np.exp(rng.uniform(np.log(3e4), np.log(3e5)))
+        sky = rng.uniform(30.0, 70.0)
+        fb, fd = max(bt, 0.02) * flux, max(1.0 - bt, 0.02) * flux
+        I_e = fb / sersic_total_flux(n, 1.0, r_e, ell_b)
+        I_0 = fd / exp_total_flux(1.0, h, ell_d)
+        truth = np.array([x0, y0, rng.uniform(0, 180), ell_b, n, I_e, r_e, rng.uniform(0, 180), ell_d, I_0, h])
+        start = truth.copy()
+        for i in range(len(truth)):
+            if i < 2:
+                start[i] += rng.uniform(-1, 1)
+            elif i in (2, 7):
+                start[i] += rng.uniform(-5, 5)
+            else:
+                start[i] *= 1.0 + rng.uniform(-0.1, 0.1)
+        start[3] = min(start[3], 0.9)
+        start[8] = min(start[8], 0.9)
+        lower = np.array([x0 - 10, y0 - 10, -360, 0.0, 0.3, 0.0, 0.3, -360, 0.0, 0.0, 0.3])
+        upper = np.array([x0 + 10, y0 + 10, 360, 0.95, 10.0, 1e9, 4.0 * side, 360, 0.95, 1e9, 4.0 * side])
+        items.append(dict(side=side, psf_size=P, fwhm=fwhm, beta=beta, sky=sky, truth=truth, start=start,
+                          lower=lower, upper=upper, seed=seed * 7919 + k))
+    return items
+
+
+def synthesize_c5(items, model_cls, sub=5):
+    """Images for c5() items: model (model_cls, FP64) + Gaussian noise, and the PSFs."""
+    out = []
+    for it in items:
+        psf = moffat_psf(it["psf_size"], it["fwhm"], it["beta"], sub=sub)
+        m = model_cls()
+        for name, new_set in C5_FUNCTIONS:
+            m.add_function(name, new_set)
+        m.finish_functions()
+        m.add_psf(psf)
+        m.setup_model_image(it["side"], it["side"])
+        m.create_model_image(it["truth"])
+        img = m.get_model_image()
+        rng = np.random.default_rng(it["seed"])
+        sigma = np.sqrt(it["sky"])
+        data = img + rng.normal(0.0, sigma, img.shape)
+        out.append((data, np.full(img.shape, sigma), psf))
+    return out

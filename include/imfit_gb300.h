@@ -187,10 +187,34 @@ int imfit_BatchJtWJDevice(imfit_model_t m, int nBatch, const double *d_params, d
  * is 1e-8, core/definitions.h:61); maxIter <= 0 selects 1000
  * (solvers/levmar_fit.cpp:38).  Outputs (each may be NULL): the fast-path
  * statistic at the result, iterations, JtWJ evaluations, and a status
- * (1 ftol, 2 xtol, 3 no further reduction at FP32 precision, 5 iteration
+ * (1 ftol, 3 no further reduction at FP32 precision, 4 stalled: no progress
+ * above the FP32 noise of the statistic for 20 rounds, 5 iteration
  * limit).  Returns 0 or a negative IMFIT_E_* code. */
 int imfit_FitLM(imfit_model_t m, double *params, const int *fixed, const double *lower, const double *upper,
                 double ftol, int maxIter, double *statistic, int *nIter, int *nEval, int *status);
+/* Levenberg-Marquardt on nBatch problems at once (lockstep: one batched JtWJ
+ * evaluation per round for all of them; each problem keeps its own damping
+ * and convergence state).  params: nBatch x nParams in/out; fixed: nParams
+ * flags shared by all (may be NULL); lower/upper: nBatch x nParams or NULL.
+ * On an image stack (imfit_SetupImageStack) problem b fits image b and
+ * nBatch must equal the stack size; otherwise all problems fit this
+ * handle's image (e.g. several starting points).  statistics, nIter, status
+ * (nBatch each) may be NULL; status codes as imfit_FitLM. */
+int imfit_FitLMBatch(imfit_model_t m, int nBatch, double *params, const int *fixed, const double *lower,
+                     const double *upper, double ftol, int maxIter, double *statistics, int *nIter, int *status);
+
+/* ---- image stacks (fast path; no counterpart in the reference) ------------- */
+/* Many cutouts fitted with one model: nImages images of nColumns x nRows
+ * pixels (row-major, image after image), per-pixel sigmas (internal weight
+ * 1/sigma as AddErrorVector with WEIGHTS_ARE_SIGMAS; sigma <= 0 or
+ * non-finite, or non-finite data, masks a pixel -- pad smaller cutouts this
+ * way) and one psfColumns x psfRows PSF per image (normalised as the
+ * reference's Convolver does).  Replaces AddImageDataVector ..
+ * FinalSetupForFitting for this handle; chi^2 statistic; fast-path entry
+ * points then take exactly nImages parameter vectors, vector b for image b.
+ * The plain FP64 entry points are per image and reject a stack. */
+int imfit_SetupImageStack(imfit_model_t m, int nImages, int nColumns, int nRows, const double *pixels,
+                          const double *sigmas, const double *psfs, int psfColumns, int psfRows);
 int imfit_Synchronize(imfit_model_t m);
 /* The CUDA stream (cudaStream_t) all work of this handle is enqueued on. */
 int imfit_GetStream(imfit_model_t m, void **stream);

@@ -1,0 +1,134 @@
+"""GPU checks of image stacks (many cutouts, one model) and of the lockstep
+batched Levenberg-Marquardt used for the uneven-cutout workload.
+
+Tolerances:
+  * stack statistic vs the FP64 oracle on each unpadded cutout: 1e-5 relative;
+  * stack J^T J / J^T dev vs a single-image ModelObject per cutout (same FP32
+    algorithm, different padding and FFT sizes): 1e-4 of sqrt(A_jj A_kk) and
+    of |b| + 1e-3 max|b|;
+  * batched LM vs one-at-a-time LM: chi^2 at the two solutions (FP64 plain
+    path) within 1e-7 relative;
+  * cutout fits vs FP64 fits (scipy's MINPACK lmdif on the oracle's FP64
+    deviates, tight tolerances): chi^2 within 1e-7 and every parameter within
+    max(1e-4 |p|, 0.02 sigma_p) -- 1e-4 relative for well-determined
+    parameters; poorly determined ones (sigma_p/p ~ 1) differ by statistically
+    meaningless amounts because the reference statistic is discontinuous at
+    the 1e-8 level where subsample counts switch.
+"""
+import numpy as np
+import pytest
+
+from helpers import relerr
+
+pytestmark = pytest.mark.gpu
+
+
+def _items(oracle_mod, count=4, max_side=72, seed=2024):
+    from imfit_gb300 import workloads
+    items = workloads.c5(count, seed=seed, max_side=max_side)
+    imgs = workloads.synthesize_c5(items, oracle_mod.OracleModel, sub=3)
+    return items, imgs
+
+
+def _single(cls, data, sigma, psf, weights_are_sigmas=100):
+    from imfit_gb300 import workloads
+    m = cls()
+    for name, new_set in workloads.C5_FUNCTIONS:
+        m.add_function(name, new_set)
+    m.finish_functions()
+    m.add_psf(psf)
+    m.add_image_data(data)
+    m.add_error_vector(sigma, weights_are_sigmas)
+    assert m.final_setup() == 0
+    return m
+
+
+def _stack(gpu, imgs):
+    """All cutouts in one stack, padded to the largest bucket among them."""
+    from imfit_gb300 import cutouts, workloads
+    cs = [cutouts.Cutout(d, s, p) for d, s, p in imgs]
+    key = tuple(max(k) for k in zip(*[cutouts.bucket_of(c) for c in cs]))
+    return cutouts.build_stack(workloads.C5_FUNCTIONS, cs, key)
+
+
+def test_stack_statistic_matches_oracle_per_cutout(gpu, oracle_mod):
+    items, imgs = _items(oracle_mod)
+    m = _stack(gpu, imgs)
+    P = np.array([it["start"] for it in items])
+    S, G = m.batch_statistic_and_gradient(P)
+    for i, (d, s, p) in enumerate(imgs):
+        o = _single(oracle_mod.OracleModel, d, s, p)
+        assert relerr(S[i], o.get_fit_statistic(P[i])) < 1e-5
+
+
+def test_stack_jtwj_equals_single_images(gpu, oracle_mod):
+    items, imgs = _items(oracle_mod, seed=77)
+    m = _stack(gpu, imgs)
+    n = len(items)
+    P = np.array([it["start"] for it in items])
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda", 0)
+    nP = P.shape[1]
+    dP = torch.tensor(P.ravel(), dtype=torch.float64, device=dev)
+    dS = torch.zeros(n, dtype=torch.float64, device=dev)
+    dA = torch.zeros(n * nP * nP, dtype=torch.float64, device=dev)
+    dB = torch.zeros(n * nP, dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+    m.batch_jtwj_device(n, dP.data_ptr(), dS.data_ptr(), dA.data_ptr(), dB.data_ptr())
+    m.synchronize()
+    S = dS.cpu().numpy()
+    A = dA.cpu().numpy().reshape(n, nP, nP)
+    B = dB.cpu().numpy().reshape(n, nP)
+    for i, (d, s, p) in enumerate(imgs):
+        g = _single(gpu.ModelObject, d, s, p)
+        s1, a1, b1 = g.jtwj(P[i])
+        assert relerr(S[i], s1) < 1e-5
+        dd = np.sqrt(np.outer(np.diag(a1), np.diag(a1)))
+        assert np.all(np.abs(A[i] - a1) <= 1e-4 * dd)
+        assert np.all(np.abs(B[i] - b1) <= 1e-4 * (np.abs(b1) + 1e-3 * np.max(np.abs(b1))))
+
+
+def test_batched_lm_matches_single_lm(gpu, oracle_mod):
+    items, imgs = _items(oracle_mod, seed=99)
+    m = _stack(gpu, imgs)
+    P = np.array([it["start"] for it in items])
+    lo = np.array([it["lower"] for it in items])
+    hi = np.array([it["upper"] for it in items])
+    rb = m.fit_lm_batch(P, lower=lo, upper=hi, ftol=1e-10)
+    assert np.all(np.isin(rb["status"], (1, 3, 4))), rb["status"]
+    for i, (d, s, p) in enumerate(imgs):
+        g = _single(gpu.ModelObject, d, s, p)
+        r1 = g.fit_lm(P[i], lower=lo[i], upper=hi[i], ftol=1e-10)
+        c_batch = g.get_fit_statistic(rb["params"][i])
+        c_single = g.get_fit_statistic(r1["params"])
+        # converged fits of the same data agree to the statistic's FP32 noise;
+        # a fit that stalled in a flat valley may stop elsewhere along it
+        tol = 1e-7 if (rb["status"][i] == 1 and r1["status"] == 1) else 1e-3
+        assert relerr(c_batch, c_single) < tol, (i, c_batch, c_single, rb["status"][i], r1["status"])
+
+
+def test_cutout_fits_match_fp64_fits(gpu, oracle_mod):
+    scipy_opt = pytest.importorskip("scipy.optimize")
+    from imfit_gb300 import cutouts, workloads
+    items, imgs = _items(oracle_mod, count=3, max_side=60, seed=5)
+    fitter = cutouts.CutoutFitter(workloads.C5_FUNCTIONS, [cutouts.Cutout(*x) for x in imgs], threads=2)
+    starts = np.array([it["start"] for it in items])
+    lo = np.array([it["lower"] for it in items])
+    hi = np.array([it["upper"] for it in items])
+    r = fitter.fit(starts, lower=lo, upper=hi, ftol=1e-12)
+    for i, (d, s, p) in enumerate(imgs):
+        o = _single(oracle_mod.OracleModel, d, s, p)
+        ref = scipy_opt.least_squares(lambda x: o.compute_deviates(x), starts[i], method="lm", xtol=1e-15,
+                                      ftol=1e-15, gtol=1e-15, max_nfev=20000)
+        got = r["params"][i]
+        chi_ref = float(ref.fun @ ref.fun)
+        chi_got = float(o.get_fit_statistic(got))
+        # the reference statistic jumps by ~1e-8 where subsample counts switch
+        # (X0, Y0, PA, ell, r_e), so an FD-based and an analytic fit stop at
+        # points whose chi^2 differs at that level
+        assert chi_got <= chi_ref * (1 + 1e-7), (i, chi_got, chi_ref)
+        g = _single(gpu.ModelObject, d, s, p)
+        _, A, _ = g.jtwj(got)
+        sigma = np.sqrt(np.diag(np.linalg.inv(A)))
+        tol = np.maximum(1e-4 * np.abs(ref.x), 0.02 * sigma)
+        assert np.all(np.abs(got - ref.x) <= tol), (i, list(zip(got, ref.x, sigma)))

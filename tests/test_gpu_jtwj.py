@@ -131,7 +131,7 @@ def _n3073(gpu):
 def test_lm_fit_reproduces_mpfit_on_n3073(gpu):
     m, d = _n3073(gpu)
     r = m.fit_lm(d["params"], lower=d["lo"], upper=d["hi"], ftol=1e-8)
-    assert r["status"] in (1, 2, 3), r
+    assert r["status"] in (1, 3, 4), r
     want = d["lm_params"]
     err = np.abs(r["params"] - want) / np.abs(want)
     assert np.all(err < 2e-4), list(zip(m.parameter_names(), r["params"], want, err))
