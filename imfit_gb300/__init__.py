@@ -67,6 +67,8 @@ _SIGS = [
     ("imfit_GetResidualImageVector", _I, [_P, _DP]),
     ("imfit_GetWeightImageVector", _I, [_P, _DP]),
     ("imfit_GetDataVector", _I, [_P, _DP]),
+    ("imfit_GetSingleFunctionImage", _I, [_P, _DP, _I, _DP]),
+    ("imfit_FindTotalFluxes", _I, [_P, _DP, _I, _I, _DP, _DP]),
     ("imfit_UseBootstrap", _I, [_P, ctypes.c_ulong]),
     ("imfit_MakeBootstrapSample", _I, [_P]),
     ("imfit_GetFitStatisticAndGradientFD", _I, [_P, _DP, _DP, _DP]),
@@ -307,6 +309,22 @@ class ModelObject:
         s = _D()
         self._ck(self.lib.imfit_GetFitStatistic(self.h, _dp(p), ctypes.byref(s)))
         return s.value
+
+    def get_single_function_image(self, params, function_index):
+        p = _f64(params)
+        out = np.empty((self.nrows, self.ncols))
+        self._ck(self.lib.imfit_GetSingleFunctionImage(self.h, _dp(p), int(function_index), _dp(out)))
+        return out
+
+    def find_total_fluxes(self, params, xsize, ysize):
+        """(total, per-function fluxes) as ModelObject::FindTotalFluxes."""
+        p = _f64(params)
+        nf = self.lib.imfit_GetNFunctions(self.h)
+        ind = np.empty(nf)
+        tot = _D()
+        self._ck(self.lib.imfit_FindTotalFluxes(self.h, _dp(p), int(xsize), int(ysize), _dp(ind),
+                                                ctypes.byref(tot)))
+        return tot.value, ind
 
     def use_bootstrap(self, seed):
         return self._ck(self.lib.imfit_UseBootstrap(self.h, seed))

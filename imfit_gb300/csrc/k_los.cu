@@ -123,3 +123,42 @@ cudaError_t launch_los64(const CompF64 *comps, const LosList64 &list, double *ou
 }
 
 }  // namespace imfit
+
+namespace imfit {
+
+// FindTotalFluxes' grid integration (core/model_object.cpp:2415-2470): the sum
+// of one component's GetValue over an xSize x ySize image with IRAF pixel
+// centres (x = j+1, y = i+1).  Grid-stride over pixels, one FP64 partial per
+// block (tree reduction in a fixed order); the host adds the partials.
+__global__ void __launch_bounds__(256) k_flux64(CompF64 c, int xSize, int ySize, double *__restrict__ partials,
+                                                int *__restrict__ flag) {
+  __shared__ double red[256];
+  const long n = (long)xSize * ySize;
+  double acc = 0.0;
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
+    const long i = k / xSize, j = k - i * xSize;
+    const double x = (double)(j + 1), y = (double)(i + 1);
+    if (c.type == F_EXPDISK3D || c.type == F_FERRERS3D) {
+      int status = 0;
+      acc += los_value64(c, x, y, status);
+      if (status == kQagsCapped) atomicOr(flag, 1);
+    } else {
+      acc += comp_value64_2d(c, x, y);
+    }
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partials[blockIdx.x] = red[0];
+}
+
+cudaError_t launch_flux64(const CompF64 &c, int xSize, int ySize, double *partials, int nBlocks, int *flag,
+                          cudaStream_t st) {
+  k_flux64<<<nBlocks, 256, 0, st>>>(c, xSize, ySize, partials, flag);
+  return cudaGetLastError();
+}
+
+}  // namespace imfit

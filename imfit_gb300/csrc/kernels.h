@@ -77,6 +77,10 @@ struct LosList64 {
 // los[k3 * (nCols*nRows) + pixel]: value of the k3-th 3-D component (FP64 QAGS per pixel)
 cudaError_t launch_los64(const CompF64 *comps, const LosList64 &list, double *los, Grid64 g, int *flag,
                          cudaStream_t st);
+// sum of one component's values over an xSize x ySize grid (FindTotalFluxes);
+// nBlocks FP64 partials
+cudaError_t launch_flux64(const CompF64 &c, int xSize, int ySize, double *partials, int nBlocks, int *flag,
+                          cudaStream_t st);
 // model pixels; 3-D components are read from 'los' (may be null without them)
 cudaError_t launch_eval64(const CompF64 *comps, int nComp, double *model, long pitch, Grid64 g,
                           const double *los, cudaStream_t st);

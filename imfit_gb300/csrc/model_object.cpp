@@ -571,13 +571,141 @@ struct imfit_model_s {
 
   // line-of-sight values of the 3-D components on one model grid, then the pixel sum
   cudaError_t evalGrid(const CompF64 *dC, double *model, long pitch, const Grid64 &g) {
-    const int nC = (int)funcs.size();
-    if (losList.n == 0) return launch_eval64(dC, nC, model, pitch, g, nullptr, stream);
-    const size_t need = (size_t)losList.n * g.nCols * g.nRows;
+    return evalGridN(dC, (int)funcs.size(), losList, model, pitch, g);
+  }
+  cudaError_t evalGridN(const CompF64 *dC, int nC, const LosList64 &ll, double *model, long pitch,
+                        const Grid64 &g) {
+    if (ll.n == 0) return launch_eval64(dC, nC, model, pitch, g, nullptr, stream);
+    const size_t need = (size_t)ll.n * g.nCols * g.nRows;
     cudaError_t e = dLos.reserve(need);
-    if (!e) e = launch_los64(dC, losList, dLos.p, g, dLosFlag.p, stream);
+    if (!e) e = launch_los64(dC, ll, dLos.p, g, dLosFlag.p, stream);
     if (!e) e = launch_eval64(dC, nC, model, pitch, g, dLos.p, stream);
     return e;
+  }
+
+  // GetSingleFunctionImage (core/model_object.cpp:1241-1336): one function on
+  // the model grid, convolved (and its oversampled regions computed with that
+  // function alone), cropped to the data size.  Like the reference it leaves
+  // that image in the model buffer.
+  int singleFunctionImage(const double *params, int fi, double *out) {
+    int st = checkEval();
+    if (st) return st;
+    const int nC = (int)funcs.size();
+    if (fi < 0 || fi >= nC) return fail(IMFIT_E_ARG, "function index out of range");
+    for (int j = 0; j < nParamsTot; j++)
+      if (!std::isfinite(params[j])) return fail(IMFIT_E_ARG, "non-finite values in parameter vector");
+    hComps.resize(nC);
+    setupComps(params, hComps.data());
+    CompF64 one = hComps[fi];
+    LosList64 ll{};
+    if (one.type == F_EXPDISK3D || one.type == F_FERRERS3D) {
+      one.pad0 = 0;
+      ll.n = 1;
+      ll.comp[0] = 0;
+    }
+    cudaError_t e = dComps.reserve(std::max(nC, 1));
+    if (!e && ll.n && !hLosFlag) e = cudaMallocHost(&hLosFlag, sizeof(int));
+    if (!e && ll.n) e = dLosFlag.reserve(1);
+    if (!e && ll.n) e = cudaMemsetAsync(dLosFlag.p, 0, sizeof(int), stream);
+    if (!e) e = cudaMemcpyAsync(dComps.p, &one, sizeof(CompF64), cudaMemcpyHostToDevice, stream);
+    Grid64 g{};
+    g.nCols = nModelCols;
+    g.nRows = nModelRows;
+    g.pc = doConv ? nPsfCols : 0;
+    g.pr = doConv ? nPsfRows : 0;
+    if (!e) e = evalGridN(dComps.p, 1, ll, dModel.p, nModelCols, g);
+    if (!e && doConv) e = conv64(dModel.p, nModelCols, nModelRows, Lx, Ly, dH.p, dSpec.p);
+    for (Region *r : regions) {
+      if (e) break;
+      Grid64 rg{};
+      rg.nCols = r->nModelCols;
+      rg.nRows = r->nModelRows;
+      rg.pc = r->nPsfCols;
+      rg.pr = r->nPsfRows;
+      rg.isRegion = 1;
+      rg.x1 = r->x1;
+      rg.y1 = r->y1;
+      rg.frac = 1.0 / r->scale;
+      rg.off = 0.5 * rg.frac - 0.5;
+      e = evalGridN(dComps.p, 1, ll, r->model.p, r->nModelCols, rg);
+      if (!e) e = conv64(r->model.p, r->nModelCols, r->nModelRows, r->Lx, r->Ly, r->H.p, r->spec.p);
+      if (!e)
+        e = launch_downsample64(r->model.p, r->nModelCols, r->nModelRows, r->nPsfCols, r->nPsfRows, dModel.p,
+                                nModelCols, nModelRows, doConv ? nPsfCols : 0, doConv ? nPsfRows : 0, r->x1, r->y1,
+                                r->scale, stream);
+    }
+    DevBuf<double> tmp;
+    if (!e) e = tmp.reserve(nDataVals);
+    if (!e)
+      e = launch_crop64(dModel.p, nModelCols, doConv ? nPsfRows : 0, doConv ? nPsfCols : 0, nDataCols, nDataRows,
+                        tmp.p, stream);
+    if (!e) e = cudaMemcpyAsync(out, tmp.p, sizeof(double) * nDataVals, cudaMemcpyDeviceToHost, stream);
+    if (!e && ll.n) e = cudaMemcpyAsync(hLosFlag, dLosFlag.p, sizeof(int), cudaMemcpyDeviceToHost, stream);
+    if (!e) e = cudaStreamSynchronize(stream);
+    if (e) return cuda_fail(e, "GetSingleFunctionImage");
+    if (ll.n) {
+      st = losCheck();
+      if (st) return st;
+    }
+    modelComputed = true;
+    return 0;
+  }
+
+  // FindTotalFluxes (core/model_object.cpp:2415-2470): every function centred
+  // on an xSize x ySize image; the analytic TotalFlux where the class has one
+  // (Sersic func_sersic.cpp:246-251, Exponential func_exp.cpp:210-213,
+  // Gaussian func_gaussian.cpp:216-219), otherwise the sum of its values over
+  // that image (on the GPU, FP64); backgrounds count zero.
+  int findTotalFluxes(const double *params, int xSize, int ySize, double *indiv, double *total) {
+    constexpr double kPi = 3.14159265358979;  // the function classes' PI (func_sersic.cpp:65)
+    if (!setsDefined) return fail(IMFIT_E_STATE, "DefineFunctionSets not called");
+    if (xSize < 1 || ySize < 1) return fail(IMFIT_E_ARG, "bad image size");
+    const int nC = (int)funcs.size();
+    const double xc = 0.5 * xSize, yc = 0.5 * ySize;
+    constexpr int kBlocks = 1024;
+    DevBuf<double> part;
+    cudaError_t e = part.reserve(kBlocks);
+    if (!e) e = dLosFlag.reserve(1);
+    if (!e && !hLosFlag) e = cudaMallocHost(&hLosFlag, sizeof(int));
+    if (!e) e = cudaMemsetAsync(dLosFlag.p, 0, sizeof(int), stream);
+    if (e) return cuda_fail(e, "FindTotalFluxes");
+    std::vector<double> hp(kBlocks);
+    double sum = 0.0;
+    for (int f = 0; f < nC; f++) {
+      const double *p = params + paramOffset[f];
+      CompF64 c;
+      comp_setup64(c, funcs[f].type, funcs[f].subsample, p, xc, yc);
+      double flux = 0.0;
+      const int t = funcs[f].type;
+      if (t == F_FLATSKY) {
+        flux = 0.0;
+      } else if (t == F_SERSIC) {
+        const double n = p[2], I_e = p[3], r_e = p[4], q = 1.0 - p[1], bn = sersic_bn(n);
+        const double bn2n = pow(bn, 2.0 * n);
+        const double L = 2 * kPi * n * exp(bn) * I_e * (r_e * r_e);
+        flux = q * L * std::tgamma(2 * n) / bn2n;
+      } else if (t == F_EXP) {
+        flux = (1.0 - p[1]) * 2.0 * kPi * p[2] * p[3] * p[3];
+      } else if (t == F_GAUSS) {
+        flux = (1.0 - p[1]) * 2.0 * kPi * p[2] * p[3] * p[3];
+      } else {
+        e = launch_flux64(c, xSize, ySize, part.p, kBlocks, dLosFlag.p, stream);
+        if (!e) e = cudaMemcpyAsync(hp.data(), part.p, sizeof(double) * kBlocks, cudaMemcpyDeviceToHost, stream);
+        if (!e) e = cudaMemcpyAsync(hLosFlag, dLosFlag.p, sizeof(int), cudaMemcpyDeviceToHost, stream);
+        if (!e) e = cudaStreamSynchronize(stream);
+        if (e) return cuda_fail(e, "FindTotalFluxes");
+        for (double v : hp) flux += v;
+        if (*hLosFlag) {
+          *hLosFlag = 0;
+          return fail(IMFIT_E_UNSUPPORTED, "a line-of-sight integral needed more subintervals than the device "
+                                           "QAGS list holds (64)");
+        }
+      }
+      if (indiv) indiv[f] = flux;
+      sum += flux;
+    }
+    if (total) *total = sum;
+    return 0;
   }
 
   // after a synchronize: did a line-of-sight integral run out of subintervals?
@@ -1796,6 +1924,19 @@ int imfit_SetupImageStack(imfit_model_t m, int nImg, int nc, int nr, const doubl
                           const double *psfs, int pc, int pr) {
   GET(m);
   return m->setupStack(nImg, nc, nr, pix, sig, psfs, pc, pr);
+}
+
+int imfit_GetSingleFunctionImage(imfit_model_t m, const double *params, int fi, double *out) {
+  GET(m);
+  if (!params || !out) return m->fail(IMFIT_E_ARG, "null argument");
+  return m->singleFunctionImage(params, fi, out);
+}
+
+int imfit_FindTotalFluxes(imfit_model_t m, const double *params, int xSize, int ySize, double *indiv,
+                          double *total) {
+  GET(m);
+  if (!params) return m->fail(IMFIT_E_ARG, "null argument");
+  return m->findTotalFluxes(params, xSize, ySize, indiv, total);
 }
 
 int imfit_Synchronize(imfit_model_t m) {

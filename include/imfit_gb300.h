@@ -137,6 +137,16 @@ int imfit_GetExpandedModelImageVector(imfit_model_t m, double *out);
 int imfit_GetResidualImageVector(imfit_model_t m, double *out);
 /* ModelObject::GetWeightImageVector (core/model_object.cpp:2359): 1/sigma^2 */
 int imfit_GetWeightImageVector(imfit_model_t m, double *out);
+/* ModelObject::GetSingleFunctionImage (core/model_object.cpp:1241): the image
+ * of function functionIndex alone (convolved, oversampled regions included),
+ * data-sized; like the reference it replaces the stored model image. */
+int imfit_GetSingleFunctionImage(imfit_model_t m, const double *params, int functionIndex, double *out);
+/* ModelObject::FindTotalFluxes (core/model_object.cpp:2415): each function
+ * centred on an xSize x ySize image, its analytic TotalFlux where the class
+ * has one, otherwise the sum of its values over that image (FP64, GPU);
+ * individualFluxes (GetNFunctions() values) and totalFlux may be NULL. */
+int imfit_FindTotalFluxes(imfit_model_t m, const double *params, int xSize, int ySize, double *individualFluxes,
+                          double *totalFlux);
 /* ModelObject::GetDataVector (core/model_object.cpp:2383) */
 int imfit_GetDataVector(imfit_model_t m, double *out);
 /* ModelObject::UseBootstrap (core/model_object.cpp:2042), seeding MT19937 like

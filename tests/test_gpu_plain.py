@@ -231,3 +231,51 @@ def test_call_order_and_input_errors(gpu):
     assert m3.final_setup() == -3
     with pytest.raises(gpu.ImfitError):
         m3.get_model_image()  # not computed yet
+
+
+def test_single_function_images_sum_to_the_model(gpu, oracle_mod):
+    """GetSingleFunctionImage: with convolution and an oversampled region the
+    per-function images add up to the model image (the pipeline is linear)."""
+    from imfit_gb300 import workloads
+    wl = workloads.small_case(seed=3, region=True)
+    workloads.synthesize(wl, oracle_mod.OracleModel)
+    m = workloads.configure(gpu.ModelObject(), wl)
+    m.create_model_image(wl.start)
+    full = m.get_model_image()
+    parts = [m.get_single_function_image(wl.start, i) for i in range(len(wl.functions))]
+    assert np.max(np.abs(sum(parts) - full)) <= 1e-12 * np.max(np.abs(full))
+    # a background alone is flat (I_sky times the PSF sum), shown here without the region
+    sky = parts[-1]
+    assert np.allclose(sky[0, 0], wl.start[-1], rtol=1e-12)
+
+
+def test_find_total_fluxes(gpu, oracle_mod):
+    """FindTotalFluxes: analytic Sersic/Exponential (against the oracle's
+    TotalFlux restatement); grid integration for a Moffat against the sum of
+    the oracle's GetValue over the same grid (the reference's integration,
+    subsampling included), and against the closed form
+    pi alpha^2 I_0 q / (beta - 1) to the accuracy of that pixel sum."""
+    m = gpu.ModelObject()
+    m.add_function("Sersic", True)
+    m.add_function("Exponential")
+    m.add_function("Moffat")
+    m.add_function("FlatSky")
+    m.finish_functions()
+    m.setup_model_image(10, 10)
+    sersic = [30.0, 0.2, 2.5, 10.0, 12.0]
+    exp_ = [50.0, 0.4, 5.0, 20.0]
+    moffat = [10.0, 0.1, 100.0, 4.0, 4.0]
+    p = [5.0, 5.0] + sersic + exp_ + moffat + [3.0]
+    size = 241
+    total, ind = m.find_total_fluxes(p, size, size)
+    assert relerr(ind[0], oracle_mod.function_total_flux("Sersic", sersic)) < 1e-12
+    assert relerr(ind[1], oracle_mod.function_total_flux("Exponential", exp_)) < 1e-12
+    c = 0.5 * size
+    ref = sum(oracle_mod.function_value("Moffat", moffat, c, c, float(j + 1), float(i + 1))
+              for i in range(size) for j in range(size))
+    assert relerr(ind[2], ref) < 1e-12
+    fwhm, beta, q = 4.0, 4.0, 0.9
+    alpha = fwhm / (2.0 * np.sqrt(2.0 ** (1.0 / beta) - 1.0))
+    assert relerr(ind[2], np.pi * alpha ** 2 * 100.0 * q / (beta - 1.0)) < 2e-3
+    assert ind[3] == 0.0
+    assert relerr(total, ind.sum()) < 1e-15
