@@ -58,6 +58,18 @@ def parse():
     return ap.parse_args()
 
 
+def max_over_ranks(value, world):
+    """Largest value over the ranks (replicas are timed separately; the job
+    takes as long as its slowest rank).  gloo on the host, no GPU collective."""
+    if world <= 1:
+        return float(value)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_info():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
 
@@ -295,12 +307,7 @@ def run_gpu(args, rank, local_rank, world):
     clk = clocks.stop()
     for a, b in ev:
         times.append(a.elapsed_time(b))
-    t_ms = float(np.sum(times))
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([t_ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_ms = float(t.item())
+    t_ms = max_over_ranks(float(np.sum(times)), world)
     value = world * B * args.steps / (t_ms / 1e3)
     m.set_kernel_timing(False)
 
@@ -327,6 +334,7 @@ def run_gpu(args, rank, local_rank, world):
         st = lib.imfit_BatchFitStatisticAndGradient(m.h, B, pp, ps, pg)
         e2e_t += time.perf_counter() - t0
         assert st == 0
+    e2e_t = max_over_ranks(e2e_t, world)
     e2e = world * B * args.steps / e2e_t
     lib.imfit_HostFree(hp)
 
@@ -341,6 +349,7 @@ def run_gpu(args, rank, local_rank, world):
         t0 = time.perf_counter()
         m.statistic_and_gradient_fd(p0)
         pt += time.perf_counter() - t0
+    pt = max_over_ranks(pt, world)
     plain = args.plain_steps / pt
 
     # roofline of the dominant kernel
@@ -422,11 +431,7 @@ def run_c5(args, rank, local_rank, world):
     torch.cuda.synchronize()
     t_fit = time.perf_counter() - t0
     clk = clocks.stop()
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([t_fit], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_fit = float(t.item())
+    t_fit = max_over_ranks(t_fit, world)
     value = world * len(items) * args.steps / t_fit
     # accuracy: FP64 fits of the smallest few cutouts
     acc = None
