@@ -150,6 +150,16 @@ __device__ __forceinline__ cplx<T> twiddle(const cplx<T> *tw, int idx, int s) {
   return w;
 }
 
+// Division by a divisor fixed for a loop: q = floor(x / d) as the high word
+// of x * ceil(2^32 / d) (exact while x * d < 2^32, which holds for every
+// index here: x < 2^16, d <= 4096).
+struct FastDiv {
+  unsigned m;
+  int d;
+  __device__ __forceinline__ explicit FastDiv(int dd) : m(dd > 1 ? 0xFFFFFFFFu / (unsigned)dd + 1u : 0u), d(dd) {}
+  __device__ __forceinline__ int div(int x) const { return d > 1 ? (int)__umulhi((unsigned)x, m) : x; }
+};
+
 // One radix-R Stockham pass over 'nl' lines of length n.
 // Element t of line l lives at buf[l*ls + t*es].
 template <typename T, int R>
@@ -159,16 +169,17 @@ __device__ __forceinline__ void stockham_pass(const cplx<T> *__restrict__ src, c
   const int m = n / R;
   const int total = m * nl;
   const int twStep = n / (Ns * R);
+  const FastDiv byNl(nl), byM(m), byNs(Ns);
   for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
     int l, j;
     if (lineFastest) {
-      l = idx % nl;
-      j = idx / nl;
+      j = byNl.div(idx);
+      l = idx - j * nl;
     } else {
-      j = idx % m;
-      l = idx / m;
+      l = byM.div(idx);
+      j = idx - l * m;
     }
-    const int k = j % Ns;
+    const int k = j - byNs.div(j) * Ns;
     const cplx<T> *in = src + l * ls;
     cplx<T> v[R];
 #pragma unroll

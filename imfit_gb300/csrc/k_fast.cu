@@ -1196,7 +1196,7 @@ cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool 
     STAGE("region_eval_r2c", rs, launch_eval(a, rw, *p.Rx, nBatch, 1, tu, rs));
     STAGE("region_cols_conv", rs,
           launch_cols<float>(a.rspec, g.rSpecPitch, g.rSpecBatch, p.Rx->L / 2 + 1, g.rWinRows, g.rSubRows, p.Hr,
-                             p.hrPitch, *p.Ry, rscale, 1, nBatch, rs, tu.colCpb));
+                             p.hrPitch, *p.Ry, rscale, 1, nBatch, rs, tu.colCpb, 0, 1, nullptr, tu.colThreads));
     STAGE("region_down", rs, launch_region_down(p, a, nBatch, rs));
   }
   STAGE("subsample", st, launch_subsample(a, mw, 0, nBatch, st));
@@ -1204,7 +1204,7 @@ cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool 
   STAGE("eval_r2c", st, launch_eval(a, mw, *p.Lx, nBatch, 0, tu, st));
   STAGE("cols_conv", st,
         launch_cols<float>(a.spec, g.specPitch, g.specBatch, p.Lx->L / 2 + 1, g.winRows, g.nDataRows, p.H, p.hPitch,
-                           *p.Ly, scale, 1, nBatch, st, tu.colCpb, p.hBatch, 1, p.hMap));
+                           *p.Ly, scale, 1, nBatch, st, tu.colCpb, p.hBatch, 1, p.hMap, tu.colThreads));
   if (fork) {
     cudaError_t e = cudaEventRecord(p.join0, rs);
     if (!e) e = cudaStreamWaitEvent(st, p.join0, 0);
@@ -1224,13 +1224,13 @@ cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool 
     STAGE("region_g_r2c", rs, launch_region_g(p, a, nBatch, rs));
     STAGE("region_cols_adjoint", rs,
           launch_cols<float>(a.rspec, g.rSpecPitch, g.rSpecBatch, p.Rx->L / 2 + 1, g.rSubRows, g.rWinRows, p.Hr,
-                             p.hrPitch, *p.Ry, rscale, 2, nBatch, rs, tu.colCpb));
+                             p.hrPitch, *p.Ry, rscale, 2, nBatch, rs, tu.colCpb, 0, 1, nullptr, tu.colThreads));
     STAGE("region_grad_rows", rs, launch_grad(a, rw, *p.Rx, nBatch, nMain, 1, tu, rs));
     if (los) STAGE("region_los_grad", rs, launch_los_grad(a, rw, nBatch, nMain + nReg + kLosCtas, rs));
   }
   STAGE("cols_adjoint", st,
         launch_cols<float>(a.spec, g.specPitch, g.specBatch, p.Lx->L / 2 + 1, g.nDataRows, g.winRows, p.H, p.hPitch,
-                           *p.Ly, scale, 2, nBatch, st, tu.colCpb, p.hBatch, 1, p.hMap));
+                           *p.Ly, scale, 2, nBatch, st, tu.colCpb, p.hBatch, 1, p.hMap, tu.colThreads));
   STAGE("grad_rows", st, launch_grad(a, mw, *p.Lx, nBatch, 0, 0, tu, st));
   if (los) STAGE("los_grad", st, launch_los_grad(a, mw, nBatch, nMain + nReg, st));
   if (fork) {
@@ -1288,7 +1288,7 @@ cudaError_t fast_jtwj(const FastPlan &p, const FastArgs &a, const JtwjArgs &J, i
       STAGE("jtwj_region_deriv_r2c", st, launch_deriv(a, region_win(g, J.drspec), *p.Rx, nBatch, 1, J, st));
       STAGE("jtwj_region_cols", st,
             launch_cols<float>(J.drspec, g.rSpecPitch, g.rSpecBatch, p.Rx->L / 2 + 1, g.rWinRows, g.rSubRows, p.Hr,
-                               p.hrPitch, *p.Ry, rscale, 1, nB, st, tu.colCpb));
+                               p.hrPitch, *p.Ry, rscale, 1, nB, st, tu.colCpb, 0, 1, nullptr, tu.colThreads));
       const int M = p.Rx->half.n;
       const size_t sm = sizeof(cplx<float>) * 3 * g.rScale * (M + 1);
       stage_begin(p, "jtwj_region_down", st);
@@ -1302,7 +1302,7 @@ cudaError_t fast_jtwj(const FastPlan &p, const FastArgs &a, const JtwjArgs &J, i
     STAGE("jtwj_deriv_r2c", st, launch_deriv(a, main_win(g, J.dspec), *p.Lx, nBatch, 0, J, st));
     STAGE("jtwj_cols", st,
           launch_cols<float>(J.dspec, g.specPitch, g.specBatch, p.Lx->L / 2 + 1, g.winRows, g.nDataRows, p.H,
-                             p.hPitch, *p.Ly, scale, 1, nB, st, tu.colCpb, p.hBatch, nD, p.hMap));
+                             p.hPitch, *p.Ly, scale, 1, nB, st, tu.colCpb, p.hBatch, nD, p.hMap, tu.colThreads));
   }
   const int M = p.Lx->half.n;
   const size_t sm = jtwj_rows_smem(M, nD, g.nDataCols, kJtwjThreads);

@@ -65,13 +65,14 @@ __global__ void __launch_bounds__(1024) k_cols(cplx<T> *__restrict__ spec, long 
   const int c0 = blockIdx.x * cpb;
   const int nl = min(cpb, nColsC - c0);
   if (nl <= 0) return;
+  const FastDiv byCpb(cpb);
   spec += blockIdx.y * batch;
   if (hBatch) {
     const int e = blockIdx.y / hDiv;
     H += (long)(hMap ? hMap[e] : e) * hBatch;
   }
   for (int idx = threadIdx.x; idx < Ly * cpb; idx += blockDim.x) {
-    const int t = idx / cpb, f = idx % cpb;
+    const int t = byCpb.div(idx), f = idx - t * cpb;
     cplx<T> v = {(T)0, (T)0};
     if (t < nRowsIn && f < nl) v = spec[(long)t * pitch + c0 + f];
     bufA[t * cpb + f] = v;
@@ -80,12 +81,12 @@ __global__ void __launch_bounds__(1024) k_cols(cplx<T> *__restrict__ spec, long 
   cplx<T> *X = block_fft(bufA, bufB, plan, cpb, 1, cpb, -1, true);
   if constexpr (MODE == 0) {
     for (int idx = threadIdx.x; idx < Ly * cpb; idx += blockDim.x) {
-      const int t = idx / cpb, f = idx % cpb;
+      const int t = byCpb.div(idx), f = idx - t * cpb;
       if (f < nl) spec[(long)t * pitch + c0 + f] = X[t * cpb + f];
     }
   } else {
   for (int idx = threadIdx.x; idx < Ly * cpb; idx += blockDim.x) {
-    const int t = idx / cpb, f = idx % cpb;
+    const int t = byCpb.div(idx), f = idx - t * cpb;
     if (f < nl) {
       cplx<T> h = H[(long)t * hPitch + c0 + f];
       if (MODE == 2) h.y = -h.y;
@@ -99,7 +100,7 @@ __global__ void __launch_bounds__(1024) k_cols(cplx<T> *__restrict__ spec, long 
   cplx<T> *other = (X == bufA) ? bufB : bufA;
   cplx<T> *Y = block_fft(X, other, plan, cpb, 1, cpb, +1, true);
   for (int idx = threadIdx.x; idx < nRowsOut * cpb; idx += blockDim.x) {
-    const int t = idx / cpb, f = idx % cpb;
+    const int t = byCpb.div(idx), f = idx - t * cpb;
     if (f < nl) spec[(long)t * pitch + c0 + f] = Y[t * cpb + f];
   }
   }
@@ -198,13 +199,14 @@ int cols_per_block(int Ly, int elemBytes, int nColsC) {
 template <typename T>
 cudaError_t launch_cols(void *spec, long pitch, long batch, int nColsC, int nRowsIn, int nRowsOut,
                         const void *H, long hPitch, const FFTLen &Ly, T scale, int mode, int nBatch,
-                        cudaStream_t st, int cpbOverride, long hBatch, int hDiv, const int *hMap) {
+                        cudaStream_t st, int cpbOverride, long hBatch, int hDiv, const int *hMap,
+                        int threadsOverride) {
   const int L = Ly.full.n;
   int cpb = cpbOverride > 0 ? cpbOverride : cols_per_block(L, sizeof(T), nColsC);
   while (cpb > 1 && (size_t)2 * L * cpb * 2 * sizeof(T) > 200 * 1024) cpb >>= 1;
   const size_t sm = sizeof(cplx<T>) * 2 * (size_t)L * cpb;
   dim3 grid((nColsC + cpb - 1) / cpb, nBatch);
-  const int nt = line_threads(L * cpb / 2);
+  const int nt = threadsOverride > 0 ? threadsOverride : line_threads(L * cpb / 2);
   auto p = plan_of<T>(Ly, false);
   cplx<T> *s = reinterpret_cast<cplx<T> *>(spec);
   const cplx<T> *h = reinterpret_cast<const cplx<T> *>(H);
@@ -241,9 +243,9 @@ template cudaError_t launch_rows_r2c<double>(const double *, long, long, int, in
 template cudaError_t launch_rows_r2c<float>(const float *, long, long, int, int, void *, long, long,
                                             const FFTLen &, int, cudaStream_t);
 template cudaError_t launch_cols<double>(void *, long, long, int, int, int, const void *, long,
-                                         const FFTLen &, double, int, int, cudaStream_t, int, long, int, const int *);
+                                         const FFTLen &, double, int, int, cudaStream_t, int, long, int, const int *, int);
 template cudaError_t launch_cols<float>(void *, long, long, int, int, int, const void *, long,
-                                        const FFTLen &, float, int, int, cudaStream_t, int, long, int, const int *);
+                                        const FFTLen &, float, int, int, cudaStream_t, int, long, int, const int *, int);
 template cudaError_t launch_rows_c2r<double>(const void *, long, long, int, double *, long, long, int,
                                              double, const FFTLen &, int, cudaStream_t);
 template cudaError_t launch_rows_c2r<float>(const void *, long, long, int, float *, long, long, int, float,

@@ -50,7 +50,7 @@ template <typename T>
 cudaError_t launch_cols(void *spec, long pitch, long batch, int nColsC, int nRowsIn, int nRowsOut,
                         const void *H, long hPitch, const FFTLen &Ly, T scale, int mode, int nBatch,
                         cudaStream_t st, int cpbOverride = 0, long hBatch = 0, int hDiv = 1,
-                        const int *hMap = nullptr);
+                        const int *hMap = nullptr, int threadsOverride = 0);
 template <typename T>
 cudaError_t launch_rows_c2r(const void *in, long inPitch, long inBatch, int nRows, T *out, long outPitch,
                             long outBatch, int outCols, T scale, const FFTLen &Lx, int nBatch,
@@ -201,6 +201,7 @@ struct FastTune {
   int rowRpb = 3;        // window rows per CTA (eval, statistic, gradient kernels)
   int rowThreads = 256;  // threads per row CTA
   int colCpb = 0;        // half-spectrum columns per CTA (0: automatic)
+  int colThreads = 0;    // threads per column CTA (0: one per complex point pair, <= 1024)
 };
 
 struct FastPlan {

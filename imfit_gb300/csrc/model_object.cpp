@@ -1228,14 +1228,17 @@ struct imfit_model_s {
       if (e) break;
       if (ms < bestMs) { bestMs = ms; bestT = t; }
     }
-    for (int cpb : {1, 2, 4}) {
-      if (e) break;
-      FastTune t = bestT;
-      t.colCpb = cpb;
-      float ms;
-      e = measure(t, ms);
-      if (e) break;
-      if (ms < bestMs) { bestMs = ms; bestT = t; }
+    for (int cpb : {1, 2, 4, 8}) {
+      for (int nt : {0, 256, 512}) {
+        if (e) break;
+        FastTune t = bestT;
+        t.colCpb = cpb;
+        t.colThreads = nt;
+        float ms;
+        e = measure(t, ms);
+        if (e) break;
+        if (ms < bestMs) { bestMs = ms; bestT = t; }
+      }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
