@@ -58,6 +58,16 @@ def parse():
     return ap.parse_args()
 
 
+def measured_traffic(config, stage):
+    """DRAM bytes per launch of a stage from the committed ncu summary (or None)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic_per_launch.json")) as f:
+            v = json.load(f).get(config, {}).get(stage)
+        return float(v) if v is not None else None
+    except (OSError, ValueError):
+        return None
+
+
 def max_over_ranks(value, world):
     """Largest value over the ranks (replicas are timed separately; the job
     takes as long as its slowest rank).  gloo on the host, no GPU collective."""
@@ -371,7 +381,7 @@ def run_gpu(args, rank, local_rank, world):
     roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
             "frac": round(achieved / hbm_peak, 4), "peak_source": peak_src,
             "algorithmic_bytes_per_launch": B * ab.get(dom, 0), "kernel_ms_in_timed_region": round(dom_avg, 5),
-            "traffic": None}
+            "traffic": measured_traffic(args.config, dom)}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
