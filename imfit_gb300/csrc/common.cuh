@@ -261,11 +261,12 @@ __host__ __device__ inline double comp_value64_2d(const CompF64 &c, double x, do
 // FP32 fast form.
 //
 // Type-specific fields of CompF32 (all derived in FP64, rounded once):
-//   Sersic:   s0=I_e s1=B=bn*log2(e) s2=log2(r_e) s3=1/n s4=bn s5=dbn/dn s6=n s7=r_e
-//   Exp:      s0=I_0 s1=log2(e)/h s2=h
-//   GRing:    s0=A s1=R s2=log2(e)/(2 sigma^2) s3=sigma
-//   Moffat:   s0=I_0 s1=1/alpha^2 s2=beta s3=alpha s4=fwhm s5=d(alpha)/d(beta)
-//   Gaussian: s0=I_0 s1=log2(e)/(2 sigma^2) s2=sigma
+//   Sersic:   s0=I_e s1=B=bn*log2(e) s2=log2(r_e) s3=1/n s4=bn s5=dbn/dn s6=n s7=r_e pad=1/r_e
+//   Exp:      s0=I_0 s1=log2(e)/h s2=h s3=1/h
+//   GRing:    s0=A s1=R s2=log2(e)/(2 sigma^2) s3=sigma s4=1/sigma^2 pad=1/sigma
+//   Moffat:   s0=I_0 s1=1/alpha^2 s2=beta s3=alpha s4=fwhm s5=d(alpha)/d(beta) s6=1/alpha s7=1/fwhm
+//   Gaussian: s0=I_0 s1=log2(e)/(2 sigma^2) s2=sigma s3=1/sigma s4=1/sigma^2
+// (reciprocals are formed in FP64 at setup so the pixel loops divide nowhere)
 //   FlatSky:  s0=I_sky
 //   ExpDisk3D:    s0=J_0 s1=1/h s2=h s3=cos(inc) s4=sin(inc) s5=alpha=2/n
 //                 s6=1/(alpha z_0) s7=z_0 subScale=n subInner=20h (half-range)
@@ -331,6 +332,7 @@ __device__ inline void comp_setup32(CompF32 &o, const CompDesc &d, const double 
       o.s6 = (float)n;
       o.s7 = (float)p[4];
       o.subScale = (float)p[4]; o.subInner = 4.f; o.subSmallK = 20.f;
+      o.pad = (float)(1.0 / p[4]);  // 1/r_e
       break;
     }
     case F_EXP: {
@@ -339,6 +341,7 @@ __device__ inline void comp_setup32(CompF32 &o, const CompDesc &d, const double 
       o.s0 = (float)p[2];
       o.s1 = (float)(kLog2e / p[3]);
       o.s2 = (float)p[3];
+      o.s3 = (float)(1.0 / p[3]);  // 1/h
       o.subScale = (float)p[3]; o.subInner = 3.f; o.subSmallK = 20.f;
       break;
     }
@@ -352,6 +355,8 @@ __device__ inline void comp_setup32(CompF32 &o, const CompDesc &d, const double 
       o.s1 = (float)p[3];
       o.s2 = (float)(kLog2e / (2.0 * p[4] * p[4]));
       o.s3 = (float)p[4];
+      o.s4 = (float)(1.0 / (p[4] * p[4]));  // 1/sigma^2
+      o.pad = (float)(1.0 / p[4]);          // 1/sigma
       break;
     }
     case F_MOFFAT: {
@@ -365,6 +370,8 @@ __device__ inline void comp_setup32(CompF32 &o, const CompDesc &d, const double 
       o.s3 = (float)alpha;
       o.s4 = (float)fwhm;
       o.s5 = (float)(alpha * t * kLn2 / (2.0 * beta * beta * (t - 1.0)));
+      o.s6 = (float)(1.0 / alpha);
+      o.s7 = (float)(1.0 / fwhm);
       o.subScale = (float)alpha; o.subInner = 3.f; o.subSmallK = 40.f;
       break;
     }
@@ -374,6 +381,8 @@ __device__ inline void comp_setup32(CompF32 &o, const CompDesc &d, const double 
       o.s0 = (float)p[2];
       o.s1 = (float)(kLog2e / (2.0 * p[3] * p[3]));
       o.s2 = (float)p[3];
+      o.s3 = (float)(1.0 / p[3]);  // 1/sigma
+      o.s4 = (float)(1.0 / (p[3] * p[3]));
       o.subScale = (float)p[3]; o.subInner = 3.f; o.subSmallK = 40.f;
       break;
     }
@@ -507,8 +516,9 @@ __device__ inline float comp_value32(const CompF32 &c, float dx, float dy, int *
 // out[0..1] = d/dX0, d/dY0; out[2..] = d/d(function parameters in order).
 // Returns the number of function parameters written after the two centre slots.
 __device__ inline int radial_grad32(const CompF32 &c, const Geo &g, float scale, float *out) {
-  const float r = fast_sqrt(g.r2);
-  const float rinv = (r > 0.f) ? 1.f / r : 0.f;
+  // 1/r from the SFU reciprocal square root, r = r2 / r (no IEEE division)
+  const float rinv = (g.r2 > 0.f) ? rsqrtf(g.r2) : 0.f;
+  const float r = g.r2 * rinv;
   float I, dIdr, np = 0;
   float pd[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // profile-parameter derivatives
   switch (c.type) {
@@ -524,16 +534,16 @@ __device__ inline int radial_grad32(const CompF32 &c, const Geo &g, float scale,
       float lnrr = (u > 0.f) ? (lr - c.s2) * (float)kLn2 : 0.f;
       pd[2] = -I * (c.s5 * (u - 1.f) - c.s4 * u * lnrr * c.s3 * c.s3);
       pd[3] = E;                 // d/dI_e
-      pd[4] = t / c.s7;          // d/dr_e = I bn u / (n r_e)
+      pd[4] = t * c.pad;         // d/dr_e = I bn u / (n r_e)
       np = 5;
       break;
     }
     case F_EXP: {
       float E = fast_ex2(-r * c.s1);
       I = c.s0 * E;
-      dIdr = -I / c.s2;
+      dIdr = -I * c.s3;
       pd[2] = E;                         // d/dI_0
-      pd[3] = I * r / (c.s2 * c.s2);     // d/dh
+      pd[3] = I * r * c.s3 * c.s3;       // d/dh
       np = 4;
       break;
     }
@@ -541,11 +551,11 @@ __device__ inline int radial_grad32(const CompF32 &c, const Geo &g, float scale,
       float dd = r - c.s1;
       float E = fast_ex2(-dd * dd * c.s2);
       I = c.s0 * E;
-      float is2 = 1.f / (c.s3 * c.s3);
+      const float is2 = c.s4;
       dIdr = -I * dd * is2;
       pd[2] = E;                              // d/dA
       pd[3] = I * dd * is2;                   // d/dR_ring
-      pd[4] = I * dd * dd * is2 / c.s3;       // d/dsigma_r
+      pd[4] = I * dd * dd * is2 * c.pad;      // d/dsigma_r
       np = 5;
       break;
     }
@@ -554,11 +564,11 @@ __device__ inline int radial_grad32(const CompF32 &c, const Geo &g, float scale,
       float lD = fast_lg2(D);
       float E = fast_ex2(-c.s2 * lD);
       I = c.s0 * E;
-      float Dinv = 1.f / D;
+      float Dinv = __fdividef(1.f, D);  // D >= 1
       dIdr = -2.f * I * c.s2 * r * c.s1 * Dinv;
-      float dIdalpha = 2.f * I * c.s2 * g.r2 * c.s1 * Dinv / c.s3;
+      float dIdalpha = 2.f * I * c.s2 * g.r2 * c.s1 * Dinv * c.s6;
       pd[2] = E;                                             // d/dI_0
-      pd[3] = dIdalpha * c.s3 / c.s4;                        // d/dfwhm
+      pd[3] = dIdalpha * c.s3 * c.s7;                        // d/dfwhm
       pd[4] = -I * lD * (float)kLn2 + dIdalpha * c.s5;       // d/dbeta
       np = 5;
       break;
@@ -566,10 +576,10 @@ __device__ inline int radial_grad32(const CompF32 &c, const Geo &g, float scale,
     case F_GAUSS: {
       float E = fast_ex2(-g.r2 * c.s1);
       I = c.s0 * E;
-      float is2 = 1.f / (c.s2 * c.s2);
+      const float is2 = c.s4;
       dIdr = -I * r * is2;
       pd[2] = E;                              // d/dI_0
-      pd[3] = I * g.r2 * is2 / c.s2;          // d/dsigma
+      pd[3] = I * g.r2 * is2 * c.s3;          // d/dsigma
       np = 4;
       break;
     }
@@ -586,7 +596,9 @@ __device__ inline int radial_grad32(const CompF32 &c, const Geo &g, float scale,
   out[2] = scale * G * (float)kDeg2Rad * g.xp * g.yp * (1.f - invq * invq);
   // dr/dell = ys^2 / (q r)
   out[3] = scale * G * g.ys * g.ys * invq;
-  for (int k = 2; k < np; k++) out[2 + k] = scale * pd[k];
+#pragma unroll
+  for (int k = 2; k < 6; k++)
+    if (k < np) out[2 + k] = scale * pd[k];
   return (int)np;
 }
 

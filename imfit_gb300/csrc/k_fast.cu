@@ -529,8 +529,9 @@ __global__ void __launch_bounds__(1024) k_fast_grad_rows(FastArgs a, WinDesc w, 
       const float *tab = a.subTab + sub_base(a, b, c, win);
       float acc[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
       float o[7];
+      const FastDiv byCols(w.cols);
       for (int idx = threadIdx.x; idx < npix; idx += blockDim.x) {
-        const int l = idx / w.cols, col = idx - l * w.cols;
+        const int l = byCols.div(idx), col = idx - l * w.cols;
         const int row = row0 + l;
         const float r = rt[2 * l * ls + col];
         float dx, dy;
@@ -552,7 +553,9 @@ __global__ void __launch_bounds__(1024) k_fast_grad_rows(FastArgs a, WinDesc w, 
             for (int t = 0; t < ns * ns; t++) {
               const Geo gs = geo32(cc, dx - 0.5f + (t / ns + 0.5f) * d, dy - 0.5f + (t % ns + 0.5f) * d);
               const int n2 = radial_grad32(cc, gs, r * d * d, o);
-              for (int q = 0; q < 2 + n2; q++) s7[q] += o[q];
+#pragma unroll
+              for (int q = 0; q < 7; q++)
+                if (q < 2 + n2) s7[q] += o[q];
             }
 #pragma unroll
             for (int q = 0; q < 7; q++) o[q] = s7[q];
