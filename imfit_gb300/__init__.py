@@ -77,6 +77,7 @@ _SIGS = [
     ("imfit_BatchFitStatisticAndGradient", _I, [_P, _I, _DP, _DP, _DP]),
     ("imfit_BatchFitStatisticAndGradientDevice", _I, [_P, _I, _P, _P, _P]),
     ("imfit_GetJtWJ", _I, [_P, _DP, _DP, _DP, _DP]),
+    ("imfit_GetJacobian", _I, [_P, _DP, _DP, _DP]),
     ("imfit_BatchJtWJDevice", _I, [_P, _I, _P, _P, _P, _P]),
     ("imfit_FitLM", _I, [_P, _DP, ctypes.POINTER(_I), _DP, _DP, _D, _I, _DP, ctypes.POINTER(_I),
                          ctypes.POINTER(_I), ctypes.POINTER(_I)]),
@@ -376,6 +377,16 @@ class ModelObject:
         b = np.empty(n)
         self._ck(self.lib.imfit_GetJtWJ(self.h, _dp(p), ctypes.byref(s), _dp(a), _dp(b)))
         return s.value, a, b
+
+    def jacobian(self, params):
+        """(J, deviates): J[j] = d dev / d param_j over the data pixels (analytic, FP32-evaluated)."""
+        p = _f64(params)
+        n = self.n_params
+        nd = self.nrows * self.ncols
+        J = np.empty((n, nd))
+        dev = np.empty(nd)
+        self._ck(self.lib.imfit_GetJacobian(self.h, _dp(p), _dp(J), _dp(dev)))
+        return J, dev
 
     def batch_jtwj_device(self, n_batch, d_params, d_stats, d_jtj, d_jtdev):
         """Device-pointer batched JtWJ (ints: raw device addresses); enqueues only."""

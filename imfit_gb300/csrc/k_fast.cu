@@ -851,7 +851,7 @@ __global__ void __launch_bounds__(1024) k_fast_jtwj_rows(FastArgs a, FastGeom g,
                                                         const cplx<float> *__restrict__ dspec,
                                                         const float *__restrict__ regDeriv,
                                                         const int *__restrict__ slot, int nD,
-                                                        float *__restrict__ part) {
+                                                        float *__restrict__ part, float *__restrict__ jac) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int b = blockIdx.y, row = blockIdx.x;
   const int M = plan.n, ls = M + 1, nP = a.nParams, nc = g.nDataCols;
@@ -898,6 +898,11 @@ __global__ void __launch_bounds__(1024) k_fast_jtwj_rows(FastArgs a, FastGeom g,
     cw[col] = cnt;
     cd[col] = cnt * dev;
     dv[col] = dev;
+    if (jac) {  // Jacobian columns [b][param][pixel] and the deviates [b][pixel] after them
+      float *jb = jac + (long)b * (nP + 1) * nPix;
+      for (int j = 0; j < nP; j++) jb[(long)j * nPix + zi] = ss[j] >= 0 ? U[(long)ss[j] * nc + col] : qb[col];
+      jb[(long)nP * nPix + zi] = dev;
+    }
   }
   __syncthreads();
   const int nPair = nP * (nP + 1) / 2, Q = nPair + nP + 1;
@@ -1312,7 +1317,7 @@ cudaError_t fast_jtwj(const FastPlan &p, const FastArgs &a, const JtwjArgs &J, i
   stage_begin(p, "jtwj_rows", st);
   k_fast_jtwj_rows<<<dim3(g.nDataRows, nBatch), kJtwjThreads, sm, st>>>(
       a, g, plan32(*p.Lx, true), reinterpret_cast<const cplx<float> *>(p.Lx->twL32),
-      reinterpret_cast<const cplx<float> *>(J.dspec), J.regDeriv, J.slot, nD, J.part);
+      reinterpret_cast<const cplx<float> *>(J.dspec), J.regDeriv, J.slot, nD, J.part, J.jac);
   if ((e = cudaGetLastError())) return e;
   stage_end(p, "jtwj_rows", st);
   const int nP = a.nParams, Q = nP * (nP + 1) / 2 + nP + 1;

@@ -231,6 +231,7 @@ struct JtwjArgs {
   double *alpha;     // [B][nP][nP]  J^T J
   double *beta;      // [B][nP]      J^T dev
   double *stat;      // [B]          sum dev^2 (the fit statistic)
+  float *jac;        // optional [B][nP + 1][nData]: d dev / d params, then the deviates
 };
 
 cudaError_t fast_setup(const FastArgs &a, int nBatch, cudaStream_t st);

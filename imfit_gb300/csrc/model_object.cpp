@@ -1326,7 +1326,8 @@ struct imfit_model_s {
   }
 
   // statistic, J^T J and J^T dev for B parameter vectors on the device
-  int enqueueJtwj(int B, const double *dP, double *dS, double *dA, double *dBt) {
+  // (jacOut, optional: [B][nP + 1][nData] FP32 Jacobian columns and deviates)
+  int enqueueJtwj(int B, const double *dP, double *dS, double *dA, double *dBt, float *jacOut = nullptr) {
     int st = prepareFast();
     if (st) return st;
     if (useCash && !pmlr)
@@ -1360,6 +1361,7 @@ struct imfit_model_s {
     J.alpha = dA;
     J.beta = dBt;
     J.stat = dS;
+    J.jac = jacOut;
     cudaError_t e = fast_jtwj(p, a, J, B, stream);
     if (e) return cuda_fail(e, "JtWJ launch");
     return 0;
@@ -1484,6 +1486,35 @@ struct imfit_model_s {
       if (status) status[i] = res[i].status;
     }
     return st < 0 ? st : 0;
+  }
+
+  // Jacobian of the deviates (mpfit's derivative vectors for side = 3,
+  // solvers/mpfit.cpp:1210-1232): column j of fjac (nDataVals values) is
+  // d dev / d param_j, FP32-evaluated, in the order ComputeDeviates writes.
+  int jacobianHost(const double *params, double *fjac, double *deviates) {
+    int st = prepareFast();
+    if (st) return st;
+    if (doBootstrap) return fail(IMFIT_E_UNSUPPORTED, "the Jacobian is per data pixel; not with a bootstrap sample");
+    if (stack.n) return fail(IMFIT_E_UNSUPPORTED, "the Jacobian is per image; use a single-image ModelObject");
+    st = ensureFastCap(1);
+    if (!st) st = ensureJtwjCap(1);
+    if (st) return st;
+    const int nP = nParamsTot;
+    DevBuf<float> jac;
+    cudaError_t e = jac.reserve((size_t)(nP + 1) * nDataVals);
+    if (!e) e = cudaMemcpyAsync(dParams.p, params, sizeof(double) * nP, cudaMemcpyHostToDevice, stream);
+    if (e) return cuda_fail(e, "Jacobian buffers");
+    curEntry = nullptr;
+    st = enqueueJtwj(1, dParams.p, dStat.p, dAlpha.p, dBeta.p, jac.p);
+    if (st) return st;
+    std::vector<float> h((size_t)(nP + 1) * nDataVals);
+    e = cudaMemcpyAsync(h.data(), jac.p, sizeof(float) * h.size(), cudaMemcpyDeviceToHost, stream);
+    if (!e) e = cudaStreamSynchronize(stream);
+    if (e) return cuda_fail(e, "Jacobian results");
+    for (size_t k = 0; k < (size_t)nP * nDataVals; k++) fjac[k] = h[k];
+    if (deviates)
+      for (long z = 0; z < nDataVals; z++) deviates[z] = h[(size_t)nP * nDataVals + z];
+    return 0;
   }
 
   int makeBootstrapSample() {
@@ -1879,6 +1910,12 @@ int imfit_BatchFitStatisticAndGradientDevice(imfit_model_t m, int B, const doubl
   GET(m);
   if (B < 1 || !dP || !dS) return m->fail(IMFIT_E_ARG, "bad batch arguments");
   return m->enqueueFast(B, dP, dS, dG);
+}
+
+int imfit_GetJacobian(imfit_model_t m, const double *params, double *fjac, double *deviates) {
+  GET(m);
+  if (!params || !fjac) return m->fail(IMFIT_E_ARG, "null argument");
+  return m->jacobianHost(params, fjac, deviates);
 }
 
 int imfit_GetJtWJ(imfit_model_t m, const double *params, double *s, double *jtj, double *jtdev) {

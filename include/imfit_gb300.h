@@ -186,6 +186,14 @@ int imfit_BatchFitStatisticAndGradientDevice(imfit_model_t m, int nBatch, const 
  * chi^2 (data, external or model-based errors) and Poisson-MLR; the Cash
  * statistic has no deviates and returns IMFIT_E_UNSUPPORTED. */
 int imfit_GetJtWJ(imfit_model_t m, const double *params, double *statistic, double *jtj, double *jtdev);
+/* Analytic Jacobian of the deviates by the same forward-mode pass: fjac is
+ * column-major, GetNDataValues() values per parameter, column j = d dev /
+ * d param_j in ComputeDeviates' order -- the derivative vectors mpfit takes
+ * from a user function for parameters with side = 3 (solvers/mpfit.cpp:1210-1232),
+ * replacing its finite differences.  deviates (may be NULL) receives the
+ * deviates at params (FP32-evaluated).  chi^2 and Poisson-MLR; not with a
+ * bootstrap sample, an image stack or 3-D components. */
+int imfit_GetJacobian(imfit_model_t m, const double *params, double *fjac, double *deviates);
 /* Batched form on DEVICE pointers (nBatch x nParams in, nBatch, nBatch x
  * nParams^2 and nBatch x nParams out), enqueued on the handle's stream. */
 int imfit_BatchJtWJDevice(imfit_model_t m, int nBatch, const double *d_params, double *d_statistics,

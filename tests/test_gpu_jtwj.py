@@ -152,3 +152,25 @@ def test_lm_fit_respects_fixed_and_limits(gpu):
     assert r["params"][6] <= 24.0
     assert np.all(r["params"] >= d["lo"]) and np.all(r["params"] <= hi)
     assert m.get_fit_statistic(r["params"]) < m.get_fit_statistic(p0)
+
+
+@pytest.mark.parametrize("region", [False, True])
+def test_jacobian_columns_vs_fd(gpu, oracle_mod, region):
+    """imfit_GetJacobian (mpfit side = 3 derivative vectors) against the
+    oracle's central-difference Jacobian of the deviates, column by column:
+    |J - J_fd| <= 2e-3 max|J_fd column| + 1e-6 max|J_fd|; deviates within
+    1e-5 of the oracle's (relative to their largest value)."""
+    wl = _case(oracle_mod, region=region, seed=53)
+    g = _build(gpu.ModelObject, wl)
+    o = _build(oracle_mod.OracleModel, wl)
+    J, dev = g.jacobian(wl.start)
+    J_fd = _fd_jacobian(o, wl.start)
+    dev_o = o.compute_deviates(wl.start)
+    assert np.max(np.abs(dev - dev_o)) <= 1e-5 * np.max(np.abs(dev_o))
+    top = np.max(np.abs(J_fd))
+    for j in range(J.shape[0]):
+        colmax = np.max(np.abs(J_fd[j]))
+        assert np.max(np.abs(J[j] - J_fd[j])) <= 2e-3 * colmax + 1e-6 * top, (g.parameter_names()[j], j)
+    # the normal equations from these columns are the JtWJ entry point's
+    s, A, b = g.jtwj(wl.start)
+    assert np.allclose(J @ J.T, A, rtol=1e-4, atol=1e-6 * np.max(np.abs(A)))
