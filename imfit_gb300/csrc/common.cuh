@@ -514,8 +514,10 @@ __device__ inline float comp_value32(const CompF32 &c, float dx, float dy, int *
 
 // Analytic derivatives of one radial component at squared radius r2:
 // out[0..1] = d/dX0, d/dY0; out[2..] = d/d(function parameters in order).
-// Returns the number of function parameters written after the two centre slots.
-__device__ inline int radial_grad32(const CompF32 &c, const Geo &g, float scale, float *out) {
+// Returns the number of function parameters written after the two centre slots;
+// *value (optional) receives the profile value itself.
+__device__ inline int radial_grad32(const CompF32 &c, const Geo &g, float scale, float *out,
+                                    float *value = nullptr) {
   // 1/r from the SFU reciprocal square root, r = r2 / r (no IEEE division)
   const float rinv = (g.r2 > 0.f) ? rsqrtf(g.r2) : 0.f;
   const float r = g.r2 * rinv;
@@ -586,6 +588,7 @@ __device__ inline int radial_grad32(const CompF32 &c, const Geo &g, float scale,
     default:
       return 0;
   }
+  if (value) *value = I;
   // geometric chain rule; G = dI/dr / r
   const float G = dIdr * rinv;
   const float invq = c.invq;

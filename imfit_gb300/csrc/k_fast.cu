@@ -182,8 +182,9 @@ __global__ void __launch_bounds__(256) k_fast_subsample(FastArgs a, WinDesc w, i
   for (int t = lane; t < ns * ns; t += 32) {
     const int ii = t / ns, jj = t - ii * ns;
     const Geo gs = geo32(cc, xs + ii * d, ys + jj * d);
-    acc[0] += radial32(cc, gs.r2);
-    const int np = radial_grad32(cc, gs, 1.f, o);
+    float v;
+    const int np = radial_grad32(cc, gs, 1.f, o, &v);
+    acc[0] += v;
 #pragma unroll
     for (int q = 0; q < 7; q++)
       if (q < 2 + np) acc[1 + q] += o[q];
@@ -604,9 +605,26 @@ __device__ __forceinline__ void los_pixel(const WinDesc &w, const CompF32 &cc, i
   yp = fmaf(-dx, cc.sinPA, dy * cc.cosPA);
 }
 
+// Kept partitions: [B][nLos][window pixels][32] panels (lo, hi) and the panel
+// counts, so the gradient pass integrates the derivatives over the forward
+// pass's panels instead of searching again.
+struct LosStore {
+  float2 *panels;
+  int *count;
+  int nLos;
+};
+
+// index of component c among the model's 3-D components
+__device__ __forceinline__ int los_index(const CompF32 *sc, int c) {
+  int k = 0;
+  for (int i = 0; i < c; i++) k += sc[i].type >= F_EXPDISK3D;
+  return k;
+}
+
 // One warp per window pixel (grid-stride): sum of the 3-D components' line of
-// sight integrals, written to w.losVal (added to the model row by eval_r2c).
-__global__ void __launch_bounds__(256) k_fast_los_eval(FastArgs a, WinDesc w) {
+// sight integrals, written to w.losVal (added to the model row by eval_r2c);
+// with a store, each partition is kept for the gradient pass.
+__global__ void __launch_bounds__(256) k_fast_los_eval(FastArgs a, WinDesc w, LosStore ks) {
   __shared__ CompF32 sc[kMaxComponents];
   const int b = blockIdx.y;
   const int nC = a.nComp;
@@ -624,7 +642,14 @@ __global__ void __launch_bounds__(256) k_fast_los_eval(FastArgs a, WinDesc w) {
       if (cc.type < F_EXPDISK3D) continue;
       float xp, yp;
       los_pixel(w, cc, row, col, xp, yp);
-      v += los_value_warp(cc, xp, yp, nd);
+      float lo, hi, total;
+      const int np = los_partition(cc, xp, yp, nd, lo, hi, total);
+      v += total;
+      if (ks.panels) {
+        const long slot = ((long)b * ks.nLos + los_index(sc, c)) * npix + p;
+        if (lane < np) ks.panels[slot * 32 + lane] = make_float2(lo, hi);
+        if (lane == 0) ks.count[slot] = np;
+      }
     }
     if (lane == 0) w.losVal[(long)b * npix + p] = v;
   }
@@ -634,7 +659,7 @@ __global__ void __launch_bounds__(256) k_fast_los_eval(FastArgs a, WinDesc w) {
 // every 3-D component, per-warp rows in shared memory (no atomics), then one
 // FP32 partial per parameter for this CTA.
 __global__ void __launch_bounds__(256) k_fast_los_grad(FastArgs a, WinDesc w, float *__restrict__ gradPart,
-                                                      int blockBase) {
+                                                      int blockBase, LosStore ks) {
   __shared__ CompF32 sc[kMaxComponents];
   __shared__ float red[8][kMaxParams];
   const int b = blockIdx.y;
@@ -655,7 +680,14 @@ __global__ void __launch_bounds__(256) k_fast_los_grad(FastArgs a, WinDesc w, fl
       if (cc.type < F_EXPDISK3D) continue;
       float xp, yp, g[kLosGrad];
       los_pixel(w, cc, row, col, xp, yp);
-      los_grad_warp(cc, xp, yp, nd, g);
+      if (ks.panels) {
+        const long slot = ((long)b * ks.nLos + los_index(sc, c)) * npix + p;
+        const int np = ks.count[slot];
+        const float2 pn = lane < np ? ks.panels[slot * 32 + lane] : make_float2(0.f, 0.f);
+        los_grad_panels(cc, xp, yp, nd, np, pn.x, pn.y, g);
+      } else {
+        los_grad_warp(cc, xp, yp, nd, g);
+      }
       if (lane == 0) {
         red[wid][cc.x0Index] += r * g[0];
         red[wid][cc.x0Index + 1] += r * g[1];
@@ -1121,13 +1153,14 @@ static void stage_end(const FastPlan &p, const char *name, cudaStream_t st) {
     stage_end(p, name, stream);          \
   } while (0)
 
-static cudaError_t launch_los_eval(const FastArgs &a, const WinDesc &w, int nBatch, cudaStream_t st) {
-  k_fast_los_eval<<<dim3(kLosCtas, nBatch), 256, 0, st>>>(a, w);
+static cudaError_t launch_los_eval(const FastArgs &a, const WinDesc &w, int nBatch, LosStore ks, cudaStream_t st) {
+  k_fast_los_eval<<<dim3(kLosCtas, nBatch), 256, 0, st>>>(a, w, ks);
   return cudaGetLastError();
 }
 
-static cudaError_t launch_los_grad(const FastArgs &a, const WinDesc &w, int nBatch, int blockBase, cudaStream_t st) {
-  k_fast_los_grad<<<dim3(kLosCtas, nBatch), 256, 0, st>>>(a, w, a.gradPart, blockBase);
+static cudaError_t launch_los_grad(const FastArgs &a, const WinDesc &w, int nBatch, int blockBase, LosStore ks,
+                                   cudaStream_t st) {
+  k_fast_los_grad<<<dim3(kLosCtas, nBatch), 256, 0, st>>>(a, w, a.gradPart, blockBase, ks);
   return cudaGetLastError();
 }
 
@@ -1191,6 +1224,11 @@ cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool 
   mw.losRt = a.losRt;
   rw.losVal = a.rLosVal;
   rw.losRt = a.rLosRt;
+  // kept partitions (only worth writing when the gradient pass follows)
+  LosStore mks{wantGrad ? reinterpret_cast<float2 *>(a.losPan) : nullptr, a.losCnt, a.nLos};
+  LosStore rks{wantGrad ? reinterpret_cast<float2 *>(a.rLosPan) : nullptr, a.rLosCnt, a.nLos};
+  if (!mks.panels) mks.count = nullptr;
+  if (!rks.panels) rks.count = nullptr;
 
   STAGE("setup", st, fast_setup(a, nBatch, st));
   if (fork) {
@@ -1200,7 +1238,7 @@ cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool 
   }
   if (g.hasRegion) {
     STAGE("region_subsample", rs, launch_subsample(a, rw, 1, nBatch, rs));
-    if (los) STAGE("region_los_eval", rs, launch_los_eval(a, rw, nBatch, rs));
+    if (los) STAGE("region_los_eval", rs, launch_los_eval(a, rw, nBatch, rks, rs));
     STAGE("region_eval_r2c", rs, launch_eval(a, rw, *p.Rx, nBatch, 1, tu, rs));
     STAGE("region_cols_conv", rs,
           launch_cols<float>(a.rspec, g.rSpecPitch, g.rSpecBatch, p.Rx->L / 2 + 1, g.rWinRows, g.rSubRows, p.Hr,
@@ -1208,7 +1246,7 @@ cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool 
     STAGE("region_down", rs, launch_region_down(p, a, nBatch, rs));
   }
   STAGE("subsample", st, launch_subsample(a, mw, 0, nBatch, st));
-  if (los) STAGE("los_eval", st, launch_los_eval(a, mw, nBatch, st));
+  if (los) STAGE("los_eval", st, launch_los_eval(a, mw, nBatch, mks, st));
   STAGE("eval_r2c", st, launch_eval(a, mw, *p.Lx, nBatch, 0, tu, st));
   STAGE("cols_conv", st,
         launch_cols<float>(a.spec, g.specPitch, g.specBatch, p.Lx->L / 2 + 1, g.winRows, g.nDataRows, p.H, p.hPitch,
@@ -1234,13 +1272,13 @@ cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool 
           launch_cols<float>(a.rspec, g.rSpecPitch, g.rSpecBatch, p.Rx->L / 2 + 1, g.rSubRows, g.rWinRows, p.Hr,
                              p.hrPitch, *p.Ry, rscale, 2, nBatch, rs, tu.colCpb, 0, 1, nullptr, tu.colThreads));
     STAGE("region_grad_rows", rs, launch_grad(a, rw, *p.Rx, nBatch, nMain, 1, tu, rs));
-    if (los) STAGE("region_los_grad", rs, launch_los_grad(a, rw, nBatch, nMain + nReg + kLosCtas, rs));
+    if (los) STAGE("region_los_grad", rs, launch_los_grad(a, rw, nBatch, nMain + nReg + kLosCtas, rks, rs));
   }
   STAGE("cols_adjoint", st,
         launch_cols<float>(a.spec, g.specPitch, g.specBatch, p.Lx->L / 2 + 1, g.nDataRows, g.winRows, p.H, p.hPitch,
                            *p.Ly, scale, 2, nBatch, st, tu.colCpb, p.hBatch, 1, p.hMap, tu.colThreads));
   STAGE("grad_rows", st, launch_grad(a, mw, *p.Lx, nBatch, 0, 0, tu, st));
-  if (los) STAGE("los_grad", st, launch_los_grad(a, mw, nBatch, nMain + nReg, st));
+  if (los) STAGE("los_grad", st, launch_los_grad(a, mw, nBatch, nMain + nReg, mks, st));
   if (fork) {
     cudaError_t e = cudaEventRecord(p.join1, rs);
     if (!e) e = cudaStreamWaitEvent(st, p.join1, 0);

@@ -178,6 +178,11 @@ struct FastArgs {
   // pixel the summed line-of-sight values and the adjoint r~, main window and
   // region window, [B][rows][cols] each (all null otherwise)
   float *losVal, *losRt, *rLosVal, *rLosRt;
+  // their line-of-sight partitions kept from the forward pass for the gradient
+  // pass ([B][nLos][window pixels][32] (lo, hi) pairs and counts), or null
+  float *losPan, *rLosPan;
+  int *losCnt, *rLosCnt;
+  int nLos;
 };
 
 // CTAs per parameter vector of each line-of-sight kernel (grid-stride, one

@@ -289,9 +289,9 @@ __device__ __forceinline__ float los_value_warp(const CompF32 &c, float xp, floa
 
 // d(value)/d(X0, Y0, function parameters) over the same panels; every lane
 // returns the full sums in g[0..kLosGrad).
-__device__ __forceinline__ void los_grad_warp(const CompF32 &c, float xp, float yp, const GkLane &nd, float *g) {
-  float myLo, myHi, total;
-  const int np = los_partition(c, xp, yp, nd, myLo, myHi, total);
+// Derivative integrals over a given partition (lane p < np holds panel p).
+__device__ __forceinline__ void los_grad_panels(const CompF32 &c, float xp, float yp, const GkLane &nd, int np,
+                                                float myLo, float myHi, float *g) {
   float acc[kLosGrad];
 #pragma unroll
   for (int q = 0; q < kLosGrad; q++) acc[q] = 0.f;
@@ -312,6 +312,12 @@ __device__ __forceinline__ void los_grad_warp(const CompF32 &c, float xp, float 
   }
 #pragma unroll
   for (int q = 0; q < kLosGrad; q++) g[q] = los_wsum(acc[q]);
+}
+
+__device__ __forceinline__ void los_grad_warp(const CompF32 &c, float xp, float yp, const GkLane &nd, float *g) {
+  float myLo, myHi, total;
+  const int np = los_partition(c, xp, yp, nd, myLo, myHi, total);
+  los_grad_panels(c, xp, yp, nd, np, myLo, myHi, g);
 }
 
 }  // namespace imfit
