@@ -1,0 +1,74 @@
+"""CPU tests of the configuration-file parser (the format of
+core/config_file_parser.cpp:494-657) and the FITS round trip."""
+import os
+
+import numpy as np
+import pytest
+
+from imfit_gb300 import config, fits
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+REF_CONFIG = "/root/reference/tests/imfit_reference/imfit_config_n3073.dat"
+
+N3073_STYLE = """# comment line
+GAIN   4.725
+READNOISE   4.3
+ORIGINAL_SKY   154.33
+
+X0   101.0    90,110
+Y0   97.0     90,110
+FUNCTION Sersic
+PA    110.0   0,180
+ell    0.2    0,1
+n      1.5    fixed
+I_e    150
+r_e    15     0,100
+
+FUNCTION   Exponential   # trailing comment
+PA    55.0   0,90      # another
+ell    0.2   0,1
+I_0   70.0   0,600
+h     45.0   0,1000
+
+X0   20.0
+Y0   30.0
+FUNCTION FlatSky
+I_sky  3.0
+"""
+
+
+def test_parse_function_sets_limits_and_fixed():
+    c = config.parse_config(N3073_STYLE)
+    assert c.gain == 4.725 and c.read_noise == 4.3 and c.original_sky == 154.33
+    assert c.functions == [("Sersic", True), ("Exponential", False), ("FlatSky", True)]
+    assert c.param_names[:7] == ["X0", "Y0", "PA", "ell", "n", "I_e", "r_e"]
+    assert len(c.values) == 2 + 5 + 4 + 2 + 1
+    assert c.fixed[4] == 1 and c.fixed.sum() == 1
+    assert np.isnan(c.lower[5]) and c.lower[2] == 0 and c.upper[2] == 180
+    again = config.parse_config(config.format_params(c, c.values))
+    assert np.array_equal(again.values, c.values) and again.functions == c.functions
+
+
+@pytest.mark.parametrize("bad", ["FUNCTION Sersic\nPA 1\n", "X0 1\nFUNCTION Sersic\n",
+                                 "X0 1 0,10\nY0 2\nFUNCTION Exponential\nPA 5 10,20\n",
+                                 "X0 1\nY0 2\nPA 3\n", "X0 1\nY0 2\nFUNCTION Sersic\nPA x\n"])
+def test_parse_errors(bad):
+    with pytest.raises(config.ConfigError):
+        config.parse_config(bad)
+
+
+@pytest.mark.skipif(not os.path.exists(REF_CONFIG), reason="reference checkout not present")
+def test_reference_config_matches_the_n3073_fixture():
+    c = config.read_config(REF_CONFIG)
+    d = np.load(os.path.join(GOLDEN, "n3073.npz"))
+    assert np.array_equal(c.values, d["params"])
+    assert np.array_equal(c.lower, d["lo"]) and np.array_equal(c.upper, d["hi"])
+    assert c.gain == float(d["gain"]) and c.read_noise == float(d["read_noise"])
+
+
+def test_fits_round_trip(tmp_path):
+    rng = np.random.default_rng(1)
+    a = rng.normal(size=(7, 5)).astype(np.float32).astype(np.float64)
+    p = tmp_path / "x.fits"
+    fits.write_image(str(p), a)
+    assert np.array_equal(fits.read_image(str(p))[0], a)

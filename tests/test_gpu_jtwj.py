@@ -174,3 +174,30 @@ def test_jacobian_columns_vs_fd(gpu, oracle_mod, region):
     # the normal equations from these columns are the JtWJ entry point's
     s, A, b = g.jtwj(wl.start)
     assert np.allclose(J @ J.T, A, rtol=1e-4, atol=1e-6 * np.max(np.abs(A)))
+
+
+def test_cli_fit_of_n3073(gpu, tmp_path):
+    """The imfit-style command line (config file + FITS images) on the n3073
+    inputs reproduces mpfit's fit (imfit_textout4) like imfit_FitLM does."""
+    from imfit_gb300 import cli, fits
+    d = np.load(os.path.join(GOLDEN, "n3073.npz"))
+    names = ["X0", "Y0", "PA", "ell", "n", "I_e", "r_e", "PA", "ell", "I_0", "h"]
+    lines = [f"GAIN {float(d['gain'])}", f"READNOISE {float(d['read_noise'])}",
+             f"ORIGINAL_SKY {float(d['original_sky'])}", ""]
+    for j, (nm, v, lo, hi) in enumerate(zip(names, d["params"], d["lo"], d["hi"])):
+        if j == 2:
+            lines.append("FUNCTION Sersic")
+        if j == 7:
+            lines.append("FUNCTION Exponential")
+        lines.append(f"{nm} {float(v)!r} {float(lo)!r},{float(hi)!r}")
+    cfgp = tmp_path / "config.dat"
+    cfgp.write_text("\n".join(lines) + "\n")
+    for name in ("data", "mask", "psf"):
+        fits.write_image(str(tmp_path / f"{name}.fits"), d[name].astype(np.float64))
+    p, s = cli.run([str(cfgp), str(tmp_path / "data.fits"), "--psf", str(tmp_path / "psf.fits"),
+                    "--mask", str(tmp_path / "mask.fits"), "--save-params", str(tmp_path / "best.dat"),
+                    "--save-model", str(tmp_path / "model.fits")])
+    err = np.abs(p - d["lm_params"]) / np.abs(d["lm_params"])
+    assert np.all(err < 2e-4), err
+    assert relerr(s, float(d["lm_chi2_printed"])) < 1e-6
+    assert (tmp_path / "best.dat").exists() and fits.read_image(str(tmp_path / "model.fits"))[0].shape == d["data"].shape
