@@ -1,17 +1,25 @@
-"""An imfit-style command line on the GPU path.
+"""imfit- and makeimage-style command lines on the GPU path.
 
     python -m imfit_gb300.cli CONFIG IMAGE [--psf F] [--mask F] [--noise F] ...
+    python -m imfit_gb300.cli makeimage CONFIG [--ncols N --nrows M | --refimage F] ...
 
-Reads an Imfit configuration file and FITS images, sets the model up in the
-reference's order (core/setup_model_object.cpp:36-157), and either prints the
-fit statistic at the initial parameters (--chisquare-only) or fits with the
-Levenberg-Marquardt driver on the GPU's J^T J (chi^2 or Poisson-MLR; the Cash
-statistic has no deviates to fit by least squares).  The option names follow
-imfit.s (core/imfit_main.cpp, core/options_imfit.h); only the ones that matter
-for the model-image path are accepted.
+Reads an Imfit configuration file and FITS images and sets the model up in
+the reference's order (core/setup_model_object.cpp:36-157).  The fitting
+command either prints the fit statistic at the initial parameters
+(--chisquare-only) or fits: Levenberg-Marquardt on the GPU's J^T J (chi^2 or
+Poisson-MLR; the Cash statistic has no deviates to fit by least squares), or,
+with --de, generation-synchronous differential evolution on the batched
+statistic.  makeimage follows core/makeimage_main.cpp:99-380: the model image,
+optionally the expanded (PSF-padded) image, single-function images and the
+component-flux table.  Option names follow core/imfit_main.cpp and
+core/makeimage_main.cpp; only the ones that matter for the model-image path
+are accepted.
 """
 import argparse
+import math
+import os
 import sys
+import time
 
 import numpy as np
 
@@ -23,11 +31,21 @@ WEIGHTS_ARE_SIGMAS, WEIGHTS_ARE_VARIANCES, WEIGHTS_ARE_WEIGHTS = 100, 110, 120
 MASK_ZERO_IS_GOOD, MASK_ZERO_IS_BAD = 10, 20
 
 
+def _add_psf_options(ap):
+    ap.add_argument("--psf")
+    ap.add_argument("--no-normalize", action="store_true", help="do not normalise the PSF images")
+    ap.add_argument("--overpsf", action="append", default=[])
+    ap.add_argument("--overpsf_scale", action="append", type=int, default=[])
+    ap.add_argument("--overpsf_region", action="append", default=[])
+    ap.add_argument("--nosubsampling", "--no-subsampling", dest="nosubsampling", action="store_true")
+    ap.add_argument("--device", type=int, default=0)
+
+
 def build_parser():
     ap = argparse.ArgumentParser(prog="imfit_gb300.cli", description=__doc__.splitlines()[0])
     ap.add_argument("config")
     ap.add_argument("image")
-    ap.add_argument("--psf")
+    _add_psf_options(ap)
     ap.add_argument("--mask")
     ap.add_argument("--noise")
     ap.add_argument("--errors-are-variances", action="store_true")
@@ -41,25 +59,91 @@ def build_parser():
     ap.add_argument("--cashstat", action="store_true")
     ap.add_argument("--poisson-mlr", action="store_true")
     ap.add_argument("--model-errors", action="store_true")
-    ap.add_argument("--nosubsampling", action="store_true")
     ap.add_argument("--chisquare-only", action="store_true")
+    ap.add_argument("--de", action="store_true", help="differential evolution instead of LM")
+    ap.add_argument("--de-lhs", action="store_true", help="--de with a Latin-hypercube initial population")
+    ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--ftol", type=float, default=1e-8)
     ap.add_argument("--max-iter", type=int, default=0)
     ap.add_argument("--save-params", default="bestfit_parameters_imfit_gb300.dat")
     ap.add_argument("--save-model")
     ap.add_argument("--save-residual")
-    ap.add_argument("--device", type=int, default=0)
     return ap
+
+
+def build_makeimage_parser():
+    ap = argparse.ArgumentParser(prog="imfit_gb300.cli makeimage",
+                                 description="model image from a configuration file")
+    ap.add_argument("config")
+    _add_psf_options(ap)
+    ap.add_argument("-o", "--output", default="modelimage.fits")
+    ap.add_argument("--refimage")
+    ap.add_argument("--ncols", type=int, default=0)
+    ap.add_argument("--nrows", type=int, default=0)
+    ap.add_argument("--save-expanded", action="store_true")
+    ap.add_argument("--output-functions", help="root name of single-function images")
+    ap.add_argument("--nosave", action="store_true")
+    ap.add_argument("--print-fluxes", action="store_true")
+    ap.add_argument("--save-fluxes")
+    ap.add_argument("--zero-point", type=float)
+    ap.add_argument("--estimation-size", type=int, default=5000)
+    ap.add_argument("--timing", type=int, default=0)
+    return ap
+
+
+def parse_region(text):
+    """'x1:x2,y1:y2' (1-based, inclusive) -> (x1, x2, y1, y2)."""
+    try:
+        xs, ys = text.split(",")
+        x1, x2 = (int(v) for v in xs.split(":"))
+        y1, y2 = (int(v) for v in ys.split(":"))
+    except ValueError:
+        raise SystemExit(f"bad oversampled-PSF region {text!r} (want x1:x2,y1:y2)")
+    return x1, x2, y1, y2
+
+
+def _add_psf(m, args):
+    if args.psf:
+        m.add_psf(fitsio.read_image(args.psf)[0], normalize=not args.no_normalize)
+
+
+def _add_oversampled_psfs(m, args):
+    """Oversampled PSFs as core/getimages.cpp:138-200 (after the image size is
+    known): one image and scale serve every region, or one per region."""
+    if not args.overpsf:
+        return
+    if not args.overpsf_region:
+        raise SystemExit("an oversampled PSF needs at least one --overpsf_region")
+    if len(args.overpsf) != len(args.overpsf_scale):
+        raise SystemExit("the number of --overpsf_scale values differs from the number of --overpsf images")
+    if len(args.overpsf) > 1 and len(args.overpsf) != len(args.overpsf_region):
+        raise SystemExit("give one oversampled PSF image, or one per region")
+    for k, region in enumerate(args.overpsf_region):
+        j = k if len(args.overpsf) > 1 else 0
+        if args.overpsf_scale[j] < 1:
+            raise SystemExit("--overpsf_scale must be a positive integer")
+        m.add_oversampled_psf(fitsio.read_image(args.overpsf[j])[0], args.overpsf_scale[j],
+                              parse_region(region), normalize=not args.no_normalize)
+
+
+def _add_functions(m, cfg, args):
+    for (name, _), opt in zip(cfg.functions, cfg.optional):
+        if opt:  # FunctionObject::SetExtraParams returns -1 for these functions
+            raise SystemExit(f"function {name} takes no optional parameters ({', '.join(opt)})")
+    for name, new_set in cfg.functions:
+        m.add_function(name, new_set, subsampling=not args.nosubsampling)
+    m.finish_functions()
+    if m.n_params != len(cfg.values):
+        raise SystemExit(f"the configuration gives {len(cfg.values)} parameters, the functions need "
+                         f"{m.n_params}")
 
 
 def setup_model(cfg, args, image):
     m = ModelObject(args.device)
-    for name, new_set in cfg.functions:
-        m.add_function(name, new_set, subsampling=not args.nosubsampling)
-    m.finish_functions()
-    if args.psf:
-        m.add_psf(fitsio.read_image(args.psf)[0])
+    _add_functions(m, cfg, args)
+    _add_psf(m, args)
     m.add_image_data(image)
+    _add_oversampled_psfs(m, args)
     gain = args.gain if args.gain is not None else cfg.gain
     rn = args.readnoise if args.readnoise is not None else cfg.read_noise
     et = args.exptime if args.exptime is not None else cfg.exp_time
@@ -86,7 +170,7 @@ def setup_model(cfg, args, image):
 
 
 def run(argv=None, out=sys.stdout):
-    """Returns (fitted parameters, statistic)."""
+    """The fitting command; returns (fitted parameters, statistic)."""
     args = build_parser().parse_args(argv)
     try:
         cfg = read_config(args.config)
@@ -99,18 +183,29 @@ def run(argv=None, out=sys.stdout):
         s = m.get_fit_statistic(p0)
         out.write(f"fit statistic = {s:.6f}\n")
         return p0, s
-    if args.cashstat:
-        raise SystemExit("the Cash statistic has no deviates: use --chisquare-only, or fit chi^2 / "
-                         "--poisson-mlr")
-    limited = ~np.isnan(cfg.lower)
-    lo = np.where(limited, cfg.lower, 0.0)
-    hi = np.where(limited, cfg.upper, 0.0)  # lower >= upper means no limit
-    r = m.fit_lm(p0, fixed=cfg.fixed, lower=lo, upper=hi, ftol=args.ftol, max_iter=args.max_iter)
-    p = r["params"]
-    s = m.get_fit_statistic(p)  # FP64 statistic at the fitted point
     n_free = int(np.sum(cfg.fixed == 0))
+    if args.de or args.de_lhs:
+        from .solvers import differential_evolution
+        try:
+            r = differential_evolution(m, p0, cfg.lower, cfg.upper, fixed=cfg.fixed.astype(bool),
+                                       ftol=args.ftol, seed=args.seed, latin_hypercube=args.de_lhs)
+        except ValueError as e:
+            raise SystemExit(str(e))
+        p = r["params"]
+        out.write(f"differential evolution: {r['generations']} generations of {r['population']} "
+                  f"({'converged' if r['converged'] else 'generation limit'})\n")
+    else:
+        if args.cashstat:
+            raise SystemExit("the Cash statistic has no deviates: use --chisquare-only, --de, or fit "
+                             "chi^2 / --poisson-mlr")
+        limited = ~np.isnan(cfg.lower)
+        lo = np.where(limited, cfg.lower, 0.0)
+        hi = np.where(limited, cfg.upper, 0.0)  # lower >= upper means no limit
+        r = m.fit_lm(p0, fixed=cfg.fixed, lower=lo, upper=hi, ftol=args.ftol, max_iter=args.max_iter)
+        p = r["params"]
+        out.write(f"status {r['status']} after {r['niter']} iterations ({r['nev']} J^T J evaluations)\n")
+    s = m.get_fit_statistic(p)  # FP64 statistic at the fitted point
     dof = m.n_valid - n_free
-    out.write(f"status {r['status']} after {r['niter']} iterations ({r['nev']} J^T J evaluations)\n")
     out.write(f"fit statistic = {s:.6f}, reduced = {s / dof:.6f} ({dof} degrees of freedom)\n")
     for name, v in zip(cfg.param_names, p):
         out.write(f"  {name:8s} {v:.6f}\n")
@@ -127,5 +222,89 @@ def run(argv=None, out=sys.stdout):
     return p, s
 
 
+def flux_table(names, fluxes, total, zero_point=None, labels=None):
+    """Lines of makeimage's component-flux table (core/makeimage_main.cpp:753-785):
+    header, one line per function, an empty line, the total."""
+    labels = labels or [""] * len(names)
+    lines = ["Component                 Flux        Magnitude   Fraction   Label"]
+    rows = [(n, f, f / total, lb) for n, f, lb in zip(names, fluxes, labels)] + [("Total", total, 1.0, "")]
+    for k, (name, flux, frac, label) in enumerate(rows):
+        if k == len(names):
+            lines.append("")
+        s = f"{name:<25s} {flux:10.4e}"
+        s += f"   {zero_point - 2.5 * math.log10(flux):6.4f}" if zero_point is not None and flux > 0 \
+            else "      ---"
+        s += f"{frac:12.5f}" if frac >= 1e-4 or frac == 0.0 else f"{frac:12.3e}"
+        if label:
+            s += f"    {label}"
+        lines.append(s)
+    return lines
+
+
+def makeimage(argv=None, out=sys.stdout):
+    """The makeimage command; returns the model image (None when only fluxes
+    were asked for) and the flux table (None when not asked for)."""
+    args = build_makeimage_parser().parse_args(argv)
+    try:
+        cfg = read_config(args.config)
+    except ConfigError as e:
+        raise SystemExit(f"error in {args.config}: {e}")
+    fluxes_only = (args.print_fluxes or args.save_fluxes) and args.nosave
+    ncols = args.ncols or int(float(cfg.options.get("NCOLS", 0)))
+    nrows = args.nrows or int(float(cfg.options.get("NROWS", 0)))
+    if not (ncols > 0 and nrows > 0):
+        if args.refimage:
+            nrows, ncols = fitsio.read_image(args.refimage)[0].shape
+        elif not args.nosave:
+            raise SystemExit("no image size: give --ncols and --nrows, or --refimage")
+        else:
+            ncols = nrows = 2  # fluxes only: the reference's minimal image
+    m = ModelObject(args.device)
+    _add_functions(m, cfg, args)
+    _add_psf(m, args)
+    m.setup_model_image(ncols, nrows)
+    _add_oversampled_psfs(m, args)
+    p = np.array(cfg.values, dtype=float)
+    model = None
+    if not fluxes_only:
+        m.create_model_image(p)
+        model = m.get_model_image()
+        if not args.nosave:
+            fitsio.write_image(args.output, model)
+            out.write(f"saved {args.output} ({ncols} x {nrows})\n")
+            if args.save_expanded:
+                head, tail = os.path.split(args.output)
+                fitsio.write_image(os.path.join(head, "expanded_" + tail), m.get_expanded_model_image())
+            if args.output_functions:
+                for k, (name, _) in enumerate(cfg.functions):
+                    fitsio.write_image(f"{args.output_functions}{k + 1}_{name}.fits",
+                                       m.get_single_function_image(p, k))
+    table = None
+    if args.print_fluxes or args.save_fluxes:
+        total, ind = m.find_total_fluxes(p, args.estimation_size, args.estimation_size)
+        table = flux_table([n for n, _ in cfg.functions], ind, total, args.zero_point, cfg.labels)
+        if args.print_fluxes:
+            out.write("\n".join(table) + "\n")
+        if args.save_fluxes:
+            with open(args.save_fluxes, "w") as f:
+                f.write(f"# Fluxes estimated on {args.estimation_size} x {args.estimation_size} image\n")
+                f.write("# " + table[0] + "\n" + "\n".join(table[1:]) + "\n")
+    if args.timing > 0:
+        t0 = time.perf_counter()
+        for _ in range(args.timing):
+            m.create_model_image(p)
+        dt = (time.perf_counter() - t0) / args.timing
+        out.write(f"mean time per image computation ({args.timing} iterations) = {dt:.7f} s\n")
+    return model, table
+
+
+def main(argv=None):
+    argv = sys.argv[1:] if argv is None else argv
+    if argv and argv[0] == "makeimage":
+        makeimage(argv[1:])
+    else:
+        run(argv)
+
+
 if __name__ == "__main__":
-    run()
+    main()

@@ -5,7 +5,11 @@ Lines are trimmed; empty lines and lines starting with '#' are skipped, and
 options ``NAME value`` (GAIN, READNOISE, ORIGINAL_SKY, EXPTIME, NCOMBINED).
 The function section is a sequence of function sets, each opened by
 ``X0 value [limits]`` and ``Y0 value [limits]``, followed by ``FUNCTION name``
-blocks whose parameter lines are ``name value [lo,hi | fixed]``.
+blocks whose parameter lines are ``name value [lo,hi | fixed]``.  A
+``# LABEL text`` comment on a FUNCTION line labels that function
+(core/config_file_parser.cpp:208-222), and an ``OPTIONAL_PARAMS_START`` ...
+``OPTIONAL_PARAMS_END`` block after it holds ``name value`` pairs for the
+function's optional parameters (core/config_file_parser.cpp:450-465).
 """
 from dataclasses import dataclass, field
 
@@ -18,6 +22,8 @@ _OPTION_NAMES = {"GAIN", "READNOISE", "ORIGINAL_SKY", "EXPTIME", "NCOMBINED"}
 class ModelConfig:
     options: dict = field(default_factory=dict)
     functions: list = field(default_factory=list)   # [(name, starts_new_set)]
+    labels: list = field(default_factory=list)      # per function, "" when unlabelled
+    optional: list = field(default_factory=list)    # per function, {name: value}
     param_names: list = field(default_factory=list)
     values: np.ndarray = None
     lower: np.ndarray = None                          # NaN: no limit
@@ -53,16 +59,21 @@ def _strip(line):
     return line.split("#", 1)[0].strip()
 
 
+def _label(line):
+    k = line.find("LABEL")
+    return "" if k < 0 else line[k + 5:].strip()
+
+
 def parse_config(text):
     """Parse the text of an Imfit configuration file."""
     lines = []
     for k, raw in enumerate(text.splitlines(), 1):
         t = raw.strip()
         if t and not t.startswith("#"):
-            lines.append((k, _strip(t)))
+            lines.append((k, _strip(t), t))
     cfg = ModelConfig()
     i = 0
-    while i < len(lines) and not lines[i][1].split()[0] == "X0":
+    while i < len(lines) and lines[i][1].split()[0] != "X0":
         parts = lines[i][1].split()
         if parts[0] == "FUNCTION":
             raise ConfigError(f"line {lines[i][0]}: FUNCTION before the first X0")
@@ -103,10 +114,23 @@ def parse_config(text):
         hi.append(h)
         fx.append(f)
 
-    for lineno, text_ in lines[i:]:
+    in_optional = False
+    for lineno, text_, raw in lines[i:]:
         parts = text_.split()
         key = parts[0]
-        if key == "X0":
+        if key == "OPTIONAL_PARAMS_START":
+            if not cfg.functions or in_optional:
+                raise ConfigError(f"line {lineno}: OPTIONAL_PARAMS_START outside a function")
+            in_optional = True
+        elif key == "OPTIONAL_PARAMS_END":
+            if not in_optional:
+                raise ConfigError(f"line {lineno}: OPTIONAL_PARAMS_END without a start")
+            in_optional = False
+        elif in_optional:
+            if len(parts) < 2:
+                raise ConfigError(f"line {lineno}: optional parameter needs a value")
+            cfg.optional[-1][parts[0]] = parts[1]
+        elif key == "X0":
             param(lineno, parts)
             new_set = True
             expecting_y0 = True
@@ -121,6 +145,8 @@ def parse_config(text):
             if len(parts) < 2:
                 raise ConfigError(f"line {lineno}: FUNCTION without a name")
             cfg.functions.append((parts[1], new_set))
+            cfg.labels.append(_label(raw))
+            cfg.optional.append({})
             new_set = False
         elif key in _OPTION_NAMES:
             raise ConfigError(f"line {lineno}: image option inside the function section")
@@ -128,6 +154,8 @@ def parse_config(text):
             if not cfg.functions:
                 raise ConfigError(f"line {lineno}: parameter before any FUNCTION")
             param(lineno, parts)
+    if in_optional:
+        raise ConfigError("OPTIONAL_PARAMS_START without an end")
     cfg.values = np.array(vals)
     cfg.lower = np.array(lo)
     cfg.upper = np.array(hi)
@@ -152,13 +180,14 @@ def format_params(cfg, params, chi2=None):
     for k, v in cfg.options.items():
         out.append(f"{k}\t{v}")
     j = 0
-    for name, new_set in cfg.functions:
+    for k, (name, new_set) in enumerate(cfg.functions):
         if new_set:
             out.append("")
             for _ in range(2):
                 out.append(f"{cfg.param_names[j]}\t{params[j]:.6f}")
                 j += 1
-        out.append(f"FUNCTION {name}")
+        label = cfg.labels[k] if k < len(cfg.labels) else ""
+        out.append(f"FUNCTION {name}" + (f"   # LABEL {label}" if label else ""))
         for _ in range(_NPARAMS[name]):
             out.append(f"{cfg.param_names[j]}\t{params[j]:.6f}")
             j += 1

@@ -1,7 +1,8 @@
 """Generate the committed golden fixtures from the reference.
 
 Run in a checkout that has the reference at /root/reference (or
-IMFIT_REFERENCE_DIR):  python tests/golden/make_golden.py
+IMFIT_REFERENCE_DIR):  python tests/golden/make_golden.py [part ...]
+(parts: n3073 makeimage ic3478 small_case; all by default)
 
 Outputs (all small .npz files next to this script):
   n3073.npz          the reference regression inputs tests/n3073rss_small.fits,
@@ -14,6 +15,11 @@ Outputs (all small .npz files next to this script):
                      (central 128x128 crop and four 16x16 corners) and
                      tests/oversampled_orig.fits (whole image) with their PSFs
                      (do_makeimage_tests:51, 68-72).
+  ic3478.npz         the reference regression input tests/ic3478rss_64x64.fits
+                     (float32 as stored) with the configuration
+                     tests/imfit_reference/imfit_config_ic3478_64x64b.dat and the
+                     printed results of its mpfit fit (imfit_textout3) and its
+                     Differential Evolution fit (imfit_textout3c_tail).
   small_case.npz     the reference's own outputs (oracle/_ref) for
                      imfit_gb300.workloads.small_case: model images, deviates and
                      statistics for chi^2 / Cash / PMLR.
@@ -88,6 +94,25 @@ def makeimage():
         psf_oversamp=psf_os.astype(np.float32), ov_region=np.array([100, 110, 100, 110]), ov_scale=3)
 
 
+def ic3478():
+    t = os.path.join(REF, "tests")
+    data, _ = fits.read_image(os.path.join(t, "ic3478rss_64x64.fits"))
+    np.savez_compressed(
+        os.path.join(HERE, "ic3478.npz"), data=data.astype(np.float32),
+        gain=4.725, read_noise=4.3, original_sky=130.1,
+        # X0 Y0 PA ell n I_e r_e and their limits
+        params=np.array([32.0, 32.0, 18.0, 0.2, 1.5, 15.0, 25.0]),
+        lo=np.array([1.0, 1.0, 0.0, 0.0, 0.0, 0.0, 0.0]),
+        hi=np.array([64.0, 64.0, 90.0, 1.0, 5.0, 500.0, 100.0]),
+        # imfit_textout3: CHI-SQUARE, reduced chi^2, best-fit values and errors
+        lm_chi2_printed=4555.947654, lm_reduced_printed=1.114196,
+        lm_params_printed=np.array([32.9439, 34.0933, 18.2612, 0.235989, 2.40028, 20.0094, 60.7612]),
+        lm_errors_printed=np.array([0.0128, 0.0156, 0.30986, 0.0023165, 0.018072, 0.40396, 0.86063]),
+        # imfit_textout3c_tail: the same fit with --de
+        de_reduced_printed=1.114196,
+        de_params_printed=np.array([32.9439, 34.0933, 18.2613, 0.235989, 2.40028, 20.0094, 60.7612]))
+
+
 def small_case():
     out = {}
     for stat in ("chi2", "cash", "pmlr"):
@@ -106,9 +131,9 @@ if __name__ == "__main__":
     if not os.path.isdir(os.path.join(REF, "core")):
         sys.exit(f"reference checkout not found at {REF}")
     oracle.build_reference()
-    n3073()
-    makeimage()
-    small_case()
+    parts = {"n3073": n3073, "makeimage": makeimage, "ic3478": ic3478, "small_case": small_case}
+    for name in (sys.argv[1:] or parts):
+        parts[name]()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

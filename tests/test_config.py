@@ -72,3 +72,45 @@ def test_fits_round_trip(tmp_path):
     p = tmp_path / "x.fits"
     fits.write_image(str(p), a)
     assert np.array_equal(fits.read_image(str(p))[0], a)
+
+
+def test_labels_optional_params_and_image_size_options():
+    """FUNCTION ... # LABEL x (core/config_file_parser.cpp:208-222), an
+    OPTIONAL_PARAMS block (config_file_parser.cpp:450-465), NCOLS/NROWS."""
+    text = """NCOLS 64
+NROWS 48
+X0 32
+Y0 24
+FUNCTION Sersic   # LABEL bulge component
+PA 30
+ell 0.5
+n 2.5
+I_e 100
+r_e 50
+FUNCTION Gaussian
+OPTIONAL_PARAMS_START
+mode  alpha
+OPTIONAL_PARAMS_END
+PA 30
+ell 0.1
+I_0 10
+sigma 3
+"""
+    cfg = config.parse_config(text)
+    assert cfg.labels == ["bulge component", ""]
+    assert cfg.optional == [{}, {"mode": "alpha"}]
+    assert cfg.options["NCOLS"] == "64" and cfg.options["NROWS"] == "48"
+    assert len(cfg.values) == 11
+    out = config.format_params(cfg, cfg.values)
+    assert "FUNCTION Sersic   # LABEL bulge component" in out
+    again = config.parse_config(out)
+    assert again.labels[0] == "bulge component" and np.allclose(again.values, cfg.values)
+    with pytest.raises(config.ConfigError):
+        config.parse_config(text.replace("OPTIONAL_PARAMS_END\n", ""))
+
+
+def test_region_strings():
+    from imfit_gb300.cli import parse_region
+    assert parse_region("100:110,20:30") == (100, 110, 20, 30)
+    with pytest.raises(SystemExit):
+        parse_region("100-110,20:30")

@@ -1,0 +1,165 @@
+"""GPU tests of the command-line front ends and the differential-evolution
+driver, against the reference's regression outputs (do_makeimage_tests,
+do_imfit_tests) held in tests/golden."""
+import io
+import os
+
+import numpy as np
+import pytest
+
+from helpers import normwise
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+SERSIC_EXP_FLAT = """NCOLS 512
+NROWS 512
+X0 256.0
+Y0 256.0
+FUNCTION Sersic   # LABEL bulge
+PA 30.0
+ell 0.5
+n 2.5
+I_e 100.0
+r_e 50.0
+FUNCTION Exponential   # LABEL disk
+PA 30.0
+ell 0.75
+I_0 10.0
+h 150.0
+FUNCTION FlatSky
+I_0 1000.0
+"""
+
+
+def test_makeimage_oversampled_golden(gpu, tmp_path):
+    """do_makeimage_tests:68: --psf, --overpsf, --overpsf_scale 3,
+    --overpsf_region 100:110,100:110 and --output-functions against
+    tests/oversampled_orig.fits (the single Gaussian image too)."""
+    from imfit_gb300 import cli, fits
+    g = np.load(os.path.join(GOLDEN, "makeimage.npz"))
+    names = ["X0", "Y0", "PA", "ell", "I_0", "sigma"]
+    lines = [f"{n} {float(v)!r}" for n, v in zip(names[:2], g["ov_params"][:2])] + ["FUNCTION Gaussian"]
+    lines += [f"{n} {float(v)!r}" for n, v in zip(names[2:], g["ov_params"][2:])]
+    (tmp_path / "c.dat").write_text("\n".join(lines) + "\n")
+    fits.write_image(str(tmp_path / "psf.fits"), g["psf_standard"])
+    fits.write_image(str(tmp_path / "opsf.fits"), g["psf_oversamp"])
+    x1, x2, y1, y2 = (int(v) for v in g["ov_region"])
+    out = str(tmp_path / "ov.fits")
+    model, _ = cli.makeimage([str(tmp_path / "c.dat"), "-o", out, "--ncols", "200", "--nrows", "200",
+                              "--psf", str(tmp_path / "psf.fits"), "--overpsf", str(tmp_path / "opsf.fits"),
+                              "--overpsf_scale", str(int(g["ov_scale"])), "--overpsf_region", f"{x1}:{x2},{y1}:{y2}",
+                              "--output-functions", str(tmp_path / "single")], out=io.StringIO())
+    saved = fits.read_image(out)[0]
+    assert normwise(model, g["ov_image"]) < 1e-7
+    assert normwise(saved, g["ov_image"]) < 2e-7  # float32 FITS, as the reference writes
+    single = fits.read_image(str(tmp_path / "single1_Gaussian.fits"))[0]
+    assert normwise(single, g["ov_image"]) < 2e-7
+
+
+def test_makeimage_fluxes_table(gpu, tmp_path):
+    """do_makeimage_tests:60 (makeimage_textout5b): --print-fluxes --nosave
+    on config_makeimage_sersic+exp512b.dat; the table lines as printed."""
+    from imfit_gb300 import cli
+    (tmp_path / "c.dat").write_text(SERSIC_EXP_FLAT)
+    buf = io.StringIO()
+    model, table = cli.makeimage([str(tmp_path / "c.dat"), "--print-fluxes", "--nosave"], out=buf)
+    assert model is None
+    assert table == ["Component                 Flux        Magnitude   Fraction   Label",
+                     "Sersic                    2.2635e+06      ---     0.86495    bulge",
+                     "Exponential               3.5343e+05      ---     0.13505    disk",
+                     "FlatSky                   0.0000e+00      ---     0.00000",
+                     "",
+                     "Total                     2.6169e+06      ---     1.00000"]
+    assert "\n".join(table) in buf.getvalue()
+
+
+def test_makeimage_single_function_images_sum_to_model(gpu, tmp_path, oracle_mod):
+    """do_makeimage_tests:65 (--output-functions with a PSF; the single images
+    sum to the model image), with --save-expanded and the config's own
+    NCOLS/NROWS, on a 96 x 80 image; the model against the oracle."""
+    from imfit_gb300 import cli, fits
+    cfg = SERSIC_EXP_FLAT.replace("NCOLS 512", "NCOLS 96").replace("NROWS 512", "NROWS 80")
+    cfg = cfg.replace("X0 256.0", "X0 48.3").replace("Y0 256.0", "Y0 40.6").replace("r_e 50.0", "r_e 9.0")
+    (tmp_path / "c.dat").write_text(cfg.replace("h 150.0", "h 15.0"))
+    yy, xx = np.mgrid[-7:8, -7:8]
+    psf = np.exp(-(xx ** 2 + yy ** 2) / 4.5)
+    fits.write_image(str(tmp_path / "psf.fits"), psf, bitpix=-64)
+    out = str(tmp_path / "m.fits")
+    model, _ = cli.makeimage([str(tmp_path / "c.dat"), "-o", out, "--psf", str(tmp_path / "psf.fits"),
+                              "--output-functions", str(tmp_path / "f"), "--save-expanded"], out=io.StringIO())
+    assert model.shape == (80, 96)
+    parts = [fits.read_image(str(tmp_path / f"f{k}_{n}.fits"))[0]
+             for k, n in ((1, "Sersic"), (2, "Exponential"), (3, "FlatSky"))]
+    assert normwise(sum(parts), model) < 3e-7
+    expanded = fits.read_image(str(tmp_path / "expanded_m.fits"))[0]
+    assert expanded.shape == (80 + 2 * 15, 96 + 2 * 15)
+    o = oracle_mod.OracleModel()
+    for name, new_set in (("Sersic", True), ("Exponential", False), ("FlatSky", False)):
+        o.add_function(name, new_set)
+    o.finish_functions()
+    o.add_psf(psf)
+    o.setup_model_image(96, 80)
+    o.create_model_image([48.3, 40.6, 30.0, 0.5, 2.5, 100.0, 9.0, 30.0, 0.75, 10.0, 15.0, 1000.0])
+    assert normwise(model, o.get_model_image()) < 1e-10
+
+
+def _ic3478_files(tmp_path):
+    from imfit_gb300 import fits
+    d = np.load(os.path.join(GOLDEN, "ic3478.npz"))
+    names = ["X0", "Y0", "PA", "ell", "n", "I_e", "r_e"]
+    lines = [f"GAIN {float(d['gain'])}", f"READNOISE {float(d['read_noise'])}",
+             f"ORIGINAL_SKY {float(d['original_sky'])}"]
+    for j, (nm, v, lo, hi) in enumerate(zip(names, d["params"], d["lo"], d["hi"])):
+        if j == 2:
+            lines.append("FUNCTION Sersic")
+        lines.append(f"{nm} {float(v)!r} {float(lo)!r},{float(hi)!r}")
+    (tmp_path / "c.dat").write_text("\n".join(lines) + "\n")
+    fits.write_image(str(tmp_path / "data.fits"), d["data"])
+    return d
+
+
+@pytest.mark.parametrize("solver", ["lm", "de"])
+def test_ic3478_fits_match_printed_results(gpu, tmp_path, solver):
+    """do_imfit_tests:68 and :75 (imfit_textout3, imfit_textout3c_tail):
+    ic3478rss_64x64.fits with imfit_config_ic3478_64x64b.dat, by LM and by
+    differential evolution (--de); the fitted values agree with the printed
+    ones to within 0.05 sigma (LM) or 0.1 sigma (DE, whose last digits are
+    set by the float32 noise of the statistic it minimises), the reduced
+    chi^2 to its six printed decimals."""
+    from imfit_gb300 import cli
+    d = _ic3478_files(tmp_path)
+    args = [str(tmp_path / "c.dat"), str(tmp_path / "data.fits"), "--save-params", str(tmp_path / "b.dat")]
+    if solver == "de":
+        args += ["--de", "--seed", "7"]
+    buf = io.StringIO()
+    p, s = cli.run(args, out=buf)
+    want = d["lm_params_printed"] if solver == "lm" else d["de_params_printed"]
+    tol = (0.05 if solver == "lm" else 0.1) * d["lm_errors_printed"]
+    assert np.all(np.abs(p - want) <= tol), (p, want)
+    chi2 = float(d["lm_chi2_printed"])
+    assert s > chi2 - 1e-6  # the FP64 statistic at the fitted point: never below the minimum
+    if solver == "lm":
+        assert s - chi2 < 2e-7 * chi2 and abs(s / (64 * 64 - 7) - float(d["lm_reduced_printed"])) < 1e-6
+    else:
+        assert s - chi2 < 1e-5 * chi2
+
+
+def test_de_driver_on_the_batched_statistic(gpu):
+    """differential_evolution on ModelObject: one batched call per
+    generation, and at the LM minimum of the same model."""
+    from imfit_gb300 import solvers
+    d = np.load(os.path.join(GOLDEN, "ic3478.npz"))
+    m = gpu.ModelObject()
+    m.add_function("Sersic", True)
+    m.finish_functions()
+    m.add_image_data(d["data"].astype(np.float64))
+    m.add_image_characteristics(float(d["gain"]), float(d["read_noise"]), 1.0, 1, float(d["original_sky"]))
+    assert m.final_setup() == 0
+    r = solvers.differential_evolution(m, d["params"], d["lo"], d["hi"], seed=1, latin_hypercube=True)
+    assert r["population"] == 56
+    assert r["batched_calls"] == r["generations"] + (2 if r["converged"] else 1)
+    lm = m.fit_lm(d["params"], lower=d["lo"], upper=d["hi"])
+    s_lm = m.get_fit_statistic(lm["params"])
+    assert r["statistic"] <= s_lm * (1 + 1e-6)
+    assert np.all(np.abs(r["params"] - lm["params"]) <= 0.1 * d["lm_errors_printed"])

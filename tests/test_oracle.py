@@ -199,3 +199,20 @@ def test_restatement_bit_identical_to_reference(oracle_mod):
         o.use_bootstrap(5)
         r.use_bootstrap(5)
         assert o.get_fit_statistic(wl.start) == r.get_fit_statistic(wl.start)
+
+
+def test_ic3478_printed_fit_statistic(oracle_mod):
+    """tests/imfit_reference/imfit_textout3: chi^2 (data-based errors) at the
+    printed best-fit parameters of ic3478rss_64x64.fits is the printed
+    CHI-SQUARE; the printed values are rounded to 6 digits, which moves chi^2
+    by far less than 1e-6 at a minimum."""
+    d = np.load(os.path.join(GOLDEN, "ic3478.npz"))
+    m = oracle_mod.OracleModel()
+    m.add_function("Sersic", True)
+    m.finish_functions()
+    m.add_image_data(d["data"].astype(np.float64))
+    m.add_image_characteristics(float(d["gain"]), float(d["read_noise"]), 1.0, 1, float(d["original_sky"]))
+    assert m.final_setup() == 0
+    s = m.get_fit_statistic(d["lm_params_printed"])
+    assert abs(s - float(d["lm_chi2_printed"])) < 1e-6 * float(d["lm_chi2_printed"]), s
+    assert abs(s / (64 * 64 - 7) - float(d["lm_reduced_printed"])) < 1e-6

@@ -1,0 +1,82 @@
+"""CPU tests of the generation-synchronous differential-evolution driver
+(solvers/DESolver.cpp semantics) on a batched numpy objective, and of the
+makeimage flux table (core/makeimage_main.cpp:753-785)."""
+import numpy as np
+import pytest
+
+from imfit_gb300 import solvers
+
+
+class Quadratic:
+    """A batched chi^2-like objective: sum ((x - c) / s)^2 + floor."""
+
+    def __init__(self, c, s, floor=100.0):
+        self.c, self.s, self.floor = np.asarray(c, float), np.asarray(s, float), floor
+        self.calls = []
+
+    def batch_statistic_and_gradient(self, P, want_grad=True):
+        assert not want_grad
+        P = np.atleast_2d(P)
+        self.calls.append(P.copy())
+        return np.sum(((P - self.c) / self.s) ** 2, axis=1) + self.floor
+
+    def get_fit_statistic(self, x):
+        return float(self.batch_statistic_and_gradient(x, want_grad=False)[0])
+
+
+def test_de_finds_the_minimum_one_batch_per_generation():
+    c = [3.0, -1.0, 0.5, 20.0]
+    q = Quadratic(c, [1.0, 0.1, 2.0, 5.0])
+    r = solvers.differential_evolution(q, [0, 0, 0, 10], [-10, -5, -5, 0], [10, 5, 5, 50], ftol=1e-10, seed=3)
+    assert r["converged"]
+    assert np.allclose(r["params"], c, atol=1e-3 * np.array([1.0, 0.1, 2.0, 5.0]))
+    assert r["statistic"] - 100.0 < 1e-5
+    # the initial population and then one batched call per generation, NP = 8 x free parameters
+    # (the last recorded call is get_fit_statistic at the best vector)
+    assert r["batched_calls"] == len(q.calls) - 1 == r["generations"] + 2
+    assert all(P.shape == (32, 4) for P in q.calls[:-1])
+    # every evaluated vector respects the limits
+    allp = np.concatenate(q.calls)
+    assert np.all(allp >= [-10, -5, -5, 0]) and np.all(allp <= [10, 5, 5, 50])
+
+
+def test_de_convergence_checked_every_ten_generations_from_forty():
+    q = Quadratic([0.0, 0.0], [1.0, 1.0], floor=1.0)
+    r = solvers.differential_evolution(q, [0.5, 0.5], [-1, -1], [1, 1], ftol=1e-3, seed=0)
+    assert r["converged"] and r["generations"] >= 40 and r["generations"] % 10 == 0
+
+
+def test_de_fixed_parameters_and_limits():
+    q = Quadratic([1.0, 2.0, 3.0], [1.0, 1.0, 1.0])
+    r = solvers.differential_evolution(q, [1.0, 7.0, 0.0], [0, 0, 0], [5, 0, 5], fixed=[False, True, False],
+                                       seed=1, ftol=1e-9)
+    assert r["population"] == 16
+    assert all(np.all(P[:, 1] == 7.0) for P in q.calls[:-1])
+    assert np.allclose(r["params"][[0, 2]], [1.0, 3.0], atol=1e-3)
+    with pytest.raises(ValueError):
+        solvers.differential_evolution(q, [1, 2, 3], [0, 0, np.nan], [5, 5, 5])
+
+
+def test_de_latin_hypercube_initial_population_is_stratified():
+    q = Quadratic([0.0, 0.0, 0.0], [1.0, 1.0, 1.0])
+    solvers.differential_evolution(q, [0, 0, 0], [0, 0, 0], [24, 24, 24], max_generations=0, latin_hypercube=True)
+    P0 = q.calls[0]
+    assert P0.shape == (24, 3)
+    for j in range(3):  # one member in each of the 24 strata of every parameter
+        assert sorted(np.floor(P0[:, j]).astype(int)) == list(range(24))
+
+
+def test_flux_table_matches_makeimage_output():
+    """Lines of tests/makeimage_reference/makeimage_textout5b (printed fluxes
+    of config_makeimage_sersic+exp512b.dat on a 5000 x 5000 image)."""
+    from imfit_gb300.cli import flux_table
+    S, E = 2.263505e6, 3.534285e5  # within the printed rounding of the reference's values
+    lines = flux_table(["Sersic", "Exponential", "FlatSky"], [S, E, 0.0], S + E, labels=["bulge", "disk", ""])
+    assert lines[0] == "Component                 Flux        Magnitude   Fraction   Label"
+    assert lines[1] == "Sersic                    2.2635e+06      ---     0.86495    bulge"
+    assert lines[2] == "Exponential               3.5343e+05      ---     0.13505    disk"
+    assert lines[3] == "FlatSky                   0.0000e+00      ---     0.00000"
+    assert lines[4] == ""
+    assert lines[5] == "Total                     2.6169e+06      ---     1.00000"
+    zp = flux_table(["Gaussian"], [1.0e4], 1.0e4, zero_point=26.0)
+    assert zp[1] == "Gaussian                  1.0000e+04   16.0000     1.00000"
