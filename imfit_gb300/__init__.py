@@ -83,6 +83,8 @@ _SIGS = [
                          ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     ("imfit_FitLMBatch", _I, [_P, _I, _DP, ctypes.POINTER(_I), _DP, _DP, _D, _I, _DP, ctypes.POINTER(_I),
                               ctypes.POINTER(_I)]),
+    ("imfit_BootstrapFitBatch", _I, [_P, _I, _DP, ctypes.POINTER(_I), _DP, _DP, _D, _I, _DP, _DP,
+                                     ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     ("imfit_SetupImageStack", _I, [_P, _I, _I, _I, _DP, _DP, _DP, _I, _I]),
     ("imfit_Synchronize", _I, [_P]),
     ("imfit_GetStream", _I, [_P, ctypes.POINTER(_P)]),
@@ -420,6 +422,25 @@ class ModelObject:
         self._ck(self.lib.imfit_FitLMBatch(self.h, B, _dp(P), fx, _dp(lo) if lo is not None else None,
                                            _dp(hi) if hi is not None else None, ftol, int(max_iter), _dp(S),
                                            it, st))
+        return dict(params=P, statistic=S, niter=np.array(it[:]), status=np.array(st[:]))
+
+    def bootstrap_fit_batch(self, n_samples, bestfit, fixed=None, lower=None, upper=None, ftol=1e-8, max_iter=0):
+        """The next n_samples bootstrap samples (after use_bootstrap(seed)), all
+        refitted at once from bestfit; dict of params (n_samples x nParams),
+        statistic, niter, status (> 0: success)."""
+        x = _f64(bestfit)
+        n = x.size
+        fx = (_I * n)(*([0] * n if fixed is None else [int(v) for v in fixed]))
+        lo = _f64(lower) if lower is not None else None
+        hi = _f64(upper) if upper is not None else None
+        P = np.empty((n_samples, n))
+        S = np.empty(n_samples)
+        it = (_I * n_samples)()
+        st = (_I * n_samples)()
+        self._ck(self.lib.imfit_BootstrapFitBatch(self.h, int(n_samples), _dp(x), fx,
+                                                  _dp(lo) if lo is not None else None,
+                                                  _dp(hi) if hi is not None else None, ftol, int(max_iter),
+                                                  _dp(P), _dp(S), it, st))
         return dict(params=P, statistic=S, niter=np.array(it[:]), status=np.array(st[:]))
 
     def setup_image_stack(self, images, sigmas, psfs):

@@ -63,6 +63,8 @@ def build_parser():
     ap.add_argument("--de", action="store_true", help="differential evolution instead of LM")
     ap.add_argument("--de-lhs", action="store_true", help="--de with a Latin-hypercube initial population")
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--bootstrap", type=int, default=0, help="number of bootstrap resampling iterations")
+    ap.add_argument("--save-bootstrap", help="file for the bootstrap best-fit parameters")
     ap.add_argument("--ftol", type=float, default=1e-8)
     ap.add_argument("--max-iter", type=int, default=0)
     ap.add_argument("--save-params", default="bestfit_parameters_imfit_gb300.dat")
@@ -212,6 +214,8 @@ def run(argv=None, out=sys.stdout):
     if args.save_params:
         with open(args.save_params, "w") as f:
             f.write(format_params(cfg, p, s))
+    if args.bootstrap > 0:
+        run_bootstrap(m, cfg, args, p, out)
     if args.save_model or args.save_residual:
         m.create_model_image(p)
         model = m.get_model_image()
@@ -220,6 +224,31 @@ def run(argv=None, out=sys.stdout):
         if args.save_residual:
             fitsio.write_image(args.save_residual, image - model)
     return p, s
+
+
+def run_bootstrap(m, cfg, args, bestfit, out):
+    """Bootstrap resampling errors (core/bootstrap_errors.cpp:86-160), all
+    refits of a chunk at once on the GPU."""
+    from .config import _NPARAMS
+    from .solvers import bootstrap_errors, bootstrap_file_lines, bootstrap_summary
+    if args.cashstat:
+        raise SystemExit("bootstrap refits use the LM driver: chi^2 or --poisson-mlr")
+    limited = ~np.isnan(cfg.lower)
+    lo = np.where(limited, cfg.lower, 0.0)
+    hi = np.where(limited, cfg.upper, 0.0)
+    seed = args.seed if args.seed > 0 else int(time.time())
+    samples, status = bootstrap_errors(m, bestfit, args.bootstrap, seed, fixed=cfg.fixed, lower=lo, upper=hi,
+                                       ftol=args.ftol, max_iter=args.max_iter)
+    if samples.shape[0] < 3:  # MIN_ITERATIONS_FOR_STATISTICS
+        out.write(f"\nNot enough successful bootstrap iterations ({samples.shape[0]}) for meaningful "
+                  "statistics!\n")
+    else:
+        out.write("\n".join(bootstrap_summary(bestfit, samples, cfg.param_names, cfg.fixed.astype(bool))) + "\n")
+    if args.save_bootstrap:
+        with open(args.save_bootstrap, "w") as f:
+            f.write("\n".join(bootstrap_file_lines(cfg.functions, cfg.param_names, _NPARAMS, samples,
+                                                   args.bootstrap)) + "\n")
+    return samples, status
 
 
 def flux_table(names, fluxes, total, zero_point=None, labels=None):

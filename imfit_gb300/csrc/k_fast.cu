@@ -373,6 +373,7 @@ __global__ void __launch_bounds__(1024) k_fast_stat_rows(FastArgs a, FastGeom g,
     a.data += img * a.dataStride;
     a.weight += img * a.dataStride;
   }
+  if (a.count && a.countStride) a.count += (a.entry ? a.entry[b] : b) * a.countStride;  // batched bootstrap
   if (nl > 0) {
     for (int idx = threadIdx.x; idx < nl * (M + 1); idx += blockDim.x) {
       const int l = idx / (M + 1), k = idx - l * (M + 1);
@@ -898,6 +899,7 @@ __global__ void __launch_bounds__(1024) k_fast_jtwj_rows(FastArgs a, FastGeom g,
     a.data += img * a.dataStride;
     a.weight += img * a.dataStride;
   }
+  if (a.count && a.countStride) a.count += (a.entry ? a.entry[b] : b) * a.countStride;  // batched bootstrap
   const cplx<float> *src = dspec + (long)b * nD * g.specBatch + (long)row * g.specPitch;
   for (int idx = threadIdx.x; idx < nD * M; idx += blockDim.x) {
     const int j = idx / M, k = idx - j * M;

@@ -147,6 +147,7 @@ struct FastArgs {
   const float *weight;   // internal weights (masked), or multiplicity-weighted
   const float *extra;    // Cash extra terms (or null)
   const float *count;    // bootstrap multiplicity per pixel (or null)
+  long countStride;      // batched bootstrap: stride between the samples' counts (0: one sample)
   long dataStride;       // image stacks: data/weight stride between batch entries (0: one image)
   const int *entry;      // image stacks: image of batch entry b is entry[b] (null: b)
   int kind;              // 0 chi^2, 1 Cash

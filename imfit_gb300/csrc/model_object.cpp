@@ -206,6 +206,8 @@ struct imfit_model_s {
   FastGeom fg{};
   FFTLen Fx, Fy, FRx, FRy;
   DevBuf<float> dH32, dHr32, dData32, dW32, dExtra32, dCount32, dBg, dRegModel, dRegG, dModelOut;
+  DevBuf<float> dCountBatch;  // batched bootstrap: [sample][data pixel] multiplicities
+  int bootBatch = 0;          // number of samples while a batched bootstrap fit runs
   DevBuf<float> dSpec32, dRSpec32;  // complex
   DevBuf<CompDesc> dDesc;
   DevBuf<CompF32> dComps32;
@@ -1132,9 +1134,10 @@ struct imfit_model_s {
     a.data = dData32.p;
     a.weight = dW32.p;
     a.extra = (useCash && pmlr) ? dExtra32.p : nullptr;
-    a.count = doBootstrap ? dCount32.p : nullptr;
+    a.count = bootBatch ? dCountBatch.p : (doBootstrap ? dCount32.p : nullptr);
+    a.countStride = bootBatch ? nDataVals : 0;
     a.dataStride = stack.n ? nDataVals : 0;
-    a.entry = stack.n ? curEntry : nullptr;
+    a.entry = (stack.n || bootBatch) ? curEntry : nullptr;
     a.kind = useCash ? 1 : 0;
     a.modelErrors = modelErrors ? 1 : 0;
     a.effGain = (float)effGain;
@@ -1404,9 +1407,10 @@ struct imfit_model_s {
     if (!st) st = ensureJtwjCap(B);
     if (st) return st;
     curEntry = nullptr;
-    if (imageMap && stack.n) {
+    const int nEntries = stack.n ? stack.n : bootBatch;
+    if (imageMap && nEntries) {
       for (int i = 0; i < B; i++)
-        if (imageMap[i] < 0 || imageMap[i] >= stack.n) return fail(IMFIT_E_ARG, "image index out of range");
+        if (imageMap[i] < 0 || imageMap[i] >= nEntries) return fail(IMFIT_E_ARG, "image index out of range");
       cudaError_t e0 = dEntry.reserve(B);
       if (!e0) e0 = cudaMemcpyAsync(dEntry.p, imageMap, sizeof(int) * B, cudaMemcpyHostToDevice, stream);
       if (e0) return cuda_fail(e0, "image map upload");
@@ -1496,7 +1500,7 @@ struct imfit_model_s {
       Bs.resize((size_t)k * n);
       for (int r = 0; r < k; r++)
         std::copy(X + (size_t)idx[r] * n, X + (size_t)(idx[r] + 1) * n, Xs.begin() + (size_t)r * n);
-      int st = jtwjHost(k, Xs.data(), Ss.data(), As.data(), Bs.data(), stack.n ? idx.data() : nullptr);
+      int st = jtwjHost(k, Xs.data(), Ss.data(), As.data(), Bs.data(), (stack.n || bootBatch) ? idx.data() : nullptr);
       if (st) return st;
       for (int r = 0; r < k; r++) {
         const int i = idx[r];
@@ -1545,16 +1549,73 @@ struct imfit_model_s {
     return 0;
   }
 
-  int makeBootstrapSample() {
-    if (!finalSetupDone) return fail(IMFIT_E_STATE, "FinalSetupForFitting not called");
-    bootIdx.assign(nValid, 0);
+  // ModelObject::MakeBootstrapSample (core/model_object.cpp:2061-2087): nValid
+  // draws of a data index by genrand_real2, rejecting pixels of weight <= 0
+  void drawBootstrap(std::vector<long> &idx) {
+    idx.assign(nValid, 0);
     for (long i = 0; i < nValid; i++) {
       long n;
       do {
         n = (long)floor(rng.real2() * nDataVals);
       } while (!(weight[n] > 0.0));
-      bootIdx[i] = n;
+      idx[i] = n;
     }
+  }
+
+  // K bootstrap refits at once (core/bootstrap_errors.cpp:160-240 runs them one
+  // after another): the next K samples of the MT19937 stream, each held as
+  // per-pixel multiplicities, fitted from bestfit by the lockstep batched LM.
+  int bootstrapFitBatch(int K, const double *bestfit, const int *fixed, const double *lower, const double *upper,
+                        double ftol, int maxIter, double *params, double *stats, int *nIter, int *status) {
+    if (!doBootstrap) return fail(IMFIT_E_STATE, "UseBootstrap not called");
+    if (stack.n) return fail(IMFIT_E_UNSUPPORTED, "bootstrap refits of an image stack");
+    if (K < 1 || !bestfit || !params) return fail(IMFIT_E_ARG, "bad bootstrap batch arguments");
+    int st = prepareFast();
+    if (st) return st;
+    std::vector<float> cnt((size_t)K * nDataVals, 0.f);
+    for (int k = 0; k < K; k++) {
+      drawBootstrap(bootIdx);
+      float *c = cnt.data() + (size_t)k * nDataVals;
+      for (long i = 0; i < nValid; i++) c[bootIdx[i]] += 1.f;
+    }
+    // the last sample drawn stays the handle's current one, as after the reference's loop
+    st = uploadBootstrap();
+    if (st) return st;
+    cudaError_t e = dCountBatch.reserve(cnt.size());
+    if (!e) e = cudaMemcpy(dCountBatch.p, cnt.data(), sizeof(float) * cnt.size(), cudaMemcpyHostToDevice);
+    if (e) return cuda_fail(e, "bootstrap multiplicities");
+    const int n = nParamsTot;
+    for (int k = 0; k < K; k++) std::copy(bestfit, bestfit + n, params + (size_t)k * n);
+    std::vector<double> lo, hi;
+    if (lower) {
+      lo.resize((size_t)K * n);
+      for (int k = 0; k < K; k++) std::copy(lower, lower + n, lo.begin() + (size_t)k * n);
+    }
+    if (upper) {
+      hi.resize((size_t)K * n);
+      for (int k = 0; k < K; k++) std::copy(upper, upper + n, hi.begin() + (size_t)k * n);
+    }
+    dropGraph();
+    bootBatch = K;
+    st = fitLMBatch(K, params, fixed, lower ? lo.data() : nullptr, upper ? hi.data() : nullptr, ftol, maxIter,
+                    stats, nIter, status);
+    bootBatch = 0;
+    dropGraph();
+    return st;
+  }
+
+  void dropGraph() {
+    if (graph.exec) cudaGraphExecDestroy(graph.exec);
+    graph = Captured{};
+  }
+
+  int makeBootstrapSample() {
+    if (!finalSetupDone) return fail(IMFIT_E_STATE, "FinalSetupForFitting not called");
+    drawBootstrap(bootIdx);
+    return uploadBootstrap();
+  }
+
+  int uploadBootstrap() {
     cudaError_t e = dBoot.reserve(nValid);
     if (!e) e = cudaMemcpy(dBoot.p, bootIdx.data(), sizeof(long) * nValid, cudaMemcpyHostToDevice);
     if (!e && fastReady) e = uploadCounts();
@@ -1978,6 +2039,14 @@ int imfit_FitLM(imfit_model_t m, double *params, const int *fixed, const double 
   if (nEval) *nEval = res.nEval;
   if (status) *status = res.status;
   return st < 0 ? st : 0;
+}
+
+int imfit_BootstrapFitBatch(imfit_model_t m, int nSamples, const double *bestfit, const int *fixed,
+                            const double *lower, const double *upper, double ftol, int maxIter, double *params,
+                            double *statistics, int *nIter, int *status) {
+  if (!m) return IMFIT_E_ARG;
+  return m->bootstrapFitBatch(nSamples, bestfit, fixed, lower, upper, ftol, maxIter, params, statistics, nIter,
+                              status);
 }
 
 int imfit_FitLMBatch(imfit_model_t m, int B, double *params, const int *fixed, const double *lower,

@@ -117,3 +117,93 @@ def differential_evolution(model, x0, lower, upper, fixed=None, F=0.7, CR=1.0,
     xb = pop[best].copy()
     return dict(params=xb, statistic=model.get_fit_statistic(xb), generations=generation,
                 converged=converged, population=NP, batched_calls=calls, fast_statistic=float(energy[best]))
+
+
+# --------------------------------------------------------------------------
+# Bootstrap resampling errors (core/bootstrap_errors.cpp:86-330,
+# core/statistics.cpp:54-100).  All refits of a chunk run at once through
+# imfit_BootstrapFitBatch; the samples are the same MT19937 index draws as the
+# reference's sequential iterations, in the same order.
+
+ONESIGMA_LOWER, ONESIGMA_UPPER = 0.1585, 0.8415
+
+
+def _round_half_away(x):
+    return int(np.floor(x + 0.5)) if x >= 0 else -int(np.floor(-x + 0.5))
+
+
+def standard_deviation(v):
+    """statistics.cpp:54-72: sample standard deviation (n - 1)."""
+    v = np.asarray(v, dtype=float)
+    s = float(np.sum((v - np.mean(v)) ** 2))
+    return float(np.sqrt(s / (v.size - 1))) if s >= 0 else 0.0
+
+
+def confidence_interval(v):
+    """statistics.cpp:84-100: the 68.3% interval from the sorted values at
+    indices round(0.1585 n) - 1 and round(0.8415 n), clamped to the range."""
+    v = np.sort(np.asarray(v, dtype=float))
+    n = v.size
+    lo = max(_round_half_away(ONESIGMA_LOWER * n) - 1, 0)
+    hi = min(_round_half_away(ONESIGMA_UPPER * n), n - 1)
+    return float(v[lo]), float(v[hi])
+
+
+def bootstrap_errors(model, bestfit, n_iterations, seed, fixed=None, lower=None, upper=None, ftol=1e-8,
+                     max_iter=0, chunk=64):
+    """Bootstrap refits of model (chi^2 or Poisson-MLR) from bestfit; returns
+    (params of the successful iterations [n_ok x nParams], statuses).  The
+    reference seeds MT19937 with seed, draws one sample in UseBootstrap and
+    then one per iteration (bootstrap_errors.cpp:171-215); so does this."""
+    if seed <= 0:
+        raise ValueError("give a positive seed (the reference seeds from the clock otherwise)")
+    model.use_bootstrap(int(seed))
+    out, statuses = [], []
+    done = 0
+    while done < n_iterations:
+        k = min(chunk, n_iterations - done)
+        r = model.bootstrap_fit_batch(k, bestfit, fixed=fixed, lower=lower, upper=upper, ftol=ftol,
+                                      max_iter=max_iter)
+        ok = r["status"] > 0
+        out.append(r["params"][ok])
+        statuses.append(r["status"])
+        done += k
+    return np.concatenate(out) if out else np.empty((0, len(bestfit))), np.concatenate(statuses)
+
+
+def bootstrap_summary(bestfit, samples, names, fixed=None):
+    """Lines of PrintBootstrapSummary (bootstrap_errors.cpp:339-369)."""
+    samples = np.asarray(samples, dtype=float)
+    n = samples.shape[0]
+    fixed = np.zeros(len(bestfit), dtype=bool) if fixed is None else np.asarray(fixed, dtype=bool)
+    lines = ["", f"Statistics for parameter values from bootstrap resampling ({n} successful iterations):",
+             "Best-fit\t\t Bootstrap      [68% conf.int., half-width]; (mean +/- standard deviation)"]
+    for i, name in enumerate(names):
+        if fixed[i]:
+            lines.append(f"{name} = {bestfit[i]:g}     [fixed parameter]")
+            continue
+        lo, hi = confidence_interval(samples[:, i])
+        sd = standard_deviation(samples[:, i])
+        lines.append(f"{name} = {bestfit[i]:g}  +{hi - bestfit[i]:g}, -{bestfit[i] - lo:g}    "
+                     f"[{lo:g} -- {hi:g}, {(hi - lo) / 2.0:g}];  ({np.mean(samples[:, i]):g} +/- {sd:g})")
+    return lines
+
+
+def bootstrap_file_lines(functions, param_names, n_params, samples, n_iterations):
+    """The --save-bootstrap file (bootstrap_errors.cpp:111-114 and
+    ModelObject::GetParamHeader / PrintModelParamsHorizontalString,
+    core/model_object.cpp:1941-2033): functions = [(name, starts_new_set)],
+    param_names = all parameter names in order, n_params = {name: count}."""
+    header = "# "
+    j, n_set = 0, 0
+    for fi, (fname, new_set) in enumerate(functions):
+        if new_set or fi == 0:
+            n_set += 1
+            header += f"X0_{n_set}\t\tY0_{n_set}\t\t"
+            j += 2
+        for _ in range(n_params[fname]):
+            header += f"{param_names[j]}_{fi + 1}\t"
+            j += 1
+    lines = ["#", f"# Bootstrap resampling output ({n_iterations} iterations requested):", header]
+    lines += ["\t".join(format(float(v), "#.10g") for v in row) for row in np.atleast_2d(samples)]
+    return lines

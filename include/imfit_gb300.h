@@ -220,6 +220,18 @@ int imfit_FitLM(imfit_model_t m, double *params, const int *fixed, const double 
  * (nBatch each) may be NULL; status codes as imfit_FitLM. */
 int imfit_FitLMBatch(imfit_model_t m, int nBatch, double *params, const int *fixed, const double *lower,
                      const double *upper, double ftol, int maxIter, double *statistics, int *nIter, int *status);
+/* Bootstrap refits, replacing the loop of BootstrapErrorsBase
+ * (core/bootstrap_errors.cpp:160-240: MakeBootstrapSample, then LevMarFit from
+ * the best-fit vector, per iteration): draws the next nSamples samples of the
+ * MT19937 stream seeded by imfit_UseBootstrap (the same index sequence as the
+ * reference's iterations), holds each as per-pixel multiplicities and fits all
+ * of them at once with the batched LM from bestfit.  fixed, lower, upper:
+ * nParams each (shared; NULL allowed).  params: nSamples x nParams out;
+ * statistics, nIter, status: nSamples each (may be NULL), status codes as
+ * imfit_FitLM (> 0: success).  chi^2 or Poisson-MLR. */
+int imfit_BootstrapFitBatch(imfit_model_t m, int nSamples, const double *bestfit, const int *fixed,
+                            const double *lower, const double *upper, double ftol, int maxIter, double *params,
+                            double *statistics, int *nIter, int *status);
 
 /* ---- image stacks (fast path; no counterpart in the reference) ------------- */
 /* Many cutouts fitted with one model: nImages images of nColumns x nRows

@@ -163,3 +163,61 @@ def test_de_driver_on_the_batched_statistic(gpu):
     s_lm = m.get_fit_statistic(lm["params"])
     assert r["statistic"] <= s_lm * (1 + 1e-6)
     assert np.all(np.abs(r["params"] - lm["params"]) <= 0.1 * d["lm_errors_printed"])
+
+
+def _ic3478_model(gpu_or_oracle_cls, d):
+    m = gpu_or_oracle_cls()
+    m.add_function("Sersic", True)
+    m.finish_functions()
+    m.add_image_data(d["data"].astype(np.float64))
+    m.add_image_characteristics(float(d["gain"]), float(d["read_noise"]), 1.0, 1, float(d["original_sky"]))
+    assert m.final_setup() == 0
+    return m
+
+
+def test_batched_bootstrap_matches_sequential_refits_and_oracle_samples(gpu, oracle_mod):
+    """imfit_BootstrapFitBatch against the reference's loop
+    (core/bootstrap_errors.cpp:171-215: UseBootstrap, then MakeBootstrapSample
+    and an LM refit per iteration) run one sample at a time on the same
+    handle type, and each sample's statistic against the FP64 oracle's
+    bootstrap statistic for the same seed and iteration."""
+    from imfit_gb300 import solvers
+    d = np.load(os.path.join(GOLDEN, "ic3478.npz"))
+    best = d["lm_params_printed"]
+    K, seed = 12, 4321
+    mb = _ic3478_model(gpu.ModelObject, d)
+    samples, status = solvers.bootstrap_errors(mb, best, K, seed, lower=d["lo"], upper=d["hi"], chunk=5)
+    assert status.shape == (K,) and np.all(status > 0) and samples.shape == (K, 7)
+    ms = _ic3478_model(gpu.ModelObject, d)
+    ms.use_bootstrap(seed)
+    o = _ic3478_model(oracle_mod.OracleModel, d)
+    o.use_bootstrap(seed)
+    for k in range(K):
+        ms.make_bootstrap_sample()
+        o.make_bootstrap_sample()
+        r = ms.fit_lm(best, lower=d["lo"], upper=d["hi"])
+        err = np.abs(r["params"] - samples[k]) / d["lm_errors_printed"]
+        assert np.all(err < 0.05), (k, err)
+        s_o = o.get_fit_statistic(samples[k])
+        s_g = ms.get_fit_statistic(samples[k])  # plain FP64 path, bootstrap sample k
+        assert abs(s_g - s_o) <= 1e-10 * s_o, (k, s_g, s_o)
+    # the spread of the refits is the parameters' uncertainty (mpfit's errors, within sampling noise)
+    sd = np.array([solvers.standard_deviation(samples[:, j]) for j in range(7)])
+    assert np.all(sd > 0.3 * d["lm_errors_printed"]) and np.all(sd < 3.0 * d["lm_errors_printed"]), sd
+
+
+def test_cli_bootstrap_output(gpu, tmp_path):
+    """--bootstrap N --save-bootstrap F: the summary block and the file
+    (header of GetParamHeader, one row per successful iteration)."""
+    from imfit_gb300 import cli
+    _ic3478_files(tmp_path)
+    buf = io.StringIO()
+    cli.run([str(tmp_path / "c.dat"), str(tmp_path / "data.fits"), "--save-params", str(tmp_path / "b.dat"),
+             "--bootstrap", "8", "--seed", "99", "--save-bootstrap", str(tmp_path / "boot.dat")], out=buf)
+    text = buf.getvalue()
+    assert "Statistics for parameter values from bootstrap resampling (8 successful iterations):" in text
+    assert "\nr_e = " in text
+    lines = (tmp_path / "boot.dat").read_text().splitlines()
+    assert lines[1] == "# Bootstrap resampling output (8 iterations requested):"
+    assert lines[2] == "# X0_1\t\tY0_1\t\tPA_1\tell_1\tn_1\tI_e_1\tr_e_1\t"
+    assert len(lines) == 3 + 8 and all(len(x.split("\t")) == 7 for x in lines[3:])

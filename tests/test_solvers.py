@@ -80,3 +80,28 @@ def test_flux_table_matches_makeimage_output():
     assert lines[5] == "Total                     2.6169e+06      ---     1.00000"
     zp = flux_table(["Gaussian"], [1.0e4], 1.0e4, zero_point=26.0)
     assert zp[1] == "Gaussian                  1.0000e+04   16.0000     1.00000"
+
+
+def test_bootstrap_statistics_follow_the_reference_formulas():
+    """core/statistics.cpp:54-100: n - 1 standard deviation; interval indices
+    round(0.1585 n) - 1 and round(0.8415 n) of the sorted values."""
+    v = np.arange(10.0)[::-1]
+    assert solvers.confidence_interval(v) == (1.0, 8.0)  # indices 1 and 8
+    assert solvers.confidence_interval([3.0, 1.0]) == (1.0, 3.0)  # clamped for n < 4
+    assert abs(solvers.standard_deviation([1.0, 2.0, 3.0, 4.0]) - np.std([1, 2, 3, 4], ddof=1)) < 1e-15
+    lines = solvers.bootstrap_summary([1.0, 5.0], np.array([[0.9, 5.0], [1.1, 5.0], [1.0, 5.0]]), ["a", "b"],
+                                      fixed=[False, True])
+    assert lines[1].endswith("(3 successful iterations):")
+    assert lines[3] == "a = 1  +0.1, -0.1    [0.9 -- 1.1, 0.1];  (1 +/- 0.1)"
+    assert lines[4] == "b = 5     [fixed parameter]"
+
+
+def test_bootstrap_file_layout():
+    """GetParamHeader / PrintModelParamsHorizontalString (core/model_object.cpp:1941-2033)."""
+    from imfit_gb300.config import _NPARAMS
+    names = ["X0", "Y0", "PA", "ell", "n", "I_e", "r_e", "I_sky"]
+    lines = solvers.bootstrap_file_lines([("Sersic", True), ("FlatSky", False)], names, _NPARAMS,
+                                         np.arange(8.0)[None, :] + 0.5, 5)
+    assert lines[:2] == ["#", "# Bootstrap resampling output (5 iterations requested):"]
+    assert lines[2] == "# X0_1\t\tY0_1\t\tPA_1\tell_1\tn_1\tI_e_1\tr_e_1\tI_sky_2\t"
+    assert lines[3].split("\t")[:2] == ["0.5000000000", "1.500000000"]
