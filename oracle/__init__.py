@@ -109,6 +109,14 @@ def _bind(lib, prefix):
         lib.orc_function_nparams.argtypes = [_S]
         lib.orc_set_fft_smooth.restype = None
         lib.orc_set_fft_smooth.argtypes = [_P, _I]
+        lib.orc_set_point_source_method.restype = _I
+        lib.orc_set_point_source_method.argtypes = [_P, _I, _I]
+        lib.orc_get_single_function_image.restype = _I
+        lib.orc_get_single_function_image.argtypes = [_P, _DP, _I, _DP]
+        lib.orc_interpolate_psf.restype = _I
+        lib.orc_interpolate_psf.argtypes = [_I, _DP, _I, _I, _DP, _DP, _L, _DP]
+        lib.orc_lanczos.restype = _D
+        lib.orc_lanczos.argtypes = [_D, _I]
     else:
         lib.ref_add_oversampled_psf.restype = _I
         lib.ref_add_oversampled_psf.argtypes = [_P, _I, _I, _DP, _I, _S, _I]
@@ -311,6 +319,18 @@ class OracleModel(_CModel):
             return None
         return out.reshape(self.nrows, self.ncols)
 
+    def set_point_source_method(self, index, method):
+        """method: 'bicubic', 'lanczos2' or 'lanczos3' (PointSource's optional parameter)."""
+        return self.lib.orc_set_point_source_method(self.h, int(index), INTERPOLATORS[method.lower()])
+
+    def get_single_function_image(self, params, function_index):
+        p = _f64(params)
+        out = np.empty((self.nrows, self.ncols))
+        st = self.lib.orc_get_single_function_image(self.h, _dp(p), int(function_index), _dp(out))
+        if st != 0:
+            raise ValueError(f"GetSingleFunctionImage failed ({st})")
+        return out
+
     def get_bootstrap_indices(self):
         out = np.empty(self.n_valid, dtype=np.int64)
         n = self.lib.orc_get_bootstrap_indices(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_long)))
@@ -346,6 +366,28 @@ class RefModel(_CModel):
                                  ctypes.byref(chi2i))
         return dict(status=st, params=p, niter=niter.value, nfev=nfev.value, chi2=chi2.value,
                     chi2_init=chi2i.value)
+
+
+INTERPOLATORS = {"bicubic": 1, "lanczos2": 2, "lanczos3": 3}
+
+
+def interpolate_psf(kind, psf, dx, dy):
+    """PsfInterpolator::GetValue (function_objects/psf_interpolators.cpp) of
+    the given kind on psf at offsets (dx, dy) from its centre."""
+    lib = _load("orc")
+    psf = _f64(psf)
+    dx = _f64(np.atleast_1d(dx))
+    dy = _f64(np.broadcast_to(dy, dx.shape))
+    out = np.empty(dx.shape)
+    st = lib.orc_interpolate_psf(INTERPOLATORS[kind], _dp(psf), psf.shape[1], psf.shape[0], _dp(dx), _dp(dy),
+                                 dx.size, _dp(out))
+    if st != 0:
+        raise ValueError(f"PSF interpolator setup failed ({st})")
+    return out
+
+
+def lanczos(x, n):
+    return _load("orc").orc_lanczos(float(x), int(n))
 
 
 def set_los_epsrel(epsrel):

@@ -31,7 +31,10 @@
 #define MAXFUNC 64
 #define MAXREGIONS 16
 
-enum { F_SERSIC = 1, F_EXP, F_FLATSKY, F_GRING, F_MOFFAT, F_GAUSS, F_EXPDISK3D, F_FERRERS3D };
+enum { F_SERSIC = 1, F_EXP, F_FLATSKY, F_GRING, F_MOFFAT, F_GAUSS, F_EXPDISK3D, F_FERRERS3D, F_POINTSOURCE,
+       F_POINTSOURCEROT };
+enum { INTERP_BICUBIC = 1, INTERP_LANCZOS2 = 2, INTERP_LANCZOS3 = 3 };
+#define IS_POINT_SOURCE(t) ((t) == F_POINTSOURCE || (t) == F_POINTSOURCEROT)
 
 typedef struct {
   int type, npar, subsampling;
@@ -44,6 +47,10 @@ typedef struct {
   double fwhm, beta, alpha, sigma;         /* Moffat, Gaussian */
   double inc, cosInc, sinInc, J_0, z_0, alpha3, scaledZ0, two_to_alpha; /* 3-D */
   double barPA, cosBarPA, sinBarPA, R_bar, qb, q_z, a2, b2, c2, nf, integLimit;
+  double I_tot;                            /* PointSource, PointSourceRot */
+  int method;                              /* requested interpolation (optional parameter "method") */
+  int osScale;                             /* PointSource::oversamplingScale (state kept between calls) */
+  const struct ointerp *interp;            /* the interpolator currently assigned */
 } ofunc;
 
 static int type_from_name(const char *name, int *npar) {
@@ -51,7 +58,8 @@ static int type_from_name(const char *name, int *npar) {
       {"Sersic", F_SERSIC, 5},           {"Exponential", F_EXP, 4},
       {"FlatSky", F_FLATSKY, 1},         {"GaussianRing", F_GRING, 5},
       {"Moffat", F_MOFFAT, 5},           {"Gaussian", F_GAUSS, 4},
-      {"ExponentialDisk3D", F_EXPDISK3D, 6}, {"FerrersBar3D", F_FERRERS3D, 8}};
+      {"ExponentialDisk3D", F_EXPDISK3D, 6}, {"FerrersBar3D", F_FERRERS3D, 8},
+      {"PointSource", F_POINTSOURCE, 1},     {"PointSourceRot", F_POINTSOURCEROT, 2}};
   for (size_t i = 0; i < sizeof(tab) / sizeof(tab[0]); i++)
     if (strcmp(name, tab[i].n) == 0) {
       if (npar) *npar = tab[i].p;
@@ -152,7 +160,176 @@ static void func_setup(ofunc *f, const double *p, double xc, double yc) {
       f->integLimit = 1.01 * ((t < f->R_bar) ? f->R_bar : t);
       break;
     }
+    case F_POINTSOURCE: /* func_pointsource.cpp:206-211 */
+      f->I_tot = p[0];
+      break;
+    case F_POINTSOURCEROT: /* func_pointsource-rot.cpp:210-221 */
+      f->PA = p[0];
+      f->I_tot = p[1];
+      f->cosPA = cos((f->PA + 90.0) * DEG2RAD);
+      f->sinPA = sin((f->PA + 90.0) * DEG2RAD);
+      break;
   }
+}
+
+/* ------------------------- PSF interpolation ---------------------------- */
+/* function_objects/psf_interpolators.cpp.  The PSF's pixel centres sit at
+ * offsets n - (N-1)/2 from its centre; outside [-(N-1)/2, (N-1)/2] the value is 0.
+ *
+ * Bicubic: the reference calls GSL's gsl_interp2d_bicubic (GSL 2.x, version
+ * not pinned by the reference; Ubuntu libgsl-dev in its CI).  Its published
+ * method: the partial derivatives z_x, z_y, z_xy at every grid point come from
+ * natural cubic splines through each grid line (z_xy = spline derivative along
+ * x of z_y), and each cell is the bicubic Hermite patch matching z, z_x, z_y,
+ * z_xy at its four corners; a point on an interior grid line belongs to the
+ * cell above it, the last grid line to the cell below.  Restated here from
+ * that description; pinned by unit_tests/unittest_psf_interpolators.t.h.
+ *
+ * Lanczos2/3: psf_interpolators.cpp:139-300 -- a sum over the (2n+1)^2 nearest
+ * samples (FindIndex = floor(x - x_0)), weights Lanczos(dx) Lanczos(dy), and
+ * the PSF read as data[ix * nColumns + iy] (x index first, as the reference
+ * indexes it). */
+typedef struct ointerp {
+  int kind, nc, nr;
+  double xb, yb;
+  double *z, *zx, *zy, *zxy; /* bicubic: [row iy][col ix] */
+  double *data;              /* lanczos: copy of the PSF, row-major */
+} ointerp;
+
+/* derivative of the natural cubic spline through (k, v[k*stride]), k < n, at
+ * every knot, written to out[k*stride] (unit knot spacing) */
+static void spline_knot_derivs(const double *v, long stride, int n, double *out) {
+  double *M = (double *)calloc((size_t)n, sizeof(double));
+  double *c = (double *)calloc((size_t)n, sizeof(double));
+  double *d = (double *)calloc((size_t)n, sizeof(double));
+  /* second derivatives M: M_0 = M_{n-1} = 0, M_{k-1} + 4 M_k + M_{k+1} = 6 (v_{k+1} - 2 v_k + v_{k-1}) */
+  if (n > 2) {
+    int m = n - 2;
+    for (int i = 0; i < m; i++) {
+      int k = i + 1;
+      double rhs = 6.0 * (v[(k + 1) * stride] - 2.0 * v[k * stride] + v[(k - 1) * stride]);
+      double diag = 4.0;
+      if (i > 0) {
+        double w = 1.0 / c[i - 1];
+        diag -= w;
+        rhs -= w * d[i - 1];
+      }
+      c[i] = diag;
+      d[i] = rhs;
+    }
+    /* back substitution: c holds the eliminated diagonal, d the eliminated rhs */
+    M[m] = d[m - 1] / c[m - 1];
+    for (int i = m - 2; i >= 0; i--) M[i + 1] = (d[i] - M[i + 2]) / c[i];
+  }
+  for (int k = 0; k < n - 1; k++)
+    out[k * stride] = (v[(k + 1) * stride] - v[k * stride]) - (2.0 * M[k] + M[k + 1]) / 6.0;
+  out[(n - 1) * stride] = (v[(n - 1) * stride] - v[(n - 2) * stride]) + (M[n - 2] + 2.0 * M[n - 1]) / 6.0;
+  free(M);
+  free(c);
+  free(d);
+}
+
+static void interp_free(ointerp *ip) {
+  free(ip->z);
+  free(ip->zx);
+  free(ip->zy);
+  free(ip->zxy);
+  free(ip->data);
+  memset(ip, 0, sizeof(*ip));
+}
+
+static int interp_build(ointerp *ip, int kind, const double *psf, int nc, int nr) {
+  interp_free(ip);
+  if (nc < 4 || nr < 4) return -2; /* model_object.cpp:356-361 */
+  ip->kind = kind;
+  ip->nc = nc;
+  ip->nr = nr;
+  ip->xb = (nc - 1) / 2.0;
+  ip->yb = (nr - 1) / 2.0;
+  long np = (long)nc * nr;
+  if (kind == INTERP_BICUBIC) {
+    ip->z = (double *)malloc(sizeof(double) * np);
+    ip->zx = (double *)malloc(sizeof(double) * np);
+    ip->zy = (double *)malloc(sizeof(double) * np);
+    ip->zxy = (double *)malloc(sizeof(double) * np);
+    memcpy(ip->z, psf, sizeof(double) * np);
+    for (int r = 0; r < nr; r++) spline_knot_derivs(ip->z + (long)r * nc, 1, nc, ip->zx + (long)r * nc);
+    for (int c = 0; c < nc; c++) spline_knot_derivs(ip->z + c, nc, nr, ip->zy + c);
+    for (int r = 0; r < nr; r++) spline_knot_derivs(ip->zy + (long)r * nc, 1, nc, ip->zxy + (long)r * nc);
+  } else {
+    ip->data = (double *)malloc(sizeof(double) * np);
+    memcpy(ip->data, psf, sizeof(double) * np);
+  }
+  return 0;
+}
+
+/* Lanczos kernel: psf_interpolators.cpp:299-309 */
+static double lanczos(double x, int n) {
+  const double pi = 3.14159265358979, pi2 = 9.86960440108936;
+  double a = fabs(x);
+  if (a < 1.0e-6) return 1.0;
+  if (a > n) return 0.0;
+  return (n * sin(pi * a) * sin(pi * a / n)) / (pi2 * a * a);
+}
+
+/* cubic Hermite basis on [0,1]: value weights for the left/right ends and
+ * slope weights for the left/right ends */
+static void hermite(double t, double *h0, double *h1, double *g0, double *g1) {
+  double t2 = t * t, t3 = t2 * t;
+  *h0 = 2.0 * t3 - 3.0 * t2 + 1.0;
+  *h1 = -2.0 * t3 + 3.0 * t2;
+  *g0 = t3 - 2.0 * t2 + t;
+  *g1 = t3 - t2;
+}
+
+static double interp_value(const ointerp *ip, double x, double y) {
+  if (x < -ip->xb || x > ip->xb || y < -ip->yb || y > ip->yb) return 0.0;
+  if (ip->kind == INTERP_BICUBIC) {
+    double fx = x + ip->xb, fy = y + ip->yb; /* grid coordinates */
+    int i = (int)floor(fx), j = (int)floor(fy);
+    if (i > ip->nc - 2) i = ip->nc - 2;
+    if (j > ip->nr - 2) j = ip->nr - 2;
+    double t = (x - (i - ip->xb)), u = (y - (j - ip->yb));
+    double a0, a1, b0, b1, c0, c1, e0, e1;
+    hermite(t, &a0, &a1, &b0, &b1);
+    hermite(u, &c0, &c1, &e0, &e1);
+    const int nc = ip->nc;
+    long k00 = (long)j * nc + i, k10 = k00 + 1, k01 = k00 + nc, k11 = k01 + 1;
+    double v = 0.0;
+    v += ip->z[k00] * a0 * c0 + ip->z[k10] * a1 * c0 + ip->z[k01] * a0 * c1 + ip->z[k11] * a1 * c1;
+    v += ip->zx[k00] * b0 * c0 + ip->zx[k10] * b1 * c0 + ip->zx[k01] * b0 * c1 + ip->zx[k11] * b1 * c1;
+    v += ip->zy[k00] * a0 * e0 + ip->zy[k10] * a1 * e0 + ip->zy[k01] * a0 * e1 + ip->zy[k11] * a1 * e1;
+    v += ip->zxy[k00] * b0 * e0 + ip->zxy[k10] * b1 * e0 + ip->zxy[k01] * b0 * e1 + ip->zxy[k11] * b1 * e1;
+    return v;
+  }
+  int n = (ip->kind == INTERP_LANCZOS2) ? 2 : 3;
+  int imx = (int)floor((x + ip->xb) / 1.0), imy = (int)floor((y + ip->yb) / 1.0);
+  double v = 0.0;
+  for (int a = -n; a <= n; a++) {
+    int ix = imx + a;
+    if (ix < 0 || ix >= ip->nc) continue;
+    double xd = ix - ip->xb;
+    for (int b = -n; b <= n; b++) {
+      int iy = imy + b;
+      if (iy < 0 || iy >= ip->nr) continue;
+      double yd = iy - ip->yb;
+      v += lanczos(x - xd, n) * lanczos(y - yd, n) * ip->data[(long)ix * ip->nc + iy];
+    }
+  }
+  return v;
+}
+
+/* PointSource::GetValue / PointSourceRot::GetValue (func_pointsource.cpp:220-229,
+ * func_pointsource-rot.cpp:229-243) */
+static double point_source_value(const ofunc *f, double x, double y) {
+  double xd = f->osScale * (x - f->x0), yd = f->osScale * (y - f->y0);
+  if (f->type == F_POINTSOURCEROT) {
+    double xp = xd * f->cosPA + yd * f->sinPA;
+    double yp = -xd * f->sinPA + yd * f->cosPA;
+    xd = xp;
+    yd = yp;
+  }
+  return f->I_tot * interp_value(f->interp, xd, yd);
 }
 
 /* CalculateIntensity(r) of the 2-D radial classes */
@@ -317,6 +494,7 @@ static double func_total_flux(const ofunc *f) {
     return f->q * L * tgamma(2 * f->n) / bn2n;
   }
   if (f->type == F_EXP) return (1.0 - f->ell) * 2.0 * 3.14159265358979 * f->I_0 * f->h * f->h;
+  if (IS_POINT_SOURCE(f->type)) return f->I_tot; /* func_pointsource.cpp:241-244 */
   return -1.0;
 }
 
@@ -432,6 +610,7 @@ typedef struct {
   double subpixFrac, startOff;
   double *model;
   oconv conv;
+  ointerp interp; /* bicubic, from the oversampled PSF as given (oversampled_region.cpp:181-186) */
 } oregion;
 
 struct orc_model {
@@ -453,6 +632,9 @@ struct orc_model {
   oregion reg[MAXREGIONS];
   int maxThreads;
   int fftSmooth;
+  int nPointSources;
+  double *psfLocal; /* AddPSFVector's copy (NormalizePSF'd when asked) */
+  ointerp mainInterp;
 };
 
 orc_model *orc_create(void) {
@@ -475,10 +657,13 @@ void orc_destroy(orc_model *m) {
   free(m->model);
   free(m->dev);
   free(m->bootIdx);
+  free(m->psfLocal);
+  interp_free(&m->mainInterp);
   if (m->doConv) conv_free(&m->conv);
   for (int i = 0; i < m->nRegions; i++) {
     free(m->reg[i].model);
     if (m->reg[i].doConv) conv_free(&m->reg[i].conv);
+    interp_free(&m->reg[i].interp);
   }
   free(m);
 }
@@ -501,9 +686,37 @@ int orc_add_function(orc_model *m, const char *name, int newSet, int subsampling
   f->type = t;
   f->npar = np;
   f->subsampling = subsampling ? 1 : 0;
+  f->method = INTERP_BICUBIC; /* func_pointsource.h:53 */
+  f->osScale = 1;
   m->setStart[m->nFunctions] = (newSet || m->nFunctions == 0) ? 1 : 0;
+  if (IS_POINT_SOURCE(t)) m->nPointSources++;
   m->nFunctions++;
   return 0;
+}
+
+/* PointSource optional parameter "method" (func_pointsource.cpp:140-180):
+ * 1 bicubic, 2 lanczos2, 3 lanczos3.  ModelObject builds one interpolator,
+ * of the first point source's kind, for all of them
+ * (model_object.cpp:294-305, 345-381). */
+int orc_set_point_source_method(orc_model *m, int index, int method) {
+  if (index < 0 || index >= m->nFunctions || !IS_POINT_SOURCE(m->f[index].type)) return -1;
+  if (method < INTERP_BICUBIC || method > INTERP_LANCZOS3) return -3;
+  if (m->f[index].type == F_POINTSOURCEROT && method == INTERP_LANCZOS3) return -3;
+  m->f[index].method = method;
+  interp_free(&m->mainInterp);
+  return 0;
+}
+
+static int ensure_main_interp(orc_model *m) {
+  if (!m->nPointSources || m->mainInterp.kind) return 0;
+  if (!m->psfLocal) return -1; /* model_object.cpp:349-353: no PSF image */
+  int method = INTERP_BICUBIC;
+  for (int n = 0; n < m->nFunctions; n++)
+    if (IS_POINT_SOURCE(m->f[n].type)) {
+      method = m->f[n].method;
+      break;
+    }
+  return interp_build(&m->mainInterp, method, m->psfLocal, m->nPsfCols, m->nPsfRows);
 }
 
 /* DefineFunctionSets + PopulateParameterNames: core/model_object.cpp:387-410 */
@@ -538,6 +751,14 @@ int orc_add_psf(orc_model *m, int ncols, int nrows, const double *psf, int norma
   memcpy(m->conv.psf, psf, sizeof(double) * np);
   m->conv.nColsPsf = normalize; /* stash the flag until the image size is known */
   m->doConv = 1;
+  free(m->psfLocal);
+  m->psfLocal = (double *)malloc(sizeof(double) * np);
+  memcpy(m->psfLocal, psf, sizeof(double) * np);
+  if (normalize) { /* NormalizePSF: model_object.cpp:2581-2594 */
+    double ks = kahan_sum(m->psfLocal, np);
+    for (long k = 0; k < np; k++) m->psfLocal[k] = m->psfLocal[k] / ks;
+  }
+  interp_free(&m->mainInterp);
   return m->modelSetupDone ? -1 : 0;
 }
 
@@ -773,6 +994,7 @@ int orc_add_oversampled_psf(orc_model *m, int ncols, int nrows, const double *ps
   r->nModelVals = (long)r->nModelCols * r->nModelRows;
   conv_setup(&r->conv, psf, ncols, nrows, normalize, r->nModelCols, r->nModelRows, m->fftSmooth);
   r->model = (double *)calloc((size_t)r->nModelVals, sizeof(double));
+  if (ncols >= 4 && nrows >= 4) interp_build(&r->interp, INTERP_BICUBIC, psf, ncols, nrows);
   m->nRegions++;
   return 0;
 }
@@ -792,6 +1014,7 @@ static void setup_functions(orc_model *m, const double *params) {
 static inline double pixel_sum(const orc_model *m, double x, double y) {
   double s = 0.0, err = 0.0, adj, tmp;
   for (int n = 0; n < m->nFunctions; n++) {
+    if (IS_POINT_SOURCE(m->f[n].type)) continue;
     adj = func_value(&m->f[n], x, y) - err;
     tmp = s + adj;
     err = (tmp - s) - adj;
@@ -821,21 +1044,56 @@ static void downsample_replace(const oregion *r, double *mainImg, int nMainCols,
     }
 }
 
-/* CreateModelImage: core/model_object.cpp:1103-1229; oversampled regions via
- * OversampledRegion::ComputeRegionAndDownsample core/oversampled_region.cpp:284-430 */
-void orc_create_model_image(orc_model *m, const double *params) {
-  setup_functions(m, params);
+/* Kahan sum over the point sources among functions [n0, n1) */
+static inline double point_source_sum(const orc_model *m, int n0, int n1, double x, double y) {
+  double s = 0.0, err = 0.0, adj, tmp;
+  for (int n = n0; n < n1; n++) {
+    if (!IS_POINT_SOURCE(m->f[n].type)) continue;
+    adj = point_source_value(&m->f[n], x, y) - err;
+    tmp = s + adj;
+    err = (tmp - s) - adj;
+    s = tmp;
+  }
+  return s;
+}
+
+/* Function set [n0, n1) (all functions, or the one of GetSingleFunctionImage)
+ * on the model grid and the oversampled regions.  Point sources are added
+ * after the convolution, with the ModelObject's interpolator on the main grid
+ * (model_object.cpp:1183-1216) and the region's bicubic one at the region's
+ * scale there (oversampled_region.cpp:363-408); each point source keeps the
+ * last region's scale afterwards, as PointSource::oversamplingScale does. */
+static void model_pass(orc_model *m, int n0, int n1, int convolveMain) {
   const long nmv = m->nModelVals;
   const int nmc = m->nModelCols;
   const int pr = m->doConv ? m->nPsfRows : 0, pc = m->doConv ? m->nPsfCols : 0;
+  int nps = 0;
+  for (int n = n0; n < n1; n++) nps += IS_POINT_SOURCE(m->f[n].type);
 #pragma omp parallel for schedule(static, 10)
   for (long k = 0; k < nmv; k++) {
     long j = k % nmc, i = k / nmc;
     double y = (double)(i - pr + 1);
     double x = (double)(j - pc + 1);
-    m->model[i * nmc + j] = pixel_sum(m, x, y);
+    double s = 0.0, err = 0.0, adj, tmp;
+    for (int n = n0; n < n1; n++) {
+      if (IS_POINT_SOURCE(m->f[n].type)) continue;
+      adj = func_value(&m->f[n], x, y) - err;
+      tmp = s + adj;
+      err = (tmp - s) - adj;
+      s = tmp;
+    }
+    m->model[i * nmc + j] = s;
   }
-  if (m->doConv) conv_apply(&m->conv, m->model);
+  if (m->doConv && convolveMain) conv_apply(&m->conv, m->model);
+  if (nps) {
+    for (int n = n0; n < n1; n++)
+      if (IS_POINT_SOURCE(m->f[n].type)) m->f[n].interp = &m->mainInterp;
+#pragma omp parallel for schedule(static, 10)
+    for (long k = 0; k < nmv; k++) {
+      long j = k % nmc, i = k / nmc;
+      m->model[i * nmc + j] += point_source_sum(m, n0, n1, (double)(j - pc + 1), (double)(i - pr + 1));
+    }
+  }
   for (int rr = 0; rr < m->nRegions; rr++) {
     oregion *r = &m->reg[rr];
     const int rmc = r->nModelCols;
@@ -844,12 +1102,53 @@ void orc_create_model_image(orc_model *m, const double *params) {
       long j = k % rmc, i = k / rmc;
       double y = r->y1 + r->startOff + (i - r->nPsfRows) * r->subpixFrac;
       double x = r->x1 + r->startOff + (j - r->nPsfCols) * r->subpixFrac;
-      r->model[i * rmc + j] = pixel_sum(m, x, y);
+      double s = 0.0, err = 0.0, adj, tmp;
+      for (int n = n0; n < n1; n++) {
+        if (IS_POINT_SOURCE(m->f[n].type)) continue;
+        adj = func_value(&m->f[n], x, y) - err;
+        tmp = s + adj;
+        err = (tmp - s) - adj;
+        s = tmp;
+      }
+      r->model[i * rmc + j] = s;
     }
     conv_apply(&r->conv, r->model);
+    if (nps) {
+      for (int n = n0; n < n1; n++)
+        if (IS_POINT_SOURCE(m->f[n].type)) {
+          m->f[n].interp = &r->interp;
+          m->f[n].osScale = r->scale;
+        }
+#pragma omp parallel for schedule(static, 10)
+      for (long k = 0; k < r->nModelVals; k++) {
+        long j = k % rmc, i = k / rmc;
+        double y = r->y1 + r->startOff + (i - r->nPsfRows) * r->subpixFrac;
+        double x = r->x1 + r->startOff + (j - r->nPsfCols) * r->subpixFrac;
+        r->model[i * rmc + j] += point_source_sum(m, n0, n1, x, y);
+      }
+    }
     downsample_replace(r, m->model, nmc, pc, pr);
   }
+}
+
+/* CreateModelImage: core/model_object.cpp:1103-1229; oversampled regions via
+ * OversampledRegion::ComputeRegionAndDownsample core/oversampled_region.cpp:284-430 */
+void orc_create_model_image(orc_model *m, const double *params) {
+  if (ensure_main_interp(m)) return;
+  setup_functions(m, params);
+  model_pass(m, 0, m->nFunctions, 1);
   m->modelComputed = 1;
+}
+
+/* GetSingleFunctionImage: core/model_object.cpp:1241-1336 (no convolution of
+ * a point source on the main grid; the regions see this function alone). */
+int orc_get_single_function_image(orc_model *m, const double *params, int index, double *out) {
+  if (index < 0 || index >= m->nFunctions || !m->model) return -1;
+  if (ensure_main_interp(m)) return -1;
+  setup_functions(m, params);
+  model_pass(m, index, index + 1, !IS_POINT_SOURCE(m->f[index].type));
+  m->modelComputed = 1;
+  return orc_get_model_image(m, out);
 }
 
 static inline long model_index(const orc_model *m, long z) {
@@ -1086,6 +1385,21 @@ int orc_fd_jacobian(orc_model *m, const double *params, double *fjac) {
 }
 
 /* --------------------------- single-function helpers --------------------- */
+/* PsfInterpolator::GetValue of a kind (1 bicubic, 2 lanczos2, 3 lanczos3) on a
+ * PSF image, at offsets (dx, dy) from its centre; n points. */
+int orc_interpolate_psf(int kind, const double *psf, int ncols, int nrows, const double *dx, const double *dy,
+                        long n, double *out) {
+  ointerp ip;
+  memset(&ip, 0, sizeof(ip));
+  int st = interp_build(&ip, kind, psf, ncols, nrows);
+  if (st) return st;
+  for (long k = 0; k < n; k++) out[k] = interp_value(&ip, dx[k], dy[k]);
+  interp_free(&ip);
+  return 0;
+}
+
+double orc_lanczos(double x, int n) { return lanczos(x, n); }
+
 double orc_function_value(const char *name, const double *params, double x0, double y0, double x,
                           double y, int subsampling) {
   ofunc f;

@@ -53,6 +53,11 @@ int orc_model_size(orc_model *m, int *ncols, int *nrows);
 int orc_fft_size(orc_model *m, int *ncols, int *nrows);
 
 void orc_create_model_image(orc_model *m, const double *params);
+int orc_set_point_source_method(orc_model *m, int index, int method);
+int orc_get_single_function_image(orc_model *m, const double *params, int index, double *out);
+int orc_interpolate_psf(int kind, const double *psf, int ncols, int nrows, const double *dx, const double *dy,
+                        long n, double *out);
+double orc_lanczos(double x, int n);
 int orc_get_model_image(orc_model *m, double *out);
 int orc_get_expanded_model_image(orc_model *m, double *out, long n);
 void orc_compute_deviates(orc_model *m, double *out, const double *params);

@@ -2,7 +2,7 @@
 
 Run in a checkout that has the reference at /root/reference (or
 IMFIT_REFERENCE_DIR):  python tests/golden/make_golden.py [part ...]
-(parts: n3073 makeimage ic3478 small_case; all by default)
+(parts: n3073 makeimage ic3478 pointsource small_case; all by default)
 
 Outputs (all small .npz files next to this script):
   n3073.npz          the reference regression inputs tests/n3073rss_small.fits,
@@ -20,6 +20,9 @@ Outputs (all small .npz files next to this script):
                      tests/imfit_reference/imfit_config_ic3478_64x64b.dat and the
                      printed results of its mpfit fit (imfit_textout3) and its
                      Differential Evolution fit (imfit_textout3c_tail).
+  pointsource.npz    unit_tests/psf_gauss_sigma0.5_5.fits (the PSF of
+                     unittest_psf_interpolators.t.h) and the makeimage output
+                     tests/oversampled_pointsource.fits (do_makeimage_tests:74).
   small_case.npz     the reference's own outputs (oracle/_ref) for
                      imfit_gb300.workloads.small_case: model images, deviates and
                      statistics for chi^2 / Cash / PMLR.
@@ -113,6 +116,16 @@ def ic3478():
         de_params_printed=np.array([32.9439, 34.0933, 18.2613, 0.235989, 2.40028, 20.0094, 60.7612]))
 
 
+def pointsource():
+    psf5, _ = fits.read_image(os.path.join(REF, "unit_tests", "psf_gauss_sigma0.5_5.fits"))
+    img, _ = fits.read_image(os.path.join(REF, "tests", "oversampled_pointsource.fits"))
+    np.savez_compressed(os.path.join(HERE, "pointsource.npz"), psf5=psf5.astype(np.float32),
+                        ps_image=img.astype(np.float32),
+                        # config_makeimage_pointsource-oversample.dat: X0 Y0 I_tot
+                        ps_params=np.array([100.0, 100.0, 1.0]), ps_region=np.array([80, 120, 80, 120]),
+                        ps_scale=3)
+
+
 def small_case():
     out = {}
     for stat in ("chi2", "cash", "pmlr"):
@@ -131,7 +144,8 @@ if __name__ == "__main__":
     if not os.path.isdir(os.path.join(REF, "core")):
         sys.exit(f"reference checkout not found at {REF}")
     oracle.build_reference()
-    parts = {"n3073": n3073, "makeimage": makeimage, "ic3478": ic3478, "small_case": small_case}
+    parts = {"n3073": n3073, "makeimage": makeimage, "ic3478": ic3478, "pointsource": pointsource,
+             "small_case": small_case}
     for name in (sys.argv[1:] or parts):
         parts[name]()
     for f in sorted(os.listdir(HERE)):

@@ -216,3 +216,47 @@ def test_ic3478_printed_fit_statistic(oracle_mod):
     s = m.get_fit_statistic(d["lm_params_printed"])
     assert abs(s - float(d["lm_chi2_printed"])) < 1e-6 * float(d["lm_chi2_printed"]), s
     assert abs(s / (64 * 64 - 7) - float(d["lm_reduced_printed"])) < 1e-6
+
+
+def test_psf_interpolators_known_answers(oracle_mod):
+    """unit_tests/unittest_psf_interpolators.t.h (DELTA = 1e-8): GSL bicubic
+    and Lanczos2 on psf_gauss_sigma0.5_5.fits, and the Lanczos kernel."""
+    d = np.load(os.path.join(GOLDEN, "pointsource.npz"))
+    psf = d["psf5"].astype(np.float64)
+    dx = np.array([0.0, 1.0, 0.0, 0.0, 0.5, 1.5, 0.0])
+    dy = np.array([0.0, 0.0, 1.0, -2.0, 0.0, 0.5, 1.5])
+    want = [0.73212016, 0.16868566, 0.16868566, 0.0014417765, 0.51973038, 0.00880937, 0.01243073]
+    assert np.all(np.abs(oracle_mod.interpolate_psf("bicubic", psf, dx, dy) - want) < 1e-8)
+    dx = np.array([0.0, 1.0, 0.0, 0.0, 0.5, 1.5, 0.0, -1.5, -1.9])
+    dy = np.array([0.0, 0.0, 1.0, -2.0, 0.0, 0.5, 1.5, -1.5, -1.9])
+    want = [0.73212016, 0.16868566, 0.16868566, 0.0014417765, 0.5054706567431267, 0.035119419221815946,
+            0.050885502118477165, 0.00352206909108757, 0.0002065470426474115]
+    assert np.all(np.abs(oracle_mod.interpolate_psf("lanczos2", psf, dx, dy) - want) < 1e-8)
+    for n, xs, ys in ((2, [0.0, 0.5, 1.0, 1.5, 2.0, 3.0], [1.0, 0.5731591682507563, 0.0, -0.06368435202786181,
+                                                         0.0, 0.0]),
+                      (3, [0.0, 0.5, 1.0, 1.5, 2.0, 2.5, 3.0, 4.0],
+                       [1.0, 0.6079271018540265, 0.0, -0.13509491152311703, 0.0, 0.02431708407416106, 0.0, 0.0])):
+        for x, y in zip(xs, ys):
+            assert abs(oracle_mod.lanczos(x, n) - y) < 1e-8 and abs(oracle_mod.lanczos(-x, n) - y) < 1e-8
+    # outside the PSF's extent: zero
+    assert np.all(oracle_mod.interpolate_psf("bicubic", psf, [2.01, 0.0], [0.0, -2.5]) == 0.0)
+
+
+def test_point_source_oversampled_golden(oracle_mod):
+    """do_makeimage_tests:74 -> tests/oversampled_pointsource.fits: a
+    PointSource (bicubic) at (100, 100), psf_standard.fits, region
+    80:120,80:120 at scale 3 with psf_oversamp.fits (interpolated as given,
+    unnormalised).  The reference image is float32: within one float32 ulp."""
+    d = np.load(os.path.join(GOLDEN, "pointsource.npz"))
+    g = np.load(os.path.join(GOLDEN, "makeimage.npz"))
+    m = oracle_mod.OracleModel()
+    m.add_function("PointSource", True)
+    m.finish_functions()
+    m.add_psf(g["psf_standard"].astype(np.float64))
+    m.setup_model_image(200, 200)
+    m.add_oversampled_psf(g["psf_oversamp"].astype(np.float64), int(d["ps_scale"]), tuple(d["ps_region"]))
+    m.create_model_image(d["ps_params"])
+    img = m.get_model_image()
+    want = d["ps_image"]
+    ulp = np.spacing(np.abs(want)).astype(np.float64)
+    assert np.all(np.abs(img - want) <= ulp + 1e-12), np.max(np.abs(img - want) / (ulp + 1e-30))
