@@ -86,6 +86,7 @@ _SIGS = [
     ("imfit_BootstrapFitBatch", _I, [_P, _I, _DP, ctypes.POINTER(_I), _DP, _DP, _D, _I, _DP, _DP,
                                      ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     ("imfit_SetupImageStack", _I, [_P, _I, _I, _I, _DP, _DP, _DP, _I, _I]),
+    ("imfit_SetFunctionOptionalParam", _I, [_P, _I, ctypes.c_char_p, ctypes.c_char_p]),
     ("imfit_Synchronize", _I, [_P]),
     ("imfit_GetStream", _I, [_P, ctypes.POINTER(_P)]),
     ("imfit_SetUseGraphs", _I, [_P, _I]),
@@ -173,13 +174,17 @@ class ModelObject:
         return self.lib.imfit_LastError(self.h).decode()
 
     # --- functions ---
-    def add_function(self, name, new_set=False, subsampling=True):
+    def add_function(self, name, new_set=False, subsampling=True, optional=None):
+        """optional: {name: value} optional parameters (e.g. {"method": "lanczos2"}
+        for PointSource)."""
         self._ck(self.lib.imfit_AddFunction(self.h, name.encode()))
         idx = len(self._funcs)
         self._funcs.append(name)
         if new_set or idx == 0:
             self._set_starts.append(idx)
         self._ck(self.lib.imfit_SetSubsampling(self.h, idx, int(subsampling)))
+        for k, v in (optional or {}).items():
+            self._ck(self.lib.imfit_SetFunctionOptionalParam(self.h, idx, str(k).encode(), str(v).encode()))
 
     def set_subsampling(self, index, flag):
         self._ck(self.lib.imfit_SetSubsampling(self.h, index, int(flag)))

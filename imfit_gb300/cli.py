@@ -129,11 +129,12 @@ def _add_oversampled_psfs(m, args):
 
 
 def _add_functions(m, cfg, args):
-    for (name, _), opt in zip(cfg.functions, cfg.optional):
-        if opt:  # FunctionObject::SetExtraParams returns -1 for these functions
-            raise SystemExit(f"function {name} takes no optional parameters ({', '.join(opt)})")
-    for name, new_set in cfg.functions:
-        m.add_function(name, new_set, subsampling=not args.nosubsampling)
+    from . import ImfitError
+    for (name, new_set), opt in zip(cfg.functions, cfg.optional):
+        try:
+            m.add_function(name, new_set, subsampling=not args.nosubsampling, optional=opt)
+        except ImfitError as e:  # e.g. SetExtraParams on a function without optional parameters
+            raise SystemExit(f"function {name}: {e}")
     m.finish_functions()
     if m.n_params != len(cfg.values):
         raise SystemExit(f"the configuration gives {len(cfg.values)} parameters, the functions need "

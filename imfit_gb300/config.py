@@ -169,7 +169,7 @@ def read_config(path):
 
 
 _NPARAMS = {"Sersic": 5, "Exponential": 4, "FlatSky": 1, "GaussianRing": 5, "Moffat": 5, "Gaussian": 4,
-            "ExponentialDisk3D": 6, "FerrersBar3D": 8}
+            "ExponentialDisk3D": 6, "FerrersBar3D": 8, "PointSource": 1, "PointSourceRot": 2}
 
 
 def format_params(cfg, params, chi2=None):

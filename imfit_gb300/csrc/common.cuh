@@ -32,7 +32,13 @@ enum FuncType : int {
   F_GAUSS = 6,       // function_objects/func_gaussian.cpp
   F_EXPDISK3D = 7,   // function_objects/func_expdisk3d.cpp
   F_FERRERS3D = 8,   // function_objects/func_ferrersbar3d.cpp
+  F_POINTSOURCE = 9,     // function_objects/func_pointsource.cpp
+  F_POINTSOURCEROT = 10, // function_objects/func_pointsource-rot.cpp
 };
+
+// PointSource classes are added after the convolution (IsPointSource,
+// core/model_object.cpp:1163-1216), from an interpolated PSF.
+__host__ __device__ inline bool is_point_source(int t) { return t == F_POINTSOURCE || t == F_POINTSOURCEROT; }
 
 constexpr int kMaxComponents = 32;
 constexpr int kMaxParams = 256;
@@ -48,7 +54,8 @@ struct CompDesc {
   int x0Index;      // index of its function set's X0 (Y0 follows)
   int nParams;
   int background;   // 1 = spatially constant (FlatSky): added after convolution
-  int pad0, pad1;
+  int psScale;      // point sources: PointSource::oversamplingScale on the main grid
+  int pad1;
 };
 
 // FP64 Setup() state, restating each class's Setup (plain path).
@@ -114,7 +121,7 @@ __host__ __device__ inline void comp_setup64(CompF64 &c, int type, int subsample
   c.q = 1.0;
   c.cosPA = 1.0;
   c.sinPA = 0.0;
-  if (type != F_FLATSKY) {
+  if (type != F_FLATSKY && type != F_POINTSOURCE) {
     double par = (p[0] + 90.0) * kDeg2Rad;
     c.cosPA = cos(par);
     c.sinPA = sin(par);
@@ -132,6 +139,12 @@ __host__ __device__ inline void comp_setup64(CompF64 &c, int type, int subsample
       break;
     case F_FLATSKY:  // func_flatsky.cpp:85-90
       c.a = p[0];
+      break;
+    case F_POINTSOURCE:  // func_pointsource.cpp:206-211
+      c.a = p[0];
+      break;
+    case F_POINTSOURCEROT:  // func_pointsource-rot.cpp:210-221 (PA + 90 as above)
+      c.a = p[1];
       break;
     case F_GRING:  // func_gaussian-ring.cpp:102-121
       c.q = 1.0 - p[1];
@@ -315,7 +328,7 @@ __device__ inline void comp_setup32(CompF32 &o, const CompDesc &d, const double 
   o.cosPA = 1.f; o.sinPA = 0.f; o.q = 1.f; o.invq = 1.f;
   o.s0 = o.s1 = o.s2 = o.s3 = o.s4 = o.s5 = o.s6 = o.s7 = 0.f;
   o.subScale = 1.f; o.subInner = 3.f; o.subSmallK = 20.f;
-  if (d.type != F_FLATSKY) {
+  if (d.type != F_FLATSKY && d.type != F_POINTSOURCE) {
     o.cosPA = (float)q.cosPA;
     o.sinPA = (float)q.sinPA;
   }
@@ -423,6 +436,14 @@ __device__ inline void comp_setup32(CompF32 &o, const CompDesc &d, const double 
       o.q = (float)(1.01 * ((t < p[4]) ? p[4] : t));  // integration half-range
       break;
     }
+    case F_POINTSOURCE:
+      o.s0 = (float)p[0];  // I_tot
+      o.s1 = (float)d.psScale;
+      break;
+    case F_POINTSOURCEROT:
+      o.s0 = (float)p[1];  // I_tot
+      o.s1 = (float)d.psScale;
+      break;
     default:
       break;
   }

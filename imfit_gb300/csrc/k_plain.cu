@@ -34,6 +34,7 @@ __global__ void __launch_bounds__(256) k_eval64(const CompF64 *__restrict__ comp
   double s = 0.0, err = 0.0;
   for (int c = 0; c < nComp; c++) {
     const int t = sc[c].type;
+    if (is_point_source(t)) continue;  // added after the convolution
     const double v = (t == F_EXPDISK3D || t == F_FERRERS3D) ? los[(long)sc[c].pad0 * n + k]
                                                               : comp_value64_2d(sc[c], x, y);
     const double adj = v - err;
@@ -49,6 +50,59 @@ cudaError_t launch_eval64(const CompF64 *comps, int nComp, double *model, long p
   const long n = (long)g.nCols * g.nRows;
   if (n == 0) return cudaSuccess;
   k_eval64<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(comps, nComp, model, pitch, g, los);
+  return cudaGetLastError();
+}
+
+// Point sources after the convolution: core/model_object.cpp:1183-1216 on the
+// main grid, core/oversampled_region.cpp:363-408 on a region grid.  Kahan sum
+// over the point sources, added to the model.  Value I_tot * P(s (x - x0),
+// s (y - y0)) (func_pointsource.cpp:220-229), rotated by PA for PointSourceRot
+// (func_pointsource-rot.cpp:229-243); s = scales.s[c], the component's
+// PointSource::oversamplingScale for this pass.
+__global__ void __launch_bounds__(256) k_point_sources64(const CompF64 *__restrict__ comps, int nComp,
+                                                         double *__restrict__ model, long pitch, Grid64 g,
+                                                         PsfInterp<double> ip, PsScales scales) {
+  __shared__ CompF64 sc[kMaxComponents];
+  for (int i = threadIdx.x; i < nComp; i += blockDim.x) sc[i] = comps[i];
+  __syncthreads();
+  const long n = (long)g.nCols * g.nRows;
+  const long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const long j = k % g.nCols, i = k / g.nCols;
+  double x, y;
+  if (!g.isRegion) {
+    y = (double)(i - g.pr + 1);
+    x = (double)(j - g.pc + 1);
+  } else {
+    y = g.y1 + g.off + (i - g.pr) * g.frac;
+    x = g.x1 + g.off + (j - g.pc) * g.frac;
+  }
+  double s = 0.0, err = 0.0;
+  for (int c = 0; c < nComp; c++) {
+    const CompF64 &f = sc[c];
+    if (!is_point_source(f.type)) continue;
+    const double os = (double)scales.s[c];
+    double xd = os * (x - f.x0), yd = os * (y - f.y0);
+    if (f.type == F_POINTSOURCEROT) {
+      const double xp = xd * f.cosPA + yd * f.sinPA;
+      const double yp = -xd * f.sinPA + yd * f.cosPA;
+      xd = xp;
+      yd = yp;
+    }
+    const double v = f.a * psf_interp64(ip, xd, yd);
+    const double adj = v - err;
+    const double tmp = s + adj;
+    err = (tmp - s) - adj;
+    s = tmp;
+  }
+  model[i * pitch + j] += s;
+}
+
+cudaError_t launch_point_sources64(const CompF64 *comps, int nComp, double *model, long pitch, Grid64 g,
+                                   PsfInterp<double> ip, const PsScales &scales, cudaStream_t st) {
+  const long n = (long)g.nCols * g.nRows;
+  if (n == 0) return cudaSuccess;
+  k_point_sources64<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(comps, nComp, model, pitch, g, ip, scales);
   return cudaGetLastError();
 }
 

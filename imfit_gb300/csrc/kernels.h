@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include "common.cuh"
+#include "psf_interp.cuh"
 
 namespace imfit {
 
@@ -84,6 +85,13 @@ cudaError_t launch_flux64(const CompF64 &c, int xSize, int ySize, double *partia
 // model pixels; 3-D components are read from 'los' (may be null without them)
 cudaError_t launch_eval64(const CompF64 *comps, int nComp, double *model, long pitch, Grid64 g,
                           const double *los, cudaStream_t st);
+// per-component PointSource::oversamplingScale of one point-source pass
+struct PsScales {
+  int s[kMaxComponents];
+};
+// point sources after the convolution
+cudaError_t launch_point_sources64(const CompF64 *comps, int nComp, double *model, long pitch, Grid64 g,
+                                   PsfInterp<double> ip, const PsScales &scales, cudaStream_t st);
 cudaError_t launch_downsample64(const double *region, int nOC, int nOR, int osPsfCols, int osPsfRows,
                                 double *mainImg, int nMainCols, int nMainRows, int mainPsfCols,
                                 int mainPsfRows, int x1, int y1, int scale, cudaStream_t st);

@@ -37,6 +37,7 @@ struct FuncInfo {
   int type;
   int nParams;
   int subsample;
+  int method = PSF_BICUBIC;  // point sources: the optional parameter "method"
   std::vector<std::string> paramNames;
 };
 
@@ -51,6 +52,8 @@ bool lookup_function(const std::string &n, FuncInfo &f) {
       {"Gaussian", {F_GAUSS, {"PA", "ell", "I_0", "sigma"}}},
       {"ExponentialDisk3D", {F_EXPDISK3D, {"PA", "inc", "J_0", "h", "n", "z_0"}}},
       {"FerrersBar3D", {F_FERRERS3D, {"PA", "inc", "barPA", "J_0", "R_bar", "q", "q_z", "n"}}},
+      {"PointSource", {F_POINTSOURCE, {"I_tot"}}},
+      {"PointSourceRot", {F_POINTSOURCEROT, {"PA", "I_tot"}}},
   };
   auto it = reg.find(n);
   if (it == reg.end()) return false;
@@ -58,8 +61,49 @@ bool lookup_function(const std::string &n, FuncInfo &f) {
   f.type = it->second.first;
   f.paramNames = it->second.second;
   f.nParams = (int)f.paramNames.size();
-  f.subsample = (f.type == F_EXPDISK3D || f.type == F_FERRERS3D) ? 0 : 1;
+  f.subsample = (f.type == F_EXPDISK3D || f.type == F_FERRERS3D || is_point_source(f.type)) ? 0 : 1;
   return true;
+}
+
+// Derivative at every knot of the natural cubic spline through v[k*stride],
+// k < n, unit knot spacing (second derivatives M from the tridiagonal system
+// M_{k-1} + 4 M_k + M_{k+1} = 6 (v_{k+1} - 2 v_k + v_{k-1}), M_0 = M_{n-1} = 0).
+void spline_knot_derivs(const double *v, long stride, int n, double *out) {
+  std::vector<double> M(n, 0.0), c(n, 0.0), d(n, 0.0);
+  if (n > 2) {
+    const int m = n - 2;
+    for (int i = 0; i < m; i++) {
+      const int k = i + 1;
+      double rhs = 6.0 * (v[(k + 1) * stride] - 2.0 * v[k * stride] + v[(k - 1) * stride]);
+      double diag = 4.0;
+      if (i > 0) {
+        const double w = 1.0 / c[i - 1];
+        diag -= w;
+        rhs -= w * d[i - 1];
+      }
+      c[i] = diag;
+      d[i] = rhs;
+    }
+    M[m] = d[m - 1] / c[m - 1];
+    for (int i = m - 2; i >= 0; i--) M[i + 1] = (d[i] - M[i + 2]) / c[i];
+  }
+  for (int k = 0; k < n - 1; k++)
+    out[k * stride] = (v[(k + 1) * stride] - v[k * stride]) - (2.0 * M[k] + M[k + 1]) / 6.0;
+  out[(n - 1) * stride] = (v[(n - 1) * stride] - v[(n - 2) * stride]) + (M[n - 2] + 2.0 * M[n - 1]) / 6.0;
+}
+
+// Host tables of a PSF interpolator (psf_interp.cuh): bicubic -> z, z_x, z_y,
+// z_xy (z_xy the x-spline derivative of z_y); Lanczos -> the PSF.
+std::vector<double> psf_interp_tables(int kind, const double *psf, int nc, int nr) {
+  const long np = (long)nc * nr;
+  if (kind != PSF_BICUBIC) return std::vector<double>(psf, psf + np);
+  std::vector<double> t(4 * np);
+  double *z = t.data(), *zx = z + np, *zy = zx + np, *zxy = zy + np;
+  std::copy(psf, psf + np, z);
+  for (int r = 0; r < nr; r++) spline_knot_derivs(z + (long)r * nc, 1, nc, zx + (long)r * nc);
+  for (int c = 0; c < nc; c++) spline_knot_derivs(z + c, nc, nr, zy + c);
+  for (int r = 0; r < nr; r++) spline_knot_derivs(zy + (long)r * nc, 1, nc, zxy + (long)r * nc);
+  return t;
 }
 
 // Kahan-summed normalisation (core/convolver.cpp:296-311, core/model_object.cpp:2581-2594)
@@ -134,6 +178,9 @@ struct Region {
   int x1, y1, nBaseCols, nBaseRows, scale;
   int nPsfCols, nPsfRows;
   std::vector<double> psf;  // normalised as the region's Convolver does
+  std::vector<double> psfRaw;  // as given: the region's bicubic point-source interpolator reads it
+  DevBuf<double> psTab;        // that interpolator's tables
+  PsfInterp<double> ps64{};
   double psfSum = 1.0;
   int nModelCols, nModelRows;
   long nModelVals;
@@ -169,6 +216,16 @@ struct imfit_model_s {
   bool doConv = false;
   int nPsfCols = 0, nPsfRows = 0;
   std::vector<double> psf;  // normalised (Convolver) copy
+  // point sources: per function PointSource::oversamplingScale (1 until an
+  // oversampled region has been computed, then that region's scale -- the
+  // reference never resets it, core/model_object.cpp:1190-1192), and the
+  // ModelObject's interpolator of the (normalised) PSF, of the first point
+  // source's kind (core/model_object.cpp:294-305, 345-381)
+  std::vector<int> psScale;
+  int nPointSources = 0;
+  DevBuf<double> dPsTab;
+  PsfInterp<double> ps64{};
+  int psKind = 0;
   bool psfNormalize = true;
   double psfSum = 1.0;
   bool modelSetupDone = false, modelComputed = false;
@@ -420,6 +477,7 @@ struct imfit_model_s {
     r->nPsfCols = pc;
     r->nPsfRows = pr;
     r->psf.assign(p, p + (size_t)pc * pr);
+    r->psfRaw = r->psf;
     if (normalize) {
       const double s = kahan_sum(r->psf.data(), (long)r->psf.size());
       for (auto &v : r->psf) v = v / s;
@@ -558,6 +616,7 @@ struct imfit_model_s {
     if (stack.n) return fail(IMFIT_E_UNSUPPORTED, "the plain FP64 path takes one image per ModelObject, not a stack");
     if (!setsDefined) return fail(IMFIT_E_STATE, "DefineFunctionSets not called");
     if (!modelSetupDone) return fail(IMFIT_E_STATE, "SetupModelImage not called");
+    if (int st = ensurePointSourceInterp()) return st;
     return 0;
   }
 
@@ -625,8 +684,10 @@ struct imfit_model_s {
     g.nRows = nModelRows;
     g.pc = doConv ? nPsfCols : 0;
     g.pr = doConv ? nPsfRows : 0;
+    const bool ps = is_point_source(one.type);
     if (!e) e = evalGridN(dComps.p, 1, ll, dModel.p, nModelCols, g);
-    if (!e && doConv) e = conv64(dModel.p, nModelCols, nModelRows, Lx, Ly, dH.p, dSpec.p);
+    if (!e && doConv && !ps) e = conv64(dModel.p, nModelCols, nModelRows, Lx, Ly, dH.p, dSpec.p);
+    if (!e && ps) e = launch_point_sources64(dComps.p, 1, dModel.p, nModelCols, g, ps64, mainScales(&fi, 1), stream);
     for (Region *r : regions) {
       if (e) break;
       Grid64 rg{};
@@ -641,6 +702,12 @@ struct imfit_model_s {
       rg.off = 0.5 * rg.frac - 0.5;
       e = evalGridN(dComps.p, 1, ll, r->model.p, r->nModelCols, rg);
       if (!e) e = conv64(r->model.p, r->nModelCols, r->nModelRows, r->Lx, r->Ly, r->H.p, r->spec.p);
+      if (!e && ps) {
+        PsScales sc{};
+        sc.s[0] = r->scale;
+        e = launch_point_sources64(dComps.p, 1, r->model.p, r->nModelCols, rg, r->ps64, sc, stream);
+        psScale[fi] = r->scale;
+      }
       if (!e)
         e = launch_downsample64(r->model.p, r->nModelCols, r->nModelRows, r->nPsfCols, r->nPsfRows, dModel.p,
                                 nModelCols, nModelRows, doConv ? nPsfCols : 0, doConv ? nPsfRows : 0, r->x1, r->y1,
@@ -700,6 +767,8 @@ struct imfit_model_s {
         flux = (1.0 - p[1]) * 2.0 * kPi * p[2] * p[3] * p[3];
       } else if (t == F_GAUSS) {
         flux = (1.0 - p[1]) * 2.0 * kPi * p[2] * p[3] * p[3];
+      } else if (is_point_source(t)) {  // func_pointsource.cpp:241-244
+        flux = (t == F_POINTSOURCE) ? p[0] : p[1];
       } else {
         e = launch_flux64(c, xSize, ySize, part.p, kBlocks, dLosFlag.p, stream);
         if (!e) e = cudaMemcpyAsync(hp.data(), part.p, sizeof(double) * kBlocks, cudaMemcpyDeviceToHost, stream);
@@ -740,6 +809,51 @@ struct imfit_model_s {
     return e;
   }
 
+  // Interpolator tables for the point sources (built on first use, again
+  // after the PSF or a point source's method changes).
+  int ensurePointSourceInterp() {
+    if (!nPointSources) return 0;
+    int kind = PSF_BICUBIC;
+    for (auto &f : funcs)
+      if (is_point_source(f.type)) {
+        kind = f.method;
+        break;
+      }
+    if (psKind != kind) {
+      if (psf.empty()) return fail(IMFIT_E_STATE, "PointSource image function being used, but no PSF image was supplied");
+      if (nPsfCols < 4 || nPsfRows < 4)
+        return fail(IMFIT_E_ARG, "PSF image is too small for interpolation with PointSource functions (4 x 4 minimum)");
+      std::vector<double> t = psf_interp_tables(kind, psf.data(), nPsfCols, nPsfRows);
+      cudaError_t e = dPsTab.reserve(t.size());
+      if (!e) e = cudaMemcpy(dPsTab.p, t.data(), sizeof(double) * t.size(), cudaMemcpyHostToDevice);
+      if (e) return cuda_fail(e, "PSF interpolator");
+      ps64 = PsfInterp<double>{kind, nPsfCols, nPsfRows, 0, (nPsfCols - 1) / 2.0, (nPsfRows - 1) / 2.0, dPsTab.p};
+      psKind = kind;
+    }
+    for (Region *r : regions) {
+      if (r->ps64.kind) continue;
+      if (r->nPsfCols < 4 || r->nPsfRows < 4)
+        return fail(IMFIT_E_ARG, "Oversampled PSF image is too small for interpolation with PointSource functions");
+      std::vector<double> t = psf_interp_tables(PSF_BICUBIC, r->psfRaw.data(), r->nPsfCols, r->nPsfRows);
+      cudaError_t e = r->psTab.reserve(t.size());
+      if (!e) e = cudaMemcpy(r->psTab.p, t.data(), sizeof(double) * t.size(), cudaMemcpyHostToDevice);
+      if (e) return cuda_fail(e, "oversampled PSF interpolator");
+      r->ps64 = PsfInterp<double>{PSF_BICUBIC, r->nPsfCols, r->nPsfRows, 0, (r->nPsfCols - 1) / 2.0,
+                                  (r->nPsfRows - 1) / 2.0, r->psTab.p};
+    }
+    return 0;
+  }
+
+  // point-source passes of components [c0, c0 + nC) of the device array dC,
+  // whose function indices are fi[0..nC): main grid at each one's current
+  // scale, then a region grid at the region's scale (the scale the components
+  // keep afterwards)
+  PsScales mainScales(const int *fi, int nC) {
+    PsScales sc{};
+    for (int c = 0; c < nC; c++) sc.s[c] = psScale[fi[c]];
+    return sc;
+  }
+
   // CreateModelImage (core/model_object.cpp:1103-1229) with comps already on the device
   cudaError_t enqueueModel(const CompF64 *dC) {
     buildLosList();
@@ -759,6 +873,10 @@ struct imfit_model_s {
     g.pr = doConv ? nPsfRows : 0;
     e = evalGrid(dC, dModel.p, nModelCols, g);
     if (!e && doConv) e = conv64(dModel.p, nModelCols, nModelRows, Lx, Ly, dH.p, dSpec.p);
+    const int nC = (int)funcs.size();
+    std::vector<int> all(nC);
+    for (int c = 0; c < nC; c++) all[c] = c;
+    if (!e && nPointSources) e = launch_point_sources64(dC, nC, dModel.p, nModelCols, g, ps64, mainScales(all.data(), nC), stream);
     for (Region *r : regions) {
       if (e) break;
       Grid64 rg{};
@@ -773,6 +891,13 @@ struct imfit_model_s {
       rg.off = 0.5 * rg.frac - 0.5;
       e = evalGrid(dC, r->model.p, r->nModelCols, rg);
       if (!e) e = conv64(r->model.p, r->nModelCols, r->nModelRows, r->Lx, r->Ly, r->H.p, r->spec.p);
+      if (!e && nPointSources) {
+        PsScales sc{};
+        for (int c = 0; c < nC; c++) sc.s[c] = r->scale;
+        e = launch_point_sources64(dC, nC, r->model.p, r->nModelCols, rg, r->ps64, sc, stream);
+        for (int c = 0; c < nC; c++)
+          if (is_point_source(funcs[c].type)) psScale[c] = r->scale;
+      }
       if (!e)
         e = launch_downsample64(r->model.p, r->nModelCols, r->nModelRows, r->nPsfCols, r->nPsfRows, dModel.p,
                                 nModelCols, nModelRows, doConv ? nPsfCols : 0, doConv ? nPsfRows : 0, r->x1, r->y1,
@@ -906,6 +1031,8 @@ struct imfit_model_s {
     if (fastReady) return 0;
     if (!finalSetupDone) return fail(IMFIT_E_STATE, "FinalSetupForFitting not called");
     if (!setsDefined) return fail(IMFIT_E_STATE, "DefineFunctionSets not called");
+    if (nPointSources)
+      return fail(IMFIT_E_UNSUPPORTED, "PointSource functions are evaluated on the plain FP64 path only");
     hasLos = false;
     for (auto &f : funcs)
       if (f.type == F_EXPDISK3D || f.type == F_FERRERS3D) hasLos = true;
@@ -1684,7 +1811,31 @@ int imfit_AddFunction(imfit_model_t m, const char *name) {
   if (!lookup_function(name, f)) return m->fail(IMFIT_E_UNSUPPORTED, std::string("unknown or unsupported function: ") + name);
   if (m->funcs.size() >= (size_t)kMaxComponents) return m->fail(IMFIT_E_UNSUPPORTED, "too many functions");
   m->funcs.push_back(f);
+  m->psScale.push_back(1);
+  if (is_point_source(f.type)) {
+    m->nPointSources++;
+    m->psKind = 0;
+  }
   m->setsDefined = false;
+  return 0;
+}
+
+int imfit_SetFunctionOptionalParam(imfit_model_t m, int i, const char *name, const char *value) {
+  GET(m);
+  if (i < 0 || i >= (int)m->funcs.size() || !name || !value) return m->fail(IMFIT_E_ARG, "bad function index or name");
+  FuncInfo &f = m->funcs[i];
+  if (!is_point_source(f.type))
+    return m->fail(IMFIT_E_UNSUPPORTED, f.name + " takes no optional parameters");
+  if (std::string(name) != "method") return m->fail(IMFIT_E_ARG, std::string("unrecognized optional parameter ") + name);
+  const std::string v(value);
+  int kind = 0;
+  if (v == "bicubic" || v == "Bicubic") kind = PSF_BICUBIC;
+  if (v == "lanczos2" || v == "Lanczos2") kind = PSF_LANCZOS2;
+  if ((v == "lanczos3" || v == "Lanczos3") && f.type == F_POINTSOURCE) kind = PSF_LANCZOS3;
+  if (!kind) return m->fail(IMFIT_E_ARG, "unidentified interpolation type " + v);
+  f.method = kind;
+  m->psKind = 0;
+  m->fastReady = false;
   return 0;
 }
 
@@ -1737,6 +1888,7 @@ int imfit_AddPSFVector(imfit_model_t m, long nPix, int nc, int nr, const double 
   m->nPsfRows = nr;
   m->doConv = true;
   m->psfNormalize = normalize != 0;
+  m->psKind = 0;  // point-source interpolator rebuilt from this PSF
   if (m->modelSetupDone) return m->fail(-1, "PSF was added after SetupModelImage() was already called");
   return 0;
 }

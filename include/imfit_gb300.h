@@ -61,8 +61,14 @@ const char *imfit_Version(void);
 /* ModelObject::AddFunction (core/model_object.cpp:279) with the factory of
  * core/add_functions.cpp:389-461: name is the config-file FUNCTION name
  * ("Sersic", "Exponential", "FlatSky", "GaussianRing", "Moffat", "Gaussian",
- * "ExponentialDisk3D", "FerrersBar3D"). */
+ * "ExponentialDisk3D", "FerrersBar3D", "PointSource", "PointSourceRot"). */
 int imfit_AddFunction(imfit_model_t m, const char *name);
+/* FunctionObject::SetExtraParams (an OPTIONAL_PARAMS entry of the
+ * configuration file) for function i: PointSource / PointSourceRot accept
+ * "method" = bicubic | lanczos2 | lanczos3 (PointSourceRot: not lanczos3)
+ * (function_objects/func_pointsource.cpp:140-180); every other function
+ * takes none (IMFIT_E_UNSUPPORTED, as SetExtraParams returns -1). */
+int imfit_SetFunctionOptionalParam(imfit_model_t m, int i, const char *name, const char *value);
 /* FunctionObject::SetSubsampling (function_objects/function_object.cpp:78) */
 int imfit_SetSubsampling(imfit_model_t m, int functionIndex, int subsample);
 /* ModelObject::DefineFunctionSets (core/model_object.cpp:387) */
