@@ -264,6 +264,96 @@ __global__ void __launch_bounds__(1024) k_fast_eval_r2c(FastArgs a, WinDesc w, F
   }
 }
 
+// ------------------------------------------------------------ point sources
+// Point source c at scaled offsets (xd, yd) = s (x - x0, y - y0) from its
+// centre: the value I_tot P(xd, yd) (rotated by PA for PointSourceRot) and,
+// when dv is given, its derivatives w.r.t. X0, Y0, I_tot and PA
+// (func_pointsource.cpp:220-229, func_pointsource-rot.cpp:229-243).
+__device__ __forceinline__ float ps_eval(const CompF32 &c, const PsfInterp<float> &ip, float xd, float yd, float s,
+                                         float *dv) {
+  float xa = xd, ya = yd;
+  if (c.type == F_POINTSOURCEROT) {
+    xa = xd * c.cosPA + yd * c.sinPA;
+    ya = -xd * c.sinPA + yd * c.cosPA;
+  }
+  float P, Px, Py;
+  psf_interp32(ip, xa, ya, P, Px, Py);
+  const float I = c.s0;
+  if (dv) {
+    if (c.type == F_POINTSOURCEROT) {
+      dv[0] = I * s * (-Px * c.cosPA + Py * c.sinPA);
+      dv[1] = I * s * (-Px * c.sinPA - Py * c.cosPA);
+      dv[3] = I * (Px * ya - Py * xa) * 0.017453292f;  // d theta / d PA = pi/180
+    } else {
+      dv[0] = -I * s * Px;
+      dv[1] = -I * s * Py;
+      dv[3] = 0.f;
+    }
+    dv[2] = P;
+  }
+  return I * P;
+}
+
+// the point source touches nothing beyond the PSF's half-diagonal
+__device__ __forceinline__ bool ps_far(const PsfInterp<float> &ip, float xd, float yd) {
+  return xd * xd + yd * yd > ip.xb * ip.xb + ip.yb * ip.yb;
+}
+
+// data pixel (row, col): offsets from point source c, unscaled
+__device__ __forceinline__ void ps_offsets(const CompF32 &c, int row, int col, float &X, float &Y) {
+  X = (float)(col + 1 - c.x0i) - c.x0r;
+  Y = (float)(row + 1 - c.y0i) - c.y0r;
+}
+
+// Main grid: sum over the point sources at data pixel (row, col), each at its
+// own current scale (CompF32::s1); with acc, also adds g * derivatives.
+__device__ float ps_main(const FastArgs &a, int b, int row, int col, float g, float *acc) {
+  float v = 0.f;
+  for (int p = 0; p < a.nPs; p++) {
+    const CompF32 &c = a.comps[b * a.nComp + a.psComp[p]];
+    float X, Y;
+    ps_offsets(c, row, col, X, Y);
+    const float s = c.s1, xd = s * X, yd = s * Y;
+    if (ps_far(a.psMain, xd, yd)) continue;
+    float dv[4];
+    v += ps_eval(c, a.psMain, xd, yd, s, acc ? dv : nullptr);
+    if (acc)
+      for (int q = 0; q < 4; q++) atomicAdd(acc + 4 * p + q, g * dv[q]);
+  }
+  return v;
+}
+
+// Oversampled region: sum over the k x k subpixels of data pixel (row, col)
+// and over the point sources, at the region's scale with the region's
+// interpolator (oversampled_region.cpp:363-408: subpixel x = x1 + (0.5/k - 0.5)
+// + j/k, so k (x - x0) = k X - (k - 1)/2 + v); with acc, adds g * derivatives
+// (dv: their subpixel sums).
+__device__ float ps_region(const FastArgs &a, int k, int b, int row, int col, float g, float *acc) {
+  float v = 0.f;
+  const float s = (float)k, h = 0.5f * (float)(k - 1);
+  for (int p = 0; p < a.nPs; p++) {
+    const CompF32 &c = a.comps[b * a.nComp + a.psComp[p]];
+    float X, Y;
+    ps_offsets(c, row, col, X, Y);
+    const float bx = s * X - h, by = s * Y - h;  // offsets of the first subpixel
+    // nearest subpixel offsets to the centre along each axis
+    const float nx = bx > 0.f ? bx : (bx + (float)(k - 1) < 0.f ? -(bx + (float)(k - 1)) : 0.f);
+    const float ny = by > 0.f ? by : (by + (float)(k - 1) < 0.f ? -(by + (float)(k - 1)) : 0.f);
+    if (ps_far(a.psReg, nx, ny)) continue;
+    float sum[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int u = 0; u < k; u++)
+      for (int w = 0; w < k; w++) {
+        float dv[4];
+        v += ps_eval(c, a.psReg, bx + (float)w, by + (float)u, s, acc ? dv : nullptr);
+        if (acc)
+          for (int q = 0; q < 4; q++) sum[q] += dv[q];
+      }
+    if (acc)
+      for (int q = 0; q < 4; q++) atomicAdd(acc + 4 * p + q, g * sum[q]);
+  }
+  return v;
+}
+
 // ---------------------------------------- region: c2r + block average
 // (also used for the derivative images of the JtWJ pass: batch index b then
 // runs over (parameter vector, parameter) pairs, no background is added and
@@ -300,6 +390,7 @@ __global__ void __launch_bounds__(1024) k_fast_region_down(FastArgs a, FastGeom 
         const cplx<float> z = Z[u * ls + (col >> 1)];
         acc += (col & 1) ? z.y : z.x;
       }
+    if (addBackground && a.nPs) acc += ps_region(a, k, b, g.ry0 + s, g.rx0 + t, 0.f, nullptr);
     out[((long)b * g.rRows + s) * g.rCols + t] = acc * inv + bg;
   }
 }
@@ -364,6 +455,8 @@ __global__ void __launch_bounds__(1024) k_fast_stat_rows(FastArgs a, FastGeom g,
   cplx<float> *bufA = bufX + rpb * ls;
   cplx<float> *bufB = bufA + rpb * ls;
   __shared__ float red[2][32];
+  __shared__ float psAcc[4 * kMaxPsFast];
+  for (int i = threadIdx.x; i < 4 * a.nPs; i += blockDim.x) psAcc[i] = 0.f;
   const int row0 = blockIdx.x * rpb;
   const int nl = min(rpb, g.nDataRows - row0);
   cplx<float> *spec = reinterpret_cast<cplx<float> *>(a.spec) + (long)b * g.specBatch;
@@ -410,10 +503,17 @@ __global__ void __launch_bounds__(1024) k_fast_stat_rows(FastArgs a, FastGeom g,
             m = a.regModel[ri];
           }
         }
+        if (a.nPs && !inReg) m += ps_main(a, b, row, col, 0.f, nullptr);
         if (a.modelOut) a.modelOut[(long)b * g.nDataRows * g.nDataCols + zi] = m;
         float gz;
         stat_term(a, zi, m, S, gz);
         SG += gz * (inReg ? a.psfSumOs : a.psfSum);
+        if (wantGrad && a.nPs && gz != 0.f) {
+          if (inReg)
+            ps_region(a, g.rScale, b, row, col, gz * (1.f / (float)(g.rScale * g.rScale)), psAcc);
+          else
+            ps_main(a, b, row, col, gz, psAcc);
+        }
         if (inReg) {
           if (wantGrad) a.regG[ri] = gz;
           gz = 0.f;
@@ -452,6 +552,11 @@ __global__ void __launch_bounds__(1024) k_fast_stat_rows(FastArgs a, FastGeom g,
       p[0] = v0;
       p[a.partStride] = v1;
     }
+  }
+  if (wantGrad && a.nPs) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < 4 * a.nPs; i += blockDim.x)
+      a.psPart[((long)b * 4 * a.nPs + i) * a.partStride + blockIdx.x] = psAcc[i];
   }
 }
 
@@ -732,6 +837,17 @@ __global__ void __launch_bounds__(256) k_fast_reduce(FastArgs a, int nGradBlocks
   } else {
     const float *p = a.gradPart + ((long)b * a.nParams + (j - 2)) * a.partStride;
     for (int i = threadIdx.x; i < nGradBlocks; i += blockDim.x) t += (double)p[i];
+    // point sources: partials of the statistic CTAs for the parameters they touch
+    for (int ps = 0; ps < a.nPs; ps++) {
+      const CompDesc &d = a.desc[a.psComp[ps]];
+      const bool rot = d.type == F_POINTSOURCEROT;
+      const int map[4] = {d.x0Index, d.x0Index + 1, d.paramOffset + (rot ? 1 : 0), rot ? d.paramOffset : -1};
+      for (int q = 0; q < 4; q++) {
+        if (map[q] != j - 2) continue;
+        const float *pp = a.psPart + ((long)b * 4 * a.nPs + 4 * ps + q) * a.partStride;
+        for (int i = threadIdx.x; i < a.nStatBlocks; i += blockDim.x) t += (double)pp[i];
+      }
+    }
   }
   t = block_sum_d(t);
   if (threadIdx.x != 0) return;
@@ -928,6 +1044,30 @@ __global__ void __launch_bounds__(1024) k_fast_jtwj_rows(FastArgs a, FastGeom g,
     const long rStride = (long)g.rRows * g.rCols;
     for (int j = 0; j < nD; j++)
       U[(long)j * nc + col] = q * (inReg ? regDeriv[((long)b * nD + j) * rStride + ri] : Zr[2 * j * ls + col]);
+    for (int ps = 0; ps < a.nPs; ps++) {  // point sources: derivatives after the convolution
+      const CompF32 &c = a.comps[b * a.nComp + a.psComp[ps]];
+      const CompDesc &d = a.desc[a.psComp[ps]];
+      float dsum[4] = {0.f, 0.f, 0.f, 0.f};
+      float X, Y;
+      ps_offsets(c, row, col, X, Y);
+      if (inReg) {
+        const int k = g.rScale;
+        const float s = (float)k, h = 0.5f * (float)(k - 1), inv = 1.f / (float)(k * k);
+        for (int u = 0; u < k; u++)
+          for (int w = 0; w < k; w++) {
+            float dvv[4];
+            ps_eval(c, a.psReg, s * X - h + (float)w, s * Y - h + (float)u, s, dvv);
+            for (int t4 = 0; t4 < 4; t4++) dsum[t4] += dvv[t4] * inv;
+          }
+      } else {
+        const float s = c.s1;
+        if (!ps_far(a.psMain, s * X, s * Y)) ps_eval(c, a.psMain, s * X, s * Y, s, dsum);
+      }
+      const bool rot = d.type == F_POINTSOURCEROT;
+      const int map[4] = {d.x0Index, d.x0Index + 1, d.paramOffset + (rot ? 1 : 0), rot ? d.paramOffset : -1};
+      for (int t4 = 0; t4 < 4; t4++)
+        if (map[t4] >= 0 && ss[map[t4]] >= 0) U[(long)ss[map[t4]] * nc + col] += q * dsum[t4];
+    }
     qb[col] = q * (inReg ? a.psfSumOs : a.psfSum);
     cw[col] = cnt;
     cd[col] = cnt * dev;

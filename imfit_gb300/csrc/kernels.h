@@ -85,6 +85,9 @@ cudaError_t launch_flux64(const CompF64 &c, int xSize, int ySize, double *partia
 // model pixels; 3-D components are read from 'los' (may be null without them)
 cudaError_t launch_eval64(const CompF64 *comps, int nComp, double *model, long pitch, Grid64 g,
                           const double *los, cudaStream_t st);
+// point sources the fast path evaluates (per model)
+constexpr int kMaxPsFast = 8;
+
 // per-component PointSource::oversamplingScale of one point-source pass
 struct PsScales {
   int s[kMaxComponents];
@@ -192,6 +195,14 @@ struct FastArgs {
   float *losPan, *rLosPan;
   int *losCnt, *rLosCnt;
   int nLos;
+  // point sources, added after the convolution: component indices, the
+  // interpolators of the main PSF and of the region's oversampled PSF, and
+  // the gradient partials of the statistic CTAs, [B][nPs][4][partStride]
+  // (d/dX0, d/dY0, d/dI_tot, d/dPA)
+  int nPs;
+  int psComp[kMaxPsFast];
+  PsfInterp<float> psMain, psReg;
+  float *psPart;
 };
 
 // CTAs per parameter vector of each line-of-sight kernel (grid-stride, one

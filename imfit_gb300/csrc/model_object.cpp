@@ -226,6 +226,11 @@ struct imfit_model_s {
   DevBuf<double> dPsTab;
   PsfInterp<double> ps64{};
   int psKind = 0;
+  // fast path: FP32 interpolator tables, the component descriptors as on the
+  // device (their psScale follows psScale), the gradient partials
+  DevBuf<float> dPsTab32, dPsRegTab32, dPsPart;
+  PsfInterp<float> psMain32{}, psReg32{};
+  std::vector<CompDesc> hDesc;
   bool psfNormalize = true;
   double psfSum = 1.0;
   bool modelSetupDone = false, modelComputed = false;
@@ -1031,8 +1036,10 @@ struct imfit_model_s {
     if (fastReady) return 0;
     if (!finalSetupDone) return fail(IMFIT_E_STATE, "FinalSetupForFitting not called");
     if (!setsDefined) return fail(IMFIT_E_STATE, "DefineFunctionSets not called");
-    if (nPointSources)
-      return fail(IMFIT_E_UNSUPPORTED, "PointSource functions are evaluated on the plain FP64 path only");
+    if (nPointSources > kMaxPsFast) return fail(IMFIT_E_UNSUPPORTED, "more than 8 point sources for the fast path");
+    if (nPointSources && regions.size() > 1)
+      return fail(IMFIT_E_UNSUPPORTED, "point sources with more than one oversampled region on the fast path");
+    if (int st0 = ensurePointSourceInterp()) return st0;
     hasLos = false;
     for (auto &f : funcs)
       if (f.type == F_EXPDISK3D || f.type == F_FERRERS3D) hasLos = true;
@@ -1139,6 +1146,25 @@ struct imfit_model_s {
       d.x0Index = x0Index[f];
       d.nParams = funcs[f].nParams;
       d.background = (funcs[f].type == F_FLATSKY) ? 1 : 0;
+      d.psScale = psScale[f];
+    }
+    hDesc = desc;
+    if (!e && nPointSources) {
+      auto up = [&](const std::vector<double> &t64, DevBuf<float> &dst) {
+        std::vector<float> t32(t64.begin(), t64.end());
+        cudaError_t ee = dst.reserve(t32.size());
+        if (!ee) ee = cudaMemcpy(dst.p, t32.data(), sizeof(float) * t32.size(), cudaMemcpyHostToDevice);
+        return ee;
+      };
+      e = up(psf_interp_tables(psKind, psf.data(), nPsfCols, nPsfRows), dPsTab32);
+      psMain32 = PsfInterp<float>{psKind, nPsfCols, nPsfRows, 0, (float)((nPsfCols - 1) / 2.0),
+                                  (float)((nPsfRows - 1) / 2.0), dPsTab32.p};
+      if (!e && !regions.empty()) {
+        Region *r = regions[0];
+        e = up(psf_interp_tables(PSF_BICUBIC, r->psfRaw.data(), r->nPsfCols, r->nPsfRows), dPsRegTab32);
+        psReg32 = PsfInterp<float>{PSF_BICUBIC, r->nPsfCols, r->nPsfRows, 0, (float)((r->nPsfCols - 1) / 2.0),
+                                   (float)((r->nPsfRows - 1) / 2.0), dPsRegTab32.p};
+      }
     }
     if (!e) e = dDesc.reserve(desc.size());
     if (!e) e = cudaMemcpy(dDesc.p, desc.data(), sizeof(CompDesc) * desc.size(), cudaMemcpyHostToDevice);
@@ -1211,6 +1237,7 @@ struct imfit_model_s {
     if (!e && g.hasRegion) e = dRegG.reserve((size_t)B * g.rRows * g.rCols);
     if (!e) e = dStatPart.reserve((size_t)B * 2 * stride);
     if (!e) e = dGradPart.reserve((size_t)B * nP * stride);
+    if (!e && nPointSources) e = dPsPart.reserve((size_t)B * 4 * nPointSources * stride);
     if (!e) e = dStat.reserve(B);
     if (!e) e = dGrad.reserve((size_t)B * nP);
     const long area = (long)kBoxMain * kBoxMain + (long)boxReg() * boxReg();
@@ -1246,7 +1273,28 @@ struct imfit_model_s {
   }
   int boxReg() const { return fg.hasRegion ? 20 * fg.rScale + 5 : 0; }
 
+  // Point sources: the device descriptors carry each one's current
+  // PointSource::oversamplingScale; an evaluation that computes the
+  // oversampled region leaves the region's scale behind for the next one
+  // (the reference's object state, core/oversampled_region.cpp:370-375).
+  void syncPointSourceState() {
+    if (!nPointSources || hDesc.size() != funcs.size()) return;
+    bool changed = false;
+    for (size_t f = 0; f < funcs.size(); f++)
+      if (is_point_source(funcs[f].type) && hDesc[f].psScale != psScale[f]) {
+        hDesc[f].psScale = psScale[f];
+        changed = true;
+      }
+    if (changed)
+      cudaMemcpyAsync(dDesc.p, hDesc.data(), sizeof(CompDesc) * hDesc.size(), cudaMemcpyHostToDevice, stream);
+    if (!regions.empty() && !psStateFrozen)
+      for (size_t f = 0; f < funcs.size(); f++)
+        if (is_point_source(funcs[f].type)) psScale[f] = regions.back()->scale;
+  }
+  bool psStateFrozen = false;  // set while the autotuner's trial runs execute
+
   FastArgs fastArgs(const double *dP, double *dS, double *dG, float *modelOut) {
+    syncPointSourceState();
     FastArgs a{};
     a.subTab = dSubTab.p;
     a.subBox = dSubBox.p;
@@ -1285,6 +1333,12 @@ struct imfit_model_s {
     a.stat = dS;
     a.grad = dG;
     a.modelOut = modelOut;
+    a.nPs = 0;
+    for (size_t f = 0; f < funcs.size() && nPointSources; f++)
+      if (is_point_source(funcs[f].type)) a.psComp[a.nPs++] = (int)f;
+    a.psMain = psMain32;
+    a.psReg = psReg32;
+    a.psPart = dPsPart.p;
     if (hasLos) {
       a.losVal = dLosVal32.p;
       a.losRt = dLosRt32.p;
@@ -1333,6 +1387,13 @@ struct imfit_model_s {
   // Row shapes are tried with the automatic column shape, then column shapes
   // with the best row shape.  Runs outside any graph capture.
   int autotuneFast(int B, const double *dP, double *dS, double *dG) {
+    // trial evaluations leave the point sources' state as it was
+    struct Freeze {
+      bool &f;
+      bool old;
+      explicit Freeze(bool &x) : f(x), old(x) { f = true; }
+      ~Freeze() { f = old; }
+    } freeze(psStateFrozen);
     auto it = tuned.find(B);
     if (it != tuned.end()) {
       tune = it->second;
