@@ -2,6 +2,7 @@
 
     python -m imfit_gb300.cli CONFIG IMAGE [--psf F] [--mask F] [--noise F] ...
     python -m imfit_gb300.cli makeimage CONFIG [--ncols N --nrows M | --refimage F] ...
+    python -m imfit_gb300.cli mcmc CONFIG IMAGE [--nchains N] [--max-chain-length N] ...
 
 Reads an Imfit configuration file and FITS images and sets the model up in
 the reference's order (core/setup_model_object.cpp:36-157).  The fitting
@@ -9,7 +10,8 @@ command either prints the fit statistic at the initial parameters
 (--chisquare-only) or fits: Levenberg-Marquardt on the GPU's J^T J (chi^2 or
 Poisson-MLR; the Cash statistic has no deviates to fit by least squares), or,
 with --de, generation-synchronous differential evolution on the batched
-statistic.  makeimage follows core/makeimage_main.cpp:99-380: the model image,
+statistic.  mcmc runs DREAM (imfit-mcmc) with one batched GPU evaluation per
+generation.  makeimage follows core/makeimage_main.cpp:99-380: the model image,
 optionally the expanded (PSF-padded) image, single-function images and the
 component-flux table.  Option names follow core/imfit_main.cpp and
 core/makeimage_main.cpp; only the ones that matter for the model-image path
@@ -328,10 +330,70 @@ def makeimage(argv=None, out=sys.stdout):
     return model, table
 
 
+def build_mcmc_parser():
+    ap = build_parser()
+    ap.prog = "imfit_gb300.cli mcmc"
+    ap.description = "DREAM MCMC (imfit-mcmc) on the batched GPU statistic"
+    ap.add_argument("-o", "--output", default="mcmc_out", help="root name of the chain files")
+    ap.add_argument("--nchains", type=int, default=0)
+    ap.add_argument("--max-chain-length", type=int, default=100000)
+    ap.add_argument("--burnin-length", type=int, default=5000)
+    ap.add_argument("--gelman-evals", type=int, default=5000)
+    ap.add_argument("--gelman-rubin-limit", type=float, default=1.01)
+    ap.add_argument("--uniform-offset", type=float, default=0.01)
+    ap.add_argument("--gaussian-offset", type=float, default=1.0e-6)
+    return ap
+
+
+def mcmc(argv=None, out=sys.stdout):
+    """The imfit-mcmc command (core/mcmc_main.cpp:150-460): chains written to
+    OUTPUT.1.txt ... OUTPUT.<nchains>.txt; returns the sampler's result."""
+    from .config import _NPARAMS
+    from .solvers import chain_file_header, chain_file_row, dream
+    args = build_mcmc_parser().parse_args(argv)
+    try:
+        cfg = read_config(args.config)
+    except ConfigError as e:
+        raise SystemExit(f"error in {args.config}: {e}")
+    image = fitsio.read_image(args.image)[0]
+    m = setup_model(cfg, args, image)
+    p0 = np.array(cfg.values, dtype=float)
+    fixed = cfg.fixed.astype(bool)
+    if np.any(np.isnan(cfg.lower[~fixed])):
+        raise SystemExit("parameter limits must be supplied for all free parameters when using MCMC")
+    head = chain_file_header(cfg.functions, cfg.param_names, _NPARAMS)
+    files = []
+
+    def write(t, states, liks, burn, pCR, accept):
+        if not files:
+            for i in range(states.shape[0]):
+                f = open(f"{args.output}.{i + 1}.txt", "w")
+                f.write(f"# imfit_gb300 mcmc, configuration file {args.config}, image {args.image}\n#\n")
+                f.write("# Column Headers\n" + head + "\n")
+                files.append(f)
+        for i, f in enumerate(files):
+            f.write(chain_file_row(states[i], liks[i], burn, pCR, accept[i]) + "\n")
+
+    try:
+        r = dream(m, p0, cfg.lower, cfg.upper, fixed=fixed, n_chains=args.nchains,
+                  max_generations=args.max_chain_length, burn_in=args.burnin_length, gelman_evals=args.gelman_evals,
+                  scale_reduction=args.gelman_rubin_limit, noise=args.uniform_offset, bstar=args.gaussian_offset,
+                  seed=args.seed, callback=write)
+    finally:
+        for f in files:
+            f.close()
+    out.write(f"{r['generations']} generations of {r['n_chains']} chains, {r['evaluations']} likelihood "
+              f"evaluations; {'converged' if r['converged'] else 'maximum chain length reached'}\n")
+    out.write(f"chains written to {args.output}.1.txt through {args.output}.{r['n_chains']}.txt\n")
+    return r
+
+
 def main(argv=None):
     argv = sys.argv[1:] if argv is None else argv
     if argv and argv[0] == "makeimage":
         makeimage(argv[1:])
+    elif argv and argv[0] == "mcmc":
+        mcmc(argv[1:])
     else:
         run(argv)
 

@@ -207,3 +207,220 @@ def bootstrap_file_lines(functions, param_names, n_params, samples, n_iterations
     lines = ["#", f"# Bootstrap resampling output ({n_iterations} iterations requested):", header]
     lines += ["\t".join(format(float(v), "#.10g") for v in row) for row in np.atleast_2d(samples)]
     return lines
+
+
+# --------------------------------------------------------------------------
+# DREAM Markov-chain Monte Carlo (cdream/dream.cpp:66-505 as imfit-mcmc sets
+# it up, core/mcmc_main.cpp:360-440): differential-evolution proposals from
+# delta chain pairs with randomised crossover (nCR = 3 values, their
+# probabilities adapted during burn-in), Metropolis acceptance on
+# log L = -statistic / 2, outlier chains moved to the best chain, and the
+# Gelman-Rubin test on the second half of the post-burn-in samples.  The
+# reference already forms every chain's proposal before evaluating any of
+# them; here those evaluations are one batched GPU call per generation.
+# Re-evaluating the previous states during burn-in (recalcLik + inBurnIn in
+# dream.cpp:290-300) returns the same deterministic values and is skipped.
+# The random stream is numpy's, not GSL's: chains are statistically, not
+# bitwise, the reference's.
+
+def _gsl_quantile_sorted(v, f):
+    """gsl_stats_quantile_from_sorted_data: linear interpolation at (n-1) f."""
+    delta = (len(v) - 1) * f
+    lo = int(np.floor(delta))
+    frac = delta - lo
+    if lo + 1 < len(v):
+        return (1.0 - frac) * v[lo] + frac * v[lo + 1]
+    return v[lo]
+
+
+def gelman_rubin(samples):
+    """cdream/gelman_rubin.cpp with adjustDF = 0: samples [n][chains][vars];
+    returns sqrt(Rhat) per variable (1 where the within-chain variance is 0)."""
+    n, m = samples.shape[0], samples.shape[1]
+    means = samples.mean(axis=0)                       # [chains][vars]
+    W = samples.var(axis=0, ddof=1).mean(axis=0)       # mean within-chain variance
+    Bdivn = means.var(axis=0, ddof=1)                  # variance of the chain means
+    sigma2 = (n - 1.0) / n * W + Bdivn
+    Vhat = sigma2 + Bdivn / m
+    with np.errstate(divide="ignore", invalid="ignore"):
+        r = np.where(W > 0.0, np.sqrt(Vhat / W), 1.0)
+    return r
+
+
+def dream(model, x0, lower, upper, fixed=None, n_chains=None, max_generations=100000, burn_in=5000,
+          gelman_evals=5000, scale_reduction=1.01, noise=0.01, bstar=1.0e-6, n_cr=3, loop_steps=10,
+          collapse_outliers=True, reenter_burnin=0.2, seed=0, callback=None):
+    """DREAM on model's batched statistic (log L = -S/2).  Defaults are
+    imfit-mcmc's (options_mcmc.h:72-79, dream_pars.cpp:8-45): n_chains = free
+    parameters, 100000 generations at most, 5000 burn-in, a Gelman-Rubin check
+    every gelman_evals generations (in loop_steps units) after burn-in,
+    R-hat limit 1.01, noise b = 0.01, b* = 1e-6, deltaMax = (nfree - 1) / 2.
+    callback(t, states[nChains][n], liks, in_burn_in, pCR, accept) is called
+    after every generation (the chain files' rows).  Returns a dict with the
+    chains [generations][chains][n], their log-likelihoods, burn-in flags and
+    the convergence state."""
+    rng = np.random.default_rng(seed)
+    x0 = np.asarray(x0, dtype=float)
+    nv = x0.size
+    lock = np.zeros(nv, dtype=bool) if fixed is None else np.asarray(fixed, dtype=bool)
+    lo = np.where(lock, x0, np.asarray(lower, dtype=float))
+    hi = np.where(lock, x0, np.asarray(upper, dtype=float))
+    if np.any(~np.isfinite(lo[~lock])) or np.any(~np.isfinite(hi[~lock])):
+        raise ValueError("MCMC needs finite limits for every free parameter")
+    nfree = int(np.sum(~lock))
+    nC = nfree if not n_chains or n_chains <= 0 else int(n_chains)
+    if nC < 3:
+        raise ValueError("DREAM needs at least 3 chains")
+    delta_max = (nfree - 1) // 2
+    gelman_loops = max(1, int(gelman_evals / 10))  # mcmc_main.cpp:412
+    free = np.where(~lock)[0]
+
+    def loglik(P, need):
+        out = np.full(P.shape[0], -np.inf)
+        if np.any(need):
+            out[need] = -0.5 * np.asarray(model.batch_statistic_and_gradient(P[need], want_grad=False))
+        return out
+
+    # Latin-hypercube start (dream_initialize.cpp:18-62)
+    perm = np.argsort(rng.random((nv, nC)), axis=1)  # samples(j, i)
+    state0 = np.empty((nC, nv))
+    for i in range(nC):
+        for j in range(nv):
+            if lock[j]:
+                state0[i, j] = lo[j]
+            else:
+                v = lo[j] + perm[j, i] * (hi[j] - lo[j]) / nC + (hi[j] - lo[j]) / nC * rng.random()
+                state0[i, j] = min(max(v, lo[j]), hi[j])
+    states = [state0]
+    liks = [loglik(state0, np.ones(nC, dtype=bool))]
+    flags = [1 if burn_in > 0 else 0]
+    in_burn = burn_in > 0
+    burn_start = 0
+    pCR = np.full(n_cr, 1.0 / n_cr)
+    delta_tot = np.ones(n_cr)
+    total_steps = np.zeros(n_cr)
+    L = np.zeros(n_cr)
+    CRm = None
+    gen_number = 0
+    cur_run = 0
+    converged = False
+    n_evals = nC
+    accepted_total = 0
+    scale_red = np.full(nv, np.inf)
+    if callback:
+        callback(0, state0, liks[0], in_burn, pCR, np.ones(nC, dtype=int))
+    t = 0
+    for t in range(1, max_generations):
+        cur = states[-1]
+        lcur = liks[-1]
+        if gen_number == 0:  # gen_CR.cpp: multinomial counts of the nCR values, shuffled
+            L = rng.multinomial(nC * loop_steps, pCR).astype(float)
+            flat = np.repeat(np.arange(1, n_cr + 1), L.astype(int))
+            rng.shuffle(flat)
+            CRm = flat.reshape(nC, loop_steps)
+        prop = cur.copy()
+        update_dim = np.full(nC, nfree)
+        for i in range(nC):
+            delta = int(rng.integers(1, delta_max + 1)) if delta_max > 1 else 1
+            r1 = rng.integers(0, nC - 1, size=delta)
+            r1 = r1 + (r1 >= i)
+            r2 = rng.integers(0, nC - 1, size=delta)
+            for a in range(delta):
+                while nC > 2 and (r2[a] == r1[a] or r2[a] == i):
+                    r2[a] = (r2[a] + 1) % nC
+            e = noise * (2.0 * rng.random(nv) - 1.0)
+            eps = rng.normal(0.0, bstar, nv)
+            pair = np.zeros(nv)
+            for a in range(delta):
+                if r1[a] != r2[a]:
+                    pair += cur[r1[a]] - cur[r2[a]]
+            cross = CRm[i, gen_number] / n_cr
+            upd = ~lock.copy()
+            if cross < 1.0:
+                drop = rng.random(nv) < 1.0 - cross
+                upd &= ~drop
+            update_dim[i] = int(np.sum(upd))
+            if update_dim[i] > 0:
+                gamma = 1.0 if (t > 1 and t % 5 == 0) else 2.38 / np.sqrt(2.0 * update_dim[i] * delta)
+                prop[i, upd] = cur[i, upd] + (1.0 + e[upd]) * gamma * pair[upd] + eps[upd]
+        inside = np.all((prop[:, free] >= lo[free]) & (prop[:, free] <= hi[free]), axis=1)
+        need = (update_dim > 0) & inside
+        lnew = loglik(prop, need)
+        n_evals += int(np.sum(need))
+        lnew[update_dim == 0] = lcur[update_dim == 0]
+        u = rng.random(nC)
+        accept = np.where(np.isneginf(lnew), 0,
+                          np.where(lnew >= lcur, 1, (np.log(u) < lnew - lcur).astype(int)))
+        new = np.where(accept[:, None] == 1, prop, cur)
+        lnew = np.where(accept == 1, lnew, lcur)
+        accepted_total += int(accept.sum())
+        if in_burn:  # crossover adaptation (dream.cpp:338-357)
+            sd = new.std(axis=0, ddof=1)
+            for i in range(nC):
+                if accept[i]:
+                    ok = (~lock) & (sd > 0.0)
+                    delta_tot[CRm[i, gen_number] - 1] += float(np.sum(((new[i, ok] - cur[i, ok]) / sd[ok]) ** 2))
+        gen_number += 1
+        if gen_number >= loop_steps:
+            gen_number = 0
+            if in_burn:
+                dsum = float(delta_tot.sum())
+                total_steps += L
+                if dsum > 0.0:
+                    pCR = (delta_tot / dsum) / total_steps
+                    pCR = pCR / pCR.sum()
+            if collapse_outliers and t < reenter_burnin * max_generations:
+                t0 = t // 2
+                past = np.array(liks[t0:t] if t > t0 else [lnew])
+                meanlik = past.mean(axis=0)
+                srt = np.sort(meanlik)
+                q1, q3 = _gsl_quantile_sorted(srt, 0.25), _gsl_quantile_sorted(srt, 0.75)
+                out = meanlik < q1 - 2.0 * (q3 - q1)
+                best = int(np.argmax(meanlik))
+                for i in np.where(out)[0]:
+                    if i == best:
+                        continue
+                    new[i] = new[best]
+                    lnew[i] = lnew[best]
+                    if not in_burn and burn_in > 0:
+                        burn_start, cur_run, in_burn = t, 0, True
+            if not in_burn:
+                cur_run += 1
+                if cur_run >= gelman_loops:
+                    first = burn_start + burn_in
+                    t0 = (t + first) // 2
+                    n = t - t0 - 1
+                    if n > 1:
+                        S = np.array(states[t0:t0 + n])
+                        scale_red = gelman_rubin(S)
+                        if np.all(scale_red[free] < scale_reduction):
+                            converged = True  # the reference stops before recording generation t
+                            break
+                    cur_run = 0
+            elif t >= burn_start + burn_in:
+                in_burn = False
+        states.append(new)
+        liks.append(lnew)
+        flags.append(1 if t < burn_start + burn_in else 0)
+        if callback:
+            callback(t, new, lnew, t < burn_start + burn_in, pCR, accept)
+    return dict(chains=np.array(states), loglik=np.array(liks), burn_in=np.array(flags), converged=converged,
+                generations=len(states), n_chains=nC, evaluations=n_evals, scale_reduction=scale_red,
+                acceptance=accepted_total / max(1, nC * t), burn_in_end=burn_start + burn_in)
+
+
+def chain_file_header(functions, param_names, n_params, n_cr=3):
+    """Column-header line of an imfit-mcmc chain file (core/mcmc_main.cpp:421-428)."""
+    head = bootstrap_file_lines(functions, param_names, n_params, np.empty((0, len(param_names))), 0)[2]
+    head += "  likelihood  burn-in    "
+    head += "".join(f"CR{i + 1}               " for i in range(n_cr - 1)) + f"CR{n_cr}        accept"
+    return head
+
+
+def chain_file_row(params, loglik, burn_in, pCR, accept):
+    """One chain-file row (cdream/dream.cpp:458-468): the parameters as
+    PrintModelParamsHorizontalString writes them, then log L, the burn-in flag,
+    the crossover probabilities (scientific, 12 digits) and the acceptance."""
+    row = "\t".join(format(float(v), "#.10g") for v in params)
+    row += f" {loglik:.12e} {int(burn_in)}  " + "".join(f"{float(p):.12e} " for p in pCR) + f"{int(accept)}"
+    return row

@@ -2,7 +2,7 @@
 
 Run in a checkout that has the reference at /root/reference (or
 IMFIT_REFERENCE_DIR):  python tests/golden/make_golden.py [part ...]
-(parts: n3073 makeimage ic3478 pointsource small_case; all by default)
+(parts: n3073 makeimage ic3478 pointsource mcmc small_case; all by default)
 
 Outputs (all small .npz files next to this script):
   n3073.npz          the reference regression inputs tests/n3073rss_small.fits,
@@ -23,6 +23,13 @@ Outputs (all small .npz files next to this script):
   pointsource.npz    unit_tests/psf_gauss_sigma0.5_5.fits (the PSF of
                      unittest_psf_interpolators.t.h) and the makeimage output
                      tests/oversampled_pointsource.fits (do_makeimage_tests:74).
+  mcmc.npz           tests/faintstar.fits with
+                     tests/imfit-mcmc_reference/config_imfit_faintstar.dat, and
+                     summaries of the reference's DREAM chain 1 for it
+                     (tests/imfit-mcmc_reference/mcmc_ref1.1.txt_skip3,
+                     do_mcmc_tests:27): post-burn-in means, standard deviations
+                     and 16/50/84 % quantiles per parameter, the number of
+                     rows and the burn-in rows.
   small_case.npz     the reference's own outputs (oracle/_ref) for
                      imfit_gb300.workloads.small_case: model images, deviates and
                      statistics for chi^2 / Cash / PMLR.
@@ -126,6 +133,22 @@ def pointsource():
                         ps_scale=3)
 
 
+def mcmc():
+    t = os.path.join(REF, "tests")
+    data, _ = fits.read_image(os.path.join(t, "faintstar.fits"))
+    rows = np.loadtxt(os.path.join(t, "imfit-mcmc_reference", "mcmc_ref1.1.txt_skip3"), comments="#")
+    post = rows[rows[:, 7] == 0][:, :6]
+    np.savez_compressed(
+        os.path.join(HERE, "mcmc.npz"), data=data.astype(np.float32), gain=4.72, read_noise=1.15,
+        original_sky=124.94,
+        # X0 Y0 PA ell I_0 sigma with their limits
+        params=np.array([5.0, 6.0, 155.0, 0.1, 250.0, 1.0]),
+        lo=np.array([3.0, 3.0, 140.0, 0.0, 220.0, 0.1]), hi=np.array([8.0, 8.0, 170.0, 0.3, 320.0, 1.5]),
+        ref_rows=rows.shape[0], ref_burn_rows=int(np.sum(rows[:, 7] == 1)),
+        ref_mean=post.mean(axis=0), ref_std=post.std(axis=0, ddof=1),
+        ref_q=np.percentile(post, [16, 50, 84], axis=0), ref_best_loglik=rows[:, 6].max())
+
+
 def small_case():
     out = {}
     for stat in ("chi2", "cash", "pmlr"):
@@ -145,7 +168,7 @@ if __name__ == "__main__":
         sys.exit(f"reference checkout not found at {REF}")
     oracle.build_reference()
     parts = {"n3073": n3073, "makeimage": makeimage, "ic3478": ic3478, "pointsource": pointsource,
-             "small_case": small_case}
+             "mcmc": mcmc, "small_case": small_case}
     for name in (sys.argv[1:] or parts):
         parts[name]()
     for f in sorted(os.listdir(HERE)):

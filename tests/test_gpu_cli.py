@@ -221,3 +221,35 @@ def test_cli_bootstrap_output(gpu, tmp_path):
     assert lines[1] == "# Bootstrap resampling output (8 iterations requested):"
     assert lines[2] == "# X0_1\t\tY0_1\t\tPA_1\tell_1\tn_1\tI_e_1\tr_e_1\t"
     assert len(lines) == 3 + 8 and all(len(x.split("\t")) == 7 for x in lines[3:])
+
+
+def test_mcmc_faintstar_posterior(gpu, tmp_path):
+    """do_mcmc_tests:27 (imfit-mcmc on tests/faintstar.fits, --no-subsampling):
+    the DREAM chains' post-burn-in posterior against the reference's chain 1
+    (tests/imfit-mcmc_reference/mcmc_ref1.1.txt_skip3) -- means within 0.3 of
+    its standard deviations, widths within 25 % -- and the chain files'
+    layout.  The samplers share the algorithm, not the random stream."""
+    from imfit_gb300 import cli, fits
+    d = np.load(os.path.join(GOLDEN, "mcmc.npz"))
+    names = ["X0", "Y0", "PA", "ell", "I_0", "sigma"]
+    lines = [f"GAIN {float(d['gain'])}", f"READNOISE {float(d['read_noise'])}",
+             f"ORIGINAL_SKY {float(d['original_sky'])}"]
+    for j, (nm, v, lo, hi) in enumerate(zip(names, d["params"], d["lo"], d["hi"])):
+        if j == 2:
+            lines.append("FUNCTION Gaussian")
+        lines.append(f"{nm} {float(v)!r} {float(lo)!r},{float(hi)!r}")
+    (tmp_path / "c.dat").write_text("\n".join(lines) + "\n")
+    fits.write_image(str(tmp_path / "star.fits"), d["data"])
+    root = str(tmp_path / "chain")
+    r = cli.mcmc([str(tmp_path / "c.dat"), str(tmp_path / "star.fits"), "--nosubsampling", "--seed", "7",
+                  "-o", root], out=io.StringIO())
+    # burn-in ends at 5000 unless an outlier chain after it sends the sampler back (dream.cpp:386-397)
+    assert r["converged"] and r["n_chains"] == 6 and r["burn_in_end"] >= 5000
+    post = r["chains"][r["burn_in"] == 0].reshape(-1, 6)
+    mean, std = post.mean(axis=0), post.std(axis=0, ddof=1)
+    assert np.all(np.abs(mean - d["ref_mean"]) < 0.3 * d["ref_std"]), (mean, d["ref_mean"])
+    assert np.all(np.abs(std / d["ref_std"] - 1.0) < 0.25), (std, d["ref_std"])
+    rows = np.loadtxt(root + ".1.txt", comments="#")
+    assert rows.shape == (r["generations"], 12) and np.all(rows[:5000, 7] == 1)
+    assert np.array_equal(rows[:, 7], r["burn_in"]) and np.all(rows[r["burn_in_end"]:, 7] == 0)
+    assert abs(rows[:, 6].max() - float(d["ref_best_loglik"])) < 0.5

@@ -105,3 +105,43 @@ def test_bootstrap_file_layout():
     assert lines[:2] == ["#", "# Bootstrap resampling output (5 iterations requested):"]
     assert lines[2] == "# X0_1\t\tY0_1\t\tPA_1\tell_1\tn_1\tI_e_1\tr_e_1\tI_sky_2\t"
     assert lines[3].split("\t")[:2] == ["0.5000000000", "1.500000000"]
+
+
+def test_dream_samples_a_gaussian_posterior():
+    """DREAM (cdream/dream.cpp) on log L = -chi^2/2 of independent Gaussians:
+    post-burn-in chains reproduce the means and widths; Gelman-Rubin passes."""
+    q = Quadratic([1.0, -2.0, 5.0, 0.3], [0.1, 0.5, 2.0, 0.05], floor=0.0)
+    r = solvers.dream(q, [0, 0, 0, 0], [-5, -10, -20, -1], [5, 10, 30, 1], burn_in=1000, gelman_evals=2000,
+                      max_generations=30000, seed=1)
+    assert r["converged"] and r["n_chains"] == 4
+    post = r["chains"][r["burn_in"] == 0].reshape(-1, 4)
+    assert np.all(np.abs(post.mean(axis=0) - q.c) < 0.15 * q.s)
+    assert np.all(np.abs(post.std(axis=0) / q.s - 1.0) < 0.15)
+    assert np.all(r["scale_reduction"] < 1.01)
+
+
+def test_gelman_rubin_and_quantiles():
+    """cdream/gelman_rubin.cpp (adjustDF = 0) and GSL's sorted-data quantile."""
+    rng = np.random.default_rng(0)
+    S = rng.normal(size=(400, 5, 2))
+    S[:, :, 1] += np.arange(5)[None, :]  # chains with different means: large R-hat
+    r = solvers.gelman_rubin(S)
+    n, m = 400, 5
+    W = S[:, :, 0].var(axis=0, ddof=1).mean()
+    B = S[:, :, 0].mean(axis=0).var(ddof=1)
+    assert abs(r[0] - np.sqrt(((n - 1) / n * W + B + B / m) / W)) < 1e-12
+    assert r[0] < 1.02 and r[1] > 2.0
+    assert solvers._gsl_quantile_sorted([1.0, 2.0, 4.0], 0.25) == 1.5
+    assert solvers._gsl_quantile_sorted([1.0, 2.0, 4.0], 0.75) == 3.0
+
+
+def test_chain_file_layout():
+    from imfit_gb300.config import _NPARAMS
+    head = solvers.chain_file_header([("Gaussian", True)], ["X0", "Y0", "PA", "ell", "I_0", "sigma"], _NPARAMS)
+    assert head == ("# X0_1\t\tY0_1\t\tPA_1\tell_1\tI_0_1\tsigma_1\t  likelihood  burn-in    CR1               "
+                    "CR2               CR3        accept")
+    row = solvers.chain_file_row([4.114481249, 4.845422845, 142.3764518, 0.1425389645, 232.4511719, 1.04774257],
+                                 -2616.014985785, 1, [1 / 3, 1 / 3, 1 / 3], 1)
+    # the first row of tests/imfit-mcmc_reference/mcmc_ref1.1.txt_skip3
+    assert row == ("4.114481249\t4.845422845\t142.3764518\t0.1425389645\t232.4511719\t1.047742570 "
+                   "-2.616014985785e+03 1  3.333333333333e-01 3.333333333333e-01 3.333333333333e-01 1")
