@@ -64,6 +64,7 @@ def build_parser():
     ap.add_argument("--chisquare-only", action="store_true")
     ap.add_argument("--de", action="store_true", help="differential evolution instead of LM")
     ap.add_argument("--de-lhs", action="store_true", help="--de with a Latin-hypercube initial population")
+    ap.add_argument("--nm", action="store_true", help="Nelder-Mead simplex instead of LM")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--bootstrap", type=int, default=0, help="number of bootstrap resampling iterations")
     ap.add_argument("--save-bootstrap", help="file for the bootstrap best-fit parameters")
@@ -199,9 +200,17 @@ def run(argv=None, out=sys.stdout):
         p = r["params"]
         out.write(f"differential evolution: {r['generations']} generations of {r['population']} "
                   f"({'converged' if r['converged'] else 'generation limit'})\n")
+    elif args.nm:
+        from .solvers import nelder_mead
+        lo = np.where(np.isnan(cfg.lower), -np.inf, cfg.lower)
+        hi = np.where(np.isnan(cfg.upper), np.inf, cfg.upper)
+        r = nelder_mead(m, p0, lo, hi, fixed=cfg.fixed.astype(bool), ftol=args.ftol)
+        p = r["params"]
+        out.write(f"Nelder-Mead simplex: {r['evaluations']} evaluations "
+                  f"({'converged' if r['converged'] else 'evaluation limit'})\n")
     else:
         if args.cashstat:
-            raise SystemExit("the Cash statistic has no deviates: use --chisquare-only, --de, or fit "
+            raise SystemExit("the Cash statistic has no deviates: use --chisquare-only, --de, --nm, or fit "
                              "chi^2 / --poisson-mlr")
         limited = ~np.isnan(cfg.lower)
         lo = np.where(limited, cfg.lower, 0.0)

@@ -424,3 +424,35 @@ def chain_file_row(params, loglik, burn_in, pCR, accept):
     row = "\t".join(format(float(v), "#.10g") for v in params)
     row += f" {loglik:.12e} {int(burn_in)}  " + "".join(f"{float(p):.12e} " for p in pCR) + f"{int(accept)}"
     return row
+
+
+def nelder_mead(model, x0, lower, upper, fixed=None, ftol=1e-8, max_evals=None):
+    """Nelder-Mead simplex on the FP64 statistic (GetFitStatistic), as
+    solvers/nmsimplex_fit.cpp:160-210 sets NLopt's NLOPT_LN_NELDERMEAD up:
+    relative and absolute f tolerance ftol, relative x tolerance ftol,
+    10000 x nParams evaluations at most, box limits.  NLopt is not in this
+    image: scipy's Nelder-Mead (Gao-Han adaptive coefficients off) stands in,
+    so the path to the minimum differs from NLopt's while the minimum does not.
+    Fixed parameters are held out of the simplex."""
+    from scipy.optimize import minimize
+    x0 = np.asarray(x0, dtype=float)
+    n = x0.size
+    fixed = np.zeros(n, dtype=bool) if fixed is None else np.asarray(fixed, dtype=bool)
+    free = np.where(~fixed)[0]
+    lo = np.asarray(lower, dtype=float)
+    hi = np.asarray(upper, dtype=float)
+    count = [0]
+
+    def f(z):
+        x = x0.copy()
+        x[free] = z
+        count[0] += 1
+        return model.get_fit_statistic(x)
+
+    bounds = [(lo[j] if np.isfinite(lo[j]) else None, hi[j] if np.isfinite(hi[j]) else None) for j in free]
+    res = minimize(f, x0[free], method="Nelder-Mead", bounds=bounds,
+                   options=dict(xatol=ftol * max(1.0, float(np.max(np.abs(x0[free])))), fatol=ftol,
+                                maxfev=max_evals or 10000 * n, adaptive=False))
+    x = x0.copy()
+    x[free] = res.x
+    return dict(params=x, statistic=model.get_fit_statistic(x), evaluations=count[0], converged=bool(res.success))

@@ -119,6 +119,19 @@ def _ic3478_files(tmp_path):
     return d
 
 
+def test_ic3478_nelder_mead_matches_printed_result(gpu, tmp_path):
+    """do_imfit_tests:70 (imfit_textout3b, --nm): the simplex ends at the
+    printed minimum (CHI-SQUARE 4555.947706, NLopt's) to 2e-7 and within
+    0.1 sigma of its printed parameters."""
+    from imfit_gb300 import cli
+    d = _ic3478_files(tmp_path)
+    p, s = cli.run([str(tmp_path / "c.dat"), str(tmp_path / "data.fits"), "--nm", "--save-params",
+                    str(tmp_path / "b.dat")], out=io.StringIO())
+    want = np.array([32.9440, 34.0933, 18.2602, 0.235985, 2.40034, 20.0081, 60.7635])
+    assert np.all(np.abs(p - want) <= 0.1 * d["lm_errors_printed"]), (p, want)
+    assert s <= 4555.947706 * (1 + 2e-7)
+
+
 @pytest.mark.parametrize("solver", ["lm", "de"])
 def test_ic3478_fits_match_printed_results(gpu, tmp_path, solver):
     """do_imfit_tests:68 and :75 (imfit_textout3, imfit_textout3c_tail):
