@@ -97,6 +97,7 @@ _SIGS = [
     ("imfit_SetConcurrentRegions", _I, [_P, _I]),
     ("imfit_SetAutotune", _I, [_P, _I]),
     ("imfit_GetLaunchShape", _I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)]),
+    ("imfit_SetLaunchShape", _I, [_P, _I, _I, _I, _I]),
     ("imfit_HostAlloc", _I, [ctypes.c_ulong, ctypes.POINTER(_P)]),
     ("imfit_HostFree", _I, [_P]),
     ("imfit_ChiSquaredDeviceNoAlloc", _I, [_P, _P, _P, _L, _P, _P]),
@@ -480,6 +481,10 @@ class ModelObject:
 
     def set_autotune(self, flag):
         return self._ck(self.lib.imfit_SetAutotune(self.h, int(flag)))
+
+    def set_launch_shape(self, rows_per_cta=-1, row_threads=256, cols_per_cta=0, col_threads=0):
+        """Pin the fast path's launch shape (rows_per_cta < 0: autotune again)."""
+        return self._ck(self.lib.imfit_SetLaunchShape(self.h, rows_per_cta, row_threads, cols_per_cta, col_threads))
 
     def launch_shape(self):
         a, b, c = _I(), _I(), _I()

@@ -38,6 +38,7 @@ struct FFTLen {
 int line_threads(int points);
 // smallest 7-smooth (2,3,5,7) integer >= n, optionally even
 int smooth_size(int n, bool even);
+
 // radix schedule (8,4,2,3,5,7 preference); returns number of passes or -1
 int radix_schedule(int n, int *radix);
 // allocate/free the device tables of one length

@@ -308,6 +308,8 @@ struct imfit_model_s {
   FastTune tune;
   std::map<int, FastTune> tuned;  // per batch size
   bool autotune = true;
+  bool hasFixedTune = false;  // imfit_SetLaunchShape
+  FastTune fixedTune;
   int fastCap = 0;
   bool useGraphs = true;
   Captured graph;
@@ -1405,8 +1407,8 @@ struct imfit_model_s {
       tuned[B] = tune;
       return 0;
     }
-    if (!autotune) {
-      tune = FastTune{};
+    if (hasFixedTune || !autotune) {
+      tune = hasFixedTune ? fixedTune : FastTune{};
       tuned[B] = tune;
       return 0;
     }
@@ -2341,6 +2343,25 @@ int imfit_SetKernelTimingStage(imfit_model_t m, const char *stage) {
 int imfit_SetAutotune(imfit_model_t m, int enable) {
   GET(m);
   m->autotune = enable != 0;
+  m->tuned.clear();
+  if (m->graph.exec) {
+    cudaGraphExecDestroy(m->graph.exec);
+    m->graph = Captured{};
+  }
+  return 0;
+}
+
+int imfit_SetLaunchShape(imfit_model_t m, int rowRpb, int rowThreads, int colCpb, int colThreads) {
+  GET(m);
+  if (rowRpb < 0) {
+    m->hasFixedTune = false;
+  } else {
+    if (rowRpb < 1 || rowRpb > 4 || rowThreads < 32 || rowThreads > 1024 || rowThreads % 32 || colCpb < 0 ||
+        colCpb > 8 || colThreads < 0 || colThreads > 1024 || colThreads % 32)
+      return m->fail(IMFIT_E_ARG, "bad launch shape");
+    m->fixedTune = FastTune{rowRpb, rowThreads, colCpb, colThreads};
+    m->hasFixedTune = true;
+  }
   m->tuned.clear();
   if (m->graph.exec) {
     cudaGraphExecDestroy(m->graph.exec);

@@ -277,6 +277,11 @@ int imfit_SetConcurrentRegions(imfit_model_t m, int enable);
  * parameters and keeps the fastest.  GetLaunchShape reports the choice. */
 int imfit_SetAutotune(imfit_model_t m, int enable);
 int imfit_GetLaunchShape(imfit_model_t m, int *rowsPerCta, int *rowThreads, int *colsPerCta);
+/* Pin the fast path's launch shape instead of autotuning (rowsPerCta < 0
+ * returns to autotuning): rows per CTA 1..4 and threads per row CTA; columns
+ * per CTA 1..8 of the column FFT (0: automatic) and threads per column CTA
+ * (0: automatic). */
+int imfit_SetLaunchShape(imfit_model_t m, int rowsPerCta, int rowThreads, int colsPerCta, int colThreads);
 /* Page-locked host memory for the host-buffer entry points (cudaMallocHost). */
 int imfit_HostAlloc(unsigned long bytes, void **ptr);
 int imfit_HostFree(void *ptr);
