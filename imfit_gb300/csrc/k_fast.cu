@@ -358,6 +358,8 @@ __device__ float ps_region(const FastArgs &a, int k, int b, int row, int col, fl
 // (also used for the derivative images of the JtWJ pass: batch index b then
 // runs over (parameter vector, parameter) pairs, no background is added and
 // the output goes to a different buffer)
+// PS: the model has point sources (their code is compiled only into the PS instance)
+template <bool PS>
 __global__ void __launch_bounds__(1024) k_fast_region_down(FastArgs a, FastGeom g, const cplx<float> *__restrict__ rspec,
                                                           FFTPlan<float> plan, const cplx<float> *__restrict__ twL,
                                                           float *__restrict__ out, int addBackground) {
@@ -390,7 +392,8 @@ __global__ void __launch_bounds__(1024) k_fast_region_down(FastArgs a, FastGeom 
         const cplx<float> z = Z[u * ls + (col >> 1)];
         acc += (col & 1) ? z.y : z.x;
       }
-    if (addBackground && a.nPs) acc += ps_region(a, k, b, g.ry0 + s, g.rx0 + t, 0.f, nullptr);
+    if constexpr (PS)
+      if (addBackground) acc += ps_region(a, k, b, g.ry0 + s, g.rx0 + t, 0.f, nullptr);
     out[((long)b * g.rRows + s) * g.rCols + t] = acc * inv + bg;
   }
 }
@@ -446,6 +449,7 @@ __device__ __forceinline__ void stat_term(const FastArgs &a, long z, float m, fl
   }
 }
 
+template <bool PS>
 __global__ void __launch_bounds__(1024) k_fast_stat_rows(FastArgs a, FastGeom g, FFTPlan<float> plan,
                                                         const cplx<float> *__restrict__ twL, int rpb, int wantGrad) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -456,7 +460,8 @@ __global__ void __launch_bounds__(1024) k_fast_stat_rows(FastArgs a, FastGeom g,
   cplx<float> *bufB = bufA + rpb * ls;
   __shared__ float red[2][32];
   __shared__ float psAcc[4 * kMaxPsFast];
-  for (int i = threadIdx.x; i < 4 * a.nPs; i += blockDim.x) psAcc[i] = 0.f;
+  if constexpr (PS)
+    for (int i = threadIdx.x; i < 4 * a.nPs; i += blockDim.x) psAcc[i] = 0.f;
   const int row0 = blockIdx.x * rpb;
   const int nl = min(rpb, g.nDataRows - row0);
   cplx<float> *spec = reinterpret_cast<cplx<float> *>(a.spec) + (long)b * g.specBatch;
@@ -503,16 +508,19 @@ __global__ void __launch_bounds__(1024) k_fast_stat_rows(FastArgs a, FastGeom g,
             m = a.regModel[ri];
           }
         }
-        if (a.nPs && !inReg) m += ps_main(a, b, row, col, 0.f, nullptr);
+        if constexpr (PS)
+          if (!inReg) m += ps_main(a, b, row, col, 0.f, nullptr);
         if (a.modelOut) a.modelOut[(long)b * g.nDataRows * g.nDataCols + zi] = m;
         float gz;
         stat_term(a, zi, m, S, gz);
         SG += gz * (inReg ? a.psfSumOs : a.psfSum);
-        if (wantGrad && a.nPs && gz != 0.f) {
-          if (inReg)
-            ps_region(a, g.rScale, b, row, col, gz * (1.f / (float)(g.rScale * g.rScale)), psAcc);
-          else
-            ps_main(a, b, row, col, gz, psAcc);
+        if constexpr (PS) {
+          if (wantGrad && gz != 0.f) {
+            if (inReg)
+              ps_region(a, g.rScale, b, row, col, gz * (1.f / (float)(g.rScale * g.rScale)), psAcc);
+            else
+              ps_main(a, b, row, col, gz, psAcc);
+          }
         }
         if (inReg) {
           if (wantGrad) a.regG[ri] = gz;
@@ -553,10 +561,12 @@ __global__ void __launch_bounds__(1024) k_fast_stat_rows(FastArgs a, FastGeom g,
       p[a.partStride] = v1;
     }
   }
-  if (wantGrad && a.nPs) {
-    __syncthreads();
-    for (int i = threadIdx.x; i < 4 * a.nPs; i += blockDim.x)
-      a.psPart[((long)b * 4 * a.nPs + i) * a.partStride + blockIdx.x] = psAcc[i];
+  if constexpr (PS) {
+    if (wantGrad) {
+      __syncthreads();
+      for (int i = threadIdx.x; i < 4 * a.nPs; i += blockDim.x)
+        a.psPart[((long)b * 4 * a.nPs + i) * a.partStride + blockIdx.x] = psAcc[i];
+    }
   }
 }
 
@@ -995,6 +1005,7 @@ __device__ __forceinline__ void deviate_slope(const FastArgs &a, long z, float m
 // parameters from sum(PSF)), then the row's partial sums of
 //   alpha_jk = sum c u_j u_k (j <= k),  beta_j = sum c u_j dev,  S = sum c dev^2
 // (c = bootstrap multiplicity) in FP32, one partial per quantity per CTA.
+template <bool PS>
 __global__ void __launch_bounds__(1024) k_fast_jtwj_rows(FastArgs a, FastGeom g, FFTPlan<float> plan,
                                                         const cplx<float> *__restrict__ twL,
                                                         const cplx<float> *__restrict__ dspec,
@@ -1044,7 +1055,7 @@ __global__ void __launch_bounds__(1024) k_fast_jtwj_rows(FastArgs a, FastGeom g,
     const long rStride = (long)g.rRows * g.rCols;
     for (int j = 0; j < nD; j++)
       U[(long)j * nc + col] = q * (inReg ? regDeriv[((long)b * nD + j) * rStride + ri] : Zr[2 * j * ls + col]);
-    for (int ps = 0; ps < a.nPs; ps++) {  // point sources: derivatives after the convolution
+    for (int ps = 0; PS && ps < a.nPs; ps++) {  // point sources: derivatives after the convolution
       const CompF32 &c = a.comps[b * a.nComp + a.psComp[ps]];
       const CompDesc &d = a.desc[a.psComp[ps]];
       float dsum[4] = {0.f, 0.f, 0.f, 0.f};
@@ -1310,8 +1321,9 @@ static cudaError_t launch_region_down(const FastPlan &p, const FastArgs &a, int 
   const FastGeom &g = p.g;
   const int M = p.Rx->half.n;
   const size_t sm = sizeof(cplx<float>) * 3 * g.rScale * (M + 1);
-  ensure_smem(k_fast_region_down, sm);
-  k_fast_region_down<<<dim3(g.rRows, nBatch), line_threads(M * g.rScale / 2), sm, st>>>(
+  auto kern = a.nPs ? k_fast_region_down<true> : k_fast_region_down<false>;
+  ensure_smem(kern, sm);
+  kern<<<dim3(g.rRows, nBatch), line_threads(M * g.rScale / 2), sm, st>>>(
       a, g, reinterpret_cast<const cplx<float> *>(a.rspec), plan32(*p.Rx, true),
       reinterpret_cast<const cplx<float> *>(p.Rx->twL32), a.regModel, 1);
   return cudaGetLastError();
@@ -1322,9 +1334,10 @@ static cudaError_t launch_stat(const FastPlan &p, const FastArgs &a, int nBatch,
   const int M = p.Lx->half.n;
   const int rpb = p.tune.rowRpb;
   const size_t sm = sizeof(cplx<float>) * 3 * rpb * (M + 1);
-  ensure_smem(k_fast_stat_rows, sm);
+  auto kern = a.nPs ? k_fast_stat_rows<true> : k_fast_stat_rows<false>;
+  ensure_smem(kern, sm);
   dim3 grid((g.nDataRows + rpb - 1) / rpb, nBatch);
-  k_fast_stat_rows<<<grid, p.tune.rowThreads, sm, st>>>(a, g, plan32(*p.Lx, true),
+  kern<<<grid, p.tune.rowThreads, sm, st>>>(a, g, plan32(*p.Lx, true),
                                           reinterpret_cast<const cplx<float> *>(p.Lx->twL32), rpb, wantGrad ? 1 : 0);
   return cudaGetLastError();
 }
@@ -1480,7 +1493,7 @@ cudaError_t fast_jtwj(const FastPlan &p, const FastArgs &a, const JtwjArgs &J, i
       const int M = p.Rx->half.n;
       const size_t sm = sizeof(cplx<float>) * 3 * g.rScale * (M + 1);
       stage_begin(p, "jtwj_region_down", st);
-      k_fast_region_down<<<dim3(g.rRows, nB), line_threads(M * g.rScale / 2), sm, st>>>(
+      k_fast_region_down<false><<<dim3(g.rRows, nB), line_threads(M * g.rScale / 2), sm, st>>>(
           a, g, reinterpret_cast<const cplx<float> *>(J.drspec), plan32(*p.Rx, true),
           reinterpret_cast<const cplx<float> *>(p.Rx->twL32), J.regDeriv, 0);
       if ((e = cudaGetLastError())) return e;
@@ -1495,7 +1508,8 @@ cudaError_t fast_jtwj(const FastPlan &p, const FastArgs &a, const JtwjArgs &J, i
   const int M = p.Lx->half.n;
   const size_t sm = jtwj_rows_smem(M, nD, g.nDataCols, kJtwjThreads);
   stage_begin(p, "jtwj_rows", st);
-  k_fast_jtwj_rows<<<dim3(g.nDataRows, nBatch), kJtwjThreads, sm, st>>>(
+  auto jrows = a.nPs ? k_fast_jtwj_rows<true> : k_fast_jtwj_rows<false>;
+  jrows<<<dim3(g.nDataRows, nBatch), kJtwjThreads, sm, st>>>(
       a, g, plan32(*p.Lx, true), reinterpret_cast<const cplx<float> *>(p.Lx->twL32),
       reinterpret_cast<const cplx<float> *>(J.dspec), J.regDeriv, J.slot, nD, J.part, J.jac);
   if ((e = cudaGetLastError())) return e;
@@ -1511,11 +1525,14 @@ cudaError_t fast_jtwj(const FastPlan &p, const FastArgs &a, const JtwjArgs &J, i
 void fast_prepare_kernels() {
   allow_max_smem((const void *)k_fast_eval_r2c);
   allow_max_smem((const void *)k_fast_grad_rows);
-  allow_max_smem((const void *)k_fast_stat_rows);
-  allow_max_smem((const void *)k_fast_region_down);
+  allow_max_smem((const void *)k_fast_stat_rows<false>);
+  allow_max_smem((const void *)k_fast_stat_rows<true>);
+  allow_max_smem((const void *)k_fast_region_down<false>);
+  allow_max_smem((const void *)k_fast_region_down<true>);
   allow_max_smem((const void *)k_fast_region_g_r2c);
   allow_max_smem((const void *)k_fast_deriv_r2c);
-  allow_max_smem((const void *)k_fast_jtwj_rows);
+  allow_max_smem((const void *)k_fast_jtwj_rows<false>);
+  allow_max_smem((const void *)k_fast_jtwj_rows<true>);
 }
 
 }  // namespace imfit
