@@ -58,14 +58,20 @@ def parse():
     return ap.parse_args()
 
 
-def measured_traffic(config, stage):
-    """DRAM bytes per launch of a stage from the committed ncu summary (or None)."""
+def measured_profile(config, stage):
+    """ncu figures of a stage from the committed summary: DRAM bytes per launch
+    and SM / issue utilisation (or None)."""
     try:
         with open(os.path.join(ROOT, "profiles", "traffic_per_launch.json")) as f:
-            v = json.load(f).get(config, {}).get(stage)
-        return float(v) if v is not None else None
+            return json.load(f).get(config, {}).get(stage)
     except (OSError, ValueError):
         return None
+
+
+def measured_traffic(config, stage):
+    """DRAM bytes per launch of a stage from the committed ncu summary (or None)."""
+    v = measured_profile(config, stage)
+    return float(v["dram_bytes"]) if v else None
 
 
 def max_over_ranks(value, world):
@@ -223,6 +229,11 @@ def algorithmic_bytes(model, wl):
         "stat_rows": 2 * N[0] * pitch * c8 + N[0] * N[1] * 8,
         "cols_adjoint": (N[0] + Ly + W[0]) * pitch * c8,
         "grad_rows": W[0] * pitch * c8,
+        # 3-D line of sight: per window pixel the value and its r~ slope out (eval),
+        # r~ in and one partial per CTA out (grad); the kept subinterval lists are
+        # scratch whose size depends on the integrands
+        "los_eval": W[0] * W[1] * 8,
+        "los_grad": W[0] * W[1] * 4,
     }
     if wl.regions:
         psf, k, (x1, x2, y1, y2) = wl.regions[0]
@@ -382,6 +393,10 @@ def run_gpu(args, rank, local_rank, world):
             "frac": round(achieved / hbm_peak, 4), "peak_source": peak_src,
             "algorithmic_bytes_per_launch": B * ab.get(dom, 0), "kernel_ms_in_timed_region": round(dom_avg, 5),
             "traffic": measured_traffic(args.config, dom)}
+    prof = measured_profile(args.config, dom)
+    if prof:  # the same kernel's compute-side utilisation (ncu, committed summary)
+        roof["ncu_sm_pct"] = prof.get("sm_pct")
+        roof["ncu_issue_active_pct"] = prof.get("issue_pct")
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
