@@ -3,6 +3,7 @@
     python -m imfit_gb300.cli CONFIG IMAGE [--psf F] [--mask F] [--noise F] ...
     python -m imfit_gb300.cli makeimage CONFIG [--ncols N --nrows M | --refimage F] ...
     python -m imfit_gb300.cli mcmc CONFIG IMAGE [--nchains N] [--max-chain-length N] ...
+    python -m imfit_gb300.cli multimfit CONFIG --image-info FILE [--nm | --de] ...
 
 Reads an Imfit configuration file and FITS images and sets the model up in
 the reference's order (core/setup_model_object.cpp:36-157).  The fitting
@@ -397,12 +398,77 @@ def mcmc(argv=None, out=sys.stdout):
     return r
 
 
+def build_multimfit_parser():
+    ap = argparse.ArgumentParser(prog="imfit_gb300.cli multimfit",
+                                 description="simultaneous fit of several images (multimfit)")
+    ap.add_argument("config")
+    ap.add_argument("-i", "--image-info", required=True)
+    ap.add_argument("--nosubsampling", "--no-subsampling", dest="nosubsampling", action="store_true")
+    ap.add_argument("--cashstat", action="store_true")
+    ap.add_argument("--poisson-mlr", "--mlr", dest="poisson_mlr", action="store_true")
+    ap.add_argument("--model-errors", action="store_true")
+    ap.add_argument("--fitstat-only", action="store_true")
+    ap.add_argument("--nm", action="store_true")
+    ap.add_argument("--de", action="store_true")
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--ftol", type=float, default=1e-8)
+    ap.add_argument("--max-iter", type=int, default=0)
+    ap.add_argument("--device", type=int, default=0)
+    return ap
+
+
+def multimfit(argv=None, out=sys.stdout):
+    """The multimfit command (core/multimfit_main.cpp): the configuration file
+    gives the model, the image-info file the images and their description
+    parameters; returns (fitted global parameters, statistic)."""
+    from .multimage import IMAGE_PARAM_NAMES, MultiImageModel, build_handles, global_vector, parse_image_info
+    args = build_multimfit_parser().parse_args(argv)
+    try:
+        cfg = read_config(args.config)
+    except ConfigError as e:
+        raise SystemExit(f"error in {args.config}: {e}")
+    with open(args.image_info) as f:
+        images = parse_image_info(f.read())
+    stat = "cash" if args.cashstat else ("pmlr" if args.poisson_mlr else "chi2")
+    handles = build_handles(cfg.functions, images, args.device, not args.nosubsampling, stat, args.model_errors)
+    mm = MultiImageModel(cfg.functions, handles)
+    p0, lo, hi, fx = global_vector(cfg, images)
+    if args.fitstat_only:
+        s = mm.get_fit_statistic(p0)
+        out.write(f"fit statistic = {s:.6f}\n")
+        return p0, s
+    if args.de:
+        from .solvers import differential_evolution
+        r = differential_evolution(mm, p0, lo, hi, fixed=fx.astype(bool), ftol=args.ftol, seed=args.seed)
+    elif args.nm:
+        from .solvers import nelder_mead
+        r = nelder_mead(mm, p0, np.where(np.isnan(lo), -np.inf, lo), np.where(np.isnan(hi), np.inf, hi),
+                        fixed=fx.astype(bool), ftol=args.ftol)
+    else:
+        if args.cashstat:
+            raise SystemExit("the Cash statistic has no deviates: use --nm or --de")
+        r = mm.fit_lm(p0, fixed=fx, lower=np.where(np.isnan(lo), 0.0, lo), upper=np.where(np.isnan(hi), 0.0, hi),
+                      ftol=args.ftol, max_iter=args.max_iter)
+    p = r["params"]
+    s = mm.get_fit_statistic(p)
+    out.write(f"fit statistic = {s:.6f}\n# Main model parameters (reference image)\n")
+    for name, v in zip(cfg.param_names, p[mm.n_image_params:]):
+        out.write(f"  {name:8s} {v:.6f}\n")
+    for i in range(1, mm.n_images):
+        out.write(f"# Image-description parameters for image {i + 1}\n")
+        for j, name in enumerate(IMAGE_PARAM_NAMES):
+            out.write(f"  {name:12s} {p[5 * (i - 1) + j]:.6f}\n")
+    return p, s
+
+
 def main(argv=None):
     argv = sys.argv[1:] if argv is None else argv
     if argv and argv[0] == "makeimage":
         makeimage(argv[1:])
     elif argv and argv[0] == "mcmc":
         mcmc(argv[1:])
+    elif argv and argv[0] == "multimfit":
+        multimfit(argv[1:])
     else:
         run(argv)
 

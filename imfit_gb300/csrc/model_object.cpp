@@ -2256,6 +2256,31 @@ int imfit_FitLM(imfit_model_t m, double *params, const int *fixed, const double 
   return st < 0 ? st : 0;
 }
 
+int imfit_MinimizeNormalEquations(int n, double *params, const int *fixed, const double *lower, const double *upper,
+                                  double ftol, int maxIter, imfit_normal_eq_fn eval, void *user, double *stat,
+                                  int *nIter, int *nEval, int *status) {
+  if (n < 1 || !params || !eval) {
+    imfit::set_global_error("MinimizeNormalEquations: bad arguments");
+    return IMFIT_E_ARG;
+  }
+  if (!(ftol > 0.0)) {
+    imfit::set_global_error("MinimizeNormalEquations: ftol must be positive");
+    return IMFIT_E_ARG;
+  }
+  LMSettings set;
+  set.ftol = ftol;
+  if (maxIter > 0) set.maxIter = maxIter;
+  LMResult res;
+  JtwjEval ev = [eval, user](const double *x, double *S, double *A, double *b) { return eval(x, S, A, b, user); };
+  int st = lm_minimize(n, params, fixed, lower, upper, set, ev, res);
+  if (stat) *stat = res.stat;
+  if (nIter) *nIter = res.nIter;
+  if (nEval) *nEval = res.nEval;
+  if (status) *status = res.status;
+  if (st < 0) imfit::set_global_error("MinimizeNormalEquations: the evaluator failed");
+  return st < 0 ? st : 0;
+}
+
 int imfit_BootstrapFitBatch(imfit_model_t m, int nSamples, const double *bestfit, const int *fixed,
                             const double *lower, const double *upper, double ftol, int maxIter, double *params,
                             double *statistics, int *nIter, int *status) {

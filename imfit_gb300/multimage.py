@@ -1,0 +1,330 @@
+"""Simultaneous fits of several images of one object (multimfit).
+
+MultiImageModel restates ModelObjectMultImage (core/model_object_multimage.cpp,
+core/param_holder.cpp, core/paramvector_processing.cpp) on top of one GPU
+ModelObject per image.  The global parameter vector is
+
+    [PIXEL_SCALE, IMAGE_PA, FLUX_SCALE, X0, Y0] of images 2..N,
+    followed by the model's parameters as the reference image sees them.
+
+Image i > 0 gets the model with the first function set centred at its own
+(X0, Y0), every later set's centre moved by the set's offset from the first,
+rotated by IMAGE_PA and scaled by PIXEL_SCALE (CalculateOffset_X0Y0,
+paramvector_processing.cpp:80-104), and each function's position angle,
+intensity and size parameters turned into that image's by PA - IMAGE_PA,
+FLUX_SCALE * I and size / PIXEL_SCALE (the Setup of every function class with
+SetImageParameters, function_object.cpp:105-110).  The statistic is the sum of
+the images' statistics, the deviates their concatenation.  Gradients and normal
+equations chain each image's (fast path) with T_i = d(image parameters) /
+d(global parameters); the LM driver is the library's own
+(imfit_MinimizeNormalEquations).  Per-image (non-global) functions are not
+supported.
+"""
+import ctypes
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import ModelObject, load_library
+
+N_IMAGE_PARAMS = 5
+IMAGE_PARAM_NAMES = ["PIXEL_SCALE", "IMAGE_PA", "FLUX_SCALE", "X0", "Y0"]
+
+# per function: index of PA (or None), intensity indices, size indices
+# (each class's Setup, e.g. func_sersic.cpp:109-117, func_exp.cpp, func_flatsky.cpp ...)
+ADJUST = {
+    "Sersic": (0, [3], [4]),
+    "Exponential": (0, [2], [3]),
+    "FlatSky": (None, [0], []),
+    "GaussianRing": (0, [2], [3, 4]),
+    "Moffat": (0, [2], [3]),
+    "Gaussian": (0, [2], [3]),
+    "ExponentialDisk3D": (0, [2], [3, 5]),
+    "FerrersBar3D": (0, [3], [4]),
+    "PointSource": (None, [0], []),
+    "PointSourceRot": (0, [1], []),
+}
+
+
+@dataclass
+class ImageInfo:
+    """One IMAGE_START block of an image-info file
+    (core/imageparams_file_parser.cpp:51-78)."""
+    data: str = None
+    error: str = None
+    mask: str = None
+    psf: str = None
+    options: dict = field(default_factory=dict)        # GAIN, READNOISE, ...
+    flags: set = field(default_factory=set)            # ERRORS_ARE_*, MASK_ZERO_IS_BAD
+    params: dict = field(default_factory=dict)         # PIXEL_SCALE ... Y0 -> (value, lo, hi, fixed)
+
+
+def parse_image_info(text):
+    """Blocks opened by IMAGE_START: file names (DATA, ERROR, MASK, PSF),
+    image characteristics, flags, and the image-description parameters with
+    optional limits or 'fixed' (same grammar as configuration files)."""
+    images = []
+    for k, raw in enumerate(text.splitlines(), 1):
+        line = raw.split("#", 1)[0].strip()
+        if not line:
+            continue
+        parts = line.split()
+        key = parts[0]
+        if key == "IMAGE_START":
+            images.append(ImageInfo())
+            continue
+        if not images:
+            raise ValueError(f"line {k}: {key} before the first IMAGE_START")
+        im = images[-1]
+        if key in ("DATA", "ERROR", "MASK", "PSF"):
+            setattr(im, key.lower(), parts[1])
+        elif key in ("ERRORS_ARE_SIGMAS", "ERRORS_ARE_VARIANCES", "ERRORS_ARE_WEIGHTS", "MASK_ZERO_IS_GOOD",
+                     "MASK_ZERO_IS_BAD"):
+            im.flags.add(key)
+        elif key in IMAGE_PARAM_NAMES:
+            v = float(parts[1])
+            lo = hi = np.nan
+            fixed = False
+            if len(parts) > 2:
+                if parts[2].lower() == "fixed":
+                    fixed = True
+                else:
+                    lo, hi = (float(x) for x in parts[2].split(","))
+            im.params[key] = (v, lo, hi, fixed)
+        else:
+            im.options[key] = parts[1]
+    if not images:
+        raise ValueError("no IMAGE_START lines found")
+    return images
+
+
+class MultiImageModel:
+    """ModelObject-like view of several images fitted with one model.
+
+    functions: [(name, starts_new_set)] as for ModelObject.add_function;
+    handles: one configured ModelObject per image (functions added, images,
+    PSF, errors, mask and statistic set, final_setup done), the reference
+    image first."""
+
+    def __init__(self, functions, handles):
+        self.functions = list(functions)
+        self.handles = list(handles)
+        self.n_images = len(self.handles)
+        self.n_image_params = N_IMAGE_PARAMS * (self.n_images - 1)
+        self.n_model = self.handles[0].n_params
+        self.n_params = self.n_image_params + self.n_model
+        for name, _ in self.functions:
+            if name not in ADJUST:
+                raise ValueError(f"function {name} has no image adjustment rule")
+        # parameter layout of the model vector
+        self._set_x0 = []
+        self._blocks = []
+        off = 0
+        for k, (name, new_set) in enumerate(self.functions):
+            if new_set or k == 0:
+                self._set_x0.append(off)
+                off += 2
+            npar = self._nparams(name)
+            self._blocks.append((name, off))
+            off += npar
+        if off != self.n_model:
+            raise ValueError("function list does not match the handles' parameter count")
+
+    @staticmethod
+    def _nparams(name):
+        from .config import _NPARAMS
+        return _NPARAMS[name]
+
+    # ---------------------------------------------------- parameter transform
+    def image_vector(self, params, i):
+        """Parameters of image i (ParamHolder::AssembleParametersForImage,
+        core/param_holder.cpp:215-270, then each function's Setup scaling)."""
+        p = np.asarray(params, dtype=float)
+        model = p[self.n_image_params:self.n_image_params + self.n_model].copy()
+        if i == 0:
+            ps, rot, fs = 1.0, 0.0, 1.0
+        else:
+            ps, rot, fs, x0i, y0i = p[N_IMAGE_PARAMS * (i - 1):N_IMAGE_PARAMS * i]
+            x0r, y0r = model[0], model[1]
+            model[0], model[1] = x0i, y0i
+            if ps <= 0:
+                raise ValueError("zero or negative PIXEL_SCALE")
+            t = np.deg2rad(rot)  # DEG2RAD * rotation (paramvector_processing.cpp:89)
+            c, s = np.cos(t), np.sin(t)
+            for k in self._set_x0[1:]:
+                dx, dy = model[k] - x0r, model[k + 1] - y0r
+                model[k] = x0i + ps * (dx * c + dy * s)
+                model[k + 1] = y0i + ps * (-dx * s + dy * c)
+        scaling = 1.0 / ps  # FunctionObject::SetImageParameters: pixelScaling = 1 / pixScale
+        for name, off in self._blocks:
+            pa, inten, size = ADJUST[name]
+            if pa is not None:
+                model[off + pa] = model[off + pa] - rot
+            for j in inten:
+                model[off + j] = model[off + j] * fs
+            for j in size:
+                model[off + j] = model[off + j] * scaling
+        return model
+
+    def transform_jacobian(self, params, i):
+        """T_i = d image_vector(params, i) / d params (central differences on
+        the parameter transform, which is smooth)."""
+        p = np.asarray(params, dtype=float)
+        T = np.zeros((self.n_model, self.n_params))
+        for j in range(self.n_params):
+            h = 1e-6 * max(1.0, abs(p[j]))
+            a, b = p.copy(), p.copy()
+            a[j] += h
+            b[j] -= h
+            T[:, j] = (self.image_vector(a, i) - self.image_vector(b, i)) / (2 * h)
+        return T
+
+    # ---------------------------------------------------- ModelObject surface
+    def get_fit_statistic(self, params):
+        """ModelObjectMultImage::GetFitStatistic (model_object_multimage.cpp:359-405):
+        the sum over images, FP64 plain path."""
+        return float(sum(m.get_fit_statistic(self.image_vector(params, i)) for i, m in enumerate(self.handles)))
+
+    def compute_deviates(self, params):
+        return np.concatenate([m.compute_deviates(self.image_vector(params, i)) for i, m in enumerate(self.handles)])
+
+    def statistic_and_gradient(self, params):
+        S, g = 0.0, np.zeros(self.n_params)
+        for i, m in enumerate(self.handles):
+            s_i, g_i = m.statistic_and_gradient(self.image_vector(params, i))
+            S += s_i
+            g += self.transform_jacobian(params, i).T @ g_i
+        return S, g
+
+    def batch_statistic_and_gradient(self, P, want_grad=True):
+        P = np.atleast_2d(np.asarray(P, dtype=float))
+        B = P.shape[0]
+        S = np.zeros(B)
+        G = np.zeros((B, self.n_params)) if want_grad else None
+        for i, m in enumerate(self.handles):
+            Pi = np.array([self.image_vector(P[b], i) for b in range(B)])
+            r = m.batch_statistic_and_gradient(Pi, want_grad=want_grad)
+            if want_grad:
+                s_i, g_i = r
+                for b in range(B):
+                    G[b] += self.transform_jacobian(P[b], i).T @ g_i[b]
+            else:
+                s_i = r
+            S += s_i
+        return (S, G) if want_grad else S
+
+    def jtwj(self, params):
+        """S, A = sum T_i^T A_i T_i, b = sum T_i^T b_i."""
+        S, A, b = 0.0, np.zeros((self.n_params, self.n_params)), np.zeros(self.n_params)
+        for i, m in enumerate(self.handles):
+            s_i, A_i, b_i = m.jtwj(self.image_vector(params, i))
+            T = self.transform_jacobian(params, i)
+            S += s_i
+            A += T.T @ A_i @ T
+            b += T.T @ b_i
+        return S, A, b
+
+    def fit_lm(self, params, fixed=None, lower=None, upper=None, ftol=1e-8, max_iter=0):
+        """Levenberg-Marquardt on the summed normal equations with the library's
+        driver (the same one imfit_FitLM runs)."""
+        lib = load_library()
+        n = self.n_params
+        x = np.array(params, dtype=float)
+        fx = (ctypes.c_int * n)(*([0] * n if fixed is None else [int(v) for v in fixed]))
+        fx = ctypes.cast(fx, ctypes.POINTER(ctypes.c_int))
+        lo = np.ascontiguousarray(lower, dtype=float) if lower is not None else None
+        hi = np.ascontiguousarray(upper, dtype=float) if upper is not None else None
+        DP = ctypes.POINTER(ctypes.c_double)
+        errors = []
+
+        @_NORMAL_EQ
+        def cb(xp, sp, ap, bp, user):
+            try:
+                xv = np.ctypeslib.as_array(xp, shape=(n,)).copy()
+                s, A, b = self.jtwj(xv)
+                sp[0] = s
+                np.ctypeslib.as_array(ap, shape=(n * n,))[:] = A.ravel()
+                np.ctypeslib.as_array(bp, shape=(n,))[:] = b
+                return 0
+            except Exception as e:  # reported after the driver returns
+                errors.append(e)
+                return -1
+
+        fn = lib.imfit_MinimizeNormalEquations
+        IP = ctypes.POINTER(ctypes.c_int)
+        fn.restype = ctypes.c_int
+        fn.argtypes = [ctypes.c_int, DP, IP, DP, DP, ctypes.c_double, ctypes.c_int, _NORMAL_EQ, ctypes.c_void_p, DP,
+                       IP, IP, IP]
+        stat = ctypes.c_double()
+        it, nev, st = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        rc = fn(n, x.ctypes.data_as(DP), fx,
+                                               lo.ctypes.data_as(DP) if lo is not None else None,
+                                               hi.ctypes.data_as(DP) if hi is not None else None, ftol,
+                                               int(max_iter), cb, None, ctypes.byref(stat), ctypes.byref(it),
+                                               ctypes.byref(nev), ctypes.byref(st))
+        if errors:
+            raise errors[0]
+        if rc != 0:
+            raise RuntimeError(lib.imfit_LastError(None).decode())
+        return dict(params=x, statistic=stat.value, niter=it.value, nev=nev.value, status=st.value)
+
+
+_NORMAL_EQ = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                              ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), ctypes.c_void_p)
+
+
+def build_handles(functions, images, device=0, subsampling=True, statistic="chi2", model_errors=False,
+                  read_image=None):
+    """One configured ModelObject per ImageInfo (multimfit_main.cpp's setup
+    of each image: PSF, data, characteristics, errors, mask, statistic)."""
+    from . import fits
+    read_image = read_image or (lambda path: fits.read_image(path)[0])
+    handles = []
+    for im in images:
+        m = ModelObject(device)
+        for name, new_set in functions:
+            m.add_function(name, new_set, subsampling=subsampling)
+        m.finish_functions()
+        if im.psf:
+            m.add_psf(read_image(im.psf))
+        m.add_image_data(read_image(im.data))
+        o = im.options
+        m.add_image_characteristics(float(o.get("GAIN", 1.0)), float(o.get("READNOISE", 0.0)),
+                                    float(o.get("EXPTIME", 1.0)), int(float(o.get("NCOMBINED", 1))),
+                                    float(o.get("ORIGINAL_SKY", 0.0)))
+        if im.error:
+            kind = 110 if "ERRORS_ARE_VARIANCES" in im.flags else (120 if "ERRORS_ARE_WEIGHTS" in im.flags else 100)
+            m.add_error_vector(read_image(im.error), kind)
+        if im.mask:
+            m.add_mask_vector(read_image(im.mask), 20 if "MASK_ZERO_IS_BAD" in im.flags else 10)
+        if statistic == "cash":
+            m.use_cash()
+        elif statistic == "pmlr":
+            m.use_pmlr()
+        if model_errors:
+            m.use_model_errors()
+        if m.final_setup() != 0:
+            raise RuntimeError("FinalSetupForFitting failed for " + str(im.data))
+        handles.append(m)
+    return handles
+
+
+def global_vector(cfg, images):
+    """(values, lower, upper, fixed) of the global vector: the image-description
+    parameters of images 2..N (defaults 1, 0, 1 and the reference model's X0,
+    Y0), then the configuration's parameters."""
+    vals, lo, hi, fx = [], [], [], []
+    defaults = {"PIXEL_SCALE": 1.0, "IMAGE_PA": 0.0, "FLUX_SCALE": 1.0, "X0": cfg.values[0], "Y0": cfg.values[1]}
+    for im in images[1:]:
+        for name in IMAGE_PARAM_NAMES:
+            v, l, h, f = im.params.get(name, (defaults[name], np.nan, np.nan, name in ("PIXEL_SCALE", "IMAGE_PA",
+                                                                                     "FLUX_SCALE")))
+            vals.append(v)
+            lo.append(l)
+            hi.append(h)
+            fx.append(int(f))
+    vals += list(cfg.values)
+    lo += list(cfg.lower)
+    hi += list(cfg.upper)
+    fx += list(cfg.fixed)
+    return np.array(vals), np.array(lo), np.array(hi), np.array(fx, dtype=int)

@@ -226,6 +226,18 @@ int imfit_FitLM(imfit_model_t m, double *params, const int *fixed, const double 
  * (nBatch each) may be NULL; status codes as imfit_FitLM. */
 int imfit_FitLMBatch(imfit_model_t m, int nBatch, double *params, const int *fixed, const double *lower,
                      const double *upper, double ftol, int maxIter, double *statistics, int *nIter, int *status);
+/* The Levenberg-Marquardt driver of imfit_FitLM on normal equations the
+ * caller supplies: eval(x, &S, A, b, user) fills the statistic S, A = J^T J
+ * (n x n, row-major) and b = J^T dev of its deviates at x and returns 0 (or a
+ * negative code, which stops the fit).  For models assembled on the host from
+ * several handles -- multimfit's ModelObjectMultImage
+ * (core/model_object_multimage.cpp:319-441): S = sum S_i, A = sum T_i^T A_i T_i,
+ * b = sum T_i^T b_i with T_i the Jacobian of image i's parameter vector.
+ * Errors: imfit_LastError(NULL). */
+typedef int (*imfit_normal_eq_fn)(const double *x, double *statistic, double *A, double *b, void *user);
+int imfit_MinimizeNormalEquations(int n, double *params, const int *fixed, const double *lower, const double *upper,
+                                  double ftol, int maxIter, imfit_normal_eq_fn eval, void *user, double *statistic,
+                                  int *nIter, int *nEval, int *status);
 /* Bootstrap refits, replacing the loop of BootstrapErrorsBase
  * (core/bootstrap_errors.cpp:160-240: MakeBootstrapSample, then LevMarFit from
  * the best-fit vector, per iteration): draws the next nSamples samples of the

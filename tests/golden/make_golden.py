@@ -2,7 +2,7 @@
 
 Run in a checkout that has the reference at /root/reference (or
 IMFIT_REFERENCE_DIR):  python tests/golden/make_golden.py [part ...]
-(parts: n3073 makeimage ic3478 pointsource mcmc small_case; all by default)
+(parts: n3073 makeimage ic3478 pointsource mcmc multimfit small_case; all by default)
 
 Outputs (all small .npz files next to this script):
   n3073.npz          the reference regression inputs tests/n3073rss_small.fits,
@@ -30,6 +30,11 @@ Outputs (all small .npz files next to this script):
                      do_mcmc_tests:27): post-burn-in means, standard deviations
                      and 16/50/84 % quantiles per parameter, the number of
                      rows and the burn-in rows.
+  multimfit.npz      tests/multimfit_reference/smallgauss_5x5_{0,1,sigma}.fits and
+                     smallDataImage1{a,b}.fits with the printed results of
+                     multimfit_textout3a (Nelder-Mead fit of
+                     config_imfit_smallgauss.dat + imageinfo_multimfit3.txt) and
+                     multimfit_textout1a (--fitstat-only, imageinfo_multimfit0.txt).
   small_case.npz     the reference's own outputs (oracle/_ref) for
                      imfit_gb300.workloads.small_case: model images, deviates and
                      statistics for chi^2 / Cash / PMLR.
@@ -149,6 +154,19 @@ def mcmc():
         ref_q=np.percentile(post, [16, 50, 84], axis=0), ref_best_loglik=rows[:, 6].max())
 
 
+def multimfit():
+    t = os.path.join(REF, "tests", "multimfit_reference")
+    r = lambda n: fits.read_image(os.path.join(t, n))[0].astype(np.float32)
+    np.savez_compressed(
+        os.path.join(HERE, "multimfit.npz"), g0=r("smallgauss_5x5_0.fits"), g1=r("smallgauss_5x5_1.fits"),
+        gsig=r("smallgauss_5x5_sigma.fits"), d1a=r("smallDataImage1a.fits"), d1b=r("smallDataImage1b.fits"),
+        # multimfit_textout3a: CHI-SQUARE and the printed parameters (X0 Y0 PA ell I_0 sigma; image 2 X0 Y0)
+        g_chi2_printed=36.070608, g_model_printed=np.array([2.5072, 2.5387, 18.9357, 0.293283, 995.047, 0.992441]),
+        g_image2_printed=np.array([2.49082, 2.47557]),
+        # multimfit_textout1a: CHI-SQUARE at the starting parameters
+        d_chi2_printed=6.75)
+
+
 def small_case():
     out = {}
     for stat in ("chi2", "cash", "pmlr"):
@@ -168,7 +186,7 @@ if __name__ == "__main__":
         sys.exit(f"reference checkout not found at {REF}")
     oracle.build_reference()
     parts = {"n3073": n3073, "makeimage": makeimage, "ic3478": ic3478, "pointsource": pointsource,
-             "mcmc": mcmc, "small_case": small_case}
+             "mcmc": mcmc, "multimfit": multimfit, "small_case": small_case}
     for name in (sys.argv[1:] or parts):
         parts[name]()
     for f in sorted(os.listdir(HERE)):

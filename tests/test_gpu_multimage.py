@@ -1,0 +1,101 @@
+"""GPU tests of simultaneous multi-image fitting (multimfit) against the
+reference's regression printouts (tests/multimfit_reference)."""
+import io
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+SMALLGAUSS = """GAIN 1
+ORIGINAL_SKY 100
+
+X0 2 0,5
+Y0 2 0,5
+FUNCTION Gaussian
+PA 0 -50,50
+ell 0.1 0,0.6
+I_0 900 500,1500
+sigma 1.5 0.1,3
+"""
+
+
+def _write(tmp_path, d):
+    from imfit_gb300 import fits
+    for k in ("g0", "g1", "gsig", "d1a", "d1b"):
+        fits.write_image(str(tmp_path / f"{k}.fits"), d[k])
+    (tmp_path / "gauss.dat").write_text(SMALLGAUSS)
+    (tmp_path / "gauss_info.txt").write_text(f"""IMAGE_START
+DATA {tmp_path / 'g0.fits'}
+ERROR {tmp_path / 'gsig.fits'}
+ORIGINAL_SKY 100.0
+IMAGE_START
+DATA {tmp_path / 'g1.fits'}
+ERROR {tmp_path / 'gsig.fits'}
+ORIGINAL_SKY 100.0
+PIXEL_SCALE 1.0 fixed
+IMAGE_PA 0.0 fixed
+FLUX_SCALE 1.0 fixed
+X0 2
+Y0 2
+GAIN 1
+ORIGINAL_SKY 100
+""")
+    (tmp_path / "flat.dat").write_text("X0 1\nY0 1\nFUNCTION FlatSky\nI0 1.0\n")
+    (tmp_path / "flat_info.txt").write_text(f"""IMAGE_START
+DATA {tmp_path / 'd1a.fits'}
+ORIGINAL_SKY 0.0
+IMAGE_START
+DATA {tmp_path / 'd1b.fits'}
+ORIGINAL_SKY 0.0
+PIXEL_SCALE 1.0 fixed
+IMAGE_PA 0.0 fixed
+FLUX_SCALE 1.0 fixed
+X0 2 fixed
+Y0 2 fixed
+""")
+
+
+def test_multimfit_fitstat_only(gpu, tmp_path):
+    """multimfit_textout1a: --fitstat-only on two 2x2 images with a FlatSky
+    model: CHI-SQUARE = 6.750000 at the starting parameters."""
+    from imfit_gb300 import cli
+    d = np.load(os.path.join(GOLDEN, "multimfit.npz"))
+    _write(tmp_path, d)
+    p, s = cli.multimfit([str(tmp_path / "flat.dat"), "--image-info", str(tmp_path / "flat_info.txt"),
+                          "--fitstat-only"], out=io.StringIO())
+    assert p.size == 8 and abs(s - float(d["d_chi2_printed"])) < 1e-12
+
+
+def test_multimfit_smallgauss_fit(gpu, tmp_path):
+    """multimfit_textout3a (Nelder-Mead, CHI-SQUARE 36.070608): the summed
+    statistic at the printed parameters is the printed minimum (to the
+    rounding of the printed digits), the LM fit on the summed normal equations
+    reaches it and lands on the printed parameters; the fast path's summed
+    statistic and gradient agree with the FP64 statistic and its differences;
+    Nelder-Mead through the command line ends at the same minimum."""
+    from imfit_gb300 import cli
+    from imfit_gb300.config import read_config
+    from imfit_gb300.multimage import MultiImageModel, build_handles, global_vector, parse_image_info
+    d = np.load(os.path.join(GOLDEN, "multimfit.npz"))
+    _write(tmp_path, d)
+    cfg = read_config(str(tmp_path / "gauss.dat"))
+    images = parse_image_info((tmp_path / "gauss_info.txt").read_text())
+    mm = MultiImageModel(cfg.functions, build_handles(cfg.functions, images))
+    p0, lo, hi, fx = global_vector(cfg, images)
+    assert mm.n_params == 11 and int(np.sum(fx == 0)) == 8
+    printed = np.concatenate([[1.0, 0.0, 1.0], d["g_image2_printed"], d["g_model_printed"]])
+    s_printed = mm.get_fit_statistic(printed)
+    chi2 = float(d["g_chi2_printed"])
+    assert abs(s_printed - chi2) < 2e-3, s_printed
+    s, g = mm.statistic_and_gradient(printed)
+    assert abs(s - s_printed) <= 1e-5 * s_printed
+    r = mm.fit_lm(p0, fixed=fx, lower=np.where(np.isnan(lo), 0.0, lo), upper=np.where(np.isnan(hi), 0.0, hi))
+    s_fit = mm.get_fit_statistic(r["params"])
+    assert r["status"] > 0 and s_fit <= chi2 + 1e-4, s_fit
+    assert np.all(np.abs(r["params"] - printed) <= np.array([0, 0, 0, 2e-3, 2e-3, 2e-3, 2e-3, 0.05, 1e-3, 0.1, 1e-3]))
+    p_nm, s_nm = cli.multimfit([str(tmp_path / "gauss.dat"), "-i", str(tmp_path / "gauss_info.txt"), "--nm"],
+                               out=io.StringIO())
+    assert s_nm <= chi2 + 1e-3
