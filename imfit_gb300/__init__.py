@@ -27,6 +27,10 @@ _P = ctypes.c_void_p
 _DP = ctypes.POINTER(ctypes.c_double)
 
 # (name, restype, argtypes) of every C-ABI entry point
+# imfit_normal_eq_fn: (x, &statistic, A, b, user) -> status
+NORMAL_EQ_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                                ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), ctypes.c_void_p)
+
 _SIGS = [
     ("imfit_ModelObject_new", _I, [_I, ctypes.POINTER(_P)]),
     ("imfit_ModelObject_delete", _I, [_P]),
@@ -86,6 +90,8 @@ _SIGS = [
     ("imfit_BootstrapFitBatch", _I, [_P, _I, _DP, ctypes.POINTER(_I), _DP, _DP, _D, _I, _DP, _DP,
                                      ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     ("imfit_SetupImageStack", _I, [_P, _I, _I, _I, _DP, _DP, _DP, _I, _I]),
+    ("imfit_MinimizeNormalEquations", _I, [_I, _DP, ctypes.POINTER(_I), _DP, _DP, _D, _I, NORMAL_EQ_FN, _P, _DP,
+                                           ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     ("imfit_SetFunctionOptionalParam", _I, [_P, _I, ctypes.c_char_p, ctypes.c_char_p]),
     ("imfit_Synchronize", _I, [_P]),
     ("imfit_GetStream", _I, [_P, ctypes.POINTER(_P)]),

@@ -25,6 +25,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
+from . import NORMAL_EQ_FN as _NORMAL_EQ
 from . import ModelObject, load_library
 
 N_IMAGE_PARAMS = 5
@@ -251,10 +252,6 @@ class MultiImageModel:
                 return -1
 
         fn = lib.imfit_MinimizeNormalEquations
-        IP = ctypes.POINTER(ctypes.c_int)
-        fn.restype = ctypes.c_int
-        fn.argtypes = [ctypes.c_int, DP, IP, DP, DP, ctypes.c_double, ctypes.c_int, _NORMAL_EQ, ctypes.c_void_p, DP,
-                       IP, IP, IP]
         stat = ctypes.c_double()
         it, nev, st = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         rc = fn(n, x.ctypes.data_as(DP), fx,
@@ -269,8 +266,6 @@ class MultiImageModel:
         return dict(params=x, statistic=stat.value, niter=it.value, nev=nev.value, status=st.value)
 
 
-_NORMAL_EQ = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
-                              ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), ctypes.c_void_p)
 
 
 def build_handles(functions, images, device=0, subsampling=True, statistic="chi2", model_errors=False,
