@@ -8,7 +8,8 @@ import pytest
 from imfit_gb300 import config, fits
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-REF_CONFIG = "/root/reference/tests/imfit_reference/imfit_config_n3073.dat"
+REF_CONFIG = os.path.join(os.environ.get("IMFIT_REFERENCE_DIR", "/root/reference"), "tests", "imfit_reference",
+                          "imfit_config_n3073.dat")
 
 N3073_STYLE = """# comment line
 GAIN   4.725
