@@ -774,7 +774,8 @@ __global__ void __launch_bounds__(256) k_fast_los_eval(FastArgs a, WinDesc w, Lo
 // One warp per window pixel: r~ * d(line-of-sight value)/d(parameters) of
 // every 3-D component, per-warp rows in shared memory (no atomics), then one
 // FP32 partial per parameter for this CTA.
-__global__ void __launch_bounds__(256) k_fast_los_grad(FastArgs a, WinDesc w, float *__restrict__ gradPart,
+// four CTAs per SM (64 registers): the measured optimum for the gradient pass
+__global__ void __launch_bounds__(256, 4) k_fast_los_grad(FastArgs a, WinDesc w, float *__restrict__ gradPart,
                                                       int blockBase, LosStore ks) {
   __shared__ CompF32 sc[kMaxComponents];
   __shared__ float red[8][kMaxParams];
