@@ -288,7 +288,7 @@ def makeimage(argv=None, out=sys.stdout):
     were asked for) and the flux table (None when not asked for)."""
     args = build_makeimage_parser().parse_args(argv)
     try:
-        cfg = read_config(args.config)
+        cfg = read_config(args.config, check_limits=False)
     except ConfigError as e:
         raise SystemExit(f"error in {args.config}: {e}")
     fluxes_only = (args.print_fluxes or args.save_fluxes) and args.nosave
@@ -461,6 +461,52 @@ def multimfit(argv=None, out=sys.stdout):
     return p, s
 
 
+def makemultimages(argv=None, out=sys.stdout):
+    """The makemultimages command (core/makemultimages_main.cpp): the model of
+    the configuration file seen through each image of an image-info file
+    (NCOLS/NROWS, optional PSF, image-description parameters), saved as
+    OUTPUT_0.fits, OUTPUT_1.fits, ...; returns the images."""
+    from .multimage import MultiImageModel, global_vector, parse_image_info
+    ap = argparse.ArgumentParser(prog="imfit_gb300.cli makemultimages")
+    ap.add_argument("config")
+    ap.add_argument("-i", "--image-info", required=True)
+    ap.add_argument("-o", "--output", default="modelimage_multi")
+    ap.add_argument("--nosubsampling", "--no-subsampling", dest="nosubsampling", action="store_true")
+    ap.add_argument("--device", type=int, default=0)
+    args = ap.parse_args(argv)
+    try:
+        cfg = read_config(args.config, check_limits=False)
+    except ConfigError as e:
+        raise SystemExit(f"error in {args.config}: {e}")
+    with open(args.image_info) as f:
+        images = parse_image_info(f.read())
+    handles = []
+    for im in images:
+        m = ModelObject(args.device)
+        for name, new_set in cfg.functions:
+            m.add_function(name, new_set, subsampling=not args.nosubsampling)
+        m.finish_functions()
+        if im.psf:
+            m.add_psf(fitsio.read_image(im.psf)[0])
+        nc, nr = int(float(im.options.get("NCOLS", 0))), int(float(im.options.get("NROWS", 0)))
+        if not (nc > 0 and nr > 0):
+            if not im.data:
+                raise SystemExit("an image needs NCOLS and NROWS (or a DATA image for its size)")
+            nr, nc = fitsio.read_image(im.data)[0].shape
+        m.setup_model_image(nc, nr)
+        handles.append(m)
+    mm = MultiImageModel(cfg.functions, handles)
+    p, _, _, _ = global_vector(cfg, images)
+    outs = []
+    for i, m in enumerate(handles):
+        m.create_model_image(mm.image_vector(p, i))
+        img = m.get_model_image()
+        fitsio.write_image(f"{args.output}_{i}.fits", img)
+        outs.append(img)
+    out.write(f"saved {len(outs)} model images as {args.output}_0.fits ... {args.output}_{len(outs) - 1}.fits\n")
+    return outs
+
+
 def main(argv=None):
     argv = sys.argv[1:] if argv is None else argv
     if argv and argv[0] == "makeimage":
@@ -469,6 +515,8 @@ def main(argv=None):
         mcmc(argv[1:])
     elif argv and argv[0] == "multimfit":
         multimfit(argv[1:])
+    elif argv and argv[0] == "makemultimages":
+        makemultimages(argv[1:])
     else:
         run(argv)
 

@@ -64,8 +64,10 @@ def _label(line):
     return "" if k < 0 else line[k + 5:].strip()
 
 
-def parse_config(text):
-    """Parse the text of an Imfit configuration file."""
+def parse_config(text, check_limits=True):
+    """Parse the text of an Imfit configuration file.  check_limits=False is
+    makeimage's reading (ReadConfigFile in makeimage mode): limits are kept
+    but not checked against the values."""
     lines = []
     for k, raw in enumerate(text.splitlines(), 1):
         t = raw.strip()
@@ -103,9 +105,9 @@ def parse_config(text):
                     a, b = (float(x) for x in lim.split(","))
                 except ValueError:
                     raise ConfigError(f"line {lineno}: bad limits {lim!r}")
-                if a > b:
+                if check_limits and a > b:
                     raise ConfigError(f"line {lineno}: lower limit above upper limit")
-                if not (a <= v <= b):
+                if check_limits and not (a <= v <= b):
                     raise ConfigError(f"line {lineno}: initial value outside its limits")
                 l, h = a, b
         cfg.param_names.append(parts[0])
@@ -163,9 +165,9 @@ def parse_config(text):
     return cfg
 
 
-def read_config(path):
+def read_config(path, check_limits=True):
     with open(path) as f:
-        return parse_config(f.read())
+        return parse_config(f.read(), check_limits)
 
 
 _NPARAMS = {"Sersic": 5, "Exponential": 4, "FlatSky": 1, "GaussianRing": 5, "Moffat": 5, "Gaussian": 4,

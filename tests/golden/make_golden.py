@@ -2,7 +2,7 @@
 
 Run in a checkout that has the reference at /root/reference (or
 IMFIT_REFERENCE_DIR):  python tests/golden/make_golden.py [part ...]
-(parts: n3073 makeimage ic3478 pointsource mcmc multimfit small_case; all by default)
+(parts: n3073 makeimage ic3478 pointsource mcmc multimfit makemultimages small_case; all by default)
 
 Outputs (all small .npz files next to this script):
   n3073.npz          the reference regression inputs tests/n3073rss_small.fits,
@@ -35,6 +35,10 @@ Outputs (all small .npz files next to this script):
                      multimfit_textout3a (Nelder-Mead fit of
                      config_imfit_smallgauss.dat + imageinfo_multimfit3.txt) and
                      multimfit_textout1a (--fitstat-only, imageinfo_multimfit0.txt).
+  makemultimages.npz the makemultimages outputs tests/makemultimages_reference/
+                     multimagetest_{0,1,2,2b,2c,2d}.fits and multimagetest_2blocks_0 /
+                     _offset_1 / _offset_2.fits (do_makemultimages_tests.sh:59-65),
+                     64 x 64 each.
   small_case.npz     the reference's own outputs (oracle/_ref) for
                      imfit_gb300.workloads.small_case: model images, deviates and
                      statistics for chi^2 / Cash / PMLR.
@@ -167,6 +171,16 @@ def multimfit():
         d_chi2_printed=6.75)
 
 
+def makemultimages():
+    t = os.path.join(REF, "tests", "makemultimages_reference")
+    names = {"img_0": "multimagetest_0", "img_1": "multimagetest_1", "img_2": "multimagetest_2",
+             "img_2b": "multimagetest_2b", "img_2c": "multimagetest_2c", "img_2d": "multimagetest_2d",
+             "blk_0": "multimagetest_2blocks_0", "blk_1": "multimagetest_2blocks_offset_1",
+             "blk_2": "multimagetest_2blocks_offset_2"}
+    out = {k: fits.read_image(os.path.join(t, v + ".fits"))[0].astype(np.float32) for k, v in names.items()}
+    np.savez_compressed(os.path.join(HERE, "makemultimages.npz"), **out)
+
+
 def small_case():
     out = {}
     for stat in ("chi2", "cash", "pmlr"):
@@ -186,7 +200,7 @@ if __name__ == "__main__":
         sys.exit(f"reference checkout not found at {REF}")
     oracle.build_reference()
     parts = {"n3073": n3073, "makeimage": makeimage, "ic3478": ic3478, "pointsource": pointsource,
-             "mcmc": mcmc, "multimfit": multimfit, "small_case": small_case}
+             "mcmc": mcmc, "multimfit": multimfit, "makemultimages": makemultimages, "small_case": small_case}
     for name in (sys.argv[1:] or parts):
         parts[name]()
     for f in sorted(os.listdir(HERE)):

@@ -99,3 +99,79 @@ def test_multimfit_smallgauss_fit(gpu, tmp_path):
     p_nm, s_nm = cli.multimfit([str(tmp_path / "gauss.dat"), "-i", str(tmp_path / "gauss_info.txt"), "--nm"],
                                out=io.StringIO())
     assert s_nm <= chi2 + 1e-3
+
+
+GLOBAL_CFG = """X0 31.0 0,4
+Y0 31.0 0,4
+FUNCTION Exponential
+PA 95.0 0,180
+ell 0.45 0,1
+I_0 90.0 0,1000
+h 15.0 0,1000
+FUNCTION Sersic
+PA 90.0
+ell 0.2
+n 2.5
+I_e 10.0
+r_e 10.0
+"""
+SECOND_SET = """
+X0 50.0
+Y0 45.0
+FUNCTION Gaussian
+PA 0
+ell 0.5
+I_0 100.0
+sigma 2.0
+"""
+
+
+def _info(third):
+    ps, pa, fs = third
+    return f"""IMAGE_START
+NCOLS 64
+NROWS 64
+IMAGE_START
+NCOLS 64
+NROWS 64
+PIXEL_SCALE 1.0 fixed
+IMAGE_PA 0.0 fixed
+FLUX_SCALE 1.0 fixed
+X0 40
+Y0 40
+IMAGE_START
+NCOLS 64
+NROWS 64
+PIXEL_SCALE {ps} fixed
+IMAGE_PA {pa} fixed
+FLUX_SCALE {fs} 10,20
+X0 10
+Y0 20
+"""
+
+
+@pytest.mark.parametrize("case,third,config,goldens", [
+    ("plain", (1.0, 0.0, 1.0), GLOBAL_CFG, ["img_0", "img_1", "img_2"]),
+    ("flux", (1.0, 0.0, 100.0), GLOBAL_CFG, [None, None, "img_2b"]),
+    ("rotation", (1.0, 90.0, 1.0), GLOBAL_CFG, [None, None, "img_2c"]),
+    ("scale", (10.0, 0.0, 1.0), GLOBAL_CFG, [None, None, "img_2d"]),
+    ("two_sets", (1.0, 0.0, 1.0), GLOBAL_CFG + SECOND_SET, ["blk_0", "blk_1", "blk_2"]),
+])
+def test_makemultimages_goldens(gpu, tmp_path, case, third, config, goldens):
+    """do_makemultimages_tests.sh:59-65: the model of one configuration seen
+    through three image descriptions (offset X0/Y0, FLUX_SCALE, IMAGE_PA,
+    PIXEL_SCALE, a second function set moved with the image) against the
+    reference's float32 output images."""
+    from imfit_gb300 import cli
+    g = np.load(os.path.join(GOLDEN, "makemultimages.npz"))
+    (tmp_path / "c.dat").write_text(config)
+    (tmp_path / "info.txt").write_text(_info(third))
+    imgs = cli.makemultimages([str(tmp_path / "c.dat"), "-i", str(tmp_path / "info.txt"), "-o",
+                               str(tmp_path / "m")], out=io.StringIO())
+    for img, key in zip(imgs, goldens):
+        if key is None:
+            continue
+        want = g[key].astype(np.float64)
+        assert img.shape == want.shape
+        tol = np.spacing(np.abs(g[key])).astype(np.float64) * 2 + 1e-30
+        assert np.all(np.abs(img - want) <= tol), (key, np.max(np.abs(img - want) / tol))
