@@ -113,7 +113,21 @@ def _add_psf(m, args):
         m.add_psf(fitsio.read_image(args.psf)[0], normalize=not args.no_normalize)
 
 
-def _add_oversampled_psfs(m, args):
+def _section_offsets(cfg, image_name):
+    """X0/Y0 shifts of an image section (core/imfit_main.cpp:211, 288-309,
+    350-356): the vector to subtract from the configuration's values and
+    limits, and to add back to fitted values."""
+    dx, dy = fitsio.image_offset(image_name)
+    off = np.zeros(len(cfg.values))
+    for j, name in enumerate(cfg.param_names):
+        if name == "X0":
+            off[j] = dx
+        elif name == "Y0":
+            off[j] = dy
+    return off, (dx, dy)
+
+
+def _add_oversampled_psfs(m, args, offset=(0, 0)):
     """Oversampled PSFs as core/getimages.cpp:138-200 (after the image size is
     known): one image and scale serve every region, or one per region."""
     if not args.overpsf:
@@ -128,8 +142,10 @@ def _add_oversampled_psfs(m, args):
         j = k if len(args.overpsf) > 1 else 0
         if args.overpsf_scale[j] < 1:
             raise SystemExit("--overpsf_scale must be a positive integer")
+        x1, x2, y1, y2 = parse_region(region)
         m.add_oversampled_psf(fitsio.read_image(args.overpsf[j])[0], args.overpsf_scale[j],
-                              parse_region(region), normalize=not args.no_normalize)
+                              (x1 - offset[0], x2 - offset[0], y1 - offset[1], y2 - offset[1]),
+                              normalize=not args.no_normalize)
 
 
 def _add_functions(m, cfg, args):
@@ -145,12 +161,12 @@ def _add_functions(m, cfg, args):
                          f"{m.n_params}")
 
 
-def setup_model(cfg, args, image):
+def setup_model(cfg, args, image, offset=(0, 0)):
     m = ModelObject(args.device)
     _add_functions(m, cfg, args)
     _add_psf(m, args)
     m.add_image_data(image)
-    _add_oversampled_psfs(m, args)
+    _add_oversampled_psfs(m, args, offset)
     gain = args.gain if args.gain is not None else cfg.gain
     rn = args.readnoise if args.readnoise is not None else cfg.read_noise
     et = args.exptime if args.exptime is not None else cfg.exp_time
@@ -184,17 +200,19 @@ def run(argv=None, out=sys.stdout):
     except ConfigError as e:
         raise SystemExit(f"error in {args.config}: {e}")
     image = fitsio.read_image(args.image)[0]
-    m = setup_model(cfg, args, image)
-    p0 = np.array(cfg.values, dtype=float)
+    off, shift = _section_offsets(cfg, args.image)
+    m = setup_model(cfg, args, image, shift)
+    p0 = np.array(cfg.values, dtype=float) - off
+    cfg_lower, cfg_upper = cfg.lower - off, cfg.upper - off  # NaN (no limit) stays NaN
     if args.chisquare_only:
         s = m.get_fit_statistic(p0)
         out.write(f"fit statistic = {s:.6f}\n")
-        return p0, s
+        return p0 + off, s
     n_free = int(np.sum(cfg.fixed == 0))
     if args.de or args.de_lhs:
         from .solvers import differential_evolution
         try:
-            r = differential_evolution(m, p0, cfg.lower, cfg.upper, fixed=cfg.fixed.astype(bool),
+            r = differential_evolution(m, p0, cfg_lower, cfg_upper, fixed=cfg.fixed.astype(bool),
                                        ftol=args.ftol, seed=args.seed, latin_hypercube=args.de_lhs)
         except ValueError as e:
             raise SystemExit(str(e))
@@ -203,8 +221,8 @@ def run(argv=None, out=sys.stdout):
                   f"({'converged' if r['converged'] else 'generation limit'})\n")
     elif args.nm:
         from .solvers import nelder_mead
-        lo = np.where(np.isnan(cfg.lower), -np.inf, cfg.lower)
-        hi = np.where(np.isnan(cfg.upper), np.inf, cfg.upper)
+        lo = np.where(np.isnan(cfg_lower), -np.inf, cfg_lower)
+        hi = np.where(np.isnan(cfg_upper), np.inf, cfg_upper)
         r = nelder_mead(m, p0, lo, hi, fixed=cfg.fixed.astype(bool), ftol=args.ftol)
         p = r["params"]
         out.write(f"Nelder-Mead simplex: {r['evaluations']} evaluations "
@@ -213,13 +231,15 @@ def run(argv=None, out=sys.stdout):
         if args.cashstat:
             raise SystemExit("the Cash statistic has no deviates: use --chisquare-only, --de, --nm, or fit "
                              "chi^2 / --poisson-mlr")
-        limited = ~np.isnan(cfg.lower)
-        lo = np.where(limited, cfg.lower, 0.0)
-        hi = np.where(limited, cfg.upper, 0.0)  # lower >= upper means no limit
+        limited = ~np.isnan(cfg_lower)
+        lo = np.where(limited, cfg_lower, 0.0)
+        hi = np.where(limited, cfg_upper, 0.0)  # lower >= upper means no limit
         r = m.fit_lm(p0, fixed=cfg.fixed, lower=lo, upper=hi, ftol=args.ftol, max_iter=args.max_iter)
         p = r["params"]
         out.write(f"status {r['status']} after {r['niter']} iterations ({r['nev']} J^T J evaluations)\n")
     s = m.get_fit_statistic(p)  # FP64 statistic at the fitted point
+    p_section = p
+    p = p + off  # reported in the full image's coordinates
     dof = m.n_valid - n_free
     out.write(f"fit statistic = {s:.6f}, reduced = {s / dof:.6f} ({dof} degrees of freedom)\n")
     for name, v in zip(cfg.param_names, p):
@@ -228,9 +248,9 @@ def run(argv=None, out=sys.stdout):
         with open(args.save_params, "w") as f:
             f.write(format_params(cfg, p, s))
     if args.bootstrap > 0:
-        run_bootstrap(m, cfg, args, p, out)
+        run_bootstrap(m, cfg, args, p_section, out, off)
     if args.save_model or args.save_residual:
-        m.create_model_image(p)
+        m.create_model_image(p_section)
         model = m.get_model_image()
         if args.save_model:
             fitsio.write_image(args.save_model, model)
@@ -239,19 +259,23 @@ def run(argv=None, out=sys.stdout):
     return p, s
 
 
-def run_bootstrap(m, cfg, args, bestfit, out):
+def run_bootstrap(m, cfg, args, bestfit, out, off=None):
     """Bootstrap resampling errors (core/bootstrap_errors.cpp:86-160), all
-    refits of a chunk at once on the GPU."""
+    refits of a chunk at once on the GPU; off: image-section shifts added back
+    to the reported values."""
+    off = np.zeros(len(bestfit)) if off is None else off
     from .config import _NPARAMS
     from .solvers import bootstrap_errors, bootstrap_file_lines, bootstrap_summary
     if args.cashstat:
         raise SystemExit("bootstrap refits use the LM driver: chi^2 or --poisson-mlr")
     limited = ~np.isnan(cfg.lower)
-    lo = np.where(limited, cfg.lower, 0.0)
-    hi = np.where(limited, cfg.upper, 0.0)
+    lo = np.where(limited, cfg.lower - off, 0.0)
+    hi = np.where(limited, cfg.upper - off, 0.0)
     seed = args.seed if args.seed > 0 else int(time.time())
     samples, status = bootstrap_errors(m, bestfit, args.bootstrap, seed, fixed=cfg.fixed, lower=lo, upper=hi,
                                        ftol=args.ftol, max_iter=args.max_iter)
+    samples = samples + off
+    bestfit = np.asarray(bestfit) + off
     if samples.shape[0] < 3:  # MIN_ITERATIONS_FOR_STATISTICS
         out.write(f"\nNot enough successful bootstrap iterations ({samples.shape[0]}) for meaningful "
                   "statistics!\n")
@@ -366,8 +390,9 @@ def mcmc(argv=None, out=sys.stdout):
     except ConfigError as e:
         raise SystemExit(f"error in {args.config}: {e}")
     image = fitsio.read_image(args.image)[0]
-    m = setup_model(cfg, args, image)
-    p0 = np.array(cfg.values, dtype=float)
+    off, shift = _section_offsets(cfg, args.image)
+    m = setup_model(cfg, args, image, shift)
+    p0 = np.array(cfg.values, dtype=float) - off
     fixed = cfg.fixed.astype(bool)
     if np.any(np.isnan(cfg.lower[~fixed])):
         raise SystemExit("parameter limits must be supplied for all free parameters when using MCMC")
@@ -381,11 +406,11 @@ def mcmc(argv=None, out=sys.stdout):
                 f.write(f"# imfit_gb300 mcmc, configuration file {args.config}, image {args.image}\n#\n")
                 f.write("# Column Headers\n" + head + "\n")
                 files.append(f)
-        for i, f in enumerate(files):
-            f.write(chain_file_row(states[i], liks[i], burn, pCR, accept[i]) + "\n")
+        for i, f in enumerate(files):  # full-image coordinates, as PrintModelParamsHorizontalString writes
+            f.write(chain_file_row(states[i] + off, liks[i], burn, pCR, accept[i]) + "\n")
 
     try:
-        r = dream(m, p0, cfg.lower, cfg.upper, fixed=fixed, n_chains=args.nchains,
+        r = dream(m, p0, cfg.lower - off, cfg.upper - off, fixed=fixed, n_chains=args.nchains,
                   max_generations=args.max_chain_length, burn_in=args.burnin_length, gelman_evals=args.gelman_evals,
                   scale_reduction=args.gelman_rubin_limit, noise=args.uniform_offset, bstar=args.gaussian_offset,
                   seed=args.seed, callback=write)

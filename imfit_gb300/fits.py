@@ -6,6 +6,8 @@ needs: a 2-D primary (or first image-extension) HDU with BITPIX 8/16/32/-32/-64,
 BSCALE/BZERO, returned as a float64 array indexed [row, column] with rows
 counted from the bottom of the image (the order Imfit's pixel vectors use).
 """
+import re
+
 import numpy as np
 
 _BLOCK = 2880
@@ -43,8 +45,37 @@ def _parse_header(raw, pos):
             return cards, pos
 
 
+def split_section(name):
+    """'file.fits[x1:x2,y1:y2]' -> ('file.fits', (x1, x2, y1, y2)) with 1-based
+    inclusive pixel ranges (x = column), as CFITSIO's image sections; a name
+    without a section -> (name, None)."""
+    m = re.fullmatch(r"(.*)\[\s*(\d+)\s*:\s*(\d+)\s*,\s*(\d+)\s*:\s*(\d+)\s*\]", name.strip())
+    if not m:
+        return name, None
+    return m.group(1), tuple(int(m.group(i)) for i in range(2, 6))
+
+
+def image_offset(name):
+    """DetermineImageOffset (core/utilities.cpp:483-489): (x1 - 1, y1 - 1) of
+    an image section, (0, 0) without one."""
+    _, sec = split_section(name)
+    return (0, 0) if sec is None else (sec[0] - 1, sec[2] - 1)
+
+
 def read_image(path):
-    """Return (float64 array [nrows, ncols], header dict) of the first 2-D image HDU."""
+    """Return (float64 array [nrows, ncols], header dict) of the first 2-D image
+    HDU; a trailing section [x1:x2,y1:y2] selects that part of the image."""
+    path, sec = split_section(path)
+    arr, hdr = _read_full(path)
+    if sec is not None:
+        x1, x2, y1, y2 = sec
+        if not (1 <= x1 <= x2 <= arr.shape[1] and 1 <= y1 <= y2 <= arr.shape[0]):
+            raise ValueError(f"image section {sec} outside the {arr.shape[1]} x {arr.shape[0]} image")
+        arr = arr[y1 - 1:y2, x1 - 1:x2].copy()
+    return arr, hdr
+
+
+def _read_full(path):
     with open(path, "rb") as f:
         raw = f.read()
     pos = 0

@@ -115,3 +115,16 @@ def test_region_strings():
     assert parse_region("100:110,20:30") == (100, 110, 20, 30)
     with pytest.raises(SystemExit):
         parse_region("100-110,20:30")
+
+
+def test_fits_image_sections(tmp_path):
+    """CFITSIO-style sections file.fits[x1:x2,y1:y2] (1-based, x = column) and
+    DetermineImageOffset (core/utilities.cpp:483-489)."""
+    a = np.arange(30.0).reshape(5, 6)
+    p = str(tmp_path / "a.fits")
+    fits.write_image(p, a, bitpix=-64)
+    sub = fits.read_image(p + "[2:4,3:5]")[0]
+    assert np.array_equal(sub, a[2:5, 1:4])
+    assert fits.image_offset(p + "[2:4,3:5]") == (1, 2) and fits.image_offset(p) == (0, 0)
+    with pytest.raises(ValueError):
+        fits.read_image(p + "[2:9,1:2]")

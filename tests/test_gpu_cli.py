@@ -266,3 +266,37 @@ def test_mcmc_faintstar_posterior(gpu, tmp_path):
     assert rows.shape == (r["generations"], 12) and np.all(rows[:5000, 7] == 1)
     assert np.array_equal(rows[:, 7], r["burn_in"]) and np.all(rows[r["burn_in_end"]:, 7] == 0)
     assert abs(rows[:, 6].max() - float(d["ref_best_loglik"])) < 0.5
+
+
+def test_image_section_offsets(gpu, tmp_path, oracle_mod):
+    """imfit on IMAGE[x1:x2,y1:y2]: X0/Y0 (values and limits) shift by the
+    section's offset while fitting and shift back in the output
+    (core/imfit_main.cpp:211, 288-309, 350-356).  The statistic through the
+    command line equals the oracle's on the cropped image with shifted
+    centres; a fit of the section reports full-image coordinates close to
+    the whole image's fit."""
+    from imfit_gb300 import cli
+    d = _ic3478_files(tmp_path)
+    sec = str(tmp_path / "data.fits") + "[5:60,3:58]"
+    p_full = d["lm_params_printed"]
+    cfgp = tmp_path / "c2.dat"
+    lines = [f"GAIN {float(d['gain'])}", f"READNOISE {float(d['read_noise'])}",
+             f"ORIGINAL_SKY {float(d['original_sky'])}"]
+    for j, (nm, v, lo, hi) in enumerate(zip(["X0", "Y0", "PA", "ell", "n", "I_e", "r_e"], p_full, d["lo"], d["hi"])):
+        if j == 2:
+            lines.append("FUNCTION Sersic")
+        lines.append(f"{nm} {float(v)!r} {float(lo)!r},{float(hi)!r}")
+    cfgp.write_text("\n".join(lines) + "\n")
+    _, s = cli.run([str(cfgp), sec, "--chisquare-only"], out=io.StringIO())
+    o = oracle_mod.OracleModel()
+    o.add_function("Sersic", True)
+    o.finish_functions()
+    o.add_image_data(d["data"].astype(np.float64)[2:58, 4:60])
+    o.add_image_characteristics(float(d["gain"]), float(d["read_noise"]), 1.0, 1, float(d["original_sky"]))
+    assert o.final_setup() == 0
+    shifted = p_full.copy()
+    shifted[0] -= 4
+    shifted[1] -= 2
+    assert abs(s - o.get_fit_statistic(shifted)) <= 1e-10 * s
+    p, _ = cli.run([str(cfgp), sec, "--save-params", str(tmp_path / "b2.dat")], out=io.StringIO())
+    assert abs(p[0] - p_full[0]) < 0.1 and abs(p[1] - p_full[1]) < 0.1
