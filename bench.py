@@ -161,13 +161,72 @@ def run_reference(args, rank, world):
 
 
 # ------------------------------------------------------------------ GPU arm
+class _Nvml:
+    """Read-only NVML queries through the driver's libnvidia-ml (SM clock,
+    maximum SM clock, current clock-event reasons) for the device torch
+    uses, found by UUID (NVML does not follow CUDA_VISIBLE_DEVICES)."""
+    CLOCK_SM = 1  # nvmlClockType_t NVML_CLOCK_SM
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown"}
+
+    def __init__(self, index):
+        import ctypes
+        import torch
+        self.c = ctypes
+        lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        self.h = ctypes.c_void_p()
+        uuid = getattr(torch.cuda.get_device_properties(index), "uuid", None)
+        st = 1
+        if uuid is not None:
+            st = lib.nvmlDeviceGetHandleByUUID(("GPU-" + str(uuid)).encode(), ctypes.byref(self.h))
+        if st != 0:
+            st = lib.nvmlDeviceGetHandleByIndex_v2(index, ctypes.byref(self.h))
+        if st != 0:
+            raise OSError("no NVML handle")
+        self.lib = lib
+        self.reasons = (getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None)
+                        or lib.nvmlDeviceGetCurrentClocksThrottleReasons)
+
+    def sample(self):
+        c, r = self.c.c_uint(), self.c.c_ulonglong()
+        if self.lib.nvmlDeviceGetClockInfo(self.h, self.CLOCK_SM, self.c.byref(c)) != 0:
+            return None
+        if self.reasons(self.h, self.c.byref(r)) != 0:
+            return None
+        return float(c.value), [nm for bit, nm in self.REASONS.items() if r.value & bit]
+
+    def max_sm(self):
+        c = self.c.c_uint()
+        return float(c.value) if self.lib.nvmlDeviceGetMaxClockInfo(self.h, self.CLOCK_SM, self.c.byref(c)) == 0 \
+            else None
+
+
 class Clocks:
+    """SM clock and throttle reasons sampled while the timed region runs:
+    NVML from a thread every 2 ms (a timed region of a few tens of ms still
+    gets samples), else nvidia-smi's 200 ms loop."""
     FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
               "clocks_event_reasons.sw_power_cap")
 
     def __init__(self, index):
+        import threading
         self.proc = None
+        self.nvml = None
+        self.samples = []
+        try:
+            self.nvml = _Nvml(index)
+        except Exception:  # no driver library, no device, an older NVML: use nvidia-smi
+            self.nvml = None
+        if self.nvml is not None:
+            self.halt = threading.Event()
+            first = self.nvml.sample()
+            if first:
+                self.samples.append(first)
+            self.thread = threading.Thread(target=self._loop, daemon=True)
+            self.thread.start()
+            return
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
@@ -175,7 +234,23 @@ class Clocks:
         except OSError:
             self.proc = None
 
+    def _loop(self):
+        while not self.halt.wait(0.002):
+            v = self.nvml.sample()
+            if v:
+                self.samples.append(v)
+
     def stop(self):
+        if self.nvml is not None:
+            self.halt.set()
+            self.thread.join()
+            last = self.nvml.sample()
+            if last:
+                self.samples.append(last)
+            sm = [c for c, _ in self.samples]
+            reasons = sorted({r for _, rs in self.samples for r in rs})
+            return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": self.nvml.max_sm(),
+                    "reasons": reasons, "samples": len(sm), "source": "nvml"}
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
@@ -199,7 +274,7 @@ class Clocks:
                 if v.lower().startswith("active"):
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "source": "nvidia-smi"}
 
 
 def algorithmic_bytes(model, wl):

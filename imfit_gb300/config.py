@@ -171,7 +171,8 @@ def read_config(path, check_limits=True):
 
 
 _NPARAMS = {"Sersic": 5, "Exponential": 4, "FlatSky": 1, "GaussianRing": 5, "Moffat": 5, "Gaussian": 4,
-            "ExponentialDisk3D": 6, "FerrersBar3D": 8, "PointSource": 1, "PointSourceRot": 2}
+            "ExponentialDisk3D": 6, "FerrersBar3D": 8, "PointSource": 1, "PointSourceRot": 2,
+            "TiltedSkyPlane": 3}
 
 
 def format_params(cfg, params, chi2=None):

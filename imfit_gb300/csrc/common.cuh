@@ -34,11 +34,21 @@ enum FuncType : int {
   F_FERRERS3D = 8,   // function_objects/func_ferrersbar3d.cpp
   F_POINTSOURCE = 9,     // function_objects/func_pointsource.cpp
   F_POINTSOURCEROT = 10, // function_objects/func_pointsource-rot.cpp
+  F_TILTEDSKY = 11,      // function_objects/func_tilted-sky-plane.cpp
 };
+
+// 3-D classes: the value is a line-of-sight integral (func_expdisk3d.cpp,
+// func_ferrersbar3d.cpp).
+__host__ __device__ inline bool is_los(int t) { return t == F_EXPDISK3D || t == F_FERRERS3D; }
 
 // PointSource classes are added after the convolution (IsPointSource,
 // core/model_object.cpp:1163-1216), from an interpolated PSF.
 __host__ __device__ inline bool is_point_source(int t) { return t == F_POINTSOURCE || t == F_POINTSOURCEROT; }
+
+// classes without a position angle
+__host__ __device__ inline bool has_pa(int t) {
+  return t != F_FLATSKY && t != F_POINTSOURCE && t != F_TILTEDSKY;
+}
 
 constexpr int kMaxComponents = 32;
 constexpr int kMaxParams = 256;
@@ -107,6 +117,7 @@ __host__ __device__ inline double sersic_dbn_dn(double n) {
 //   Sersic:   a=n b=I_e c=r_e d=bn e=invn
 //   Exp:      a=I_0 b=h
 //   FlatSky:  a=I_sky
+//   TiltedSkyPlane: a=I_0 b=m_x c=m_y
 //   GRing:    a=A b=R_ring c=sigma_r d=2 sigma^2
 //   Moffat:   a=I_0 b=fwhm c=beta d=alpha
 //   Gaussian: a=I_0 b=sigma d=2 sigma^2
@@ -121,7 +132,7 @@ __host__ __device__ inline void comp_setup64(CompF64 &c, int type, int subsample
   c.q = 1.0;
   c.cosPA = 1.0;
   c.sinPA = 0.0;
-  if (type != F_FLATSKY && type != F_POINTSOURCE) {
+  if (has_pa(type)) {
     double par = (p[0] + 90.0) * kDeg2Rad;
     c.cosPA = cos(par);
     c.sinPA = sin(par);
@@ -139,6 +150,9 @@ __host__ __device__ inline void comp_setup64(CompF64 &c, int type, int subsample
       break;
     case F_FLATSKY:  // func_flatsky.cpp:85-90
       c.a = p[0];
+      break;
+    case F_TILTEDSKY:  // func_tilted-sky-plane.cpp:85-93
+      c.a = p[0]; c.b = p[1]; c.c = p[2];
       break;
     case F_POINTSOURCE:  // func_pointsource.cpp:206-211
       c.a = p[0];
@@ -243,6 +257,7 @@ __host__ __device__ inline double radial64(const CompF64 &c, double r) {
 // (func_sersic.cpp:147-189; identical structure in the other radial classes).
 __host__ __device__ inline double comp_value64_2d(const CompF64 &c, double x, double y) {
   if (c.type == F_FLATSKY) return c.a;
+  if (c.type == F_TILTEDSKY) return c.a + c.b * (x - c.x0) + c.c * (y - c.y0);  // func_tilted-sky-plane.cpp:98-104
   double x_diff = x - c.x0, y_diff = y - c.y0;
   double xp = x_diff * c.cosPA + y_diff * c.sinPA;
   double yps = (-x_diff * c.sinPA + y_diff * c.cosPA) / c.q;
@@ -281,6 +296,7 @@ __host__ __device__ inline double comp_value64_2d(const CompF64 &c, double x, do
 //   Gaussian: s0=I_0 s1=log2(e)/(2 sigma^2) s2=sigma s3=1/sigma s4=1/sigma^2
 // (reciprocals are formed in FP64 at setup so the pixel loops divide nowhere)
 //   FlatSky:  s0=I_sky
+//   TiltedSkyPlane: s0=I_0 s1=m_x s2=m_y
 //   ExpDisk3D:    s0=J_0 s1=1/h s2=h s3=cos(inc) s4=sin(inc) s5=alpha=2/n
 //                 s6=1/(alpha z_0) s7=z_0 subScale=n subInner=20h (half-range)
 //   FerrersBar3D: s0=J_0 s1=R_bar s2=q s3=cos(inc) s4=sin(inc) s5,s6=cos,sin(barPA+90)
@@ -328,7 +344,7 @@ __device__ inline void comp_setup32(CompF32 &o, const CompDesc &d, const double 
   o.cosPA = 1.f; o.sinPA = 0.f; o.q = 1.f; o.invq = 1.f;
   o.s0 = o.s1 = o.s2 = o.s3 = o.s4 = o.s5 = o.s6 = o.s7 = 0.f;
   o.subScale = 1.f; o.subInner = 3.f; o.subSmallK = 20.f;
-  if (d.type != F_FLATSKY && d.type != F_POINTSOURCE) {
+  if (has_pa(d.type)) {
     o.cosPA = (float)q.cosPA;
     o.sinPA = (float)q.sinPA;
   }
@@ -360,6 +376,11 @@ __device__ inline void comp_setup32(CompF32 &o, const CompDesc &d, const double 
     }
     case F_FLATSKY:
       o.s0 = (float)p[0];
+      break;
+    case F_TILTEDSKY:
+      o.s0 = (float)p[0];
+      o.s1 = (float)p[1];
+      o.s2 = (float)p[2];
       break;
     case F_GRING: {
       const double qq = 1.0 - p[1];
@@ -513,6 +534,19 @@ __device__ inline float radial32(const CompF32 &c, float r2) {
     case F_FLATSKY: return c.s0;
     default: return 0.f;
   }
+}
+
+// TiltedSkyPlane at offsets (dx, dy) from its function set's centre
+// (func_tilted-sky-plane.cpp:98-104) and its derivatives, in the slot layout
+// of radial_grad32 below: X0, Y0, I_0, m_x, m_y.  Returns 3.
+__device__ inline float plane32(const CompF32 &c, float dx, float dy) { return fmaf(c.s1, dx, fmaf(c.s2, dy, c.s0)); }
+__device__ inline int plane_grad32(const CompF32 &c, float dx, float dy, float scale, float *out) {
+  out[0] = -scale * c.s1;
+  out[1] = -scale * c.s2;
+  out[2] = scale;
+  out[3] = scale * dx;
+  out[4] = scale * dy;
+  return 3;
 }
 
 // Value of a component at pixel offset (dx,dy), with the reference's

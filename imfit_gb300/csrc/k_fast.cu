@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(128) k_fast_setup(FastArgs a) {
   const double *p = P + d.paramOffset;
   if (lane == 0) {
     if (w == 0) {
-      if (d.type != F_FLATSKY) {
+      if (has_pa(d.type)) {
         double sn, cs;
         sincospi((p[0] + 90.0) / 180.0, &sn, &cs);
         q.cosPA = cs;
@@ -131,6 +131,11 @@ __device__ __forceinline__ long sub_base(const FastArgs &a, int b, int c, int w)
   const long areaM = (long)a.boxMain * a.boxMain, areaR = (long)a.boxReg * a.boxReg;
   return (((long)b * a.nComp + c) * (areaM + areaR) + (w ? areaM : 0)) * 8;
 }
+
+// components evaluated pixel by pixel in the row kernels (FlatSky and the
+// point sources are added after the convolution, the 3-D classes by the
+// line-of-sight kernels)
+__device__ __forceinline__ bool in_rows(int t) { return t != F_FLATSKY && !is_los(t) && !is_point_source(t); }
 
 __device__ __forceinline__ bool subsampling_type(int t) {
   return t == F_SERSIC || t == F_EXP || t == F_MOFFAT || t == F_GAUSS;
@@ -241,14 +246,14 @@ __global__ void __launch_bounds__(1024) k_fast_eval_r2c(FastArgs a, WinDesc w, F
       if (col < w.cols) {
         for (int c = 0; c < nC; c++) {
           const CompF32 &cc = sc[c];
-          if (cc.type == F_FLATSKY || cc.type >= F_EXPDISK3D) continue;
+          if (!in_rows(cc.type)) continue;
           float dx, dy;
           win_offsets(w, cc, row, col, dx, dy);
           const Geo g = geo32(cc, dx, dy);
           if (sub_count(cc, g) > 1)
             v[e] += sub_value(a, boxes + 2 * c, b, c, win, cc, row, col, dx, dy);
           else
-            v[e] += radial32(cc, g.r2);
+            v[e] += cc.type == F_TILTEDSKY ? plane32(cc, dx, dy) : radial32(cc, g.r2);
         }
         if (w.losVal) v[e] += w.losVal[((long)b * w.rows + row) * w.cols + col];
       }
@@ -641,7 +646,7 @@ __global__ void __launch_bounds__(1024) k_fast_grad_rows(FastArgs a, WinDesc w, 
       }
     for (int c = 0; c < nC; c++) {
       const CompF32 &cc = sc[c];
-      if (cc.type == F_FLATSKY || cc.type >= F_EXPDISK3D) continue;
+      if (!in_rows(cc.type)) continue;
       const int side = win ? a.boxReg : a.boxMain;
       const float *tab = a.subTab + sub_base(a, b, c, win);
       float acc[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
@@ -680,7 +685,7 @@ __global__ void __launch_bounds__(1024) k_fast_grad_rows(FastArgs a, WinDesc w, 
           }
         } else {
           if (r == 0.f) continue;
-          np = radial_grad32(cc, g, r, o);
+          np = cc.type == F_TILTEDSKY ? plane_grad32(cc, dx, dy, r, o) : radial_grad32(cc, g, r, o);
         }
 #pragma unroll
         for (int q = 0; q < 7; q++)
@@ -733,7 +738,7 @@ struct LosStore {
 // index of component c among the model's 3-D components
 __device__ __forceinline__ int los_index(const CompF32 *sc, int c) {
   int k = 0;
-  for (int i = 0; i < c; i++) k += sc[i].type >= F_EXPDISK3D;
+  for (int i = 0; i < c; i++) k += is_los(sc[i].type);
   return k;
 }
 
@@ -755,7 +760,7 @@ __global__ void __launch_bounds__(256) k_fast_los_eval(FastArgs a, WinDesc w, Lo
     float v = 0.f;
     for (int c = 0; c < nC; c++) {
       const CompF32 &cc = sc[c];
-      if (cc.type < F_EXPDISK3D) continue;
+      if (!is_los(cc.type)) continue;
       float xp, yp;
       los_pixel(w, cc, row, col, xp, yp);
       float lo, hi, total;
@@ -794,7 +799,7 @@ __global__ void __launch_bounds__(256, 4) k_fast_los_grad(FastArgs a, WinDesc w,
     const int row = (int)(p / w.cols), col = (int)(p - (long)row * w.cols);
     for (int c = 0; c < nC; c++) {
       const CompF32 &cc = sc[c];
-      if (cc.type < F_EXPDISK3D) continue;
+      if (!is_los(cc.type)) continue;
       float xp, yp, g[kLosGrad];
       los_pixel(w, cc, row, col, xp, yp);
       if (ks.panels) {
@@ -911,7 +916,7 @@ __global__ void __launch_bounds__(1024) k_fast_deriv_r2c(FastArgs a, WinDesc w, 
   for (int col = threadIdx.x; col < w.cols; col += blockDim.x) {
     for (int c = 0; c < nC; c++) {
       const CompF32 &cc = sc[c];
-      if (cc.type == F_FLATSKY || cc.type >= F_EXPDISK3D) continue;
+      if (!in_rows(cc.type)) continue;
       float dx, dy;
       win_offsets(w, cc, row, col, dx, dy);
       const Geo g = geo32(cc, dx, dy);
@@ -938,7 +943,7 @@ __global__ void __launch_bounds__(1024) k_fast_deriv_r2c(FastArgs a, WinDesc w, 
         }
         np = 5;  // unused slots are zero
       } else {
-        np = radial_grad32(cc, g, 1.f, o);
+        np = cc.type == F_TILTEDSKY ? plane_grad32(cc, dx, dy, 1.f, o) : radial_grad32(cc, g, 1.f, o);
       }
       np = min(np, npar[c]);
       int s = ss[cc.x0Index];

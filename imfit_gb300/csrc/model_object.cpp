@@ -54,6 +54,7 @@ bool lookup_function(const std::string &n, FuncInfo &f) {
       {"FerrersBar3D", {F_FERRERS3D, {"PA", "inc", "barPA", "J_0", "R_bar", "q", "q_z", "n"}}},
       {"PointSource", {F_POINTSOURCE, {"I_tot"}}},
       {"PointSourceRot", {F_POINTSOURCEROT, {"PA", "I_tot"}}},
+      {"TiltedSkyPlane", {F_TILTEDSKY, {"I_0", "m_x", "m_y"}}},
   };
   auto it = reg.find(n);
   if (it == reg.end()) return false;
@@ -763,7 +764,7 @@ struct imfit_model_s {
       comp_setup64(c, funcs[f].type, funcs[f].subsample, p, xc, yc);
       double flux = 0.0;
       const int t = funcs[f].type;
-      if (t == F_FLATSKY) {
+      if (t == F_FLATSKY || t == F_TILTEDSKY) {  // IsBackground: model_object.cpp:2449-2450
         flux = 0.0;
       } else if (t == F_SERSIC) {
         const double n = p[2], I_e = p[3], r_e = p[4], q = 1.0 - p[1], bn = sersic_bn(n);

@@ -44,6 +44,7 @@ ADJUST = {
     "FerrersBar3D": (0, [3], [4]),
     "PointSource": (None, [0], []),
     "PointSourceRot": (0, [1], []),
+    "TiltedSkyPlane": (None, [0], []),  # slopes unscaled (func_tilted-sky-plane.cpp:74-80)
 }
 
 

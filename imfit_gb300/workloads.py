@@ -141,7 +141,8 @@ def param_names(functions):
              "FlatSky": ["I_sky"], "GaussianRing": ["PA", "ell", "A", "R_ring", "sigma_r"],
              "Moffat": ["PA", "ell", "I_0", "fwhm", "beta"], "Gaussian": ["PA", "ell", "I_0", "sigma"],
              "ExponentialDisk3D": ["PA", "inc", "J_0", "h", "n", "z_0"],
-             "FerrersBar3D": ["PA", "inc", "barPA", "J_0", "R_bar", "q", "q_z", "n"]}
+             "FerrersBar3D": ["PA", "inc", "barPA", "J_0", "R_bar", "q", "q_z", "n"],
+             "PointSource": ["I_tot"], "PointSourceRot": ["PA", "I_tot"], "TiltedSkyPlane": ["I_0", "m_x", "m_y"]}
     out = []
     for i, (name, new_set) in enumerate(functions):
         if new_set or i == 0:

@@ -61,7 +61,8 @@ const char *imfit_Version(void);
 /* ModelObject::AddFunction (core/model_object.cpp:279) with the factory of
  * core/add_functions.cpp:389-461: name is the config-file FUNCTION name
  * ("Sersic", "Exponential", "FlatSky", "GaussianRing", "Moffat", "Gaussian",
- * "ExponentialDisk3D", "FerrersBar3D", "PointSource", "PointSourceRot"). */
+ * "ExponentialDisk3D", "FerrersBar3D", "PointSource", "PointSourceRot",
+ * "TiltedSkyPlane"). */
 int imfit_AddFunction(imfit_model_t m, const char *name);
 /* FunctionObject::SetExtraParams (an OPTIONAL_PARAMS entry of the
  * configuration file) for function i: PointSource / PointSourceRot accept

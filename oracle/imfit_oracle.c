@@ -32,7 +32,7 @@
 #define MAXREGIONS 16
 
 enum { F_SERSIC = 1, F_EXP, F_FLATSKY, F_GRING, F_MOFFAT, F_GAUSS, F_EXPDISK3D, F_FERRERS3D, F_POINTSOURCE,
-       F_POINTSOURCEROT };
+       F_POINTSOURCEROT, F_TILTEDSKY };
 enum { INTERP_BICUBIC = 1, INTERP_LANCZOS2 = 2, INTERP_LANCZOS3 = 3 };
 #define IS_POINT_SOURCE(t) ((t) == F_POINTSOURCE || (t) == F_POINTSOURCEROT)
 
@@ -43,6 +43,7 @@ typedef struct {
   double n, I_e, r_e, bn, invn;            /* Sersic */
   double I_0, h;                           /* Exponential, Moffat/Gaussian I_0 */
   double I_sky;                            /* FlatSky */
+  double m_x, m_y;                         /* TiltedSkyPlane (I_0 above) */
   double A, R_ring, sigma_r, twosig2;      /* GaussianRing, Gaussian */
   double fwhm, beta, alpha, sigma;         /* Moffat, Gaussian */
   double inc, cosInc, sinInc, J_0, z_0, alpha3, scaledZ0, two_to_alpha; /* 3-D */
@@ -59,7 +60,8 @@ static int type_from_name(const char *name, int *npar) {
       {"FlatSky", F_FLATSKY, 1},         {"GaussianRing", F_GRING, 5},
       {"Moffat", F_MOFFAT, 5},           {"Gaussian", F_GAUSS, 4},
       {"ExponentialDisk3D", F_EXPDISK3D, 6}, {"FerrersBar3D", F_FERRERS3D, 8},
-      {"PointSource", F_POINTSOURCE, 1},     {"PointSourceRot", F_POINTSOURCEROT, 2}};
+      {"PointSource", F_POINTSOURCE, 1},     {"PointSourceRot", F_POINTSOURCEROT, 2},
+      {"TiltedSkyPlane", F_TILTEDSKY, 3}};
   for (size_t i = 0; i < sizeof(tab) / sizeof(tab[0]); i++)
     if (strcmp(name, tab[i].n) == 0) {
       if (npar) *npar = tab[i].p;
@@ -89,7 +91,8 @@ static double calc_bn(double n) {
  *   Moffat        function_objects/func_moffat.cpp:111-131
  *   Gaussian      function_objects/func_gaussian.cpp:104-119
  *   ExpDisk3D     function_objects/func_expdisk3d.cpp:149-171
- *   FerrersBar3D  function_objects/func_ferrersbar3d.cpp:125-165 */
+ *   FerrersBar3D  function_objects/func_ferrersbar3d.cpp:125-165
+ *   TiltedSkyPlane function_objects/func_tilted-sky-plane.cpp:85-93 */
 static void func_setup(ofunc *f, const double *p, double xc, double yc) {
   f->x0 = xc;
   f->y0 = yc;
@@ -110,6 +113,9 @@ static void func_setup(ofunc *f, const double *p, double xc, double yc) {
       break;
     case F_FLATSKY:
       f->I_sky = p[0];
+      break;
+    case F_TILTEDSKY:
+      f->I_0 = p[0]; f->m_x = p[1]; f->m_y = p[2];
       break;
     case F_GRING:
       f->PA = p[0]; f->ell = p[1]; f->A = p[2]; f->R_ring = p[3]; f->sigma_r = p[4];
@@ -454,9 +460,11 @@ static double los_integral(const ofunc *f, double x, double y, int *nsub) {
 }
 
 /* GetValue(x,y): func_sersic.cpp:147-189 (same structure in the other radial
- * classes), FlatSky func_flatsky.cpp:95-98, 3-D classes via los_integral. */
+ * classes), FlatSky func_flatsky.cpp:95-98, TiltedSkyPlane
+ * func_tilted-sky-plane.cpp:98-104, 3-D classes via los_integral. */
 static double func_value(const ofunc *f, double x, double y) {
   if (f->type == F_FLATSKY) return f->I_sky;
+  if (f->type == F_TILTEDSKY) return f->I_0 + f->m_x * (x - f->x0) + f->m_y * (y - f->y0);
   if (f->type == F_EXPDISK3D || f->type == F_FERRERS3D) return los_integral(f, x, y, NULL);
   double x_diff = x - f->x0, y_diff = y - f->y0;
   double q = (f->type == F_FLATSKY) ? 1.0 : f->q;

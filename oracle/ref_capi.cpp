@@ -29,6 +29,7 @@
 #include "function_objects/func_gaussian.h"
 #include "function_objects/func_expdisk3d.h"
 #include "function_objects/func_ferrersbar3d.h"
+#include "function_objects/func_tilted-sky-plane.h"
 #include "mpfit.h"
 #include "mersenne_twister.h"
 
@@ -46,6 +47,7 @@ FunctionObject *make_function(const char *name) {
   if (n == "Gaussian") return new Gaussian();
   if (n == "ExponentialDisk3D") return new ExponentialDisk3D();
   if (n == "FerrersBar3D") return new FerrersBar3D();
+  if (n == "TiltedSkyPlane") return new TiltedSkyPlane();
   return nullptr;
 }
 

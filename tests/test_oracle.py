@@ -52,6 +52,15 @@ def test_function_known_answers(oracle_mod, name, params, center, cases):
         assert abs(got - want) <= 1e-9, (name, x, y, got, want)
 
 
+def test_tilted_sky_plane_expression(oracle_mod):
+    """TiltedSkyPlane (no known answers in the reference's unit tests): the
+    GetValue expression I_0 + m_x (x - x0) + m_y (y - y0)
+    (func_tilted-sky-plane.cpp:98-104) in the parameter order I_0, m_x, m_y."""
+    for (x, y) in [(1.0, 1.0), (17.5, -3.25), (400.0, 250.0)]:
+        got = oracle_mod.function_value("TiltedSkyPlane", [7.5, 0.125, -0.0625], 10.0, 20.0, x, y)
+        assert got == 7.5 + 0.125 * (x - 10.0) + -0.0625 * (y - 20.0)
+
+
 def test_sersic_total_flux_known_answers(oracle_mod):
     # unit_tests/unittest_funcs.t.h:447-500
     for ell, n, want, tol in [(0.0, 1.0, 1194.839934018338, 1e-9), (0.25, 1.0, 0.75 * 1194.839934018338, 1e-9),
@@ -199,6 +208,28 @@ def test_restatement_bit_identical_to_reference(oracle_mod):
         o.use_bootstrap(5)
         r.use_bootstrap(5)
         assert o.get_fit_statistic(wl.start) == r.get_fit_statistic(wl.start)
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(os.environ.get("IMFIT_REFERENCE_DIR", "/root/reference"), "core")),
+                    reason="reference checkout not present")
+def test_tilted_sky_plane_matches_reference(oracle_mod):
+    """Sersic + TiltedSkyPlane (own function set) convolved with an
+    off-centre PSF: the oracle's model image equals the reference's."""
+    oracle_mod.build_reference()
+    yy, xx = np.mgrid[0:15, 0:15] - 7.0
+    psf = np.exp(-((xx - 0.6) ** 2 + yy ** 2) / 5.0)
+    p = [20.3, 18.6, 25.0, 0.3, 1.8, 30.0, 5.0, 21.0, 19.0, 12.0, 0.05, -0.03]
+    imgs = []
+    for cls in (oracle_mod.OracleModel, oracle_mod.RefModel):
+        m = cls()
+        m.add_function("Sersic", True)
+        m.add_function("TiltedSkyPlane", True)
+        m.finish_functions()
+        m.add_psf(psf)
+        m.setup_model_image(41, 37)
+        m.create_model_image(p)
+        imgs.append(m.get_model_image())
+    assert np.array_equal(imgs[0], imgs[1])
 
 
 def test_ic3478_printed_fit_statistic(oracle_mod):
