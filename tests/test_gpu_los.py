@@ -166,3 +166,36 @@ def test_jtwj_rejects_los_components(gpu, oracle_mod):
     with pytest.raises(gpu.ImfitError) as e:
         g.jtwj(wl.start)
     assert e.value.code == -4
+
+
+def test_fast_los_with_a_point_source(gpu, oracle_mod):
+    """ExponentialDisk3D + PointSource (its own function set): the 3-D
+    kernels integrate the disk only and the point source is added after the
+    convolution -- fast statistic against the FP64 oracle, adjoint gradient
+    against the oracle's central differences."""
+    from imfit_gb300 import workloads
+    size = 64
+    truth = np.array([32.3, 31.8, 30.0, 85.0, 0.5, 5.0, 1.0, 0.75, 20.4, 40.6, 300.0])
+    wl = workloads.Workload("los+ps", size, size, [("ExponentialDisk3D", True), ("PointSource", True)], truth,
+                            psf=workloads.gaussian_psf(15, 1.5), seed=17, noise="gaussian", noise_sigma=2.0)
+    wl.errors = np.full((size, size), 2.0)
+    workloads.synthesize(wl, oracle_mod.OracleModel)
+    g = workloads.configure(gpu.ModelObject(), wl)
+    o = workloads.configure(oracle_mod.OracleModel(), wl)
+    p = truth * np.array([1.0, 1.0, 1.03, 0.99, 1.05, 0.96, 1.0, 1.04, 1.0, 1.0, 1.1])
+    p[[0, 8, 9]] += [0.3, -0.4, 0.25]
+    s, grad = g.statistic_and_gradient(p)
+    so = o.get_fit_statistic(p)
+    assert relerr(s, so) < 1e-5, (s, so)
+    fd = np.empty(len(p))
+    for j in range(len(p)):
+        h = 1e-4 * max(abs(p[j]), 1.0)
+        a = np.array(p, dtype=float)
+        b = a.copy()
+        a[j] += h
+        b[j] -= h
+        fd[j] = (o.get_fit_statistic(a) - o.get_fit_statistic(b)) / (2 * h)
+    # the point source's derivatives come from the FP32 interpolant's slopes:
+    # the point-source tests' bound 3e-3 |g_fd| + 3e-4 max|g_fd|
+    bound = 3e-3 * np.abs(fd) + 3e-4 * np.max(np.abs(fd))
+    assert np.all(np.abs(grad - fd) <= bound), [(n, a, b) for n, a, b in zip(g.parameter_names(), grad, fd)]
