@@ -143,6 +143,44 @@ def exported_symbols():
     return [s[0] for s in _SIGS]
 
 
+def minimize_normal_equations(fun, x0, fixed=None, lower=None, upper=None, ftol=1e-8, max_iter=0):
+    """The library's Levenberg-Marquardt driver (imfit_MinimizeNormalEquations)
+    on a caller's normal equations: fun(x) -> (S, A, b) with S = sum dev^2,
+    A = J^T J, b = J^T dev.  Limits are used where lower < upper.  Returns a
+    dict with the parameters, S there, iterations, evaluations and the status
+    (1 ftol, 2 xtol, 3 no step, 4 stalled, 5 iteration limit)."""
+    lib = load_library()
+    x = np.array(x0, dtype=float)
+    n = x.size
+    fx = (_I * n)(*([0] * n if fixed is None else [int(v) for v in fixed]))
+    lo = _f64(lower) if lower is not None else None
+    hi = _f64(upper) if upper is not None else None
+    errors = []
+
+    @NORMAL_EQ_FN
+    def cb(xp, sp, ap, bp, user):
+        try:
+            s, A, b = fun(np.ctypeslib.as_array(xp, shape=(n,)).copy())
+            sp[0] = s
+            np.ctypeslib.as_array(ap, shape=(n * n,))[:] = np.asarray(A, dtype=float).ravel()
+            np.ctypeslib.as_array(bp, shape=(n,))[:] = b
+            return 0
+        except Exception as e:  # reported after the driver returns
+            errors.append(e)
+            return -1
+
+    stat = _D()
+    it, nev, st = _I(), _I(), _I()
+    rc = lib.imfit_MinimizeNormalEquations(n, _dp(x), fx, _dp(lo) if lo is not None else None,
+                                           _dp(hi) if hi is not None else None, ftol, int(max_iter), cb, None,
+                                           ctypes.byref(stat), ctypes.byref(it), ctypes.byref(nev), ctypes.byref(st))
+    if errors:
+        raise errors[0]
+    if rc != 0:
+        raise RuntimeError(lib.imfit_LastError(None).decode())
+    return dict(params=x, statistic=stat.value, niter=it.value, nev=nev.value, status=st.value)
+
+
 def _dp(a):
     return a.ctypes.data_as(_DP)
 

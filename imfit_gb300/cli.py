@@ -26,7 +26,7 @@ import time
 
 import numpy as np
 
-from . import ModelObject
+from . import ImfitError, ModelObject
 from . import fits as fitsio
 from .config import ConfigError, format_params, read_config
 
@@ -60,7 +60,7 @@ def build_parser():
     ap.add_argument("--ncombined", type=int)
     ap.add_argument("--sky", type=float, help="original sky level (ORIGINAL_SKY)")
     ap.add_argument("--cashstat", action="store_true")
-    ap.add_argument("--poisson-mlr", action="store_true")
+    ap.add_argument("--poisson-mlr", "--mlr", dest="poisson_mlr", action="store_true")
     ap.add_argument("--model-errors", action="store_true")
     ap.add_argument("--chisquare-only", action="store_true")
     ap.add_argument("--de", action="store_true", help="differential evolution instead of LM")
@@ -176,10 +176,10 @@ def setup_model(cfg, args, image, offset=(0, 0)):
     if args.noise:
         kind = WEIGHTS_ARE_VARIANCES if args.errors_are_variances else (
             WEIGHTS_ARE_WEIGHTS if args.errors_are_weights else WEIGHTS_ARE_SIGMAS)
-        m.add_error_vector(fitsio.read_image(args.noise)[0], kind)
+        m.add_error_vector(_matching_image(args.noise, "noise", image, args.image), kind)
     if args.mask:
-        m.add_mask_vector(fitsio.read_image(args.mask)[0], MASK_ZERO_IS_BAD if args.mask_zero_is_bad
-                          else MASK_ZERO_IS_GOOD)
+        m.add_mask_vector(_matching_image(args.mask, "mask", image, args.image),
+                          MASK_ZERO_IS_BAD if args.mask_zero_is_bad else MASK_ZERO_IS_GOOD)
     if args.cashstat:
         m.use_cash()
     elif args.poisson_mlr:
@@ -187,13 +187,58 @@ def setup_model(cfg, args, image, offset=(0, 0)):
     if args.model_errors:
         m.use_model_errors()
     st = m.final_setup()
-    if st != 0:
-        raise RuntimeError(f"FinalSetupForFitting returned {st}")
+    if st != 0:  # too few valid pixels, or non-finite weights (core/imfit_main.cpp:279-283)
+        raise SystemExit(f"*** ERROR: Failure in ModelObject::FinalSetupForFitting! ({m.last_error})")
     return m
 
 
-def run(argv=None, out=sys.stdout):
-    """The fitting command; returns (fitted parameters, statistic)."""
+def _matching_image(path, kind, image, image_path):
+    """A noise or mask image, which must have the data image's dimensions
+    (GetImageAndCheckSize, core/getimages.cpp:34-58)."""
+    arr = fitsio.read_image(path)[0]
+    if arr.shape != image.shape:
+        raise SystemExit(f"*** ERROR: Dimensions of {kind} image ({path}: {arr.shape[1]} columns, {arr.shape[0]} "
+                         f"rows)\ndo not match dimensions of data image ({image.shape[1]} columns, "
+                         f"{image.shape[0]} rows)!")
+    return arr
+
+
+def information_criteria(statistic, n_free, n_valid):
+    """Bias-corrected AIC (Burnham & Anderson 2002, p. 66) and BIC of a fit,
+    the statistic standing for -2 ln L (core/statistics.cpp:139-175)."""
+    k = float(n_free)
+    aic = statistic + 2.0 * k + 2.0 * k * (k + 1.0) / (n_valid - k - 1.0)
+    bic = statistic + k * math.log(n_valid)
+    return aic, bic
+
+
+def parameter_errors(m, p, fixed, lower, upper):
+    """One-sigma parameter errors as mpfit reports them after an LM fit
+    (solvers/mpfit.cpp:1016-1047): the square roots of the diagonal of the
+    inverse of J^T J over the free parameters, J the Jacobian of the
+    deviates; a parameter held at one of its limits, fixed, or without
+    influence on the deviates (a zero column) gets 0.  None when the model
+    has no J^T J (3-D line-of-sight components)."""
+    try:
+        A = m.jtwj(p)[1]
+    except ImfitError:
+        return None
+    p = np.asarray(p, dtype=float)
+    limited = ~np.isnan(lower)
+    pegged = limited & ((p == lower) | (p == upper))
+    use = (np.asarray(fixed) == 0) & ~pegged & (np.diag(A) > 0)
+    err = np.zeros(len(p))
+    if np.any(use):
+        cov = np.linalg.inv(A[np.ix_(use, use)])
+        err[use] = np.sqrt(np.clip(np.diag(cov), 0.0, None))
+    return err
+
+
+def run(argv=None, out=sys.stdout, details=None):
+    """The fitting command; returns (fitted parameters, statistic).  A dict
+    passed as details receives n_valid, n_free, aic, bic and, after an LM
+    fit, the parameter errors."""
+    details = {} if details is None else details
     args = build_parser().parse_args(argv)
     try:
         cfg = read_config(args.config)
@@ -241,9 +286,15 @@ def run(argv=None, out=sys.stdout):
     p_section = p
     p = p + off  # reported in the full image's coordinates
     dof = m.n_valid - n_free
+    aic, bic = information_criteria(s, n_free, m.n_valid)
+    errors = None
+    if not (args.de or args.de_lhs or args.nm):
+        errors = parameter_errors(m, p_section, cfg.fixed, cfg_lower, cfg_upper)
+    details.update(n_valid=m.n_valid, n_free=n_free, aic=aic, bic=bic, errors=errors)
     out.write(f"fit statistic = {s:.6f}, reduced = {s / dof:.6f} ({dof} degrees of freedom)\n")
-    for name, v in zip(cfg.param_names, p):
-        out.write(f"  {name:8s} {v:.6f}\n")
+    out.write(f"AIC = {aic:f}, BIC = {bic:f}\n")
+    for k, (name, v) in enumerate(zip(cfg.param_names, p)):
+        out.write(f"  {name:8s} {v:.6f}" + (f"  +/- {errors[k]:.6g}" if errors is not None else "") + "\n")
     if args.save_params:
         with open(args.save_params, "w") as f:
             f.write(format_params(cfg, p, s))

@@ -1,26 +1,32 @@
 // lm.cpp -- Levenberg-Marquardt on the normal equations (FP64, host).
 //
-// One iteration: A = J^T J and b = J^T dev at x come from the evaluator (the
-// GPU's forward-mode JtWJ pass); the damped system
-//   (A + lambda diag(A)) d = -b
-// is solved by Cholesky over the free parameters that have an effect and are
-// not held at a limit by the sign of the gradient; the trial point is clamped
-// to the limits and accepted when it lowers S (or, below the evaluator's noise
-// floor, when it does not raise it).  lambda follows Nielsen's rule (Nielsen
-// 1999, IMM-REP-1999-05): on success lambda *= max(1/3, 1 - (2 rho - 1)^3)
-// with rho the ratio of actual to predicted reduction, on failure lambda *= nu,
-// nu doubling with each consecutive failure.  Stall stop: when kStallRounds
-// consecutive rounds have not lowered the best S by more than noise/10
-// relative, the iteration stops (the remaining progress is below what the
-// FP32-evaluated S can resolve; typically a degenerate valley or a limit).
-// Convergence: the undamped Gauss-Newton step predicts a relative reduction
-// of S of at most ftol (the ftol test of solvers/mpfit.cpp:943-956); that
-// step is then taken.  The test is made on the Gauss-Newton prediction, which
-// rests on J^T J and J^T dev (smooth in the parameters), rather than on
-// differences of S between steps: the FP32-evaluated S carries rounding
-// jitter of about 1e-7 relative, so near the minimum those differences say
-// nothing, and a heavily damped step's tiny predicted reduction is no sign of
-// convergence either.
+// The iteration is mpfit's (solvers/mpfit.cpp:551-1060, MINPACK lmder after
+// More 1978, "The Levenberg-Marquardt algorithm: implementation and theory"),
+// restated on the normal equations that the evaluator supplies (A = J^T J and
+// b = J^T dev at x, from the GPU's forward-mode JtWJ pass) instead of a QR
+// factorisation of J:
+//  * scaling D = the running maximum of J's column norms sqrt(A_jj); trust
+//    radius delta, initially 100 ||D x|| (mpfit's stepfactor), on the first
+//    iteration cut to the first step's length;
+//  * step p = -(A + par D^2)^-1 b with the damping par chosen by MINPACK's
+//    lmpar iteration so that ||D p|| is within 10 % of delta (par = 0 when the
+//    Gauss-Newton step is shorter), over the free parameters that have an
+//    effect and are not pegged (at a limit with the gradient pointing out);
+//  * limits (mpfit.cpp:802-835): the whole step is scaled by the largest
+//    alpha <= 1 that keeps every parameter within its limits, and the
+//    parameter that sets alpha lands exactly on its limit;
+//  * ratio of actual to predicted reduction, delta and par updated by
+//    lmder's rules, the step accepted when the ratio is >= 1e-4;
+//  * stops: mpfit's ftol test on the actual and predicted reductions, its
+//    xtol test (delta <= 1e-10 ||D x||), the iteration limit.
+// Two additions for an evaluator whose statistic is FP32-summed per CTA and
+// so carries rounding jitter of about 1e-7 relative (differences of S below
+// that say nothing): convergence is also declared when the undamped
+// Gauss-Newton step predicts a relative reduction of at most ftol -- that
+// step is then taken if it does not raise S beyond the jitter -- and a step
+// whose predicted reduction is below the jitter is accepted when S does not
+// rise beyond it.  Stall stop: when kStallRounds consecutive rounds have not
+// lowered the best S by more than the jitter / 10, the iteration stops.
 #include "lm.h"
 
 #include <algorithm>
@@ -125,19 +131,6 @@ inline bool has_effect(double Ajj, double xj, double S) {
   return Ajj > 0.0 && std::isfinite(Ajj) && Ajj * s * s > 1e-12 * S;
 }
 
-// Nielsen's damping update after a step with gain ratio rho (success) or a failure.
-inline void nielsen(bool success, double rho, double &lambda, double &nu) {
-  if (success) {
-    const double t = 2.0 * rho - 1.0;
-    lambda *= std::max(1.0 / 3.0, 1.0 - t * t * t);
-    lambda = std::max(lambda, 1e-15);
-    nu = 2.0;
-  } else {
-    lambda *= nu;
-    nu *= 2.0;
-  }
-}
-
 bool lm_step(int n, const double *A, const double *b, const std::vector<int> &act, double lam,
              std::vector<double> &d) {
   const int na = (int)act.size();
@@ -177,303 +170,342 @@ bool lm_step(int n, const double *A, const double *b, const std::vector<int> &ac
   return true;
 }
 
-}  // namespace
+// ----------------------------------------------------------------- trust region
+constexpr double kDwarf = 2.2250738585072014e-308;  // smallest normal double
+constexpr double kStepFactor = 100.0;                // mpfit's default stepfactor
+constexpr double kXtol = 1e-10;                      // mpfit's default xtol
 
-int lm_minimize(int n, double *x, const int *fixed, const double *lower, const double *upper,
-                const LMSettings &set, const JtwjEval &eval, LMResult &res) {
-  res = LMResult{};
-  auto limited = [&](int j) { return lower && upper && lower[j] < upper[j]; };
-  auto clampv = [&](int j, double v) {
-    if (!limited(j)) return v;
-    return std::min(std::max(v, lower[j]), upper[j]);
-  };
-  std::vector<int> freeIdx;
-  for (int j = 0; j < n; j++) {
-    if (!(fixed && fixed[j])) freeIdx.push_back(j);
-    x[j] = clampv(j, x[j]);
+// Cholesky factor of (A + par D^2) over the active parameters (D: one entry
+// per active parameter); false if not positive definite.
+bool damped_factor(int n, const double *A, const std::vector<int> &act, const std::vector<double> &D, double par,
+                   std::vector<double> &L) {
+  const int na = (int)act.size();
+  L.assign((size_t)na * na, 0.0);
+  for (int i = 0; i < na; i++) {
+    for (int k = 0; k < na; k++) L[(size_t)i * na + k] = A[(size_t)act[i] * n + act[k]];
+    L[(size_t)i * na + i] += par * D[i] * D[i];
   }
-  std::vector<double> A((size_t)n * n), b(n), At((size_t)n * n), bt(n), xt(n);
-  double S = 0.0;
-  int st = eval(x, &S, A.data(), b.data());
-  res.nEval = 1;
-  if (st) return res.status = st;
-  res.statInit = res.stat = S;
-  if (freeIdx.empty()) return res.status = 1;
-  double lambda = 1e-3, nu = 2.0;
-
-  // active free parameters: with an effect on S (A_jj > 0) and not held at a
-  // limit by the gradient's sign
-  auto active = [&]() {
-    std::vector<int> act;
-    for (int j : freeIdx) {
-      if (!has_effect(A[(size_t)j * n + j], x[j], S)) continue;
-      if (limited(j)) {
-        if (x[j] <= lower[j] && b[j] > 0.0) continue;  // S decreases towards smaller x_j
-        if (x[j] >= upper[j] && b[j] < 0.0) continue;
-      }
-      act.push_back(j);
-    }
-    return act;
-  };
-  auto solve = [&](const std::vector<int> &act, double lam, std::vector<double> &d) {
-    return lm_step(n, A.data(), b.data(), act, lam, d);
-  };
-  // trial point and the quadratic model's relative reduction for it; clamped
-  // reports whether a limit cut the step
-  bool clamped = false;
-  auto trial = [&](const std::vector<int> &act, const std::vector<double> &d) {
-    clamped = false;
-    for (int j = 0; j < n; j++) xt[j] = x[j];
-    for (size_t i = 0; i < act.size(); i++) {
-      xt[act[i]] = clampv(act[i], x[act[i]] + d[i]);
-      if (xt[act[i]] != x[act[i]] + d[i]) clamped = true;
-    }
-    double bd = 0.0, dad = 0.0;
-    for (int i = 0; i < n; i++) {
-      const double di = xt[i] - x[i];
-      if (di == 0.0) continue;
-      bd += b[i] * di;
-      for (int k = 0; k < n; k++) dad += di * A[(size_t)i * n + k] * (xt[k] - x[k]);
-    }
-    return -(2.0 * bd + dad) / S;
-  };
-
-  double sBest = S;
-  int stall = 0;
-  for (int it = 0; it < set.maxIter; it++) {
-    res.nIter = it + 1;
-    if (S < sBest * (1.0 - 0.1 * set.noise)) {
-      sBest = S;
-      stall = 0;
-    } else if (++stall >= kStallRounds) {
-      return res.status = 4;
-    }
-    const std::vector<int> act = active();
-    if (act.empty()) return res.status = 1;
-    std::vector<double> d;
-    // convergence: the undamped Gauss-Newton step gains at most ftol
-    if (solve(act, 0.0, d)) {
-      const double pred0 = trial(act, d);
-      if (pred0 <= set.ftol && !clamped) {
-        st = eval(xt.data(), &res.stat, At.data(), bt.data());
-        res.nEval++;
-        if (st) return res.status = st;
-        if (res.stat <= S * (1.0 + set.noise)) {
-          for (int j = 0; j < n; j++) x[j] = xt[j];
-        } else {
-          res.stat = S;
-        }
-        return res.status = 1;
-      }
-    }
-    for (;;) {
-      if (!solve(act, lambda, d)) {
-        nielsen(false, 0.0, lambda, nu);
-        if (lambda > 1e16) return res.status = 3;
-        continue;
-      }
-      const double pred = trial(act, d);
-      double St;
-      st = eval(xt.data(), &St, At.data(), bt.data());
-      res.nEval++;
-      if (st) return res.status = st;
-      const bool better = std::isfinite(St) && (St < S || (pred < set.noise && St <= S * (1.0 + set.noise)));
-      if (better) {
-        const double rho = (pred > set.noise) ? (S - St) / (pred * S) : 1.0;
-        for (int j = 0; j < n; j++) x[j] = xt[j];
-        S = St;
-        res.stat = S;
-        A.swap(At);
-        b.swap(bt);
-        nielsen(true, rho, lambda, nu);
-        break;
-      }
-      nielsen(false, 0.0, lambda, nu);
-      if (lambda > 1e16) return res.status = 3;
-    }
-  }
-  return res.status = 5;
+  return cholesky(na, L);
 }
 
-}  // namespace imfit
+// MINPACK's lmpar on the normal equations: the damping par >= 0 and the step
+// p (one entry per active parameter) for which ||D p|| is within 10 % of
+// delta, or par = 0 and the Gauss-Newton step when that is shorter than
+// 1.1 delta.  par enters as the previous value (the iteration's start) and
+// leaves as the one used.  False when no step can be formed.
+bool tr_step(int n, const double *A, const double *b, const std::vector<int> &act, const std::vector<double> &D,
+             double delta, double &par, std::vector<double> &p) {
+  const int na = (int)act.size();
+  std::vector<double> L, w(na), y(na), rhs(na);
+  for (int i = 0; i < na; i++) rhs[i] = -b[act[i]];
+  auto dnorm = [&](const std::vector<double> &v) {
+    double t = 0.0;
+    for (int i = 0; i < na; i++) t += (D[i] * v[i]) * (D[i] * v[i]);
+    return std::sqrt(t);
+  };
+  auto wnorm2 = [&](const std::vector<double> &v, double dx) {  // w^T (L L^T)^-1 w, w = D^2 v / dx
+    for (int i = 0; i < na; i++) w[i] = D[i] * D[i] * v[i] / dx;
+    chol_solve(na, L, w.data(), y.data());
+    double t = 0.0;
+    for (int i = 0; i < na; i++) t += w[i] * y[i];
+    return t;
+  };
+  const bool gn = lm_step(n, A, b, act, 0.0, p);
+  double dxnorm = gn ? dnorm(p) : INFINITY;
+  double fp = dxnorm - delta;
+  if (gn && fp <= 0.1 * delta) {
+    par = 0.0;
+    return true;
+  }
+  double parl = 0.0;
+  if (gn && damped_factor(n, A, act, D, 0.0, L)) {  // full rank: Newton's lower bound at par = 0
+    const double t2 = wnorm2(p, dxnorm);
+    if (t2 > 0.0 && std::isfinite(t2)) parl = fp / (delta * t2);
+  }
+  double gnorm = 0.0;
+  for (int i = 0; i < na; i++) gnorm += (b[act[i]] / D[i]) * (b[act[i]] / D[i]);
+  gnorm = std::sqrt(gnorm);
+  double paru = gnorm / delta;
+  if (paru == 0.0) paru = kDwarf / std::min(delta, 0.1);
+  par = std::min(std::max(par, parl), paru);
+  if (par == 0.0) par = gn ? gnorm / dxnorm : paru;
+  p.assign(na, 0.0);
+  bool have = false;
+  for (int iter = 0; iter < 10; iter++) {
+    if (par == 0.0) par = std::max(kDwarf, 0.001 * paru);
+    if (!damped_factor(n, A, act, D, par, L)) {
+      parl = par;
+      par *= 10.0;
+      continue;
+    }
+    chol_solve(na, L, rhs.data(), p.data());
+    have = true;
+    dxnorm = dnorm(p);
+    const double prev = fp;
+    fp = dxnorm - delta;
+    if (std::fabs(fp) <= 0.1 * delta || (parl == 0.0 && fp <= prev && prev < 0.0) || iter == 9) break;
+    const double parc = fp / (delta * wnorm2(p, dxnorm));
+    if (fp > 0.0) parl = std::max(parl, par);
+    if (fp < 0.0) paru = std::min(paru, par);
+    par = std::max(parl, par + parc);
+  }
+  return have;
+}
 
-namespace imfit {
-
-namespace {
-
-// One problem's state in the lockstep batch.
-struct LMState {
-  std::vector<double> A, b;
-  double S = 0.0, lambda = 1e-3, nu = 2.0;
-  double sBest = 0.0;
-  int stall = 0;
-  bool done = false, finalStep = false;
-  double pred = 0.0;
+// One problem's state.
+struct TrState {
+  std::vector<double> A, b, diag;  // diag: D over all n parameters
+  double S = 0.0, delta = 0.0, par = 0.0, xnorm = 0.0, sBest = 0.0;
+  int stall = 0, accepted = 0;
+  bool started = false, done = false, finalStep = false;
   std::vector<int> act;
-  std::vector<double> step;  // trial - x over all n
+  double pred = 0.0, dirder = 0.0, pnorm = 0.0;
 };
+
+// Limits of one problem (lower/upper: n entries or null).
+struct Limits {
+  const double *lo, *hi;
+  bool limited(int j) const { return lo && hi && lo[j] < hi[j]; }
+  double clamp(int j, double v) const { return limited(j) ? std::min(std::max(v, lo[j]), hi[j]) : v; }
+};
+
+// Next trial point t of problem q at x, or the problem's end (q.done, status
+// returned; 0 while running).
+int propose(TrState &q, int n, const double *x, double *t, const std::vector<int> &freeIdx, const Limits &lim,
+            const LMSettings &set) {
+  for (int j = 0; j < n; j++) t[j] = x[j];
+  if (q.S < q.sBest * (1.0 - 0.1 * set.noise)) {
+    q.sBest = q.S;
+    q.stall = 0;
+  } else if (++q.stall >= kStallRounds) {
+    q.done = true;
+    return 4;
+  }
+  // active parameters: free, with an effect, not pegged by the gradient's sign
+  q.act.clear();
+  for (int j : freeIdx) {
+    if (!has_effect(q.A[(size_t)j * n + j], x[j], q.S)) continue;
+    if (lim.limited(j)) {
+      if (x[j] <= lim.lo[j] && q.b[j] > 0.0) continue;  // S decreases towards smaller x_j
+      if (x[j] >= lim.hi[j] && q.b[j] < 0.0) continue;
+    }
+    q.act.push_back(j);
+  }
+  if (q.act.empty()) {
+    q.done = true;
+    return 1;
+  }
+  const int na = (int)q.act.size();
+  if (!q.started) {
+    q.diag.assign(n, 1.0);
+    for (int j = 0; j < n; j++) {
+      const double c = std::sqrt(std::max(q.A[(size_t)j * n + j], 0.0));
+      if (c > 0.0 && std::isfinite(c)) q.diag[j] = c;
+    }
+    double xn = 0.0;
+    for (int j : q.act) xn += (q.diag[j] * x[j]) * (q.diag[j] * x[j]);
+    q.xnorm = std::sqrt(xn);
+    q.delta = q.xnorm > 0.0 ? kStepFactor * q.xnorm : kStepFactor;
+    q.started = true;
+  } else {
+    for (int j : q.act) q.diag[j] = std::max(q.diag[j], std::sqrt(std::max(q.A[(size_t)j * n + j], 0.0)));
+  }
+  auto model = [&](const double *tt) {  // the quadratic model's relative reduction for t - x
+    double bd = 0.0, dad = 0.0;
+    for (int i = 0; i < n; i++) {
+      const double di = tt[i] - x[i];
+      if (di == 0.0) continue;
+      bd += q.b[i] * di;
+      for (int k = 0; k < n; k++) dad += di * q.A[(size_t)i * n + k] * (tt[k] - x[k]);
+    }
+    return -(2.0 * bd + dad) / q.S;
+  };
+  std::vector<double> p;
+  // convergence: the undamped Gauss-Newton step gains at most ftol
+  q.finalStep = false;
+  if (lm_step(n, q.A.data(), q.b.data(), q.act, 0.0, p)) {
+    bool clamped = false;
+    for (int k = 0; k < na; k++) {
+      const int j = q.act[k];
+      t[j] = lim.clamp(j, x[j] + p[k]);
+      if (t[j] != x[j] + p[k]) clamped = true;
+    }
+    if (!clamped && model(t) <= set.ftol) {
+      q.finalStep = true;
+      return 0;
+    }
+    for (int j = 0; j < n; j++) t[j] = x[j];
+  }
+  std::vector<double> D(na);
+  for (int k = 0; k < na; k++) D[k] = q.diag[q.act[k]];
+  if (!tr_step(n, q.A.data(), q.b.data(), q.act, D, q.delta, q.par, p)) {
+    q.done = true;
+    return 3;
+  }
+  // limits: scale the whole step; the parameter that sets alpha lands on its limit
+  double alpha = 1.0;
+  int hit = -1;
+  double hitVal = 0.0;
+  for (int k = 0; k < na; k++) {
+    const int j = q.act[k];
+    if (!lim.limited(j) || p[k] == 0.0) continue;
+    double a = 1.0;
+    if (p[k] < 0.0 && x[j] + p[k] < lim.lo[j]) a = (lim.lo[j] - x[j]) / p[k];
+    if (p[k] > 0.0 && x[j] + p[k] > lim.hi[j]) a = (lim.hi[j] - x[j]) / p[k];
+    if (a < alpha) {
+      alpha = std::max(a, 0.0);
+      hit = j;
+      hitVal = p[k] < 0.0 ? lim.lo[j] : lim.hi[j];
+    }
+  }
+  double pn = 0.0, pAp = 0.0;
+  for (int k = 0; k < na; k++) {
+    const int j = q.act[k];
+    p[k] *= alpha;
+    t[j] = lim.clamp(j, x[j] + p[k]);
+    pn += (D[k] * p[k]) * (D[k] * p[k]);
+  }
+  if (hit >= 0) t[hit] = hitVal;
+  for (int i = 0; i < na; i++)
+    for (int k = 0; k < na; k++) pAp += p[i] * q.A[(size_t)q.act[i] * n + q.act[k]] * p[k];
+  q.pnorm = std::sqrt(pn);
+  if (q.accepted == 0) q.delta = std::min(q.delta, q.pnorm);
+  const double t1 = std::max(pAp, 0.0) / q.S, t2 = alpha * q.par * q.pnorm * q.pnorm / q.S;
+  q.pred = t1 + 2.0 * t2;
+  q.dirder = -(t1 + t2);
+  return 0;
+}
+
+// Outcome of problem q's trial t (statistic St, At, bt there): accept or
+// reject, update delta and par, test for convergence.  Returns the final
+// status, or 0 while running.
+int settle(TrState &q, int n, double *x, const double *t, double St, const double *At, const double *bt,
+           const LMSettings &set) {
+  if (q.finalStep) {
+    q.done = true;
+    if (std::isfinite(St) && St <= q.S * (1.0 + set.noise)) {
+      for (int j = 0; j < n; j++) x[j] = t[j];
+      q.S = St;
+    }
+    return 1;
+  }
+  const bool finite = std::isfinite(St);
+  const double actred = (finite && 0.01 * St < q.S) ? 1.0 - St / q.S : -1.0;  // 0.1 fnorm1 < fnorm
+  const double ratio = q.pred != 0.0 ? actred / q.pred : 0.0;
+  if (ratio <= 0.25) {
+    double temp = actred >= 0.0 ? 0.5 : 0.5 * q.dirder / (q.dirder + 0.5 * actred);
+    if (!(0.01 * St < q.S) || temp < 0.1 || !std::isfinite(temp)) temp = 0.1;
+    q.delta = temp * std::min(q.delta, q.pnorm / 0.1);
+    q.par /= temp;
+  } else if (q.par == 0.0 || ratio >= 0.75) {
+    q.delta = q.pnorm / 0.5;
+    q.par *= 0.5;
+  }
+  const bool accept = finite && (ratio >= 1e-4 || (q.pred < set.noise && St <= q.S * (1.0 + set.noise)));
+  if (accept) {
+    for (int j = 0; j < n; j++) x[j] = t[j];
+    q.S = St;
+    std::copy(At, At + (size_t)n * n, q.A.begin());
+    std::copy(bt, bt + n, q.b.begin());
+    double xn = 0.0;
+    for (int j : q.act) xn += (q.diag[j] * x[j]) * (q.diag[j] * x[j]);
+    q.xnorm = std::sqrt(xn);
+    q.accepted++;
+  }
+  if (std::fabs(actred) <= set.ftol && q.pred <= set.ftol && 0.5 * ratio <= 1.0) {
+    q.done = true;
+    return 1;
+  }
+  if (q.delta <= kXtol * q.xnorm || !(q.delta > kDwarf)) {
+    q.done = true;
+    return 2;
+  }
+  if (q.accepted >= set.maxIter) {
+    q.done = true;
+    return 5;
+  }
+  return 0;
+}
 
 }  // namespace
 
 int lm_minimize_batch(int B, int n, double *X, const int *fixed, const double *lower, const double *upper,
                       const LMSettings &set, const JtwjBatchEval &eval, LMResult *res) {
-  auto limited = [&](int i, int j) { return lower && upper && lower[(size_t)i * n + j] < upper[(size_t)i * n + j]; };
-  auto clampv = [&](int i, int j, double v) {
-    if (!limited(i, j)) return v;
-    return std::min(std::max(v, lower[(size_t)i * n + j]), upper[(size_t)i * n + j]);
+  auto limits = [&](int i) {
+    return Limits{lower ? lower + (size_t)i * n : nullptr, upper ? upper + (size_t)i * n : nullptr};
   };
   std::vector<int> freeIdx;
   for (int j = 0; j < n; j++)
     if (!(fixed && fixed[j])) freeIdx.push_back(j);
   for (int i = 0; i < B; i++) {
     res[i] = LMResult{};
-    for (int j = 0; j < n; j++) X[(size_t)i * n + j] = clampv(i, j, X[(size_t)i * n + j]);
+    const Limits lim = limits(i);
+    for (int j = 0; j < n; j++) X[(size_t)i * n + j] = lim.clamp(j, X[(size_t)i * n + j]);
   }
   std::vector<double> S((size_t)B), A((size_t)B * n * n), b((size_t)B * n), T((size_t)B * n);
   std::vector<unsigned char> live((size_t)B, 1);
   int st = eval(X, live.data(), S.data(), A.data(), b.data());
   if (st) return st;
-  std::vector<LMState> ps(B);
+  std::vector<TrState> ps(B);
   for (int i = 0; i < B; i++) {
-    ps[i].S = S[i];
-    ps[i].sBest = S[i];
-    ps[i].A.assign(A.begin() + (size_t)i * n * n, A.begin() + (size_t)(i + 1) * n * n);
-    ps[i].b.assign(b.begin() + (size_t)i * n, b.begin() + (size_t)(i + 1) * n);
+    TrState &q = ps[i];
+    q.S = q.sBest = S[i];
+    q.A.assign(A.begin() + (size_t)i * n * n, A.begin() + (size_t)(i + 1) * n * n);
+    q.b.assign(b.begin() + (size_t)i * n, b.begin() + (size_t)(i + 1) * n);
     res[i].statInit = res[i].stat = S[i];
     res[i].nEval = 1;
+    res[i].nIter = 1;
     if (freeIdx.empty()) {
-      ps[i].done = true;
+      q.done = true;
       res[i].status = 1;
     }
   }
-  // damped (lam > 0) or Gauss-Newton (lam = 0) step of problem i over its active set
-  auto solve = [&](int i, double lam, std::vector<double> &d) {
-    return lm_step(n, ps[i].A.data(), ps[i].b.data(), ps[i].act, lam, d);
-  };
-  // trial vector of problem i into T, returns the model's relative reduction;
-  // clamped reports whether a limit cut the step
-  bool clamped = false;
-  auto trial = [&](int i, const std::vector<double> &d) {
-    LMState &q = ps[i];
-    const double *x = X + (size_t)i * n;
-    double *t = T.data() + (size_t)i * n;
-    clamped = false;
-    for (int j = 0; j < n; j++) t[j] = x[j];
-    for (size_t k = 0; k < q.act.size(); k++) {
-      t[q.act[k]] = clampv(i, q.act[k], x[q.act[k]] + d[k]);
-      if (t[q.act[k]] != x[q.act[k]] + d[k]) clamped = true;
-    }
-    double bd = 0.0, dad = 0.0;
-    for (int r = 0; r < n; r++) {
-      const double dr = t[r] - x[r];
-      if (dr == 0.0) continue;
-      bd += q.b[r] * dr;
-      for (int c = 0; c < n; c++) dad += dr * q.A[(size_t)r * n + c] * (t[c] - x[c]);
-    }
-    return -(2.0 * bd + dad) / q.S;
-  };
-
-  for (int it = 0; it < set.maxIter; it++) {
+  // rounds: one trial per running problem, evaluated together; a rejected
+  // trial costs a round but no iteration (as mpfit's inner loop)
+  const long maxRounds = 20L * set.maxIter + 100;
+  for (long round = 0; round < maxRounds; round++) {
     bool any = false;
     for (int i = 0; i < B; i++) {
-      LMState &q = ps[i];
+      TrState &q = ps[i];
       double *t = T.data() + (size_t)i * n;
-      for (int j = 0; j < n; j++) t[j] = X[(size_t)i * n + j];
-      if (q.done) continue;
-      if (q.S < q.sBest * (1.0 - 0.1 * set.noise)) {
-        q.sBest = q.S;
-        q.stall = 0;
-      } else if (++q.stall >= kStallRounds) {
-        q.done = true;
-        res[i].status = 4;
+      const double *x = X + (size_t)i * n;
+      if (q.done) {
+        for (int j = 0; j < n; j++) t[j] = x[j];
+        continue;
+      }
+      const int s = propose(q, n, x, t, freeIdx, limits(i), set);
+      if (q.done) {
+        res[i].status = s;
         continue;
       }
       any = true;
-      res[i].nIter = it + 1;
-      // active parameters: free and not held at a limit by the gradient's sign
-      q.act.clear();
-      for (int j : freeIdx) {
-        const double xj = X[(size_t)i * n + j];
-        if (!has_effect(q.A[(size_t)j * n + j], xj, q.S)) continue;
-        if (limited(i, j)) {
-          if (xj <= lower[(size_t)i * n + j] && q.b[j] > 0.0) continue;
-          if (xj >= upper[(size_t)i * n + j] && q.b[j] < 0.0) continue;
-        }
-        q.act.push_back(j);
-      }
-      if (q.act.empty()) {
-        q.done = true;
-        res[i].status = 1;
-        continue;
-      }
-      std::vector<double> d;
-      q.finalStep = false;
-      if (solve(i, 0.0, d)) {
-        const double pred0 = trial(i, d);
-        if (pred0 <= set.ftol && !clamped) {
-          q.finalStep = true;
-          continue;
-        }
-      }
-      bool ok = false;
-      while (!ok) {
-        ok = solve(i, q.lambda, d);
-        if (!ok) {
-          nielsen(false, 0.0, q.lambda, q.nu);
-          if (q.lambda > 1e16) break;
-        }
-      }
-      if (!ok) {
-        for (int j = 0; j < n; j++) t[j] = X[(size_t)i * n + j];
-        q.done = true;
-        res[i].status = 3;
-        continue;
-      }
-      q.pred = trial(i, d);
     }
     if (!any) break;
     for (int i = 0; i < B; i++) live[i] = ps[i].done ? 0 : 1;
     st = eval(T.data(), live.data(), S.data(), A.data(), b.data());
     if (st) return st;
     for (int i = 0; i < B; i++) {
-      LMState &q = ps[i];
+      TrState &q = ps[i];
       if (q.done) continue;
       res[i].nEval++;
-      double *x = X + (size_t)i * n;
-      const double *t = T.data() + (size_t)i * n;
-      const double St = S[i];
-      const bool better = std::isfinite(St) &&
-                          (St < q.S || ((q.finalStep || q.pred < set.noise) && St <= q.S * (1.0 + set.noise)));
-      if (q.finalStep) {
-        if (better) {
-          for (int j = 0; j < n; j++) x[j] = t[j];
-          q.S = St;
-        }
-        res[i].stat = q.S;
-        res[i].status = 1;
-        q.done = true;
-        continue;
-      }
-      if (better) {
-        const double rho = (q.pred > set.noise) ? (q.S - St) / (q.pred * q.S) : 1.0;
-        for (int j = 0; j < n; j++) x[j] = t[j];
-        q.S = St;
-        res[i].stat = St;
-        q.A.assign(A.begin() + (size_t)i * n * n, A.begin() + (size_t)(i + 1) * n * n);
-        q.b.assign(b.begin() + (size_t)i * n, b.begin() + (size_t)(i + 1) * n);
-        nielsen(true, rho, q.lambda, q.nu);
-      } else {
-        nielsen(false, 0.0, q.lambda, q.nu);
-        if (q.lambda > 1e16) {
-          q.done = true;
-          res[i].status = 3;
-        }
-      }
+      const int s = settle(q, n, X + (size_t)i * n, T.data() + (size_t)i * n, S[i], A.data() + (size_t)i * n * n,
+                           b.data() + (size_t)i * n, set);
+      res[i].stat = q.S;
+      res[i].nIter = q.accepted + 1;
+      if (q.done) res[i].status = s;
     }
   }
   for (int i = 0; i < B; i++)
     if (!ps[i].done) res[i].status = 5;
   return 0;
+}
+
+int lm_minimize(int n, double *x, const int *fixed, const double *lower, const double *upper,
+                const LMSettings &set, const JtwjEval &eval, LMResult &res) {
+  JtwjBatchEval one = [&eval](const double *X, const unsigned char *active, double *S, double *A, double *b) {
+    return active[0] ? eval(X, S, A, b) : 0;
+  };
+  return lm_minimize_batch(1, n, x, fixed, lower, upper, set, one, &res);
 }
 
 }  // namespace imfit

@@ -19,8 +19,8 @@ struct LMSettings {
 };
 
 struct LMResult {
-  int status = 0;        // 1 ftol, 3 damping exhausted, 4 stalled below the S noise, 5 iteration limit, <0 error
-  int nIter = 0;
+  int status = 0;        // 1 ftol, 2 xtol, 3 no step, 4 stalled below the S noise, 5 iteration limit, <0 error
+  int nIter = 0;         // accepted steps + 1 (mpfit's niter)
   int nEval = 0;
   double stat = 0.0;     // S at the returned parameters (from the evaluator)
   double statInit = 0.0;

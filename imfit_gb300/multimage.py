@@ -20,13 +20,11 @@ d(global parameters); the LM driver is the library's own
 (imfit_MinimizeNormalEquations).  Per-image (non-global) functions are not
 supported.
 """
-import ctypes
 from dataclasses import dataclass, field
 
 import numpy as np
 
-from . import NORMAL_EQ_FN as _NORMAL_EQ
-from . import ModelObject, load_library
+from . import ModelObject
 
 N_IMAGE_PARAMS = 5
 IMAGE_PARAM_NAMES = ["PIXEL_SCALE", "IMAGE_PA", "FLUX_SCALE", "X0", "Y0"]
@@ -229,42 +227,8 @@ class MultiImageModel:
     def fit_lm(self, params, fixed=None, lower=None, upper=None, ftol=1e-8, max_iter=0):
         """Levenberg-Marquardt on the summed normal equations with the library's
         driver (the same one imfit_FitLM runs)."""
-        lib = load_library()
-        n = self.n_params
-        x = np.array(params, dtype=float)
-        fx = (ctypes.c_int * n)(*([0] * n if fixed is None else [int(v) for v in fixed]))
-        fx = ctypes.cast(fx, ctypes.POINTER(ctypes.c_int))
-        lo = np.ascontiguousarray(lower, dtype=float) if lower is not None else None
-        hi = np.ascontiguousarray(upper, dtype=float) if upper is not None else None
-        DP = ctypes.POINTER(ctypes.c_double)
-        errors = []
-
-        @_NORMAL_EQ
-        def cb(xp, sp, ap, bp, user):
-            try:
-                xv = np.ctypeslib.as_array(xp, shape=(n,)).copy()
-                s, A, b = self.jtwj(xv)
-                sp[0] = s
-                np.ctypeslib.as_array(ap, shape=(n * n,))[:] = A.ravel()
-                np.ctypeslib.as_array(bp, shape=(n,))[:] = b
-                return 0
-            except Exception as e:  # reported after the driver returns
-                errors.append(e)
-                return -1
-
-        fn = lib.imfit_MinimizeNormalEquations
-        stat = ctypes.c_double()
-        it, nev, st = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
-        rc = fn(n, x.ctypes.data_as(DP), fx,
-                                               lo.ctypes.data_as(DP) if lo is not None else None,
-                                               hi.ctypes.data_as(DP) if hi is not None else None, ftol,
-                                               int(max_iter), cb, None, ctypes.byref(stat), ctypes.byref(it),
-                                               ctypes.byref(nev), ctypes.byref(st))
-        if errors:
-            raise errors[0]
-        if rc != 0:
-            raise RuntimeError(lib.imfit_LastError(None).decode())
-        return dict(params=x, statistic=stat.value, niter=it.value, nev=nev.value, status=st.value)
+        from . import minimize_normal_equations
+        return minimize_normal_equations(self.jtwj, params, fixed, lower, upper, ftol, max_iter)
 
 
 

@@ -206,15 +206,18 @@ int imfit_GetJacobian(imfit_model_t m, const double *params, double *fjac, doubl
 int imfit_BatchJtWJDevice(imfit_model_t m, int nBatch, const double *d_params, double *d_statistics,
                           double *d_jtj, double *d_jtdev);
 /* Levenberg-Marquardt fit (FP64 normal-equation solve on the host, JtWJ from
- * imfit_GetJtWJ).  params: start values in, fitted values out.  fixed (may be
+ * imfit_GetJtWJ): mpfit's trust-region iteration (solvers/mpfit.cpp:551-1060:
+ * column-norm scaling, lmpar damping, whole-step scaling at limits, its ftol
+ * and xtol tests).  params: start values in, fitted values out.  fixed (may be
  * NULL): nonzero = held fixed.  lower/upper (may be NULL): limits, used where
  * lower < upper.  ftol: relative-reduction tolerance (the reference's default
  * is 1e-8, core/definitions.h:61); maxIter <= 0 selects 1000
  * (solvers/levmar_fit.cpp:38).  Outputs (each may be NULL): the fast-path
  * statistic at the result, iterations, JtWJ evaluations, and a status
- * (1 ftol, 3 no further reduction at FP32 precision, 4 stalled: no progress
- * above the FP32 noise of the statistic for 20 rounds, 5 iteration
- * limit).  Returns 0 or a negative IMFIT_E_* code. */
+ * (1 ftol, 2 xtol: trust radius below 1e-10 of the scaled parameter norm,
+ * 3 no step can be formed, 4 stalled: no progress above the FP32 noise of
+ * the statistic for 20 rounds, 5 iteration limit).  Returns 0 or a
+ * negative IMFIT_E_* code. */
 int imfit_FitLM(imfit_model_t m, double *params, const int *fixed, const double *lower, const double *upper,
                 double ftol, int maxIter, double *statistic, int *nIter, int *nEval, int *status);
 /* Levenberg-Marquardt on nBatch problems at once (lockstep: one batched JtWJ

@@ -2,7 +2,8 @@
 
 Run in a checkout that has the reference at /root/reference (or
 IMFIT_REFERENCE_DIR):  python tests/golden/make_golden.py [part ...]
-(parts: n3073 makeimage ic3478 pointsource mcmc multimfit makemultimages small_case; all by default)
+(parts: n3073 makeimage ic3478 pointsource mcmc multimfit makemultimages small_case
+imfit_regressions; all by default)
 
 Outputs (all small .npz files next to this script):
   n3073.npz          the reference regression inputs tests/n3073rss_small.fits,
@@ -42,7 +43,18 @@ Outputs (all small .npz files next to this script):
   small_case.npz     the reference's own outputs (oracle/_ref) for
                      imfit_gb300.workloads.small_case: model images, deviates and
                      statistics for chi^2 / Cash / PMLR.
+  imfit_regressions.npz
+                     inputs (images as stored, configuration files as text) and
+                     printed results of the reference's imfit regression runs
+                     do_imfit_tests:66, 87, 89, 97, 121-124, 147-149, 165-178
+                     (imfit_textout2, 3e, 3e2, 4b, 5a/5b/5c_tail, 6, 6b, 7a-7f,
+                     8a; the linux_x86_64 copies where the reference keeps
+                     per-platform outputs): per case the command's options, the
+                     best-fit values and printed errors, the printed statistic
+                     (or the one implied by the printed AIC), AIC, BIC, and the
+                     error line of the runs that stop with an error.
 """
+import re
 import os
 import sys
 
@@ -195,12 +207,103 @@ def small_case():
     np.savez_compressed(os.path.join(HERE, "small_case.npz"), **out)
 
 
+# (case, configuration, image, options with fixture file names, printed output)
+REGRESSIONS = [
+    ("2", "imfit_config_ic3478_64x64.dat", "ic3478rss_64x64.fits", ["--gain=4.725", "--readnoise=4.3", "--sky=130.1"],
+     "linux_x86_64/imfit_textout2"),
+    ("3e", "imfit_config_ic3478_64x64c.dat", "ic3478rss_64x64.fits", ["--noise=ic3478rss_64x64_sigma.fits"],
+     "linux_x86_64/imfit_textout3e"),
+    ("3e2", "imfit_config_ic3478_64x64c.dat", "ic3478rss_64x64.fits",
+     ["--noise=ic3478rss_64x64_variance.fits", "--errors-are-variances"], "linux_x86_64/imfit_textout3e2"),
+    ("4b", "imfit_config_n3073.dat", "n3073rss_small_cps.fits",
+     ["--mask", "n3073rss_small_mask.fits", "--psf", "psf_moffat_35_n4699z.fits", "--exptime=53.907456",
+      "--sky=2.8628692847238053"], "linux_x86_64/imfit_textout4b"),
+    ("5a", "config_imfit_poisson.dat", "testimage_poisson_lowsn20.fits", ["--cashstat", "--nm"],
+     "imfit_textout5a_tail"),
+    ("5b", "config_imfit_poisson.dat", "testimage_poisson_lowsn20.fits", ["--mlr", "--nm"], "imfit_textout5b_tail"),
+    ("5c", "config_imfit_poisson.dat", "testimage_poisson_lowsn20.fits", ["--mlr"], "imfit_textout5c_tail"),
+    ("6", "imfit_config_ic3478_64x64b.dat", "ic3478rss_64x64.fits", ["--mask", "totalmask_64x64.fits"],
+     "imfit_textout6"),
+    ("6b", "imfit_config_ic3478_64x64b.dat", "ic3478rss_64x64.fits", ["--mask", "n3073rss_small_mask.fits"],
+     "imfit_textout6b"),
+    ("7a", "config_3x3_flatsky.dat", "testimage_3x3_nan.fits", [], "imfit_textout7a"),
+    ("7b", "config_3x3_flatsky.dat", "testimage_3x3_ones.fits", ["--mask=testimage_3x3_mask-with-nan.fits"],
+     "imfit_textout7b"),
+    ("7c", "config_3x3_flatsky.dat", "testimage_3x3_ones.fits", ["--noise=testimage_3x3_nan.fits"],
+     "imfit_textout7c"),
+    ("7d", "config_3x3_flatsky.dat", "testimage_3x3_onezero.fits", [], "imfit_textout7d"),
+    ("7e", "config_3x3_flatsky.dat", "testimage_3x3_onezero.fits", ["--mask=mask_for_onezero.fits"],
+     "imfit_textout7e"),
+    ("7f", "config_imfit_2gauss_small.dat", "testimage_2gauss_psf.fits", ["--nm"], "imfit_textout7f"),
+    ("8a", "config_imfit_ptsource.dat", "psf_moffat_fwhm2.fits", ["--psf=psf_moffat_fwhm2_35x35.fits"],
+     "linux_x86_64/imfit_textout8a"),
+]
+
+
+def _parse_textout(path):
+    """Printed statistic, AIC, BIC, parameter names / values / errors (NaN
+    where none is printed) and the first ERROR line of an imfit printout."""
+    lines = open(path).read().splitlines()
+    res = dict(stat=np.nan, aic=np.nan, bic=np.nan, names=[], values=[], errors=[], error="")
+    start = None
+    for k, ln in enumerate(lines):
+        m = re.match(r"\s*(CHI-SQUARE|CASH STATISTIC|POISSON-MLR STATISTIC) = (\S+)", ln)
+        if m:
+            res["stat"] = float(m.group(2))
+        m = re.match(r"AIC = (\S+), BIC = (\S+)", ln)
+        if m:
+            res["aic"], res["bic"], start = float(m.group(1)), float(m.group(2)), k
+        if "ERROR" in ln and not res["error"]:
+            res["error"] = ln.strip()
+    if start is not None:
+        for ln in lines[start + 1:]:
+            if ln.startswith("Saving") or ln.startswith("(Elapsed"):
+                break
+            t = ln.split()
+            if not t or t[0] == "FUNCTION":
+                continue
+            res["names"].append(t[0])
+            res["values"].append(float(t[1]))
+            res["errors"].append(float(t[4]) if len(t) > 4 and t[2:4] == ["#", "+/-"] else np.nan)
+    return res
+
+
+def imfit_regressions():
+    t = os.path.join(REF, "tests")
+    cfg_dir = os.path.join(t, "imfit_reference")
+    out = {"cases": np.array([c[0] for c in REGRESSIONS])}
+    files = set()
+    for case, cfg, img, opts, textout in REGRESSIONS:
+        out[f"config__{cfg}"] = np.array(open(os.path.join(cfg_dir, cfg)).read())
+        files.add(img)
+        for o in opts:
+            v = o.split("=", 1)[1] if "=" in o else o
+            if v.endswith(".fits"):
+                files.add(v)
+        r = _parse_textout(os.path.join(cfg_dir, textout))
+        out[f"{case}__config"] = np.array(cfg)
+        out[f"{case}__image"] = np.array(img)
+        out[f"{case}__options"] = np.array(opts if opts else [""])
+        out[f"{case}__names"] = np.array(r["names"] if r["names"] else [""])
+        out[f"{case}__values"] = np.array(r["values"], dtype=float)
+        out[f"{case}__errors"] = np.array(r["errors"], dtype=float)
+        for k in ("stat", "aic", "bic"):
+            out[f"{case}__{k}"] = np.float64(r[k])
+        out[f"{case}__error"] = np.array(r["error"])
+    for f in sorted(files):
+        data, hdr = fits.read_image(os.path.join(t, f))
+        # float32 images as stored; integer masks and float64 images as float64
+        out[f"file__{f}"] = data.astype(np.float32) if int(hdr["BITPIX"]) == -32 else data
+    np.savez_compressed(os.path.join(HERE, "imfit_regressions.npz"), **out)
+
+
 if __name__ == "__main__":
     if not os.path.isdir(os.path.join(REF, "core")):
         sys.exit(f"reference checkout not found at {REF}")
     oracle.build_reference()
     parts = {"n3073": n3073, "makeimage": makeimage, "ic3478": ic3478, "pointsource": pointsource,
-             "mcmc": mcmc, "multimfit": multimfit, "makemultimages": makemultimages, "small_case": small_case}
+             "mcmc": mcmc, "multimfit": multimfit, "makemultimages": makemultimages, "small_case": small_case,
+             "imfit_regressions": imfit_regressions}
     for name in (sys.argv[1:] or parts):
         parts[name]()
     for f in sorted(os.listdir(HERE)):

@@ -128,3 +128,18 @@ def test_fits_image_sections(tmp_path):
     assert fits.image_offset(p + "[2:4,3:5]") == (1, 2) and fits.image_offset(p) == (0, 0)
     with pytest.raises(ValueError):
         fits.read_image(p + "[2:9,1:2]")
+
+
+def test_information_criteria_reproduce_printed_aic_bic():
+    """AIC (bias-corrected) and BIC from the printed statistic, the free
+    parameters and the valid pixels, as imfit prints them
+    (imfit_textout2: 7 free, 4096 pixels; imfit_textout8a: 3 free, 1600;
+    imfit_textout7a: 3 free, 8)."""
+    import os
+    import numpy as np
+    from imfit_gb300.cli import information_criteria
+    d = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "imfit_regressions.npz"))
+    for case, k, n in (("2", 7, 4096), ("3e", 6, 4096), ("8a", 3, 1600), ("7a", 3, 8)):
+        aic, bic = information_criteria(float(d[f"{case}__stat"]), k, n)
+        # the printed statistic is itself rounded to 1e-6
+        assert abs(aic - float(d[f"{case}__aic"])) <= 1.5e-6 and abs(bic - float(d[f"{case}__bic"])) <= 1.5e-6, case

@@ -183,7 +183,10 @@ def test_fast_los_with_a_point_source(gpu, oracle_mod):
     g = workloads.configure(gpu.ModelObject(), wl)
     o = workloads.configure(oracle_mod.OracleModel(), wl)
     p = truth * np.array([1.0, 1.0, 1.03, 0.99, 1.05, 0.96, 1.0, 1.04, 1.0, 1.0, 1.1])
-    p[[0, 8, 9]] += [0.3, -0.4, 0.25]
+    # centres off the pixel grid: with the point source's centre on a pixel
+    # centre every sample falls on a knot of the bicubic interpolant, where
+    # its second derivative jumps and central differences are biased
+    p[[0, 8, 9]] += [0.3, -0.37, 0.25]
     s, grad = g.statistic_and_gradient(p)
     so = o.get_fit_statistic(p)
     assert relerr(s, so) < 1e-5, (s, so)

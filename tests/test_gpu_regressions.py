@@ -1,0 +1,113 @@
+"""The reference's imfit regression runs (do_imfit_tests:66, 87, 89, 97,
+121-124, 147-149, 165-178) through the imfit-style command line on the GPU,
+against the printed outputs held in tests/golden/imfit_regressions.npz
+(imfit_textout2, 3e, 3e2, 4b, 5a-5c, 6, 6b, 7a-7f, 8a):
+
+* Levenberg-Marquardt runs: best-fit values within 0.05 of the printed
+  one-sigma errors (plus the printing's rounding), the statistic to its six
+  printed decimals, AIC and BIC as printed, and the parameter errors within
+  1 % of mpfit's (0 where mpfit reports 0: fixed, pegged at a limit, or
+  without influence on the model);
+* Nelder-Mead runs (the reference's NLopt simplex, stood in by scipy's): the
+  same minimum -- statistic within 2e-7 relative, values within 0.1 sigma
+  (sigma from an LM fit of the same case);
+* runs the reference stops with an error stop here with the same error."""
+import io
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+D = np.load(os.path.join(GOLDEN, "imfit_regressions.npz"))
+
+LM_CASES = ["2", "3e", "3e2", "4b", "5c", "7a", "7b", "7c", "7e", "8a"]
+NM_CASES = ["5a", "5b", "7f"]
+ERROR_CASES = {"6": "Failure in ModelObject::FinalSetupForFitting!",
+               "6b": "Dimensions of mask image",
+               "7d": "Failure in ModelObject::FinalSetupForFitting!"}
+
+
+def _args(tmp_path, case, drop=()):
+    """The case's command line with its fixture files written to tmp_path."""
+    from imfit_gb300 import fits
+
+    def path(name):
+        arr = D[f"file__{name}"]
+        out = tmp_path / name
+        if not out.exists():
+            fits.write_image(str(out), arr, bitpix=-32 if arr.dtype == np.float32 else -64)
+        return str(out)
+
+    cfg = str(D[f"{case}__config"])
+    (tmp_path / cfg).write_text(str(D[f"config__{cfg}"]))
+    args = [str(tmp_path / cfg), path(str(D[f"{case}__image"]))]
+    for o in (str(x) for x in D[f"{case}__options"]):
+        if not o or o in drop:
+            continue
+        if "=" in o and o.endswith(".fits"):
+            k, v = o.split("=", 1)
+            args.append(f"{k}={path(v)}")
+        elif o.endswith(".fits"):
+            args.append(path(o))
+        else:
+            args.append(o)
+    return args
+
+
+def _printed(case):
+    v, e = D[f"{case}__values"], D[f"{case}__errors"]
+    stat = float(D[f"{case}__stat"])
+    return v, e, stat, float(D[f"{case}__aic"]), float(D[f"{case}__bic"])
+
+
+def _stat_from_aic(aic, k, n):
+    return aic - 2.0 * k - 2.0 * k * (k + 1.0) / (n - k - 1.0)
+
+
+@pytest.mark.parametrize("case", LM_CASES)
+def test_lm_runs_match_printed_results(gpu, tmp_path, case):
+    from imfit_gb300 import cli
+    det = {}
+    p, s = cli.run(_args(tmp_path, case), out=io.StringIO(), details=det)
+    v, e, stat, aic, bic = _printed(case)
+    if np.isnan(stat):
+        stat = _stat_from_aic(aic, det["n_free"], det["n_valid"])
+    assert abs(s - stat) <= 2e-7 * abs(stat) + 1e-6, (s, stat)
+    assert abs(det["aic"] - aic) <= 2e-7 * abs(aic) + 2e-6 and abs(det["bic"] - bic) <= 2e-7 * abs(bic) + 2e-6
+    rounding = 1e-5 * np.abs(v) + 1e-12
+    assert np.all(np.abs(p - v) <= 0.05 * e + rounding), list(zip(p, v, e))
+    err = det["errors"]
+    assert err is not None
+    assert np.all(np.abs(err - e) <= 0.01 * e + 1e-5 * np.abs(e) + 1e-12), list(zip(err, e))
+
+
+@pytest.mark.parametrize("case", NM_CASES)
+def test_simplex_runs_reach_the_printed_minimum(gpu, tmp_path, case):
+    from imfit_gb300 import cli
+    det = {}
+    p, s = cli.run(_args(tmp_path, case), out=io.StringIO(), details=det)
+    v, _, stat, aic, _ = _printed(case)
+    if np.isnan(stat):
+        stat = _stat_from_aic(aic, det["n_free"], det["n_valid"])
+    assert stat - 1e-6 * abs(stat) <= s <= stat + 2e-7 * abs(stat) + 1e-6, (s, stat)
+    # the parameters' scale: one-sigma errors of an LM fit of the same case
+    # (Cash has no deviates: the Poisson-MLR fit of the same data stands in)
+    lm = {}
+    drop = ("--nm", "--cashstat")
+    extra = ["--mlr"] if case == "5a" else []
+    cli.run(_args(tmp_path, case, drop) + extra, out=io.StringIO(), details=lm)
+    sigma = lm["errors"]
+    # a parameter the LM fit holds at a limit has no sigma: 0.5 in its own units
+    sigma = np.where(sigma > 0, sigma, 0.5)
+    assert np.all(np.abs(p - v) <= 0.1 * sigma + 1e-5 * np.abs(v)), list(zip(p, v, sigma))
+
+
+@pytest.mark.parametrize("case", sorted(ERROR_CASES))
+def test_runs_the_reference_stops_stop_here(gpu, tmp_path, case):
+    from imfit_gb300 import cli
+    assert ERROR_CASES[case] in str(D[f"{case}__error"])
+    with pytest.raises(SystemExit) as e:
+        cli.run(_args(tmp_path, case), out=io.StringIO())
+    assert ERROR_CASES[case] in str(e.value)
