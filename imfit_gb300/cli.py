@@ -110,7 +110,7 @@ def parse_region(text):
 
 def _add_psf(m, args):
     if args.psf:
-        m.add_psf(fitsio.read_image(args.psf)[0], normalize=not args.no_normalize)
+        m.add_psf(_read(args.psf, "PSF image"), normalize=not args.no_normalize)
 
 
 def _section_offsets(cfg, image_name):
@@ -143,7 +143,7 @@ def _add_oversampled_psfs(m, args, offset=(0, 0)):
         if args.overpsf_scale[j] < 1:
             raise SystemExit("--overpsf_scale must be a positive integer")
         x1, x2, y1, y2 = parse_region(region)
-        m.add_oversampled_psf(fitsio.read_image(args.overpsf[j])[0], args.overpsf_scale[j],
+        m.add_oversampled_psf(_read(args.overpsf[j], "oversampled PSF image"), args.overpsf_scale[j],
                               (x1 - offset[0], x2 - offset[0], y1 - offset[1], y2 - offset[1]),
                               normalize=not args.no_normalize)
 
@@ -192,10 +192,20 @@ def setup_model(cfg, args, image, offset=(0, 0)):
     return m
 
 
+def _read(path, kind):
+    """An input image; an unreadable one stops the command with the
+    reference's messages (core/image_io.cpp:169-170, core/getimages.cpp:41-45,
+    core/imfit_main.cpp:200-204)."""
+    try:
+        return fitsio.read_image(path)[0]
+    except (OSError, ValueError) as e:
+        raise SystemExit(f"*** WARNING: {e}!\n*** ERROR: Unable to read {kind} file \"{path}\"!")
+
+
 def _matching_image(path, kind, image, image_path):
     """A noise or mask image, which must have the data image's dimensions
     (GetImageAndCheckSize, core/getimages.cpp:34-58)."""
-    arr = fitsio.read_image(path)[0]
+    arr = _read(path, kind)
     if arr.shape != image.shape:
         raise SystemExit(f"*** ERROR: Dimensions of {kind} image ({path}: {arr.shape[1]} columns, {arr.shape[0]} "
                          f"rows)\ndo not match dimensions of data image ({image.shape[1]} columns, "
@@ -244,7 +254,7 @@ def run(argv=None, out=sys.stdout, details=None):
         cfg = read_config(args.config)
     except ConfigError as e:
         raise SystemExit(f"error in {args.config}: {e}")
-    image = fitsio.read_image(args.image)[0]
+    image = _read(args.image, "image")
     off, shift = _section_offsets(cfg, args.image)
     m = setup_model(cfg, args, image, shift)
     p0 = np.array(cfg.values, dtype=float) - off
@@ -440,7 +450,7 @@ def mcmc(argv=None, out=sys.stdout):
         cfg = read_config(args.config)
     except ConfigError as e:
         raise SystemExit(f"error in {args.config}: {e}")
-    image = fitsio.read_image(args.image)[0]
+    image = _read(args.image, "image")
     off, shift = _section_offsets(cfg, args.image)
     m = setup_model(cfg, args, image, shift)
     p0 = np.array(cfg.values, dtype=float) - off

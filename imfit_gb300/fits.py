@@ -2,9 +2,13 @@
 
 Imfit reads and writes FITS images through CFITSIO (reference
 core/image_io.cpp:241-375).  This module covers what the model-image path
-needs: a 2-D primary (or first image-extension) HDU with BITPIX 8/16/32/-32/-64,
-BSCALE/BZERO, returned as a float64 array indexed [row, column] with rows
-counted from the bottom of the image (the order Imfit's pixel vectors use).
+needs: a 2-D image HDU with BITPIX 8/16/32/-32/-64, BSCALE/BZERO, returned
+as a float64 array indexed [row, column] with rows counted from the bottom of
+the image (the order Imfit's pixel vectors use).  Names follow CFITSIO's
+extended syntax as far as Imfit's tests use it: 'file.fits[N]' selects HDU
+N (0 = primary), a plain name the primary HDU; an HDU without a 2-D image
+is an error (core/image_io.cpp:160-171).  'file.fits[x1:x2,y1:y2]' selects
+an image section, 'file.fits[N][x1:x2,y1:y2]' both.
 """
 import re
 
@@ -48,11 +52,19 @@ def _parse_header(raw, pos):
 def split_section(name):
     """'file.fits[x1:x2,y1:y2]' -> ('file.fits', (x1, x2, y1, y2)) with 1-based
     inclusive pixel ranges (x = column), as CFITSIO's image sections; a name
-    without a section -> (name, None)."""
+    without a section -> (name, None).  An HDU selector stays on the name."""
     m = re.fullmatch(r"(.*)\[\s*(\d+)\s*:\s*(\d+)\s*,\s*(\d+)\s*:\s*(\d+)\s*\]", name.strip())
     if not m:
         return name, None
     return m.group(1), tuple(int(m.group(i)) for i in range(2, 6))
+
+
+def split_hdu(name):
+    """'file.fits[N]' -> ('file.fits', N); a name without one -> (name, None)."""
+    m = re.fullmatch(r"(.*)\[\s*(\d+)\s*\]", name.strip())
+    if not m:
+        return name, None
+    return m.group(1), int(m.group(2))
 
 
 def image_offset(name):
@@ -66,7 +78,8 @@ def read_image(path):
     """Return (float64 array [nrows, ncols], header dict) of the first 2-D image
     HDU; a trailing section [x1:x2,y1:y2] selects that part of the image."""
     path, sec = split_section(path)
-    arr, hdr = _read_full(path)
+    path, hdu = split_hdu(path)
+    arr, hdr = _read_full(path, 0 if hdu is None else hdu)
     if sec is not None:
         x1, x2, y1, y2 = sec
         if not (1 <= x1 <= x2 <= arr.shape[1] and 1 <= y1 <= y2 <= arr.shape[0]):
@@ -75,23 +88,27 @@ def read_image(path):
     return arr, hdr
 
 
-def _read_full(path):
+def _read_full(path, hdu=0):
     with open(path, "rb") as f:
         raw = f.read()
-    pos = 0
+    pos, k = 0, 0
     while pos < len(raw):
         hdr, pos = _parse_header(raw, pos)
         naxis = int(hdr.get("NAXIS", 0))
         bitpix = int(hdr["BITPIX"])
         dims = [int(hdr.get(f"NAXIS{i + 1}", 0)) for i in range(naxis)]
         nbytes = abs(bitpix) // 8 * (int(np.prod(dims)) if naxis else 0)
-        if naxis >= 2 and nbytes > 0 and hdr.get("XTENSION", "IMAGE") in ("IMAGE", None):
+        image = naxis == 2 and nbytes > 0 and hdr.get("XTENSION", "IMAGE") in ("IMAGE", None)
+        if image and hdu == k:
             data = np.frombuffer(raw, dtype=_DT[bitpix], count=int(np.prod(dims)), offset=pos)
             arr = data.astype(np.float64).reshape(dims[1], dims[0])
             arr = arr * float(hdr.get("BSCALE", 1.0)) + float(hdr.get("BZERO", 0.0))
             return arr, hdr
+        if hdu == k:
+            break
         pos += ((nbytes + _BLOCK - 1) // _BLOCK) * _BLOCK
-    raise ValueError(f"no 2-D image HDU in {path}")
+        k += 1
+    raise ValueError(f"Unable to find valid 2D image in extension {hdu} (HDU {hdu + 1}) of {path}")
 
 
 def write_image(path, arr, bitpix=-32):

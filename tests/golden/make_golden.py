@@ -46,13 +46,16 @@ Outputs (all small .npz files next to this script):
   imfit_regressions.npz
                      inputs (images as stored, configuration files as text) and
                      printed results of the reference's imfit regression runs
-                     do_imfit_tests:66, 87, 89, 97, 121-124, 147-149, 165-178
-                     (imfit_textout2, 3e, 3e2, 4b, 5a/5b/5c_tail, 6, 6b, 7a-7f,
-                     8a; the linux_x86_64 copies where the reference keeps
+                     do_imfit_tests:66, 87, 89, 97, 121-124, 147-162, 165-178
+                     (imfit_textout2, 3e, 3e2, 4b, 5a/5b/5c_tail, 6, 6b-6h,
+                     7a-7f, 8a; the linux_x86_64 copies where the reference keeps
                      per-platform outputs): per case the command's options, the
                      best-fit values and printed errors, the printed statistic
                      (or the one implied by the printed AIC), AIC, BIC, and the
-                     error line of the runs that stop with an error.
+                     error line of the runs that stop with an error; and the
+                     saved bootstrap iterations of --seed 10 --bootstrap 5 on
+                     ic3478rss_64x64.fits and its section [10:64,10:64]
+                     (do_imfit_tests:133-134, bootstrap_output_seed10*_tail.dat).
 """
 import re
 import os
@@ -226,6 +229,14 @@ REGRESSIONS = [
      "imfit_textout6"),
     ("6b", "imfit_config_ic3478_64x64b.dat", "ic3478rss_64x64.fits", ["--mask", "n3073rss_small_mask.fits"],
      "imfit_textout6b"),
+    ("6c", "imfit_config_ic3478_64x64b.dat", "test_emptyhdu.fits", [], "imfit_textout6c"),
+    ("6d", "imfit_config_ic3478_64x64b.dat", "test_table.fits", [], "imfit_textout6d"),
+    ("6e", "imfit_config_ic3478_64x64b.dat", "ic3478rss_64x64.fits", ["--mask", "test_emptyhdu.fits"],
+     "imfit_textout6e"),
+    ("6f", "imfit_config_ic3478_64x64b.dat", "test_multiextension_hdu0empty.fits[0]", [], "imfit_textout6f"),
+    ("6g", "config_imfit_small-gaussian.dat", "test_multiextension_hdu0empty.fits[1]", [], "imfit_textout6g"),
+    ("6h", "config_imfit_small-gaussian.dat", "test_multiextension_hdu0empty.fits[1][1:8,1:8]", [],
+     "imfit_textout6h"),
     ("7a", "config_3x3_flatsky.dat", "testimage_3x3_nan.fits", [], "imfit_textout7a"),
     ("7b", "config_3x3_flatsky.dat", "testimage_3x3_ones.fits", ["--mask=testimage_3x3_mask-with-nan.fits"],
      "imfit_textout7b"),
@@ -238,6 +249,10 @@ REGRESSIONS = [
     ("8a", "config_imfit_ptsource.dat", "psf_moffat_fwhm2.fits", ["--psf=psf_moffat_fwhm2_35x35.fits"],
      "linux_x86_64/imfit_textout8a"),
 ]
+
+
+# regression inputs whose HDU layout matters (an empty primary HDU, a table)
+RAW_FILES = {"test_emptyhdu.fits", "test_table.fits", "test_multiextension_hdu0empty.fits"}
 
 
 def _parse_textout(path):
@@ -275,7 +290,7 @@ def imfit_regressions():
     files = set()
     for case, cfg, img, opts, textout in REGRESSIONS:
         out[f"config__{cfg}"] = np.array(open(os.path.join(cfg_dir, cfg)).read())
-        files.add(img)
+        files.add(img.split("[")[0])
         for o in opts:
             v = o.split("=", 1)[1] if "=" in o else o
             if v.endswith(".fits"):
@@ -290,7 +305,19 @@ def imfit_regressions():
         for k in ("stat", "aic", "bic"):
             out[f"{case}__{k}"] = np.float64(r[k])
         out[f"{case}__error"] = np.array(r["error"])
+    # bootstrap refits with --seed 10 --bootstrap 5 on the whole image and on
+    # its section [10:64,10:64] (do_imfit_tests:133-134, 312-323): the last 7
+    # lines of the saved iterations
+    for key, name in (("full", "bootstrap_output_seed10_tail.dat"), ("section", "bootstrap_output_seed10_2_tail.dat")):
+        lines = open(os.path.join(cfg_dir, "linux_x86_64", name)).read().splitlines()
+        out[f"boot__{key}__header"] = np.array(lines[:2])
+        out[f"boot__{key}__rows"] = np.array([[float(v) for v in ln.split()] for ln in lines[2:]])
+    out["config__imfit_config_ic3478_64x64b.dat"] = np.array(
+        open(os.path.join(cfg_dir, "imfit_config_ic3478_64x64b.dat")).read())
     for f in sorted(files):
+        if f in RAW_FILES:  # several HDUs, kept byte for byte
+            out[f"raw__{f}"] = np.frombuffer(open(os.path.join(t, f), "rb").read(), dtype=np.uint8)
+            continue
         data, hdr = fits.read_image(os.path.join(t, f))
         # float32 images as stored; integer masks and float64 images as float64
         out[f"file__{f}"] = data.astype(np.float32) if int(hdr["BITPIX"]) == -32 else data

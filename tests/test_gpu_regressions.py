@@ -1,7 +1,7 @@
 """The reference's imfit regression runs (do_imfit_tests:66, 87, 89, 97,
-121-124, 147-149, 165-178) through the imfit-style command line on the GPU,
+121-124, 133-134, 147-162, 165-178) through the imfit-style command line on the GPU,
 against the printed outputs held in tests/golden/imfit_regressions.npz
-(imfit_textout2, 3e, 3e2, 4b, 5a-5c, 6, 6b, 7a-7f, 8a):
+(imfit_textout2, 3e, 3e2, 4b, 5a-5c, 6, 6b-6h, 7a-7f, 8a):
 
 * Levenberg-Marquardt runs: best-fit values within 0.05 of the printed
   one-sigma errors (plus the printing's rounding), the statistic to its six
@@ -22,10 +22,14 @@ pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 D = np.load(os.path.join(GOLDEN, "imfit_regressions.npz"))
 
-LM_CASES = ["2", "3e", "3e2", "4b", "5c", "7a", "7b", "7c", "7e", "8a"]
+LM_CASES = ["2", "3e", "3e2", "4b", "5c", "6g", "6h", "7a", "7b", "7c", "7e", "8a"]
 NM_CASES = ["5a", "5b", "7f"]
 ERROR_CASES = {"6": "Failure in ModelObject::FinalSetupForFitting!",
                "6b": "Dimensions of mask image",
+               "6c": "Unable to read image file",
+               "6d": "Unable to read image file",
+               "6e": "Unable to read mask file",
+               "6f": "Unable to read image file",
                "7d": "Failure in ModelObject::FinalSetupForFitting!"}
 
 
@@ -34,11 +38,15 @@ def _args(tmp_path, case, drop=()):
     from imfit_gb300 import fits
 
     def path(name):
-        arr = D[f"file__{name}"]
-        out = tmp_path / name
+        base, suffix = name.split("[")[0], name[len(name.split("[")[0]):]  # HDU / section suffix
+        out = tmp_path / base
         if not out.exists():
-            fits.write_image(str(out), arr, bitpix=-32 if arr.dtype == np.float32 else -64)
-        return str(out)
+            if f"raw__{base}" in D.files:
+                out.write_bytes(D[f"raw__{base}"].tobytes())
+            else:
+                arr = D[f"file__{base}"]
+                fits.write_image(str(out), arr, bitpix=-32 if arr.dtype == np.float32 else -64)
+        return str(out) + suffix
 
     cfg = str(D[f"{case}__config"])
     (tmp_path / cfg).write_text(str(D[f"config__{cfg}"]))
@@ -111,3 +119,27 @@ def test_runs_the_reference_stops_stop_here(gpu, tmp_path, case):
     with pytest.raises(SystemExit) as e:
         cli.run(_args(tmp_path, case), out=io.StringIO())
     assert ERROR_CASES[case] in str(e.value)
+
+
+@pytest.mark.parametrize("key,section", [("full", ""), ("section", "[10:64,10:64]")])
+def test_bootstrap_iterations_match_the_reference(gpu, tmp_path, key, section):
+    """do_imfit_tests:133-134: --seed 10 --bootstrap 5 --save-bootstrap on
+    ic3478rss_64x64.fits and on its section [10:64,10:64] (whose saved values
+    carry the section's offsets added back).  The resampling indices are the
+    reference's MT19937 stream, so each refit is of the same resampled image
+    as the reference's: every saved value within 0.01 sigma (the printed
+    errors of the full-image fit) of the reference's."""
+    from imfit_gb300 import cli, fits
+    cfg = "imfit_config_ic3478_64x64b.dat"
+    (tmp_path / cfg).write_text(str(D[f"config__{cfg}"]))
+    img = tmp_path / "ic3478rss_64x64.fits"
+    fits.write_image(str(img), D["file__ic3478rss_64x64.fits"])
+    out = tmp_path / "boot.dat"
+    cli.run([str(tmp_path / cfg), str(img) + section, "--seed", "10", "--bootstrap", "5", "--save-bootstrap",
+             str(out)], out=io.StringIO())
+    lines = out.read_text().splitlines()
+    header, rows = list(D[f"boot__{key}__header"]), D[f"boot__{key}__rows"]
+    assert lines[-7:-5] == header
+    got = np.array([[float(v) for v in ln.split()] for ln in lines[-5:]])
+    sigma = D["2__errors"]
+    assert np.all(np.abs(got - rows) <= 0.01 * sigma), (got - rows) / sigma
