@@ -13,9 +13,11 @@ Outputs (all small .npz files next to this script):
                      the full-precision values from the reference's own code
                      compiled here (oracle/_ref), and its mpfit LM fit.
   makeimage.npz      reference makeimage outputs tests/sersic+exp_orig.fits
-                     (central 128x128 crop and four 16x16 corners) and
-                     tests/oversampled_orig.fits (whole image) with their PSFs
-                     (do_makeimage_tests:51, 68-72).
+                     (central 128x128 crop and four 16x16 corners),
+                     tests/oversampled_orig.fits and oversampled2both_orig.fits
+                     with their PSFs, tests/biggertest_orig.fits, and the
+                     configurations of the last two (do_makeimage_tests:48,
+                     51, 68-72).
   ic3478.npz         the reference regression input tests/ic3478rss_64x64.fits
                      (float32 as stored) with the configuration
                      tests/imfit_reference/imfit_config_ic3478_64x64b.dat and the
@@ -116,8 +118,17 @@ def makeimage():
     ov, _ = fits.read_image(os.path.join(t, "oversampled_orig.fits"))
     psf_std, _ = fits.read_image(os.path.join(t, "psf_standard.fits"))
     psf_os, _ = fits.read_image(os.path.join(t, "psf_oversamp.fits"))
+    ov2, _ = fits.read_image(os.path.join(t, "oversampled2both_orig.fits"))
+    big, _ = fits.read_image(os.path.join(t, "biggertest_orig.fits"))
+    mref = os.path.join(t, "makeimage_reference")
     np.savez_compressed(
         os.path.join(HERE, "makeimage.npz"),
+        # do_makeimage_tests:48 (--ncols 64 --nrows 64) and :70-72 (two oversampled
+        # regions, one PSF image for both or one each): configurations as text
+        big_config=np.array(open(os.path.join(mref, "config_biggertest_4c.dat")).read()),
+        big_image=big.astype(np.float32),
+        ov2_config=np.array(open(os.path.join(mref, "config_makeimage_gauss-oversample2.dat")).read()),
+        ov2_image=ov2.astype(np.float32),
         # tests/makeimage_reference/config_makeimage_sersic+exp512.dat
         se_params=np.array([256.0, 256.0, 30.0, 0.5, 2.5, 100.0, 50.0, 30.0, 0.75, 10.0, 150.0]),
         se_center=se[192:320, 192:320].astype(np.float32),

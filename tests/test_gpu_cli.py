@@ -57,6 +57,57 @@ def test_makeimage_oversampled_golden(gpu, tmp_path):
     assert normwise(single, g["ov_image"]) < 2e-7
 
 
+def _within_float32_ulp(model, golden):
+    """FP64 model against a float32 reference image: within one float32 ulp,
+    plus 1e-12 of the image maximum for the FFT's round-off far from the
+    sources (values ~1e-16 there, which the reference's own comparison
+    ignores below 1e-7)."""
+    g = np.asarray(golden, dtype=np.float32)
+    ulp = np.spacing(np.abs(g)).astype(np.float64)
+    return np.all(np.abs(model - g.astype(np.float64)) <= ulp + 1e-12 * np.max(np.abs(g)))
+
+
+def test_makeimage_biggertest_golden(gpu, tmp_path):
+    """do_makeimage_tests:48: config_biggertest_4c.dat (three function sets,
+    X0/Y0 outside their limits -- makeimage does not check limits) at
+    64 x 64 against tests/biggertest_orig.fits, every pixel within one
+    float32 ulp."""
+    from imfit_gb300 import cli, fits
+    g = np.load(os.path.join(GOLDEN, "makeimage.npz"))
+    (tmp_path / "c.dat").write_text(str(g["big_config"]))
+    out = str(tmp_path / "big.fits")
+    model, _ = cli.makeimage([str(tmp_path / "c.dat"), "-o", out, "--ncols", "64", "--nrows", "64"],
+                             out=io.StringIO())
+    assert _within_float32_ulp(model, g["big_image"])
+    assert np.array_equal(fits.read_image(out)[0], g["big_image"].astype(np.float64))
+
+
+@pytest.mark.parametrize("two_psfs", [False, True])
+def test_makeimage_two_oversampled_regions_golden(gpu, tmp_path, two_psfs):
+    """do_makeimage_tests:70 and :72: two oversampled regions (100:110,100:110
+    and 20:30,20:30) with one PSF image for both, or one each, against
+    tests/oversampled2both_orig.fits within one float32 ulp; the
+    single-function images sum to the model (do_makeimage_tests:215)."""
+    from imfit_gb300 import cli, fits
+    g = np.load(os.path.join(GOLDEN, "makeimage.npz"))
+    (tmp_path / "c.dat").write_text(str(g["ov2_config"]))
+    fits.write_image(str(tmp_path / "psf.fits"), g["psf_standard"])
+    fits.write_image(str(tmp_path / "opsf.fits"), g["psf_oversamp"])
+    opsf = str(tmp_path / "opsf.fits")
+    args = [str(tmp_path / "c.dat"), "-o", str(tmp_path / "ov2.fits"), "--psf", str(tmp_path / "psf.fits")]
+    if two_psfs:
+        args += ["--overpsf", opsf, "--overpsf_scale", "3", "--overpsf_region", "100:110,100:110",
+                 "--overpsf", opsf, "--overpsf_scale", "3", "--overpsf_region", "20:30,20:30"]
+    else:
+        args += ["--overpsf", opsf, "--overpsf_scale", "3", "--overpsf_region", "100:110,100:110",
+                 "--overpsf_region", "20:30,20:30", "--output-functions", str(tmp_path / "double")]
+    model, _ = cli.makeimage(args, out=io.StringIO())
+    assert _within_float32_ulp(model, g["ov2_image"])
+    if not two_psfs:
+        parts = [fits.read_image(str(tmp_path / f"double{k}_Gaussian.fits"))[0] for k in (1, 2)]
+        assert np.allclose(parts[0] + parts[1], model, rtol=0, atol=1e-6)
+
+
 def test_makeimage_fluxes_table(gpu, tmp_path):
     """do_makeimage_tests:60 (makeimage_textout5b): --print-fluxes --nosave
     on config_makeimage_sersic+exp512b.dat; the table lines as printed."""
