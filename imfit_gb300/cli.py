@@ -507,7 +507,8 @@ def multimfit(argv=None, out=sys.stdout):
     """The multimfit command (core/multimfit_main.cpp): the configuration file
     gives the model, the image-info file the images and their description
     parameters; returns (fitted global parameters, statistic)."""
-    from .multimage import IMAGE_PARAM_NAMES, MultiImageModel, build_handles, global_vector, parse_image_info
+    from .multimage import (IMAGE_PARAM_NAMES, MultiImageModel, build_handles, global_vector, parse_image_info,
+                            section_offsets)
     args = build_multimfit_parser().parse_args(argv)
     try:
         cfg = read_config(args.config)
@@ -519,10 +520,12 @@ def multimfit(argv=None, out=sys.stdout):
     handles = build_handles(cfg.functions, images, args.device, not args.nosubsampling, stat, args.model_errors)
     mm = MultiImageModel(cfg.functions, handles)
     p0, lo, hi, fx = global_vector(cfg, images)
+    off = section_offsets(cfg, images)  # image sections: X0/Y0 in the sections' pixel frames
+    p0, lo, hi = p0 - off, lo - off, hi - off
     if args.fitstat_only:
         s = mm.get_fit_statistic(p0)
         out.write(f"fit statistic = {s:.6f}\n")
-        return p0, s
+        return p0 + off, s
     if args.de:
         from .solvers import differential_evolution
         r = differential_evolution(mm, p0, lo, hi, fixed=fx.astype(bool), ftol=args.ftol, seed=args.seed)
@@ -535,8 +538,8 @@ def multimfit(argv=None, out=sys.stdout):
             raise SystemExit("the Cash statistic has no deviates: use --nm or --de")
         r = mm.fit_lm(p0, fixed=fx, lower=np.where(np.isnan(lo), 0.0, lo), upper=np.where(np.isnan(hi), 0.0, hi),
                       ftol=args.ftol, max_iter=args.max_iter)
-    p = r["params"]
-    s = mm.get_fit_statistic(p)
+    s = mm.get_fit_statistic(r["params"])
+    p = r["params"] + off  # reported in the full images' pixel frames
     out.write(f"fit statistic = {s:.6f}\n# Main model parameters (reference image)\n")
     for name, v in zip(cfg.param_names, p[mm.n_image_params:]):
         out.write(f"  {name:8s} {v:.6f}\n")

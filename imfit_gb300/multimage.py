@@ -269,6 +269,26 @@ def build_handles(functions, images, device=0, subsampling=True, statistic="chi2
     return handles
 
 
+def section_offsets(cfg, images):
+    """CorrectForImageOffsets (core/utilities_multimfit.cpp:34-95): the vector
+    to subtract from the global vector's values and limits (and to add back
+    to fitted values) when images are image sections -- each later image's
+    X0/Y0 description parameters by that image's (x1 - 1, y1 - 1), the
+    model's X0/Y0 by the reference image's."""
+    from . import fits
+    nip = N_IMAGE_PARAMS * (len(images) - 1)
+    off = np.zeros(nip + len(cfg.values))
+    for i, im in enumerate(images[1:], start=1):
+        off[N_IMAGE_PARAMS * (i - 1) + 3:N_IMAGE_PARAMS * i] = fits.image_offset(im.data)
+    dx, dy = fits.image_offset(images[0].data)
+    for j, name in enumerate(cfg.param_names):
+        if name == "X0":
+            off[nip + j] = dx
+        elif name == "Y0":
+            off[nip + j] = dy
+    return off
+
+
 def global_vector(cfg, images):
     """(values, lower, upper, fixed) of the global vector: the image-description
     parameters of images 2..N (defaults 1, 0, 1 and the reference model's X0,

@@ -37,7 +37,11 @@ Outputs (all small .npz files next to this script):
                      smallDataImage1{a,b}.fits with the printed results of
                      multimfit_textout3a (Nelder-Mead fit of
                      config_imfit_smallgauss.dat + imageinfo_multimfit3.txt) and
-                     multimfit_textout1a (--fitstat-only, imageinfo_multimfit0.txt).
+                     multimfit_textout1a (--fitstat-only, imageinfo_multimfit0.txt);
+                     the configurations, image-info files and printed results
+                     of multimfit_textout1c-1e and 3b-3e (do_multimfit_tests.sh:63-92:
+                     Nelder-Mead and LM fits, limits on the image-description
+                     parameters, image sections, no error images, model errors).
   makemultimages.npz the makemultimages outputs tests/makemultimages_reference/
                      multimagetest_{0,1,2,2b,2c,2d}.fits and multimagetest_2blocks_0 /
                      _offset_1 / _offset_2.fits (do_makemultimages_tests.sh:59-65),
@@ -194,7 +198,35 @@ def multimfit():
         g_chi2_printed=36.070608, g_model_printed=np.array([2.5072, 2.5387, 18.9357, 0.293283, 995.047, 0.992441]),
         g_image2_printed=np.array([2.49082, 2.47557]),
         # multimfit_textout1a: CHI-SQUARE at the starting parameters
-        d_chi2_printed=6.75)
+        d_chi2_printed=6.75, **_multimfit_cases(t))
+
+
+# do_multimfit_tests.sh:63-92: (case, configuration, image-info file, options)
+MULTIMFIT_CASES = [
+    ("1c", "config_imfit_smalldataimages.dat", "imageinfo_multimfit0.txt", ["--nm"]),
+    ("1d", "config_imfit_smalldataimages_with-limits.dat", "imageinfo_multimfit0.txt", []),
+    ("1e", "config_imfit_smalldataimages.dat", "imageinfo_multimfit0_with-limits.txt", []),
+    ("3b", "config_imfit_smallgauss.dat", "imageinfo_multimfit3b.txt", ["--nm"]),
+    ("3c", "config_imfit_smallgauss.dat", "imageinfo_multimfit3c.txt", ["--nm"]),
+    ("3d", "config_imfit_smallgauss.dat", "imageinfo_multimfit3_noerror.txt", ["--nm"]),
+    ("3e", "config_imfit_smallgauss.dat", "imageinfo_multimfit3_noerror.txt", ["--nm", "--model-errors"]),
+]
+
+
+def _multimfit_cases(t):
+    """Configurations and image-info files as text, and the printed CHI-SQUARE
+    and parameter values (model first, then image 2's description
+    parameters, as multimfit prints them) of multimfit_textout<case>."""
+    out = {"cases": np.array([c[0] for c in MULTIMFIT_CASES])}
+    for case, cfg, info, opts in MULTIMFIT_CASES:
+        r = _parse_textout(os.path.join(t, f"multimfit_textout{case}"))
+        out[f"{case}__config"] = np.array(open(os.path.join(t, cfg)).read())
+        out[f"{case}__info"] = np.array(open(os.path.join(t, info)).read())
+        out[f"{case}__options"] = np.array(opts if opts else [""])
+        out[f"{case}__names"] = np.array(r["names"])
+        out[f"{case}__values"] = np.array(r["values"])
+        out[f"{case}__stat"] = np.float64(r["stat"])
+    return out
 
 
 def makemultimages():
@@ -286,7 +318,7 @@ def _parse_textout(path):
             if ln.startswith("Saving") or ln.startswith("(Elapsed"):
                 break
             t = ln.split()
-            if not t or t[0] == "FUNCTION":
+            if not t or t[0] == "FUNCTION" or t[0].startswith("#"):
                 continue
             res["names"].append(t[0])
             res["values"].append(float(t[1]))

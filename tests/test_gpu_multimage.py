@@ -175,3 +175,42 @@ def test_makemultimages_goldens(gpu, tmp_path, case, third, config, goldens):
         assert img.shape == want.shape
         tol = np.spacing(np.abs(g[key])).astype(np.float64) * 2 + 1e-30
         assert np.all(np.abs(img - want) <= tol), (key, np.max(np.abs(img - want) / tol))
+
+
+_REF_NAMES = {"g0": "smallgauss_5x5_0.fits", "g1": "smallgauss_5x5_1.fits", "gsig": "smallgauss_5x5_sigma.fits",
+              "d1a": "smallDataImage1a.fits", "d1b": "smallDataImage1b.fits"}
+# per printed parameter (model first, then image 2's description parameters):
+# FlatSky cases -- X0, Y0 of the model have no effect (None: not compared)
+_TOL_FLAT = [None, None, 2e-4, 0, 0, 1e-3, 0, 0]
+# Gaussian cases -- twice the LM bounds of the smallgauss fit above (the
+# simplex stops within its own tolerance of the minimum)
+_TOL_GAUSS = [4e-3, 4e-3, 0.1, 2e-3, 0.2, 2e-3, 0, 0, 0, 4e-3, 4e-3]
+
+
+@pytest.mark.parametrize("case", ["1c", "1d", "1e", "3b", "3c", "3d", "3e"])
+def test_multimfit_regression_runs(gpu, tmp_path, case):
+    """do_multimfit_tests.sh:63-92 (multimfit_textout1c-1e, 3b-3e): Nelder-Mead
+    and LM fits with limits on a FlatSky level and on FLUX_SCALE, image
+    sections of the reference and of the second image (X0/Y0 offsets), no
+    error images, --model-errors: the fitted statistic at the printed one
+    (1e-4 relative for the simplex, 1e-7 for LM) and the parameters within
+    the tolerances above of the printed values."""
+    from imfit_gb300 import cli, fits
+    d = np.load(os.path.join(GOLDEN, "multimfit.npz"))
+    for k, name in _REF_NAMES.items():
+        fits.write_image(str(tmp_path / name), d[k])
+    (tmp_path / "c.dat").write_text(str(d[f"{case}__config"]))
+    info = str(d[f"{case}__info"]).replace("tests/multimfit_reference/", str(tmp_path) + "/")
+    (tmp_path / "info.txt").write_text(info)
+    opts = [o for o in (str(x) for x in d[f"{case}__options"]) if o]
+    p, s = cli.multimfit([str(tmp_path / "c.dat"), "-i", str(tmp_path / "info.txt")] + opts, out=io.StringIO())
+    printed, stat = d[f"{case}__values"], float(d[f"{case}__stat"])
+    nm = "--nm" in opts
+    assert abs(s - stat) <= (1e-4 if nm else 1e-7) * stat + 1e-6, (s, stat)
+    n_model = len(p) - 5
+    got = np.concatenate([p[5:], p[:5]])  # printed order: model, then image 2
+    assert n_model == len(printed) - 5
+    tol = _TOL_FLAT if len(printed) == 8 else _TOL_GAUSS
+    for k, t in enumerate(tol):
+        if t is not None:
+            assert abs(got[k] - printed[k]) <= t + 1e-6 * abs(printed[k]), (k, got, printed)
