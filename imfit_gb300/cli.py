@@ -74,6 +74,7 @@ def build_parser():
     ap.add_argument("--save-params", default="bestfit_parameters_imfit_gb300.dat")
     ap.add_argument("--save-model")
     ap.add_argument("--save-residual")
+    ap.add_argument("--save-weights", help="file for the weight image (1/sigma^2, masked pixels 0)")
     return ap
 
 
@@ -308,6 +309,8 @@ def run(argv=None, out=sys.stdout, details=None):
     if args.save_params:
         with open(args.save_params, "w") as f:
             f.write(format_params(cfg, p, s))
+    if args.save_weights:  # GetWeightImageVector: 1/sigma^2 at the fitted model (core/imfit_main.cpp:466-476)
+        fitsio.write_image(args.save_weights, m.get_weights(), bitpix=-64)
     if args.bootstrap > 0:
         run_bootstrap(m, cfg, args, p_section, out, off)
     if args.save_model or args.save_residual:

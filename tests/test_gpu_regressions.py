@@ -143,3 +143,24 @@ def test_bootstrap_iterations_match_the_reference(gpu, tmp_path, key, section):
     got = np.array([[float(v) for v in ln.split()] for ln in lines[-5:]])
     sigma = D["2__errors"]
     assert np.all(np.abs(got - rows) <= 0.01 * sigma), (got - rows) / sigma
+
+
+def test_saved_weight_images_data_and_model_errors(gpu, tmp_path):
+    """do_imfit_tests:138-139: --save-weights after fitting a FlatSky to a
+    constant image, once with data-based errors and once with --model-errors:
+    the fitted model equals the data, so the two weight images (1/sigma^2)
+    are the same, here 1 / (I / gain + read noise^2 / gain^2)."""
+    from imfit_gb300 import cli, fits
+    img = np.full((32, 40), 250.0)
+    fits.write_image(str(tmp_path / "flat.fits"), img, bitpix=-64)
+    (tmp_path / "c.dat").write_text("GAIN 4.0\nREADNOISE 2.0\nX0 20 1,40\nY0 16 1,32\nFUNCTION FlatSky\n"
+                                    "I_sky 200 0,1000\n")
+    out = {}
+    for tag, extra in (("data", []), ("model", ["--model-errors"])):
+        w = tmp_path / f"w_{tag}.fits"
+        cli.run([str(tmp_path / "c.dat"), str(tmp_path / "flat.fits"), "--save-weights", str(w)] + extra,
+                out=io.StringIO())
+        out[tag] = fits.read_image(str(w))[0]
+    want = 1.0 / (250.0 / 4.0 + 2.0 ** 2 / 4.0 ** 2)
+    assert np.allclose(out["data"], want, rtol=1e-12)
+    assert np.allclose(out["model"], out["data"], rtol=1e-7)
