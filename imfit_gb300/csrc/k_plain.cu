@@ -10,9 +10,90 @@
 
 namespace imfit {
 
+// Coordinates of model pixel (i, j): IRAF pixel centres on the main grid,
+// subpixel centres on a region grid.
+__device__ __forceinline__ void pixel_xy64(const Grid64 &g, long i, long j, double &x, double &y) {
+  if (!g.isRegion) {
+    y = (double)(i - g.pr + 1);
+    x = (double)(j - g.pc + 1);
+  } else {
+    y = g.y1 + g.off + (i - g.pr) * g.frac;
+    x = g.x1 + g.off + (j - g.pc) * g.frac;
+  }
+}
+
+// Subsample count at (x, y), with comp_value64_2d's expressions.
+__device__ __forceinline__ int n_subsamples_at64(const CompF64 &c, double x, double y) {
+  const double x_diff = x - c.x0, y_diff = y - c.y0;
+  const double xp = x_diff * c.cosPA + y_diff * c.sinPA;
+  const double yps = (-x_diff * c.sinPA + y_diff * c.cosPA) / c.q;
+  return n_subsamples64(c, sqrt(xp * xp + yps * yps));
+}
+
+// Box of 2 subHalf x 2 subHalf pixels around component c's centre: every
+// pixel within radius 10 of it (the only ones the subsampling rules touch)
+// lies inside.  Origin (j0, i0).
+__device__ __forceinline__ void sub_box64(const Grid64 &g, const CompF64 &c, long &j0, long &i0) {
+  double jc, ic;
+  if (!g.isRegion) {
+    jc = c.x0 + g.pc - 1;
+    ic = c.y0 + g.pr - 1;
+  } else {
+    jc = (c.x0 - g.x1 - g.off) / g.frac + g.pc;
+    ic = (c.y0 - g.y1 - g.off) / g.frac + g.pr;
+  }
+  j0 = (long)floor(jc) - g.subHalf + 1;
+  i0 = (long)floor(ic) - g.subHalf + 1;
+}
+
+size_t sub_table_size(const Grid64 &g, int nComp) {
+  const long S = 2L * g.subHalf;
+  return (size_t)nComp * S * S;
+}
+
+// One warp per (component, box pixel) that needs subsampling: the ns x ns
+// subsamples of comp_value64_2d (same expressions, same (ii, jj) order within
+// each lane's share) split over the lanes, the 32 partial sums added by a
+// fixed shuffle tree.  The reference sums them in one sequence; the two orders
+// differ by FP64 rounding only (~1e-16 relative), while one thread summing up
+// to 10^4 subsamples (a Gaussian with sigma ~1: ns = 40 per axis) would set the
+// whole image's latency.
+__global__ void __launch_bounds__(256) k_sub64(const CompF64 *__restrict__ comps, Grid64 g) {
+  const CompF64 cc = comps[blockIdx.y];
+  if (!cc.subsample) return;
+  const long S = 2L * g.subHalf;
+  const long p = blockIdx.x * (long)(blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (p >= S * S) return;
+  long j0, i0;
+  sub_box64(g, cc, j0, i0);
+  const long i = i0 + p / S, j = j0 + p % S;
+  if (i < 0 || i >= g.nRows || j < 0 || j >= g.nCols) return;
+  double x, y;
+  pixel_xy64(g, i, j, x, y);
+  const int ns = n_subsamples_at64(cc, x, y);
+  if (ns <= 1) return;
+  const int lane = threadIdx.x & 31;
+  const double d = 1.0 / ns;
+  const double xs0 = x - 0.5 + 0.5 * d;
+  const double ys0 = y - 0.5 + 0.5 * d;
+  double sum = 0.0;
+  for (int t = lane; t < ns * ns; t += 32) {
+    const int ii = t / ns, jj = t - ii * ns;
+    const double xi = xs0 + ii * d;
+    const double yi = ys0 + jj * d;
+    const double x_diff = xi - cc.x0, y_diff = yi - cc.y0;
+    const double xp = x_diff * cc.cosPA + y_diff * cc.sinPA;
+    const double yps = (-x_diff * cc.sinPA + y_diff * cc.cosPA) / cc.q;
+    sum += radial64(cc, sqrt(xp * xp + yps * yps));
+  }
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  if (lane == 0) g.sub[(long)blockIdx.y * S * S + p] = sum / (ns * ns);
+}
+
 // CreateModelImage pixel loop: core/model_object.cpp:1144-1175 (main grid),
 // OversampledRegion::ComputeRegionAndDownsample core/oversampled_region.cpp:301-327
-// (region grid).  One thread per model pixel; Kahan sum over components.
+// (region grid).  One thread per model pixel; Kahan sum over components;
+// subsampled pixels from k_sub64's table.
 __global__ void __launch_bounds__(256) k_eval64(const CompF64 *__restrict__ comps, int nComp,
                                                 double *__restrict__ model, long pitch, Grid64 g,
                                                 const double *__restrict__ los) {
@@ -24,19 +105,34 @@ __global__ void __launch_bounds__(256) k_eval64(const CompF64 *__restrict__ comp
   if (k >= n) return;
   const long j = k % g.nCols, i = k / g.nCols;
   double x, y;
-  if (!g.isRegion) {
-    y = (double)(i - g.pr + 1);
-    x = (double)(j - g.pc + 1);
-  } else {
-    y = g.y1 + g.off + (i - g.pr) * g.frac;
-    x = g.x1 + g.off + (j - g.pc) * g.frac;
-  }
+  pixel_xy64(g, i, j, x, y);
+  const long S = 2L * g.subHalf;
   double s = 0.0, err = 0.0;
   for (int c = 0; c < nComp; c++) {
     const int t = sc[c].type;
     if (is_point_source(t)) continue;  // added after the convolution
-    const double v = (t == F_EXPDISK3D || t == F_FERRERS3D) ? los[(long)sc[c].pad0 * n + k]
-                                                              : comp_value64_2d(sc[c], x, y);
+    double v;
+    if (t == F_EXPDISK3D || t == F_FERRERS3D) {
+      v = los[(long)sc[c].pad0 * n + k];
+    } else if (!g.sub || t == F_FLATSKY || t == F_TILTEDSKY) {
+      v = comp_value64_2d(sc[c], x, y);
+    } else {
+      // comp_value64_2d with the subsampled pixels read from the table
+      const CompF64 &cc = sc[c];
+      const double x_diff = x - cc.x0, y_diff = y - cc.y0;
+      const double xp = x_diff * cc.cosPA + y_diff * cc.sinPA;
+      const double yps = (-x_diff * cc.sinPA + y_diff * cc.cosPA) / cc.q;
+      const double r = sqrt(xp * xp + yps * yps);
+      if (n_subsamples64(cc, r) > 1) {
+        long j0, i0;
+        sub_box64(g, cc, j0, i0);
+        const long bi = i - i0, bj = j - j0;
+        v = (bi >= 0 && bi < S && bj >= 0 && bj < S) ? g.sub[(long)c * S * S + bi * S + bj]
+                                                     : comp_value64_2d(cc, x, y);
+      } else {
+        v = radial64(cc, r);
+      }
+    }
     const double adj = v - err;
     const double tmp = s + adj;
     err = (tmp - s) - adj;
@@ -49,6 +145,10 @@ cudaError_t launch_eval64(const CompF64 *comps, int nComp, double *model, long p
                           const double *los, cudaStream_t st) {
   const long n = (long)g.nCols * g.nRows;
   if (n == 0) return cudaSuccess;
+  if (g.sub) {
+    const long S = 2L * g.subHalf;
+    k_sub64<<<dim3((unsigned)((S * S + 7) / 8), (unsigned)nComp), 256, 0, st>>>(comps, g);
+  }
   k_eval64<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(comps, nComp, model, pitch, g, los);
   return cudaGetLastError();
 }

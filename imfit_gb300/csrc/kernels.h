@@ -68,7 +68,15 @@ struct Grid64 {
   int isRegion;
   int x1, y1;
   double off, frac;
+  // subsampled pixels, computed beforehand by one warp each: sub[c][S*S] over
+  // a box of S = 2 subHalf pixels around component c's centre (null: each
+  // pixel's thread sums its subsamples itself)
+  double *sub;
+  int subHalf;
 };
+
+// Scratch size (doubles) of the subsampled-pixel table of nComp components on g.
+size_t sub_table_size(const Grid64 &g, int nComp);
 
 // 3-D (line-of-sight) components of a model: their indices in the component
 // list; component c's CompF64::pad0 holds its position k3 in this list.

@@ -259,6 +259,7 @@ struct imfit_model_s {
   // 3-D (line-of-sight) components: per-pixel values computed before the pixel sum
   LosList64 losList{};
   DevBuf<double> dLos;
+  DevBuf<double> dSub;  // subsampled-pixel table of the plain path (k_sub64)
   DevBuf<int> dLosFlag;
   int *hLosFlag = nullptr;  // pinned copy of the "list too short" flag
   double *hPinned = nullptr;  // pinned scratch for small transfers
@@ -653,10 +654,17 @@ struct imfit_model_s {
     return evalGridN(dC, (int)funcs.size(), losList, model, pitch, g);
   }
   cudaError_t evalGridN(const CompF64 *dC, int nC, const LosList64 &ll, double *model, long pitch,
-                        const Grid64 &g) {
+                        const Grid64 &g0) {
+    // subsampled pixels: a table filled one warp per pixel (scratch reused by
+    // every grid; the launches are ordered on the one stream)
+    Grid64 g = g0;
+    g.subHalf = g.isRegion ? (int)std::ceil(10.0 / g.frac) + 1 : 11;
+    cudaError_t e = dSub.reserve(std::max<size_t>(sub_table_size(g, nC), 1));
+    if (e) return e;
+    g.sub = dSub.p;
     if (ll.n == 0) return launch_eval64(dC, nC, model, pitch, g, nullptr, stream);
     const size_t need = (size_t)ll.n * g.nCols * g.nRows;
-    cudaError_t e = dLos.reserve(need);
+    e = dLos.reserve(need);
     if (!e) e = launch_los64(dC, ll, dLos.p, g, dLosFlag.p, stream);
     if (!e) e = launch_eval64(dC, nC, model, pitch, g, dLos.p, stream);
     return e;
@@ -919,7 +927,10 @@ struct imfit_model_s {
     return e;
   }
 
-  int createModelImage(const double *params) {
+  // finish = false: only enqueued (the caller synchronises and then calls
+  // losCheck); a pageable source is staged by cudaMemcpyAsync before it
+  // returns, so hComps may be reused at once
+  int createModelImage(const double *params, bool finish = true) {
     int st = checkEval();
     if (st) return st;
     const int nC = (int)funcs.size();
@@ -928,10 +939,12 @@ struct imfit_model_s {
     cudaError_t e = dComps.reserve(nC);
     if (!e) e = cudaMemcpyAsync(dComps.p, hComps.data(), sizeof(CompF64) * nC, cudaMemcpyHostToDevice, stream);
     if (!e) e = enqueueModel(dComps.p);
-    if (!e) e = cudaStreamSynchronize(stream);  // hComps is pageable and reused
+    if (!e && finish) e = cudaStreamSynchronize(stream);
     if (e) return cuda_fail(e, "CreateModelImage");
-    st = losCheck();
-    if (st) return st;
+    if (finish) {
+      st = losCheck();
+      if (st) return st;
+    }
     modelComputed = true;
     return 0;
   }
@@ -961,7 +974,7 @@ struct imfit_model_s {
 
   int getFitStatistic(const double *params, double *out, int forceKind = -1) {
     if (!finalSetupDone) return fail(IMFIT_E_STATE, "FinalSetupForFitting not called");
-    int st = createModelImage(params);
+    int st = createModelImage(params, false);
     if (st) return st;
     int kind = forceKind >= 0 ? forceKind : statKind();
     if (kind == 2) kind = 1;  // GetFitStatistic -> CashStatistic for PMLR (core/model_object.cpp:1620-1626)
@@ -970,20 +983,22 @@ struct imfit_model_s {
     if (!e) e = cudaMemcpyAsync(h, dRes.p, sizeof(double), cudaMemcpyDeviceToHost, stream);
     if (!e) e = cudaStreamSynchronize(stream);
     if (e) return cuda_fail(e, "GetFitStatistic");
+    st = losCheck();
+    if (st) return st;
     *out = h[0];
     return 0;
   }
 
   int computeDeviates(double *y, const double *params) {
     if (!finalSetupDone) return fail(IMFIT_E_STATE, "FinalSetupForFitting not called");
-    int st = createModelImage(params);
+    int st = createModelImage(params, false);
     if (st) return st;
     StatArgs64 a = statArgs(pmlr ? 2 : 0);
     cudaError_t e = launch_deviates64(a, dDev.p, nullptr, stream);
     if (!e) e = cudaMemcpyAsync(y, dDev.p, sizeof(double) * a.nz, cudaMemcpyDeviceToHost, stream);
     if (!e) e = cudaStreamSynchronize(stream);
     if (e) return cuda_fail(e, "ComputeDeviates");
-    return 0;
+    return losCheck();
   }
 
   // statistic + FD gradient (1 + nParams plain evaluations)
