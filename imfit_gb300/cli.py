@@ -150,7 +150,6 @@ def _add_oversampled_psfs(m, args, offset=(0, 0)):
 
 
 def _add_functions(m, cfg, args):
-    from . import ImfitError
     for (name, new_set), opt in zip(cfg.functions, cfg.optional):
         try:
             m.add_function(name, new_set, subsampling=not args.nosubsampling, optional=opt)
