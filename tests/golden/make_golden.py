@@ -39,7 +39,7 @@ Outputs (all small .npz files next to this script):
                      config_imfit_smallgauss.dat + imageinfo_multimfit3.txt) and
                      multimfit_textout1a (--fitstat-only, imageinfo_multimfit0.txt);
                      the configurations, image-info files and printed results
-                     of multimfit_textout1c-1e and 3b-3e (do_multimfit_tests.sh:63-92:
+                     of multimfit_textout1b-1e and 3b-3f (do_multimfit_tests.sh:61-92:
                      Nelder-Mead and LM fits, limits on the image-description
                      parameters, image sections, no error images, model errors).
   makemultimages.npz the makemultimages outputs tests/makemultimages_reference/
@@ -201,8 +201,10 @@ def multimfit():
         d_chi2_printed=6.75, **_multimfit_cases(t))
 
 
-# do_multimfit_tests.sh:63-92: (case, configuration, image-info file, options)
+# do_multimfit_tests.sh:61-92: (case, configuration, image-info file, options); the
+# reference keeps 1b and 3f only as macOS printouts (macos_x86_64/)
 MULTIMFIT_CASES = [
+    ("1b", "config_imfit_smalldataimages.dat", "imageinfo_multimfit0.txt", []),
     ("1c", "config_imfit_smalldataimages.dat", "imageinfo_multimfit0.txt", ["--nm"]),
     ("1d", "config_imfit_smalldataimages_with-limits.dat", "imageinfo_multimfit0.txt", []),
     ("1e", "config_imfit_smalldataimages.dat", "imageinfo_multimfit0_with-limits.txt", []),
@@ -210,6 +212,7 @@ MULTIMFIT_CASES = [
     ("3c", "config_imfit_smallgauss.dat", "imageinfo_multimfit3c.txt", ["--nm"]),
     ("3d", "config_imfit_smallgauss.dat", "imageinfo_multimfit3_noerror.txt", ["--nm"]),
     ("3e", "config_imfit_smallgauss.dat", "imageinfo_multimfit3_noerror.txt", ["--nm", "--model-errors"]),
+    ("3f", "config_imfit_smallgauss.dat", "imageinfo_multimfit3_noerror.txt", ["--mlr"]),
 ]
 
 
@@ -219,7 +222,10 @@ def _multimfit_cases(t):
     parameters, as multimfit prints them) of multimfit_textout<case>."""
     out = {"cases": np.array([c[0] for c in MULTIMFIT_CASES])}
     for case, cfg, info, opts in MULTIMFIT_CASES:
-        r = _parse_textout(os.path.join(t, f"multimfit_textout{case}"))
+        name = f"multimfit_textout{case}"
+        if not os.path.exists(os.path.join(t, name)):
+            name = os.path.join("macos_x86_64", name)
+        r = _parse_textout(os.path.join(t, name))
         out[f"{case}__config"] = np.array(open(os.path.join(t, cfg)).read())
         out[f"{case}__info"] = np.array(open(os.path.join(t, info)).read())
         out[f"{case}__options"] = np.array(opts if opts else [""])

@@ -187,10 +187,10 @@ _TOL_FLAT = [None, None, 2e-4, 0, 0, 1e-3, 0, 0]
 _TOL_GAUSS = [4e-3, 4e-3, 0.1, 2e-3, 0.2, 2e-3, 0, 0, 0, 4e-3, 4e-3]
 
 
-@pytest.mark.parametrize("case", ["1c", "1d", "1e", "3b", "3c", "3d", "3e"])
+@pytest.mark.parametrize("case", ["1b", "1c", "1d", "1e", "3b", "3c", "3d", "3e", "3f"])
 def test_multimfit_regression_runs(gpu, tmp_path, case):
-    """do_multimfit_tests.sh:63-92 (multimfit_textout1c-1e, 3b-3e): Nelder-Mead
-    and LM fits with limits on a FlatSky level and on FLUX_SCALE, image
+    """do_multimfit_tests.sh:61-92 (multimfit_textout1b-1e, 3b-3f): Nelder-Mead
+    and LM fits (chi^2 and Poisson-MLR) with limits on a FlatSky level and on FLUX_SCALE, image
     sections of the reference and of the second image (X0/Y0 offsets), no
     error images, --model-errors: the fitted statistic at the printed one
     (1e-4 relative for the simplex, 1e-7 for LM) and the parameters within
