@@ -105,8 +105,9 @@ def parse_config(text, check_limits=True):
                     a, b = (float(x) for x in lim.split(","))
                 except ValueError:
                     raise ConfigError(f"line {lineno}: bad limits {lim!r}")
-                if check_limits and a > b:
-                    raise ConfigError(f"line {lineno}: lower limit above upper limit")
+                if check_limits and a >= b:  # equal limits are an error too: "fixed" holds a value
+                    raise ConfigError(f"line {lineno}: first parameter limit ({a:g}) must be < second limit "
+                                      f"({b:g})")
                 if check_limits and not (a <= v <= b):
                     raise ConfigError(f"line {lineno}: initial value outside its limits")
                 l, h = a, b

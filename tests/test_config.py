@@ -143,3 +143,25 @@ def test_information_criteria_reproduce_printed_aic_bic():
         aic, bic = information_criteria(float(d[f"{case}__stat"]), k, n)
         # the printed statistic is itself rounded to 1e-6
         assert abs(aic - float(d[f"{case}__aic"])) <= 1.5e-6 and abs(bic - float(d[f"{case}__bic"])) <= 1.5e-6, case
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(os.environ.get("IMFIT_REFERENCE_DIR", "/root/reference"),
+                                                   "tests")), reason="reference checkout not present")
+@pytest.mark.parametrize("name", ["makeimage_reference/config_makeimage_sersictest512_bad1.dat",
+                                  "makeimage_reference/config_makeimage_sersictest512_bad2.dat",
+                                  "makeimage_reference/config_makeimage_sersictest512_bad3.dat",
+                                  "makeimage_reference/config_makeimage_sersictest512_bad4.dat",
+                                  "makeimage_reference/config_makeimage_sersictest512_bad5.dat",
+                                  "imfit_reference/config_imfit_sersictest512_badlimits1.dat",
+                                  "imfit_reference/config_imfit_sersictest512_badlimits2.dat",
+                                  "imfit_reference/config_imfit_sersictest512_badlimits3.dat",
+                                  "config_imfit_sersictest512_badlimits4.dat",
+                                  "imfit_reference/config_imfit_badparamline.dat"])
+def test_reference_bad_configurations_are_rejected(name):
+    """The configuration files the reference's regression runs reject
+    (do_imfit_tests:194-201, do_makeimage_tests:78-82; "Failure reading
+    configuration file"): each is rejected here too."""
+    from imfit_gb300 import config
+    root = os.path.join(os.environ.get("IMFIT_REFERENCE_DIR", "/root/reference"), "tests")
+    with pytest.raises(config.ConfigError):
+        config.read_config(os.path.join(root, name))
