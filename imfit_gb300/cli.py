@@ -213,6 +213,20 @@ def _matching_image(path, kind, image, image_path):
     return arr
 
 
+def fit_statistic_lines(statistic, kind, n_free, n_valid):
+    """The lines imfit prints for --chisquare-only (PrintFitStatistic,
+    core/print_results.cpp:160-181); kind: "chi2", "cash" or "pmlr"."""
+    dof = n_valid - n_free
+    aic, bic = information_criteria(statistic, n_free, n_valid)
+    if kind == "cash":
+        lines = [f"  CASH STATISTIC = {statistic:f}"]
+    elif kind == "pmlr":
+        lines = [f"  POISSON-MLR STATISTIC = {statistic:f}", "", f"Reduced Chi^2 equivalent = {statistic / dof:f}"]
+    else:
+        lines = [f"  CHI-SQUARE = {statistic:f}    ({dof} DOF)", "", f"Reduced Chi^2 = {statistic / dof:f}"]
+    return lines + [f"AIC = {aic:f}, BIC = {bic:f}"]
+
+
 def information_criteria(statistic, n_free, n_valid):
     """Bias-corrected AIC (Burnham & Anderson 2002, p. 66) and BIC of a fit,
     the statistic standing for -2 ln L (core/statistics.cpp:139-175)."""
@@ -259,11 +273,12 @@ def run(argv=None, out=sys.stdout, details=None):
     m = setup_model(cfg, args, image, shift)
     p0 = np.array(cfg.values, dtype=float) - off
     cfg_lower, cfg_upper = cfg.lower - off, cfg.upper - off  # NaN (no limit) stays NaN
+    n_free = int(np.sum(cfg.fixed == 0))
     if args.chisquare_only:
         s = m.get_fit_statistic(p0)
-        out.write(f"fit statistic = {s:.6f}\n")
+        kind = "cash" if args.cashstat else ("pmlr" if args.poisson_mlr else "chi2")
+        out.write("\n".join(fit_statistic_lines(s, kind, n_free, m.n_valid)) + "\n")
         return p0 + off, s
-    n_free = int(np.sum(cfg.fixed == 0))
     if args.de or args.de_lhs:
         from .solvers import differential_evolution
         try:

@@ -164,3 +164,38 @@ def test_saved_weight_images_data_and_model_errors(gpu, tmp_path):
     want = 1.0 / (250.0 / 4.0 + 2.0 ** 2 / 4.0 ** 2)
     assert np.allclose(out["data"], want, rtol=1e-12)
     assert np.allclose(out["model"], out["data"], rtol=1e-7)
+
+
+def test_chisquare_only_printouts(gpu, tmp_path):
+    """do_imfit_tests:98-99 (imfit_textout4c, 4d): --chisquare-only on the
+    n3073 case, with data-based chi^2 (the printed lines, character for
+    character) and with --cashstat (the printed numbers)."""
+    from imfit_gb300 import cli, fits
+    d = np.load(os.path.join(GOLDEN, "n3073.npz"))
+    names = ["X0", "Y0", "PA", "ell", "n", "I_e", "r_e", "PA", "ell", "I_0", "h"]
+    lines = [f"GAIN {float(d['gain'])}", f"READNOISE {float(d['read_noise'])}",
+             f"ORIGINAL_SKY {float(d['original_sky'])}"]
+    for j, (nm, v, lo, hi) in enumerate(zip(names, d["params"], d["lo"], d["hi"])):
+        if j in (2, 7):
+            lines.append("FUNCTION Sersic" if j == 2 else "FUNCTION Exponential")
+        lines.append(f"{nm} {float(v)!r} {float(lo)!r},{float(hi)!r}")
+    (tmp_path / "c.dat").write_text("\n".join(lines) + "\n")
+    for k, arr in (("data", d["data"]), ("mask", d["mask"]), ("psf", d["psf"])):
+        fits.write_image(str(tmp_path / f"{k}.fits"), arr)
+    base = [str(tmp_path / "c.dat"), str(tmp_path / "data.fits"), "--mask", str(tmp_path / "mask.fits"),
+            "--psf", str(tmp_path / "psf.fits"), "--chisquare-only"]
+    out = io.StringIO()
+    cli.run(base, out=out)
+    assert out.getvalue().splitlines() == ["  CHI-SQUARE = 235606.146670    (28743 DOF)", "",
+                                           "Reduced Chi^2 = 8.196992",
+                                           "AIC = 235628.155855, BIC = 235719.078524"]
+    # the Cash value, -3.06e8, prints one ulp-level digit past what a different
+    # summation order keeps: the numbers within 2e-6 (1e-14 relative)
+    out = io.StringIO()
+    cli.run(base + ["--cashstat"], out=out)
+    got = out.getvalue().splitlines()
+    assert len(got) == 2 and got[0].startswith("  CASH STATISTIC = ") and got[1].startswith("AIC = ")
+    cash = float(got[0].split("=")[1])
+    aic, bic = (float(x.split("=")[1]) for x in got[1].split(","))
+    for v, want in ((cash, -305659765.743167), (aic, -305659743.733982), (bic, -305659652.811314)):
+        assert abs(v - want) <= 2e-6, (v, want)
