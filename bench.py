@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--c5-threads", type=int, default=8, help="host threads driving the C5 size buckets")
     ap.add_argument("--c5-check", type=int, default=4, help="C5 cutouts re-fitted in FP64 on the CPU")
     ap.add_argument("--no-graphs", action="store_true", help="launch kernels one by one (for profilers)")
+    ap.add_argument("--jtwj", action="store_true",
+                    help="time the forward-mode normal equations (J^T W J, J^T W dev) instead of the gradient")
     return ap.parse_args()
 
 
@@ -108,14 +110,20 @@ def config_block(wl, extra=None):
 
 
 # ------------------------------------------------------------------ CPU arm
-def cpu_time(wl, units):
+CPU_WHAT = ("the project's C restatement of the reference's path (oracle/imfit_oracle.c: the reference's "
+            "ModelObject/Convolver/FunctionObject arithmetic, OpenMP over pixels), with the project's own FP64 "
+            "FFT on 7-smooth padded sizes standing in for FFTW; neither the reference's sources nor FFTW are "
+            "on the GPU host")
+
+
+def cpu_time(wl, units, threads=None):
     """Time `units` statistic+gradient units (1 + n_params evaluations each) of
-    the CPU port with all host threads; returns (evals/s, threads)."""
+    the CPU port with all host threads (or `threads`); returns (units/s, threads)."""
     import oracle
     oracle.build_restatement()
     m = oracle.OracleModel()
     m.set_fft_smooth(True)
-    threads = os.cpu_count() or 1
+    threads = threads or os.cpu_count() or 1
     m.set_max_threads(threads)
     from imfit_gb300 import workloads
     workloads.configure(m, wl)
@@ -155,7 +163,7 @@ def run_reference(args, rank, world):
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": f"{len(rates)} statistic+gradient units of {wl.name} "
                                        f"({wl.n_params + 1} FP64 model evaluations each), FFTs padded to "
-                                       f"7-smooth sizes"},
+                                       f"7-smooth sizes", "what": CPU_WHAT},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -323,6 +331,116 @@ def algorithmic_bytes(model, wl):
     return out
 
 
+# ------------------------------------------------- per-unit roofline (B, F)
+# transcendental (MUFU) operations of one profile evaluation: Sersic sqrt, lg2,
+# ex2, ex2; Exponential sqrt, ex2; GaussianRing sqrt, ex2; Moffat lg2, ex2;
+# Gaussian ex2; constant and planar backgrounds none
+SFU_PER_EVAL = {"Sersic": 4, "Exponential": 2, "GaussianRing": 2, "Moffat": 2, "Gaussian": 1,
+                "FlatSky": 0, "TiltedSkyPlane": 0}
+# CalculateSubsamples (func_sersic.cpp, func_exp.cpp, func_moffat.cpp,
+# func_gaussian.cpp): (index of the scale parameter in the function's own
+# parameters, inner radius with 20 subsamples, small-scale count)
+SUB_RULE = {"Sersic": (4, 4.0, 20), "Exponential": (3, 3.0, 20), "Moffat": (3, 3.0, 40), "Gaussian": (3, 3.0, 40)}
+
+
+def _n_subsamples(kind, scale, r):
+    _, rin, small = SUB_RULE[kind]
+    ns = np.ones(r.shape, dtype=np.int64)
+    near = r < 10.0
+    tiny = near & (scale <= 1.0) & (r <= 1.0)
+    ns[tiny] = min(100, int(small / scale)) if scale > 0 else 100
+    inner = near & ~tiny & (r <= rin)
+    ns[inner] = 20
+    outer = near & ~tiny & ~inner
+    ns[outer] = np.minimum(100, (20.0 / np.maximum(r[outer], 1e-30)).astype(np.int64))
+    return np.maximum(ns, 1)
+
+
+def sfu_ops_per_unit(wl, p):
+    """F(U): MUFU operations of one statistic + gradient evaluation at p: every
+    window pixel evaluated twice (forward, gradient recompute) and every
+    subsample of the pixels within radius 10 once (the precomputed table), on
+    the main window and, at k x resolution, on the oversampled region's window.
+    None for the 3-D line-of-sight functions (their count depends on the
+    adaptive integration)."""
+    from imfit_gb300 import workloads
+    names = workloads.param_names(wl.functions)
+    P = wl.psf.shape[0] if wl.psf is not None else 1
+    grids = [(np.arange(1 - P // 2, wl.ncols + P // 2 + 1, dtype=np.float64),
+              np.arange(1 - P // 2, wl.nrows + P // 2 + 1, dtype=np.float64))]
+    for psf, k, (x1, x2, y1, y2) in wl.regions:
+        h = psf.shape[0] // 2
+        grids.append((x1 + (0.5 / k - 0.5) + np.arange(-h, (x2 - x1 + 1) * k + h) / k,
+                      y1 + (0.5 / k - 0.5) + np.arange(-h, (y2 - y1 + 1) * k + h) / k))
+    total = 0
+    off = 0
+    x0 = y0 = 0.0
+    for i, (fn, new_set) in enumerate(wl.functions):
+        if new_set or i == 0:
+            x0, y0 = p[off], p[off + 1]
+            off += 2
+        nfp = {"Sersic": 5, "Exponential": 4, "FlatSky": 1, "GaussianRing": 5, "Moffat": 5, "Gaussian": 4,
+               "TiltedSkyPlane": 3}.get(fn)
+        if nfp is None:
+            return None
+        fp = p[off:off + nfp]
+        off += nfp
+        m = SFU_PER_EVAL[fn]
+        if m == 0:
+            continue
+        pa = np.deg2rad(fp[0] + 90.0)
+        q = 1.0 - fp[1]
+        for xs, ys in grids:
+            dx = xs[None, :] - x0
+            dy = ys[:, None] - y0
+            xp = dx * np.cos(pa) + dy * np.sin(pa)
+            yp = (-dx * np.sin(pa) + dy * np.cos(pa)) / q
+            r = np.sqrt(xp * xp + yp * yp)
+            total += 2 * m * r.size
+            if fn in SUB_RULE:
+                ns = _n_subsamples(fn, fp[SUB_RULE[fn][0]], r)
+                total += m * int(np.sum((ns * ns)[ns > 1]))
+    assert off == len(names)
+    return int(total)
+
+
+def survey_bytes_per_unit(wl):
+    """B(U) of the per-unit roofline as the survey defines it, on the
+    reference's padded grids (N_model = N + 2P, N_pad = N_model + P - 1):
+    data and weights in FP32, plus forward and adjoint of one r2c -> column
+    pass x PSF -> c2r convolution (5 complex passes + real read and write)
+    on the main grid and on each oversampled region."""
+    P = wl.psf.shape[0] if wl.psf is not None else 0
+
+    def conv(n_model, p):
+        n_pad = n_model + p - 1
+        return 2 * (40 * n_pad * (n_pad // 2 + 1) + 8 * n_model * n_model)
+
+    b = wl.ncols * wl.nrows * 8 + (conv(wl.nrows + 2 * P, P) if P else 0)
+    for psf, k, (x1, x2, y1, y2) in wl.regions:
+        po = psf.shape[0]
+        b += conv((x2 - x1 + 1) * k + 2 * po, po)
+    return int(b)
+
+
+def accuracy_vs_oracle(m, wl, P):
+    """Fast statistic and plain FP64 statistic of the GPU library against the
+    FP64 oracle (oracle/: the reference's algorithm on the reference's padded
+    sizes) on the same inputs, for up to four of the step's parameter vectors."""
+    import oracle
+    from imfit_gb300 import workloads
+    oracle.build_restatement()
+    o = workloads.configure(oracle.OracleModel(), wl)
+    o.set_max_threads(os.cpu_count() or 1)
+    fast, plain = [], []
+    for p in P[:4]:
+        so = o.get_fit_statistic(p)
+        fast.append(abs(m.fit_statistic_fast(p) - so) / abs(so))
+        plain.append(abs(m.get_fit_statistic(p) - so) / abs(so))
+    return {"stat_rel_err_vs_oracle": max(fast), "plain_fp64_stat_rel_err_vs_oracle": max(plain),
+            "vectors_checked": len(fast), "oracle": "oracle.OracleModel (FP64 C restatement, reference padding)"}
+
+
 def run_gpu(args, rank, local_rank, world):
     import torch
 
@@ -340,13 +458,20 @@ def run_gpu(args, rank, local_rank, world):
     P = np.array(wl.batch if wl.batch is not None else [wl.start], dtype=np.float64)
     B = P.shape[0]
 
-    # accuracy against the FP64 path on the same inputs
+    # accuracy: against the FP64 oracle (the reference's algorithm restated in
+    # C, on the reference's own padded FFT sizes) on the same inputs, and
+    # against this GPU's plain FP64 path
+    accuracy = accuracy_vs_oracle(m, wl, P) if rank == 0 else None
     s64 = m.get_fit_statistic(p0)
     s_fast, g_fast = m.statistic_and_gradient(p0)
     s_fd, g_fd = m.statistic_and_gradient_fd(p0)
-    stat_rel = abs(s_fast - s64) / abs(s64)
     gscale = np.abs(g_fd) + 1e-3 * np.max(np.abs(g_fd))
-    grad_rel_median = float(np.median(np.abs(g_fast - g_fd) / gscale))
+    gerr = np.abs(g_fast - g_fd) / gscale
+    if accuracy is not None:
+        accuracy.update({"stat_rel_err_vs_gpu_fp64": abs(s_fast - s64) / abs(s64),
+                         "grad_err_vs_gpu_fp64_fd": {"median": float(np.median(gerr)), "max": float(np.max(gerr)),
+                                                     "norm": "|g - g_fd| / (|g_fd| + 1e-3 max|g_fd|), "
+                                                             "forward differences, subsampling on"}})
 
     d_params = torch.tensor(P.ravel(), dtype=torch.float64, device=dev)
     d_stat = torch.zeros(B, dtype=torch.float64, device=dev)
@@ -389,7 +514,7 @@ def run_gpu(args, rank, local_rank, world):
     torch.cuda.synchronize()
     clocks = Clocks(local_rank)
     # NVTX range "timed_region": lets a profiler restrict its launch list to
-    # the timed steps (ncu --nvtx --nvtx-include "timed_region/")
+    # the timed steps (ncu --clock-control none --nvtx --nvtx-include "timed_region/")
     torch.cuda.nvtx.range_push("timed_region")
     with torch.cuda.stream(stream):
         for i in range(args.steps):
@@ -470,15 +595,39 @@ def run_gpu(args, rank, local_rank, world):
             "traffic": measured_traffic(args.config, dom)}
     prof = measured_profile(args.config, dom)
     if prof:  # the same kernel's compute-side utilisation (ncu, committed summary)
-        roof["ncu_sm_pct"] = prof.get("sm_pct")
-        roof["ncu_issue_active_pct"] = prof.get("issue_pct")
+        roof["ncu"] = {k: prof.get(k) for k in ("sm_pct", "issue_pct", "warps_active_pct", "alu_pct", "fma_pct",
+                                                "xu_pct", "dram_pct") if prof.get(k) is not None}
+        roof["limiter"] = prof.get("limiter")
+    # per-unit roofline T_roof = B / BW_HBM + F / P_SFU (one statistic + gradient
+    # evaluation); frac = T_roof x achieved units/s
+    try:
+        p_sfu = imfit_gb300.measure_sfu_rate(local_rank)
+    except Exception:  # measurement helper unavailable: report without it
+        p_sfu = None
+    F = sfu_ops_per_unit(wl, p0)
+    has_los = any(f in ("ExponentialDisk3D", "FerrersBar3D") for f, _ in wl.functions)
+    b_path = int(sum(v for k, v in ab.items() if has_los or not k.startswith("los_")))
+    b_survey = survey_bytes_per_unit(wl)
+    if F is not None and p_sfu:
+        t_roof = b_path / (hbm_peak * 1e9) + F / p_sfu
+        roof["per_unit"] = {"T_roof_us": round(t_roof * 1e6, 3), "frac": round(t_roof * value / world, 4),
+                            "bytes": b_path, "bytes_survey_padding": b_survey,
+                            "T_roof_us_survey_padding": round((b_survey / (hbm_peak * 1e9) + F / p_sfu) * 1e6, 3),
+                            "sfu_ops": F, "p_sfu_ops_per_s": p_sfu, "bw_gbs": hbm_peak,
+                            "bytes_definition": "sum of the fast path's per-kernel algorithmic bytes (FP32 spectra "
+                                                "on 7-smooth padded windows) for one unit",
+                            "sfu_definition": "2 x window pixels x MUFU ops per profile + subsamples of pixels "
+                                              "within radius 10, main window and oversampled region"}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         rate, threads = cpu_time(wl, args.cpu_units)
+        rate1, _ = cpu_time(wl, 1, threads=1)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "one_thread": {"value": rate1, "unit": UNIT, "cores": 1, "sample": f"1 unit of {wl.name}"},
                "sample": f"{args.cpu_units} statistic+gradient units of {wl.name} "
-                         f"({nP + 1} FP64 model evaluations each, forward differences)"}
+                         f"({nP + 1} FP64 model evaluations each, forward differences)",
+               "what": CPU_WHAT}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -490,7 +639,7 @@ def run_gpu(args, rank, local_rank, world):
                 "plain_fp64_fd": {"value": plain * world, "unit": UNIT, "steps": args.plain_steps,
                                   "evals_per_step": nP + 1},
                 "speedup_vs_plain_fp64_fd": {"device": value / (plain * world), "e2e": e2e / (plain * world)},
-                "accuracy": {"stat_rel_err_vs_fp64": stat_rel, "grad_rel_err_median_vs_fd": grad_rel_median},
+                "accuracy": accuracy,
                 "roofline": roof, "launch_shape": m.launch_shape(), "kernels_serial_calibration": kernel_table, "gpu_launches": kernels_per_step * args.steps,
                 "clocks": clk, "cpu_baseline": cpu}
         print(json.dumps(line), flush=True)
@@ -597,6 +746,56 @@ def run_c5(args, rank, local_rank, world):
         print(json.dumps(line), flush=True)
 
 
+def run_jtwj(args, rank, local_rank, world):
+    """Forward-mode normal equations of the LM path (imfit_BatchJtWJDevice):
+    statistic, J^T W J and J^T W dev for the step's parameter vectors; one
+    step = one call, L2 flushed before each.  Reported on its own line (not the
+    headline metric)."""
+    import torch
+
+    import imfit_gb300
+    from imfit_gb300 import build, workloads
+    build.build()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    wl = workload(args.config)
+    workloads.synthesize(wl, lambda: imfit_gb300.ModelObject(local_rank))
+    m = workloads.configure(imfit_gb300.ModelObject(local_rank), wl)
+    nP = wl.n_params
+    P = np.array(wl.batch if wl.batch is not None else [wl.start], dtype=np.float64)
+    B = P.shape[0]
+    stream = torch.cuda.ExternalStream(m.stream(), device=dev)
+    d_p = torch.tensor(P.ravel(), dtype=torch.float64, device=dev)
+    d_s = torch.zeros(B, dtype=torch.float64, device=dev)
+    d_a = torch.zeros(B * nP * nP, dtype=torch.float64, device=dev)
+    d_b = torch.zeros(B * nP, dtype=torch.float64, device=dev)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    m.set_use_graphs(not args.no_graphs)
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            flush.fill_(1.0)
+            m.batch_jtwj_device(B, d_p.data_ptr(), d_s.data_ptr(), d_a.data_ptr(), d_b.data_ptr())
+    torch.cuda.synchronize()
+    clocks = Clocks(local_rank)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    torch.cuda.nvtx.range_push("timed_region")
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            ev[i][0].record(stream)
+            m.batch_jtwj_device(B, d_p.data_ptr(), d_s.data_ptr(), d_a.data_ptr(), d_b.data_ptr())
+            ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
+    clk = clocks.stop()
+    t_ms = max_over_ranks(float(sum(a.elapsed_time(b) for a, b in ev)), world)
+    if rank == 0:
+        print(json.dumps({"metric": "forward-mode J^T W J evaluations/s", "value": world * B * args.steps / (t_ms / 1e3),
+                          "unit": "evals/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": t_ms / args.steps, "higher_is_better": True,
+                          "config": config_block(wl), "clocks": clk}), flush=True)
+
+
 def main():
     args = parse()
     rank, local_rank, world = dist_info()
@@ -612,6 +811,8 @@ def main():
         run_reference(args, rank, world)
     elif args.config == "C5":
         run_c5(args, rank, local_rank, world)
+    elif args.jtwj:
+        run_jtwj(args, rank, local_rank, world)
     else:
         run_gpu(args, rank, local_rank, world)
     if world > 1:

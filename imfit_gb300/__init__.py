@@ -104,6 +104,7 @@ _SIGS = [
     ("imfit_SetAutotune", _I, [_P, _I]),
     ("imfit_GetLaunchShape", _I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     ("imfit_SetLaunchShape", _I, [_P, _I, _I, _I, _I]),
+    ("imfit_MeasureSfuRate", _I, [_I, _DP]),
     ("imfit_HostAlloc", _I, [ctypes.c_ulong, ctypes.POINTER(_P)]),
     ("imfit_HostFree", _I, [_P]),
     ("imfit_ChiSquaredDeviceNoAlloc", _I, [_P, _P, _P, _L, _P, _P]),
@@ -141,6 +142,16 @@ def load_library(build_if_missing=True):
 
 def exported_symbols():
     return [s[0] for s in _SIGS]
+
+
+def measure_sfu_rate(device=0):
+    """Measured MUFU throughput of the device (transcendental ops/s)."""
+    lib = load_library()
+    v = ctypes.c_double()
+    st = lib.imfit_MeasureSfuRate(device, ctypes.byref(v))
+    if st != 0:
+        raise ImfitError(st, "imfit_MeasureSfuRate failed")
+    return v.value
 
 
 def minimize_normal_equations(fun, x0, fixed=None, lower=None, upper=None, ftol=1e-8, max_iter=0):

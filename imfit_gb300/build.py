@@ -26,6 +26,7 @@ UNITS = [
     ("k_noalloc.cu", ["--fmad=false"]),
     ("lm.cpp", []),
     ("k_los.cu", ["--fmad=false"]),
+    ("k_probe.cu", []),
 ]
 
 

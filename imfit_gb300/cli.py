@@ -62,7 +62,7 @@ def build_parser():
     ap.add_argument("--cashstat", action="store_true")
     ap.add_argument("--poisson-mlr", "--mlr", dest="poisson_mlr", action="store_true")
     ap.add_argument("--model-errors", action="store_true")
-    ap.add_argument("--chisquare-only", action="store_true")
+    ap.add_argument("--chisquare-only", "--fitstat-only", dest="chisquare_only", action="store_true")
     ap.add_argument("--de", action="store_true", help="differential evolution instead of LM")
     ap.add_argument("--de-lhs", action="store_true", help="--de with a Latin-hypercube initial population")
     ap.add_argument("--nm", action="store_true", help="Nelder-Mead simplex instead of LM")
@@ -510,7 +510,7 @@ def build_multimfit_parser():
     ap.add_argument("--cashstat", action="store_true")
     ap.add_argument("--poisson-mlr", "--mlr", dest="poisson_mlr", action="store_true")
     ap.add_argument("--model-errors", action="store_true")
-    ap.add_argument("--fitstat-only", action="store_true")
+    ap.add_argument("--fitstat-only", "--chisquare-only", dest="fitstat_only", action="store_true")
     ap.add_argument("--nm", action="store_true")
     ap.add_argument("--de", action="store_true")
     ap.add_argument("--seed", type=int, default=0)
@@ -540,8 +540,12 @@ def multimfit(argv=None, out=sys.stdout):
     off = section_offsets(cfg, images)  # image sections: X0/Y0 in the sections' pixel frames
     p0, lo, hi = p0 - off, lo - off, hi - off
     if args.fitstat_only:
+        # PrintFitStatistic (core/multimfit_main.cpp:686-692 -> core/print_results.cpp:160-181),
+        # the valid pixels summed over the images
         s = mm.get_fit_statistic(p0)
-        out.write(f"fit statistic = {s:.6f}\n")
+        n_free = int(np.sum(fx == 0))
+        n_valid = int(sum(h.n_valid for h in handles))
+        out.write("\n" + "\n".join(fit_statistic_lines(s, stat, n_free, n_valid)) + "\n\n")
         return p0 + off, s
     if args.de:
         from .solvers import differential_evolution

@@ -14,6 +14,8 @@
 //
 // Compiled with --fmad=false, like the plain FP64 kernels, so the arithmetic
 // matches them term for term.
+#include <cuda.h>  // CUcontext / CUresult types; driver calls go through cudaGetDriverEntryPointByVersion
+
 #include <cstdio>
 #include <mutex>
 
@@ -73,25 +75,84 @@ __global__ void __launch_bounds__(kThreads) k_chi2_noalloc_final(const double *_
   }
 }
 
-// Device address of g_noalloc_partials, looked up once per device with that
-// device current.  In host code the symbol itself is only a host-side handle.
-constexpr int kMaxDevices = 64;
-std::mutex g_lock;
-double *g_scratch[kMaxDevices] = {nullptr};
+// Device address of g_noalloc_partials, looked up with cudaGetSymbolAddress
+// once per CUDA context (with its device current) and cached under the
+// context's driver-assigned ID.  In host code the symbol itself is only a
+// host-side handle.  The ID is unique for the life of the process, so a
+// context re-created after cudaDeviceReset, or a caller's own driver-API
+// context on the same device, gets a fresh lookup instead of a stale address.
+// Where the driver's context queries are unavailable the cache falls back to
+// the device ordinal.
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long *);
 
-cudaError_t scratch_for_current_device(double **out) {
+struct ScratchSlot {
+  unsigned long long ctx;  // context ID (or ordinal + 1 in the fallback)
+  double *ptr;
+};
+constexpr int kMaxSlots = 64;
+std::mutex g_lock;
+ScratchSlot g_slots[kMaxSlots] = {};
+int g_nextSlot = 0;
+bool g_triedDriver = false;
+CtxGetCurrentFn g_getCurrent = nullptr;
+CtxGetIdFn g_getId = nullptr;
+
+// caller holds g_lock
+bool context_key(unsigned long long *key) {
+  if (!g_triedDriver) {
+    g_triedDriver = true;
+    cudaDriverEntryPointQueryResult q;
+    void *f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      g_getCurrent = reinterpret_cast<CtxGetCurrentFn>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      g_getId = reinterpret_cast<CtxGetIdFn>(f);
+  }
+  if (!g_getCurrent || !g_getId) return false;
+  CUcontext c = nullptr;
+  if (g_getCurrent(&c) != CUDA_SUCCESS || !c) return false;
+  unsigned long long id = 0;
+  if (g_getId(c, &id) != CUDA_SUCCESS) return false;
+  *key = id | (1ull << 63);  // disjoint from the ordinal keys
+  return true;
+}
+
+cudaError_t scratch_for_current_context(double **out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e) return e;
-  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
   std::lock_guard<std::mutex> g(g_lock);
-  if (!g_scratch[dev]) {
-    void *p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_partials);
-    if (e) return e;
-    g_scratch[dev] = static_cast<double *>(p);
+  unsigned long long key = 0;
+  bool haveKey = context_key(&key);
+  if (haveKey) {
+    for (const ScratchSlot &s : g_slots)
+      if (s.ptr && s.ctx == key) {
+        *out = s.ptr;
+        return cudaSuccess;
+      }
   }
-  *out = g_scratch[dev];
+  void *p = nullptr;
+  e = cudaGetSymbolAddress(&p, g_noalloc_partials);  // also makes the device's context current
+  if (e) return e;
+  if (!haveKey && !context_key(&key)) key = (unsigned long long)dev + 1;
+  if (!haveKey && key == (unsigned long long)dev + 1) {
+    // fallback keyed by ordinal: reuse this device's slot
+    for (ScratchSlot &s : g_slots)
+      if (s.ptr && s.ctx == key) {
+        s.ptr = static_cast<double *>(p);
+        *out = s.ptr;
+        return cudaSuccess;
+      }
+  }
+  ScratchSlot &s = g_slots[g_nextSlot];
+  g_nextSlot = (g_nextSlot + 1) % kMaxSlots;
+  s.ctx = key;
+  s.ptr = static_cast<double *>(p);
+  *out = s.ptr;
   return cudaSuccess;
 }
 
@@ -113,7 +174,7 @@ extern "C" int imfit_ChiSquaredDeviceNoAlloc(const double *d_model, const double
     return IMFIT_E_ARG;
   }
   double *scratch = nullptr;
-  cudaError_t e = scratch_for_current_device(&scratch);
+  cudaError_t e = scratch_for_current_context(&scratch);
   if (e) {
     set_global_error(cudaGetErrorString(e));
     return IMFIT_E_CUDA;

@@ -298,6 +298,12 @@ int imfit_GetLaunchShape(imfit_model_t m, int *rowsPerCta, int *rowThreads, int 
  * per CTA 1..8 of the column FFT (0: automatic) and threads per column CTA
  * (0: automatic). */
 int imfit_SetLaunchShape(imfit_model_t m, int rowsPerCta, int rowThreads, int colsPerCta, int colThreads);
+/* Measured MUFU (SFU) throughput of a device, in transcendental operations per
+ * second (lg2.approx / ex2.approx, every SM at full occupancy, CUDA events,
+ * best of three): the P_SFU of the per-unit roofline
+ * T_roof = bytes / HBM bandwidth + SFU operations / P_SFU.  Measurement helper
+ * with no counterpart in the reference; it changes no device setting. */
+int imfit_MeasureSfuRate(int device, double *opsPerSecond);
 /* Page-locked host memory for the host-buffer entry points (cudaMallocHost). */
 int imfit_HostAlloc(unsigned long bytes, void **ptr);
 int imfit_HostFree(void *ptr);
@@ -317,9 +323,11 @@ int imfit_HostFree(void *ptr);
  * file-scope device array of IMFIT_NOALLOC_MAX_BLOCKS * 5 doubles (160 KiB)
  * that every GPU using the library keeps until the process exits.  Inputs
  * larger than IMFIT_NOALLOC_MAX_PIXELS are rejected with IMFIT_E_ARG (see
- * imfit_LastError(NULL)).  The first call on each device looks up the array's
- * device address (with that device current); make that first call before any
- * stream capture.  All calls share the one array, so calls that overlap on
+ * imfit_LastError(NULL)).  The first call in each CUDA context looks up the
+ * array's device address (with that context's device current) and caches it
+ * under the context's driver ID, so a context re-created after
+ * cudaDeviceReset looks it up afresh; make that first call before any stream
+ * capture.  All calls share the one array, so calls that overlap on
  * the GPU (different streams, or different host threads, on one device)
  * race; serialise them.  The call only enqueues work on `stream`. */
 #define IMFIT_NOALLOC_MAX_BLOCKS 4096

@@ -22,7 +22,29 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 RESTATEMENT_SO = os.path.join(HERE, "_build", "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libimfit_ref.so")
-REFERENCE_DIR = os.environ.get("IMFIT_REFERENCE_DIR", "/root/reference")
+
+
+def _reference_dir():
+    """The reference checkout: IMFIT_REFERENCE_DIR, else the build recipe's
+    default (REFDIR in oracle/Makefile)."""
+    d = os.environ.get("IMFIT_REFERENCE_DIR")
+    if d:
+        return d
+    try:
+        r = subprocess.run(["make", "-s", "--no-print-directory", "-C", HERE, "print-refdir"],
+                           capture_output=True, text=True, timeout=30)
+        return r.stdout.strip() if r.returncode == 0 else ""
+    except (OSError, subprocess.SubprocessError):
+        return ""
+
+
+REFERENCE_DIR = _reference_dir()
+
+
+def reference_checkout():
+    """True where the reference's sources are present (never on a host that
+    only received this repository)."""
+    return bool(REFERENCE_DIR) and os.path.isdir(os.path.join(REFERENCE_DIR, "core"))
 
 # input-type codes (core/definitions.h)
 WEIGHTS_ARE_SIGMAS, WEIGHTS_ARE_VARIANCES, WEIGHTS_ARE_WEIGHTS = 100, 110, 120
@@ -37,7 +59,7 @@ def build_restatement():
 
 def build_reference():
     """Compile the reference's own sources (needs the reference checkout)."""
-    if not os.path.isdir(os.path.join(REFERENCE_DIR, "core")):
+    if not reference_checkout():
         return False
     subprocess.run(["make", "-s", "-C", HERE, "ref", f"REFDIR={REFERENCE_DIR}"], check=True)
     return True

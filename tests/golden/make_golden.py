@@ -1,9 +1,9 @@
 """Generate the committed golden fixtures from the reference.
 
-Run in a checkout that has the reference at /root/reference (or
-IMFIT_REFERENCE_DIR):  python tests/golden/make_golden.py [part ...]
+Run where the reference checkout is present (IMFIT_REFERENCE_DIR, else the
+oracle build recipe's REFDIR):  python tests/golden/make_golden.py [part ...]
 (parts: n3073 makeimage ic3478 pointsource mcmc multimfit makemultimages small_case
-imfit_regressions; all by default)
+imfit_regressions bench_sizes los3d; all by default)
 
 Outputs (all small .npz files next to this script):
   n3073.npz          the reference regression inputs tests/n3073rss_small.fits,
@@ -62,6 +62,15 @@ Outputs (all small .npz files next to this script):
                      saved bootstrap iterations of --seed 10 --bootstrap 5 on
                      ic3478rss_64x64.fits and its section [10:64,10:64]
                      (do_imfit_tests:133-134, bootstrap_output_seed10*_tail.dat).
+  bench_sizes.npz    the reference's own values (oracle/_ref) for the benchmark
+                     configurations C1-C4 at their full sizes (tests/bench_cases.py):
+                     a digest of the synthesized data, and per parameter vector
+                     the fit statistic and the model image's row sums, column
+                     sums and a fixed sample of 512 pixels.
+  los3d.npz          the reference's own values for a 96x96 ExponentialDisk3D +
+                     FerrersBar3D model (the C3 workload at 96 px, 15x15 PSF):
+                     the data, the model image without and with the PSF, and
+                     the chi^2 at the true and start vectors.
 """
 import re
 import os
@@ -259,6 +268,40 @@ def small_case():
     np.savez_compressed(os.path.join(HERE, "small_case.npz"), **out)
 
 
+def bench_sizes():
+    sys.path.insert(0, os.path.dirname(HERE))
+    import bench_cases
+    out = {}
+    for name in bench_cases.NAMES:
+        wl = bench_cases.build(name)
+        out[f"{name}_data"] = bench_cases.data_digest(wl)
+        m = workloads.configure(oracle.RefModel(), wl)
+        for tag, p in bench_cases.vectors(wl):
+            out[f"{name}_{tag}_params"] = np.asarray(p, dtype=np.float64)
+            out[f"{name}_{tag}_stat"] = m.get_fit_statistic(p)
+            rows, cols, sample = bench_cases.digest(m.get_model_image())
+            out[f"{name}_{tag}_rows"] = rows
+            out[f"{name}_{tag}_cols"] = cols
+            out[f"{name}_{tag}_sample"] = sample
+    np.savez_compressed(os.path.join(HERE, "bench_sizes.npz"), **out)
+
+
+def los3d():
+    wl = workloads.c3(size=96, psf_size=15)
+    workloads.synthesize(wl, oracle.RefModel)
+    out = {"data": wl.data, "truth": wl.truth, "start": wl.start, "psf": wl.psf}
+    nopsf = workloads.c3(size=96, psf_size=15)
+    nopsf.psf = None
+    m0 = workloads.configure(oracle.RefModel(), nopsf, with_data=False)
+    m = workloads.configure(oracle.RefModel(), wl)
+    for tag, p in (("truth", wl.truth), ("start", wl.start)):
+        m0.create_model_image(p)
+        out[f"{tag}_model_nopsf"] = m0.get_model_image()
+        out[f"{tag}_stat"] = m.get_fit_statistic(p)
+        out[f"{tag}_model"] = m.get_model_image()
+    np.savez_compressed(os.path.join(HERE, "los3d.npz"), **out)
+
+
 # (case, configuration, image, options with fixture file names, printed output)
 REGRESSIONS = [
     ("2", "imfit_config_ic3478_64x64.dat", "ic3478rss_64x64.fits", ["--gain=4.725", "--readnoise=4.3", "--sky=130.1"],
@@ -379,7 +422,7 @@ if __name__ == "__main__":
     oracle.build_reference()
     parts = {"n3073": n3073, "makeimage": makeimage, "ic3478": ic3478, "pointsource": pointsource,
              "mcmc": mcmc, "multimfit": multimfit, "makemultimages": makemultimages, "small_case": small_case,
-             "imfit_regressions": imfit_regressions}
+             "imfit_regressions": imfit_regressions, "bench_sizes": bench_sizes, "los3d": los3d}
     for name in (sys.argv[1:] or parts):
         parts[name]()
     for f in sorted(os.listdir(HERE)):

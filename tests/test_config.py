@@ -5,11 +5,11 @@ import os
 import numpy as np
 import pytest
 
+import oracle
 from imfit_gb300 import config, fits
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-REF_CONFIG = os.path.join(os.environ.get("IMFIT_REFERENCE_DIR", "/root/reference"), "tests", "imfit_reference",
-                          "imfit_config_n3073.dat")
+REF_CONFIG = os.path.join(oracle.REFERENCE_DIR, "tests", "imfit_reference", "imfit_config_n3073.dat")
 
 N3073_STYLE = """# comment line
 GAIN   4.725
@@ -145,8 +145,7 @@ def test_information_criteria_reproduce_printed_aic_bic():
         assert abs(aic - float(d[f"{case}__aic"])) <= 1.5e-6 and abs(bic - float(d[f"{case}__bic"])) <= 1.5e-6, case
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(os.environ.get("IMFIT_REFERENCE_DIR", "/root/reference"),
-                                                   "tests")), reason="reference checkout not present")
+@pytest.mark.skipif(not oracle.reference_checkout(), reason="reference checkout not present")
 @pytest.mark.parametrize("name", ["makeimage_reference/config_makeimage_sersictest512_bad1.dat",
                                   "makeimage_reference/config_makeimage_sersictest512_bad2.dat",
                                   "makeimage_reference/config_makeimage_sersictest512_bad3.dat",
@@ -162,6 +161,6 @@ def test_reference_bad_configurations_are_rejected(name):
     (do_imfit_tests:194-201, do_makeimage_tests:78-82; "Failure reading
     configuration file"): each is rejected here too."""
     from imfit_gb300 import config
-    root = os.path.join(os.environ.get("IMFIT_REFERENCE_DIR", "/root/reference"), "tests")
+    root = os.path.join(oracle.REFERENCE_DIR, "tests")
     with pytest.raises(config.ConfigError):
         config.read_config(os.path.join(root, name))

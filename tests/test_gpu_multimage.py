@@ -64,9 +64,15 @@ def test_multimfit_fitstat_only(gpu, tmp_path):
     from imfit_gb300 import cli
     d = np.load(os.path.join(GOLDEN, "multimfit.npz"))
     _write(tmp_path, d)
-    p, s = cli.multimfit([str(tmp_path / "flat.dat"), "--image-info", str(tmp_path / "flat_info.txt"),
-                          "--fitstat-only"], out=io.StringIO())
-    assert p.size == 8 and abs(s - float(d["d_chi2_printed"])) < 1e-12
+    for flag in ("--fitstat-only", "--chisquare-only"):
+        buf = io.StringIO()
+        p, s = cli.multimfit([str(tmp_path / "flat.dat"), "--image-info", str(tmp_path / "flat_info.txt"), flag],
+                             out=buf)
+        assert p.size == 8 and abs(s - float(d["d_chi2_printed"])) < 1e-12
+        # the printout's statistic lines (multimfit_textout1a:28-31)
+        assert buf.getvalue().strip().splitlines() == ["CHI-SQUARE = 6.750000    (5 DOF)", "",
+                                                       "Reduced Chi^2 = 1.350000",
+                                                       "AIC = 18.750000, BIC = 12.988325"]
 
 
 def test_multimfit_smallgauss_fit(gpu, tmp_path):
