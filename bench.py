@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--cpu-units", type=int, default=3, help="statistic+gradient units in the CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--config", default="C2", choices=["C1", "C2", "C3", "C4", "C5"])
+    ap.add_argument("--batch", type=int, default=0,
+                    help="C4: evaluate only the first N of the 256 parameter vectors (small profiling cases)")
     ap.add_argument("--c5-count", type=int, default=4096, help="cutouts in the C5 batch")
     ap.add_argument("--c5-threads", type=int, default=8, help="host threads driving the C5 size buckets")
     ap.add_argument("--c5-check", type=int, default=4, help="C5 cutouts re-fitted in FP64 on the CPU")
@@ -92,9 +94,12 @@ def dist_info():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
 
 
-def workload(name):
+def workload(name, batch=0):
     from imfit_gb300 import workloads
-    return {"C1": workloads.c1, "C2": workloads.c2, "C3": workloads.c3, "C4": workloads.c4}[name]()
+    wl = {"C1": workloads.c1, "C2": workloads.c2, "C3": workloads.c3, "C4": workloads.c4}[name]()
+    if batch and wl.batch is not None:
+        wl.batch = wl.batch[:batch]
+    return wl
 
 
 def config_block(wl, extra=None):
@@ -144,7 +149,7 @@ def cpu_time(wl, units, threads=None):
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    wl = workload(args.config)
+    wl = workload(args.config, args.batch)
     import oracle
     from imfit_gb300 import workloads
     workloads.synthesize(wl, oracle.OracleModel)
@@ -449,7 +454,7 @@ def run_gpu(args, rank, local_rank, world):
     build.build()
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
-    wl = workload(args.config)
+    wl = workload(args.config, args.batch)
     workloads.synthesize(wl, lambda: imfit_gb300.ModelObject(local_rank))
     m = workloads.configure(imfit_gb300.ModelObject(local_rank), wl)
     nP = wl.n_params
@@ -758,7 +763,7 @@ def run_jtwj(args, rank, local_rank, world):
     build.build()
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
-    wl = workload(args.config)
+    wl = workload(args.config, args.batch)
     workloads.synthesize(wl, lambda: imfit_gb300.ModelObject(local_rank))
     m = workloads.configure(imfit_gb300.ModelObject(local_rank), wl)
     nP = wl.n_params

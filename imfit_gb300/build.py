@@ -22,6 +22,7 @@ UNITS = [
     ("k_plain.cu", ["--fmad=false"]),
     ("k_fft.cu", []),
     ("k_fast.cu", []),
+    ("k_cols32.cu", []),
     ("model_object.cpp", ["-x", "cu"]),
     ("k_noalloc.cu", ["--fmad=false"]),
     ("lm.cpp", []),

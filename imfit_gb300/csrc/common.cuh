@@ -516,22 +516,41 @@ __device__ inline float fast_sqrt(float x) {
   return y;
 }
 
-// Profile value of a radial component at squared radius r2 (FP32).
+// Profile value of a radial component at squared radius r2 (FP32), for a
+// component type fixed at compile time (the pixel loops are instantiated per
+// type, so the per-pixel work carries no type dispatch and loads only the
+// constants its type uses).
+template <int TY>
+__device__ __forceinline__ float radial_t(const CompF32 &c, float r2) {
+  if constexpr (TY == F_SERSIC) {
+    float lr = 0.5f * fast_lg2(r2);
+    float u = fast_ex2((lr - c.s2) * c.s3);
+    return c.s0 * fast_ex2(c.s1 - c.s1 * u);
+  } else if constexpr (TY == F_EXP) {
+    return c.s0 * fast_ex2(-fast_sqrt(r2) * c.s1);
+  } else if constexpr (TY == F_GRING) {
+    float d = fast_sqrt(r2) - c.s1;
+    return c.s0 * fast_ex2(-d * d * c.s2);
+  } else if constexpr (TY == F_MOFFAT) {
+    return c.s0 * fast_ex2(-c.s2 * fast_lg2(fmaf(r2, c.s1, 1.f)));
+  } else if constexpr (TY == F_GAUSS) {
+    return c.s0 * fast_ex2(-r2 * c.s1);
+  } else if constexpr (TY == F_FLATSKY) {
+    return c.s0;
+  } else {
+    return 0.f;
+  }
+}
+
+// The same with the type chosen at run time.
 __device__ inline float radial32(const CompF32 &c, float r2) {
   switch (c.type) {
-    case F_SERSIC: {
-      float lr = 0.5f * fast_lg2(r2);
-      float u = fast_ex2((lr - c.s2) * c.s3);
-      return c.s0 * fast_ex2(c.s1 - c.s1 * u);
-    }
-    case F_EXP: return c.s0 * fast_ex2(-fast_sqrt(r2) * c.s1);
-    case F_GRING: {
-      float d = fast_sqrt(r2) - c.s1;
-      return c.s0 * fast_ex2(-d * d * c.s2);
-    }
-    case F_MOFFAT: return c.s0 * fast_ex2(-c.s2 * fast_lg2(fmaf(r2, c.s1, 1.f)));
-    case F_GAUSS: return c.s0 * fast_ex2(-r2 * c.s1);
-    case F_FLATSKY: return c.s0;
+    case F_SERSIC: return radial_t<F_SERSIC>(c, r2);
+    case F_EXP: return radial_t<F_EXP>(c, r2);
+    case F_GRING: return radial_t<F_GRING>(c, r2);
+    case F_MOFFAT: return radial_t<F_MOFFAT>(c, r2);
+    case F_GAUSS: return radial_t<F_GAUSS>(c, r2);
+    case F_FLATSKY: return radial_t<F_FLATSKY>(c, r2);
     default: return 0.f;
   }
 }
@@ -567,81 +586,81 @@ __device__ inline float comp_value32(const CompF32 &c, float dx, float dy, int *
   return s * (d * d);
 }
 
-// Analytic derivatives of one radial component at squared radius r2:
-// out[0..1] = d/dX0, d/dY0; out[2..] = d/d(function parameters in order).
-// Returns the number of function parameters written after the two centre slots;
-// *value (optional) receives the profile value itself.
-__device__ inline int radial_grad32(const CompF32 &c, const Geo &g, float scale, float *out,
-                                    float *value = nullptr) {
+// Function parameters of a radial type (the derivative slots after X0, Y0).
+template <int TY>
+__host__ __device__ constexpr int n_fparams() {
+  return TY == F_SERSIC ? 5 : TY == F_EXP ? 4 : TY == F_GRING ? 5 : TY == F_MOFFAT ? 5 : TY == F_GAUSS ? 4
+         : TY == F_TILTEDSKY ? 3 : 0;
+}
+
+// types whose GetValue subsamples near the centre (CalculateSubsamples)
+template <int TY>
+__host__ __device__ constexpr bool subsampling_t() {
+  return TY == F_SERSIC || TY == F_EXP || TY == F_MOFFAT || TY == F_GAUSS;
+}
+
+// Analytic derivatives of one radial component at squared radius r2, for a
+// type fixed at compile time:
+// out[0..1] = d/dX0, d/dY0; out[2..] = d/d(function parameters in order), each
+// multiplied by scale.  Returns the number of function parameters written
+// after the two centre slots; *value (optional) receives the profile value.
+template <int TY>
+__device__ __forceinline__ int radial_grad_t(const CompF32 &c, const Geo &g, float scale, float *out,
+                                             float *value = nullptr) {
   // 1/r from the SFU reciprocal square root, r = r2 / r (no IEEE division)
   const float rinv = (g.r2 > 0.f) ? rsqrtf(g.r2) : 0.f;
   const float r = g.r2 * rinv;
-  float I, dIdr, np = 0;
+  float I, dIdr;
+  constexpr int np = n_fparams<TY>();
   float pd[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // profile-parameter derivatives
-  switch (c.type) {
-    case F_SERSIC: {
-      float lr = 0.5f * fast_lg2(g.r2);
-      float u = fast_ex2((lr - c.s2) * c.s3);
-      float E = fast_ex2(c.s1 - c.s1 * u);
-      I = c.s0 * E;
-      // dI/dr = -I bn u / (n r)
-      float t = I * c.s4 * u * c.s3;
-      dIdr = -t * rinv;
-      // d/dn: -I [ bn'(u-1) - bn u ln(r/r_e) / n^2 ]
-      float lnrr = (u > 0.f) ? (lr - c.s2) * (float)kLn2 : 0.f;
-      pd[2] = -I * (c.s5 * (u - 1.f) - c.s4 * u * lnrr * c.s3 * c.s3);
-      pd[3] = E;                 // d/dI_e
-      pd[4] = t * c.pad;         // d/dr_e = I bn u / (n r_e)
-      np = 5;
-      break;
-    }
-    case F_EXP: {
-      float E = fast_ex2(-r * c.s1);
-      I = c.s0 * E;
-      dIdr = -I * c.s3;
-      pd[2] = E;                         // d/dI_0
-      pd[3] = I * r * c.s3 * c.s3;       // d/dh
-      np = 4;
-      break;
-    }
-    case F_GRING: {
-      float dd = r - c.s1;
-      float E = fast_ex2(-dd * dd * c.s2);
-      I = c.s0 * E;
-      const float is2 = c.s4;
-      dIdr = -I * dd * is2;
-      pd[2] = E;                              // d/dA
-      pd[3] = I * dd * is2;                   // d/dR_ring
-      pd[4] = I * dd * dd * is2 * c.pad;      // d/dsigma_r
-      np = 5;
-      break;
-    }
-    case F_MOFFAT: {
-      float D = fmaf(g.r2, c.s1, 1.f);
-      float lD = fast_lg2(D);
-      float E = fast_ex2(-c.s2 * lD);
-      I = c.s0 * E;
-      float Dinv = __fdividef(1.f, D);  // D >= 1
-      dIdr = -2.f * I * c.s2 * r * c.s1 * Dinv;
-      float dIdalpha = 2.f * I * c.s2 * g.r2 * c.s1 * Dinv * c.s6;
-      pd[2] = E;                                             // d/dI_0
-      pd[3] = dIdalpha * c.s3 * c.s7;                        // d/dfwhm
-      pd[4] = -I * lD * (float)kLn2 + dIdalpha * c.s5;       // d/dbeta
-      np = 5;
-      break;
-    }
-    case F_GAUSS: {
-      float E = fast_ex2(-g.r2 * c.s1);
-      I = c.s0 * E;
-      const float is2 = c.s4;
-      dIdr = -I * r * is2;
-      pd[2] = E;                              // d/dI_0
-      pd[3] = I * g.r2 * is2 * c.s3;          // d/dsigma
-      np = 4;
-      break;
-    }
-    default:
-      return 0;
+  if constexpr (TY == F_SERSIC) {
+    float lr = 0.5f * fast_lg2(g.r2);
+    float u = fast_ex2((lr - c.s2) * c.s3);
+    float E = fast_ex2(c.s1 - c.s1 * u);
+    I = c.s0 * E;
+    // dI/dr = -I bn u / (n r)
+    float t = I * c.s4 * u * c.s3;
+    dIdr = -t * rinv;
+    // d/dn: -I [ bn'(u-1) - bn u ln(r/r_e) / n^2 ]
+    float lnrr = (u > 0.f) ? (lr - c.s2) * (float)kLn2 : 0.f;
+    pd[2] = -I * (c.s5 * (u - 1.f) - c.s4 * u * lnrr * c.s3 * c.s3);
+    pd[3] = E;                 // d/dI_e
+    pd[4] = t * c.pad;         // d/dr_e = I bn u / (n r_e)
+  } else if constexpr (TY == F_EXP) {
+    float E = fast_ex2(-r * c.s1);
+    I = c.s0 * E;
+    dIdr = -I * c.s3;
+    pd[2] = E;                         // d/dI_0
+    pd[3] = I * r * c.s3 * c.s3;       // d/dh
+  } else if constexpr (TY == F_GRING) {
+    float dd = r - c.s1;
+    float E = fast_ex2(-dd * dd * c.s2);
+    I = c.s0 * E;
+    const float is2 = c.s4;
+    dIdr = -I * dd * is2;
+    pd[2] = E;                              // d/dA
+    pd[3] = I * dd * is2;                   // d/dR_ring
+    pd[4] = I * dd * dd * is2 * c.pad;      // d/dsigma_r
+  } else if constexpr (TY == F_MOFFAT) {
+    float D = fmaf(g.r2, c.s1, 1.f);
+    float lD = fast_lg2(D);
+    float E = fast_ex2(-c.s2 * lD);
+    I = c.s0 * E;
+    float Dinv = __fdividef(1.f, D);  // D >= 1
+    dIdr = -2.f * I * c.s2 * r * c.s1 * Dinv;
+    float dIdalpha = 2.f * I * c.s2 * g.r2 * c.s1 * Dinv * c.s6;
+    pd[2] = E;                                             // d/dI_0
+    pd[3] = dIdalpha * c.s3 * c.s7;                        // d/dfwhm
+    pd[4] = -I * lD * (float)kLn2 + dIdalpha * c.s5;       // d/dbeta
+  } else if constexpr (TY == F_GAUSS) {
+    float E = fast_ex2(-g.r2 * c.s1);
+    I = c.s0 * E;
+    const float is2 = c.s4;
+    dIdr = -I * r * is2;
+    pd[2] = E;                              // d/dI_0
+    pd[3] = I * g.r2 * is2 * c.s3;          // d/dsigma
+  } else {
+    return 0;
   }
   if (value) *value = I;
   // geometric chain rule; G = dI/dr / r
@@ -657,7 +676,20 @@ __device__ inline int radial_grad32(const CompF32 &c, const Geo &g, float scale,
 #pragma unroll
   for (int k = 2; k < 6; k++)
     if (k < np) out[2 + k] = scale * pd[k];
-  return (int)np;
+  return np;
+}
+
+// The same with the type chosen at run time.
+__device__ inline int radial_grad32(const CompF32 &c, const Geo &g, float scale, float *out,
+                                    float *value = nullptr) {
+  switch (c.type) {
+    case F_SERSIC: return radial_grad_t<F_SERSIC>(c, g, scale, out, value);
+    case F_EXP: return radial_grad_t<F_EXP>(c, g, scale, out, value);
+    case F_GRING: return radial_grad_t<F_GRING>(c, g, scale, out, value);
+    case F_MOFFAT: return radial_grad_t<F_MOFFAT>(c, g, scale, out, value);
+    case F_GAUSS: return radial_grad_t<F_GAUSS>(c, g, scale, out, value);
+    default: return 0;
+  }
 }
 
 }  // namespace imfit

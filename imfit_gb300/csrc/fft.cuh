@@ -32,15 +32,23 @@ __device__ __forceinline__ cplx<T> mul_si(cplx<T> a, int s) { return s > 0 ? cpl
 
 constexpr int kMaxRadixPasses = 16;
 
-// Plan of one transform length: radices applied in order, plus the twiddle
+// Plan of one transform length: radices applied in order (4 bits each,
+// first pass in the low bits: a scalar, so kernels keep the plan in
+// registers instead of indexing an array in local memory), plus the twiddle
 // table tw[k] = exp(-2*pi*i*k/n), k in [0,n).
 template <typename T>
 struct FFTPlan {
   int n;
   int npass;
-  int radix[kMaxRadixPasses];
+  unsigned long long radix;
   const cplx<T> *tw;
 };
+
+inline unsigned long long pack_radix(const int *radix, int npass) {
+  unsigned long long r = 0;
+  for (int i = 0; i < npass && i < kMaxRadixPasses; i++) r |= (unsigned long long)(radix[i] & 15) << (4 * i);
+  return r;
+}
 
 // length-R DFT in registers, sign s (-1 forward, +1 inverse)
 template <typename T>
@@ -150,14 +158,20 @@ __device__ __forceinline__ cplx<T> twiddle(const cplx<T> *tw, int idx, int s) {
   return w;
 }
 
-// Division by a divisor fixed for a loop: q = floor(x / d) as the high word
-// of x * ceil(2^32 / d) (exact while x * d < 2^32, which holds for every
-// index here: x < 2^16, d <= 4096).
+// Division by a divisor fixed for a loop, for 0 <= x < 2^21 and d >= 1:
+// q = floor((x + 0.5) * (1/d)) with the SFU reciprocal.  (x + 0.5) / d lies
+// at least 0.5/d away from every integer, and the computed product is within
+// 1.5 * 2^-23 relative of it (reciprocal within 1 ulp, one rounded multiply),
+// an error below that margin while x < 2^21.  Every index divided here is
+// below 2^16.  Replaces a 32-bit integer division (about twenty
+// instructions) by four, and its set-up by one.
 struct FastDiv {
-  unsigned m;
+  float inv;
   int d;
-  __device__ __forceinline__ explicit FastDiv(int dd) : m(dd > 1 ? 0xFFFFFFFFu / (unsigned)dd + 1u : 0u), d(dd) {}
-  __device__ __forceinline__ int div(int x) const { return d > 1 ? (int)__umulhi((unsigned)x, m) : x; }
+  __device__ __forceinline__ explicit FastDiv(int dd) : d(dd) {
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"((float)dd));
+  }
+  __device__ __forceinline__ int div(int x) const { return (int)(((float)x + 0.5f) * inv); }
 };
 
 // One radix-R Stockham pass over 'nl' lines of length n.
@@ -203,20 +217,23 @@ __device__ __forceinline__ void stockham_pass(const cplx<T> *__restrict__ src, c
 
 // Full transform of nl lines; ping-pongs between a and b.  Returns the buffer
 // that holds the result.  Must be called by all threads of the CTA.
+// tw: the twiddle table to read (null: the plan's own, in global memory;
+// kernels that stage the table in shared memory pass their copy).
 template <typename T>
 __device__ cplx<T> *block_fft(cplx<T> *a, cplx<T> *b, const FFTPlan<T> &p, int nl, int ls, int es,
-                              int s, bool lineFastest) {
+                              int s, bool lineFastest, const cplx<T> *tw = nullptr) {
   int Ns = 1;
   cplx<T> *src = a, *dst = b;
+  if (!tw) tw = p.tw;
   for (int ps = 0; ps < p.npass; ps++) {
-    const int R = p.radix[ps];
+    const int R = (int)((p.radix >> (4 * ps)) & 15ull);
     switch (R) {
-      case 2: stockham_pass<T, 2>(src, dst, p.n, Ns, nl, ls, es, p.tw, s, lineFastest); break;
-      case 3: stockham_pass<T, 3>(src, dst, p.n, Ns, nl, ls, es, p.tw, s, lineFastest); break;
-      case 4: stockham_pass<T, 4>(src, dst, p.n, Ns, nl, ls, es, p.tw, s, lineFastest); break;
-      case 5: stockham_pass<T, 5>(src, dst, p.n, Ns, nl, ls, es, p.tw, s, lineFastest); break;
-      case 7: stockham_pass<T, 7>(src, dst, p.n, Ns, nl, ls, es, p.tw, s, lineFastest); break;
-      default: stockham_pass<T, 8>(src, dst, p.n, Ns, nl, ls, es, p.tw, s, lineFastest); break;
+      case 2: stockham_pass<T, 2>(src, dst, p.n, Ns, nl, ls, es, tw, s, lineFastest); break;
+      case 3: stockham_pass<T, 3>(src, dst, p.n, Ns, nl, ls, es, tw, s, lineFastest); break;
+      case 4: stockham_pass<T, 4>(src, dst, p.n, Ns, nl, ls, es, tw, s, lineFastest); break;
+      case 5: stockham_pass<T, 5>(src, dst, p.n, Ns, nl, ls, es, tw, s, lineFastest); break;
+      case 7: stockham_pass<T, 7>(src, dst, p.n, Ns, nl, ls, es, tw, s, lineFastest); break;
+      default: stockham_pass<T, 8>(src, dst, p.n, Ns, nl, ls, es, tw, s, lineFastest); break;
     }
     __syncthreads();
     Ns *= R;

@@ -1,0 +1,201 @@
+// k_cols32.cu -- column pass of the FP32 convolution (fast path).
+//
+// The middle step of Convolver::ConvolveImage (core/convolver.cpp:365-411):
+// for each group of CPB adjacent half-spectrum columns, the column FFT, the
+// multiplication by the cached PSF spectrum (or its conjugate: the adjoint
+// correlation) with the 1/(Lx Ly) rescale, and the inverse column FFT, with
+// one read and one write of the spectrum.
+//
+// Memory side (what the per-kernel profile showed to be the limit: long
+// scoreboard stalls on one dependent 8-byte load per thread per element and
+// a second round of PSF-spectrum loads after the forward FFT):
+//   * every global read of the CTA -- the column group, the PSF spectrum's
+//     matching columns and the twiddle table -- is issued at once as
+//     cp.async copies into shared memory, so their latencies overlap each
+//     other and the PSF spectrum arrives while the forward FFT runs;
+//   * rows are moved in 16-byte pieces (two complex values; the spectrum
+//     and PSF-spectrum pitches are even, so every piece is 16-byte aligned),
+//     and written back with 16-byte vector stores;
+//   * the FFT passes read their twiddles from the shared-memory copy.
+// Rows at or beyond nRowsIn are the implicit zero padding and are never read.
+#include "kernels.h"
+#include "fft.cuh"
+
+namespace imfit {
+
+namespace {
+
+__device__ __forceinline__ unsigned smem_addr(const void *p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void cp_async8(void *dst, const void *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
+// Copy the first `pairs` 16-byte pieces (complex pairs) of CPB columns of
+// one row, zero the rest of the group; CPB == 1 moves one 8-byte value.
+template <int CPB>
+__device__ __forceinline__ void load_row(cplx<float> *dst, const cplx<float> *src, int pairs) {
+  if constexpr (CPB == 1) {
+    cp_async8(dst, src);
+  } else {
+#pragma unroll
+    for (int q = 0; q < CPB / 2; q++) {
+      if (q < pairs)
+        cp_async16(dst + 2 * q, src + 2 * q);
+      else
+        *reinterpret_cast<float4 *>(dst + 2 * q) = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  }
+}
+
+template <int CPB>
+__device__ __forceinline__ void zero_row(cplx<float> *dst) {
+  if constexpr (CPB == 1) {
+    *dst = cplx<float>{0.f, 0.f};
+  } else {
+#pragma unroll
+    for (int q = 0; q < CPB / 2; q++) *reinterpret_cast<float4 *>(dst + 2 * q) = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+}
+
+template <int CPB>
+__device__ __forceinline__ void store_row(cplx<float> *dst, const cplx<float> *src, int pairs) {
+  if constexpr (CPB == 1) {
+    *dst = *src;
+  } else {
+#pragma unroll
+    for (int q = 0; q < CPB / 2; q++)
+      if (q < pairs) *reinterpret_cast<float4 *>(dst + 2 * q) = *reinterpret_cast<const float4 *>(src + 2 * q);
+  }
+}
+
+// MODE 1: multiply by H (convolution); MODE 2: by conj(H) (adjoint correlation).
+// Batch entry y uses H + e * hBatch with e = y / hDiv, or hMap[e] when a map
+// is given (hBatch 0: one PSF spectrum for every entry).
+template <int MODE, int CPB>
+__global__ void __launch_bounds__(1024) k_cols32(cplx<float> *__restrict__ spec, long pitch, long batch,
+                                                int nColsC, int nRowsIn, int nRowsOut,
+                                                const cplx<float> *__restrict__ H, long hPitch, FFTPlan<float> plan,
+                                                float scale, long hBatch, int hDiv, const int *__restrict__ hMap) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int Ly = plan.n;
+  cplx<float> *tw = reinterpret_cast<cplx<float> *>(smem_raw);
+  cplx<float> *bufA = tw + Ly;
+  cplx<float> *bufB = bufA + (long)Ly * CPB;
+  cplx<float> *bufH = bufB + (long)Ly * CPB;
+  const int c0 = blockIdx.x * CPB;
+  const int nl = min(CPB, nColsC - c0);
+  if (nl <= 0) return;
+  const int pairs = (nl + 1) >> 1;
+  spec += blockIdx.y * batch + c0;
+  if (hBatch) {
+    const int e = blockIdx.y / hDiv;
+    H += (long)(hMap ? hMap[e] : e) * hBatch;
+  }
+  H += c0;
+  // all global reads of the CTA in flight at once
+  for (int t = threadIdx.x; t < Ly; t += blockDim.x) {
+    if (t < nRowsIn)
+      load_row<CPB>(bufA + (long)t * CPB, spec + (long)t * pitch, pairs);
+    else
+      zero_row<CPB>(bufA + (long)t * CPB);
+    load_row<CPB>(bufH + (long)t * CPB, H + (long)t * hPitch, pairs);
+  }
+  for (int i = threadIdx.x; 2 * i < Ly; i += blockDim.x) cp_async16(tw + 2 * i, plan.tw + 2 * i);
+  cp_async_wait_all();
+  __syncthreads();
+  cplx<float> *X = block_fft(bufA, bufB, plan, CPB, 1, CPB, -1, true, tw);
+  for (int idx = threadIdx.x; idx < Ly * CPB; idx += blockDim.x) {
+    cplx<float> h = bufH[idx];
+    if (MODE == 2) h.y = -h.y;
+    cplx<float> v = cmul(X[idx], h);
+    X[idx] = {v.x * scale, v.y * scale};
+  }
+  __syncthreads();
+  cplx<float> *other = (X == bufA) ? bufB : bufA;
+  cplx<float> *Y = block_fft(X, other, plan, CPB, 1, CPB, +1, true, tw);
+  for (int t = threadIdx.x; t < nRowsOut; t += blockDim.x)
+    store_row<CPB>(spec + (long)t * pitch, Y + (long)t * CPB, pairs);
+}
+
+template <int MODE, int CPB>
+cudaError_t launch_one(cplx<float> *s, long pitch, long batch, int nColsC, int nRowsIn, int nRowsOut,
+                       const cplx<float> *h, long hPitch, const FFTPlan<float> &p, float scale, int nBatch,
+                       cudaStream_t st, int threads, long hBatch, int hDiv, const int *hMap) {
+  auto kern = k_cols32<MODE, CPB>;
+  allow_max_smem((const void *)kern);
+  const size_t sm = sizeof(cplx<float>) * (size_t)p.n * (1 + 3 * CPB);
+  dim3 grid((nColsC + CPB - 1) / CPB, nBatch);
+  kern<<<grid, threads, sm, st>>>(s, pitch, batch, nColsC, nRowsIn, nRowsOut, h, hPitch, p, scale, hBatch, hDiv,
+                                  hMap);
+  return cudaGetLastError();
+}
+
+template <int MODE>
+cudaError_t launch_mode(int cpb, cplx<float> *s, long pitch, long batch, int nColsC, int nRowsIn, int nRowsOut,
+                        const cplx<float> *h, long hPitch, const FFTPlan<float> &p, float scale, int nBatch,
+                        cudaStream_t st, int threads, long hBatch, int hDiv, const int *hMap) {
+  switch (cpb) {
+    case 1: return launch_one<MODE, 1>(s, pitch, batch, nColsC, nRowsIn, nRowsOut, h, hPitch, p, scale, nBatch, st,
+                                       threads, hBatch, hDiv, hMap);
+    case 2: return launch_one<MODE, 2>(s, pitch, batch, nColsC, nRowsIn, nRowsOut, h, hPitch, p, scale, nBatch, st,
+                                       threads, hBatch, hDiv, hMap);
+    case 4: return launch_one<MODE, 4>(s, pitch, batch, nColsC, nRowsIn, nRowsOut, h, hPitch, p, scale, nBatch, st,
+                                       threads, hBatch, hDiv, hMap);
+    default: return launch_one<MODE, 8>(s, pitch, batch, nColsC, nRowsIn, nRowsOut, h, hPitch, p, scale, nBatch,
+                                        st, threads, hBatch, hDiv, hMap);
+  }
+}
+
+}  // namespace
+
+size_t cols32_smem(int Ly, int cpb) { return sizeof(cplx<float>) * (size_t)Ly * (1 + 3 * cpb); }
+
+cudaError_t launch_cols32(void *spec, long pitch, long batch, int nColsC, int nRowsIn, int nRowsOut, const void *H,
+                          long hPitch, const FFTLen &Ly, float scale, int mode, int nBatch, cudaStream_t st, int cpb,
+                          long hBatch, int hDiv, const int *hMap, int threads) {
+  if ((pitch & 1) || (hPitch & 1) || (Ly.full.n & 1) || mode < 1 || mode > 2) return cudaErrorInvalidValue;
+  int optin = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (cpb <= 0) cpb = (nColsC * nBatch >= 4 * 152) ? 4 : 2;
+  if (cpb != 1 && cpb != 2 && cpb != 4) cpb = 8;
+  while (cpb > 1 && cols32_smem(Ly.full.n, cpb) > (size_t)optin) cpb >>= 1;
+  if (cols32_smem(Ly.full.n, cpb) > (size_t)optin) return cudaErrorInvalidValue;
+  if (threads <= 0) threads = line_threads(Ly.full.n * cpb / 4);
+  FFTPlan<float> p;
+  p.n = Ly.full.n;
+  p.npass = Ly.full.npass;
+  p.radix = pack_radix(Ly.full.radix, Ly.full.npass);
+  p.tw = reinterpret_cast<const cplx<float> *>(Ly.full.tw32);
+  cplx<float> *s = reinterpret_cast<cplx<float> *>(spec);
+  const cplx<float> *h = reinterpret_cast<const cplx<float> *>(H);
+  if (mode == 1)
+    return launch_mode<1>(cpb, s, pitch, batch, nColsC, nRowsIn, nRowsOut, h, hPitch, p, scale, nBatch, st, threads,
+                          hBatch, hDiv, hMap);
+  return launch_mode<2>(cpb, s, pitch, batch, nColsC, nRowsIn, nRowsOut, h, hPitch, p, scale, nBatch, st, threads,
+                        hBatch, hDiv, hMap);
+}
+
+void cols32_prepare_kernels() {
+  allow_max_smem((const void *)k_cols32<1, 1>);
+  allow_max_smem((const void *)k_cols32<1, 2>);
+  allow_max_smem((const void *)k_cols32<1, 4>);
+  allow_max_smem((const void *)k_cols32<1, 8>);
+  allow_max_smem((const void *)k_cols32<2, 1>);
+  allow_max_smem((const void *)k_cols32<2, 2>);
+  allow_max_smem((const void *)k_cols32<2, 4>);
+  allow_max_smem((const void *)k_cols32<2, 8>);
+}
+
+}  // namespace imfit

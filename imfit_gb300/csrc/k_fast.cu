@@ -156,6 +156,25 @@ __device__ __forceinline__ void box_origin(const WinDesc &w, const CompF32 &c, i
   }
 }
 
+// Lane's share of the ns x ns subsamples of one pixel: acc[0] += value,
+// acc[1..] += derivatives (X0, Y0, then the function parameters).
+template <int TY>
+__device__ __forceinline__ void subsample_sum(const CompF32 &cc, int ns, float xs, float ys, float d, int lane,
+                                              float *acc) {
+  constexpr int NP = n_fparams<TY>();
+  float o[7];
+  const FastDiv byNs(ns);
+  for (int t = lane; t < ns * ns; t += 32) {
+    const int ii = byNs.div(t), jj = t - ii * ns;
+    const Geo gs = geo32(cc, xs + ii * d, ys + jj * d);
+    float v;
+    radial_grad_t<TY>(cc, gs, 1.f, o, &v);
+    acc[0] += v;
+#pragma unroll
+    for (int q = 0; q < 2 + NP; q++) acc[1 + q] += o[q];
+  }
+}
+
 // One warp per box pixel: the average over the pixel's ns x ns subsamples of
 // the profile and of its 7 derivatives (X0, Y0, then the function parameters).
 __global__ void __launch_bounds__(256) k_fast_subsample(FastArgs a, WinDesc w, int win) {
@@ -173,7 +192,8 @@ __global__ void __launch_bounds__(256) k_fast_subsample(FastArgs a, WinDesc w, i
   const int lane = threadIdx.x & 31;
   const int p = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (p >= side * side) return;
-  const int row = row0 + p / side, col = col0 + p % side;
+  const int pr = FastDiv(side).div(p);
+  const int row = row0 + pr, col = col0 + (p - pr * side);
   if (row < 0 || row >= w.rows || col < 0 || col >= w.cols) return;
   float dx, dy;
   win_offsets(w, cc, row, col, dx, dy);
@@ -183,16 +203,11 @@ __global__ void __launch_bounds__(256) k_fast_subsample(FastArgs a, WinDesc w, i
   const float d = 1.f / ns;
   const float xs = dx - 0.5f + 0.5f * d, ys = dy - 0.5f + 0.5f * d;
   float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-  float o[7];
-  for (int t = lane; t < ns * ns; t += 32) {
-    const int ii = t / ns, jj = t - ii * ns;
-    const Geo gs = geo32(cc, xs + ii * d, ys + jj * d);
-    float v;
-    const int np = radial_grad32(cc, gs, 1.f, o, &v);
-    acc[0] += v;
-#pragma unroll
-    for (int q = 0; q < 7; q++)
-      if (q < 2 + np) acc[1 + q] += o[q];
+  switch (cc.type) {
+    case F_SERSIC: subsample_sum<F_SERSIC>(cc, ns, xs, ys, d, lane, acc); break;
+    case F_EXP: subsample_sum<F_EXP>(cc, ns, xs, ys, d, lane, acc); break;
+    case F_MOFFAT: subsample_sum<F_MOFFAT>(cc, ns, xs, ys, d, lane, acc); break;
+    default: subsample_sum<F_GAUSS>(cc, ns, xs, ys, d, lane, acc); break;
   }
 #pragma unroll
   for (int q = 0; q < 8; q++) acc[q] = warp_sum(acc[q]);
@@ -215,6 +230,44 @@ __device__ __forceinline__ float sub_value(const FastArgs &a, const int *box, in
 }
 
 // ------------------------------------------------------ eval + row r2c
+// Adds component cc's value at every pixel of the CTA's rows to the row
+// buffer (one thread per complex point = two pixels; every pass maps the
+// same points to the same thread, so the passes need no barrier).
+template <int TY>
+__device__ __forceinline__ void eval_pixels(const CompF32 cc, const WinDesc &w, int row0, int nl, int M, int ls,
+                                            const FastDiv &byM, cplx<float> *buf, const float *tab, int side,
+                                            int bc0, int br0) {
+  for (int idx = threadIdx.x; idx < nl * M; idx += blockDim.x) {
+    const int l = byM.div(idx), k = idx - l * M;
+    const int row = row0 + l;
+    float v[2] = {0.f, 0.f};
+#pragma unroll
+    for (int e = 0; e < 2; e++) {
+      const int col = 2 * k + e;
+      if (col >= w.cols) continue;
+      float dx, dy;
+      win_offsets(w, cc, row, col, dx, dy);
+      if constexpr (TY == F_TILTEDSKY) {
+        v[e] = plane32(cc, dx, dy);
+      } else {
+        const Geo g = geo32(cc, dx, dy);
+        if (subsampling_t<TY>() && cc.subsample && g.r2 < 100.f && n_subsamples32(cc, fast_sqrt(g.r2)) > 1) {
+          // subsampled pixel: the precomputed table (a direct average outside
+          // the box, which the radius bound rules out)
+          const int br = row - br0, bc = col - bc0;
+          v[e] = (br >= 0 && br < side && bc >= 0 && bc < side) ? tab[((long)br * side + bc) * 8]
+                                                                : comp_value32(cc, dx, dy, nullptr);
+        } else {
+          v[e] = radial_t<TY>(cc, g.r2);
+        }
+      }
+    }
+    cplx<float> &z = buf[l * ls + k];
+    z.x += v[0];
+    z.y += v[1];
+  }
+}
+
 __global__ void __launch_bounds__(1024) k_fast_eval_r2c(FastArgs a, WinDesc w, FFTPlan<float> plan,
                                                        const cplx<float> *__restrict__ twL, int rpb, int win) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -235,36 +288,41 @@ __global__ void __launch_bounds__(1024) k_fast_eval_r2c(FastArgs a, WinDesc w, F
   const int nl = min(rpb, w.rows - row0);
   __syncthreads();
   if (nl <= 0) return;
-  // one thread per complex point (two pixels)
+  const FastDiv byM(M), byM1(M + 1);
   for (int idx = threadIdx.x; idx < nl * M; idx += blockDim.x) {
-    const int l = idx / M, k = idx - l * M;
-    const int row = row0 + l;
-    float v[2] = {0.f, 0.f};
-#pragma unroll
-    for (int e = 0; e < 2; e++) {
-      const int col = 2 * k + e;
-      if (col < w.cols) {
-        for (int c = 0; c < nC; c++) {
-          const CompF32 &cc = sc[c];
-          if (!in_rows(cc.type)) continue;
-          float dx, dy;
-          win_offsets(w, cc, row, col, dx, dy);
-          const Geo g = geo32(cc, dx, dy);
-          if (sub_count(cc, g) > 1)
-            v[e] += sub_value(a, boxes + 2 * c, b, c, win, cc, row, col, dx, dy);
-          else
-            v[e] += cc.type == F_TILTEDSKY ? plane32(cc, dx, dy) : radial32(cc, g.r2);
-        }
-        if (w.losVal) v[e] += w.losVal[((long)b * w.rows + row) * w.cols + col];
-      }
+    const int l = byM.div(idx);
+    bufA[l * ls + idx - l * M] = {0.f, 0.f};
+  }
+  const int side = win ? a.boxReg : a.boxMain;
+  for (int c = 0; c < nC; c++) {
+    const CompF32 cc = sc[c];
+    if (!in_rows(cc.type)) continue;
+    const float *tab = a.subTab + sub_base(a, b, c, win);
+    const int bc0 = boxes[2 * c], br0 = boxes[2 * c + 1];
+    switch (cc.type) {
+      case F_SERSIC: eval_pixels<F_SERSIC>(cc, w, row0, nl, M, ls, byM, bufA, tab, side, bc0, br0); break;
+      case F_EXP: eval_pixels<F_EXP>(cc, w, row0, nl, M, ls, byM, bufA, tab, side, bc0, br0); break;
+      case F_GRING: eval_pixels<F_GRING>(cc, w, row0, nl, M, ls, byM, bufA, tab, side, bc0, br0); break;
+      case F_MOFFAT: eval_pixels<F_MOFFAT>(cc, w, row0, nl, M, ls, byM, bufA, tab, side, bc0, br0); break;
+      case F_GAUSS: eval_pixels<F_GAUSS>(cc, w, row0, nl, M, ls, byM, bufA, tab, side, bc0, br0); break;
+      case F_TILTEDSKY: eval_pixels<F_TILTEDSKY>(cc, w, row0, nl, M, ls, byM, bufA, tab, side, bc0, br0); break;
+      default: break;
     }
-    bufA[l * ls + k] = {v[0], v[1]};
+  }
+  if (w.losVal) {  // the 3-D components' line-of-sight sums
+    for (int idx = threadIdx.x; idx < nl * M; idx += blockDim.x) {
+      const int l = byM.div(idx), k = idx - l * M;
+      const float *lv = w.losVal + ((long)b * w.rows + row0 + l) * w.cols;
+      cplx<float> &z = bufA[l * ls + k];
+      if (2 * k < w.cols) z.x += lv[2 * k];
+      if (2 * k + 1 < w.cols) z.y += lv[2 * k + 1];
+    }
   }
   __syncthreads();
   cplx<float> *Z = block_fft(bufA, bufB, plan, nl, ls, 1, -1, false);
   cplx<float> *out = w.spec + (long)b * w.specBatch;
   for (int idx = threadIdx.x; idx < nl * (M + 1); idx += blockDim.x) {
-    const int l = idx / (M + 1), k = idx - l * (M + 1);
+    const int l = byM1.div(idx), k = idx - l * (M + 1);
     out[(long)(row0 + l) * w.specPitch + k] = r2c_post(Z + l * ls, k, M, twL);
   }
 }
@@ -376,13 +434,14 @@ __global__ void __launch_bounds__(1024) k_fast_region_down(FastArgs a, FastGeom 
   cplx<float> *bufA = bufX + k * ls;
   cplx<float> *bufB = bufA + k * ls;
   const cplx<float> *in = rspec + (long)b * g.rSpecBatch + (long)(s * k) * g.rSpecPitch;
+  const FastDiv byM(M), byM1(M + 1);
   for (int idx = threadIdx.x; idx < k * (M + 1); idx += blockDim.x) {
-    const int l = idx / (M + 1), kk = idx - l * (M + 1);
+    const int l = byM1.div(idx), kk = idx - l * (M + 1);
     bufX[l * ls + kk] = in[(long)l * g.rSpecPitch + kk];
   }
   __syncthreads();
   for (int idx = threadIdx.x; idx < k * M; idx += blockDim.x) {
-    const int l = idx / M, kk = idx - l * M;
+    const int l = byM.div(idx), kk = idx - l * M;
     bufA[l * ls + kk] = c2r_pre(bufX + l * ls, kk, M, twL);
   }
   __syncthreads();
@@ -477,14 +536,15 @@ __global__ void __launch_bounds__(1024) k_fast_stat_rows(FastArgs a, FastGeom g,
     a.weight += img * a.dataStride;
   }
   if (a.count && a.countStride) a.count += (a.entry ? a.entry[b] : b) * a.countStride;  // batched bootstrap
+  const FastDiv byM(M), byM1(M + 1);
   if (nl > 0) {
     for (int idx = threadIdx.x; idx < nl * (M + 1); idx += blockDim.x) {
-      const int l = idx / (M + 1), k = idx - l * (M + 1);
+      const int l = byM1.div(idx), k = idx - l * (M + 1);
       bufX[l * ls + k] = spec[(long)(row0 + l) * g.specPitch + k];
     }
     __syncthreads();
     for (int idx = threadIdx.x; idx < nl * M; idx += blockDim.x) {
-      const int l = idx / M, k = idx - l * M;
+      const int l = byM.div(idx), k = idx - l * M;
       bufA[l * ls + k] = c2r_pre(bufX + l * ls, k, M, twL);
     }
     __syncthreads();
@@ -493,7 +553,7 @@ __global__ void __launch_bounds__(1024) k_fast_stat_rows(FastArgs a, FastGeom g,
     const float bg = a.bgLevel[2 * b];
     // one thread per complex point = two data columns
     for (int idx = threadIdx.x; idx < nl * M; idx += blockDim.x) {
-      const int l = idx / M, k = idx - l * M;
+      const int l = byM.div(idx), k = idx - l * M;
       const int row = row0 + l;
       const cplx<float> zz = Z[l * ls + k];
       float gv[2] = {0.f, 0.f};
@@ -540,7 +600,7 @@ __global__ void __launch_bounds__(1024) k_fast_stat_rows(FastArgs a, FastGeom g,
       cplx<float> *other = (G == bufA) ? bufB : bufA;
       cplx<float> *R = block_fft(G, other, plan, nl, ls, 1, -1, false);
       for (int idx = threadIdx.x; idx < nl * (M + 1); idx += blockDim.x) {
-        const int l = idx / (M + 1), k = idx - l * (M + 1);
+        const int l = byM1.div(idx), k = idx - l * (M + 1);
         spec[(long)(row0 + l) * g.specPitch + k] = r2c_post(R + l * ls, k, M, twL);
       }
     }
@@ -600,6 +660,54 @@ __global__ void __launch_bounds__(1024) k_fast_region_g_r2c(FastArgs a, FastGeom
 }
 
 // ---------------------------------------- gradient pass over the window
+// acc[0..1+NP] += r~ * dm/dtheta over the CTA's window pixels for component cc
+// (X0, Y0, then its function parameters); subsampled pixels from the table.
+template <int TY>
+__device__ __forceinline__ void grad_pixels(const CompF32 cc, const WinDesc &w, const float *rt, int ls, int row0,
+                                            int npix, const FastDiv &byCols, const float *tab, int side, int bc0,
+                                            int br0, float *acc) {
+  constexpr int NP = n_fparams<TY>();
+  float o[7];
+  for (int idx = threadIdx.x; idx < npix; idx += blockDim.x) {
+    const int l = byCols.div(idx), col = idx - l * w.cols;
+    const int row = row0 + l;
+    const float r = rt[2 * l * ls + col];
+    float dx, dy;
+    win_offsets(w, cc, row, col, dx, dy);
+    if constexpr (TY == F_TILTEDSKY) {
+      if (r == 0.f) continue;
+      plane_grad32(cc, dx, dy, r, o);
+    } else {
+      const Geo g = geo32(cc, dx, dy);
+      if (subsampling_t<TY>() && cc.subsample && g.r2 < 100.f) {
+        const int ns = n_subsamples32(cc, fast_sqrt(g.r2));
+        if (ns > 1) {
+          const int br = row - br0, bc = col - bc0;
+          if (br >= 0 && br < side && bc >= 0 && bc < side) {
+            const float *t = tab + ((long)br * side + bc) * 8 + 1;
+#pragma unroll
+            for (int q = 0; q < 2 + NP; q++) acc[q] += r * t[q];
+          } else {
+            // outside the precomputed box (not reached for radius < 10): direct average
+            const float d = 1.f / ns;
+            for (int t = 0; t < ns * ns; t++) {
+              const Geo gs = geo32(cc, dx - 0.5f + (t / ns + 0.5f) * d, dy - 0.5f + (t % ns + 0.5f) * d);
+              radial_grad_t<TY>(cc, gs, r * d * d, o);
+#pragma unroll
+              for (int q = 0; q < 2 + NP; q++) acc[q] += o[q];
+            }
+          }
+          continue;
+        }
+      }
+      if (r == 0.f) continue;
+      radial_grad_t<TY>(cc, g, r, o);
+    }
+#pragma unroll
+    for (int q = 0; q < 2 + NP; q++) acc[q] += o[q];
+  }
+}
+
 __global__ void __launch_bounds__(1024) k_fast_grad_rows(FastArgs a, WinDesc w, FFTPlan<float> plan,
                                                         const cplx<float> *__restrict__ twL, int rpb,
                                                         float *__restrict__ gradPart, int blockBase, int win) {
@@ -624,14 +732,15 @@ __global__ void __launch_bounds__(1024) k_fast_grad_rows(FastArgs a, WinDesc w, 
   const int row0 = blockIdx.x * rpb;
   const int nl = min(rpb, w.rows - row0);
   const cplx<float> *spec = w.spec + (long)b * w.specBatch;
+  const FastDiv byM(M), byM1(M + 1), byCols(w.cols);
   for (int idx = threadIdx.x; idx < max(nl, 0) * (M + 1); idx += blockDim.x) {
-    const int l = idx / (M + 1), k = idx - l * (M + 1);
+    const int l = byM1.div(idx), k = idx - l * (M + 1);
     bufX[l * ls + k] = spec[(long)(row0 + l) * w.specPitch + k];
   }
   __syncthreads();
   if (nl > 0) {
     for (int idx = threadIdx.x; idx < nl * M; idx += blockDim.x) {
-      const int l = idx / M, k = idx - l * M;
+      const int l = byM.div(idx), k = idx - l * M;
       bufA[l * ls + k] = c2r_pre(bufX + l * ls, k, M, twL);
     }
     __syncthreads();
@@ -641,55 +750,26 @@ __global__ void __launch_bounds__(1024) k_fast_grad_rows(FastArgs a, WinDesc w, 
     const int npix = nl * w.cols;
     if (w.losRt)
       for (int idx = threadIdx.x; idx < npix; idx += blockDim.x) {
-        const int l = idx / w.cols, col = idx - l * w.cols;
+        const int l = byCols.div(idx), col = idx - l * w.cols;
         w.losRt[((long)b * w.rows + row0 + l) * w.cols + col] = rt[2 * l * ls + col];
       }
     for (int c = 0; c < nC; c++) {
-      const CompF32 &cc = sc[c];
+      const CompF32 cc = sc[c];
       if (!in_rows(cc.type)) continue;
       const int side = win ? a.boxReg : a.boxMain;
       const float *tab = a.subTab + sub_base(a, b, c, win);
+      const int bc0 = boxes[2 * c], br0 = boxes[2 * c + 1];
       float acc[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-      float o[7];
-      const FastDiv byCols(w.cols);
-      for (int idx = threadIdx.x; idx < npix; idx += blockDim.x) {
-        const int l = byCols.div(idx), col = idx - l * w.cols;
-        const int row = row0 + l;
-        const float r = rt[2 * l * ls + col];
-        float dx, dy;
-        win_offsets(w, cc, row, col, dx, dy);
-        const Geo g = geo32(cc, dx, dy);
-        int np;
-        if (sub_count(cc, g) > 1) {
-          const int br = row - boxes[2 * c + 1], bc = col - boxes[2 * c];
-          if (br >= 0 && br < side && bc >= 0 && bc < side) {
-            const float *t = tab + ((long)br * side + bc) * 8 + 1;
-#pragma unroll
-            for (int q = 0; q < 7; q++) o[q] = r * t[q];
-            np = 5;  // unused slots of the table are zero
-          } else {
-            // outside the precomputed box (not reached for radius < 10): direct average
-            const int ns = sub_count(cc, g);
-            const float d = 1.f / ns;
-            float s7[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-            for (int t = 0; t < ns * ns; t++) {
-              const Geo gs = geo32(cc, dx - 0.5f + (t / ns + 0.5f) * d, dy - 0.5f + (t % ns + 0.5f) * d);
-              const int n2 = radial_grad32(cc, gs, r * d * d, o);
-#pragma unroll
-              for (int q = 0; q < 7; q++)
-                if (q < 2 + n2) s7[q] += o[q];
-            }
-#pragma unroll
-            for (int q = 0; q < 7; q++) o[q] = s7[q];
-            np = 5;
-          }
-        } else {
-          if (r == 0.f) continue;
-          np = cc.type == F_TILTEDSKY ? plane_grad32(cc, dx, dy, r, o) : radial_grad32(cc, g, r, o);
-        }
-#pragma unroll
-        for (int q = 0; q < 7; q++)
-          if (q < 2 + np) acc[q] += o[q];
+      switch (cc.type) {
+        case F_SERSIC: grad_pixels<F_SERSIC>(cc, w, rt, ls, row0, npix, byCols, tab, side, bc0, br0, acc); break;
+        case F_EXP: grad_pixels<F_EXP>(cc, w, rt, ls, row0, npix, byCols, tab, side, bc0, br0, acc); break;
+        case F_GRING: grad_pixels<F_GRING>(cc, w, rt, ls, row0, npix, byCols, tab, side, bc0, br0, acc); break;
+        case F_MOFFAT: grad_pixels<F_MOFFAT>(cc, w, rt, ls, row0, npix, byCols, tab, side, bc0, br0, acc); break;
+        case F_GAUSS: grad_pixels<F_GAUSS>(cc, w, rt, ls, row0, npix, byCols, tab, side, bc0, br0, acc); break;
+        case F_TILTEDSKY:
+          grad_pixels<F_TILTEDSKY>(cc, w, rt, ls, row0, npix, byCols, tab, side, bc0, br0, acc);
+          break;
+        default: break;
       }
       // block reduction of acc[0..6]
 #pragma unroll
@@ -882,13 +962,56 @@ __global__ void __launch_bounds__(256) k_fast_reduce(FastArgs a, int nGradBlocks
 }
 
 // ------------------------------------ forward-mode derivative images (JtWJ)
+// Adds component cc's dm/dtheta at every pixel of window row `row` to the
+// derivative lines sl[q] (q: X0, Y0, then its function parameters; -1 = not
+// a derivative line); each column belongs to one thread.
+template <int TY>
+__device__ __forceinline__ void deriv_pixels(const CompF32 cc, const WinDesc &w, int row, const int *sl,
+                                             float *lines, int ls, const float *tab, int side, int bc0, int br0) {
+  constexpr int NP = n_fparams<TY>();
+  for (int col = threadIdx.x; col < w.cols; col += blockDim.x) {
+    float dx, dy;
+    win_offsets(w, cc, row, col, dx, dy);
+    float o[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if constexpr (TY == F_TILTEDSKY) {
+      plane_grad32(cc, dx, dy, 1.f, o);
+    } else {
+      const Geo g = geo32(cc, dx, dy);
+      const int ns = (subsampling_t<TY>() && cc.subsample && g.r2 < 100.f) ? n_subsamples32(cc, fast_sqrt(g.r2)) : 1;
+      if (ns > 1) {
+        const int br = row - br0, bc = col - bc0;
+        if (br >= 0 && br < side && bc >= 0 && bc < side) {
+          const float *t = tab + ((long)br * side + bc) * 8 + 1;
+#pragma unroll
+          for (int q = 0; q < 2 + NP; q++) o[q] = t[q];
+        } else {
+          // outside the precomputed box (not reached for radius < 10): direct average
+          const float d = 1.f / ns;
+          float t7[7];
+          for (int t = 0; t < ns * ns; t++) {
+            const Geo gs = geo32(cc, dx - 0.5f + (t / ns + 0.5f) * d, dy - 0.5f + (t % ns + 0.5f) * d);
+            radial_grad_t<TY>(cc, gs, d * d, t7);
+#pragma unroll
+            for (int q = 0; q < 2 + NP; q++) o[q] += t7[q];
+          }
+        }
+      } else {
+        radial_grad_t<TY>(cc, g, 1.f, o);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 2 + NP; q++)
+      if (sl[q] >= 0) lines[2 * sl[q] * ls + col] += o[q];
+  }
+}
+
 // One CTA per (window row, parameter vector): dm/dtheta_j of every
 // non-background parameter at every pixel of the row -- analytic, subsampled
 // pixels from the precomputed table -- accumulated into nD real lines in
 // shared memory (a pixel belongs to one thread, so no atomics), then the nD
 // row FFTs.  Derivative spectra of parameter vector b are the nD consecutive
 // entries b*nD .. b*nD+nD-1 of the spectrum batch.
-__global__ void __launch_bounds__(1024) k_fast_deriv_r2c(FastArgs a, WinDesc w, FFTPlan<float> plan,
+__global__ void __launch_bounds__(512) k_fast_deriv_r2c(FastArgs a, WinDesc w, FFTPlan<float> plan,
                                                         const cplx<float> *__restrict__ twL,
                                                         const int *__restrict__ slot, int nD, int win) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -913,56 +1036,33 @@ __global__ void __launch_bounds__(1024) k_fast_deriv_r2c(FastArgs a, WinDesc w, 
   __syncthreads();
   float *lines = reinterpret_cast<float *>(bufA);  // real line j: lines[2 * j * ls + col]
   const int side = win ? a.boxReg : a.boxMain;
-  for (int col = threadIdx.x; col < w.cols; col += blockDim.x) {
-    for (int c = 0; c < nC; c++) {
-      const CompF32 &cc = sc[c];
-      if (!in_rows(cc.type)) continue;
-      float dx, dy;
-      win_offsets(w, cc, row, col, dx, dy);
-      const Geo g = geo32(cc, dx, dy);
-      float o[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-      int np;
-      const int ns = sub_count(cc, g);
-      if (ns > 1) {
-        const int br = row - boxes[2 * c + 1], bc = col - boxes[2 * c];
-        if (br >= 0 && br < side && bc >= 0 && bc < side) {
-          const float *t = a.subTab + sub_base(a, b, c, win) + ((long)br * side + bc) * 8 + 1;
+  for (int c = 0; c < nC; c++) {
+    const CompF32 cc = sc[c];
+    if (!in_rows(cc.type)) continue;
+    // the derivative lines this component's parameters feed (-1: none)
+    int sl[7];
+    sl[0] = ss[cc.x0Index];
+    sl[1] = ss[cc.x0Index + 1];
 #pragma unroll
-          for (int q = 0; q < 7; q++) o[q] = t[q];
-        } else {
-          // outside the precomputed box (not reached for radius < 10): direct average
-          const float d = 1.f / ns;
-          float t7[7];
-          for (int t = 0; t < ns * ns; t++) {
-            const Geo gs = geo32(cc, dx - 0.5f + (t / ns + 0.5f) * d, dy - 0.5f + (t % ns + 0.5f) * d);
-            const int n2 = radial_grad32(cc, gs, d * d, t7);
-#pragma unroll
-            for (int q = 0; q < 7; q++)
-              if (q < 2 + n2) o[q] += t7[q];
-          }
-        }
-        np = 5;  // unused slots are zero
-      } else {
-        np = cc.type == F_TILTEDSKY ? plane_grad32(cc, dx, dy, 1.f, o) : radial_grad32(cc, g, 1.f, o);
-      }
-      np = min(np, npar[c]);
-      int s = ss[cc.x0Index];
-      if (s >= 0) lines[2 * s * ls + col] += o[0];
-      s = ss[cc.x0Index + 1];
-      if (s >= 0) lines[2 * s * ls + col] += o[1];
-#pragma unroll
-      for (int q = 0; q < 5; q++) {
-        if (q >= np) break;
-        s = ss[cc.paramOffset + q];
-        if (s >= 0) lines[2 * s * ls + col] += o[2 + q];
-      }
+    for (int q = 0; q < 5; q++) sl[2 + q] = q < npar[c] ? ss[cc.paramOffset + q] : -1;
+    const float *tab = a.subTab + sub_base(a, b, c, win);
+    const int bc0 = boxes[2 * c], br0 = boxes[2 * c + 1];
+    switch (cc.type) {
+      case F_SERSIC: deriv_pixels<F_SERSIC>(cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
+      case F_EXP: deriv_pixels<F_EXP>(cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
+      case F_GRING: deriv_pixels<F_GRING>(cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
+      case F_MOFFAT: deriv_pixels<F_MOFFAT>(cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
+      case F_GAUSS: deriv_pixels<F_GAUSS>(cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
+      case F_TILTEDSKY: deriv_pixels<F_TILTEDSKY>(cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
+      default: break;
     }
   }
   __syncthreads();
   cplx<float> *Z = block_fft(bufA, bufB, plan, nD, ls, 1, -1, false);
   cplx<float> *out = w.spec + (long)b * nD * w.specBatch + (long)row * w.specPitch;
+  const FastDiv byM1(M + 1);
   for (int idx = threadIdx.x; idx < nD * (M + 1); idx += blockDim.x) {
-    const int j = idx / (M + 1), k = idx - j * (M + 1);
+    const int j = byM1.div(idx), k = idx - j * (M + 1);
     out[(long)j * w.specBatch + k] = r2c_post(Z + j * ls, k, M, twL);
   }
 }
@@ -1034,8 +1134,9 @@ __global__ void __launch_bounds__(1024) k_fast_jtwj_rows(FastArgs a, FastGeom g,
   }
   if (a.count && a.countStride) a.count += (a.entry ? a.entry[b] : b) * a.countStride;  // batched bootstrap
   const cplx<float> *src = dspec + (long)b * nD * g.specBatch + (long)row * g.specPitch;
+  const FastDiv byM(M);
   for (int idx = threadIdx.x; idx < nD * M; idx += blockDim.x) {
-    const int j = idx / M, k = idx - j * M;
+    const int j = byM.div(idx), k = idx - j * M;
     bufA[j * ls + k] = c2r_pre(src + (long)j * g.specBatch, k, M, twL);
   }
   __syncthreads();
@@ -1177,7 +1278,7 @@ static FFTPlan<float> plan32(const FFTLen &L, bool half) {
   const FFTTable &t = half ? L.half : L.full;
   p.n = t.n;
   p.npass = t.npass;
-  for (int i = 0; i < kMaxRadixPasses; i++) p.radix[i] = t.radix[i];
+  p.radix = pack_radix(t.radix, t.npass);
   p.tw = reinterpret_cast<const cplx<float> *>(t.tw32);
   return p;
 }
@@ -1402,7 +1503,7 @@ cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool 
     if (los) STAGE("region_los_eval", rs, launch_los_eval(a, rw, nBatch, rks, rs));
     STAGE("region_eval_r2c", rs, launch_eval(a, rw, *p.Rx, nBatch, 1, tu, rs));
     STAGE("region_cols_conv", rs,
-          launch_cols<float>(a.rspec, g.rSpecPitch, g.rSpecBatch, p.Rx->L / 2 + 1, g.rWinRows, g.rSubRows, p.Hr,
+          launch_cols32(a.rspec, g.rSpecPitch, g.rSpecBatch, p.Rx->L / 2 + 1, g.rWinRows, g.rSubRows, p.Hr,
                              p.hrPitch, *p.Ry, rscale, 1, nBatch, rs, tu.colCpb, 0, 1, nullptr, tu.colThreads));
     STAGE("region_down", rs, launch_region_down(p, a, nBatch, rs));
   }
@@ -1410,7 +1511,7 @@ cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool 
   if (los) STAGE("los_eval", st, launch_los_eval(a, mw, nBatch, mks, st));
   STAGE("eval_r2c", st, launch_eval(a, mw, *p.Lx, nBatch, 0, tu, st));
   STAGE("cols_conv", st,
-        launch_cols<float>(a.spec, g.specPitch, g.specBatch, p.Lx->L / 2 + 1, g.winRows, g.nDataRows, p.H, p.hPitch,
+        launch_cols32(a.spec, g.specPitch, g.specBatch, p.Lx->L / 2 + 1, g.winRows, g.nDataRows, p.H, p.hPitch,
                            *p.Ly, scale, 1, nBatch, st, tu.colCpb, p.hBatch, 1, p.hMap, tu.colThreads));
   if (fork) {
     cudaError_t e = cudaEventRecord(p.join0, rs);
@@ -1430,13 +1531,13 @@ cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool 
   if (g.hasRegion) {
     STAGE("region_g_r2c", rs, launch_region_g(p, a, nBatch, rs));
     STAGE("region_cols_adjoint", rs,
-          launch_cols<float>(a.rspec, g.rSpecPitch, g.rSpecBatch, p.Rx->L / 2 + 1, g.rSubRows, g.rWinRows, p.Hr,
+          launch_cols32(a.rspec, g.rSpecPitch, g.rSpecBatch, p.Rx->L / 2 + 1, g.rSubRows, g.rWinRows, p.Hr,
                              p.hrPitch, *p.Ry, rscale, 2, nBatch, rs, tu.colCpb, 0, 1, nullptr, tu.colThreads));
     STAGE("region_grad_rows", rs, launch_grad(a, rw, *p.Rx, nBatch, nMain, 1, tu, rs));
     if (los) STAGE("region_los_grad", rs, launch_los_grad(a, rw, nBatch, nMain + nReg + kLosCtas, rks, rs));
   }
   STAGE("cols_adjoint", st,
-        launch_cols<float>(a.spec, g.specPitch, g.specBatch, p.Lx->L / 2 + 1, g.nDataRows, g.winRows, p.H, p.hPitch,
+        launch_cols32(a.spec, g.specPitch, g.specBatch, p.Lx->L / 2 + 1, g.nDataRows, g.winRows, p.H, p.hPitch,
                            *p.Ly, scale, 2, nBatch, st, tu.colCpb, p.hBatch, 1, p.hMap, tu.colThreads));
   STAGE("grad_rows", st, launch_grad(a, mw, *p.Lx, nBatch, 0, 0, tu, st));
   if (los) STAGE("los_grad", st, launch_los_grad(a, mw, nBatch, nMain + nReg, mks, st));
@@ -1494,7 +1595,7 @@ cudaError_t fast_jtwj(const FastPlan &p, const FastArgs &a, const JtwjArgs &J, i
       const float rscale = 1.f / ((float)p.Rx->L * (float)p.Ry->L);
       STAGE("jtwj_region_deriv_r2c", st, launch_deriv(a, region_win(g, J.drspec), *p.Rx, nBatch, 1, J, st));
       STAGE("jtwj_region_cols", st,
-            launch_cols<float>(J.drspec, g.rSpecPitch, g.rSpecBatch, p.Rx->L / 2 + 1, g.rWinRows, g.rSubRows, p.Hr,
+            launch_cols32(J.drspec, g.rSpecPitch, g.rSpecBatch, p.Rx->L / 2 + 1, g.rWinRows, g.rSubRows, p.Hr,
                                p.hrPitch, *p.Ry, rscale, 1, nB, st, tu.colCpb, 0, 1, nullptr, tu.colThreads));
       const int M = p.Rx->half.n;
       const size_t sm = sizeof(cplx<float>) * 3 * g.rScale * (M + 1);
@@ -1508,7 +1609,7 @@ cudaError_t fast_jtwj(const FastPlan &p, const FastArgs &a, const JtwjArgs &J, i
     const float scale = 1.f / ((float)p.Lx->L * (float)p.Ly->L);
     STAGE("jtwj_deriv_r2c", st, launch_deriv(a, main_win(g, J.dspec), *p.Lx, nBatch, 0, J, st));
     STAGE("jtwj_cols", st,
-          launch_cols<float>(J.dspec, g.specPitch, g.specBatch, p.Lx->L / 2 + 1, g.winRows, g.nDataRows, p.H,
+          launch_cols32(J.dspec, g.specPitch, g.specBatch, p.Lx->L / 2 + 1, g.winRows, g.nDataRows, p.H,
                              p.hPitch, *p.Ly, scale, 1, nB, st, tu.colCpb, p.hBatch, nD, p.hMap, tu.colThreads));
   }
   const int M = p.Lx->half.n;
@@ -1529,6 +1630,7 @@ cudaError_t fast_jtwj(const FastPlan &p, const FastArgs &a, const JtwjArgs &J, i
 }
 
 void fast_prepare_kernels() {
+  cols32_prepare_kernels();
   allow_max_smem((const void *)k_fast_eval_r2c);
   allow_max_smem((const void *)k_fast_grad_rows);
   allow_max_smem((const void *)k_fast_stat_rows<false>);

@@ -34,8 +34,9 @@ __global__ void __launch_bounds__(1024) k_rows_r2c(const T *__restrict__ in, lon
   if (nl <= 0) return;
   in += b * inBatch;
   out += b * outBatch;
+  const FastDiv byM(M), byM1(M + 1);
   for (int idx = threadIdx.x; idx < nl * M; idx += blockDim.x) {
-    const int l = idx / M, k = idx % M;
+    const int l = byM.div(idx), k = idx - l * M;
     const T *src = in + (long)(row0 + l) * inPitch;
     const int c0 = 2 * k, c1 = 2 * k + 1;
     cplx<T> z;
@@ -46,7 +47,7 @@ __global__ void __launch_bounds__(1024) k_rows_r2c(const T *__restrict__ in, lon
   __syncthreads();
   cplx<T> *Z = block_fft(bufA, bufB, plan, nl, ls, 1, -1, false);
   for (int idx = threadIdx.x; idx < nl * (M + 1); idx += blockDim.x) {
-    const int l = idx / (M + 1), k = idx % (M + 1);
+    const int l = byM1.div(idx), k = idx - l * (M + 1);
     out[(long)(row0 + l) * outPitch + k] = r2c_post(Z + l * ls, k, M, twL);
   }
 }
@@ -122,19 +123,20 @@ __global__ void __launch_bounds__(1024) k_rows_c2r(const cplx<T> *__restrict__ i
   if (nl <= 0) return;
   in += blockIdx.y * inBatch;
   out += blockIdx.y * outBatch;
+  const FastDiv byM(M), byM1(M + 1), byOut(outCols);
   for (int idx = threadIdx.x; idx < nl * (M + 1); idx += blockDim.x) {
-    const int l = idx / (M + 1), k = idx % (M + 1);
+    const int l = byM1.div(idx), k = idx - l * (M + 1);
     bufX[l * ls + k] = in[(long)(row0 + l) * inPitch + k];
   }
   __syncthreads();
   for (int idx = threadIdx.x; idx < nl * M; idx += blockDim.x) {
-    const int l = idx / M, k = idx % M;
+    const int l = byM.div(idx), k = idx - l * M;
     bufA[l * ls + k] = c2r_pre(bufX + l * ls, k, M, twL);
   }
   __syncthreads();
   cplx<T> *Z = block_fft(bufA, bufB, plan, nl, ls, 1, +1, false);
   for (int idx = threadIdx.x; idx < nl * outCols; idx += blockDim.x) {
-    const int l = idx / outCols, c = idx % outCols;
+    const int l = byOut.div(idx), c = idx - l * outCols;
     const cplx<T> z = Z[l * ls + (c >> 1)];
     out[(long)(row0 + l) * outPitch + c] = scale * ((c & 1) ? z.y : z.x);
   }
@@ -147,7 +149,7 @@ static FFTPlan<T> plan_of(const FFTLen &L, bool half) {
   const FFTTable &t = half ? L.half : L.full;
   p.n = t.n;
   p.npass = t.npass;
-  for (int i = 0; i < kMaxRadixPasses; i++) p.radix[i] = t.radix[i];
+  p.radix = pack_radix(t.radix, t.npass);
   p.tw = reinterpret_cast<const cplx<T> *>(sizeof(T) == 8 ? (const void *)t.tw64 : (const void *)t.tw32);
   return p;
 }

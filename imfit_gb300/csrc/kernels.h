@@ -53,6 +53,18 @@ cudaError_t launch_cols(void *spec, long pitch, long batch, int nColsC, int nRow
                         const void *H, long hPitch, const FFTLen &Ly, T scale, int mode, int nBatch,
                         cudaStream_t st, int cpbOverride = 0, long hBatch = 0, int hDiv = 1,
                         const int *hMap = nullptr, int threadsOverride = 0);
+// Column pass of the FP32 convolution (k_cols32.cu): mode 1 multiplies by H,
+// mode 2 by conj(H); pitch and hPitch even (16-byte rows pieces); cpb
+// columns per CTA in {1, 2, 4, 8} (0: automatic), threads 0: automatic.
+cudaError_t launch_cols32(void *spec, long pitch, long batch, int nColsC, int nRowsIn, int nRowsOut, const void *H,
+                          long hPitch, const FFTLen &Ly, float scale, int mode, int nBatch, cudaStream_t st,
+                          int cpb = 0, long hBatch = 0, int hDiv = 1, const int *hMap = nullptr, int threads = 0);
+size_t cols32_smem(int Ly, int cpb);
+void cols32_prepare_kernels();
+// complex pitch of a half spectrum of real length L: L/2 + 1 rounded up to
+// even, so every row starts on a 16-byte boundary
+inline int even_pitch(int L) { return ((L / 2 + 1) + 1) & ~1; }
+
 template <typename T>
 cudaError_t launch_rows_c2r(const void *in, long inPitch, long inBatch, int nRows, T *out, long outPitch,
                             long outBatch, int outCols, T scale, const FFTLen &Lx, int nBatch,

@@ -1080,12 +1080,12 @@ struct imfit_model_s {
     if (fftlen_create(Fx, smooth_size(g.winCols, true)) || fftlen_create(Fy, smooth_size(g.winRows, true)))
       return fail(IMFIT_E_CUDA, "FFT tables");
     if (Fx.L / 2 > 4096 || Fy.L > 4096) return fail(IMFIT_E_UNSUPPORTED, "image too large for the fast path");
-    g.specPitch = Fx.L / 2 + 1;
+    g.specPitch = even_pitch(Fx.L);
     g.specBatch = (long)Fy.L * g.specPitch;
     // PSF placed so that circular output (r,c) is the data pixel (r,c)
     int st = 0;
     if (stack.n) {
-      const size_t hb = 2 * (size_t)Fy.L * (Fx.L / 2 + 1);
+      const size_t hb = 2 * (size_t)Fy.L * even_pitch(Fx.L);
       cudaError_t e0 = dH32.reserve(hb * stack.n);
       if (e0) return cuda_fail(e0, "stack PSF spectra");
       for (int i = 0; i < stack.n && !st; i++)
@@ -1126,7 +1126,7 @@ struct imfit_model_s {
       if (fftlen_create(FRx, smooth_size(g.rWinCols, true)) || fftlen_create(FRy, smooth_size(g.rWinRows, true)))
         return fail(IMFIT_E_CUDA, "FFT tables");
       if (FRx.L / 2 > 4096 || FRy.L > 4096) return fail(IMFIT_E_UNSUPPORTED, "region too large for the fast path");
-      g.rSpecPitch = FRx.L / 2 + 1;
+      g.rSpecPitch = even_pitch(FRx.L);
       g.rSpecBatch = (long)FRy.L * g.rSpecPitch;
       st = shiftedSpectrum32(r->psf, r->nPsfCols, r->nPsfRows, FRx, FRy, dHr32);
       if (st) return st;
@@ -1217,12 +1217,13 @@ struct imfit_model_s {
 
   int shiftedSpectrum32(const std::vector<double> &p, int pc, int pr, const FFTLen &fx, const FFTLen &fy,
                         DevBuf<float> &H32) {
-    cudaError_t e = H32.reserve(2 * (size_t)fy.L * (fx.L / 2 + 1));
+    cudaError_t e = H32.reserve(2 * (size_t)fy.L * even_pitch(fx.L));
     if (e) return cuda_fail(e, "FP32 PSF spectrum");
     return shiftedSpectrum32To(p.data(), pc, pr, fx, fy, H32.p);
   }
 
-  // FP32 spectrum of one PSF (centre wrapped to (0,0)) written to dst
+  // FP32 spectrum of one PSF (centre wrapped to (0,0)) written to dst, rows
+  // at the even pitch even_pitch(fx.L) (the padding column zero)
   int shiftedSpectrum32To(const double *p, int pc, int pr, const FFTLen &fx, const FFTLen &fy, float *dst) {
     std::vector<double> pad((size_t)fx.L * fy.L, 0.0);
     for (int k = 0; k < pr; k++)
@@ -1234,8 +1235,15 @@ struct imfit_model_s {
     DevBuf<double> H64;
     int st = spectrum64(pad, fx, fy, H64);
     if (st) return st;
-    const size_t nc = 2 * (size_t)fy.L * (fx.L / 2 + 1);
-    cudaError_t e = launch_f64_to_f32(H64.p, dst, (long)nc, stream);
+    const size_t w = fx.L / 2 + 1, pitch = even_pitch(fx.L);
+    const size_t nc = 2 * (size_t)fy.L * w;
+    DevBuf<float> tmp;
+    cudaError_t e = tmp.reserve(nc);
+    if (!e) e = launch_f64_to_f32(H64.p, tmp.p, (long)nc, stream);
+    if (!e) e = cudaMemsetAsync(dst, 0, sizeof(float) * 2 * pitch * fy.L, stream);
+    if (!e)
+      e = cudaMemcpy2DAsync(dst, sizeof(float) * 2 * pitch, tmp.p, sizeof(float) * 2 * w, sizeof(float) * 2 * w,
+                            fy.L, cudaMemcpyDeviceToDevice, stream);
     if (!e) e = cudaStreamSynchronize(stream);
     if (e) return cuda_fail(e, "FP32 PSF spectrum");
     return 0;
@@ -1393,9 +1401,9 @@ struct imfit_model_s {
     p.Ry = &FRy;
     p.H = dH32.p;
     p.Hr = dHr32.p;
-    p.hPitch = Fx.L / 2 + 1;
-    p.hrPitch = FRx.L / 2 + 1;
-    p.hBatch = stack.n ? (long)Fy.L * (Fx.L / 2 + 1) : 0;
+    p.hPitch = even_pitch(Fx.L);
+    p.hrPitch = FRx.L ? even_pitch(FRx.L) : 0;
+    p.hBatch = stack.n ? (long)Fy.L * even_pitch(Fx.L) : 0;
     p.hMap = stack.n ? curEntry : nullptr;
     return p;
   }
@@ -1466,7 +1474,7 @@ struct imfit_model_s {
       if (ms < bestMs) { bestMs = ms; bestT = t; }
     }
     for (int cpb : {1, 2, 4, 8}) {
-      for (int nt : {0, 256, 512}) {
+      for (int nt : {0, 128, 256, 512}) {
         if (e) break;
         FastTune t = bestT;
         t.colCpb = cpb;

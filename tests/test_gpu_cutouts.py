@@ -106,9 +106,15 @@ def test_batched_lm_matches_single_lm(gpu, oracle_mod):
         if any(pegged):
             # a degenerate fit (here the disk shrinking onto the bulge until its
             # ellipticity reaches a limit) ends in a corner that the trajectory
-            # picks; the FP32 rounding of the two evaluators differs, so the
-            # two drivers may pick different corners -- both must end at one
-            assert all(pegged) and rb["status"][i] > 0 and r1["status"] > 0, (i, rb["params"][i], r1["params"])
+            # picks; the FP32 rounding of the batched and the single evaluation
+            # differs, so the two drivers may stop in different corners, or one
+            # of them in a corner and the other inside: both must have stopped
+            # by a convergence test, and a fit that ended inside the limits must
+            # be at least as good as one held in a corner
+            assert rb["status"][i] > 0 and r1["status"] > 0, (i, rb["status"][i], r1["status"])
+            if not all(pegged):
+                inner, corner = (c_single, c_batch) if pegged[0] else (c_batch, c_single)
+                assert inner <= corner * (1 + 1e-6), (i, c_batch, c_single, pegged)
             continue
         # converged interior fits of the same data agree to the statistic's
         # FP32 noise; a fit that stalled in a flat valley may stop elsewhere
