@@ -88,6 +88,7 @@ __global__ void __launch_bounds__(1024) k_cols32(cplx<float> *__restrict__ spec,
                                                 const cplx<float> *__restrict__ H, long hPitch, FFTPlan<float> plan,
                                                 float scale, long hBatch, int hDiv, const int *__restrict__ hMap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  pdl_wait();
   const int Ly = plan.n;
   cplx<float> *tw = reinterpret_cast<cplx<float> *>(smem_raw);
   cplx<float> *bufA = tw + Ly;
@@ -124,6 +125,7 @@ __global__ void __launch_bounds__(1024) k_cols32(cplx<float> *__restrict__ spec,
   __syncthreads();
   cplx<float> *other = (X == bufA) ? bufB : bufA;
   cplx<float> *Y = block_fft(X, other, plan, CPB, 1, CPB, +1, true, tw);
+  pdl_trigger();
   for (int t = threadIdx.x; t < nRowsOut; t += blockDim.x)
     store_row<CPB>(spec + (long)t * pitch, Y + (long)t * CPB, pairs);
 }
@@ -136,9 +138,8 @@ cudaError_t launch_one(cplx<float> *s, long pitch, long batch, int nColsC, int n
   allow_max_smem((const void *)kern);
   const size_t sm = sizeof(cplx<float>) * (size_t)p.n * (1 + 3 * CPB);
   dim3 grid((nColsC + CPB - 1) / CPB, nBatch);
-  kern<<<grid, threads, sm, st>>>(s, pitch, batch, nColsC, nRowsIn, nRowsOut, h, hPitch, p, scale, hBatch, hDiv,
-                                  hMap);
-  return cudaGetLastError();
+  return launch_pdl(kern, grid, dim3(threads), sm, st, s, pitch, batch, nColsC, nRowsIn, nRowsOut, h, hPitch, p,
+                    scale, hBatch, hDiv, hMap);
 }
 
 template <int MODE>

@@ -26,6 +26,7 @@
 
 #include "kernels.h"
 #include "fft.cuh"
+#include "ffsum.cuh"
 #include "los_fast.cuh"
 
 namespace imfit {
@@ -86,12 +87,14 @@ __device__ __forceinline__ int sub_count(const CompF32 &c, const Geo &g) {
 }
 
 // --------------------------------------------------------------- setup
-// One CTA per (component, parameter vector); warp w computes the w-th group
-// of FP64 transcendentals, thread 0 assembles the FP32 component record.
-__global__ void __launch_bounds__(128) k_fast_setup(FastArgs a) {
-  const int c = blockIdx.x, b = blockIdx.y;
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+// FP64 Setup of component c of parameter vector b into rec (FunctionObject::
+// Setup, core/model_object.cpp:1126-1135).  Warp w computes the w-th group of
+// FP64 transcendentals, thread 0 assembles the FP32 record; all threads of
+// the CTA (at least 128) call it.  With bg, also the constant background
+// levels of vector b (FlatSky sum x sum of the PSF, main and region).
+__device__ void setup_component(const FastArgs &a, int c, int b, CompF32 &rec, bool bg) {
   __shared__ SetupFP64 q;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const CompDesc d = a.desc[c];
   const double *P = a.params + (long)b * a.nParams;
   const double *p = P + d.paramOffset;
@@ -108,21 +111,17 @@ __global__ void __launch_bounds__(128) k_fast_setup(FastArgs a) {
       if (d.type == F_MOFFAT) q.t = exp2(1.0 / p[4]);
     } else if (w == 2) {
       if (d.type == F_SERSIC) q.log2re = log2(p[4]);
-    } else if (w == 3 && c == 0) {
-      double bg = 0.0;
+    } else if (w == 3 && bg) {
+      double s = 0.0;
       for (int k = 0; k < a.nComp; k++)
-        if (a.desc[k].background) bg += P[a.desc[k].paramOffset];
-      a.bgLevel[2 * b] = (float)(bg * a.psfSum);
-      a.bgLevel[2 * b + 1] = (float)(bg * a.psfSumOs);
+        if (a.desc[k].background) s += P[a.desc[k].paramOffset];
+      a.bgLevel[2 * b] = (float)(s * a.psfSum);
+      a.bgLevel[2 * b + 1] = (float)(s * a.psfSumOs);
     }
   }
   __syncthreads();
-  if (threadIdx.x == 0) comp_setup32(a.comps[b * a.nComp + c], d, P, q);
-}
-
-cudaError_t fast_setup(const FastArgs &a, int nBatch, cudaStream_t st) {
-  k_fast_setup<<<dim3(a.nComp, nBatch), 128, 0, st>>>(a);
-  return cudaGetLastError();
+  if (threadIdx.x == 0) comp_setup32(rec, d, P, q);
+  __syncthreads();
 }
 
 // ------------------------------------------- subsampled pixels (precomputed)
@@ -175,47 +174,66 @@ __device__ __forceinline__ void subsample_sum(const CompF32 &cc, int ns, float x
   }
 }
 
-// One warp per box pixel: the average over the pixel's ns x ns subsamples of
-// the profile and of its 7 derivatives (X0, Y0, then the function parameters).
-__global__ void __launch_bounds__(256) k_fast_subsample(FastArgs a, WinDesc w, int win) {
+// First kernel of an evaluation.  CTA (x, c, b) sets up component c of
+// parameter vector b in FP64 (the CTA with x = 0 publishes the record, and for
+// c = 0 the background levels and a zeroed completion counter for the final
+// reduction), then precomputes the subsampled pixels of component c: one warp
+// per box pixel (grid-stride), the average over the pixel's ns x ns
+// subsamples of the profile and of its 7 derivatives (X0, Y0, then the
+// function parameters).  CTAs [0, nMainCtas) cover the main window's box, the
+// rest the oversampled region's.
+__global__ void __launch_bounds__(256) k_fast_subsample(FastArgs a, WinDesc mw, WinDesc rw, int nMainCtas) {
+  pdl_wait();
   const int b = blockIdx.z, c = blockIdx.y;
-  const CompF32 cc = a.comps[b * a.nComp + c];
+  if (blockIdx.x != 0 && !(a.desc[c].subsample && subsampling_type(a.desc[c].type))) return;
+  __shared__ CompF32 rec;
+  setup_component(a, c, b, rec, blockIdx.x == 0 && c == 0);
+  const CompF32 cc = rec;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    a.comps[b * a.nComp + c] = cc;
+    if (c == 0 && a.done) a.done[b] = 0u;
+  }
   if (!cc.subsample || !subsampling_type(cc.type)) return;
+  const int win = (int)blockIdx.x >= nMainCtas ? 1 : 0;
+  const WinDesc &w = win ? rw : mw;
+  const int cta = win ? (int)blockIdx.x - nMainCtas : (int)blockIdx.x;
+  const int nCtas = win ? (int)gridDim.x - nMainCtas : nMainCtas;
   const int side = win ? a.boxReg : a.boxMain;
   int col0, row0;
   box_origin(w, cc, side, col0, row0);
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+  if (cta == 0 && threadIdx.x == 0) {
     int *o = a.subBox + (((long)b * a.nComp + c) * 2 + win) * 2;
     o[0] = col0;
     o[1] = row0;
   }
-  const int lane = threadIdx.x & 31;
-  const int p = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (p >= side * side) return;
-  const int pr = FastDiv(side).div(p);
-  const int row = row0 + pr, col = col0 + (p - pr * side);
-  if (row < 0 || row >= w.rows || col < 0 || col >= w.cols) return;
-  float dx, dy;
-  win_offsets(w, cc, row, col, dx, dy);
-  const Geo g = geo32(cc, dx, dy);
-  const int ns = sub_count(cc, g);
-  if (ns <= 1) return;
-  const float d = 1.f / ns;
-  const float xs = dx - 0.5f + 0.5f * d, ys = dy - 0.5f + 0.5f * d;
-  float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-  switch (cc.type) {
-    case F_SERSIC: subsample_sum<F_SERSIC>(cc, ns, xs, ys, d, lane, acc); break;
-    case F_EXP: subsample_sum<F_EXP>(cc, ns, xs, ys, d, lane, acc); break;
-    case F_MOFFAT: subsample_sum<F_MOFFAT>(cc, ns, xs, ys, d, lane, acc); break;
-    default: subsample_sum<F_GAUSS>(cc, ns, xs, ys, d, lane, acc); break;
-  }
+  const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const FastDiv bySide(side);
+  for (int p = cta * nw + (threadIdx.x >> 5); p < side * side; p += nCtas * nw) {
+    const int pr = bySide.div(p);
+    const int row = row0 + pr, col = col0 + (p - pr * side);
+    if (row < 0 || row >= w.rows || col < 0 || col >= w.cols) continue;
+    float dx, dy;
+    win_offsets(w, cc, row, col, dx, dy);
+    const Geo g = geo32(cc, dx, dy);
+    const int ns = sub_count(cc, g);
+    if (ns <= 1) continue;
+    const float d = 1.f / ns;
+    const float xs = dx - 0.5f + 0.5f * d, ys = dy - 0.5f + 0.5f * d;
+    float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    switch (cc.type) {
+      case F_SERSIC: subsample_sum<F_SERSIC>(cc, ns, xs, ys, d, lane, acc); break;
+      case F_EXP: subsample_sum<F_EXP>(cc, ns, xs, ys, d, lane, acc); break;
+      case F_MOFFAT: subsample_sum<F_MOFFAT>(cc, ns, xs, ys, d, lane, acc); break;
+      default: subsample_sum<F_GAUSS>(cc, ns, xs, ys, d, lane, acc); break;
+    }
 #pragma unroll
-  for (int q = 0; q < 8; q++) acc[q] = warp_sum(acc[q]);
-  if (lane == 0) {
-    float *dst = a.subTab + sub_base(a, b, c, win) + (long)p * 8;
-    const float dd = d * d;
+    for (int q = 0; q < 8; q++) acc[q] = warp_sum(acc[q]);
+    if (lane == 0) {
+      float *dst = a.subTab + sub_base(a, b, c, win) + (long)p * 8;
+      const float dd = d * d;
 #pragma unroll
-    for (int q = 0; q < 8; q++) dst[q] = acc[q] * dd;
+      for (int q = 0; q < 8; q++) dst[q] = acc[q] * dd;
+    }
   }
 }
 
@@ -270,6 +288,7 @@ __device__ __forceinline__ void eval_pixels(const CompF32 cc, const WinDesc &w, 
 
 __global__ void __launch_bounds__(1024) k_fast_eval_r2c(FastArgs a, WinDesc w, FFTPlan<float> plan,
                                                        const cplx<float> *__restrict__ twL, int rpb, int win) {
+  pdl_wait();
   extern __shared__ __align__(16) unsigned char smem[];
   const int b = blockIdx.y;
   const int M = plan.n, ls = M + 1;
@@ -320,6 +339,7 @@ __global__ void __launch_bounds__(1024) k_fast_eval_r2c(FastArgs a, WinDesc w, F
   }
   __syncthreads();
   cplx<float> *Z = block_fft(bufA, bufB, plan, nl, ls, 1, -1, false);
+  pdl_trigger();
   cplx<float> *out = w.spec + (long)b * w.specBatch;
   for (int idx = threadIdx.x; idx < nl * (M + 1); idx += blockDim.x) {
     const int l = byM1.div(idx), k = idx - l * (M + 1);
@@ -426,6 +446,7 @@ template <bool PS>
 __global__ void __launch_bounds__(1024) k_fast_region_down(FastArgs a, FastGeom g, const cplx<float> *__restrict__ rspec,
                                                           FFTPlan<float> plan, const cplx<float> *__restrict__ twL,
                                                           float *__restrict__ out, int addBackground) {
+  pdl_wait();
   extern __shared__ __align__(16) unsigned char smem[];
   const int b = blockIdx.y, s = blockIdx.x;  // replaced data row within the region
   const int k = g.rScale;
@@ -459,6 +480,81 @@ __global__ void __launch_bounds__(1024) k_fast_region_down(FastArgs a, FastGeom 
     if constexpr (PS)
       if (addBackground) acc += ps_region(a, k, b, g.ry0 + s, g.rx0 + t, 0.f, nullptr);
     out[((long)b * g.rRows + s) * g.rCols + t] = acc * inv + bg;
+  }
+}
+
+// ------------------------------------------------------------- reduce
+// Double-float sums of the per-CTA partials of parameter vector b in a fixed
+// order (deterministic), one warp per output quantity: the statistic, the
+// background term and, with nGradBlocks > 0, every gradient entry.  Run by
+// the last CTA of the evaluation's final pass (finish_cta), whose partials
+// are then all written.
+// Double-float sum of p[lane], p[lane + 32], ... below n: four independent
+// loads in flight per lane, four partial sums combined in a fixed order.
+__device__ __forceinline__ ffloat lane_sum(const float2 *p, int n, int lane) {
+  ffloat t0 = {0.f, 0.f}, t1 = t0, t2 = t0, t3 = t0;
+  int i = lane;
+  for (; i + 96 < n; i += 128) {
+    const float2 v0 = __ldcg(p + i), v1 = __ldcg(p + i + 32), v2 = __ldcg(p + i + 64), v3 = __ldcg(p + i + 96);
+    t0 = ff_add(t0, ff_load(v0));
+    t1 = ff_add(t1, ff_load(v1));
+    t2 = ff_add(t2, ff_load(v2));
+    t3 = ff_add(t3, ff_load(v3));
+  }
+  for (; i < n; i += 32) t0 = ff_add(t0, ff_load(__ldcg(p + i)));
+  return ff_add(ff_add(t0, t1), ff_add(t2, t3));
+}
+
+__device__ void reduce_entry(const FastArgs &a, int b, int nGradBlocks) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int nq = 2 + (nGradBlocks > 0 ? a.nParams : 0);
+  for (int j = wid; j < nq; j += nw) {
+    ffloat t;
+    if (j < 2) {
+      t = lane_sum(a.statPart + ((long)b * 2 + j) * a.partStride, a.nStatBlocks, lane);
+    } else {
+      t = lane_sum(a.gradPart + ((long)b * a.nParams + (j - 2)) * a.partStride, nGradBlocks, lane);
+      // point sources: partials of the statistic CTAs for the parameters they touch
+      for (int ps = 0; ps < a.nPs; ps++) {
+        const CompDesc &d = a.desc[a.psComp[ps]];
+        const bool rot = d.type == F_POINTSOURCEROT;
+        const int map[4] = {d.x0Index, d.x0Index + 1, d.paramOffset + (rot ? 1 : 0), rot ? d.paramOffset : -1};
+        for (int q = 0; q < 4; q++) {
+          if (map[q] != j - 2) continue;
+          t = ff_add(t, lane_sum(a.psPart + ((long)b * 4 * a.nPs + 4 * ps + q) * a.partStride, a.nStatBlocks, lane));
+        }
+      }
+    }
+    t = ff_warp_sum(t);
+    if (lane != 0) continue;
+    const double v = ff_value(t);
+    if (j == 0) {
+      a.stat[b] = v;
+    } else if (j == 1) {
+      if (nGradBlocks > 0)
+        for (int c = 0; c < a.nComp; c++)
+          if (a.desc[c].background) a.grad[(long)b * a.nParams + a.desc[c].paramOffset] = v;
+    } else {
+      bool bgParam = false;
+      for (int c = 0; c < a.nComp; c++)
+        if (a.desc[c].background && a.desc[c].paramOffset == j - 2) bgParam = true;
+      if (!bgParam) a.grad[(long)b * a.nParams + (j - 2)] = v;
+    }
+  }
+}
+
+// Called by every thread of a CTA after its partials are written: the CTA
+// that completes the evaluation's `total` CTAs for vector b performs the final
+// reduction (threadfence-reduction pattern: no CTA waits for another).
+__device__ __forceinline__ void finish_cta(const FastArgs &a, int b, int total, int nGradBlocks) {
+  __shared__ int last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = (atomicAdd(a.done + b, 1u) == (unsigned)total - 1u);
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    reduce_entry(a, b, nGradBlocks);
   }
 }
 
@@ -515,14 +611,16 @@ __device__ __forceinline__ void stat_term(const FastArgs &a, long z, float m, fl
 
 template <bool PS>
 __global__ void __launch_bounds__(1024) k_fast_stat_rows(FastArgs a, FastGeom g, FFTPlan<float> plan,
-                                                        const cplx<float> *__restrict__ twL, int rpb, int wantGrad) {
+                                                        const cplx<float> *__restrict__ twL, int rpb, int wantGrad,
+                                                        int doneTotal) {
+  pdl_wait();
   extern __shared__ __align__(16) unsigned char smem[];
   const int b = blockIdx.y;
   const int M = plan.n, ls = M + 1;
   cplx<float> *bufX = reinterpret_cast<cplx<float> *>(smem);
   cplx<float> *bufA = bufX + rpb * ls;
   cplx<float> *bufB = bufA + rpb * ls;
-  __shared__ float red[2][32];
+  __shared__ ffloat red[2][32];
   __shared__ float psAcc[4 * kMaxPsFast];
   if constexpr (PS)
     for (int i = threadIdx.x; i < 4 * a.nPs; i += blockDim.x) psAcc[i] = 0.f;
@@ -605,39 +703,43 @@ __global__ void __launch_bounds__(1024) k_fast_stat_rows(FastArgs a, FastGeom g,
       }
     }
   }
-  // CTA partial sums of (S, SG): FP32 tree over this CTA's pixels
+  pdl_trigger();
+  // CTA partial sums of (S, SG): FP32 over the thread's pixels and the warp,
+  // double-float across warps
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   S = warp_sum(S);
   SG = warp_sum(SG);
   if (lane == 0) {
-    red[0][wid] = S;
-    red[1][wid] = SG;
+    red[0][wid] = ff_make(S);
+    red[1][wid] = ff_make(SG);
   }
   __syncthreads();
   if (wid == 0) {
     const int nw = blockDim.x >> 5;
-    float v0 = lane < nw ? red[0][lane] : 0.f;
-    float v1 = lane < nw ? red[1][lane] : 0.f;
-    v0 = warp_sum(v0);
-    v1 = warp_sum(v1);
+    ffloat v0 = lane < nw ? red[0][lane] : ffloat{0.f, 0.f};
+    ffloat v1 = lane < nw ? red[1][lane] : ffloat{0.f, 0.f};
+    v0 = ff_warp_sum(v0);
+    v1 = ff_warp_sum(v1);
     if (lane == 0) {
-      float *p = a.statPart + (long)b * 2 * a.partStride + blockIdx.x;
-      p[0] = v0;
-      p[a.partStride] = v1;
+      float2 *p = a.statPart + (long)b * 2 * a.partStride + blockIdx.x;
+      p[0] = ff_store(v0);
+      p[a.partStride] = ff_store(v1);
     }
   }
   if constexpr (PS) {
     if (wantGrad) {
       __syncthreads();
       for (int i = threadIdx.x; i < 4 * a.nPs; i += blockDim.x)
-        a.psPart[((long)b * 4 * a.nPs + i) * a.partStride + blockIdx.x] = psAcc[i];
+        a.psPart[((long)b * 4 * a.nPs + i) * a.partStride + blockIdx.x] = make_float2(psAcc[i], 0.f);
     }
   }
+  if (doneTotal > 0) finish_cta(a, b, doneTotal, 0);
 }
 
 // --------------------------- region adjoint seed: g/k^2 on subpixels, r2c
 __global__ void __launch_bounds__(1024) k_fast_region_g_r2c(FastArgs a, FastGeom g, cplx<float> *__restrict__ rspec,
                                                            FFTPlan<float> plan, const cplx<float> *__restrict__ twL) {
+  pdl_wait();
   extern __shared__ __align__(16) unsigned char smem[];
   const int b = blockIdx.y, u = blockIdx.x;  // subpixel row
   const int M = plan.n, ls = M + 1;
@@ -710,17 +812,19 @@ __device__ __forceinline__ void grad_pixels(const CompF32 cc, const WinDesc &w, 
 
 __global__ void __launch_bounds__(1024) k_fast_grad_rows(FastArgs a, WinDesc w, FFTPlan<float> plan,
                                                         const cplx<float> *__restrict__ twL, int rpb,
-                                                        float *__restrict__ gradPart, int blockBase, int win) {
+                                                        float2 *__restrict__ gradPart, int blockBase, int win,
+                                                        int doneTotal) {
+  pdl_wait();
   extern __shared__ __align__(16) unsigned char smem[];
   const int b = blockIdx.y;
   const int M = plan.n, ls = M + 1;
   CompF32 *sc = reinterpret_cast<CompF32 *>(smem);
   int *boxes = reinterpret_cast<int *>(sc + kMaxComponents);
-  float *gsm = reinterpret_cast<float *>(boxes + 2 * kMaxComponents);
+  ffloat *gsm = reinterpret_cast<ffloat *>(boxes + 2 * kMaxComponents);
   cplx<float> *bufX = reinterpret_cast<cplx<float> *>(gsm + kMaxParams);
   cplx<float> *bufA = bufX + rpb * ls;
   cplx<float> *bufB = bufA + rpb * ls;
-  __shared__ float red[32][8];
+  __shared__ ffloat red[32][7];
   const int nC = a.nComp, nP = a.nParams;
   for (int i = threadIdx.x; i < nC; i += blockDim.x) {
     sc[i] = a.comps[b * nC + i];
@@ -728,7 +832,7 @@ __global__ void __launch_bounds__(1024) k_fast_grad_rows(FastArgs a, WinDesc w, 
     boxes[2 * i] = o[0];
     boxes[2 * i + 1] = o[1];
   }
-  for (int i = threadIdx.x; i < nP; i += blockDim.x) gsm[i] = 0.f;
+  for (int i = threadIdx.x; i < nP; i += blockDim.x) gsm[i] = ffloat{0.f, 0.f};
   const int row0 = blockIdx.x * rpb;
   const int nl = min(rpb, w.rows - row0);
   const cplx<float> *spec = w.spec + (long)b * w.specBatch;
@@ -771,29 +875,30 @@ __global__ void __launch_bounds__(1024) k_fast_grad_rows(FastArgs a, WinDesc w, 
           break;
         default: break;
       }
-      // block reduction of acc[0..6]
+      // CTA reduction of acc[0..6]: FP32 over the warp, double-float across warps
 #pragma unroll
       for (int q = 0; q < 7; q++) acc[q] = warp_sum(acc[q]);
       if (lane == 0) {
 #pragma unroll
-        for (int q = 0; q < 7; q++) red[wid][q] = acc[q];
+        for (int q = 0; q < 7; q++) red[wid][q] = ff_make(acc[q]);
       }
       __syncthreads();
       if (threadIdx.x < 7) {
-        float t = 0.f;
-        for (int i = 0; i < nw; i++) t += red[i][threadIdx.x];
+        ffloat t = {0.f, 0.f};
+        for (int i = 0; i < nw; i++) t = ff_add(t, red[i][threadIdx.x]);
         const int q = threadIdx.x;
         const int npf = a.desc[c].nParams;
-        if (q == 0) gsm[cc.x0Index] += t;
-        else if (q == 1) gsm[cc.x0Index + 1] += t;
-        else if (q - 2 < npf) gsm[cc.paramOffset + q - 2] += t;
+        const int slot = q == 0 ? cc.x0Index : q == 1 ? cc.x0Index + 1 : (q - 2 < npf ? cc.paramOffset + q - 2 : -1);
+        if (slot >= 0) gsm[slot] = ff_add(gsm[slot], t);
       }
       __syncthreads();
     }
   }
   __syncthreads();
-  float *out = gradPart + (long)b * nP * a.partStride + blockBase + blockIdx.x;
-  for (int i = threadIdx.x; i < nP; i += blockDim.x) out[(long)i * a.partStride] = gsm[i];
+  pdl_trigger();
+  float2 *out = gradPart + (long)b * nP * a.partStride + blockBase + blockIdx.x;
+  for (int i = threadIdx.x; i < nP; i += blockDim.x) out[(long)i * a.partStride] = ff_store(gsm[i]);
+  if (doneTotal > 0) finish_cta(a, b, doneTotal, doneTotal);
 }
 
 // ------------------------------------------------- 3-D line-of-sight terms
@@ -826,6 +931,7 @@ __device__ __forceinline__ int los_index(const CompF32 *sc, int c) {
 // sight integrals, written to w.losVal (added to the model row by eval_r2c);
 // with a store, each partition is kept for the gradient pass.
 __global__ void __launch_bounds__(256) k_fast_los_eval(FastArgs a, WinDesc w, LosStore ks) {
+  pdl_wait();
   __shared__ CompF32 sc[kMaxComponents];
   const int b = blockIdx.y;
   const int nC = a.nComp;
@@ -860,8 +966,9 @@ __global__ void __launch_bounds__(256) k_fast_los_eval(FastArgs a, WinDesc w, Lo
 // every 3-D component, per-warp rows in shared memory (no atomics), then one
 // FP32 partial per parameter for this CTA.
 // four CTAs per SM (64 registers): the measured optimum for the gradient pass
-__global__ void __launch_bounds__(256, 4) k_fast_los_grad(FastArgs a, WinDesc w, float *__restrict__ gradPart,
-                                                      int blockBase, LosStore ks) {
+__global__ void __launch_bounds__(256, 4) k_fast_los_grad(FastArgs a, WinDesc w, float2 *__restrict__ gradPart,
+                                                      int blockBase, LosStore ks, int doneTotal) {
+  pdl_wait();
   __shared__ CompF32 sc[kMaxComponents];
   __shared__ float red[8][kMaxParams];
   const int b = blockIdx.y;
@@ -901,10 +1008,11 @@ __global__ void __launch_bounds__(256, 4) k_fast_los_grad(FastArgs a, WinDesc w,
   __syncthreads();
   const int nw = blockDim.x >> 5;
   for (int j = threadIdx.x; j < nP; j += blockDim.x) {
-    float t = 0.f;
-    for (int i = 0; i < nw; i++) t += red[i][j];
-    gradPart[((long)b * nP + j) * a.partStride + blockBase + blockIdx.x] = t;
+    ffloat t = {0.f, 0.f};
+    for (int i = 0; i < nw; i++) t = ff_add(t, red[i][j]);
+    gradPart[((long)b * nP + j) * a.partStride + blockBase + blockIdx.x] = ff_store(t);
   }
+  if (doneTotal > 0) finish_cta(a, b, doneTotal, doneTotal);
 }
 
 // ------------------------------------------------------------- reduce
@@ -922,43 +1030,6 @@ __device__ __forceinline__ double block_sum_d(double v) {
     v = warp_sum_d(v);
   }
   return v;
-}
-
-__global__ void __launch_bounds__(256) k_fast_reduce(FastArgs a, int nGradBlocks) {
-  const int j = blockIdx.x, b = blockIdx.y;
-  double t = 0.0;
-  if (j < 2) {
-    const float *p = a.statPart + ((long)b * 2 + j) * a.partStride;
-    for (int i = threadIdx.x; i < a.nStatBlocks; i += blockDim.x) t += (double)p[i];
-  } else {
-    const float *p = a.gradPart + ((long)b * a.nParams + (j - 2)) * a.partStride;
-    for (int i = threadIdx.x; i < nGradBlocks; i += blockDim.x) t += (double)p[i];
-    // point sources: partials of the statistic CTAs for the parameters they touch
-    for (int ps = 0; ps < a.nPs; ps++) {
-      const CompDesc &d = a.desc[a.psComp[ps]];
-      const bool rot = d.type == F_POINTSOURCEROT;
-      const int map[4] = {d.x0Index, d.x0Index + 1, d.paramOffset + (rot ? 1 : 0), rot ? d.paramOffset : -1};
-      for (int q = 0; q < 4; q++) {
-        if (map[q] != j - 2) continue;
-        const float *pp = a.psPart + ((long)b * 4 * a.nPs + 4 * ps + q) * a.partStride;
-        for (int i = threadIdx.x; i < a.nStatBlocks; i += blockDim.x) t += (double)pp[i];
-      }
-    }
-  }
-  t = block_sum_d(t);
-  if (threadIdx.x != 0) return;
-  if (j == 0) {
-    a.stat[b] = t;
-  } else if (j == 1) {
-    if (nGradBlocks > 0)
-      for (int c = 0; c < a.nComp; c++)
-        if (a.desc[c].background) a.grad[(long)b * a.nParams + a.desc[c].paramOffset] = t;
-  } else {
-    bool bgParam = false;
-    for (int c = 0; c < a.nComp; c++)
-      if (a.desc[c].background && a.desc[c].paramOffset == j - 2) bgParam = true;
-    if (!bgParam) a.grad[(long)b * a.nParams + (j - 2)] = t;
-  }
 }
 
 // ------------------------------------ forward-mode derivative images (JtWJ)
@@ -1334,11 +1405,18 @@ static void ensure_smem(K kern, size_t bytes) {
   allow_max_smem((const void *)kern);
 }
 
-static cudaError_t launch_subsample(const FastArgs &a, const WinDesc &w, int win, int nBatch, cudaStream_t st) {
-  const int side = win ? a.boxReg : a.boxMain;
-  dim3 grid((side * side + 7) / 8, a.nComp, nBatch);
-  k_fast_subsample<<<grid, 256, 0, st>>>(a, w, win);
-  return cudaGetLastError();
+// Set-up + subsample tables of both windows in one launch: CTAs per
+// (component, vector) and window chosen so that the whole grid is about one
+// wave of 8 CTAs per SM (each CTA repeats the component's FP64 set-up once),
+// at most one warp per box pixel.
+static cudaError_t launch_subsample(const FastArgs &a, const WinDesc &mw, const WinDesc &rw, bool region, int nBatch,
+                                    cudaStream_t st) {
+  const int sets = a.nComp * nBatch * (region ? 2 : 1);
+  const int cap = std::max(1, 8 * 152 / std::max(sets, 1));
+  const int nMain = std::max(1, std::min((a.boxMain * a.boxMain + 7) / 8, cap));
+  const int nReg = region ? std::max(1, std::min((a.boxReg * a.boxReg + 7) / 8, cap)) : 0;
+  dim3 grid(nMain + nReg, a.nComp, nBatch);
+  return launch_pdl(k_fast_subsample, grid, dim3(256), 0, st, a, mw, region ? rw : mw, nMain);
 }
 
 static cudaError_t launch_eval(const FastArgs &a, const WinDesc &w, const FFTLen &L, int nBatch, int win,
@@ -1349,22 +1427,20 @@ static cudaError_t launch_eval(const FastArgs &a, const WinDesc &w, const FFTLen
                     sizeof(cplx<float>) * 2 * rpb * (M + 1) + 16;
   ensure_smem(k_fast_eval_r2c, sm);
   dim3 grid((w.rows + rpb - 1) / rpb, nBatch);
-  k_fast_eval_r2c<<<grid, tu.rowThreads, sm, st>>>(a, w, plan32(L, true), reinterpret_cast<const cplx<float> *>(L.twL32), rpb,
-                                         win);
-  return cudaGetLastError();
+  return launch_pdl(k_fast_eval_r2c, grid, dim3(tu.rowThreads), sm, st, a, w, plan32(L, true),
+                    reinterpret_cast<const cplx<float> *>(L.twL32), rpb, win);
 }
 
 static cudaError_t launch_grad(const FastArgs &a, const WinDesc &w, const FFTLen &L, int nBatch, int blockBase,
-                               int win, const FastTune &tu, cudaStream_t st) {
+                               int win, const FastTune &tu, cudaStream_t st, int doneTotal) {
   const int M = L.half.n;
   const int rpb = tu.rowRpb;
   const size_t sm = sizeof(CompF32) * kMaxComponents + sizeof(int) * 2 * kMaxComponents +
-                    sizeof(float) * kMaxParams + sizeof(cplx<float>) * 3 * rpb * (M + 1) + 16;
+                    sizeof(ffloat) * kMaxParams + sizeof(cplx<float>) * 3 * rpb * (M + 1) + 16;
   ensure_smem(k_fast_grad_rows, sm);
   dim3 grid((w.rows + rpb - 1) / rpb, nBatch);
-  k_fast_grad_rows<<<grid, tu.rowThreads, sm, st>>>(a, w, plan32(L, true), reinterpret_cast<const cplx<float> *>(L.twL32), rpb,
-                                                   a.gradPart, blockBase, win);
-  return cudaGetLastError();
+  return launch_pdl(k_fast_grad_rows, grid, dim3(tu.rowThreads), sm, st, a, w, plan32(L, true),
+                    reinterpret_cast<const cplx<float> *>(L.twL32), rpb, a.gradPart, blockBase, win, doneTotal);
 }
 
 static void record(cudaEvent_t ev, cudaStream_t st) {
@@ -1414,14 +1490,13 @@ static void stage_end(const FastPlan &p, const char *name, cudaStream_t st) {
   } while (0)
 
 static cudaError_t launch_los_eval(const FastArgs &a, const WinDesc &w, int nBatch, LosStore ks, cudaStream_t st) {
-  k_fast_los_eval<<<dim3(kLosCtas, nBatch), 256, 0, st>>>(a, w, ks);
-  return cudaGetLastError();
+  return launch_pdl(k_fast_los_eval, dim3(kLosCtas, nBatch), dim3(256), 0, st, a, w, ks);
 }
 
 static cudaError_t launch_los_grad(const FastArgs &a, const WinDesc &w, int nBatch, int blockBase, LosStore ks,
-                                   cudaStream_t st) {
-  k_fast_los_grad<<<dim3(kLosCtas, nBatch), 256, 0, st>>>(a, w, a.gradPart, blockBase, ks);
-  return cudaGetLastError();
+                                   cudaStream_t st, int doneTotal) {
+  return launch_pdl(k_fast_los_grad, dim3(kLosCtas, nBatch), dim3(256), 0, st, a, w, a.gradPart, blockBase, ks,
+                    doneTotal);
 }
 
 static cudaError_t launch_region_down(const FastPlan &p, const FastArgs &a, int nBatch, cudaStream_t st) {
@@ -1430,13 +1505,13 @@ static cudaError_t launch_region_down(const FastPlan &p, const FastArgs &a, int 
   const size_t sm = sizeof(cplx<float>) * 3 * g.rScale * (M + 1);
   auto kern = a.nPs ? k_fast_region_down<true> : k_fast_region_down<false>;
   ensure_smem(kern, sm);
-  kern<<<dim3(g.rRows, nBatch), line_threads(M * g.rScale / 2), sm, st>>>(
-      a, g, reinterpret_cast<const cplx<float> *>(a.rspec), plan32(*p.Rx, true),
-      reinterpret_cast<const cplx<float> *>(p.Rx->twL32), a.regModel, 1);
-  return cudaGetLastError();
+  return launch_pdl(kern, dim3(g.rRows, nBatch), dim3(line_threads(M * g.rScale / 2)), sm, st, a, g,
+                    reinterpret_cast<const cplx<float> *>(a.rspec), plan32(*p.Rx, true),
+                    reinterpret_cast<const cplx<float> *>(p.Rx->twL32), a.regModel, 1);
 }
 
-static cudaError_t launch_stat(const FastPlan &p, const FastArgs &a, int nBatch, bool wantGrad, cudaStream_t st) {
+static cudaError_t launch_stat(const FastPlan &p, const FastArgs &a, int nBatch, bool wantGrad, cudaStream_t st,
+                               int doneTotal) {
   const FastGeom &g = p.g;
   const int M = p.Lx->half.n;
   const int rpb = p.tune.rowRpb;
@@ -1444,25 +1519,19 @@ static cudaError_t launch_stat(const FastPlan &p, const FastArgs &a, int nBatch,
   auto kern = a.nPs ? k_fast_stat_rows<true> : k_fast_stat_rows<false>;
   ensure_smem(kern, sm);
   dim3 grid((g.nDataRows + rpb - 1) / rpb, nBatch);
-  kern<<<grid, p.tune.rowThreads, sm, st>>>(a, g, plan32(*p.Lx, true),
-                                          reinterpret_cast<const cplx<float> *>(p.Lx->twL32), rpb, wantGrad ? 1 : 0);
-  return cudaGetLastError();
+  return launch_pdl(kern, grid, dim3(p.tune.rowThreads), sm, st, a, g, plan32(*p.Lx, true),
+                    reinterpret_cast<const cplx<float> *>(p.Lx->twL32), rpb, wantGrad ? 1 : 0, doneTotal);
 }
 
 static cudaError_t launch_region_g(const FastPlan &p, const FastArgs &a, int nBatch, cudaStream_t st) {
   const FastGeom &g = p.g;
   const int M = p.Rx->half.n;
   const size_t sm = sizeof(cplx<float>) * 2 * (M + 1);
-  k_fast_region_g_r2c<<<dim3(g.rSubRows, nBatch), line_threads(M), sm, st>>>(
-      a, g, reinterpret_cast<cplx<float> *>(a.rspec), plan32(*p.Rx, true),
-      reinterpret_cast<const cplx<float> *>(p.Rx->twL32));
-  return cudaGetLastError();
+  return launch_pdl(k_fast_region_g_r2c, dim3(g.rSubRows, nBatch), dim3(line_threads(M)), sm, st, a, g,
+                    reinterpret_cast<cplx<float> *>(a.rspec), plan32(*p.Rx, true),
+                    reinterpret_cast<const cplx<float> *>(p.Rx->twL32));
 }
 
-static cudaError_t launch_reduce(const FastArgs &a, int nBatch, int nGrad, int wantGrad, cudaStream_t st) {
-  k_fast_reduce<<<dim3(2 + (wantGrad ? a.nParams : 0), nBatch), 256, 0, st>>>(a, wantGrad ? nGrad : 0);
-  return cudaGetLastError();
-}
 
 // The whole statistic (+ gradient) evaluation.  With p.side set, the
 // oversampled-region pipeline runs on the side stream, forked after the
@@ -1470,6 +1539,7 @@ static cudaError_t launch_reduce(const FastArgs &a, int nBatch, int nGrad, int w
 // before the final reduction (adjoint).
 cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool wantGrad, cudaStream_t st) {
   const FastGeom &g = p.g;
+  if (!a.done) return cudaErrorInvalidValue;  // the final reduction needs the completion counters
   if (p.timer) p.timer->n = 0;
   if (p.timer && !p.timer->only) stage_end(p, "start", st);
   const bool fork = g.hasRegion && p.side;
@@ -1492,14 +1562,13 @@ cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool 
   if (!mks.panels) mks.count = nullptr;
   if (!rks.panels) rks.count = nullptr;
 
-  STAGE("setup", st, fast_setup(a, nBatch, st));
+  STAGE("subsample", st, launch_subsample(a, mw, rw, g.hasRegion != 0, nBatch, st));
   if (fork) {
     cudaError_t e = cudaEventRecord(p.fork0, st);
     if (!e) e = cudaStreamWaitEvent(rs, p.fork0, 0);
     if (e) return e;
   }
   if (g.hasRegion) {
-    STAGE("region_subsample", rs, launch_subsample(a, rw, 1, nBatch, rs));
     if (los) STAGE("region_los_eval", rs, launch_los_eval(a, rw, nBatch, rks, rs));
     STAGE("region_eval_r2c", rs, launch_eval(a, rw, *p.Rx, nBatch, 1, tu, rs));
     STAGE("region_cols_conv", rs,
@@ -1507,7 +1576,6 @@ cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool 
                              p.hrPitch, *p.Ry, rscale, 1, nBatch, rs, tu.colCpb, 0, 1, nullptr, tu.colThreads));
     STAGE("region_down", rs, launch_region_down(p, a, nBatch, rs));
   }
-  STAGE("subsample", st, launch_subsample(a, mw, 0, nBatch, st));
   if (los) STAGE("los_eval", st, launch_los_eval(a, mw, nBatch, mks, st));
   STAGE("eval_r2c", st, launch_eval(a, mw, *p.Lx, nBatch, 0, tu, st));
   STAGE("cols_conv", st,
@@ -1518,11 +1586,10 @@ cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool 
     if (!e) e = cudaStreamWaitEvent(st, p.join0, 0);
     if (e) return e;
   }
-  STAGE("stat_rows", st, launch_stat(p, a, nBatch, wantGrad, st));
-  if (!wantGrad) {
-    STAGE("reduce", st, launch_reduce(a, nBatch, 0, 0, st));
-    return cudaSuccess;
-  }
+  // without the gradient the statistic pass is the last one: its final CTA
+  // per vector adds the partials up; with it, the gradient passes' last CTA does
+  STAGE("stat_rows", st, launch_stat(p, a, nBatch, wantGrad, st, wantGrad ? 0 : fast_stat_blocks(g, tu)));
+  if (!wantGrad) return cudaSuccess;
   if (fork) {
     cudaError_t e = cudaEventRecord(p.fork1, st);
     if (!e) e = cudaStreamWaitEvent(rs, p.fork1, 0);
@@ -1533,20 +1600,19 @@ cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool 
     STAGE("region_cols_adjoint", rs,
           launch_cols32(a.rspec, g.rSpecPitch, g.rSpecBatch, p.Rx->L / 2 + 1, g.rSubRows, g.rWinRows, p.Hr,
                              p.hrPitch, *p.Ry, rscale, 2, nBatch, rs, tu.colCpb, 0, 1, nullptr, tu.colThreads));
-    STAGE("region_grad_rows", rs, launch_grad(a, rw, *p.Rx, nBatch, nMain, 1, tu, rs));
-    if (los) STAGE("region_los_grad", rs, launch_los_grad(a, rw, nBatch, nMain + nReg + kLosCtas, rks, rs));
+    STAGE("region_grad_rows", rs, launch_grad(a, rw, *p.Rx, nBatch, nMain, 1, tu, rs, nTot));
+    if (los) STAGE("region_los_grad", rs, launch_los_grad(a, rw, nBatch, nMain + nReg + kLosCtas, rks, rs, nTot));
   }
   STAGE("cols_adjoint", st,
         launch_cols32(a.spec, g.specPitch, g.specBatch, p.Lx->L / 2 + 1, g.nDataRows, g.winRows, p.H, p.hPitch,
                            *p.Ly, scale, 2, nBatch, st, tu.colCpb, p.hBatch, 1, p.hMap, tu.colThreads));
-  STAGE("grad_rows", st, launch_grad(a, mw, *p.Lx, nBatch, 0, 0, tu, st));
-  if (los) STAGE("los_grad", st, launch_los_grad(a, mw, nBatch, nMain + nReg, mks, st));
+  STAGE("grad_rows", st, launch_grad(a, mw, *p.Lx, nBatch, 0, 0, tu, st, nTot));
+  if (los) STAGE("los_grad", st, launch_los_grad(a, mw, nBatch, nMain + nReg, mks, st, nTot));
   if (fork) {
     cudaError_t e = cudaEventRecord(p.join1, rs);
     if (!e) e = cudaStreamWaitEvent(st, p.join1, 0);
     if (e) return e;
   }
-  STAGE("reduce", st, launch_reduce(a, nBatch, nTot, 1, st));
   return cudaSuccess;
 }
 

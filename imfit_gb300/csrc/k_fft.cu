@@ -257,6 +257,7 @@ template cudaError_t launch_rows_c2r<float>(const void *, long, long, int, float
 
 // ------------------------------------------------------------ FFT tables
 #include <cmath>
+#include <cstdlib>
 #include <mutex>
 #include <set>
 #include <utility>
@@ -275,6 +276,14 @@ void fft_prepare_kernels() {
   allow_max_smem((const void *)k_cols<double, 0>);
   allow_max_smem((const void *)k_cols<double, 1>);
   allow_max_smem((const void *)k_cols<double, 2>);
+}
+
+bool pdl_enabled() {
+  static const bool on = [] {
+    const char *v = getenv("IMFIT_PDL");
+    return !(v && v[0] == '0');
+  }();
+  return on;
 }
 
 void allow_max_smem(const void *kernel) {

@@ -3,10 +3,41 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <utility>
 #include "common.cuh"
 #include "psf_interp.cuh"
 
 namespace imfit {
+
+// ---------------------------------------------------------------------------
+// Programmatic dependent launch (PDL) for the fast path's chain of kernels.
+// Each kernel is launched with programmatic stream serialization, so the next
+// kernel of the stream (or graph) is scheduled while this one drains; every
+// such kernel waits (griddepcontrol.wait) for its predecessor's completion and
+// memory before it reads anything the predecessor wrote, and signals
+// (griddepcontrol.launch_dependents) once its main work is issued.  The wait is
+// the hardware dependency of the launch, not a spin loop.  IMFIT_PDL=0 in the
+// environment launches plainly (the waits then return at once).
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;\n" :::); }
+
+bool pdl_enabled();
+
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                       Args &&...args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl_enabled() ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 // Raise a kernel's dynamic shared-memory limit to the device's opt-in maximum,
 // once per (device, kernel).  The limit is never lowered, so launches of one
@@ -191,14 +222,21 @@ struct FastArgs {
   void *rspec;           // region half spectrum
   float *regModel;       // [B][rRows][rCols] downsampled region model
   float *regG;           // [B][rRows][rCols] dS/dM for region pixels
-  // per-CTA partial sums (FP32 over one CTA's pixels); the final reduction
-  // over CTAs is FP64.  Layouts [B][quantity][partStride].
-  float *statPart;       // quantities: S, sum of g * sum(PSF)
-  float *gradPart;       // quantities: the nParams gradient entries
+  // per-CTA partial sums, double-float (hi, lo) pairs: each thread sums its
+  // few pixels in FP32 and the warp's 32 thread sums in FP32; every level
+  // above (across warps, across CTAs) adds in double-float; the final value
+  // is returned in FP64.
+  // Layouts [B][quantity][partStride].
+  float2 *statPart;      // quantities: S, sum of g * sum(PSF)
+  float2 *gradPart;      // quantities: the nParams gradient entries
   int partStride;        // >= number of CTAs of any launch shape
   int nStatBlocks, nGradBlocks, nRegGradBlocks;
   double *stat;          // [B]
   double *grad;          // [B][nParams]
+  // [B] completion counters: the last CTA of the final pass of an evaluation
+  // (statistic pass without a gradient, else the gradient passes) adds the
+  // partials up; zeroed by the first kernel of each evaluation
+  unsigned *done;
   float *modelOut;       // optional: [B][N] model image (FP32) for inspection
   // subsampled pixels, precomputed warp-per-pixel over the whole GPU: for each
   // (batch, component, window) a square box of window pixels around the
@@ -223,7 +261,7 @@ struct FastArgs {
   int nPs;
   int psComp[kMaxPsFast];
   PsfInterp<float> psMain, psReg;
-  float *psPart;
+  float2 *psPart;
 };
 
 // CTAs per parameter vector of each line-of-sight kernel (grid-stride, one
@@ -280,7 +318,6 @@ struct JtwjArgs {
   float *jac;        // optional [B][nP + 1][nData]: d dev / d params, then the deviates
 };
 
-cudaError_t fast_setup(const FastArgs &a, int nBatch, cudaStream_t st);
 cudaError_t fast_jtwj(const FastPlan &p, const FastArgs &a, const JtwjArgs &J, int nBatch, cudaStream_t st);
 size_t fast_jtwj_smem(const FastPlan &p, int nD);
 cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool wantGrad, cudaStream_t st);

@@ -229,7 +229,8 @@ struct imfit_model_s {
   int psKind = 0;
   // fast path: FP32 interpolator tables, the component descriptors as on the
   // device (their psScale follows psScale), the gradient partials
-  DevBuf<float> dPsTab32, dPsRegTab32, dPsPart;
+  DevBuf<float> dPsTab32, dPsRegTab32;
+  DevBuf<float2> dPsPart;
   PsfInterp<float> psMain32{}, psReg32{};
   std::vector<CompDesc> hDesc;
   bool psfNormalize = true;
@@ -278,7 +279,7 @@ struct imfit_model_s {
   DevBuf<float> dSubTab;
   DevBuf<int> dSubBox;
   DevBuf<double> dParams, dStat, dGrad;
-  DevBuf<float> dStatPart, dGradPart;
+  DevBuf<float2> dStatPart, dGradPart;
   // image stack (fast path only): batch entry b has its own image, weights and PSF
   struct Stack {
     int n = 0, pc = 0, pr = 0;
@@ -306,6 +307,7 @@ struct imfit_model_s {
   int nDeriv = 0, jtwjCap = 0;
   DevBuf<int> dSlot;
   DevBuf<float> dDSpec32, dDRSpec32, dRegDeriv, dJPart;
+  DevBuf<unsigned> dDone;
   DevBuf<double> dAlpha, dBeta;
   FastTune tune;
   std::map<int, FastTune> tuned;  // per batch size
@@ -1265,6 +1267,8 @@ struct imfit_model_s {
     if (!e) e = dGradPart.reserve((size_t)B * nP * stride);
     if (!e && nPointSources) e = dPsPart.reserve((size_t)B * 4 * nPointSources * stride);
     if (!e) e = dStat.reserve(B);
+    if (!e) e = dDone.reserve(B);
+    if (!e) e = cudaMemset(dDone.p, 0, sizeof(unsigned) * B);
     if (!e) e = dGrad.reserve((size_t)B * nP);
     const long area = (long)kBoxMain * kBoxMain + (long)boxReg() * boxReg();
     if (!e) e = dSubTab.reserve((size_t)B * nC * area * 8);
@@ -1358,6 +1362,7 @@ struct imfit_model_s {
     a.nRegGradBlocks = fast_reg_grad_blocks(fg, tune);
     a.stat = dS;
     a.grad = dG;
+    a.done = dDone.p;
     a.modelOut = modelOut;
     a.nPs = 0;
     for (size_t f = 0; f < funcs.size() && nPointSources; f++)
