@@ -104,6 +104,8 @@ _SIGS = [
     ("imfit_SetAutotune", _I, [_P, _I]),
     ("imfit_GetLaunchShape", _I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     ("imfit_SetLaunchShape", _I, [_P, _I, _I, _I, _I]),
+    ("imfit_SetFFTPlan", _I, [_P, _I, _I]),
+    ("imfit_GetFFTPlan", _I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     ("imfit_MeasureSfuRate", _I, [_I, _DP]),
     ("imfit_HostAlloc", _I, [ctypes.c_ulong, ctypes.POINTER(_P)]),
     ("imfit_HostFree", _I, [_P]),
@@ -142,6 +144,18 @@ def load_library(build_if_missing=True):
 
 def exported_symbols():
     return [s[0] for s in _SIGS]
+
+
+def radix_schedule(n, order=0):
+    """The radices of an n-point transform in the library's order `order`
+    (0: 8, 4, 2 then 3, 5, 7; 1: 7, 5, 3 then 8, 4, 2; 2: 4, 2 then 3, 5, 7)."""
+    seq = {0: (8, 4, 2, 3, 5, 7), 1: (7, 5, 3, 8, 4, 2), 2: (4, 2, 3, 5, 7)}[order]
+    out = []
+    for p in seq:
+        while n % p == 0:
+            out.append(p)
+            n //= p
+    return out if n == 1 else None
 
 
 def measure_sfu_rate(device=0):
@@ -541,10 +555,25 @@ class ModelObject:
         """Pin the fast path's launch shape (rows_per_cta < 0: autotune again)."""
         return self._ck(self.lib.imfit_SetLaunchShape(self.h, rows_per_cta, row_threads, cols_per_cta, col_threads))
 
+    def set_fft_plan(self, candidate=-1, radix_order=0):
+        """Pin the fast path's padded-length candidate (0..2) and radix order
+        (0..2), or return to autotuning (candidate < 0)."""
+        self._ck(self.lib.imfit_SetFFTPlan(self.h, candidate, radix_order))
+
+    def fft_plan(self):
+        """(Lx, Ly, radix order) of the fast path's main window."""
+        lx, ly, v = _I(), _I(), _I()
+        self._ck(self.lib.imfit_GetFFTPlan(self.h, ctypes.byref(lx), ctypes.byref(ly), ctypes.byref(v)))
+        return lx.value, ly.value, v.value
+
     def launch_shape(self):
+        """Launch shape and FFT plan the fast path uses (after its first call)."""
         a, b, c = _I(), _I(), _I()
         self._ck(self.lib.imfit_GetLaunchShape(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
-        return {"rows_per_cta": a.value, "row_threads": b.value, "cols_per_cta": c.value}
+        lx, ly, order = self.fft_plan()
+        return {"rows_per_cta": a.value, "row_threads": b.value, "cols_per_cta": c.value, "Lx": lx, "Ly": ly,
+                "radix_order": order, "row_radices": radix_schedule(lx // 2, order) if lx else [],
+                "col_radices": radix_schedule(ly, order) if ly else []}
 
     def kernel_times(self):
         """[(kernel name, ms)] of the most recent fast evaluation."""

@@ -314,19 +314,43 @@ int smooth_size(int n, bool even) {
   }
 }
 
-int radix_schedule(int n, int *radix) {
+// Radix orders the fast path's autotuner chooses among (the transform is the
+// same; the pass count, the work per pass and the twiddle traffic differ):
+//   0: 8s, then 4s and 2s, then the odd radices 3, 5, 7;
+//   1: the odd radices 7, 5, 3 first, then 8s, 4s, 2s;
+//   2: 4s (and a final 2) instead of 8s, then 3, 5, 7.
+int radix_schedule(int n, int *radix, int variant) {
   int np = 0;
-  while (n % 8 == 0 && np < kMaxRadixPasses) { radix[np++] = 8; n /= 8; }
-  while (n % 4 == 0 && np < kMaxRadixPasses) { radix[np++] = 4; n /= 4; }
-  while (n % 2 == 0 && np < kMaxRadixPasses) { radix[np++] = 2; n /= 2; }
-  for (int p : {3, 5, 7})
-    while (n % p == 0 && np < kMaxRadixPasses) { radix[np++] = p; n /= p; }
+  auto take = [&](int p) {
+    while (n % p == 0 && np < kMaxRadixPasses) {
+      radix[np++] = p;
+      n /= p;
+    }
+  };
+  if (variant == 1) {
+    for (int p : {7, 5, 3, 8, 4, 2}) take(p);
+  } else if (variant == 2) {
+    for (int p : {4, 2, 3, 5, 7}) take(p);
+  } else {
+    for (int p : {8, 4, 2, 3, 5, 7}) take(p);
+  }
   return (n == 1) ? np : -1;
 }
 
-static cudaError_t table_create(FFTTable &t, int n) {
+// The `count` smallest 7-smooth lengths >= n (even if asked) within
+// maxRatio * n (the smallest one always).
+int smooth_candidates(int n, bool even, int count, double maxRatio, int *out) {
+  int k = 0;
+  for (int m = smooth_size(n, even); k < count; m = smooth_size(m + 1, even)) {
+    if (k > 0 && m > maxRatio * n) break;
+    out[k++] = m;
+  }
+  return k;
+}
+
+static cudaError_t table_create(FFTTable &t, int n, int variant) {
   t.n = n;
-  t.npass = radix_schedule(n, t.radix);
+  t.npass = radix_schedule(n, t.radix, variant);
   if (t.npass < 0) return cudaErrorInvalidValue;
   std::vector<double> w64(2 * (size_t)n);
   std::vector<float> w32(2 * (size_t)n);
@@ -347,12 +371,13 @@ static cudaError_t table_create(FFTTable &t, int n) {
   return cudaMemcpy(t.tw32, w32.data(), sizeof(float) * 2 * (size_t)n, cudaMemcpyHostToDevice);
 }
 
-cudaError_t fftlen_create(FFTLen &L, int len) {
+cudaError_t fftlen_create(FFTLen &L, int len, int variant) {
   L.L = len;
-  cudaError_t e = table_create(L.full, len);
+  L.variant = variant;
+  cudaError_t e = table_create(L.full, len, variant);
   if (e) return e;
   if (len % 2 == 0) {
-    e = table_create(L.half, len / 2);
+    e = table_create(L.half, len / 2, variant);
     if (e) return e;
     const int M = len / 2;
     std::vector<double> w64(2 * (size_t)(M + 1));

@@ -59,6 +59,7 @@ struct FFTTable {
 // split twiddles exp(-2 pi i k / L), k = 0..L/2.
 struct FFTLen {
   int L = 0;
+  int variant = 0;  // radix order (radix_schedule)
   FFTTable half;
   FFTTable full;
   void *twL64 = nullptr;
@@ -70,10 +71,14 @@ int line_threads(int points);
 // smallest 7-smooth (2,3,5,7) integer >= n, optionally even
 int smooth_size(int n, bool even);
 
-// radix schedule (8,4,2,3,5,7 preference); returns number of passes or -1
-int radix_schedule(int n, int *radix);
+// radix schedule of order `variant` (0: 8,4,2,3,5,7; 1: 7,5,3,8,4,2;
+// 2: 4,2,3,5,7); returns the number of passes or -1
+int radix_schedule(int n, int *radix, int variant = 0);
+constexpr int kRadixVariants = 3;
+// the `count` smallest 7-smooth lengths >= n within maxRatio * n; returns how many
+int smooth_candidates(int n, bool even, int count, double maxRatio, int *out);
 // allocate/free the device tables of one length
-cudaError_t fftlen_create(FFTLen &L, int len);
+cudaError_t fftlen_create(FFTLen &L, int len, int variant = 0);
 void fftlen_destroy(FFTLen &L);
 
 template <typename T>

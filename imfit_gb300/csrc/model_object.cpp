@@ -314,6 +314,17 @@ struct imfit_model_s {
   bool autotune = true;
   bool hasFixedTune = false;  // imfit_SetLaunchShape
   FastTune fixedTune;
+  // FFT plan of the fast path: padded length = the fftCand-th smallest
+  // 7-smooth even length >= the window (within 10 %), radix order fftVariant
+  // (radix_schedule); chosen by the autotuner unless pinned (imfit_SetFFTPlan)
+  int fftCand = 0, fftVariant = 0;
+  bool fftPinned = false, fftTuned = false;
+  static constexpr int kFftCandidates = 3;
+  int fftLength(int w) const {
+    int c[kFftCandidates];
+    const int n = smooth_candidates(w, true, kFftCandidates, 1.1, c);
+    return c[std::min(fftCand, n - 1)];
+  }
   int fastCap = 0;
   bool useGraphs = true;
   Captured graph;
@@ -1079,7 +1090,7 @@ struct imfit_model_s {
     g.yOrig = 2 - pr + pr / 2;
     fftlen_destroy(Fx);
     fftlen_destroy(Fy);
-    if (fftlen_create(Fx, smooth_size(g.winCols, true)) || fftlen_create(Fy, smooth_size(g.winRows, true)))
+    if (fftlen_create(Fx, fftLength(g.winCols), fftVariant) || fftlen_create(Fy, fftLength(g.winRows), fftVariant))
       return fail(IMFIT_E_CUDA, "FFT tables");
     if (Fx.L / 2 > 4096 || Fy.L > 4096) return fail(IMFIT_E_UNSUPPORTED, "image too large for the fast path");
     g.specPitch = even_pitch(Fx.L);
@@ -1125,7 +1136,8 @@ struct imfit_model_s {
       g.rStartOff = (float)(0.5 * frac - 0.5);
       fftlen_destroy(FRx);
       fftlen_destroy(FRy);
-      if (fftlen_create(FRx, smooth_size(g.rWinCols, true)) || fftlen_create(FRy, smooth_size(g.rWinRows, true)))
+      if (fftlen_create(FRx, fftLength(g.rWinCols), fftVariant) ||
+          fftlen_create(FRy, fftLength(g.rWinRows), fftVariant))
         return fail(IMFIT_E_CUDA, "FFT tables");
       if (FRx.L / 2 > 4096 || FRy.L > 4096) return fail(IMFIT_E_UNSUPPORTED, "region too large for the fast path");
       g.rSpecPitch = even_pitch(FRx.L);
@@ -1445,6 +1457,11 @@ struct imfit_model_s {
     if (cudaEventCreate(&e0) || cudaEventCreate(&e1)) return fail(IMFIT_E_CUDA, "autotune events");
     const bool timingWas = timing;
     timing = false;
+    auto release = [&]() {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      timing = timingWas;
+    };
     auto measure = [&](const FastTune &t, float &best) -> cudaError_t {
       tune = t;
       FastArgs a = fastArgs(dP, dS, dG ? dG : dGrad.p, nullptr);
@@ -1465,10 +1482,49 @@ struct imfit_model_s {
       }
       return e;
     };
+    cudaError_t e = cudaSuccess;
+    // the FFT plan first (padded lengths x radix orders, default launch shape),
+    // once per handle: a single image only (image stacks keep the smallest
+    // lengths of their bucket).  A new plan re-runs the fast set-up, which
+    // resizes the plan-dependent buffers (spectra) through ensureFastCap here
+    // and ensureJtwjCap in the callers that need it, after this returns.
+    if (!stack.n && !fftPinned && !fftTuned) {
+      int bestC = 0, bestV = 0;
+      float bestPlan = 1e30f;
+      for (int cand = 0; cand < kFftCandidates && !e; cand++) {
+        for (int var = 0; var < kRadixVariants && !e; var++) {
+          fftCand = cand;
+          fftVariant = var;
+          fastReady = false;
+          int st = prepareFast();
+          if (!st) st = ensureFastCap(B);
+          if (st) {
+            release();
+            return st;
+          }
+          float ms;
+          e = measure(FastTune{}, ms);
+          if (!e && ms < bestPlan) {
+            bestPlan = ms;
+            bestC = cand;
+            bestV = var;
+          }
+        }
+      }
+      fftCand = bestC;
+      fftVariant = bestV;
+      fastReady = false;
+      int st = e ? 0 : prepareFast();
+      if (!st && !e) st = ensureFastCap(B);
+      if (st) {
+        release();
+        return st;
+      }
+      fftTuned = true;
+    }
     const int rowShapes[][2] = {{1, 128}, {1, 256}, {2, 256}, {3, 256}, {4, 256}, {2, 512}, {4, 512}};
     FastTune bestT{};
     float bestMs = 1e30f;
-    cudaError_t e = cudaSuccess;
     for (auto &rs : rowShapes) {
       FastTune t{};
       t.rowRpb = rs[0];
@@ -1490,9 +1546,7 @@ struct imfit_model_s {
         if (ms < bestMs) { bestMs = ms; bestT = t; }
       }
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    timing = timingWas;
+    release();
     if (e) return cuda_fail(e, "autotune");
     tune = bestT;
     tuned[B] = tune;
@@ -1588,13 +1642,15 @@ struct imfit_model_s {
     if (stack.n && (curEntry ? B > stack.n : B != stack.n))
       return fail(IMFIT_E_ARG, "an image stack evaluates exactly one parameter vector per image");
     st = ensureFastCap(B);
-    if (!st) st = ensureJtwjCap(B);
     if (st) return st;
     if (!dP || !dS || !dA || !dBt) return fail(IMFIT_E_ARG, "JtWJ: null device buffer");
     if (tuned.find(B) == tuned.end()) {
       st = autotuneFast(B, dP, dS, nullptr);
       if (st) return st;
     }
+    // after the autotuner: its choice of FFT plan sets the derivative spectra's size
+    st = ensureJtwjCap(B);
+    if (st) return st;
     FastArgs a = fastArgs(dP, dS, dGrad.p, dModelOut.p);
     FastPlan p = fastPlan();
     int optin = 0;
@@ -2421,6 +2477,35 @@ int imfit_SetLaunchShape(imfit_model_t m, int rowRpb, int rowThreads, int colCpb
     cudaGraphExecDestroy(m->graph.exec);
     m->graph = Captured{};
   }
+  return 0;
+}
+
+int imfit_SetFFTPlan(imfit_model_t m, int candidate, int radixOrder) {
+  GET(m);
+  if (candidate < 0) {
+    m->fftPinned = false;
+    m->fftTuned = false;
+  } else {
+    if (candidate >= imfit_model_s::kFftCandidates || radixOrder < 0 || radixOrder >= kRadixVariants)
+      return m->fail(IMFIT_E_ARG, "bad FFT plan");
+    m->fftCand = candidate;
+    m->fftVariant = radixOrder;
+    m->fftPinned = true;
+  }
+  m->fastReady = false;
+  m->tuned.clear();
+  if (m->graph.exec) {
+    cudaGraphExecDestroy(m->graph.exec);
+    m->graph = Captured{};
+  }
+  return 0;
+}
+
+int imfit_GetFFTPlan(imfit_model_t m, int *Lx, int *Ly, int *radixOrder) {
+  GET(m);
+  if (Lx) *Lx = m->Fx.L;
+  if (Ly) *Ly = m->Fy.L;
+  if (radixOrder) *radixOrder = m->fftVariant;
   return 0;
 }
 

@@ -304,6 +304,17 @@ int imfit_SetLaunchShape(imfit_model_t m, int rowsPerCta, int rowThreads, int co
  * T_roof = bytes / HBM bandwidth + SFU operations / P_SFU.  Measurement helper
  * with no counterpart in the reference; it changes no device setting. */
 int imfit_MeasureSfuRate(int device, double *opsPerSecond);
+/* FFT plan of the fast path (no counterpart in the reference, which plans
+ * FFTW with FFTW_ESTIMATE on the smallest padded size, core/convolver.cpp:253-256).
+ * The padded length of each axis is one of the three smallest 7-smooth even
+ * lengths >= the window (within 10 %), the radix order one of three
+ * (0: radix 8, 4, 2 then 3, 5, 7; 1: 7, 5, 3 then 8, 4, 2; 2: 4, 2 then
+ * 3, 5, 7).  By default the autotuner times every pair on the first fast call
+ * and keeps the fastest; SetFFTPlan pins candidate (0..2) and order (0..2), or
+ * returns to autotuning with candidate < 0.  GetFFTPlan reports the lengths
+ * in use (Lx, Ly of the main window) and the order. */
+int imfit_SetFFTPlan(imfit_model_t m, int candidate, int radixOrder);
+int imfit_GetFFTPlan(imfit_model_t m, int *Lx, int *Ly, int *radixOrder);
 /* Page-locked host memory for the host-buffer entry points (cudaMallocHost). */
 int imfit_HostAlloc(unsigned long bytes, void **ptr);
 int imfit_HostFree(void *ptr);
