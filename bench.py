@@ -55,7 +55,9 @@ def parse():
                     help="C4: evaluate only the first N of the 256 parameter vectors (small profiling cases)")
     ap.add_argument("--c5-count", type=int, default=4096, help="cutouts in the C5 batch")
     ap.add_argument("--c5-threads", type=int, default=8, help="host threads driving the C5 size buckets")
-    ap.add_argument("--c5-check", type=int, default=4, help="C5 cutouts re-fitted in FP64 on the CPU")
+    ap.add_argument("--c5-mode", default="set", choices=["set", "buckets"],
+                    help="C5: one cutout set (one launch per stage) or size buckets of image stacks")
+    ap.add_argument("--c5-check", type=int, default=12, help="C5 cutouts re-fitted in FP64 on the CPU")
     ap.add_argument("--no-graphs", action="store_true", help="launch kernels one by one (for profilers)")
     ap.add_argument("--jtwj", action="store_true",
                     help="time the forward-mode normal equations (J^T W J, J^T W dev) instead of the gradient")
@@ -667,7 +669,8 @@ def run_c5(args, rank, local_rank, world):
     t_synth = time.time() - t0
     cs = [cutouts.Cutout(d, s, p) for d, s, p in imgs]
     t0 = time.time()
-    fitter = cutouts.CutoutFitter(workloads.C5_FUNCTIONS, cs, device=local_rank, threads=args.c5_threads)
+    fitter = cutouts.CutoutFitter(workloads.C5_FUNCTIONS, cs, device=local_rank, threads=args.c5_threads,
+                                  mode=args.c5_mode)
     t_setup = time.time() - t0
     starts = np.array([it["start"] for it in items])
     lo = np.array([it["lower"] for it in items])
@@ -687,14 +690,21 @@ def run_c5(args, rank, local_rank, world):
     clk = clocks.stop()
     t_fit = max_over_ranks(t_fit, world)
     value = world * len(items) * args.steps / t_fit
-    # accuracy: FP64 fits of the smallest few cutouts
+    # accuracy against FP64 fits (oracle deviates, scipy's trust-region least
+    # squares with the same limits and tight tolerances) of a few cutouts of
+    # side <= 120 px spread over the sizes: (1) the FP64 minimum nearest to our
+    # fit (the FP64 fit started from our parameters) -- how far our solution
+    # is from a true FP64 minimum; (2) the FP64 fit from the same start --
+    # whether both optimisers end in the same basin (the model is multimodal:
+    # bulge and disk can trade places, ellipticities pin at limits).
     acc = None
     if rank == 0 and args.c5_check > 0:
         import scipy.optimize as so
 
         import oracle
         oracle.build_restatement()
-        order = np.argsort([it["side"] for it in items])[: args.c5_check]
+        small = [i for i in np.argsort([it["side"] for it in items]) if items[i]["side"] <= 120]
+        order = [small[int(k)] for k in np.linspace(0, len(small) - 1, min(args.c5_check, len(small)))]
         errs = []
         for i in order:
             d, sg, p = imgs[i]
@@ -706,10 +716,12 @@ def run_c5(args, rank, local_rank, world):
             o.add_image_data(d)
             o.add_error_vector(sg)
             o.final_setup()
-            ref = so.least_squares(lambda x: o.compute_deviates(x), starts[i], bounds=(lo[i], hi[i]),
-                                   method="trf", x_scale="jac", xtol=1e-15, ftol=1e-15, gtol=1e-15,
-                                   max_nfev=20000)
             got = r["params"][i]
+            fit64 = lambda x0: so.least_squares(lambda x: o.compute_deviates(x), x0, bounds=(lo[i], hi[i]),
+                                                method="trf", x_scale="jac", xtol=1e-15, ftol=1e-15, gtol=1e-15,
+                                                max_nfev=20000)
+            near = fit64(np.clip(got, lo[i], hi[i]))
+            same = fit64(starts[i])
             g = imfit_gb300.ModelObject(local_rank)
             for name, new_set in workloads.C5_FUNCTIONS:
                 g.add_function(name, new_set)
@@ -720,19 +732,34 @@ def run_c5(args, rank, local_rank, world):
             g.final_setup()
             _, A, _ = g.jtwj(got)
             sig = np.sqrt(np.abs(np.diag(np.linalg.pinv(A))))
-            chi_ref = float(ref.fun @ ref.fun)
-            diff = got - ref.x
+            chi_got = o.get_fit_statistic(got)
+            chi_near, chi_same = float(near.fun @ near.fun), float(same.fun @ same.fun)
+            diff = got - near.x
             for j in (2, 7):  # position angles: PA and PA + 180 are the same model
                 diff[j] = (diff[j] + 90.0) % 180.0 - 90.0
+            relv = np.abs(diff) / np.maximum(np.abs(near.x), 1e-12)
+            osv = np.abs(diff) / np.maximum(sig, 1e-300)
             errs.append({"side": int(items[i]["side"]),
-                         "max_rel_err": float(np.max(np.abs(diff) / np.maximum(np.abs(ref.x), 1e-12))),
-                         "max_err_over_sigma": float(np.max(np.abs(diff) / np.maximum(sig, 1e-300))),
-                         "chi2_rel_diff": float((o.get_fit_statistic(got) - chi_ref) / chi_ref)})
+                         "max_rel_err": float(np.max(relv)),
+                         "max_err_over_sigma": float(np.max(osv)),
+                         "chi2_rel_diff_vs_nearest_fp64": float((chi_got - chi_near) / chi_near),
+                         "chi2_rel_diff_vs_same_start_fp64": float((chi_got - chi_same) / chi_same),
+                         "rel": relv, "over_sigma": osv})
+        rel = np.array([e["rel"] for e in errs])
+        osg = np.array([e["over_sigma"] for e in errs])
+        same = np.array([e["chi2_rel_diff_vs_same_start_fp64"] for e in errs])
         acc = {"cutouts_checked": int(len(order)),
-               "reference": "scipy least_squares (trf, same limits) on the oracle's FP64 deviates",
-               "max_param_rel_err": max(e["max_rel_err"] for e in errs),
-               "max_param_err_over_sigma": max(e["max_err_over_sigma"] for e in errs),
-               "per_cutout": errs}
+               "reference": "nearest FP64 minimum: scipy least_squares (trf, same limits, tolerances 1e-15) on the "
+                            "oracle's FP64 deviates, started from this fit",
+               "max_param_rel_err": float(rel.max()),
+               "max_param_err_over_sigma": float(osg.max()),
+               "fraction_params_within_1e-4_rel": float(np.mean(rel <= 1e-4)),
+               "fraction_params_within_1e-4_rel_or_0.01_sigma": float(np.mean((rel <= 1e-4) | (osg <= 0.01))),
+               "fraction_params_within_1e-4_rel_per_param": [float(v) for v in np.mean(rel <= 1e-4, axis=0)],
+               "same_start_fp64": {"fraction_same_chi2_1e-6": float(np.mean(np.abs(same) <= 1e-6)),
+                                   "fraction_lower_chi2_here": float(np.mean(same < -1e-6)),
+                                   "fraction_higher_chi2_here": float(np.mean(same > 1e-6))},
+               "per_cutout": [{k: v for k, v in e.items() if k not in ("rel", "over_sigma")} for e in errs]}
     if rank == 0:
         sides = np.array([it["side"] for it in items])
         line = {"metric": "cutout fits/s (batched LM, forward-mode JtWJ, FP32 eval / FP64 reductions and solve)",
@@ -743,7 +770,9 @@ def run_c5(args, rank, local_rank, world):
                 "config": {"workload": f"C5: {len(items)} cutouts, side {sides.min()}-{sides.max()} px "
                                        f"(mean area {float((sides ** 2).mean()):.0f} px), Sersic+Exponential, "
                                        "Moffat PSF 25-63 px, chi^2",
-                           "buckets": len(fitter.buckets), "host_threads": args.c5_threads,
+                           "mode": args.c5_mode + (" (one handle, one launch per stage over all cutouts)"
+                                                   if args.c5_mode == "set" else ""),
+                           "buckets": len(fitter.buckets), "host_threads": args.c5_threads if fitter.buckets else 1,
                            "parallelism": "single GPU"},
                 "lm": {"status_counts": {str(k): int(v) for k, v in zip(*np.unique(r["status"], return_counts=True))},
                        "mean_rounds": float(np.mean(r["niter"]))},

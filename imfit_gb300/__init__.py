@@ -90,6 +90,9 @@ _SIGS = [
     ("imfit_BootstrapFitBatch", _I, [_P, _I, _DP, ctypes.POINTER(_I), _DP, _DP, _D, _I, _DP, _DP,
                                      ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     ("imfit_SetupImageStack", _I, [_P, _I, _I, _I, _DP, _DP, _DP, _I, _I]),
+    ("imfit_SetupCutouts", _I, [_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), _DP, _DP, ctypes.POINTER(_I),
+                                ctypes.POINTER(_I), _DP]),
+    ("imfit_CutoutsJtWJ", _I, [_P, _I, ctypes.POINTER(_I), _DP, _DP, _DP, _DP]),
     ("imfit_MinimizeNormalEquations", _I, [_I, _DP, ctypes.POINTER(_I), _DP, _DP, _D, _I, NORMAL_EQ_FN, _P, _DP,
                                            ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     ("imfit_SetFunctionOptionalParam", _I, [_P, _I, ctypes.c_char_p, ctypes.c_char_p]),
@@ -526,6 +529,36 @@ class ModelObject:
         n, nr, nc = im.shape
         return self._ck(self.lib.imfit_SetupImageStack(self.h, n, nc, nr, _dp(im), _dp(sg), _dp(ps),
                                                        ps.shape[2], ps.shape[1]))
+
+    def setup_cutouts(self, images, sigmas, psfs):
+        """A cutout set: lists of images (rows x cols, each its own size), their
+        sigma images (or scalars) and their odd-sized PSFs."""
+        n = len(images)
+        ims = [_f64(im) for im in images]
+        sgs = [_f64(np.broadcast_to(sg, im.shape)) for im, sg in zip(ims, sigmas)]
+        pss = [_f64(p) for p in psfs]
+        IA = ctypes.c_int * n
+        cols = IA(*[im.shape[1] for im in ims])
+        rows = IA(*[im.shape[0] for im in ims])
+        pc = IA(*[p.shape[1] for p in pss])
+        pr = IA(*[p.shape[0] for p in pss])
+        pix = np.concatenate([im.ravel() for im in ims])
+        sig = np.concatenate([sg.ravel() for sg in sgs])
+        psf = np.concatenate([p.ravel() for p in pss])
+        self._n_cutouts = n
+        return self._ck(self.lib.imfit_SetupCutouts(self.h, n, cols, rows, _dp(pix), _dp(sig), pc, pr, _dp(psf)))
+
+    def cutouts_jtwj(self, cutouts, params):
+        """(statistics, J^T J, J^T dev) of the given cutouts at params (K x nParams)."""
+        idx = np.ascontiguousarray(cutouts, dtype=np.int32)
+        P = _f64(np.atleast_2d(params))
+        K, n = P.shape[0], self.n_params
+        S = np.empty(K)
+        A = np.empty((K, n, n))
+        B = np.empty((K, n))
+        self._ck(self.lib.imfit_CutoutsJtWJ(self.h, K, idx.ctypes.data_as(ctypes.POINTER(_I)), _dp(P), _dp(S),
+                                            _dp(A), _dp(B)))
+        return S, A, B
 
     def synchronize(self):
         return self._ck(self.lib.imfit_Synchronize(self.h))

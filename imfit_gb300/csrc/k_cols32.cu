@@ -79,30 +79,26 @@ __device__ __forceinline__ void store_row(cplx<float> *dst, const cplx<float> *s
   }
 }
 
+}  // namespace
+
+// Column group body, shared with the ragged cutout kernels: the CPB columns
+// starting at c0 of the spectrum `spec` (pitch, Ly = plan.n rows, nColsC
+// columns), H (hPitch) the PSF spectrum of the same geometry, in the dynamic
+// shared memory smem_raw (Ly * (1 + 3 * CPB) complex values).
 // MODE 1: multiply by H (convolution); MODE 2: by conj(H) (adjoint correlation).
-// Batch entry y uses H + e * hBatch with e = y / hDiv, or hMap[e] when a map
-// is given (hBatch 0: one PSF spectrum for every entry).
 template <int MODE, int CPB>
-__global__ void __launch_bounds__(1024) k_cols32(cplx<float> *__restrict__ spec, long pitch, long batch,
-                                                int nColsC, int nRowsIn, int nRowsOut,
-                                                const cplx<float> *__restrict__ H, long hPitch, FFTPlan<float> plan,
-                                                float scale, long hBatch, int hDiv, const int *__restrict__ hMap) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  pdl_wait();
+__device__ __forceinline__ void cols_group(unsigned char *smem_raw, cplx<float> *spec, long pitch, int nColsC,
+                                           int nRowsIn, int nRowsOut, const cplx<float> *H, long hPitch,
+                                           const FFTPlan<float> &plan, float scale, int c0) {
   const int Ly = plan.n;
   cplx<float> *tw = reinterpret_cast<cplx<float> *>(smem_raw);
   cplx<float> *bufA = tw + Ly;
   cplx<float> *bufB = bufA + (long)Ly * CPB;
   cplx<float> *bufH = bufB + (long)Ly * CPB;
-  const int c0 = blockIdx.x * CPB;
   const int nl = min(CPB, nColsC - c0);
   if (nl <= 0) return;
   const int pairs = (nl + 1) >> 1;
-  spec += blockIdx.y * batch + c0;
-  if (hBatch) {
-    const int e = blockIdx.y / hDiv;
-    H += (long)(hMap ? hMap[e] : e) * hBatch;
-  }
+  spec += c0;
   H += c0;
   // all global reads of the CTA in flight at once
   for (int t = threadIdx.x; t < Ly; t += blockDim.x) {
@@ -128,6 +124,25 @@ __global__ void __launch_bounds__(1024) k_cols32(cplx<float> *__restrict__ spec,
   pdl_trigger();
   for (int t = threadIdx.x; t < nRowsOut; t += blockDim.x)
     store_row<CPB>(spec + (long)t * pitch, Y + (long)t * CPB, pairs);
+}
+
+namespace {
+
+// Batch entry y uses H + e * hBatch with e = y / hDiv, or hMap[e] when a map
+// is given (hBatch 0: one PSF spectrum for every entry).
+template <int MODE, int CPB>
+__global__ void __launch_bounds__(1024) k_cols32(cplx<float> *__restrict__ spec, long pitch, long batch,
+                                                int nColsC, int nRowsIn, int nRowsOut,
+                                                const cplx<float> *__restrict__ H, long hPitch, FFTPlan<float> plan,
+                                                float scale, long hBatch, int hDiv, const int *__restrict__ hMap) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  pdl_wait();
+  if (hBatch) {
+    const int e = blockIdx.y / hDiv;
+    H += (long)(hMap ? hMap[e] : e) * hBatch;
+  }
+  cols_group<MODE, CPB>(smem_raw, spec + blockIdx.y * batch, pitch, nColsC, nRowsIn, nRowsOut, H, hPitch, plan,
+                        scale, blockIdx.x * CPB);
 }
 
 template <int MODE, int CPB>
@@ -159,6 +174,30 @@ cudaError_t launch_mode(int cpb, cplx<float> *s, long pitch, long batch, int nCo
 }
 
 }  // namespace
+
+// Column pass of a ragged cutout set: CTA t serves column group g of spectrum
+// `line` of the slot that owns t (each cutout its own lengths and pitch).
+constexpr int kRagCpb = 2;
+__global__ void __launch_bounds__(256) k_rag_cols(RagArgs r) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  pdl_wait();
+  const int t = blockIdx.x;
+  const int k = rag_slot(r.start, r.K, t);
+  const RagEntry &E = r.ent[r.act[k]];
+  const int local = t - r.start[k];
+  const int line = local / E.colGroups, g = local - line * E.colGroups;
+  cplx<float> *spec = r.spec + (r.lines == 1 ? E.specOff : (long)r.lines * E.specOff + (long)line * E.specSize);
+  const float scale = 1.f / ((float)E.Lx * (float)E.Ly);
+  cols_group<1, kRagCpb>(smem_raw, spec, E.pitch, E.Lx / 2 + 1, E.winRows, E.nDataRows, r.H + E.hOff, E.pitch,
+                         E.colPlan, scale, g * kRagCpb);
+}
+
+cudaError_t launch_rag_cols(const RagArgs &r, int total, int maxLy, cudaStream_t st) {
+  if (total <= 0) return cudaSuccess;
+  allow_max_smem((const void *)k_rag_cols);
+  const size_t sm = sizeof(cplx<float>) * (size_t)maxLy * (1 + 3 * kRagCpb);
+  return launch_pdl(k_rag_cols, dim3(total), dim3(128), sm, st, r);
+}
 
 size_t cols32_smem(int Ly, int cpb) { return sizeof(cplx<float>) * (size_t)Ly * (1 + 3 * cpb); }
 

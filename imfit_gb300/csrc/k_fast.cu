@@ -1695,6 +1695,385 @@ cudaError_t fast_jtwj(const FastPlan &p, const FastArgs &a, const JtwjArgs &J, i
   return cudaSuccess;
 }
 
+// ======================================================= ragged cutout sets
+// The J^T W J evaluation of a ragged cutout set (one model, many cutouts of
+// different sizes; see RagEntry): the same stages as fast_forward + fast_jtwj
+// for a single image, each one launch over all active cutouts.  Per-evaluation
+// state (parameters, component records, subsample tables, background levels,
+// outputs) is indexed by the slot k of the active list; per-cutout data
+// (images, PSF spectra, spectra, model images, row partials) by its entry.
+
+__device__ __forceinline__ WinDesc rag_win(const RagEntry &E, cplx<float> *spec) {
+  WinDesc w{};
+  w.cols = E.winCols;
+  w.rows = E.winRows;
+  w.isRegion = 0;
+  w.xOrig = E.xOrig;
+  w.yOrig = E.yOrig;
+  w.specPitch = E.pitch;
+  w.specBatch = E.specSize;
+  w.spec = spec;
+  return w;
+}
+
+// Set-up of component c for slot k, then its subsampled pixels (one warp per
+// box pixel, grid-stride over the gridDim.x CTAs of the slot and component).
+__global__ void __launch_bounds__(256) k_rag_subsample(FastArgs a, RagArgs r) {
+  pdl_wait();
+  const int k = blockIdx.z, c = blockIdx.y;
+  if (blockIdx.x != 0 && !(a.desc[c].subsample && subsampling_type(a.desc[c].type))) return;
+  __shared__ CompF32 rec;
+  setup_component(a, c, k, rec, blockIdx.x == 0 && c == 0);
+  const CompF32 cc = rec;
+  if (blockIdx.x == 0 && threadIdx.x == 0) a.comps[k * a.nComp + c] = cc;
+  if (!cc.subsample || !subsampling_type(cc.type)) return;
+  const RagEntry &E = r.ent[r.act[k]];
+  const WinDesc w = rag_win(E, nullptr);
+  const int side = a.boxMain;
+  int col0, row0;
+  box_origin(w, cc, side, col0, row0);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    int *o = a.subBox + ((long)k * a.nComp + c) * 4;
+    o[0] = col0;
+    o[1] = row0;
+  }
+  const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const FastDiv bySide(side);
+  for (int p = blockIdx.x * nw + (threadIdx.x >> 5); p < side * side; p += gridDim.x * nw) {
+    const int pr = bySide.div(p);
+    const int row = row0 + pr, col = col0 + (p - pr * side);
+    if (row < 0 || row >= w.rows || col < 0 || col >= w.cols) continue;
+    float dx, dy;
+    win_offsets(w, cc, row, col, dx, dy);
+    const Geo g = geo32(cc, dx, dy);
+    const int ns = sub_count(cc, g);
+    if (ns <= 1) continue;
+    const float d = 1.f / ns;
+    const float xs = dx - 0.5f + 0.5f * d, ys = dy - 0.5f + 0.5f * d;
+    float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    switch (cc.type) {
+      case F_SERSIC: subsample_sum<F_SERSIC>(cc, ns, xs, ys, d, lane, acc); break;
+      case F_EXP: subsample_sum<F_EXP>(cc, ns, xs, ys, d, lane, acc); break;
+      case F_MOFFAT: subsample_sum<F_MOFFAT>(cc, ns, xs, ys, d, lane, acc); break;
+      default: subsample_sum<F_GAUSS>(cc, ns, xs, ys, d, lane, acc); break;
+    }
+#pragma unroll
+    for (int q = 0; q < 8; q++) acc[q] = warp_sum(acc[q]);
+    if (lane == 0) {
+      float *dst = a.subTab + sub_base(a, k, c, 0) + (long)p * 8;
+      const float dd = d * d;
+#pragma unroll
+      for (int q = 0; q < 8; q++) dst[q] = acc[q] * dd;
+    }
+  }
+}
+
+// One window row of one cutout per CTA: evaluated model row, row r2c.
+__global__ void __launch_bounds__(512) k_rag_eval_r2c(FastArgs a, RagArgs r) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  pdl_wait();
+  const int t = blockIdx.x;
+  const int k = rag_slot(r.start, r.K, t);
+  const RagEntry &E = r.ent[r.act[k]];
+  const int row = t - r.start[k];
+  const int M = E.rowPlan.n, ls = M + 1;
+  CompF32 *sc = reinterpret_cast<CompF32 *>(smem);
+  int *boxes = reinterpret_cast<int *>(sc + kMaxComponents);
+  cplx<float> *bufA = reinterpret_cast<cplx<float> *>(boxes + 2 * kMaxComponents);
+  cplx<float> *bufB = bufA + ls;
+  const int nC = a.nComp;
+  for (int i = threadIdx.x; i < nC; i += blockDim.x) {
+    sc[i] = a.comps[k * nC + i];
+    const int *o = a.subBox + ((long)k * nC + i) * 4;
+    boxes[2 * i] = o[0];
+    boxes[2 * i + 1] = o[1];
+  }
+  for (int i = threadIdx.x; i < M; i += blockDim.x) bufA[i] = {0.f, 0.f};
+  __syncthreads();
+  const WinDesc w = rag_win(E, r.spec + E.specOff);
+  const FastDiv byM(M);
+  for (int c = 0; c < nC; c++) {
+    const CompF32 cc = sc[c];
+    if (!in_rows(cc.type)) continue;
+    const float *tab = a.subTab + sub_base(a, k, c, 0);
+    const int bc0 = boxes[2 * c], br0 = boxes[2 * c + 1], side = a.boxMain;
+    switch (cc.type) {
+      case F_SERSIC: eval_pixels<F_SERSIC>(cc, w, row, 1, M, ls, byM, bufA, tab, side, bc0, br0); break;
+      case F_EXP: eval_pixels<F_EXP>(cc, w, row, 1, M, ls, byM, bufA, tab, side, bc0, br0); break;
+      case F_GRING: eval_pixels<F_GRING>(cc, w, row, 1, M, ls, byM, bufA, tab, side, bc0, br0); break;
+      case F_MOFFAT: eval_pixels<F_MOFFAT>(cc, w, row, 1, M, ls, byM, bufA, tab, side, bc0, br0); break;
+      case F_GAUSS: eval_pixels<F_GAUSS>(cc, w, row, 1, M, ls, byM, bufA, tab, side, bc0, br0); break;
+      case F_TILTEDSKY: eval_pixels<F_TILTEDSKY>(cc, w, row, 1, M, ls, byM, bufA, tab, side, bc0, br0); break;
+      default: break;
+    }
+  }
+  __syncthreads();
+  cplx<float> *Z = block_fft(bufA, bufB, E.rowPlan, 1, ls, 1, -1, false);
+  pdl_trigger();
+  cplx<float> *out = w.spec + (long)row * E.pitch;
+  for (int kk = threadIdx.x; kk <= M; kk += blockDim.x) out[kk] = r2c_post(Z, kk, M, E.twL);
+}
+
+// One data row of one cutout per CTA: inverse row FFT of the convolved
+// spectrum, the FP32 model row (plus the constant background) to r.model.
+__global__ void __launch_bounds__(512) k_rag_model_rows(FastArgs a, RagArgs r) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  pdl_wait();
+  const int t = blockIdx.x;
+  const int k = rag_slot(r.start, r.K, t);
+  const RagEntry &E = r.ent[r.act[k]];
+  const int row = t - r.start[k];
+  const int M = E.rowPlan.n, ls = M + 1;
+  cplx<float> *bufX = reinterpret_cast<cplx<float> *>(smem);
+  cplx<float> *bufA = bufX + ls;
+  cplx<float> *bufB = bufA + ls;
+  const cplx<float> *in = r.spec + E.specOff + (long)row * E.pitch;
+  for (int kk = threadIdx.x; kk <= M; kk += blockDim.x) bufX[kk] = in[kk];
+  __syncthreads();
+  for (int kk = threadIdx.x; kk < M; kk += blockDim.x) bufA[kk] = c2r_pre(bufX, kk, M, E.twL);
+  __syncthreads();
+  const cplx<float> *Z = block_fft(bufA, bufB, E.rowPlan, 1, ls, 1, +1, false);
+  pdl_trigger();
+  const float *zr = reinterpret_cast<const float *>(Z);
+  const float bg = a.bgLevel[2 * k];
+  float *m = r.model + E.dataOff + (long)row * E.nDataCols;
+  for (int col = threadIdx.x; col < E.nDataCols; col += blockDim.x) m[col] = zr[col] + bg;
+}
+
+// One window row of one cutout per CTA: the nD derivative rows (typed pixel
+// passes), their row FFTs, to derivative spectrum j of the cutout.
+__global__ void __launch_bounds__(512) k_rag_deriv_r2c(FastArgs a, RagArgs r, const int *__restrict__ slot, int nD) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  pdl_wait();
+  const int t = blockIdx.x;
+  const int k = rag_slot(r.start, r.K, t);
+  const RagEntry &E = r.ent[r.act[k]];
+  const int row = t - r.start[k];
+  const int M = E.rowPlan.n, ls = M + 1;
+  CompF32 *sc = reinterpret_cast<CompF32 *>(smem);
+  int *boxes = reinterpret_cast<int *>(sc + kMaxComponents);
+  int *npar = boxes + 2 * kMaxComponents;
+  int *ss = npar + kMaxComponents;
+  cplx<float> *bufA = reinterpret_cast<cplx<float> *>(ss + kMaxParams);
+  cplx<float> *bufB = bufA + nD * ls;
+  const int nC = a.nComp;
+  for (int i = threadIdx.x; i < nC; i += blockDim.x) {
+    sc[i] = a.comps[k * nC + i];
+    const int *o = a.subBox + ((long)k * nC + i) * 4;
+    boxes[2 * i] = o[0];
+    boxes[2 * i + 1] = o[1];
+    npar[i] = a.desc[i].nParams;
+  }
+  for (int i = threadIdx.x; i < a.nParams; i += blockDim.x) ss[i] = slot[i];
+  for (int i = threadIdx.x; i < nD * ls; i += blockDim.x) bufA[i] = {0.f, 0.f};
+  __syncthreads();
+  float *lines = reinterpret_cast<float *>(bufA);
+  const WinDesc w = rag_win(E, nullptr);
+  for (int c = 0; c < nC; c++) {
+    const CompF32 cc = sc[c];
+    if (!in_rows(cc.type)) continue;
+    int sl[7];
+    sl[0] = ss[cc.x0Index];
+    sl[1] = ss[cc.x0Index + 1];
+#pragma unroll
+    for (int q = 0; q < 5; q++) sl[2 + q] = q < npar[c] ? ss[cc.paramOffset + q] : -1;
+    const float *tab = a.subTab + sub_base(a, k, c, 0);
+    const int bc0 = boxes[2 * c], br0 = boxes[2 * c + 1], side = a.boxMain;
+    switch (cc.type) {
+      case F_SERSIC: deriv_pixels<F_SERSIC>(cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
+      case F_EXP: deriv_pixels<F_EXP>(cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
+      case F_GRING: deriv_pixels<F_GRING>(cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
+      case F_MOFFAT: deriv_pixels<F_MOFFAT>(cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
+      case F_GAUSS: deriv_pixels<F_GAUSS>(cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
+      case F_TILTEDSKY: deriv_pixels<F_TILTEDSKY>(cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
+      default: break;
+    }
+  }
+  __syncthreads();
+  cplx<float> *Z = block_fft(bufA, bufB, E.rowPlan, nD, ls, 1, -1, false);
+  pdl_trigger();
+  cplx<float> *out = r.spec + (long)nD * E.specOff + (long)row * E.pitch;
+  const FastDiv byM1(M + 1);
+  for (int idx = threadIdx.x; idx < nD * (M + 1); idx += blockDim.x) {
+    const int j = byM1.div(idx), kk = idx - j * (M + 1);
+    out[(long)j * E.specSize + kk] = r2c_post(Z + j * ls, kk, M, E.twL);
+  }
+}
+
+// One data row of one cutout per CTA: inverse FFTs of the nD convolved
+// derivative rows, the Jacobian rows u_j = q dM/dtheta_j of the deviates and
+// the row's FP32 partial sums of alpha_jk (j <= k), beta_j and S.
+__global__ void __launch_bounds__(512) k_rag_jtwj_rows(FastArgs a, RagArgs r, const int *__restrict__ slot, int nD) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  pdl_wait();
+  const int t = blockIdx.x;
+  const int k = rag_slot(r.start, r.K, t);
+  const RagEntry &E = r.ent[r.act[k]];
+  const int row = t - r.start[k];
+  const int M = E.rowPlan.n, ls = M + 1, nP = a.nParams, nc = E.nDataCols;
+  int *ss = reinterpret_cast<int *>(smem);
+  cplx<float> *bufA = reinterpret_cast<cplx<float> *>(ss + kMaxParams);
+  cplx<float> *bufB = bufA + nD * ls;
+  float *U = reinterpret_cast<float *>(bufB + nD * ls);  // nD + 3 rows of nc floats
+  float *red = U + (long)(nD + 3) * nc;                  // blockDim.x floats
+  for (int i = threadIdx.x; i < nP; i += blockDim.x) ss[i] = slot[i];
+  const cplx<float> *src = r.spec + (long)nD * E.specOff + (long)row * E.pitch;
+  const FastDiv byM(M);
+  for (int idx = threadIdx.x; idx < nD * M; idx += blockDim.x) {
+    const int j = byM.div(idx), kk = idx - j * M;
+    bufA[j * ls + kk] = c2r_pre(src + (long)j * E.specSize, kk, M, E.twL);
+  }
+  __syncthreads();
+  const cplx<float> *Z = block_fft(bufA, bufB, E.rowPlan, nD, ls, 1, +1, false);
+  const float *Zr = reinterpret_cast<const float *>(Z);
+  float *qb = U + (long)nD * nc, *cd = qb + nc, *dv = cd + nc;
+  for (int col = threadIdx.x; col < nc; col += blockDim.x) {
+    const long z = E.dataOff + (long)row * nc + col;
+    const float m = r.model[z];
+    float dev, q;
+    deviate_slope(a, z, m, dev, q);
+    for (int j = 0; j < nD; j++) U[(long)j * nc + col] = q * Zr[2 * j * ls + col];
+    qb[col] = q * a.psfSum;
+    cd[col] = dev;
+    dv[col] = dev;
+  }
+  __syncthreads();
+  pdl_trigger();
+  const int nPair = nP * (nP + 1) / 2, Q = nPair + nP + 1;
+  const int T = blockDim.x;
+  int nseg = T / Q;
+  nseg = nseg < 1 ? 1 : (nseg > 32 ? 32 : nseg);
+  const int perRound = T / nseg;
+  const int myQ = threadIdx.x / nseg, seg = threadIdx.x - myQ * nseg;
+  for (int q0 = 0; q0 < Q; q0 += perRound) {
+    const int qi = q0 + myQ;
+    float acc = 0.f;
+    if (myQ < perRound && qi < Q) {
+      const float *X, *Y;
+      if (qi < nPair) {
+        int j = 0, rr = qi;
+        while (rr >= nP - j) {
+          rr -= nP - j;
+          j++;
+        }
+        const int kk = j + rr;
+        X = ss[j] >= 0 ? U + (long)ss[j] * nc : qb;
+        Y = ss[kk] >= 0 ? U + (long)ss[kk] * nc : qb;
+      } else if (qi < nPair + nP) {
+        const int j = qi - nPair;
+        X = ss[j] >= 0 ? U + (long)ss[j] * nc : qb;
+        Y = cd;
+      } else {
+        X = cd;
+        Y = dv;
+      }
+      for (int col = seg; col < nc; col += nseg) acc += X[col] * Y[col];
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    if (threadIdx.x < perRound && q0 + threadIdx.x < Q) {
+      float tt = 0.f;
+      for (int i = 0; i < nseg; i++) tt += red[threadIdx.x * nseg + i];
+      r.part[(long)(q0 + threadIdx.x) * r.totalRows + E.rowOff + row] = tt;
+    }
+    __syncthreads();
+  }
+}
+
+// FP64 sums over each cutout's row partials: grid (quantity, slot).
+__global__ void __launch_bounds__(256) k_rag_jtwj_reduce(FastArgs a, RagArgs r, double *__restrict__ alpha,
+                                                        double *__restrict__ beta, double *__restrict__ stat) {
+  pdl_wait();
+  const int qi = blockIdx.x, k = blockIdx.y, nP = a.nParams;
+  const int nPair = nP * (nP + 1) / 2;
+  const RagEntry &E = r.ent[r.act[k]];
+  const float *p = r.part + (long)qi * r.totalRows + E.rowOff;
+  double t = 0.0;
+  for (int i = threadIdx.x; i < E.nDataRows; i += blockDim.x) t += (double)p[i];
+  t = block_sum_d(t);
+  if (threadIdx.x != 0) return;
+  if (qi < nPair) {
+    int j = 0, rr = qi;
+    while (rr >= nP - j) {
+      rr -= nP - j;
+      j++;
+    }
+    const int kk = j + rr;
+    alpha[((long)k * nP + j) * nP + kk] = t;
+    alpha[((long)k * nP + kk) * nP + j] = t;
+  } else if (qi < nPair + nP) {
+    beta[(long)k * nP + (qi - nPair)] = t;
+  } else {
+    stat[k] = t;
+  }
+}
+
+static size_t rag_eval_smem(int maxM) {
+  return sizeof(CompF32) * kMaxComponents + sizeof(int) * 2 * kMaxComponents + sizeof(cplx<float>) * 2 * (maxM + 1) +
+         16;
+}
+
+constexpr int kRagRowThreads = 128;
+constexpr int kRagJtwjThreads = 256;
+
+size_t rag_jtwj_smem(int maxM, int nD, int maxCols) {
+  const size_t deriv = sizeof(CompF32) * kMaxComponents + sizeof(int) * (3 * kMaxComponents + kMaxParams) +
+                       sizeof(cplx<float>) * 2 * (size_t)nD * (maxM + 1) + 16;
+  const size_t rows = sizeof(int) * kMaxParams + sizeof(cplx<float>) * 2 * (size_t)nD * (maxM + 1) +
+                      sizeof(float) * ((size_t)(nD + 3) * maxCols + kRagJtwjThreads) + 16;
+  return std::max(deriv, rows);
+}
+
+// The whole ragged J^T W J evaluation: forward model (set-up + subsample,
+// window rows + row FFT, column pass x PSF, inverse rows -> model images),
+// derivative images (window rows, column pass x PSF), the per-row products
+// and their FP64 sums per cutout.  r.spec holds the forward spectra, dspec the
+// derivative spectra; starts/totals are the slots' prefix sums and totals per
+// kind of work.
+cudaError_t rag_jtwj(const FastArgs &a, RagArgs r, cplx<float> *dspec, const int *const starts[kRagWorkKinds],
+                     const int totals[kRagWorkKinds], const int *slot, int nD, int maxM, int maxLy, int maxCols,
+                     double *alpha, double *beta, double *stat, cudaStream_t st) {
+  const int K = r.K;
+  if (K <= 0) return cudaSuccess;
+  cudaError_t e;
+  // set-up + subsample tables: about 8 CTAs per SM over all slots and components
+  const int cap = std::max(1, 8 * 152 / std::max(a.nComp * K, 1));
+  const int nSub = std::max(1, std::min((a.boxMain * a.boxMain + 7) / 8, cap));
+  if ((e = launch_pdl(k_rag_subsample, dim3(nSub, a.nComp, K), dim3(256), 0, st, a, r))) return e;
+  r.start = starts[kRagWinRows];
+  allow_max_smem((const void *)k_rag_eval_r2c);
+  if ((e = launch_pdl(k_rag_eval_r2c, dim3(totals[kRagWinRows]), dim3(kRagRowThreads), rag_eval_smem(maxM), st, a,
+                      r)))
+    return e;
+  r.start = starts[kRagCols];
+  r.lines = 1;
+  if ((e = launch_rag_cols(r, totals[kRagCols], maxLy, st))) return e;
+  r.start = starts[kRagDataRows];
+  allow_max_smem((const void *)k_rag_model_rows);
+  if ((e = launch_pdl(k_rag_model_rows, dim3(totals[kRagDataRows]), dim3(kRagRowThreads),
+                      sizeof(cplx<float>) * 3 * (maxM + 1), st, a, r)))
+    return e;
+  const size_t smJ = rag_jtwj_smem(maxM, nD, maxCols);
+  RagArgs rd = r;
+  rd.spec = dspec;
+  if (nD > 0) {
+    rd.start = starts[kRagWinRows];
+    allow_max_smem((const void *)k_rag_deriv_r2c);
+    if ((e = launch_pdl(k_rag_deriv_r2c, dim3(totals[kRagWinRows]), dim3(kRagJtwjThreads), smJ, st, a, rd, slot,
+                        nD)))
+      return e;
+    rd.start = starts[kRagDerivCols];
+    rd.lines = nD;
+    if ((e = launch_rag_cols(rd, totals[kRagDerivCols], maxLy, st))) return e;
+  }
+  rd.start = starts[kRagDataRows];
+  allow_max_smem((const void *)k_rag_jtwj_rows);
+  if ((e = launch_pdl(k_rag_jtwj_rows, dim3(totals[kRagDataRows]), dim3(kRagJtwjThreads), smJ, st, a, rd, slot, nD)))
+    return e;
+  const int nP = a.nParams, Q = nP * (nP + 1) / 2 + nP + 1;
+  return launch_pdl(k_rag_jtwj_reduce, dim3(Q, K), dim3(256), 0, st, a, rd, alpha, beta, stat);
+}
+
 void fast_prepare_kernels() {
   cols32_prepare_kernels();
   allow_max_smem((const void *)k_fast_eval_r2c);

@@ -5,6 +5,7 @@
 #include <cstdint>
 #include <utility>
 #include "common.cuh"
+#include "fft.cuh"
 #include "psf_interp.cuh"
 
 namespace imfit {
@@ -324,6 +325,65 @@ struct JtwjArgs {
 };
 
 cudaError_t fast_jtwj(const FastPlan &p, const FastArgs &a, const JtwjArgs &J, int nBatch, cudaStream_t st);
+
+// ------------------------------------------------------- ragged cutout sets
+// Many cutouts of different sizes fitted with one model in one handle: each
+// cutout keeps its own size, PSF and FFT plan (no padding to a common size),
+// and every stage of an evaluation is ONE launch over all active cutouts --
+// a flat grid whose CTA t serves the slot k with start[k] <= t < start[k+1]
+// (binary search over the prefix sums of the slots' work counts).
+struct RagEntry {
+  int nDataCols, nDataRows;  // the cutout
+  int winCols, winRows;      // window W = N + P - 1
+  int xOrig, yOrig;          // IRAF coordinate of window pixel (0,0)
+  int Lx, Ly;                // padded FFT lengths (7-smooth, even)
+  int pitch;                 // complex pitch of its half spectrum (even)
+  int colGroups;             // column groups of its column pass
+  long specOff;              // complex offset of its spectrum (specSize values)
+  long specSize;             // Ly * pitch
+  long dataOff;              // offset of its data / weight / model pixels
+  long hOff;                 // complex offset of its PSF spectrum
+  long rowOff;               // offset of its data rows in the per-row partials
+  FFTPlan<float> rowPlan;    // Lx/2-point complex transform (rows)
+  FFTPlan<float> colPlan;    // Ly-point transform (columns)
+  const cplx<float> *twL;    // Lx split twiddles
+};
+
+struct RagArgs {
+  const RagEntry *ent;     // [entries]
+  const int *act;          // [K] entry of slot k
+  const int *start;        // [K + 1] prefix sums of the launch's work count per slot
+  int K;
+  int lines;               // column pass: spectra per entry (1, or nD derivative spectra)
+  cplx<float> *spec;       // spectra (forward: specOff; derivatives: nD * specOff + j * specSize)
+  const cplx<float> *H;    // PSF spectra (hOff)
+  float *model;            // FP32 model images (dataOff)
+  float *part;             // per-row partials [Q][totalRows] (rowOff)
+  long totalRows;
+};
+
+// slot of CTA t: the largest k with start[k] <= t (start[0] = 0)
+__device__ __forceinline__ int rag_slot(const int *start, int K, int t) {
+  int lo = 0, hi = K - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (start[mid] <= t)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+// work counts per slot of each ragged stage
+enum RagWork { kRagWinRows = 0, kRagDataRows = 1, kRagCols = 2, kRagDerivCols = 3, kRagWorkKinds = 4 };
+
+cudaError_t rag_jtwj(const FastArgs &a, RagArgs r, cplx<float> *dspec, const int *const starts[kRagWorkKinds],
+                     const int totals[kRagWorkKinds], const int *slot, int nD, int maxM, int maxLy, int maxCols,
+                     double *alpha, double *beta, double *stat, cudaStream_t st);
+// shared memory of the ragged derivative and row-product kernels
+size_t rag_jtwj_smem(int maxM, int nD, int maxCols);
+cudaError_t launch_rag_cols(const RagArgs &r, int total, int maxLy, cudaStream_t st);
 size_t fast_jtwj_smem(const FastPlan &p, int nD);
 cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool wantGrad, cudaStream_t st);
 // one-time kernel attribute set-up (call before any stream capture)

@@ -30,7 +30,9 @@
 #include "lm.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <thread>
 #include <vector>
 
 namespace imfit {
@@ -429,6 +431,27 @@ int settle(TrState &q, int n, double *x, const double *t, double St, const doubl
 
 }  // namespace
 
+// f(i) for i in [0, n) on up to 16 host threads (the problems of a batch are
+// independent: each step and acceptance touches only problem i's state);
+// serial for small batches.
+template <typename F>
+static void parallel_for(int n, const F &f) {
+  const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+  const int nt = std::min(std::min(hw, 16), (n + 31) / 32);
+  if (nt <= 1) {
+    for (int i = 0; i < n; i++) f(i);
+    return;
+  }
+  std::atomic<int> next(0);
+  std::vector<std::thread> pool;
+  pool.reserve(nt);
+  for (int t = 0; t < nt; t++)
+    pool.emplace_back([&]() {
+      for (int i = next.fetch_add(1); i < n; i = next.fetch_add(1)) f(i);
+    });
+  for (auto &th : pool) th.join();
+}
+
 int lm_minimize_batch(int B, int n, double *X, const int *fixed, const double *lower, const double *upper,
                       const LMSettings &set, const JtwjBatchEval &eval, LMResult *res) {
   auto limits = [&](int i) {
@@ -464,36 +487,34 @@ int lm_minimize_batch(int B, int n, double *X, const int *fixed, const double *l
   // trial costs a round but no iteration (as mpfit's inner loop)
   const long maxRounds = 20L * set.maxIter + 100;
   for (long round = 0; round < maxRounds; round++) {
-    bool any = false;
-    for (int i = 0; i < B; i++) {
+    parallel_for(B, [&](int i) {
       TrState &q = ps[i];
       double *t = T.data() + (size_t)i * n;
       const double *x = X + (size_t)i * n;
       if (q.done) {
         for (int j = 0; j < n; j++) t[j] = x[j];
-        continue;
+        return;
       }
       const int s = propose(q, n, x, t, freeIdx, limits(i), set);
-      if (q.done) {
-        res[i].status = s;
-        continue;
-      }
-      any = true;
-    }
+      if (q.done) res[i].status = s;
+    });
+    bool any = false;
+    for (int i = 0; i < B; i++)
+      if (!ps[i].done) any = true;
     if (!any) break;
     for (int i = 0; i < B; i++) live[i] = ps[i].done ? 0 : 1;
     st = eval(T.data(), live.data(), S.data(), A.data(), b.data());
     if (st) return st;
-    for (int i = 0; i < B; i++) {
+    parallel_for(B, [&](int i) {
       TrState &q = ps[i];
-      if (q.done) continue;
+      if (q.done || !live[i]) return;
       res[i].nEval++;
       const int s = settle(q, n, X + (size_t)i * n, T.data() + (size_t)i * n, S[i], A.data() + (size_t)i * n * n,
                            b.data() + (size_t)i * n, set);
       res[i].stat = q.S;
       res[i].nIter = q.accepted + 1;
       if (q.done) res[i].status = s;
-    }
+    });
   }
   for (int i = 0; i < B; i++)
     if (!ps[i].done) res[i].status = 5;

@@ -303,6 +303,27 @@ struct imfit_model_s {
     return k;
   }
   // forward-mode JtWJ state: derivative slot per parameter (-1: background)
+  // ragged cutout set (imfit_SetupCutouts): every cutout its own size, PSF and
+  // FFT plan; evaluations are one launch per stage over the active cutouts
+  struct RagSet {
+    int n = 0;
+    std::vector<RagEntry> ent;
+    std::map<int, std::unique_ptr<FFTLen>> lens;
+    long totalPix = 0, totalSpec = 0, totalRows = 0, totalH = 0;
+    int maxM = 0, maxLy = 0, maxCols = 0;
+    std::vector<int> work;  // act, then the prefix arrays, uploaded per evaluation
+    ~RagSet() {
+      for (auto &kv : lens) fftlen_destroy(*kv.second);
+    }
+  } rag;
+  DevBuf<RagEntry> dRagEnt;
+  DevBuf<float> dRagData, dRagW, dRagH, dRagModel, dRagPart, dRagSpec, dRagDSpec, dRagBg, dRagSubTab;
+  DevBuf<CompF32> dRagComps;
+  DevBuf<int> dRagSubBox, dRagWork, dRagSlot;
+  DevBuf<double> dRagParams, dRagS, dRagA, dRagB;
+  DevBuf<CompDesc> dRagDesc;
+  int ragNDeriv = 0;
+  std::vector<int> hRagSlot;
   std::vector<int> hSlot;
   int nDeriv = 0, jtwjCap = 0;
   DevBuf<int> dSlot;
@@ -1751,9 +1772,236 @@ struct imfit_model_s {
     return 0;
   }
 
+  // ---------------------------------------------------- ragged cutout sets
+  // nImg cutouts: cutout i has cols[i] x rows[i] pixels (data and sigma
+  // concatenated row-major, cutout after cutout) and a pcols[i] x prows[i]
+  // PSF (odd sizes, concatenated; normalised here with a Kahan sum).  Pixels
+  // with a non-finite value or sigma <= 0 are masked.  chi^2 with the given
+  // sigmas; the model's functions must be pixel functions (no 3-D or point
+  // sources) and the handle may hold no image of its own.
+  int setupCutouts(int nImg, const int *cols, const int *rows, const double *img, const double *sigma,
+                   const int *pcols, const int *prows, const double *psfs) {
+    if (!setsDefined) return fail(IMFIT_E_STATE, "DefineFunctionSets not called");
+    if (nImg < 1 || !cols || !rows || !img || !sigma || !pcols || !prows || !psfs)
+      return fail(IMFIT_E_ARG, "bad cutout-set arguments");
+    if (dataValsSet || stack.n || rag.n) return fail(IMFIT_E_STATE, "image data already added to this ModelObject");
+    if (!regions.empty() || useCash || doBootstrap) return fail(IMFIT_E_UNSUPPORTED, "cutout sets use chi^2 only");
+    for (auto &f : funcs)
+      if (is_los(f.type) || is_point_source(f.type))
+        return fail(IMFIT_E_UNSUPPORTED, "cutout sets take pixel functions only (no 3-D or point sources)");
+    if ((int)funcs.size() > kMaxComponents) return fail(IMFIT_E_UNSUPPORTED, "too many components");
+    RagSet &R = rag;
+    R.ent.assign(nImg, RagEntry{});
+    R.totalPix = R.totalSpec = R.totalRows = 0;
+    R.maxM = R.maxLy = R.maxCols = 0;
+    std::vector<long> psfOff(nImg);
+    long np = 0;
+    for (int i = 0; i < nImg; i++) {
+      const int nc = cols[i], nr = rows[i], pc = pcols[i], pr = prows[i];
+      if (nc < 1 || nr < 1 || pc < 1 || pr < 1 || !(pc & 1) || !(pr & 1))
+        return fail(IMFIT_E_ARG, "cutout sizes must be positive and PSF sizes odd");
+      psfOff[i] = np;
+      np += (long)pc * pr;
+      RagEntry &E = R.ent[i];
+      E.nDataCols = nc;
+      E.nDataRows = nr;
+      E.winCols = nc + pc - 1;
+      E.winRows = nr + pr - 1;
+      E.xOrig = 2 - pc + pc / 2;
+      E.yOrig = 2 - pr + pr / 2;
+      E.Lx = smooth_size(E.winCols, true);
+      E.Ly = smooth_size(E.winRows, true);
+      if (E.Lx / 2 > 4096 || E.Ly > 4096) return fail(IMFIT_E_UNSUPPORTED, "cutout too large for the fast path");
+      E.pitch = even_pitch(E.Lx);
+      E.colGroups = (E.Lx / 2 + 1 + 1) / 2;
+      E.specSize = (long)E.Ly * E.pitch;
+      E.specOff = R.totalSpec;
+      E.hOff = R.totalSpec;  // one PSF spectrum per cutout, same geometry
+      E.dataOff = R.totalPix;
+      E.rowOff = R.totalRows;
+      R.totalPix += (long)nc * nr;
+      R.totalSpec += E.specSize;
+      R.totalRows += nr;
+      R.maxM = std::max(R.maxM, E.Lx / 2);
+      R.maxLy = std::max(R.maxLy, E.Ly);
+      R.maxCols = std::max(R.maxCols, nc);
+    }
+    R.totalH = R.totalSpec;
+    // FFT tables per distinct length
+    auto table = [&](int L) -> FFTLen * {
+      auto it = R.lens.find(L);
+      if (it != R.lens.end()) return it->second.get();
+      std::unique_ptr<FFTLen> t(new FFTLen());
+      if (fftlen_create(*t, L)) return nullptr;
+      FFTLen *raw = t.get();
+      R.lens[L] = std::move(t);
+      return raw;
+    };
+    auto plan = [](const FFTTable &t) {
+      FFTPlan<float> p;
+      p.n = t.n;
+      p.npass = t.npass;
+      p.radix = pack_radix(t.radix, t.npass);
+      p.tw = reinterpret_cast<const cplx<float> *>(t.tw32);
+      return p;
+    };
+    // data, weights, PSF spectra
+    std::vector<float> d32(R.totalPix), w32(R.totalPix);
+    for (long z = 0; z < R.totalPix; z++) {
+      const double d = img[z], sg = sigma[z];
+      const bool good = std::isfinite(d) && std::isfinite(sg) && sg > 0.0;
+      d32[z] = good ? (float)d : 0.f;
+      w32[z] = good ? (float)(1.0 / sg) : 0.f;
+    }
+    cudaError_t e = dRagData.reserve(R.totalPix);
+    if (!e) e = dRagW.reserve(R.totalPix);
+    if (!e) e = cudaMemcpy(dRagData.p, d32.data(), sizeof(float) * R.totalPix, cudaMemcpyHostToDevice);
+    if (!e) e = cudaMemcpy(dRagW.p, w32.data(), sizeof(float) * R.totalPix, cudaMemcpyHostToDevice);
+    if (!e) e = dRagH.reserve(2 * (size_t)R.totalH);
+    if (e) return cuda_fail(e, "cutout-set buffers");
+    for (int i = 0; i < nImg; i++) {
+      RagEntry &E = R.ent[i];
+      const int pc = pcols[i], pr = prows[i];
+      std::vector<double> q(psfs + psfOff[i], psfs + psfOff[i] + (long)pc * pr);
+      for (double v : q)
+        if (!std::isfinite(v)) return fail(IMFIT_E_ARG, "PSF image has one or more non-finite values");
+      const double ks = kahan_sum(q.data(), (long)q.size());
+      if (!(ks > 0.0)) return fail(IMFIT_E_ARG, "Sum of PSF pixel values is <= 0 -- PSF cannot be normalized");
+      for (double &v : q) v = v / ks;
+      FFTLen *fx = table(E.Lx), *fy = table(E.Ly);
+      if (!fx || !fy) return fail(IMFIT_E_CUDA, "FFT tables");
+      int st = shiftedSpectrum32To(q.data(), pc, pr, *fx, *fy, dRagH.p + 2 * E.hOff);
+      if (st) return st;
+      E.rowPlan = plan(fx->half);
+      E.colPlan = plan(fy->full);
+      E.twL = reinterpret_cast<const cplx<float> *>(fx->twL32);
+    }
+    e = dRagEnt.reserve(nImg);
+    if (!e) e = cudaMemcpy(dRagEnt.p, R.ent.data(), sizeof(RagEntry) * nImg, cudaMemcpyHostToDevice);
+    // component descriptors and derivative slots (every parameter but constant backgrounds)
+    std::vector<CompDesc> desc(funcs.size());
+    for (size_t f = 0; f < funcs.size(); f++) {
+      CompDesc &dd = desc[f];
+      dd = CompDesc{};
+      dd.type = funcs[f].type;
+      dd.subsample = funcs[f].subsample;
+      dd.paramOffset = paramOffset[f];
+      dd.x0Index = x0Index[f];
+      dd.nParams = funcs[f].nParams;
+      dd.background = (funcs[f].type == F_FLATSKY) ? 1 : 0;
+    }
+    hRagSlot.assign(nParamsTot, 0);
+    for (auto &dd : desc)
+      if (dd.background) hRagSlot[dd.paramOffset] = -1;
+    ragNDeriv = 0;
+    for (int j = 0; j < nParamsTot; j++)
+      if (hRagSlot[j] >= 0) hRagSlot[j] = ragNDeriv++;
+    if (!e) e = dRagDesc.reserve(desc.size());
+    if (!e) e = cudaMemcpy(dRagDesc.p, desc.data(), sizeof(CompDesc) * desc.size(), cudaMemcpyHostToDevice);
+    if (!e) e = dRagSlot.reserve(std::max(nParamsTot, 1));
+    if (!e) e = cudaMemcpy(dRagSlot.p, hRagSlot.data(), sizeof(int) * nParamsTot, cudaMemcpyHostToDevice);
+    // evaluation buffers, sized for all cutouts active
+    const int nP = nParamsTot, nC = (int)funcs.size(), Q = nP * (nP + 1) / 2 + nP + 1;
+    if (!e) e = dRagSpec.reserve(2 * (size_t)R.totalSpec);
+    if (!e && ragNDeriv) e = dRagDSpec.reserve(2 * (size_t)ragNDeriv * R.totalSpec);
+    if (!e) e = dRagModel.reserve(R.totalPix);
+    if (!e) e = dRagPart.reserve((size_t)Q * R.totalRows);
+    if (!e) e = dRagParams.reserve((size_t)nImg * nP);
+    if (!e) e = dRagS.reserve(nImg);
+    if (!e) e = dRagA.reserve((size_t)nImg * nP * nP);
+    if (!e) e = dRagB.reserve((size_t)nImg * nP);
+    if (!e) e = dRagComps.reserve((size_t)nImg * nC);
+    if (!e) e = dRagBg.reserve(2 * (size_t)nImg);
+    if (!e) e = dRagSubTab.reserve((size_t)nImg * nC * kBoxMain * kBoxMain * 8);
+    if (!e) e = dRagSubBox.reserve((size_t)nImg * nC * 4);
+    if (!e) e = dRagWork.reserve((size_t)(kRagWorkKinds + 1) * (nImg + 1));
+    if (e) return cuda_fail(e, "cutout-set buffers");
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    if (rag_jtwj_smem(R.maxM, ragNDeriv, R.maxCols) > (size_t)optin)
+      return fail(IMFIT_E_UNSUPPORTED, "cutout set: the largest cutout needs more shared memory than a CTA has");
+    R.n = nImg;
+    nValid = R.totalPix;
+    finalSetupDone = true;
+    return 0;
+  }
+
+  // statistic, J^T J and J^T dev of the cutouts entries[0..K) at params (K x nP, host)
+  int ragJtwjHost(int K, const int *entries, const double *params, double *stats, double *alpha, double *beta) {
+    if (!rag.n) return fail(IMFIT_E_STATE, "no cutout set (imfit_SetupCutouts)");
+    if (K < 1 || K > rag.n || !entries || !params || !stats || !alpha || !beta)
+      return fail(IMFIT_E_ARG, "bad cutout-set J^T J arguments");
+    RagSet &R = rag;
+    const int nP = nParamsTot;
+    // work lists: act, then per kind the prefix sums of the slots' counts
+    std::vector<int> &w = R.work;
+    w.assign((size_t)(kRagWorkKinds + 1) * (K + 1), 0);
+    int *act = w.data();
+    int *pre[kRagWorkKinds];
+    for (int t = 0; t < kRagWorkKinds; t++) pre[t] = w.data() + (size_t)(t + 1) * (K + 1);
+    for (int k = 0; k < K; k++) {
+      const int en = entries[k];
+      if (en < 0 || en >= R.n) return fail(IMFIT_E_ARG, "cutout index out of range");
+      act[k] = en;
+      const RagEntry &E = R.ent[en];
+      pre[kRagWinRows][k + 1] = pre[kRagWinRows][k] + E.winRows;
+      pre[kRagDataRows][k + 1] = pre[kRagDataRows][k] + E.nDataRows;
+      pre[kRagCols][k + 1] = pre[kRagCols][k] + E.colGroups;
+      pre[kRagDerivCols][k + 1] = pre[kRagDerivCols][k] + E.colGroups * ragNDeriv;
+    }
+    cudaError_t e = cudaMemcpyAsync(dRagWork.p, w.data(), sizeof(int) * w.size(), cudaMemcpyHostToDevice, stream);
+    if (!e)
+      e = cudaMemcpyAsync(dRagParams.p, params, sizeof(double) * (size_t)K * nP, cudaMemcpyHostToDevice, stream);
+    if (e) return cuda_fail(e, "cutout-set upload");
+    FastArgs a{};
+    a.desc = dRagDesc.p;
+    a.nComp = (int)funcs.size();
+    a.nParams = nP;
+    a.params = dRagParams.p;
+    a.comps = dRagComps.p;
+    a.bgLevel = dRagBg.p;
+    a.data = dRagData.p;
+    a.weight = dRagW.p;
+    a.kind = 0;
+    a.effGain = 1.f;
+    a.psfSum = 1.f;
+    a.psfSumOs = 1.f;
+    a.subTab = dRagSubTab.p;
+    a.subBox = dRagSubBox.p;
+    a.boxMain = kBoxMain;
+    a.boxReg = 0;
+    RagArgs r{};
+    r.ent = dRagEnt.p;
+    r.act = dRagWork.p;
+    r.K = K;
+    r.lines = 1;
+    r.spec = reinterpret_cast<cplx<float> *>(dRagSpec.p);
+    r.H = reinterpret_cast<const cplx<float> *>(dRagH.p);
+    r.model = dRagModel.p;
+    r.part = dRagPart.p;
+    r.totalRows = R.totalRows;
+    const int *starts[kRagWorkKinds];
+    int totals[kRagWorkKinds];
+    for (int t = 0; t < kRagWorkKinds; t++) {
+      starts[t] = dRagWork.p + (size_t)(t + 1) * (K + 1);
+      totals[t] = pre[t][K];
+    }
+    r.start = starts[kRagWinRows];
+    e = rag_jtwj(a, r, reinterpret_cast<cplx<float> *>(dRagDSpec.p), starts, totals, dRagSlot.p, ragNDeriv, R.maxM,
+                 R.maxLy, R.maxCols, dRagA.p, dRagB.p, dRagS.p, stream);
+    if (e) return cuda_fail(e, "cutout-set J^T J launch");
+    e = cudaMemcpyAsync(stats, dRagS.p, sizeof(double) * K, cudaMemcpyDeviceToHost, stream);
+    if (!e) e = cudaMemcpyAsync(alpha, dRagA.p, sizeof(double) * (size_t)K * nP * nP, cudaMemcpyDeviceToHost, stream);
+    if (!e) e = cudaMemcpyAsync(beta, dRagB.p, sizeof(double) * (size_t)K * nP, cudaMemcpyDeviceToHost, stream);
+    if (!e) e = cudaStreamSynchronize(stream);
+    if (e) return cuda_fail(e, "cutout-set J^T J results");
+    return 0;
+  }
+
   int fitLMBatch(int B, double *params, const int *fixed, const double *lower, const double *upper, double ftol,
                  int maxIter, double *stats, int *nIter, int *status) {
     const int n = nParamsTot;
+    if (rag.n && B != rag.n) return fail(IMFIT_E_ARG, "a cutout set fits exactly one parameter vector per cutout");
     LMSettings set;
     set.ftol = ftol;
     if (maxIter > 0) set.maxIter = maxIter;
@@ -1768,6 +2016,23 @@ struct imfit_model_s {
         if (act[i]) idx.push_back(i);
       const int k = (int)idx.size();
       if (k == 0) return 0;
+      if (rag.n) {  // cutout set: one launch per stage over the active cutouts
+        Xs.resize((size_t)k * n);
+        Ss.resize(k);
+        As.resize((size_t)k * n * n);
+        Bs.resize((size_t)k * n);
+        for (int r = 0; r < k; r++)
+          std::copy(X + (size_t)idx[r] * n, X + (size_t)(idx[r] + 1) * n, Xs.begin() + (size_t)r * n);
+        int st = ragJtwjHost(k, idx.data(), Xs.data(), Ss.data(), As.data(), Bs.data());
+        if (st) return st;
+        for (int r = 0; r < k; r++) {
+          const int i = idx[r];
+          S[i] = Ss[r];
+          std::copy(As.begin() + (size_t)r * n * n, As.begin() + (size_t)(r + 1) * n * n, A + (size_t)i * n * n);
+          std::copy(Bs.begin() + (size_t)r * n, Bs.begin() + (size_t)(r + 1) * n, b + (size_t)i * n);
+        }
+        return 0;
+      }
       if (k == B) return jtwjHost(B, X, S, A, b);
       Xs.resize((size_t)k * n);
       Ss.resize(k);
@@ -2380,6 +2645,18 @@ int imfit_FitLMBatch(imfit_model_t m, int B, double *params, const int *fixed, c
   if (B < 1 || !params) return m->fail(IMFIT_E_ARG, "bad batch arguments");
   if (!(ftol > 0.0)) return m->fail(IMFIT_E_ARG, "ftol must be positive");
   return m->fitLMBatch(B, params, fixed, lower, upper, ftol, maxIter, stats, nIter, status);
+}
+
+int imfit_SetupCutouts(imfit_model_t m, int nImg, const int *cols, const int *rows, const double *pix,
+                       const double *sig, const int *psfCols, const int *psfRows, const double *psfs) {
+  GET(m);
+  return m->setupCutouts(nImg, cols, rows, pix, sig, psfCols, psfRows, psfs);
+}
+
+int imfit_CutoutsJtWJ(imfit_model_t m, int K, const int *cutouts, const double *params, double *stats,
+                      double *jtj, double *jtdev) {
+  GET(m);
+  return m->ragJtwjHost(K, cutouts, params, stats, jtj, jtdev);
 }
 
 int imfit_SetupImageStack(imfit_model_t m, int nImg, int nc, int nr, const double *pix, const double *sig,

@@ -1,6 +1,11 @@
 """Fitting many cutouts of uneven sizes with one model on the GPU.
 
-Cutouts are grouped into size buckets; each bucket becomes one image stack
+Default ("set"): all cutouts go into ONE handle as a cutout set
+(``ModelObject.setup_cutouts``): each cutout keeps its own size, PSF and FFT
+plan, and every stage of each Levenberg-Marquardt round is one kernel launch
+over all cutouts still being fitted (``fit_lm_batch``).
+
+Alternative ("buckets"): cutouts are grouped into size buckets; each bucket becomes one image stack
 (``ModelObject.setup_image_stack``): every cutout is padded to the bucket's
 size with masked pixels (sigma 0) at the bottom and right, so its pixel
 coordinates are unchanged, and its PSF is padded with zeros around its centre
@@ -71,12 +76,29 @@ def build_stack(functions, cutouts, key, device=0, autotune=False):
     return m
 
 
-class CutoutFitter:
-    """Bucketed image stacks for a list of cutouts (set up once, fitted many times)."""
+def build_set(functions, cutouts, device=0):
+    """ModelObject holding every cutout as one cutout set (each at its own size)."""
+    m = imfit_gb300.ModelObject(device)
+    for name, new_set in functions:
+        m.add_function(name, new_set)
+    m.finish_functions()
+    m.setup_cutouts([c.data for c in cutouts], [c.sigma for c in cutouts], [c.psf for c in cutouts])
+    return m
 
-    def __init__(self, functions, cutouts, device=0, threads=8):
+
+class CutoutFitter:
+    """The cutouts of a list set up once and fitted many times: one cutout set
+    (mode "set", default) or size buckets of image stacks fitted from host
+    threads (mode "buckets")."""
+
+    def __init__(self, functions, cutouts, device=0, threads=8, mode="set"):
         self.functions = functions
         self.n = len(cutouts)
+        self.mode = mode
+        if mode == "set":
+            self.model = build_set(functions, cutouts, device)
+            self.buckets = []
+            return
         groups = {}
         for i, c in enumerate(cutouts):
             groups.setdefault(bucket_of(c), []).append(i)
@@ -95,6 +117,9 @@ class CutoutFitter:
     def fit(self, starts, lower=None, upper=None, fixed=None, ftol=1e-8, max_iter=0):
         """Fit every cutout from starts (n x nParams); returns dict of arrays in cutout order."""
         starts = np.asarray(starts, dtype=np.float64)
+        if self.mode == "set":
+            r = self.model.fit_lm_batch(starts, fixed=fixed, lower=lower, upper=upper, ftol=ftol, max_iter=max_iter)
+            return dict(params=r["params"], statistic=r["statistic"], niter=r["niter"], status=r["status"])
         out_p = np.empty_like(starts)
         out_s = np.empty(self.n)
         out_it = np.empty(self.n, dtype=int)

@@ -267,6 +267,26 @@ int imfit_BootstrapFitBatch(imfit_model_t m, int nSamples, const double *bestfit
  * The plain FP64 entry points are per image and reject a stack. */
 int imfit_SetupImageStack(imfit_model_t m, int nImages, int nColumns, int nRows, const double *pixels,
                           const double *sigmas, const double *psfs, int psfColumns, int psfRows);
+/* ---- cutout sets (fast path; no counterpart in the reference, which fits
+ * its images one after another, core/bootstrap_errors.cpp:205-215) ---------- */
+/* Many cutouts of DIFFERENT sizes fitted with one model in one handle, each
+ * at its own size with its own PSF and FFT plan (no padding to a common
+ * size).  Cutout i has columns[i] x rows[i] pixels; pixels and sigmas hold
+ * the cutouts one after another (row-major each); psfColumns[i] x psfRows[i]
+ * (odd) PSFs likewise in psfs, normalised as the reference's Convolver does.
+ * sigma <= 0 or non-finite, or non-finite data, masks a pixel.  chi^2 only;
+ * pixel functions only (no 3-D functions, point sources or oversampled
+ * regions).  Every stage of an evaluation is one kernel launch over all the
+ * cutouts being evaluated.  imfit_FitLMBatch then fits nImages vectors,
+ * vector i to cutout i (the active cutouts of each round in one launch per
+ * stage). */
+int imfit_SetupCutouts(imfit_model_t m, int nImages, const int *columns, const int *rows, const double *pixels,
+                       const double *sigmas, const int *psfColumns, const int *psfRows, const double *psfs);
+/* Statistic, J^T J (nParams x nParams) and J^T dev of the cutouts
+ * cutouts[0..K) at params (K x nParams), on the host; outputs K, K x nParams^2
+ * and K x nParams values in the same order. */
+int imfit_CutoutsJtWJ(imfit_model_t m, int K, const int *cutouts, const double *params, double *statistics,
+                      double *jtj, double *jtdev);
 int imfit_Synchronize(imfit_model_t m);
 /* The CUDA stream (cudaStream_t) all work of this handle is enqueued on. */
 int imfit_GetStream(imfit_model_t m, void **stream);

@@ -147,3 +147,71 @@ def test_cutout_fits_match_fp64_fits(gpu, oracle_mod):
         sigma = np.sqrt(np.diag(np.linalg.inv(A)))
         tol = np.maximum(1e-4 * np.abs(ref.x), 0.02 * sigma)
         assert np.all(np.abs(got - ref.x) <= tol), (i, list(zip(got, ref.x, sigma)))
+
+
+# ------------------------------------------------------------- cutout sets
+def _set(gpu, imgs):
+    from imfit_gb300 import cutouts, workloads
+    return cutouts.build_set(workloads.C5_FUNCTIONS, [cutouts.Cutout(*x) for x in imgs])
+
+
+def test_cutout_set_jtwj_equals_single_images(gpu, oracle_mod):
+    """Each cutout of a set at its own size: statistic vs the FP64 oracle 1e-5,
+    J^T J and J^T dev vs a single-image handle per cutout (same FP32
+    algorithm, same padded sizes) within 1e-4, for all cutouts and for a
+    subset in a different order (the slots of a compacted LM round)."""
+    items, imgs = _items(oracle_mod, count=6, max_side=96, seed=31)
+    m = _set(gpu, imgs)
+    P = np.array([it["start"] for it in items])
+    for order in (list(range(len(items))), [4, 1, 5]):
+        S, A, B = m.cutouts_jtwj(order, P[order])
+        for r, i in enumerate(order):
+            d, s, p = imgs[i]
+            assert relerr(S[r], _single(oracle_mod.OracleModel, d, s, p).get_fit_statistic(P[i])) < 1e-5
+            g = _single(gpu.ModelObject, d, s, p)
+            s1, a1, b1 = g.jtwj(P[i])
+            assert relerr(S[r], s1) < 1e-5
+            dd = np.sqrt(np.outer(np.diag(a1), np.diag(a1)))
+            assert np.all(np.abs(A[r] - a1) <= 1e-4 * dd), (i, np.max(np.abs(A[r] - a1) / dd))
+            assert np.all(np.abs(B[r] - b1) <= 1e-4 * (np.abs(b1) + 1e-3 * np.max(np.abs(b1))))
+
+
+def test_cutout_set_fits_match_single_fits(gpu, oracle_mod):
+    """The batched LM on a cutout set (one launch per stage per round) reaches
+    the single-image LM's chi^2 on every cutout (interior minima, 1e-7)."""
+    items, imgs = _items(oracle_mod, count=5, max_side=80, seed=99)
+    m = _set(gpu, imgs)
+    P = np.array([it["start"] for it in items])
+    lo = np.array([it["lower"] for it in items])
+    hi = np.array([it["upper"] for it in items])
+    rb = m.fit_lm_batch(P, lower=lo, upper=hi, ftol=1e-10)
+    assert np.all(rb["status"] > 0), rb["status"]
+    for i, (d, s, p) in enumerate(imgs):
+        g = _single(gpu.ModelObject, d, s, p)
+        r1 = g.fit_lm(P[i], lower=lo[i], upper=hi[i], ftol=1e-10)
+        c_set, c_single = g.get_fit_statistic(rb["params"][i]), g.get_fit_statistic(r1["params"])
+        pegged = [bool(np.any((x == lo[i]) | (x == hi[i]))) for x in (rb["params"][i], r1["params"])]
+        if any(pegged):
+            if not all(pegged):
+                inner, corner = (c_single, c_set) if pegged[0] else (c_set, c_single)
+                assert inner <= corner * (1 + 1e-6), (i, c_set, c_single)
+            continue
+        tol = 1e-7 if (rb["status"][i] == 1 and r1["status"] == 1) else 1e-3
+        assert relerr(c_set, c_single) < tol, (i, c_set, c_single, rb["status"][i], r1["status"])
+
+
+def test_cutout_set_rejects_what_it_does_not_take(gpu):
+    from imfit_gb300 import workloads
+    m = gpu.ModelObject()
+    m.add_function("Sersic", True)
+    m.finish_functions()
+    img = np.ones((20, 20))
+    with pytest.raises(gpu.ImfitError):
+        m.setup_cutouts([img], [1.0], [np.ones((4, 4))])  # even PSF
+    m2 = gpu.ModelObject()
+    for name, new_set in workloads.C5_FUNCTIONS:
+        m2.add_function(name, new_set)
+    m2.finish_functions()
+    m2.setup_cutouts([img, np.ones((30, 25))], [1.0, 2.0], [np.ones((5, 5)), np.ones((7, 7))])
+    with pytest.raises(gpu.ImfitError):
+        m2.fit_lm_batch(np.ones((3, m2.n_params)))  # one vector per cutout
