@@ -535,7 +535,7 @@ def multimfit(argv=None, out=sys.stdout):
         images = parse_image_info(f.read())
     stat = "cash" if args.cashstat else ("pmlr" if args.poisson_mlr else "chi2")
     handles = build_handles(cfg.functions, images, args.device, not args.nosubsampling, stat, args.model_errors)
-    mm = MultiImageModel(cfg.functions, handles)
+    mm = MultiImageModel(cfg.functions, handles, [im.local_functions for im in images])
     p0, lo, hi, fx = global_vector(cfg, images)
     off = section_offsets(cfg, images)  # image sections: X0/Y0 in the sections' pixel frames
     p0, lo, hi = p0 - off, lo - off, hi - off
@@ -568,6 +568,11 @@ def multimfit(argv=None, out=sys.stdout):
         out.write(f"# Image-description parameters for image {i + 1}\n")
         for j, name in enumerate(IMAGE_PARAM_NAMES):
             out.write(f"  {name:12s} {p[5 * (i - 1) + j]:.6f}\n")
+    for i, im in enumerate(images):
+        if im.local is not None:
+            out.write(f"# Per-image function parameters for image {i + 1}\n")
+            for name, v in zip(im.local.param_names, p[mm.local_slice(i)]):
+                out.write(f"  {name:8s} {v:.6f}\n")
     return p, s
 
 
@@ -593,7 +598,8 @@ def makemultimages(argv=None, out=sys.stdout):
     handles = []
     for im in images:
         m = ModelObject(args.device)
-        for name, new_set in cfg.functions:
+        # global functions, then the image's own (core/makemultimages_main.cpp:266-300)
+        for name, new_set in list(cfg.functions) + im.local_functions:
             m.add_function(name, new_set, subsampling=not args.nosubsampling)
         m.finish_functions()
         if im.psf:
@@ -605,7 +611,7 @@ def makemultimages(argv=None, out=sys.stdout):
             nr, nc = fitsio.read_image(im.data)[0].shape
         m.setup_model_image(nc, nr)
         handles.append(m)
-    mm = MultiImageModel(cfg.functions, handles)
+    mm = MultiImageModel(cfg.functions, handles, [im.local_functions for im in images])
     p, _, _, _ = global_vector(cfg, images)
     outs = []
     for i, m in enumerate(handles):

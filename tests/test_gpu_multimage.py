@@ -220,3 +220,157 @@ def test_multimfit_regression_runs(gpu, tmp_path, case):
     for k, t in enumerate(tol):
         if t is not None:
             assert abs(got[k] - printed[k]) <= t + 1e-6 * abs(printed[k]), (k, got, printed)
+
+
+PER_IMAGE_CFG = """GAIN 1
+X0 20.0 10,30
+Y0 21.0 10,30
+FUNCTION Gaussian
+PA 30 0,90
+ell 0.3 0,0.8
+I_0 200 50,500
+sigma 3.0 1,6
+"""
+PER_IMAGE_LOCAL = """FUNCTIONS_START
+X0 1 fixed
+Y0 1 fixed
+FUNCTION FlatSky
+I_sky 5.0 0,20
+X0 30.0 25,35
+Y0 10.0 5,15
+FUNCTION Gaussian
+PA 0 fixed
+ell 0 fixed
+I_0 80 20,200
+sigma 1.5 0.5,4
+"""
+# image 1: the global Gaussian alone; image 2: the Gaussian at its own X0/Y0
+# with FLUX_SCALE 1.5, plus its own sky and star
+PER_IMAGE_TRUTH = dict(global_=[20.0, 21.0, 30.0, 0.3, 200.0, 3.0], desc2=[1.0, 0.0, 1.5, 17.5, 23.0],
+                       local2=[1.0, 1.0, 5.0, 30.0, 10.0, 0.0, 0.0, 80.0, 1.5])
+
+
+def _per_image_setup(oracle_mod, shape=(40, 44)):
+    """Data of both images made by the FP64 oracle from hand-written per-image
+    vectors (global functions first, then image 2's own)."""
+    g, d2, l2 = PER_IMAGE_TRUTH["global_"], PER_IMAGE_TRUTH["desc2"], PER_IMAGE_TRUTH["local2"]
+    v1 = list(g)
+    v2 = [d2[3], d2[4], g[2], g[3], g[4] * d2[2], g[5]] + list(l2)
+    glob = [("Gaussian", True)]
+    local = [("FlatSky", True), ("Gaussian", True)]
+
+    def oracle_model(funcs, data=None):
+        m = oracle_mod.OracleModel()
+        for name, new_set in funcs:
+            m.add_function(name, new_set)
+        m.finish_functions()
+        if data is None:
+            m.setup_model_image(shape[1], shape[0])
+        else:
+            m.add_image_data(data)
+            m.add_image_characteristics(1.0, 0.0, 1.0, 1, 0.0)
+            m.add_error_vector(np.full(shape, 2.0), 100)
+            assert m.final_setup() == 0
+        return m
+
+    m1, m2 = oracle_model(glob), oracle_model(glob + local)
+    m1.create_model_image(np.array(v1))
+    m2.create_model_image(np.array(v2))
+    data = [m1.get_model_image().copy(), m2.get_model_image().copy()]
+    return data, (oracle_model(glob, data[0]), oracle_model(glob + local, data[1])), glob, local
+
+
+def test_multimfit_per_image_functions(gpu, oracle_mod, tmp_path):
+    """Per-image functions (a FUNCTIONS_START section in image 2's block):
+    the summed statistic at a perturbed vector equals the FP64 oracle's on
+    per-image vectors written by hand (global model transformed, image 2's
+    own functions appended unchanged, core/param_holder.cpp:215-270); the
+    fast gradient matches central differences of the statistic; LM on the
+    summed normal equations recovers the truth from noise-free data; the
+    command line fits the same files and prints the per-image block."""
+    from imfit_gb300 import cli, fits
+    from imfit_gb300.config import parse_config
+    from imfit_gb300.multimage import MultiImageModel, build_handles, global_vector, parse_image_info
+    data, (o1, o2), glob, local = _per_image_setup(oracle_mod)
+    for k, img in enumerate(data):
+        fits.write_image(str(tmp_path / f"im{k}.fits"), img)
+        fits.write_image(str(tmp_path / f"sig{k}.fits"), np.full(img.shape, 2.0))
+    (tmp_path / "c.dat").write_text(PER_IMAGE_CFG)
+    (tmp_path / "info.txt").write_text(f"""IMAGE_START
+DATA {tmp_path / 'im0.fits'}
+ERROR {tmp_path / 'sig0.fits'}
+IMAGE_START
+DATA {tmp_path / 'im1.fits'}
+ERROR {tmp_path / 'sig1.fits'}
+PIXEL_SCALE 1.0 fixed
+IMAGE_PA 0.0 fixed
+FLUX_SCALE 1.2 0.5,3
+X0 17.0 12,22
+Y0 22.0 18,28
+""" + PER_IMAGE_LOCAL)
+    cfg = parse_config(PER_IMAGE_CFG)
+    images = parse_image_info((tmp_path / "info.txt").read_text())
+    assert images[1].local_functions == local
+    mm = MultiImageModel(cfg.functions, build_handles(cfg.functions, images), [im.local_functions for im in images])
+    assert mm.n_local == [0, 9] and mm.n_params == 5 + 6 + 9
+    p0, lo, hi, fx = global_vector(cfg, images)
+    truth = np.array(PER_IMAGE_TRUTH["desc2"] + PER_IMAGE_TRUTH["global_"] + PER_IMAGE_TRUTH["local2"])
+    # statistic at a perturbed vector against the oracle on hand-written vectors
+    q = truth + np.where(fx == 0, 0.03 * np.abs(truth) + 0.05, 0.0)
+    gq = q[5:11]
+    v1 = gq
+    v2 = np.concatenate([[q[3], q[4], gq[2], gq[3], gq[4] * q[2], gq[5]], q[11:]])
+    want = o1.get_fit_statistic(v1) + o2.get_fit_statistic(v2)
+    s = mm.get_fit_statistic(q)
+    assert abs(s - want) <= 1e-10 * want, (s, want)
+    # fast gradient against central differences of the FP64 statistic
+    s_f, grad = mm.statistic_and_gradient(q)
+    assert abs(s_f - want) <= 1e-5 * want
+    fd = np.zeros(len(q))
+    for j in range(len(q)):
+        h = 1e-5 * max(abs(q[j]), 1.0)
+        a, b = q.copy(), q.copy()
+        a[j] += h
+        b[j] -= h
+        fd[j] = (mm.get_fit_statistic(a) - mm.get_fit_statistic(b)) / (2 * h)
+    free = fx == 0
+    scale = np.abs(fd[free]) + 1e-3 * np.max(np.abs(fd[free]))
+    assert np.all(np.abs(grad[free] - fd[free]) <= 2e-3 * scale), list(zip(grad[free], fd[free]))
+    # LM from the file's starting values
+    r = mm.fit_lm(p0, fixed=fx, lower=np.where(np.isnan(lo), 0.0, lo), upper=np.where(np.isnan(hi), 0.0, hi))
+    assert r["status"] > 0
+    assert np.all(np.abs(r["params"] - truth) <= 1e-3 * np.maximum(np.abs(truth), 1.0)), (r["params"], truth)
+    buf = io.StringIO()
+    p_cli, s_cli = cli.multimfit([str(tmp_path / "c.dat"), "-i", str(tmp_path / "info.txt")], out=buf)
+    assert len(p_cli) == mm.n_params and s_cli < 1e-6
+    assert "# Per-image function parameters for image 2" in buf.getvalue()
+    assert np.all(np.abs(p_cli - truth) <= 1e-3 * np.maximum(np.abs(truth), 1.0))
+
+
+def test_makemultimages_per_image_functions(gpu, oracle_mod, tmp_path):
+    """makemultimages adds an image's own functions after the global ones
+    (core/makemultimages_main.cpp:266-300): image 2's output is the oracle's
+    model of the global Gaussian moved and scaled plus its sky and star."""
+    from imfit_gb300 import cli
+    data, _, _, _ = _per_image_setup(oracle_mod)
+    g, d2, l2 = PER_IMAGE_TRUTH["global_"], PER_IMAGE_TRUTH["desc2"], PER_IMAGE_TRUTH["local2"]
+    cfg = "\n".join(f"{k} {v}" for k, v in zip(["X0", "Y0"], g[:2])) + "\nFUNCTION Gaussian\n" + \
+        "\n".join(f"{k} {v}" for k, v in zip(["PA", "ell", "I_0", "sigma"], g[2:])) + "\n"
+    local = PER_IMAGE_LOCAL.replace("I_sky 5.0 0,20", f"I_sky {l2[2]}").replace("I_0 80 20,200", f"I_0 {l2[7]}")
+    (tmp_path / "c.dat").write_text(cfg)
+    (tmp_path / "info.txt").write_text(f"""IMAGE_START
+NCOLS 44
+NROWS 40
+IMAGE_START
+NCOLS 44
+NROWS 40
+PIXEL_SCALE {d2[0]} fixed
+IMAGE_PA {d2[1]} fixed
+FLUX_SCALE {d2[2]} fixed
+X0 {d2[3]}
+Y0 {d2[4]}
+""" + local)
+    imgs = cli.makemultimages([str(tmp_path / "c.dat"), "-i", str(tmp_path / "info.txt"), "-o", str(tmp_path / "m")],
+                              out=io.StringIO())
+    for img, want in zip(imgs, data):
+        assert np.max(np.abs(img - want)) <= 1e-10 * np.max(np.abs(want))

@@ -79,3 +79,76 @@ X0   20
     assert ims[1].params["X0"][0] == 20.0
     with pytest.raises(ValueError):
         multimage.parse_image_info("DATA x.fits\n")
+
+
+PER_IMAGE_INFO = """IMAGE_START
+DATA  ref.fits
+IMAGE_START
+DATA  second.fits
+PIXEL_SCALE   0.5   fixed
+X0   20
+Y0   25
+FUNCTIONS_START
+X0   10   5,15
+Y0   12
+FUNCTION PointSource   # LABEL star
+I_tot   300   fixed
+X0   30
+Y0   31
+FUNCTION FlatSky
+I_sky   4.0
+IMAGE_START
+DATA  third.fits
+"""
+
+
+def test_image_info_per_image_functions():
+    """FUNCTIONS_START ends an image's own lines; the rest of its block is a
+    function section (core/imageparams_file_parser.cpp:531-547, 626-650)."""
+    ims = multimage.parse_image_info(PER_IMAGE_INFO)
+    assert len(ims) == 3 and ims[0].local is None and ims[2].local is None and ims[2].data == "third.fits"
+    loc = ims[1].local
+    assert ims[1].params["X0"][0] == 20.0 and ims[1].data == "second.fits"
+    assert loc.functions == [("PointSource", True), ("FlatSky", True)]
+    assert loc.labels[0] == "star"
+    assert list(loc.values) == [10.0, 12.0, 300.0, 30.0, 31.0, 4.0]
+    assert loc.lower[0] == 5.0 and loc.upper[0] == 15.0 and loc.fixed[2] == 1
+    with pytest.raises(ValueError):
+        multimage.parse_image_info("IMAGE_START\nDATA a.fits\nFUNCTIONS_START\n")
+
+
+def test_per_image_parameters_follow_the_global_model():
+    """[image descriptions][global model][image 1 locals][image 2 locals] ...;
+    locals copied unchanged after the transformed global model
+    (core/param_holder.cpp:257-268), not scaled by the image description."""
+    cfg_values = list(MODEL)
+    ims = multimage.parse_image_info(PER_IMAGE_INFO)
+    local = [im.local_functions for im in ims]
+    handles = [FakeHandle(len(MODEL)), FakeHandle(len(MODEL) + 6), FakeHandle(len(MODEL))]
+    mm = multimage.MultiImageModel(FUNCS, handles, local)
+    assert mm.n_local == [0, 6, 0] and mm.n_params == 10 + len(MODEL) + 6
+    desc = [0.5, 12.0, 2.0, 20.0, 25.0, 1.0, 0.0, 1.0, 50.0, 40.0]
+    loc = [10.0, 12.0, 300.0, 30.0, 31.0, 4.0]
+    p = np.array(desc + cfg_values + loc)
+    v1 = mm.image_vector(p, 1)
+    assert len(v1) == len(MODEL) + 6 and list(v1[len(MODEL):]) == loc
+    assert v1[5] == 10.0 * 2.0  # global intensity still scaled
+    assert np.array_equal(mm.image_vector(p, 2), np.array(MODEL))
+    T = mm.transform_jacobian(p, 1)
+    assert T.shape == (len(MODEL) + 6, len(p))
+    assert np.array_equal(T[len(MODEL):, mm.local_slice(1)], np.eye(6))
+    assert np.all(T[:len(MODEL), mm.local_slice(1)] == 0) and np.all(T[len(MODEL):, :mm.local_slice(1).start] == 0)
+    with pytest.raises(ValueError):
+        multimage.MultiImageModel(FUNCS, [FakeHandle(len(MODEL))] * 3, local)
+
+
+def test_global_vector_and_names_with_per_image_functions():
+    from imfit_gb300.config import parse_config
+    cfg = parse_config("X0 50 40,60\nY0 40\nFUNCTION FlatSky\nI_sky 7\n")
+    ims = multimage.parse_image_info(PER_IMAGE_INFO)
+    vals, lo, hi, fx = multimage.global_vector(cfg, ims)
+    assert len(vals) == 10 + 3 + 6
+    assert list(vals[13:]) == [10.0, 12.0, 300.0, 30.0, 31.0, 4.0]
+    assert lo[13] == 5.0 and hi[13] == 15.0 and fx[15] == 1
+    names = multimage.parameter_names(cfg, ims)
+    assert names[0] == "PIXEL_SCALE_2" and names[10] == "X0" and names[13] == "X0_2" and names[-1] == "I_sky_2"
