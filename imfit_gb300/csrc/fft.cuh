@@ -35,13 +35,16 @@ constexpr int kMaxRadixPasses = 16;
 // Plan of one transform length: radices applied in order (4 bits each,
 // first pass in the low bits: a scalar, so kernels keep the plan in
 // registers instead of indexing an array in local memory), plus the twiddle
-// table tw[k] = exp(-2*pi*i*k/n), k in [0,n).
+// table, pass by pass: pass p (radix R, span Ns) holds exp(-2*pi*i*r*k/(Ns*R))
+// at off_p + (r-1)*Ns + k (r in [1,R), k in [0,Ns), off_p the sum of
+// (R_q - 1) * Ns_q over the earlier passes); n entries allocated.
 template <typename T>
 struct FFTPlan {
   int n;
   int npass;
   unsigned long long radix;
   const cplx<T> *tw;
+  int padFirst = 0;  // kernels that support it: first intermediate in the padded layout (fft_pad_first)
 };
 
 inline unsigned long long pack_radix(const int *radix, int npass) {
@@ -174,15 +177,37 @@ struct FastDiv {
   __device__ __forceinline__ int div(int x) const { return (int)(((float)x + 0.5f) * inv); }
 };
 
+// Shared-memory index with PAD extra elements after every 16: a radix-R first
+// pass writes each thread's R outputs at consecutive indices, so lanes store
+// R * (lines interleaved) elements apart and, for R = 4 or 8, up to eight
+// lanes of a half-warp hit the same banks; two pad elements per 16 spread
+// them.  Groups of 16 aligned elements stay contiguous (and 16-byte aligned
+// when they start at an even index).
+template <int PAD>
+__device__ __forceinline__ int pad_idx(int i) {
+  return PAD ? i + PAD * (i >> 4) : i;
+}
+
+// Elements a buffer of n unpadded elements occupies in the padded layout.
+__host__ __device__ inline int padded_len(int n, int pad) { return n + pad * (n >> 4) + pad; }
+
+// Plans whose first pass is radix 4 or 8 (and that have a second pass) write
+// their first intermediate in the padded layout.
+__host__ __device__ inline bool fft_pad_first(int npass, unsigned long long radix) {
+  const int r0 = (int)(radix & 15ull);
+  return npass >= 2 && (r0 == 4 || r0 == 8);
+}
+
 // One radix-R Stockham pass over 'nl' lines of length n.
-// Element t of line l lives at buf[l*ls + t*es].
-template <typename T, int R>
+// Element t of line l lives at buf[l*ls + t*es] (PIN / POUT: the padding of
+// the source / destination layout); tw is this pass's part of the plan's
+// twiddle table.
+template <typename T, int R, int PIN = 0, int POUT = 0>
 __device__ __forceinline__ void stockham_pass(const cplx<T> *__restrict__ src, cplx<T> *__restrict__ dst,
                                               int n, int Ns, int nl, int ls, int es,
                                               const cplx<T> *__restrict__ tw, int s, bool lineFastest) {
   const int m = n / R;
   const int total = m * nl;
-  const int twStep = n / (Ns * R);
   const FastDiv byNl(nl), byM(m), byNs(Ns);
   for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
     int l, j;
@@ -194,13 +219,12 @@ __device__ __forceinline__ void stockham_pass(const cplx<T> *__restrict__ src, c
       j = idx - l * m;
     }
     const int k = j - byNs.div(j) * Ns;
-    const cplx<T> *in = src + l * ls;
     cplx<T> v[R];
 #pragma unroll
-    for (int r = 0; r < R; r++) v[r] = in[(j + r * m) * es];
+    for (int r = 0; r < R; r++) v[r] = src[pad_idx<PIN>(l * ls + (j + r * m) * es)];
     if (k != 0) {
 #pragma unroll
-      for (int r = 1; r < R; r++) v[r] = cmul(v[r], twiddle(tw, r * k * twStep, s));
+      for (int r = 1; r < R; r++) v[r] = cmul(v[r], twiddle(tw, (r - 1) * Ns + k, s));
     }
     if (R == 2) dft2(v);
     if (R == 3) dft3(v, s);
@@ -208,10 +232,22 @@ __device__ __forceinline__ void stockham_pass(const cplx<T> *__restrict__ src, c
     if (R == 5) dft5(v, s);
     if (R == 7) dft7(v, s);
     if (R == 8) dft8(v, s);
-    cplx<T> *out = dst + l * ls;
     const int base = (j - k) * R + k;
 #pragma unroll
-    for (int t = 0; t < R; t++) out[(base + t * Ns) * es] = v[t];
+    for (int t = 0; t < R; t++) dst[pad_idx<POUT>(l * ls + (base + t * Ns) * es)] = v[t];
+  }
+}
+
+template <typename T, int PIN, int POUT>
+__device__ __forceinline__ void radix_pass(int R, const cplx<T> *src, cplx<T> *dst, int n, int Ns, int nl, int ls,
+                                           int es, const cplx<T> *tw, int s, bool lineFastest) {
+  switch (R) {
+    case 2: stockham_pass<T, 2, PIN, POUT>(src, dst, n, Ns, nl, ls, es, tw, s, lineFastest); break;
+    case 3: stockham_pass<T, 3, PIN, POUT>(src, dst, n, Ns, nl, ls, es, tw, s, lineFastest); break;
+    case 4: stockham_pass<T, 4, PIN, POUT>(src, dst, n, Ns, nl, ls, es, tw, s, lineFastest); break;
+    case 5: stockham_pass<T, 5, PIN, POUT>(src, dst, n, Ns, nl, ls, es, tw, s, lineFastest); break;
+    case 7: stockham_pass<T, 7, PIN, POUT>(src, dst, n, Ns, nl, ls, es, tw, s, lineFastest); break;
+    default: stockham_pass<T, 8, PIN, POUT>(src, dst, n, Ns, nl, ls, es, tw, s, lineFastest); break;
   }
 }
 
@@ -219,7 +255,11 @@ __device__ __forceinline__ void stockham_pass(const cplx<T> *__restrict__ src, c
 // that holds the result.  Must be called by all threads of the CTA.
 // tw: the twiddle table to read (null: the plan's own, in global memory;
 // kernels that stage the table in shared memory pass their copy).
-template <typename T>
+// PADFIRST: the intermediate written by the first pass (and read by the
+// second) uses the padded layout, so both buffers must hold
+// padded_len(nl * ls, 2) elements; input and result are unpadded.  Only for
+// plans of at least two passes.
+template <typename T, bool PADFIRST = false>
 __device__ cplx<T> *block_fft(cplx<T> *a, cplx<T> *b, const FFTPlan<T> &p, int nl, int ls, int es,
                               int s, bool lineFastest, const cplx<T> *tw = nullptr) {
   int Ns = 1;
@@ -227,15 +267,14 @@ __device__ cplx<T> *block_fft(cplx<T> *a, cplx<T> *b, const FFTPlan<T> &p, int n
   if (!tw) tw = p.tw;
   for (int ps = 0; ps < p.npass; ps++) {
     const int R = (int)((p.radix >> (4 * ps)) & 15ull);
-    switch (R) {
-      case 2: stockham_pass<T, 2>(src, dst, p.n, Ns, nl, ls, es, tw, s, lineFastest); break;
-      case 3: stockham_pass<T, 3>(src, dst, p.n, Ns, nl, ls, es, tw, s, lineFastest); break;
-      case 4: stockham_pass<T, 4>(src, dst, p.n, Ns, nl, ls, es, tw, s, lineFastest); break;
-      case 5: stockham_pass<T, 5>(src, dst, p.n, Ns, nl, ls, es, tw, s, lineFastest); break;
-      case 7: stockham_pass<T, 7>(src, dst, p.n, Ns, nl, ls, es, tw, s, lineFastest); break;
-      default: stockham_pass<T, 8>(src, dst, p.n, Ns, nl, ls, es, tw, s, lineFastest); break;
-    }
+    if (PADFIRST && ps == 0)
+      radix_pass<T, 0, 2>(R, src, dst, p.n, Ns, nl, ls, es, tw, s, lineFastest);
+    else if (PADFIRST && ps == 1)
+      radix_pass<T, 2, 0>(R, src, dst, p.n, Ns, nl, ls, es, tw, s, lineFastest);
+    else
+      radix_pass<T, 0, 0>(R, src, dst, p.n, Ns, nl, ls, es, tw, s, lineFastest);
     __syncthreads();
+    tw += (R - 1) * Ns;
     Ns *= R;
     cplx<T> *t = src;
     src = dst;

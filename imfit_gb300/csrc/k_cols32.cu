@@ -84,20 +84,23 @@ __device__ __forceinline__ void store_row(cplx<float> *dst, const cplx<float> *s
 // Column group body, shared with the ragged cutout kernels: the CPB columns
 // starting at c0 of the spectrum `spec` (pitch, Ly = plan.n rows, nColsC
 // columns), H (hPitch) the PSF spectrum of the same geometry, in the dynamic
-// shared memory smem_raw (Ly * (1 + 3 * CPB) complex values).
+// shared memory smem_raw (cols32_smem bytes: twiddles, two FFT buffers of
+// padded_len(Ly * CPB) elements, the PSF columns).
 // MODE 1: multiply by H (convolution); MODE 2: by conj(H) (adjoint correlation).
 template <int MODE, int CPB>
 __device__ __forceinline__ void cols_group(unsigned char *smem_raw, cplx<float> *spec, long pitch, int nColsC,
                                            int nRowsIn, int nRowsOut, const cplx<float> *H, long hPitch,
                                            const FFTPlan<float> &plan, float scale, int c0) {
   const int Ly = plan.n;
+  const int bufLen = padded_len(Ly * CPB, 2);
   cplx<float> *tw = reinterpret_cast<cplx<float> *>(smem_raw);
   cplx<float> *bufA = tw + Ly;
-  cplx<float> *bufB = bufA + (long)Ly * CPB;
-  cplx<float> *bufH = bufB + (long)Ly * CPB;
+  cplx<float> *bufB = bufA + bufLen;
+  cplx<float> *bufH = bufB + bufLen;
   const int nl = min(CPB, nColsC - c0);
   if (nl <= 0) return;
   const int pairs = (nl + 1) >> 1;
+  const bool padFirst = plan.padFirst != 0;
   spec += c0;
   H += c0;
   // all global reads of the CTA in flight at once
@@ -111,7 +114,8 @@ __device__ __forceinline__ void cols_group(unsigned char *smem_raw, cplx<float> 
   for (int i = threadIdx.x; 2 * i < Ly; i += blockDim.x) cp_async16(tw + 2 * i, plan.tw + 2 * i);
   cp_async_wait_all();
   __syncthreads();
-  cplx<float> *X = block_fft(bufA, bufB, plan, CPB, 1, CPB, -1, true, tw);
+  cplx<float> *X = padFirst ? block_fft<float, true>(bufA, bufB, plan, CPB, 1, CPB, -1, true, tw)
+                            : block_fft<float, false>(bufA, bufB, plan, CPB, 1, CPB, -1, true, tw);
   for (int idx = threadIdx.x; idx < Ly * CPB; idx += blockDim.x) {
     cplx<float> h = bufH[idx];
     if (MODE == 2) h.y = -h.y;
@@ -120,7 +124,8 @@ __device__ __forceinline__ void cols_group(unsigned char *smem_raw, cplx<float> 
   }
   __syncthreads();
   cplx<float> *other = (X == bufA) ? bufB : bufA;
-  cplx<float> *Y = block_fft(X, other, plan, CPB, 1, CPB, +1, true, tw);
+  cplx<float> *Y = padFirst ? block_fft<float, true>(X, other, plan, CPB, 1, CPB, +1, true, tw)
+                            : block_fft<float, false>(X, other, plan, CPB, 1, CPB, +1, true, tw);
   pdl_trigger();
   for (int t = threadIdx.x; t < nRowsOut; t += blockDim.x)
     store_row<CPB>(spec + (long)t * pitch, Y + (long)t * CPB, pairs);
@@ -151,7 +156,7 @@ cudaError_t launch_one(cplx<float> *s, long pitch, long batch, int nColsC, int n
                        cudaStream_t st, int threads, long hBatch, int hDiv, const int *hMap) {
   auto kern = k_cols32<MODE, CPB>;
   allow_max_smem((const void *)kern);
-  const size_t sm = sizeof(cplx<float>) * (size_t)p.n * (1 + 3 * CPB);
+  const size_t sm = cols32_smem(p.n, CPB);
   dim3 grid((nColsC + CPB - 1) / CPB, nBatch);
   return launch_pdl(kern, grid, dim3(threads), sm, st, s, pitch, batch, nColsC, nRowsIn, nRowsOut, h, hPitch, p,
                     scale, hBatch, hDiv, hMap);
@@ -195,11 +200,13 @@ __global__ void __launch_bounds__(256) k_rag_cols(RagArgs r) {
 cudaError_t launch_rag_cols(const RagArgs &r, int total, int maxLy, cudaStream_t st) {
   if (total <= 0) return cudaSuccess;
   allow_max_smem((const void *)k_rag_cols);
-  const size_t sm = sizeof(cplx<float>) * (size_t)maxLy * (1 + 3 * kRagCpb);
+  const size_t sm = cols32_smem(maxLy, kRagCpb);
   return launch_pdl(k_rag_cols, dim3(total), dim3(128), sm, st, r);
 }
 
-size_t cols32_smem(int Ly, int cpb) { return sizeof(cplx<float>) * (size_t)Ly * (1 + 3 * cpb); }
+size_t cols32_smem(int Ly, int cpb) {
+  return sizeof(cplx<float>) * ((size_t)Ly * (1 + cpb) + 2 * (size_t)padded_len(Ly * cpb, 2));
+}
 
 cudaError_t launch_cols32(void *spec, long pitch, long batch, int nColsC, int nRowsIn, int nRowsOut, const void *H,
                           long hPitch, const FFTLen &Ly, float scale, int mode, int nBatch, cudaStream_t st, int cpb,
@@ -218,6 +225,7 @@ cudaError_t launch_cols32(void *spec, long pitch, long batch, int nColsC, int nR
   p.npass = Ly.full.npass;
   p.radix = pack_radix(Ly.full.radix, Ly.full.npass);
   p.tw = reinterpret_cast<const cplx<float> *>(Ly.full.tw32);
+  p.padFirst = fft_pad_enabled() && fft_pad_first(p.npass, p.radix);
   cplx<float> *s = reinterpret_cast<cplx<float> *>(spec);
   const cplx<float> *h = reinterpret_cast<const cplx<float> *>(H);
   if (mode == 1)

@@ -2,21 +2,28 @@
 // gradient.
 //
 // Per parameter vector b the statistic S(theta) and dS/dtheta are formed by
-//   setup      FP64 per-component geometry and Sersic b_n      (FunctionObject::Setup)
+//   subsample  FP64 per-component geometry and Sersic b_n (FunctionObject::Setup)
+//              by the first warps, then the subsampled box pixels of the main
+//              window and of the oversampled region, warp-cooperatively,
+//              into a table of values and derivatives
 //   eval_r2c   model window rows evaluated in FP32 (SFU lg2/ex2), subsampled
-//              pixels summed warp-cooperatively, then the row FFT -- the model
+//              pixels read from the table, then the row FFT -- the model
 //              image never goes to HBM                         (CreateModelImage pixel loop)
-//   cols       column FFT x PSF spectrum x inverse column FFT  (Convolver::ConvolveImage)
+//   cols       column FFT x PSF spectrum x inverse column FFT  (Convolver::ConvolveImage,
+//              k_cols32.cu)
 //   region     oversampled region: same pipeline at k x resolution and a
 //              fused block-average                             (OversampledRegion, DownsampleAndReplace)
-//   stat_rows  inverse row FFT, statistic terms accumulated in FP64, the
-//              adjoint seed g = dS/dM written and immediately row-FFT'd
-//                                                              (ChiSquared / CashStatistic)
+//   stat_rows  inverse row FFT, statistic terms in FP32 per pixel, summed in
+//              double-float above the warp; the adjoint seed g = dS/dM
+//              written and immediately row-FFT'd                (ChiSquared / CashStatistic)
 //   cols(conj) the adjoint: correlation of g with the PSF
 //   grad_rows  inverse row FFT, then one pass over the window accumulating
-//              r~ * dm/dtheta for every parameter (subsampled pixels again
-//              warp-cooperative), FP64 per-block partials
-//   reduce     deterministic final sums.
+//              r~ * dm/dtheta for every parameter (table for subsampled
+//              pixels), per-CTA double-float partials; the last CTA to finish
+//              (a completion counter) forms the final sums in a fixed order.
+// Consecutive kernels overlap their launch with the previous kernel's tail
+// (programmatic dependent launch: each waits on griddepcontrol before reading
+// what its predecessor wrote).
 // The "valid" window W = N + P - 1 (rather than the reference's N + 2P model
 // plus N + 3P - 1 padding) is exactly the set of model pixels the data
 // crop depends on; constant backgrounds (FlatSky) are added after the
@@ -182,14 +189,16 @@ __device__ __forceinline__ void subsample_sum(const CompF32 &cc, int ns, float x
 // subsamples of the profile and of its 7 derivatives (X0, Y0, then the
 // function parameters).  CTAs [0, nMainCtas) cover the main window's box, the
 // rest the oversampled region's.
-__global__ void __launch_bounds__(256) k_fast_subsample(FastArgs a, WinDesc mw, WinDesc rw, int nMainCtas) {
+__global__ void __launch_bounds__(256) k_fast_subsample(FastArgs a, WinDesc mw, WinDesc rw, int nMainCtas,
+                                                        int publish) {
   pdl_wait();
   const int b = blockIdx.z, c = blockIdx.y;
-  if (blockIdx.x != 0 && !(a.desc[c].subsample && subsampling_type(a.desc[c].type))) return;
+  const bool subs = a.desc[c].subsample && subsampling_type(a.desc[c].type);
+  if ((blockIdx.x != 0 || !publish) && !subs) return;
   __shared__ CompF32 rec;
-  setup_component(a, c, b, rec, blockIdx.x == 0 && c == 0);
+  setup_component(a, c, b, rec, publish && blockIdx.x == 0 && c == 0);
   const CompF32 cc = rec;
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+  if (publish && blockIdx.x == 0 && threadIdx.x == 0) {
     a.comps[b * a.nComp + c] = cc;
     if (c == 0 && a.done) a.done[b] = 0u;
   }
@@ -1176,6 +1185,95 @@ __device__ __forceinline__ void deviate_slope(const FastArgs &a, long z, float m
   q = (dev > 0.f) ? ((T < 0.f) ? -1.f : 1.f) * w * dT / dev : 0.f;
 }
 
+// Row partial sums of J^T W J as the upper triangle of one augmented Gram
+// matrix: with a_j (j < nP) the Jacobian rows of the deviates, a_nP = dev and
+// c the pixel weights (bootstrap multiplicities; W = false: all 1),
+//   G = sum over the row's columns of c a a^T,
+// G_jk (j <= k < nP) = alpha_jk, G_j,nP = beta_j, G_nP,nP = S, stored in the
+// order alpha (row-major upper triangle), beta, S.  Warps take 4 x 4 tiles of
+// the triangle over one chunk of the columns (lanes on consecutive columns:
+// conflict-free shared loads, 16 FMAs per 8 loads), reduce each tile entry
+// across the warp, and the chunks' sums are added in a fixed order.
+// Row j of a is at U + ss[j] * uStride (ss[j] < 0: the background row qb),
+// row nP at dv, rows past nP at zero (nc zeros).  red holds jtwj_splits() x Q
+// floats.  All threads of the CTA call it; ends with a barrier.
+__host__ __device__ inline int jtwj_tiles(int nP) {
+  const int nt = (nP + 4) / 4;  // tiles per side of the (nP + 1)^2 matrix
+  return nt * (nt + 1) / 2;
+}
+__host__ __device__ inline int jtwj_splits(int nP, int threads) {
+  const int s = 4 * (threads / 32) / jtwj_tiles(nP);
+  return s < 1 ? 1 : (s > 16 ? 16 : s);
+}
+__host__ __device__ inline int jtwj_aux_floats(int nP, int nc, int threads) {
+  const int Q = nP * (nP + 1) / 2 + nP + 1;
+  return 4 * nc + jtwj_splits(nP, threads) * Q;
+}
+
+template <bool W>
+__device__ __forceinline__ void jtwj_gram(const float *U, long uStride, const int *ss, const float *qb,
+                                          const float *dv, const float *zero, const float *cw, int nc, int nP,
+                                          float *red, float *out, long outStride) {
+  const int n1 = nP + 1, nt = (n1 + 3) / 4, nTiles = nt * (nt + 1) / 2;
+  const int nPair = nP * (nP + 1) / 2, Q = nPair + nP + 1;
+  const int nw = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nSplit = jtwj_splits(nP, blockDim.x);
+  const int chunk = (((nc + nSplit - 1) / nSplit) + 31) & ~31;
+  for (int item = warp; item < nTiles * nSplit; item += nw) {
+    const int sp = item / nTiles;
+    int I = 0, r = item - sp * nTiles;
+    while (r >= nt - I) {
+      r -= nt - I;
+      I++;
+    }
+    const int J = I + r;
+    const float *X[4], *Y[4];
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+      const int jx = 4 * I + t, jy = 4 * J + t;
+      X[t] = jx < nP ? (ss[jx] >= 0 ? U + ss[jx] * uStride : qb) : (jx == nP ? dv : zero);
+      Y[t] = jy < nP ? (ss[jy] >= 0 ? U + ss[jy] * uStride : qb) : (jy == nP ? dv : zero);
+    }
+    float acc[4][4];
+#pragma unroll
+    for (int t = 0; t < 4; t++)
+#pragma unroll
+      for (int u = 0; u < 4; u++) acc[t][u] = 0.f;
+    const int c1 = min(nc, (sp + 1) * chunk);
+    for (int col = sp * chunk + lane; col < c1; col += 32) {
+      float x[4], y[4];
+      const float c = W ? cw[col] : 1.f;
+#pragma unroll
+      for (int t = 0; t < 4; t++) {
+        x[t] = W ? X[t][col] * c : X[t][col];
+        y[t] = Y[t][col];
+      }
+#pragma unroll
+      for (int t = 0; t < 4; t++)
+#pragma unroll
+        for (int u = 0; u < 4; u++) acc[t][u] = fmaf(x[t], y[u], acc[t][u]);
+    }
+#pragma unroll
+    for (int t = 0; t < 4; t++)
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int j = 4 * I + t, k = 4 * J + u;
+        if (j > k || k >= n1) continue;  // uniform across the warp
+        const float v = warp_sum(acc[t][u]);
+        if (lane == 0) {
+          const int qi = k < nP ? j * nP - j * (j - 1) / 2 + (k - j) : (j < nP ? nPair + j : nPair + nP);
+          red[sp * Q + qi] = v;
+        }
+      }
+  }
+  __syncthreads();
+  for (int qi = threadIdx.x; qi < Q; qi += blockDim.x) {
+    float t = 0.f;
+    for (int sp = 0; sp < nSplit; sp++) t += red[sp * Q + qi];
+    out[qi * outStride] = t;
+  }
+}
+
 // One CTA per (data row, parameter vector): inverse row FFT of the nD
 // convolved derivative rows, the per-pixel Jacobian rows u_j = q dM/dtheta_j
 // (region pixels from the downsampled region derivatives, background
@@ -1195,8 +1293,6 @@ __global__ void __launch_bounds__(1024) k_fast_jtwj_rows(FastArgs a, FastGeom g,
   int *ss = reinterpret_cast<int *>(smem);
   cplx<float> *bufA = reinterpret_cast<cplx<float> *>(ss + kMaxParams);
   cplx<float> *bufB = bufA + nD * ls;
-  float *U = reinterpret_cast<float *>(bufB + nD * ls);  // nD + 4 rows of nc floats
-  float *red = U + (long)(nD + 4) * nc;                  // blockDim.x floats
   for (int i = threadIdx.x; i < nP; i += blockDim.x) ss[i] = slot[i];
   if (a.dataStride) {  // image stack: this entry's data and weights
     const long img = a.entry ? a.entry[b] : b;
@@ -1211,9 +1307,16 @@ __global__ void __launch_bounds__(1024) k_fast_jtwj_rows(FastArgs a, FastGeom g,
     bufA[j * ls + k] = c2r_pre(src + (long)j * g.specBatch, k, M, twL);
   }
   __syncthreads();
-  const cplx<float> *Z = block_fft(bufA, bufB, plan, nD, ls, 1, +1, false);
-  const float *Zr = reinterpret_cast<const float *>(Z);
-  float *qb = U + (long)nD * nc, *cw = qb + nc, *cd = cw + nc, *dv = cd + nc;
+  cplx<float> *Z = block_fft(bufA, bufB, plan, nD, ls, 1, +1, false);
+  // the Jacobian rows overwrite the real rows they are formed from (row j at
+  // Zr + 2 j ls); the per-pixel vectors and the chunk sums use the other FFT
+  // buffer when they fit there, else the space after bufB
+  float *Zr = reinterpret_cast<float *>(Z);
+  const long uStride = 2L * ls;
+  float *aux = (jtwj_aux_floats(nP, nc, blockDim.x) <= 2 * nD * ls)
+                   ? reinterpret_cast<float *>(Z == bufA ? bufB : bufA)
+                   : reinterpret_cast<float *>(bufB + nD * ls);
+  float *qb = aux, *cw = qb + nc, *dv = cw + nc, *zero = dv + nc, *red = zero + nc;
   const long nPix = (long)g.nDataRows * nc;
   for (int col = threadIdx.x; col < nc; col += blockDim.x) {
     const long zi = (long)row * nc + col;
@@ -1231,8 +1334,10 @@ __global__ void __launch_bounds__(1024) k_fast_jtwj_rows(FastArgs a, FastGeom g,
       }
     }
     const long rStride = (long)g.rRows * g.rCols;
-    for (int j = 0; j < nD; j++)
-      U[(long)j * nc + col] = q * (inReg ? regDeriv[((long)b * nD + j) * rStride + ri] : Zr[2 * j * ls + col]);
+    for (int j = 0; j < nD; j++) {
+      float *u = Zr + j * uStride + col;
+      *u = q * (inReg ? regDeriv[((long)b * nD + j) * rStride + ri] : *u);
+    }
     for (int ps = 0; PS && ps < a.nPs; ps++) {  // point sources: derivatives after the convolution
       const CompF32 &c = a.comps[b * a.nComp + a.psComp[ps]];
       const CompDesc &d = a.desc[a.psComp[ps]];
@@ -1255,65 +1360,25 @@ __global__ void __launch_bounds__(1024) k_fast_jtwj_rows(FastArgs a, FastGeom g,
       const bool rot = d.type == F_POINTSOURCEROT;
       const int map[4] = {d.x0Index, d.x0Index + 1, d.paramOffset + (rot ? 1 : 0), rot ? d.paramOffset : -1};
       for (int t4 = 0; t4 < 4; t4++)
-        if (map[t4] >= 0 && ss[map[t4]] >= 0) U[(long)ss[map[t4]] * nc + col] += q * dsum[t4];
+        if (map[t4] >= 0 && ss[map[t4]] >= 0) Zr[ss[map[t4]] * uStride + col] += q * dsum[t4];
     }
     qb[col] = q * (inReg ? a.psfSumOs : a.psfSum);
     cw[col] = cnt;
-    cd[col] = cnt * dev;
     dv[col] = dev;
+    zero[col] = 0.f;
     if (jac) {  // Jacobian columns [b][param][pixel] and the deviates [b][pixel] after them
       float *jb = jac + (long)b * (nP + 1) * nPix;
-      for (int j = 0; j < nP; j++) jb[(long)j * nPix + zi] = ss[j] >= 0 ? U[(long)ss[j] * nc + col] : qb[col];
+      for (int j = 0; j < nP; j++) jb[(long)j * nPix + zi] = ss[j] >= 0 ? Zr[ss[j] * uStride + col] : qb[col];
       jb[(long)nP * nPix + zi] = dev;
     }
   }
   __syncthreads();
-  const int nPair = nP * (nP + 1) / 2, Q = nPair + nP + 1;
-  const int T = blockDim.x;
-  int nseg = T / Q;
-  nseg = nseg < 1 ? 1 : (nseg > 32 ? 32 : nseg);
-  const int perRound = T / nseg;
-  const int myQ = threadIdx.x / nseg, seg = threadIdx.x - myQ * nseg;
-  for (int q0 = 0; q0 < Q; q0 += perRound) {
-    const int qi = q0 + myQ;
-    float acc = 0.f;
-    if (myQ < perRound && qi < Q) {
-      const float *X, *Y, *C;
-      if (qi < nPair) {
-        int j = 0, r = qi;
-        while (r >= nP - j) {
-          r -= nP - j;
-          j++;
-        }
-        const int k = j + r;
-        X = ss[j] >= 0 ? U + (long)ss[j] * nc : qb;
-        Y = ss[k] >= 0 ? U + (long)ss[k] * nc : qb;
-        C = cw;
-      } else if (qi < nPair + nP) {
-        const int j = qi - nPair;
-        X = ss[j] >= 0 ? U + (long)ss[j] * nc : qb;
-        Y = cd;
-        C = nullptr;
-      } else {
-        X = cd;
-        Y = dv;
-        C = nullptr;
-      }
-      if (C) {
-        for (int col = seg; col < nc; col += nseg) acc += C[col] * X[col] * Y[col];
-      } else {
-        for (int col = seg; col < nc; col += nseg) acc += X[col] * Y[col];
-      }
-    }
-    red[threadIdx.x] = acc;
-    __syncthreads();
-    if (threadIdx.x < perRound && q0 + threadIdx.x < Q) {
-      float t = 0.f;
-      for (int i = 0; i < nseg; i++) t += red[threadIdx.x * nseg + i];
-      part[((long)b * Q + q0 + threadIdx.x) * a.partStride + blockIdx.x] = t;
-    }
-    __syncthreads();
-  }
+  const int Q = nP * (nP + 1) / 2 + nP + 1;
+  float *out = part + (long)b * Q * a.partStride + blockIdx.x;
+  if (a.count)
+    jtwj_gram<true>(Zr, uStride, ss, qb, dv, zero, cw, nc, nP, red, out, a.partStride);
+  else
+    jtwj_gram<false>(Zr, uStride, ss, qb, dv, zero, cw, nc, nP, red, out, a.partStride);
 }
 
 // FP64 sums of the per-row partials: grid (quantity, parameter vector).
@@ -1405,18 +1470,21 @@ static void ensure_smem(K kern, size_t bytes) {
   allow_max_smem((const void *)kern);
 }
 
-// Set-up + subsample tables of both windows in one launch: CTAs per
-// (component, vector) and window chosen so that the whole grid is about one
-// wave of 8 CTAs per SM (each CTA repeats the component's FP64 set-up once),
-// at most one warp per box pixel.
-static cudaError_t launch_subsample(const FastArgs &a, const WinDesc &mw, const WinDesc &rw, bool region, int nBatch,
+// Set-up + subsample tables: CTAs per (component, vector) and window chosen
+// so that the grid is about one wave of 8 CTAs per SM (each CTA repeats the
+// component's FP64 set-up once), at most one warp per box pixel.  windows:
+// 1 the main window (publishes the component records, background levels and
+// completion counters), 2 the oversampled region only (on the side stream,
+// concurrently with 1), 3 both in one launch.
+static cudaError_t launch_subsample(const FastArgs &a, const WinDesc &mw, const WinDesc &rw, int windows, int nBatch,
                                     cudaStream_t st) {
-  const int sets = a.nComp * nBatch * (region ? 2 : 1);
+  const bool wm = windows & 1, wr = (windows & 2) != 0;
+  const int sets = a.nComp * nBatch * ((wm ? 1 : 0) + (wr ? 1 : 0));
   const int cap = std::max(1, 8 * 152 / std::max(sets, 1));
-  const int nMain = std::max(1, std::min((a.boxMain * a.boxMain + 7) / 8, cap));
-  const int nReg = region ? std::max(1, std::min((a.boxReg * a.boxReg + 7) / 8, cap)) : 0;
+  const int nMain = wm ? std::max(1, std::min((a.boxMain * a.boxMain + 7) / 8, cap)) : 0;
+  const int nReg = wr ? std::max(1, std::min((a.boxReg * a.boxReg + 7) / 8, cap)) : 0;
   dim3 grid(nMain + nReg, a.nComp, nBatch);
-  return launch_pdl(k_fast_subsample, grid, dim3(256), 0, st, a, mw, region ? rw : mw, nMain);
+  return launch_pdl(k_fast_subsample, grid, dim3(256), 0, st, a, wm ? mw : rw, wr ? rw : mw, nMain, wm ? 1 : 0);
 }
 
 static cudaError_t launch_eval(const FastArgs &a, const WinDesc &w, const FFTLen &L, int nBatch, int win,
@@ -1562,11 +1630,23 @@ cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool 
   if (!mks.panels) mks.count = nullptr;
   if (!rks.panels) rks.count = nullptr;
 
-  STAGE("subsample", st, launch_subsample(a, mw, rw, g.hasRegion != 0, nBatch, st));
-  if (fork) {
+  if (fork && split_subsample_enabled()) {
+    // the region's subsample table on the side stream, concurrently with the
+    // main window's (which publishes the component records the region needs)
     cudaError_t e = cudaEventRecord(p.fork0, st);
     if (!e) e = cudaStreamWaitEvent(rs, p.fork0, 0);
     if (e) return e;
+    STAGE("subsample", st, launch_subsample(a, mw, rw, 1, nBatch, st));
+    if ((e = cudaEventRecord(p.sub0, st))) return e;
+    STAGE("region_subsample", rs, launch_subsample(a, mw, rw, 2, nBatch, rs));
+    if ((e = cudaStreamWaitEvent(rs, p.sub0, 0))) return e;
+  } else {
+    STAGE("subsample", st, launch_subsample(a, mw, rw, g.hasRegion ? 3 : 1, nBatch, st));
+    if (fork) {
+      cudaError_t e = cudaEventRecord(p.fork0, st);
+      if (!e) e = cudaStreamWaitEvent(rs, p.fork0, 0);
+      if (e) return e;
+    }
   }
   if (g.hasRegion) {
     if (los) STAGE("region_los_eval", rs, launch_los_eval(a, rw, nBatch, rks, rs));
@@ -1622,16 +1702,20 @@ static size_t deriv_smem(int M, int nD) {
          sizeof(cplx<float>) * 2 * (size_t)nD * (M + 1) + 16;
 }
 
-static size_t jtwj_rows_smem(int M, int nD, int nCols, int threads) {
+// The two FFT buffers, plus room for the per-pixel vectors and chunk sums of
+// jtwj_gram when they do not fit in the buffer the transform leaves free.
+static size_t jtwj_rows_smem(int M, int nD, int nP, int nCols, int threads) {
+  const long aux = jtwj_aux_floats(nP, nCols, threads);
+  const long spare = 2L * nD * (M + 1);
   return sizeof(int) * kMaxParams + sizeof(cplx<float>) * 2 * (size_t)nD * (M + 1) +
-         sizeof(float) * ((size_t)(nD + 4) * nCols + threads) + 16;
+         (aux <= spare ? 0 : sizeof(float) * (size_t)aux) + 16;
 }
 
 static constexpr int kJtwjThreads = 512;
 
-size_t fast_jtwj_smem(const FastPlan &p, int nD) {
+size_t fast_jtwj_smem(const FastPlan &p, int nD, int nP) {
   size_t s = deriv_smem(p.Lx->half.n, nD);
-  s = std::max(s, jtwj_rows_smem(p.Lx->half.n, nD, p.g.nDataCols, kJtwjThreads));
+  s = std::max(s, jtwj_rows_smem(p.Lx->half.n, nD, nP, p.g.nDataCols, kJtwjThreads));
   if (p.g.hasRegion) s = std::max(s, deriv_smem(p.Rx->half.n, nD));
   return s;
 }
@@ -1679,7 +1763,7 @@ cudaError_t fast_jtwj(const FastPlan &p, const FastArgs &a, const JtwjArgs &J, i
                              p.hPitch, *p.Ly, scale, 1, nB, st, tu.colCpb, p.hBatch, nD, p.hMap, tu.colThreads));
   }
   const int M = p.Lx->half.n;
-  const size_t sm = jtwj_rows_smem(M, nD, g.nDataCols, kJtwjThreads);
+  const size_t sm = jtwj_rows_smem(M, nD, a.nParams, g.nDataCols, kJtwjThreads);
   stage_begin(p, "jtwj_rows", st);
   auto jrows = a.nPs ? k_fast_jtwj_rows<true> : k_fast_jtwj_rows<false>;
   jrows<<<dim3(g.nDataRows, nBatch), kJtwjThreads, sm, st>>>(
@@ -1914,8 +1998,6 @@ __global__ void __launch_bounds__(512) k_rag_jtwj_rows(FastArgs a, RagArgs r, co
   int *ss = reinterpret_cast<int *>(smem);
   cplx<float> *bufA = reinterpret_cast<cplx<float> *>(ss + kMaxParams);
   cplx<float> *bufB = bufA + nD * ls;
-  float *U = reinterpret_cast<float *>(bufB + nD * ls);  // nD + 3 rows of nc floats
-  float *red = U + (long)(nD + 3) * nc;                  // blockDim.x floats
   for (int i = threadIdx.x; i < nP; i += blockDim.x) ss[i] = slot[i];
   const cplx<float> *src = r.spec + (long)nD * E.specOff + (long)row * E.pitch;
   const FastDiv byM(M);
@@ -1924,60 +2006,29 @@ __global__ void __launch_bounds__(512) k_rag_jtwj_rows(FastArgs a, RagArgs r, co
     bufA[j * ls + kk] = c2r_pre(src + (long)j * E.specSize, kk, M, E.twL);
   }
   __syncthreads();
-  const cplx<float> *Z = block_fft(bufA, bufB, E.rowPlan, nD, ls, 1, +1, false);
-  const float *Zr = reinterpret_cast<const float *>(Z);
-  float *qb = U + (long)nD * nc, *cd = qb + nc, *dv = cd + nc;
+  cplx<float> *Z = block_fft(bufA, bufB, E.rowPlan, nD, ls, 1, +1, false);
+  // Jacobian rows in place over the real rows (row j at Zr + 2 j ls); the
+  // per-pixel vectors in the free FFT buffer when they fit, else after bufB
+  float *Zr = reinterpret_cast<float *>(Z);
+  const long uStride = 2L * ls;
+  float *aux = (jtwj_aux_floats(nP, nc, blockDim.x) <= 2 * nD * ls)
+                   ? reinterpret_cast<float *>(Z == bufA ? bufB : bufA)
+                   : reinterpret_cast<float *>(bufB + nD * ls);
+  float *qb = aux, *dv = qb + 2 * nc, *zero = dv + nc, *red = zero + nc;
   for (int col = threadIdx.x; col < nc; col += blockDim.x) {
     const long z = E.dataOff + (long)row * nc + col;
     const float m = r.model[z];
     float dev, q;
     deviate_slope(a, z, m, dev, q);
-    for (int j = 0; j < nD; j++) U[(long)j * nc + col] = q * Zr[2 * j * ls + col];
+    for (int j = 0; j < nD; j++) Zr[j * uStride + col] *= q;
     qb[col] = q * a.psfSum;
-    cd[col] = dev;
     dv[col] = dev;
+    zero[col] = 0.f;
   }
   __syncthreads();
   pdl_trigger();
-  const int nPair = nP * (nP + 1) / 2, Q = nPair + nP + 1;
-  const int T = blockDim.x;
-  int nseg = T / Q;
-  nseg = nseg < 1 ? 1 : (nseg > 32 ? 32 : nseg);
-  const int perRound = T / nseg;
-  const int myQ = threadIdx.x / nseg, seg = threadIdx.x - myQ * nseg;
-  for (int q0 = 0; q0 < Q; q0 += perRound) {
-    const int qi = q0 + myQ;
-    float acc = 0.f;
-    if (myQ < perRound && qi < Q) {
-      const float *X, *Y;
-      if (qi < nPair) {
-        int j = 0, rr = qi;
-        while (rr >= nP - j) {
-          rr -= nP - j;
-          j++;
-        }
-        const int kk = j + rr;
-        X = ss[j] >= 0 ? U + (long)ss[j] * nc : qb;
-        Y = ss[kk] >= 0 ? U + (long)ss[kk] * nc : qb;
-      } else if (qi < nPair + nP) {
-        const int j = qi - nPair;
-        X = ss[j] >= 0 ? U + (long)ss[j] * nc : qb;
-        Y = cd;
-      } else {
-        X = cd;
-        Y = dv;
-      }
-      for (int col = seg; col < nc; col += nseg) acc += X[col] * Y[col];
-    }
-    red[threadIdx.x] = acc;
-    __syncthreads();
-    if (threadIdx.x < perRound && q0 + threadIdx.x < Q) {
-      float tt = 0.f;
-      for (int i = 0; i < nseg; i++) tt += red[threadIdx.x * nseg + i];
-      r.part[(long)(q0 + threadIdx.x) * r.totalRows + E.rowOff + row] = tt;
-    }
-    __syncthreads();
-  }
+  jtwj_gram<false>(Zr, uStride, ss, qb, dv, zero, nullptr, nc, nP, red, r.part + (long)E.rowOff + row,
+                   r.totalRows);
 }
 
 // FP64 sums over each cutout's row partials: grid (quantity, slot).
@@ -2016,11 +2067,11 @@ static size_t rag_eval_smem(int maxM) {
 constexpr int kRagRowThreads = 128;
 constexpr int kRagJtwjThreads = 256;
 
-size_t rag_jtwj_smem(int maxM, int nD, int maxCols) {
+size_t rag_jtwj_smem(int maxM, int nD, int nP, int maxCols) {
   const size_t deriv = sizeof(CompF32) * kMaxComponents + sizeof(int) * (3 * kMaxComponents + kMaxParams) +
                        sizeof(cplx<float>) * 2 * (size_t)nD * (maxM + 1) + 16;
   const size_t rows = sizeof(int) * kMaxParams + sizeof(cplx<float>) * 2 * (size_t)nD * (maxM + 1) +
-                      sizeof(float) * ((size_t)(nD + 3) * maxCols + kRagJtwjThreads) + 16;
+                      sizeof(float) * (size_t)jtwj_aux_floats(nP, maxCols, kRagJtwjThreads) + 16;
   return std::max(deriv, rows);
 }
 
@@ -2053,7 +2104,7 @@ cudaError_t rag_jtwj(const FastArgs &a, RagArgs r, cplx<float> *dspec, const int
   if ((e = launch_pdl(k_rag_model_rows, dim3(totals[kRagDataRows]), dim3(kRagRowThreads),
                       sizeof(cplx<float>) * 3 * (maxM + 1), st, a, r)))
     return e;
-  const size_t smJ = rag_jtwj_smem(maxM, nD, maxCols);
+  const size_t smJ = rag_jtwj_smem(maxM, nD, a.nParams, maxCols);
   RagArgs rd = r;
   rd.spec = dspec;
   if (nD > 0) {

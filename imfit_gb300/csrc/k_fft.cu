@@ -286,6 +286,26 @@ bool pdl_enabled() {
   return on;
 }
 
+// Padded first intermediate of the column FFTs (fft_pad_first); IMFIT_FFT_PAD=0
+// keeps every layout unpadded.
+bool fft_pad_enabled() {
+  static const bool on = [] {
+    const char *v = getenv("IMFIT_FFT_PAD");
+    return !(v && v[0] == '0');
+  }();
+  return on;
+}
+
+// Oversampled-region subsample table on the side stream, concurrently with
+// the main window's; IMFIT_SPLIT_SUBSAMPLE=0 computes both in one launch.
+bool split_subsample_enabled() {
+  static const bool on = [] {
+    const char *v = getenv("IMFIT_SPLIT_SUBSAMPLE");
+    return !(v && v[0] == '0');
+  }();
+  return on;
+}
+
 void allow_max_smem(const void *kernel) {
   static std::mutex lock;
   static std::set<std::pair<int, const void *>> done;
@@ -348,20 +368,37 @@ int smooth_candidates(int n, bool even, int count, double maxRatio, int *out) {
   return k;
 }
 
+// Twiddles of the plan, pass by pass: pass p (radix R, span Ns, starting at
+// offset off_p = sum over earlier passes of (R_q - 1) Ns_q) holds
+// exp(-2 pi i r k / (Ns R)) at off_p + (r - 1) Ns + k, r in [1, R), k in
+// [0, Ns) -- n - 1 entries in all.  Threads of a pass with consecutive k then
+// read consecutive entries (no shared-memory bank conflicts once staged);
+// each value is the one a single table exp(-2 pi i m / n) holds at
+// m = r k n / (Ns R).
 static cudaError_t table_create(FFTTable &t, int n, int variant) {
   t.n = n;
   t.npass = radix_schedule(n, t.radix, variant);
   if (t.npass < 0) return cudaErrorInvalidValue;
-  std::vector<double> w64(2 * (size_t)n);
-  std::vector<float> w32(2 * (size_t)n);
+  std::vector<double> full(2 * (size_t)n);
   for (int k = 0; k < n; k++) {
-    // angle reduced to [0, pi/2]-symmetric evaluation for accuracy
     const double a = 2.0 * M_PI * (double)k / (double)n;
-    w64[2 * k] = cos(a);
-    w64[2 * k + 1] = -sin(a);
-    w32[2 * k] = (float)w64[2 * k];
-    w32[2 * k + 1] = (float)w64[2 * k + 1];
+    full[2 * k] = cos(a);
+    full[2 * k + 1] = -sin(a);
   }
+  std::vector<double> w64(2 * (size_t)n, 0.0);
+  std::vector<float> w32(2 * (size_t)n, 0.f);
+  long off = 0;
+  for (int p = 0, Ns = 1; p < t.npass; Ns *= t.radix[p], p++) {
+    const int R = t.radix[p], step = n / (Ns * R);
+    for (int r = 1; r < R; r++)
+      for (int k = 0; k < Ns; k++) {
+        const long e = off + (long)(r - 1) * Ns + k, m = (long)r * k * step;
+        w64[2 * e] = full[2 * m];
+        w64[2 * e + 1] = full[2 * m + 1];
+      }
+    off += (long)(R - 1) * Ns;
+  }
+  for (size_t i = 0; i < w64.size(); i++) w32[i] = (float)w64[i];
   cudaError_t e = cudaMalloc(&t.tw64, sizeof(double) * 2 * (size_t)n);
   if (e) return e;
   e = cudaMalloc(&t.tw32, sizeof(float) * 2 * (size_t)n);

@@ -23,6 +23,8 @@ __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;\n" :::); }
 
 bool pdl_enabled();
+bool fft_pad_enabled();
+bool split_subsample_enabled();
 
 template <typename... KArgs, typename... Args>
 cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
@@ -301,6 +303,7 @@ struct FastPlan {
   // and the events that fork it from / join it back to the main stream
   cudaStream_t side = nullptr;
   cudaEvent_t fork0 = nullptr, join0 = nullptr, fork1 = nullptr, join1 = nullptr;
+  cudaEvent_t sub0 = nullptr;  // main window's subsample table done (component records published)
   FastGeom g;
   const FFTLen *Lx, *Ly, *Rx, *Ry;  // main and region lengths
   const void *H, *Hr;               // FP32 PSF spectra (main, region)
@@ -382,9 +385,9 @@ cudaError_t rag_jtwj(const FastArgs &a, RagArgs r, cplx<float> *dspec, const int
                      const int totals[kRagWorkKinds], const int *slot, int nD, int maxM, int maxLy, int maxCols,
                      double *alpha, double *beta, double *stat, cudaStream_t st);
 // shared memory of the ragged derivative and row-product kernels
-size_t rag_jtwj_smem(int maxM, int nD, int maxCols);
+size_t rag_jtwj_smem(int maxM, int nD, int nP, int maxCols);
 cudaError_t launch_rag_cols(const RagArgs &r, int total, int maxLy, cudaStream_t st);
-size_t fast_jtwj_smem(const FastPlan &p, int nD);
+size_t fast_jtwj_smem(const FastPlan &p, int nD, int nP);
 cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool wantGrad, cudaStream_t st);
 // one-time kernel attribute set-up (call before any stream capture)
 void fast_prepare_kernels();

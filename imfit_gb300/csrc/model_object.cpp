@@ -353,7 +353,7 @@ struct imfit_model_s {
   bool timing = false;
   std::string timingStage;           // empty: time every kernel (serially)
   cudaStream_t side = nullptr;       // oversampled-region pipeline
-  cudaEvent_t forkEv[2] = {nullptr, nullptr}, joinEv[2] = {nullptr, nullptr};
+  cudaEvent_t forkEv[2] = {nullptr, nullptr}, joinEv[2] = {nullptr, nullptr}, subEv = nullptr;
   bool concurrent = true;
 
   ~imfit_model_s() {
@@ -377,6 +377,7 @@ struct imfit_model_s {
       if (forkEv[i]) cudaEventDestroy(forkEv[i]);
       if (joinEv[i]) cudaEventDestroy(joinEv[i]);
     }
+    if (subEv) cudaEventDestroy(subEv);
     if (side) cudaStreamDestroy(side);
     if (stream) cudaStreamDestroy(stream);
   }
@@ -1431,6 +1432,7 @@ struct imfit_model_s {
       p.fork1 = forkEv[1];
       p.join0 = joinEv[0];
       p.join1 = joinEv[1];
+      p.sub0 = subEv;
     }
     p.g = fg;
     p.Lx = &Fx;
@@ -1676,7 +1678,7 @@ struct imfit_model_s {
     FastPlan p = fastPlan();
     int optin = 0;
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
-    if (fast_jtwj_smem(p, nDeriv) > (size_t)optin)
+    if (fast_jtwj_smem(p, nDeriv, nParamsTot) > (size_t)optin)
       return fail(IMFIT_E_UNSUPPORTED, "J^T J: too many parameters for this image width (shared memory)");
     JtwjArgs J{};
     J.dspec = dDSpec32.p;
@@ -1843,6 +1845,7 @@ struct imfit_model_s {
       p.npass = t.npass;
       p.radix = pack_radix(t.radix, t.npass);
       p.tw = reinterpret_cast<const cplx<float> *>(t.tw32);
+      p.padFirst = fft_pad_enabled() && fft_pad_first(p.npass, p.radix);
       return p;
     };
     // data, weights, PSF spectra
@@ -1918,7 +1921,7 @@ struct imfit_model_s {
     if (e) return cuda_fail(e, "cutout-set buffers");
     int optin = 0;
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
-    if (rag_jtwj_smem(R.maxM, ragNDeriv, R.maxCols) > (size_t)optin)
+    if (rag_jtwj_smem(R.maxM, ragNDeriv, nParamsTot, R.maxCols) > (size_t)optin)
       return fail(IMFIT_E_UNSUPPORTED, "cutout set: the largest cutout needs more shared memory than a CTA has");
     R.n = nImg;
     nValid = R.totalPix;
@@ -2195,6 +2198,7 @@ int imfit_ModelObject_new(int device, imfit_model_t *out) {
     e = cudaEventCreateWithFlags(&m->forkEv[i], cudaEventDisableTiming);
     if (!e) e = cudaEventCreateWithFlags(&m->joinEv[i], cudaEventDisableTiming);
   }
+  if (!e) e = cudaEventCreateWithFlags(&m->subEv, cudaEventDisableTiming);
   if (e) {
     g_createError = std::string("stream/event creation: ") + cudaGetErrorString(e);
     delete m;

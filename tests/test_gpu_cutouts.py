@@ -169,6 +169,7 @@ def test_cutout_set_jtwj_equals_single_images(gpu, oracle_mod):
             d, s, p = imgs[i]
             assert relerr(S[r], _single(oracle_mod.OracleModel, d, s, p).get_fit_statistic(P[i])) < 1e-5
             g = _single(gpu.ModelObject, d, s, p)
+            g.set_fft_plan(0, 0)  # the set's plan: smallest 7-smooth lengths, first radix order
             s1, a1, b1 = g.jtwj(P[i])
             assert relerr(S[r], s1) < 1e-5
             dd = np.sqrt(np.outer(np.diag(a1), np.diag(a1)))

@@ -293,8 +293,8 @@ def test_multimfit_per_image_functions(gpu, oracle_mod, tmp_path):
     from imfit_gb300.multimage import MultiImageModel, build_handles, global_vector, parse_image_info
     data, (o1, o2), glob, local = _per_image_setup(oracle_mod)
     for k, img in enumerate(data):
-        fits.write_image(str(tmp_path / f"im{k}.fits"), img)
-        fits.write_image(str(tmp_path / f"sig{k}.fits"), np.full(img.shape, 2.0))
+        fits.write_image(str(tmp_path / f"im{k}.fits"), img, bitpix=-64)  # FP64: the oracle's own data
+        fits.write_image(str(tmp_path / f"sig{k}.fits"), np.full(img.shape, 2.0), bitpix=-64)
     (tmp_path / "c.dat").write_text(PER_IMAGE_CFG)
     (tmp_path / "info.txt").write_text(f"""IMAGE_START
 DATA {tmp_path / 'im0.fits'}
@@ -342,7 +342,8 @@ Y0 22.0 18,28
     assert np.all(np.abs(r["params"] - truth) <= 1e-3 * np.maximum(np.abs(truth), 1.0)), (r["params"], truth)
     buf = io.StringIO()
     p_cli, s_cli = cli.multimfit([str(tmp_path / "c.dat"), "-i", str(tmp_path / "info.txt")], out=buf)
-    assert len(p_cli) == mm.n_params and s_cli < 1e-6
+    # noise-free data: the minimum is 0 up to the FP32 evaluation's floor (start: ~7e4)
+    assert len(p_cli) == mm.n_params and s_cli < 1e-3
     assert "# Per-image function parameters for image 2" in buf.getvalue()
     assert np.all(np.abs(p_cli - truth) <= 1e-3 * np.maximum(np.abs(truth), 1.0))
 
