@@ -312,7 +312,18 @@ struct SetupFP64 {
   double bn, dbn;       // Sersic b_n and db_n/dn
   double log2re;        // Sersic log2(r_e)
   double t;             // Moffat 2^(1/beta)
+  // reciprocals, each computed by its own warp before the record is assembled
+  double invq;          // 1 / (1 - ell)
+  double inv3, inv4;    // 1 / p[3], 1 / p[4] (the types that divide by them)
+  double invn;          // Sersic 1 / n
 };
+
+// Which reciprocals of SetupFP64 a type uses (setup work split over warps).
+__host__ __device__ inline bool uses_invq(int t) {
+  return t == F_SERSIC || t == F_EXP || t == F_GRING || t == F_MOFFAT || t == F_GAUSS;
+}
+__host__ __device__ inline bool uses_inv3(int t) { return t == F_EXP || t == F_MOFFAT || t == F_GAUSS; }
+__host__ __device__ inline bool uses_inv4(int t) { return t == F_SERSIC || t == F_GRING; }
 
 // b_n written in powers of 1/n (one division), same coefficients as
 // function_objects/helper_funcs.cpp:14-29
@@ -351,26 +362,26 @@ __device__ inline void comp_setup32(CompF32 &o, const CompDesc &d, const double 
   switch (d.type) {
     case F_SERSIC: {
       const double qq = 1.0 - p[1], n = p[2];
-      o.q = (float)qq; o.invq = (float)(1.0 / qq);
+      o.q = (float)qq; o.invq = (float)q.invq;
       o.s0 = (float)p[3];
       o.s1 = (float)(q.bn * kLog2e);
       o.s2 = (float)q.log2re;
-      o.s3 = (float)(1.0 / n);
+      o.s3 = (float)q.invn;
       o.s4 = (float)q.bn;
       o.s5 = (float)q.dbn;
       o.s6 = (float)n;
       o.s7 = (float)p[4];
       o.subScale = (float)p[4]; o.subInner = 4.f; o.subSmallK = 20.f;
-      o.pad = (float)(1.0 / p[4]);  // 1/r_e
+      o.pad = (float)q.inv4;  // 1/r_e
       break;
     }
     case F_EXP: {
       const double qq = 1.0 - p[1];
-      o.q = (float)qq; o.invq = (float)(1.0 / qq);
+      o.q = (float)qq; o.invq = (float)q.invq;
       o.s0 = (float)p[2];
-      o.s1 = (float)(kLog2e / p[3]);
+      o.s1 = (float)(kLog2e * q.inv3);
       o.s2 = (float)p[3];
-      o.s3 = (float)(1.0 / p[3]);  // 1/h
+      o.s3 = (float)q.inv3;  // 1/h
       o.subScale = (float)p[3]; o.subInner = 3.f; o.subSmallK = 20.f;
       break;
     }
@@ -383,21 +394,21 @@ __device__ inline void comp_setup32(CompF32 &o, const CompDesc &d, const double 
       o.s2 = (float)p[2];
       break;
     case F_GRING: {
-      const double qq = 1.0 - p[1];
-      o.q = (float)qq; o.invq = (float)(1.0 / qq);
+      const double qq = 1.0 - p[1], is2 = q.inv4 * q.inv4;
+      o.q = (float)qq; o.invq = (float)q.invq;
       o.s0 = (float)p[2];
       o.s1 = (float)p[3];
-      o.s2 = (float)(kLog2e / (2.0 * p[4] * p[4]));
+      o.s2 = (float)(0.5 * kLog2e * is2);
       o.s3 = (float)p[4];
-      o.s4 = (float)(1.0 / (p[4] * p[4]));  // 1/sigma^2
-      o.pad = (float)(1.0 / p[4]);          // 1/sigma
+      o.s4 = (float)is2;       // 1/sigma^2
+      o.pad = (float)q.inv4;   // 1/sigma
       break;
     }
     case F_MOFFAT: {
       const double qq = 1.0 - p[1];
       const double beta = p[4], fwhm = p[3], t = q.t;
       const double alpha = 0.5 * fwhm / sqrt(t - 1.0);
-      o.q = (float)qq; o.invq = (float)(1.0 / qq);
+      o.q = (float)qq; o.invq = (float)q.invq;
       o.s0 = (float)p[2];
       o.s1 = (float)(1.0 / (alpha * alpha));
       o.s2 = (float)beta;
@@ -405,18 +416,18 @@ __device__ inline void comp_setup32(CompF32 &o, const CompDesc &d, const double 
       o.s4 = (float)fwhm;
       o.s5 = (float)(alpha * t * kLn2 / (2.0 * beta * beta * (t - 1.0)));
       o.s6 = (float)(1.0 / alpha);
-      o.s7 = (float)(1.0 / fwhm);
+      o.s7 = (float)q.inv3;  // 1/fwhm
       o.subScale = (float)alpha; o.subInner = 3.f; o.subSmallK = 40.f;
       break;
     }
     case F_GAUSS: {
-      const double qq = 1.0 - p[1];
-      o.q = (float)qq; o.invq = (float)(1.0 / qq);
+      const double qq = 1.0 - p[1], is2 = q.inv3 * q.inv3;
+      o.q = (float)qq; o.invq = (float)q.invq;
       o.s0 = (float)p[2];
-      o.s1 = (float)(kLog2e / (2.0 * p[3] * p[3]));
+      o.s1 = (float)(0.5 * kLog2e * is2);
       o.s2 = (float)p[3];
-      o.s3 = (float)(1.0 / p[3]);  // 1/sigma
-      o.s4 = (float)(1.0 / (p[3] * p[3]));
+      o.s3 = (float)q.inv3;  // 1/sigma
+      o.s4 = (float)is2;
       o.subScale = (float)p[3]; o.subInner = 3.f; o.subSmallK = 40.f;
       break;
     }

@@ -95,35 +95,59 @@ __device__ __forceinline__ int sub_count(const CompF32 &c, const Geo &g) {
 
 // --------------------------------------------------------------- setup
 // FP64 Setup of component c of parameter vector b into rec (FunctionObject::
-// Setup, core/model_object.cpp:1126-1135).  Warp w computes the w-th group of
-// FP64 transcendentals, thread 0 assembles the FP32 record; all threads of
-// the CTA (at least 128) call it.  With bg, also the constant background
-// levels of vector b (FlatSky sum x sum of the PSF, main and region).
+// Setup, core/model_object.cpp:1126-1135).  Each FP64 quantity -- the
+// orientation (sincospi), Sersic b_n and log2 r_e, Moffat 2^(1/beta), the
+// reciprocals the record needs, the background levels -- is computed by its
+// own warp (FP64 operations have long latencies here: a transcendental takes
+// about a microsecond), thread 0 then only assembles the FP32 record; all
+// threads of the CTA call it.  With bg, also the constant background levels
+// of vector b (FlatSky sum x sum of the PSF, main and region).
 __device__ void setup_component(const FastArgs &a, int c, int b, CompF32 &rec, bool bg) {
   __shared__ SetupFP64 q;
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   const CompDesc d = a.desc[c];
   const double *P = a.params + (long)b * a.nParams;
   const double *p = P + d.paramOffset;
   if (lane == 0) {
-    if (w == 0) {
-      if (has_pa(d.type)) {
-        double sn, cs;
-        sincospi((p[0] + 90.0) / 180.0, &sn, &cs);
-        q.cosPA = cs;
-        q.sinPA = sn;
+    for (int task = w; task < 8; task += nw) {
+      switch (task) {
+        case 0:
+          if (has_pa(d.type)) {
+            double sn, cs;
+            sincospi((p[0] + 90.0) * (1.0 / 180.0), &sn, &cs);
+            q.cosPA = cs;
+            q.sinPA = sn;
+          }
+          break;
+        case 1:
+          if (d.type == F_SERSIC) sersic_bn_horner(p[2], q.bn, q.dbn);
+          if (d.type == F_MOFFAT) q.t = exp2(1.0 / p[4]);
+          break;
+        case 2:
+          if (d.type == F_SERSIC) q.log2re = log2(p[4]);
+          break;
+        case 3:
+          if (bg) {
+            double s = 0.0;
+            for (int k = 0; k < a.nComp; k++)
+              if (a.desc[k].background) s += P[a.desc[k].paramOffset];
+            a.bgLevel[2 * b] = (float)(s * a.psfSum);
+            a.bgLevel[2 * b + 1] = (float)(s * a.psfSumOs);
+          }
+          break;
+        case 4:
+          if (uses_invq(d.type)) q.invq = 1.0 / (1.0 - p[1]);
+          break;
+        case 5:
+          if (uses_inv3(d.type)) q.inv3 = 1.0 / p[3];
+          break;
+        case 6:
+          if (uses_inv4(d.type)) q.inv4 = 1.0 / p[4];
+          break;
+        default:
+          if (d.type == F_SERSIC) q.invn = 1.0 / p[2];
+          break;
       }
-    } else if (w == 1) {
-      if (d.type == F_SERSIC) sersic_bn_horner(p[2], q.bn, q.dbn);
-      if (d.type == F_MOFFAT) q.t = exp2(1.0 / p[4]);
-    } else if (w == 2) {
-      if (d.type == F_SERSIC) q.log2re = log2(p[4]);
-    } else if (w == 3 && bg) {
-      double s = 0.0;
-      for (int k = 0; k < a.nComp; k++)
-        if (a.desc[k].background) s += P[a.desc[k].paramOffset];
-      a.bgLevel[2 * b] = (float)(s * a.psfSum);
-      a.bgLevel[2 * b + 1] = (float)(s * a.psfSumOs);
     }
   }
   __syncthreads();
@@ -181,68 +205,243 @@ __device__ __forceinline__ void subsample_sum(const CompF32 &cc, int ns, float x
   }
 }
 
-// First kernel of an evaluation.  CTA (x, c, b) sets up component c of
-// parameter vector b in FP64 (the CTA with x = 0 publishes the record, and for
-// c = 0 the background levels and a zeroed completion counter for the final
-// reduction), then precomputes the subsampled pixels of component c: one warp
-// per box pixel (grid-stride), the average over the pixel's ns x ns
-// subsamples of the profile and of its 7 derivatives (X0, Y0, then the
-// function parameters).  CTAs [0, nMainCtas) cover the main window's box, the
-// rest the oversampled region's.
-__global__ void __launch_bounds__(256) k_fast_subsample(FastArgs a, WinDesc mw, WinDesc rw, int nMainCtas,
-                                                        int publish) {
+constexpr int kLatN = 20;  // subsample count of the shared lattice (see k_fast_region_lattice)
+
+// Subsampled box pixels of one window.  The CTAs of (component, vector) take
+// the box pixels round-robin (pixel p to CTA p mod gridDim), blockDim at a
+// time: every thread classifies one pixel, the pixels that subsample go to
+// two shared lists, and then
+//   * pixels with at most kThreadNs^2 subsamples are summed by groups of
+//     kGroup lanes (the lanes split the subsamples, a shuffle tree adds them);
+//   * larger ones by a whole warp each -- lanes split the subsamples or, in
+//     the oversampled region, pixels on the shared lattice sum their block of
+//     it (lane i takes block column i).
+// Table entry: [value, X0, Y0, function parameters...] averaged.
+constexpr int kThreadNs = 5;
+constexpr int kGroup = 8;
+
+struct LatView {
+  const float *lat;  // [8][U][U] of this (vector, component), or null
+  int U, q0, q1, m;
+};
+
+template <int TY>
+__device__ void subsample_pixels(const WinDesc &w, const CompF32 &cc, int side, int col0, int row0, float *tab,
+                                 const LatView &L) {
+  __shared__ int smallList[256], bigList[256];
+  __shared__ int nSmall, nBig;
+  constexpr int NP = n_fparams<TY>();
+  const int lane = threadIdx.x & 31, nw = blockDim.x >> 5, warp = threadIdx.x >> 5;
+  const FastDiv bySide(side);
+  const int area = side * side;
+  const int perCta = (area - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
+  auto offsets = [&](int p, int &pr, int &pc, float &dx, float &dy) {
+    pr = bySide.div(p);
+    pc = p - pr * side;
+    const int row = row0 + pr, col = col0 + pc;
+    if (row < 0 || row >= w.rows || col < 0 || col >= w.cols) return false;
+    win_offsets(w, cc, row, col, dx, dy);
+    return true;
+  };
+  for (int base = 0; base < perCta; base += blockDim.x) {
+    if (threadIdx.x == 0) nSmall = nBig = 0;
+    __syncthreads();
+    const int i = base + (int)threadIdx.x;
+    if (i < perCta) {
+      const int p = (int)blockIdx.x + i * (int)gridDim.x;
+      int pr, pc;
+      float dx, dy;
+      if (offsets(p, pr, pc, dx, dy)) {
+        const int ns = sub_count(cc, geo32(cc, dx, dy));
+        if (ns > kThreadNs)
+          bigList[atomicAdd(&nBig, 1)] = p;
+        else if (ns > 1)
+          smallList[atomicAdd(&nSmall, 1)] = p;
+      }
+    }
+    __syncthreads();
+    // small counts: kGroup lanes per pixel, 32 / kGroup pixels per warp pass
+    // (the loop bound is uniform over the warp: every lane reaches the shuffles)
+    constexpr int kPer = 32 / kGroup;
+    const int gl = lane % kGroup;
+    for (int e0 = warp * kPer; e0 < nSmall; e0 += nw * kPer) {
+      const int e = e0 + lane / kGroup;
+      int ns = 0, p = 0;
+      float dx = 0.f, dy = 0.f;
+      if (e < nSmall) {
+        int pr, pc;
+        p = smallList[e];
+        offsets(p, pr, pc, dx, dy);
+        ns = sub_count(cc, geo32(cc, dx, dy));
+      }
+      const float d = ns > 0 ? 1.f / ns : 0.f, xs = dx - 0.5f + 0.5f * d, ys = dy - 0.5f + 0.5f * d;
+      float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      float o[7];
+      for (int t = gl; t < ns * ns; t += kGroup) {
+        const int ii = t / ns, jj = t - ii * ns;
+        const Geo gs = geo32(cc, xs + ii * d, ys + jj * d);
+        float v;
+        radial_grad_t<TY>(cc, gs, 1.f, o, &v);
+        acc[0] += v;
+#pragma unroll
+        for (int q = 0; q < 2 + NP; q++) acc[1 + q] += o[q];
+      }
+#pragma unroll
+      for (int q = 0; q < 8; q++)
+#pragma unroll
+        for (int off = kGroup / 2; off > 0; off >>= 1) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], off);
+      if (gl == 0 && ns > 0) {
+        float *dst = tab + (long)p * 8;
+#pragma unroll
+        for (int q = 0; q < 8; q++) dst[q] = acc[q] * (d * d);
+      }
+    }
+    // large counts: one warp per pixel
+    for (int e = warp; e < nBig; e += nw) {
+      const int p = bigList[e];
+      int pr, pc;
+      float dx, dy;
+      offsets(p, pr, pc, dx, dy);
+      const int ns = sub_count(cc, geo32(cc, dx, dy));
+      const float d = 1.f / ns;
+      float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      if (L.lat && ns == kLatN && pr >= L.q0 && pr <= L.q1 && pc >= L.q0 && pc <= L.q1) {
+        if (lane < kLatN) {  // lane i: block column i (consecutive lanes read consecutive floats)
+          const long ch = (long)L.U * L.U;
+          const float *col = L.lat + (long)((pr - L.q0) * L.m) * L.U + (pc - L.q0) * L.m + lane;
+#pragma unroll
+          for (int q = 0; q < 8; q++) {
+            float t = 0.f;
+#pragma unroll
+            for (int k = 0; k < kLatN; k++) t += col[q * ch + (long)k * L.U];
+            acc[q] = t;
+          }
+        }
+      } else {
+        subsample_sum<TY>(cc, ns, dx - 0.5f + 0.5f * d, dy - 0.5f + 0.5f * d, d, lane, acc);
+      }
+#pragma unroll
+      for (int q = 0; q < 8; q++) acc[q] = warp_sum(acc[q]);
+      if (lane == 0) {
+        float *dst = tab + (long)p * 8;
+#pragma unroll
+        for (int q = 0; q < 8; q++) dst[q] = acc[q] * (d * d);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// First kernel of an evaluation: CTA (c, b) sets up component c of parameter
+// vector b in FP64 and publishes the FP32 record, the subsample boxes of both
+// windows and, for c = 0, the background levels and a zeroed completion
+// counter for the final reduction.
+__global__ void __launch_bounds__(256) k_fast_setup(FastArgs a, WinDesc mw, WinDesc rw, int hasRegion) {
+  pdl_wait();
+  const int c = blockIdx.x, b = blockIdx.y;
+  __shared__ CompF32 rec;
+  setup_component(a, c, b, rec, c == 0);
+  if (threadIdx.x == 0) {
+    a.comps[b * a.nComp + c] = rec;
+    if (c == 0 && a.done) a.done[b] = 0u;
+    if (rec.subsample && subsampling_type(rec.type)) {
+      int *o = a.subBox + ((long)b * a.nComp + c) * 4;
+      box_origin(mw, rec, a.boxMain, o[0], o[1]);
+      if (hasRegion) box_origin(rw, rec, a.boxReg, o[2], o[3]);
+    }
+  }
+}
+
+// Subsampled pixels of the main window: one warp per box pixel (grid-stride
+// over the CTAs of component c, vector b), the average over the pixel's
+// ns x ns subsamples of the profile and of its 7 derivatives (X0, Y0, then
+// the function parameters).
+__global__ void __launch_bounds__(256) k_fast_subsample(FastArgs a, WinDesc w) {
   pdl_wait();
   const int b = blockIdx.z, c = blockIdx.y;
-  const bool subs = a.desc[c].subsample && subsampling_type(a.desc[c].type);
-  if ((blockIdx.x != 0 || !publish) && !subs) return;
-  __shared__ CompF32 rec;
-  setup_component(a, c, b, rec, publish && blockIdx.x == 0 && c == 0);
-  const CompF32 cc = rec;
-  if (publish && blockIdx.x == 0 && threadIdx.x == 0) {
-    a.comps[b * a.nComp + c] = cc;
-    if (c == 0 && a.done) a.done[b] = 0u;
-  }
+  const CompF32 cc = a.comps[b * a.nComp + c];
   if (!cc.subsample || !subsampling_type(cc.type)) return;
-  const int win = (int)blockIdx.x >= nMainCtas ? 1 : 0;
-  const WinDesc &w = win ? rw : mw;
-  const int cta = win ? (int)blockIdx.x - nMainCtas : (int)blockIdx.x;
-  const int nCtas = win ? (int)gridDim.x - nMainCtas : nMainCtas;
-  const int side = win ? a.boxReg : a.boxMain;
-  int col0, row0;
-  box_origin(w, cc, side, col0, row0);
-  if (cta == 0 && threadIdx.x == 0) {
-    int *o = a.subBox + (((long)b * a.nComp + c) * 2 + win) * 2;
-    o[0] = col0;
-    o[1] = row0;
+  const int *o = a.subBox + ((long)b * a.nComp + c) * 4;
+  float *tab = a.subTab + sub_base(a, b, c, 0);
+  const LatView none{nullptr, 0, 0, 0, 0};
+  switch (cc.type) {
+    case F_SERSIC: subsample_pixels<F_SERSIC>(w, cc, a.boxMain, o[0], o[1], tab, none); break;
+    case F_EXP: subsample_pixels<F_EXP>(w, cc, a.boxMain, o[0], o[1], tab, none); break;
+    case F_MOFFAT: subsample_pixels<F_MOFFAT>(w, cc, a.boxMain, o[0], o[1], tab, none); break;
+    default: subsample_pixels<F_GAUSS>(w, cc, a.boxMain, o[0], o[1], tab, none); break;
   }
-  const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  const FastDiv bySide(side);
-  for (int p = cta * nw + (threadIdx.x >> 5); p < side * side; p += nCtas * nw) {
-    const int pr = bySide.div(p);
-    const int row = row0 + pr, col = col0 + (p - pr * side);
-    if (row < 0 || row >= w.rows || col < 0 || col >= w.cols) continue;
-    float dx, dy;
-    win_offsets(w, cc, row, col, dx, dy);
-    const Geo g = geo32(cc, dx, dy);
-    const int ns = sub_count(cc, g);
-    if (ns <= 1) continue;
-    const float d = 1.f / ns;
-    const float xs = dx - 0.5f + 0.5f * d, ys = dy - 0.5f + 0.5f * d;
-    float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    switch (cc.type) {
-      case F_SERSIC: subsample_sum<F_SERSIC>(cc, ns, xs, ys, d, lane, acc); break;
-      case F_EXP: subsample_sum<F_EXP>(cc, ns, xs, ys, d, lane, acc); break;
-      case F_MOFFAT: subsample_sum<F_MOFFAT>(cc, ns, xs, ys, d, lane, acc); break;
-      default: subsample_sum<F_GAUSS>(cc, ns, xs, ys, d, lane, acc); break;
-    }
+}
+
+// ------------------------------- oversampled region: shared subsample lattice
+// In an oversampled region (scale k) the subsamples of a pixel span a whole
+// main-image pixel around its centre (the function's own GetValue, e.g.
+// func_sersic.cpp:163-183, called at the subpixel centres), so neighbouring
+// subpixels' subsample grids overlap.  The pixels within the constant-count
+// radius have kLatN x kLatN subsamples; when k divides kLatN they all lie on
+// one lattice of spacing 1 / kLatN, pixel (br, bc) covering the kLatN x kLatN
+// block that starts at ((br - q0) m, (bc - q0) m), m = kLatN / k.  The
+// lattice over the box pixels [q0, q0 + 2h] (h = a.latHalf, which covers
+// radius 4 around the centre; q0 = side / 2 - h) is evaluated once, one
+// thread per point (k_fast_region_lattice), and those pixels' table entries
+// are its block sums (k_fast_region_sub, lane i summing block column i).  For
+// the 1024x1024 benchmark model with its 40x40 region at k = 5: 2 x 188^2
+// lattice points plus about 78,000 direct subsamples instead of 714,000
+// direct subsamples.
+
+template <int TY>
+__device__ __forceinline__ void lattice_point(const CompF32 &cc, float x, float y, float *dst, long chStride) {
+  constexpr int C = 3 + n_fparams<TY>();
+  const Geo gs = geo32(cc, x, y);
+  float o[7], v;
+  radial_grad_t<TY>(cc, gs, 1.f, o, &v);
+  dst[0] = v;
 #pragma unroll
-    for (int q = 0; q < 8; q++) acc[q] = warp_sum(acc[q]);
-    if (lane == 0) {
-      float *dst = a.subTab + sub_base(a, b, c, win) + (long)p * 8;
-      const float dd = d * d;
+  for (int q = 0; q < C - 1; q++) dst[(q + 1) * chStride] = o[q];
 #pragma unroll
-      for (int q = 0; q < 8; q++) dst[q] = acc[q] * dd;
-    }
+  for (int q = C; q < 8; q++) dst[q * chStride] = 0.f;
+}
+
+__global__ void __launch_bounds__(256) k_fast_region_lattice(FastArgs a, WinDesc w) {
+  pdl_wait();
+  const int b = blockIdx.z, c = blockIdx.y;
+  const CompF32 cc = a.comps[b * a.nComp + c];
+  if (!cc.subsample || !subsampling_type(cc.type)) return;
+  const int U = a.latSide, side = a.boxReg, q0 = side / 2 - a.latHalf;
+  const int pt = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pt >= U * U) return;
+  const int yb = pt / U, xa = pt - yb * U;
+  const int *o = a.subBox + ((long)b * a.nComp + c) * 4;
+  float dx0, dy0;
+  win_offsets(w, cc, o[3] + q0, o[2] + q0, dx0, dy0);
+  const float d = 1.f / kLatN;
+  const float x = dx0 - 0.5f + 0.5f * d + (float)xa * d, y = dy0 - 0.5f + 0.5f * d + (float)yb * d;
+  const long chStride = (long)U * U;
+  float *dst = a.lat + ((long)b * a.nComp + c) * 8 * chStride + pt;
+  switch (cc.type) {
+    case F_SERSIC: lattice_point<F_SERSIC>(cc, x, y, dst, chStride); break;
+    case F_EXP: lattice_point<F_EXP>(cc, x, y, dst, chStride); break;
+    case F_MOFFAT: lattice_point<F_MOFFAT>(cc, x, y, dst, chStride); break;
+    default: lattice_point<F_GAUSS>(cc, x, y, dst, chStride); break;
+  }
+}
+
+// Subsampled pixels of the oversampled region (subsample_pixels, with the
+// shared lattice when there is one).
+__global__ void __launch_bounds__(256) k_fast_region_sub(FastArgs a, WinDesc w) {
+  pdl_wait();
+  const int b = blockIdx.z, c = blockIdx.y;
+  const CompF32 cc = a.comps[b * a.nComp + c];
+  if (!cc.subsample || !subsampling_type(cc.type)) return;
+  const int side = a.boxReg;
+  const int *o = a.subBox + ((long)b * a.nComp + c) * 4;
+  float *tab = a.subTab + sub_base(a, b, c, 1);
+  LatView L{nullptr, a.latSide, side / 2 - a.latHalf, side / 2 + a.latHalf, kLatN / w.scale};
+  if (a.lat) L.lat = a.lat + ((long)b * a.nComp + c) * 8 * (long)a.latSide * a.latSide;
+  switch (cc.type) {
+    case F_SERSIC: subsample_pixels<F_SERSIC>(w, cc, side, o[2], o[3], tab, L); break;
+    case F_EXP: subsample_pixels<F_EXP>(w, cc, side, o[2], o[3], tab, L); break;
+    case F_MOFFAT: subsample_pixels<F_MOFFAT>(w, cc, side, o[2], o[3], tab, L); break;
+    default: subsample_pixels<F_GAUSS>(w, cc, side, o[2], o[3], tab, L); break;
   }
 }
 
@@ -1470,21 +1669,33 @@ static void ensure_smem(K kern, size_t bytes) {
   allow_max_smem((const void *)kern);
 }
 
-// Set-up + subsample tables: CTAs per (component, vector) and window chosen
-// so that the grid is about one wave of 8 CTAs per SM (each CTA repeats the
-// component's FP64 set-up once), at most one warp per box pixel.  windows:
-// 1 the main window (publishes the component records, background levels and
-// completion counters), 2 the oversampled region only (on the side stream,
-// concurrently with 1), 3 both in one launch.
-static cudaError_t launch_subsample(const FastArgs &a, const WinDesc &mw, const WinDesc &rw, int windows, int nBatch,
-                                    cudaStream_t st) {
-  const bool wm = windows & 1, wr = (windows & 2) != 0;
-  const int sets = a.nComp * nBatch * ((wm ? 1 : 0) + (wr ? 1 : 0));
-  const int cap = std::max(1, 8 * 152 / std::max(sets, 1));
-  const int nMain = wm ? std::max(1, std::min((a.boxMain * a.boxMain + 7) / 8, cap)) : 0;
-  const int nReg = wr ? std::max(1, std::min((a.boxReg * a.boxReg + 7) / 8, cap)) : 0;
-  dim3 grid(nMain + nReg, a.nComp, nBatch);
-  return launch_pdl(k_fast_subsample, grid, dim3(256), 0, st, a, wm ? mw : rw, wr ? rw : mw, nMain, wm ? 1 : 0);
+// Set-up: one CTA per (component, vector).
+static cudaError_t launch_setup(const FastArgs &a, const WinDesc &mw, const WinDesc &rw, bool region, int nBatch,
+                                cudaStream_t st) {
+  return launch_pdl(k_fast_setup, dim3(a.nComp, nBatch), dim3(256), 0, st, a, mw, rw, region ? 1 : 0);
+}
+
+// Subsample table of the main window: CTAs per (component, vector) chosen so
+// that the grid is about one wave of 8 CTAs per SM, at most one warp per box
+// pixel.
+static cudaError_t launch_subsample(const FastArgs &a, const WinDesc &mw, int nBatch, cudaStream_t st) {
+  const int cap = std::max(1, 8 * 152 / std::max(a.nComp * nBatch, 1));
+  const int n = std::max(1, std::min((a.boxMain * a.boxMain + 7) / 8, cap));
+  return launch_pdl(k_fast_subsample, dim3(n, a.nComp, nBatch), dim3(256), 0, st, a, mw);
+}
+
+// Subsample table of the oversampled region: the shared lattice (when the
+// region's scale divides its subsample count), then the table.
+static cudaError_t launch_region_sub(const FastArgs &a, const WinDesc &rw, int nBatch, cudaStream_t st) {
+  cudaError_t e = cudaSuccess;
+  if (a.lat) {
+    const int pts = a.latSide * a.latSide;
+    e = launch_pdl(k_fast_region_lattice, dim3((pts + 255) / 256, a.nComp, nBatch), dim3(256), 0, st, a, rw);
+    if (e) return e;
+  }
+  const int cap = std::max(1, 8 * 152 / std::max(a.nComp * nBatch, 1));
+  const int n = std::max(1, std::min((a.boxReg * a.boxReg + 7) / 8, cap));
+  return launch_pdl(k_fast_region_sub, dim3(n, a.nComp, nBatch), dim3(256), 0, st, a, rw);
 }
 
 static cudaError_t launch_eval(const FastArgs &a, const WinDesc &w, const FFTLen &L, int nBatch, int win,
@@ -1630,24 +1841,14 @@ cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool 
   if (!mks.panels) mks.count = nullptr;
   if (!rks.panels) rks.count = nullptr;
 
-  if (fork && split_subsample_enabled()) {
-    // the region's subsample table on the side stream, concurrently with the
-    // main window's (which publishes the component records the region needs)
+  STAGE("setup", st, launch_setup(a, mw, rw, g.hasRegion != 0, nBatch, st));
+  if (fork) {
     cudaError_t e = cudaEventRecord(p.fork0, st);
     if (!e) e = cudaStreamWaitEvent(rs, p.fork0, 0);
     if (e) return e;
-    STAGE("subsample", st, launch_subsample(a, mw, rw, 1, nBatch, st));
-    if ((e = cudaEventRecord(p.sub0, st))) return e;
-    STAGE("region_subsample", rs, launch_subsample(a, mw, rw, 2, nBatch, rs));
-    if ((e = cudaStreamWaitEvent(rs, p.sub0, 0))) return e;
-  } else {
-    STAGE("subsample", st, launch_subsample(a, mw, rw, g.hasRegion ? 3 : 1, nBatch, st));
-    if (fork) {
-      cudaError_t e = cudaEventRecord(p.fork0, st);
-      if (!e) e = cudaStreamWaitEvent(rs, p.fork0, 0);
-      if (e) return e;
-    }
   }
+  if (g.hasRegion) STAGE("region_subsample", rs, launch_region_sub(a, rw, nBatch, rs));
+  STAGE("subsample", st, launch_subsample(a, mw, nBatch, st));
   if (g.hasRegion) {
     if (los) STAGE("region_los_eval", rs, launch_los_eval(a, rw, nBatch, rks, rs));
     STAGE("region_eval_r2c", rs, launch_eval(a, rw, *p.Rx, nBatch, 1, tu, rs));

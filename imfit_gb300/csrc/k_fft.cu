@@ -296,16 +296,6 @@ bool fft_pad_enabled() {
   return on;
 }
 
-// Oversampled-region subsample table on the side stream, concurrently with
-// the main window's; IMFIT_SPLIT_SUBSAMPLE=0 computes both in one launch.
-bool split_subsample_enabled() {
-  static const bool on = [] {
-    const char *v = getenv("IMFIT_SPLIT_SUBSAMPLE");
-    return !(v && v[0] == '0');
-  }();
-  return on;
-}
-
 void allow_max_smem(const void *kernel) {
   static std::mutex lock;
   static std::set<std::pair<int, const void *>> done;
@@ -375,10 +365,12 @@ int smooth_candidates(int n, bool even, int count, double maxRatio, int *out) {
 // read consecutive entries (no shared-memory bank conflicts once staged);
 // each value is the one a single table exp(-2 pi i m / n) holds at
 // m = r k n / (Ns R).
-static cudaError_t table_create(FFTTable &t, int n, int variant) {
+static cudaError_t table_create(FFTTable &t, int n, int variant, bool reversed = false) {
   t.n = n;
   t.npass = radix_schedule(n, t.radix, variant);
   if (t.npass < 0) return cudaErrorInvalidValue;
+  if (reversed)
+    for (int i = 0, j = t.npass - 1; i < j; i++, j--) std::swap(t.radix[i], t.radix[j]);
   std::vector<double> full(2 * (size_t)n);
   for (int k = 0; k < n; k++) {
     const double a = 2.0 * M_PI * (double)k / (double)n;
@@ -413,6 +405,8 @@ cudaError_t fftlen_create(FFTLen &L, int len, int variant) {
   L.variant = variant;
   cudaError_t e = table_create(L.full, len, variant);
   if (e) return e;
+  e = table_create(L.fullRev, len, variant, true);
+  if (e) return e;
   if (len % 2 == 0) {
     e = table_create(L.half, len / 2, variant);
     if (e) return e;
@@ -445,6 +439,7 @@ static void table_destroy(FFTTable &t) {
 
 void fftlen_destroy(FFTLen &L) {
   table_destroy(L.full);
+  table_destroy(L.fullRev);
   table_destroy(L.half);
   if (L.twL64) cudaFree(L.twL64);
   if (L.twL32) cudaFree(L.twL32);

@@ -24,7 +24,6 @@ __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.lau
 
 bool pdl_enabled();
 bool fft_pad_enabled();
-bool split_subsample_enabled();
 
 template <typename... KArgs, typename... Args>
 cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
@@ -65,6 +64,7 @@ struct FFTLen {
   int variant = 0;  // radix order (radix_schedule)
   FFTTable half;
   FFTTable full;
+  FFTTable fullRev;  // full length, radices in reverse order (the column pass's inverse half)
   void *twL64 = nullptr;
   void *twL32 = nullptr;
 };
@@ -253,6 +253,11 @@ struct FastArgs {
   float *subTab;         // [B][nComp][2 windows][boxArea(w)][8]
   int *subBox;           // [B][nComp][2][2]  box origin (col, row) in window coordinates
   int boxMain, boxReg;   // box sides (pixels)
+  // oversampled region: the shared subsample lattice (null when the region's
+  // scale does not divide its subsample count), [B][nComp][8][latSide^2],
+  // over the box pixels within latHalf of the box centre
+  float *lat;
+  int latSide, latHalf;
   // 3-D (line-of-sight) components, when the model has any: per window
   // pixel the summed line-of-sight values and the adjoint r~, main window and
   // region window, [B][rows][cols] each (all null otherwise)
@@ -303,7 +308,6 @@ struct FastPlan {
   // and the events that fork it from / join it back to the main stream
   cudaStream_t side = nullptr;
   cudaEvent_t fork0 = nullptr, join0 = nullptr, fork1 = nullptr, join1 = nullptr;
-  cudaEvent_t sub0 = nullptr;  // main window's subsample table done (component records published)
   FastGeom g;
   const FFTLen *Lx, *Ly, *Rx, *Ry;  // main and region lengths
   const void *H, *Hr;               // FP32 PSF spectra (main, region)

@@ -278,6 +278,7 @@ struct imfit_model_s {
   DevBuf<CompF32> dComps32;
   DevBuf<float> dSubTab;
   DevBuf<int> dSubBox;
+  DevBuf<float> dLat;  // oversampled region's subsample lattice
   DevBuf<double> dParams, dStat, dGrad;
   DevBuf<float2> dStatPart, dGradPart;
   // image stack (fast path only): batch entry b has its own image, weights and PSF
@@ -353,7 +354,7 @@ struct imfit_model_s {
   bool timing = false;
   std::string timingStage;           // empty: time every kernel (serially)
   cudaStream_t side = nullptr;       // oversampled-region pipeline
-  cudaEvent_t forkEv[2] = {nullptr, nullptr}, joinEv[2] = {nullptr, nullptr}, subEv = nullptr;
+  cudaEvent_t forkEv[2] = {nullptr, nullptr}, joinEv[2] = {nullptr, nullptr};
   bool concurrent = true;
 
   ~imfit_model_s() {
@@ -377,7 +378,6 @@ struct imfit_model_s {
       if (forkEv[i]) cudaEventDestroy(forkEv[i]);
       if (joinEv[i]) cudaEventDestroy(joinEv[i]);
     }
-    if (subEv) cudaEventDestroy(subEv);
     if (side) cudaStreamDestroy(side);
     if (stream) cudaStreamDestroy(stream);
   }
@@ -1307,6 +1307,7 @@ struct imfit_model_s {
     const long area = (long)kBoxMain * kBoxMain + (long)boxReg() * boxReg();
     if (!e) e = dSubTab.reserve((size_t)B * nC * area * 8);
     if (!e) e = dSubBox.reserve((size_t)B * nC * 4);
+    if (!e && latSide() > 0) e = dLat.reserve((size_t)B * nC * 8 * latSide() * latSide());
     if (!e && hasLos) {
       const size_t mw = (size_t)B * g.winRows * g.winCols, rw = (size_t)B * g.rWinRows * g.rWinCols;
       e = dLosVal32.reserve(mw);
@@ -1336,6 +1337,14 @@ struct imfit_model_s {
     return std::max(fg.nDataRows, fg.winRows + (fg.hasRegion ? fg.rWinRows : 0) + los);
   }
   int boxReg() const { return fg.hasRegion ? 20 * fg.rScale + 5 : 0; }
+  // the region's subsample lattice: pixels within radius 4 of a centre (every
+  // pixel with the constant 20 x 20 count) lie within 4k + 1 box pixels of the
+  // box centre; 20 / k lattice points per pixel step
+  int latHalf() const { return 4 * fg.rScale + 1; }
+  int latSide() const {
+    if (!fg.hasRegion || fg.rScale < 1 || 20 % fg.rScale != 0) return 0;
+    return 2 * latHalf() * (20 / fg.rScale) + 20;
+  }
 
   // Point sources: the device descriptors carry each one's current
   // PointSource::oversamplingScale; an evaluation that computes the
@@ -1364,6 +1373,9 @@ struct imfit_model_s {
     a.subBox = dSubBox.p;
     a.boxMain = kBoxMain;
     a.boxReg = boxReg();
+    a.lat = latSide() > 0 ? dLat.p : nullptr;
+    a.latSide = latSide();
+    a.latHalf = latHalf();
     a.desc = dDesc.p;
     a.nComp = (int)funcs.size();
     a.nParams = nParamsTot;
@@ -1432,7 +1444,6 @@ struct imfit_model_s {
       p.fork1 = forkEv[1];
       p.join0 = joinEv[0];
       p.join1 = joinEv[1];
-      p.sub0 = subEv;
     }
     p.g = fg;
     p.Lx = &Fx;
@@ -2198,7 +2209,6 @@ int imfit_ModelObject_new(int device, imfit_model_t *out) {
     e = cudaEventCreateWithFlags(&m->forkEv[i], cudaEventDisableTiming);
     if (!e) e = cudaEventCreateWithFlags(&m->joinEv[i], cudaEventDisableTiming);
   }
-  if (!e) e = cudaEventCreateWithFlags(&m->subEv, cudaEventDisableTiming);
   if (e) {
     g_createError = std::string("stream/event creation: ") + cudaGetErrorString(e);
     delete m;
