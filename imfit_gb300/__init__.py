@@ -87,6 +87,7 @@ _SIGS = [
                          ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     ("imfit_FitLMBatch", _I, [_P, _I, _DP, ctypes.POINTER(_I), _DP, _DP, _D, _I, _DP, ctypes.POINTER(_I),
                               ctypes.POINTER(_I)]),
+    ("imfit_GetLMBatchStats", _I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_L), _DP, _DP]),
     ("imfit_BootstrapFitBatch", _I, [_P, _I, _DP, ctypes.POINTER(_I), _DP, _DP, _D, _I, _DP, _DP,
                                      ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     ("imfit_SetupImageStack", _I, [_P, _I, _I, _I, _DP, _DP, _DP, _I, _I]),
@@ -151,8 +152,9 @@ def exported_symbols():
 
 def radix_schedule(n, order=0):
     """The radices of an n-point transform in the library's order `order`
-    (0: 8, 4, 2 then 3, 5, 7; 1: 7, 5, 3 then 8, 4, 2; 2: 4, 2 then 3, 5, 7)."""
-    seq = {0: (8, 4, 2, 3, 5, 7), 1: (7, 5, 3, 8, 4, 2), 2: (4, 2, 3, 5, 7)}[order]
+    (0: 8, 9, 4, 2 then 3, 5, 7; 1: 7, 5, 9, 3 then 8, 4, 2; 2: 4, 2, 9 then
+    3, 5, 7)."""
+    seq = {0: (8, 9, 4, 2, 3, 5, 7), 1: (7, 5, 9, 3, 8, 4, 2), 2: (4, 2, 9, 3, 5, 7)}[order]
     out = []
     for p in seq:
         while n % p == 0:
@@ -501,6 +503,14 @@ class ModelObject:
                                            _dp(hi) if hi is not None else None, ftol, int(max_iter), _dp(S),
                                            it, st))
         return dict(params=P, statistic=S, niter=np.array(it[:]), status=np.array(st[:]))
+
+    def lm_batch_stats(self):
+        """Timing of the last fit_lm_batch: rounds, problem evaluations, seconds
+        in the J^T W J evaluations and in the whole call."""
+        r, ev, te, tt = _I(), _L(), ctypes.c_double(), ctypes.c_double()
+        self._ck(self.lib.imfit_GetLMBatchStats(self.h, ctypes.byref(r), ctypes.byref(ev), ctypes.byref(te),
+                                                ctypes.byref(tt)))
+        return dict(rounds=r.value, evaluations=ev.value, eval_s=te.value, total_s=tt.value)
 
     def bootstrap_fit_batch(self, n_samples, bestfit, fixed=None, lower=None, upper=None, ftol=1e-8, max_iter=0):
         """The next n_samples bootstrap samples (after use_bootstrap(seed)), all

@@ -7,7 +7,7 @@
 // performs a length-R DFT in registers and writes dst[(j/Ns)*Ns*R + (j mod Ns) + t*Ns]
 // (the self-sorting Stockham formulation), so no bit reversal is needed and
 // the output is in natural order after the last pass.  Lengths are products
-// of 2, 3, 4, 5, 7 and 8; padded sizes are always chosen from that set.
+// of 2, 3, 4, 5, 7, 8 and 9; padded sizes are always chosen from that set.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -153,6 +153,38 @@ __device__ __forceinline__ void dft8(cplx<T> *v, int s) {
   v[7] = csub(e[3], o3);
 }
 
+// length-9 DFT as 3 x 3 (Cooley-Tukey, n = n1 + 3 n2, k = k2 + 3 k1): length-3
+// DFTs over n2, twiddles W9^(n1 k2) with W9 = exp(s 2 pi i / 9), length-3 DFTs
+// over n1; cos / sin of 2 pi e / 9 for e = 1, 2, 4.
+template <typename T>
+__device__ __forceinline__ void dft9(cplx<T> *v, int s) {
+  const T c1 = (T)0.766044443118978035202, s1 = (T)0.642787609686539326323;
+  const T c2 = (T)0.173648177666930348852, s2 = (T)0.984807753012208059367;
+  const T c4 = (T)-0.939692620785908384054, s4 = (T)0.342020143325668733044;
+  cplx<T> y[3][3];
+#pragma unroll
+  for (int n1 = 0; n1 < 3; n1++) {
+    cplx<T> a[3] = {v[n1], v[n1 + 3], v[n1 + 6]};
+    dft3(a, s);
+    y[n1][0] = a[0];
+    y[n1][1] = a[1];
+    y[n1][2] = a[2];
+  }
+  const T sg = (T)s;
+  y[1][1] = cmul(y[1][1], cplx<T>{c1, sg * s1});
+  y[1][2] = cmul(y[1][2], cplx<T>{c2, sg * s2});
+  y[2][1] = cmul(y[2][1], cplx<T>{c2, sg * s2});
+  y[2][2] = cmul(y[2][2], cplx<T>{c4, sg * s4});
+#pragma unroll
+  for (int k2 = 0; k2 < 3; k2++) {
+    cplx<T> b[3] = {y[0][k2], y[1][k2], y[2][k2]};
+    dft3(b, s);
+    v[k2] = b[0];
+    v[k2 + 3] = b[1];
+    v[k2 + 6] = b[2];
+  }
+}
+
 // Twiddle exp(s*2*pi*i*idx/n) from the forward table.
 template <typename T>
 __device__ __forceinline__ cplx<T> twiddle(const cplx<T> *tw, int idx, int s) {
@@ -232,6 +264,7 @@ __device__ __forceinline__ void stockham_pass(const cplx<T> *__restrict__ src, c
     if (R == 5) dft5(v, s);
     if (R == 7) dft7(v, s);
     if (R == 8) dft8(v, s);
+    if (R == 9) dft9(v, s);
     const int base = (j - k) * R + k;
 #pragma unroll
     for (int t = 0; t < R; t++) dst[pad_idx<POUT>(l * ls + (base + t * Ns) * es)] = v[t];
@@ -247,6 +280,7 @@ __device__ __forceinline__ void radix_pass(int R, const cplx<T> *src, cplx<T> *d
     case 4: stockham_pass<T, 4, PIN, POUT>(src, dst, n, Ns, nl, ls, es, tw, s, lineFastest); break;
     case 5: stockham_pass<T, 5, PIN, POUT>(src, dst, n, Ns, nl, ls, es, tw, s, lineFastest); break;
     case 7: stockham_pass<T, 7, PIN, POUT>(src, dst, n, Ns, nl, ls, es, tw, s, lineFastest); break;
+    case 9: stockham_pass<T, 9, PIN, POUT>(src, dst, n, Ns, nl, ls, es, tw, s, lineFastest); break;
     default: stockham_pass<T, 8, PIN, POUT>(src, dst, n, Ns, nl, ls, es, tw, s, lineFastest); break;
   }
 }

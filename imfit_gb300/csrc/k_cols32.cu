@@ -143,6 +143,7 @@ __device__ __forceinline__ void dft_r(cplx<float> *v, int s) {
   if (R == 5) dft5(v, s);
   if (R == 7) dft7(v, s);
   if (R == 8) dft8(v, s);
+  if (R == 9) dft9(v, s);
 }
 
 // The forward transform's last pass (radix R, span n / R), the product with
@@ -152,11 +153,17 @@ __device__ __forceinline__ void dft_r(cplx<float> *v, int s) {
 // butterfly needs, so the spectrum between the two transforms never goes
 // to shared memory.  pin / pout: padding of the source / destination layout.
 template <int MODE, int CPB, int R>
-__device__ void fused_mid(const cplx<float> *X, cplx<float> *Y, const cplx<float> *Hs, int n, int pin, int pout,
-                          const cplx<float> *tw, float scale) {
+__device__ void fused_mid(const cplx<float> *X, cplx<float> *Y, const cplx<float> *__restrict__ H, long hPitch,
+                          int nl, int n, int pin, int pout, const cplx<float> *tw, float scale) {
   const int m = n / R;
   for (int idx = threadIdx.x; idx < m * CPB; idx += blockDim.x) {
     const int j = idx / CPB, l = idx - j * CPB;
+    // the PSF spectrum's values for this thread, read from global memory (it
+    // is shared by every vector of the batch and stays in L2) while the
+    // butterfly runs
+    cplx<float> hv[R];
+#pragma unroll
+    for (int t = 0; t < R; t++) hv[t] = (l < nl) ? H[(long)(j + t * m) * hPitch + l] : cplx<float>{0.f, 0.f};
     cplx<float> v[R];
 #pragma unroll
     for (int r = 0; r < R; r++) v[r] = X[pad_rt((j + r * m) * CPB + l, pin)];
@@ -167,7 +174,7 @@ __device__ void fused_mid(const cplx<float> *X, cplx<float> *Y, const cplx<float
     dft_r<R>(v, -1);
 #pragma unroll
     for (int t = 0; t < R; t++) {
-      cplx<float> h = Hs[(j + t * m) * CPB + l];
+      cplx<float> h = hv[t];
       if (MODE == 2) h.y = -h.y;
       const cplx<float> z = cmul(v[t], h);
       v[t] = {z.x * scale, z.y * scale};
@@ -203,15 +210,16 @@ __device__ void last_to_global(const cplx<float> *X, cplx<float> *spec, long pit
 }
 
 template <int MODE, int CPB>
-__device__ void fused_mid_r(int R, const cplx<float> *X, cplx<float> *Y, const cplx<float> *Hs, int n, int pin,
-                            int pout, const cplx<float> *tw, float scale) {
+__device__ void fused_mid_r(int R, const cplx<float> *X, cplx<float> *Y, const cplx<float> *H, long hPitch, int nl,
+                            int n, int pin, int pout, const cplx<float> *tw, float scale) {
   switch (R) {
-    case 2: fused_mid<MODE, CPB, 2>(X, Y, Hs, n, pin, pout, tw, scale); break;
-    case 3: fused_mid<MODE, CPB, 3>(X, Y, Hs, n, pin, pout, tw, scale); break;
-    case 4: fused_mid<MODE, CPB, 4>(X, Y, Hs, n, pin, pout, tw, scale); break;
-    case 5: fused_mid<MODE, CPB, 5>(X, Y, Hs, n, pin, pout, tw, scale); break;
-    case 7: fused_mid<MODE, CPB, 7>(X, Y, Hs, n, pin, pout, tw, scale); break;
-    default: fused_mid<MODE, CPB, 8>(X, Y, Hs, n, pin, pout, tw, scale); break;
+    case 2: fused_mid<MODE, CPB, 2>(X, Y, H, hPitch, nl, n, pin, pout, tw, scale); break;
+    case 3: fused_mid<MODE, CPB, 3>(X, Y, H, hPitch, nl, n, pin, pout, tw, scale); break;
+    case 4: fused_mid<MODE, CPB, 4>(X, Y, H, hPitch, nl, n, pin, pout, tw, scale); break;
+    case 5: fused_mid<MODE, CPB, 5>(X, Y, H, hPitch, nl, n, pin, pout, tw, scale); break;
+    case 7: fused_mid<MODE, CPB, 7>(X, Y, H, hPitch, nl, n, pin, pout, tw, scale); break;
+    case 9: fused_mid<MODE, CPB, 9>(X, Y, H, hPitch, nl, n, pin, pout, tw, scale); break;
+    default: fused_mid<MODE, CPB, 8>(X, Y, H, hPitch, nl, n, pin, pout, tw, scale); break;
   }
 }
 
@@ -224,6 +232,7 @@ __device__ void last_to_global_r(int R, const cplx<float> *X, cplx<float> *spec,
     case 4: last_to_global<CPB, 4>(X, spec, pitch, n, pin, tw, nRowsOut, nl); break;
     case 5: last_to_global<CPB, 5>(X, spec, pitch, n, pin, tw, nRowsOut, nl); break;
     case 7: last_to_global<CPB, 7>(X, spec, pitch, n, pin, tw, nRowsOut, nl); break;
+    case 9: last_to_global<CPB, 9>(X, spec, pitch, n, pin, tw, nRowsOut, nl); break;
     default: last_to_global<CPB, 8>(X, spec, pitch, n, pin, tw, nRowsOut, nl); break;
   }
 }
@@ -276,6 +285,7 @@ __device__ __forceinline__ void mid_pass(int R, const cplx<float> *src, cplx<flo
     case 4: col_pass<CPB, 4>(src, dst, n, Ns, pin, pout, tw, s); break;
     case 5: col_pass<CPB, 5>(src, dst, n, Ns, pin, pout, tw, s); break;
     case 7: col_pass<CPB, 7>(src, dst, n, Ns, pin, pout, tw, s); break;
+    case 9: col_pass<CPB, 9>(src, dst, n, Ns, pin, pout, tw, s); break;
     default: col_pass<CPB, 8>(src, dst, n, Ns, pin, pout, tw, s); break;
   }
 }
@@ -286,8 +296,9 @@ __device__ __forceinline__ void mid_pass(int R, const cplx<float> *src, cplx<flo
 // forward transform's passes but the last, the fused last-forward x PSF x
 // first-inverse pass, the inverse's middle passes (plan I: the same radices
 // reversed), and its last pass straight to global memory.  Shared memory
-// (cols32_fused_smem): both plans' twiddles, two FFT buffers of
-// padded_len(Ly * CPB) elements, the PSF columns.
+// (cols32_fused_smem): both plans' twiddles and two FFT buffers of
+// padded_len(Ly * CPB) elements; the PSF spectrum is read from global memory
+// in the fused pass.
 template <int MODE, int CPB>
 __device__ __forceinline__ void cols_group_fused(unsigned char *smem_raw, cplx<float> *spec, long pitch, int nColsC,
                                                  int nRowsIn, int nRowsOut, const cplx<float> *H, long hPitch,
@@ -299,7 +310,6 @@ __device__ __forceinline__ void cols_group_fused(unsigned char *smem_raw, cplx<f
   cplx<float> *twI = twF + Ly;
   cplx<float> *bufA = twI + Ly;
   cplx<float> *bufB = bufA + bufLen;
-  cplx<float> *bufH = bufB + bufLen;
   const int nl = min(CPB, nColsC - c0);
   if (nl <= 0) return;
   const int pairs = (nl + 1) >> 1;
@@ -311,7 +321,6 @@ __device__ __forceinline__ void cols_group_fused(unsigned char *smem_raw, cplx<f
       load_row<CPB>(bufA + (long)t * CPB, spec + (long)t * pitch, pairs);
     else
       zero_row<CPB>(bufA + (long)t * CPB);
-    load_row<CPB>(bufH + (long)t * CPB, H + (long)t * hPitch, pairs);
   }
   for (int i = threadIdx.x; 2 * i < Ly; i += blockDim.x) {
     cp_async16(twF + 2 * i, F.tw + 2 * i);
@@ -335,7 +344,7 @@ __device__ __forceinline__ void cols_group_fused(unsigned char *smem_raw, cplx<f
     dst = t;
   }
   const int Rm = (int)((F.radix >> (4 * last)) & 15ull);
-  fused_mid_r<MODE, CPB>(Rm, src, dst, bufH, Ly, last == 1 ? padF : 0, padI, tw, scale);
+  fused_mid_r<MODE, CPB>(Rm, src, dst, H, hPitch, nl, Ly, last == 1 ? padF : 0, padI, tw, scale);
   __syncthreads();
   {
     cplx<float> *t = src;
@@ -391,7 +400,7 @@ cudaError_t launch_one(cplx<float> *s, long pitch, long batch, int nColsC, int n
                        const int *hMap) {
   auto kern = k_cols32<MODE, CPB>;
   allow_max_smem((const void *)kern);
-  const size_t sm = cols32_smem(p.n, CPB) + (pI.tw ? sizeof(cplx<float>) * (size_t)p.n : 0);
+  const size_t sm = pI.tw ? cols32_fused_smem(p.n, CPB) : cols32_smem(p.n, CPB);
   dim3 grid((nColsC + CPB - 1) / CPB, nBatch);
   return launch_pdl(kern, grid, dim3(threads), sm, st, s, pitch, batch, nColsC, nRowsIn, nRowsOut, h, hPitch, p,
                     pI, scale, hBatch, hDiv, hMap);
@@ -440,6 +449,11 @@ cudaError_t launch_rag_cols(const RagArgs &r, int total, int maxLy, cudaStream_t
   return launch_pdl(k_rag_cols, dim3(total), dim3(128), sm, st, r);
 }
 
+// the fused form: both plans' twiddles and the two FFT buffers
+size_t cols32_fused_smem(int Ly, int cpb) {
+  return sizeof(cplx<float>) * (2 * (size_t)Ly + 2 * (size_t)padded_len(Ly * cpb, 2));
+}
+
 size_t cols32_smem(int Ly, int cpb) {
   return sizeof(cplx<float>) * ((size_t)Ly * (1 + cpb) + 2 * (size_t)padded_len(Ly * cpb, 2));
 }
@@ -453,9 +467,9 @@ cudaError_t launch_cols32(void *spec, long pitch, long batch, int nColsC, int nR
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (cpb <= 0) cpb = (nColsC * nBatch >= 4 * 152) ? 4 : 2;
   if (cpb != 1 && cpb != 2 && cpb != 4) cpb = 8;
-  const size_t twI = sizeof(cplx<float>) * (size_t)Ly.full.n;  // the reversed plan's twiddles
-  while (cpb > 1 && cols32_smem(Ly.full.n, cpb) + twI > (size_t)optin) cpb >>= 1;
-  if (cols32_smem(Ly.full.n, cpb) + twI > (size_t)optin) return cudaErrorInvalidValue;
+  auto need = [&](int c) { return std::max(cols32_smem(Ly.full.n, c), cols32_fused_smem(Ly.full.n, c)); };
+  while (cpb > 1 && need(cpb) > (size_t)optin) cpb >>= 1;
+  if (need(cpb) > (size_t)optin) return cudaErrorInvalidValue;
   if (threads <= 0) threads = line_threads(Ly.full.n * cpb / 4);
   FFTPlan<float> p;
   p.n = Ly.full.n;

@@ -337,12 +337,14 @@ int radix_schedule(int n, int *radix, int variant) {
       n /= p;
     }
   };
-  if (variant == 1) {
-    for (int p : {7, 5, 3, 8, 4, 2}) take(p);
-  } else if (variant == 2) {
-    for (int p : {4, 2, 3, 5, 7}) take(p);
-  } else {
+  if (variant == kRadixPlain) {
     for (int p : {8, 4, 2, 3, 5, 7}) take(p);
+  } else if (variant == 1) {
+    for (int p : {7, 5, 9, 3, 8, 4, 2}) take(p);
+  } else if (variant == 2) {
+    for (int p : {4, 2, 9, 3, 5, 7}) take(p);
+  } else {
+    for (int p : {8, 9, 4, 2, 3, 5, 7}) take(p);
   }
   return (n == 1) ? np : -1;
 }

@@ -81,6 +81,10 @@ constexpr int kRadixVariants = 3;
 // the `count` smallest 7-smooth lengths >= n within maxRatio * n; returns how many
 int smooth_candidates(int n, bool even, int count, double maxRatio, int *out);
 // allocate/free the device tables of one length
+// Radix order of the plain FP64 path: 8, 4, 2, 3, 5, 7 (no radix-9 butterflies,
+// so its FFT rounding stays that of the validated drop-in); the fast path's
+// orders are 0..kRadixVariants-1.
+constexpr int kRadixPlain = -1;
 cudaError_t fftlen_create(FFTLen &L, int len, int variant = 0);
 void fftlen_destroy(FFTLen &L);
 
@@ -99,6 +103,7 @@ cudaError_t launch_cols32(void *spec, long pitch, long batch, int nColsC, int nR
                           long hPitch, const FFTLen &Ly, float scale, int mode, int nBatch, cudaStream_t st,
                           int cpb = 0, long hBatch = 0, int hDiv = 1, const int *hMap = nullptr, int threads = 0);
 size_t cols32_smem(int Ly, int cpb);
+size_t cols32_fused_smem(int Ly, int cpb);
 void cols32_prepare_kernels();
 // complex pitch of a half spectrum of real length L: L/2 + 1 rounded up to
 // even, so every row starts on a 16-byte boundary

@@ -7,6 +7,7 @@
 // reference's expressions (bit-identical by construction); the results are
 // uploaded once at FinalSetupForFitting.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -484,8 +485,8 @@ struct imfit_model_s {
       nModelCols = nc + 2 * nPsfCols;
       nModelRows = nr + 2 * nPsfRows;
       // reference padding N_model + P - 1 (core/convolver.cpp:217-219), rounded up to a 7-smooth size
-      int e1 = fftlen_create(Lx, smooth_size(nModelCols + nPsfCols - 1, true));
-      int e2 = fftlen_create(Ly, smooth_size(nModelRows + nPsfRows - 1, true));
+      int e1 = fftlen_create(Lx, smooth_size(nModelCols + nPsfCols - 1, true), kRadixPlain);
+      int e2 = fftlen_create(Ly, smooth_size(nModelRows + nPsfRows - 1, true), kRadixPlain);
       if (e1 || e2) return fail(IMFIT_E_CUDA, "FFT tables");
       int st = spectrum64(wrap_psf(psf, nPsfCols, nPsfRows, Lx.L, Ly.L), Lx, Ly, dH);
       if (st) return st;
@@ -543,8 +544,8 @@ struct imfit_model_s {
       return fail(IMFIT_E_UNSUPPORTED,
                   "oversampled region shape would make DownsampleAndReplace read/write outside its images");
     }
-    int e1 = fftlen_create(r->Lx, smooth_size(r->nModelCols + pc - 1, true));
-    int e2 = fftlen_create(r->Ly, smooth_size(r->nModelRows + pr - 1, true));
+    int e1 = fftlen_create(r->Lx, smooth_size(r->nModelCols + pc - 1, true), kRadixPlain);
+    int e2 = fftlen_create(r->Ly, smooth_size(r->nModelRows + pr - 1, true), kRadixPlain);
     if (e1 || e2) {
       delete r;
       return fail(IMFIT_E_CUDA, "FFT tables");
@@ -2012,6 +2013,13 @@ struct imfit_model_s {
     return 0;
   }
 
+  struct LMBatchStats {
+    int rounds = 0;          // J^T W J evaluations (rounds of the lockstep LM, the first included)
+    long evaluations = 0;    // problem evaluations over all rounds
+    double evalSeconds = 0;  // wall time inside them
+    double totalSeconds = 0;
+  } lmStats;
+
   int fitLMBatch(int B, double *params, const int *fixed, const double *lower, const double *upper, double ftol,
                  int maxIter, double *stats, int *nIter, int *status) {
     const int n = nParamsTot;
@@ -2065,7 +2073,20 @@ struct imfit_model_s {
       return 0;
     };
     std::vector<LMResult> res(B);
-    int st = lm_minimize_batch(B, n, params, fixed, lower, upper, set, ev, res.data());
+    // where the time goes: the J^T W J evaluations (device work and transfers)
+    // and the rest (the host's LM steps)
+    lmStats = LMBatchStats{};
+    JtwjBatchEval timed = [&](const double *X, const unsigned char *act, double *S, double *A, double *b) {
+      const auto t0 = std::chrono::steady_clock::now();
+      const int r = ev(X, act, S, A, b);
+      lmStats.evalSeconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      lmStats.rounds++;
+      for (int i = 0; i < B; i++) lmStats.evaluations += act[i] ? 1 : 0;
+      return r;
+    };
+    const auto t0 = std::chrono::steady_clock::now();
+    int st = lm_minimize_batch(B, n, params, fixed, lower, upper, set, timed, res.data());
+    lmStats.totalSeconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     for (int i = 0; i < B; i++) {
       if (stats) stats[i] = res[i].stat;
       if (nIter) nIter[i] = res[i].nIter;
@@ -2659,6 +2680,15 @@ int imfit_FitLMBatch(imfit_model_t m, int B, double *params, const int *fixed, c
   if (B < 1 || !params) return m->fail(IMFIT_E_ARG, "bad batch arguments");
   if (!(ftol > 0.0)) return m->fail(IMFIT_E_ARG, "ftol must be positive");
   return m->fitLMBatch(B, params, fixed, lower, upper, ftol, maxIter, stats, nIter, status);
+}
+
+int imfit_GetLMBatchStats(imfit_model_t m, int *rounds, long *evaluations, double *evalSeconds, double *totalSeconds) {
+  if (!m) return IMFIT_E_ARG;
+  if (rounds) *rounds = m->lmStats.rounds;
+  if (evaluations) *evaluations = m->lmStats.evaluations;
+  if (evalSeconds) *evalSeconds = m->lmStats.evalSeconds;
+  if (totalSeconds) *totalSeconds = m->lmStats.totalSeconds;
+  return IMFIT_OK;
 }
 
 int imfit_SetupCutouts(imfit_model_t m, int nImg, const int *cols, const int *rows, const double *pix,

@@ -230,6 +230,11 @@ int imfit_FitLM(imfit_model_t m, double *params, const int *fixed, const double 
  * (nBatch each) may be NULL; status codes as imfit_FitLM. */
 int imfit_FitLMBatch(imfit_model_t m, int nBatch, double *params, const int *fixed, const double *lower,
                      const double *upper, double ftol, int maxIter, double *statistics, int *nIter, int *status);
+/* Timing of the most recent imfit_FitLMBatch: the J^T W J evaluations (rounds
+ * of the lockstep LM, problem evaluations over them, wall seconds inside
+ * them, device work and transfers included) and the call's total wall
+ * seconds (the rest is the host's LM steps).  Any pointer may be NULL. */
+int imfit_GetLMBatchStats(imfit_model_t m, int *rounds, long *evaluations, double *evalSeconds, double *totalSeconds);
 /* The Levenberg-Marquardt driver of imfit_FitLM on normal equations the
  * caller supplies: eval(x, &S, A, b, user) fills the statistic S, A = J^T J
  * (n x n, row-major) and b = J^T dev of its deviates at x and returns 0 (or a
@@ -328,8 +333,8 @@ int imfit_MeasureSfuRate(int device, double *opsPerSecond);
  * FFTW with FFTW_ESTIMATE on the smallest padded size, core/convolver.cpp:253-256).
  * The padded length of each axis is one of the three smallest 7-smooth even
  * lengths >= the window (within 10 %), the radix order one of three
- * (0: radix 8, 4, 2 then 3, 5, 7; 1: 7, 5, 3 then 8, 4, 2; 2: 4, 2 then
- * 3, 5, 7).  By default the autotuner times every pair on the first fast call
+ * (0: radix 8, 9, 4, 2 then 3, 5, 7; 1: 7, 5, 9, 3 then 8, 4, 2; 2: 4, 2, 9
+ * then 3, 5, 7).  By default the autotuner times every pair on the first fast call
  * and keeps the fastest; SetFFTPlan pins candidate (0..2) and order (0..2), or
  * returns to autotuning with candidate < 0.  GetFFTPlan reports the lengths
  * in use (Lx, Ly of the main window) and the order. */
