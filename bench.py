@@ -748,6 +748,10 @@ def run_c5(args, rank, local_rank, world):
             tol_h = 1e-9 * np.maximum(1.0, np.abs(hi[i]))
             pegged = ((np.abs(near.x - lo[i]) <= tol_l) | (np.abs(near.x - hi[i]) <= tol_h) |
                       (np.abs(got - lo[i]) <= tol_l) | (np.abs(got - hi[i]) <= tol_h))
+            # parameters without effect at the FP64 minimum (a position angle at zero
+            # ellipticity): no sigma, reported with the pegged ones
+            cn = np.linalg.norm(near.jac, axis=0)
+            pegged |= cn <= 1e-9 * np.max(cn)
             chi_got = o.get_fit_statistic(got)
             chi_near, chi_same = float(near.fun @ near.fun), float(same.fun @ same.fun)
             diff = got - near.x
@@ -771,7 +775,8 @@ def run_c5(args, rank, local_rank, world):
                "reference": "nearest FP64 minimum: scipy least_squares (trf, same limits, tolerances 1e-15) on the "
                             "oracle's FP64 deviates, started from this fit",
                "pegged_params": int(sum(e["pegged_params"] for e in errs)),
-               "note": "parameters at a limit in either fit are excluded from the error statistics",
+               "note": "parameters at a limit in either fit, or without effect at the FP64 minimum, are excluded "
+                       "from the error statistics (pegged_params)",
                "max_param_rel_err": float(rel.max()),
                "max_param_err_over_sigma": float(osg.max()),
                "fraction_params_within_1e-4_rel": float(np.mean(rel <= 1e-4)),

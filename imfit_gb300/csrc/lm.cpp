@@ -437,7 +437,7 @@ int settle(TrState &q, int n, double *x, const double *t, double St, const doubl
 template <typename F>
 static void parallel_for(int n, const F &f) {
   const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
-  const int nt = std::min(std::min(hw, 16), (n + 31) / 32);
+  const int nt = std::min(std::min(hw, 16), n / 64);
   if (nt <= 1) {
     for (int i = 0; i < n; i++) f(i);
     return;
@@ -486,28 +486,35 @@ int lm_minimize_batch(int B, int n, double *X, const int *fixed, const double *l
   // rounds: one trial per running problem, evaluated together; a rejected
   // trial costs a round but no iteration (as mpfit's inner loop)
   const long maxRounds = 20L * set.maxIter + 100;
+  // the host steps visit only the problems still running (the last rounds of
+  // a large batch have few; below 64 of them parallel_for runs serially)
+  std::vector<int> run;
+  run.reserve(B);
+  for (int i = 0; i < B; i++) live[i] = ps[i].done ? 0 : 1;
   for (long round = 0; round < maxRounds; round++) {
-    parallel_for(B, [&](int i) {
+    run.clear();
+    for (int i = 0; i < B; i++)
+      if (!ps[i].done) run.push_back(i);
+    if (run.empty()) break;
+    const int nr = (int)run.size();
+    parallel_for(nr, [&](int k) {
+      const int i = run[k];
       TrState &q = ps[i];
-      double *t = T.data() + (size_t)i * n;
-      const double *x = X + (size_t)i * n;
-      if (q.done) {
-        for (int j = 0; j < n; j++) t[j] = x[j];
-        return;
-      }
-      const int s = propose(q, n, x, t, freeIdx, limits(i), set);
+      const int s = propose(q, n, X + (size_t)i * n, T.data() + (size_t)i * n, freeIdx, limits(i), set);
       if (q.done) res[i].status = s;
     });
     bool any = false;
-    for (int i = 0; i < B; i++)
-      if (!ps[i].done) any = true;
+    for (int i : run) {
+      live[i] = ps[i].done ? 0 : 1;
+      any = any || live[i];
+    }
     if (!any) break;
-    for (int i = 0; i < B; i++) live[i] = ps[i].done ? 0 : 1;
     st = eval(T.data(), live.data(), S.data(), A.data(), b.data());
     if (st) return st;
-    parallel_for(B, [&](int i) {
+    parallel_for(nr, [&](int k) {
+      const int i = run[k];
       TrState &q = ps[i];
-      if (q.done || !live[i]) return;
+      if (!live[i]) return;
       res[i].nEval++;
       const int s = settle(q, n, X + (size_t)i * n, T.data() + (size_t)i * n, S[i], A.data() + (size_t)i * n * n,
                            b.data() + (size_t)i * n, set);
@@ -515,6 +522,8 @@ int lm_minimize_batch(int B, int n, double *X, const int *fixed, const double *l
       res[i].nIter = q.accepted + 1;
       if (q.done) res[i].status = s;
     });
+    for (int i : run)
+      if (ps[i].done) live[i] = 0;
   }
   for (int i = 0; i < B; i++)
     if (!ps[i].done) res[i].status = 5;

@@ -1497,24 +1497,42 @@ struct imfit_model_s {
       cudaEventDestroy(e1);
       timing = timingWas;
     };
+    // Each candidate runs the way later calls will: replayed from a CUDA
+    // graph when graphs are on (launch costs and the programmatic-dependent
+    // overlap then match), else launched kernel by kernel.  Best of three
+    // timings of four evaluations (the candidates differ by a few percent,
+    // comparable to the run-to-run noise of a single timing).
     auto measure = [&](const FastTune &t, float &best) -> cudaError_t {
       tune = t;
       FastArgs a = fastArgs(dP, dS, dG ? dG : dGrad.p, nullptr);
       FastPlan p = fastPlan();
-      cudaError_t e = fast_forward(p, a, B, dG != nullptr, stream);  // warm
-      if (e) return e;
-      // best of two timings of four evaluations each (the shapes differ by a
-      // few percent, comparable to run-to-run noise of a single timing)
+      cudaGraphExec_t ex = nullptr;
+      cudaError_t e = cudaSuccess;
+      if (useGraphs) {
+        cudaGraph_t gr;
+        e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
+        if (e) return e;
+        cudaError_t e2 = fast_forward(p, a, B, dG != nullptr, stream);
+        e = cudaStreamEndCapture(stream, &gr);
+        if (e2) return e2;
+        if (e) return e;
+        e = cudaGraphInstantiate(&ex, gr, 0);
+        cudaGraphDestroy(gr);
+        if (e) return e;
+      }
+      auto run = [&]() { return ex ? cudaGraphLaunch(ex, stream) : fast_forward(p, a, B, dG != nullptr, stream); };
+      e = run();  // warm
       best = 1e30f;
-      for (int trial = 0; trial < 2 && !e; trial++) {
+      for (int trial = 0; trial < 3 && !e; trial++) {
         e = cudaEventRecord(e0, stream);
-        for (int r = 0; r < 4 && !e; r++) e = fast_forward(p, a, B, dG != nullptr, stream);
+        for (int r = 0; r < 4 && !e; r++) e = run();
         if (!e) e = cudaEventRecord(e1, stream);
         if (!e) e = cudaEventSynchronize(e1);
         float ms = 0.f;
         if (!e) e = cudaEventElapsedTime(&ms, e0, e1);
         best = std::min(best, ms);
       }
+      if (ex) cudaGraphExecDestroy(ex);
       return e;
     };
     cudaError_t e = cudaSuccess;
