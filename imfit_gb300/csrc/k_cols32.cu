@@ -427,7 +427,7 @@ cudaError_t launch_mode(int cpb, cplx<float> *s, long pitch, long batch, int nCo
 
 // Column pass of a ragged cutout set: CTA t serves column group g of spectrum
 // `line` of the slot that owns t (each cutout its own lengths and pitch).
-constexpr int kRagCpb = 2;
+constexpr int kRagCpb = kRagColsPerCta;
 __global__ void __launch_bounds__(256) k_rag_cols(RagArgs r) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   pdl_wait();
@@ -438,14 +438,18 @@ __global__ void __launch_bounds__(256) k_rag_cols(RagArgs r) {
   const int line = local / E.colGroups, g = local - line * E.colGroups;
   cplx<float> *spec = r.spec + (r.lines == 1 ? E.specOff : (long)r.lines * E.specOff + (long)line * E.specSize);
   const float scale = 1.f / ((float)E.Lx * (float)E.Ly);
-  cols_group<1, kRagCpb>(smem_raw, spec, E.pitch, E.Lx / 2 + 1, E.winRows, E.nDataRows, r.H + E.hOff, E.pitch,
-                         E.colPlan, scale, g * kRagCpb);
+  if (E.colPlanI.tw)
+    cols_group_fused<1, kRagCpb>(smem_raw, spec, E.pitch, E.Lx / 2 + 1, E.winRows, E.nDataRows, r.H + E.hOff,
+                                 E.pitch, E.colPlan, E.colPlanI, scale, g * kRagCpb);
+  else
+    cols_group<1, kRagCpb>(smem_raw, spec, E.pitch, E.Lx / 2 + 1, E.winRows, E.nDataRows, r.H + E.hOff, E.pitch,
+                           E.colPlan, scale, g * kRagCpb);
 }
 
 cudaError_t launch_rag_cols(const RagArgs &r, int total, int maxLy, cudaStream_t st) {
   if (total <= 0) return cudaSuccess;
   allow_max_smem((const void *)k_rag_cols);
-  const size_t sm = cols32_smem(maxLy, kRagCpb);
+  const size_t sm = std::max(cols32_smem(maxLy, kRagCpb), cols32_fused_smem(maxLy, kRagCpb));
   return launch_pdl(k_rag_cols, dim3(total), dim3(128), sm, st, r);
 }
 

@@ -344,6 +344,9 @@ cudaError_t fast_jtwj(const FastPlan &p, const FastArgs &a, const JtwjArgs &J, i
 // and every stage of an evaluation is ONE launch over all active cutouts --
 // a flat grid whose CTA t serves the slot k with start[k] <= t < start[k+1]
 // (binary search over the prefix sums of the slots' work counts).
+// spectrum columns per CTA of a cutout set's column pass
+constexpr int kRagColsPerCta = 4;
+
 struct RagEntry {
   int nDataCols, nDataRows;  // the cutout
   int winCols, winRows;      // window W = N + P - 1
@@ -358,6 +361,7 @@ struct RagEntry {
   long rowOff;               // offset of its data rows in the per-row partials
   FFTPlan<float> rowPlan;    // Lx/2-point complex transform (rows)
   FFTPlan<float> colPlan;    // Ly-point transform (columns)
+  FFTPlan<float> colPlanI;   // the same radices reversed (the column pass's inverse half; tw null: unfused)
   const cplx<float> *twL;    // Lx split twiddles
 };
 

@@ -1845,7 +1845,7 @@ struct imfit_model_s {
       E.Ly = smooth_size(E.winRows, true);
       if (E.Lx / 2 > 4096 || E.Ly > 4096) return fail(IMFIT_E_UNSUPPORTED, "cutout too large for the fast path");
       E.pitch = even_pitch(E.Lx);
-      E.colGroups = (E.Lx / 2 + 1 + 1) / 2;
+      E.colGroups = (E.Lx / 2 + 1 + kRagColsPerCta - 1) / kRagColsPerCta;
       E.specSize = (long)E.Ly * E.pitch;
       E.specOff = R.totalSpec;
       E.hOff = R.totalSpec;  // one PSF spectrum per cutout, same geometry
@@ -1907,6 +1907,8 @@ struct imfit_model_s {
       if (st) return st;
       E.rowPlan = plan(fx->half);
       E.colPlan = plan(fy->full);
+      E.colPlanI = plan(fy->fullRev);
+      if (E.colPlan.npass < 2) E.colPlanI.tw = nullptr;  // a single pass: the unfused column group
       E.twL = reinterpret_cast<const cplx<float> *>(fx->twL32);
     }
     e = dRagEnt.reserve(nImg);
@@ -2244,6 +2246,7 @@ int imfit_ModelObject_new(int device, imfit_model_t *out) {
   m->device = device;
   e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
   if (!e) e = cudaStreamCreateWithFlags(&m->side, cudaStreamNonBlocking);
+
   for (int i = 0; i < 2 && !e; i++) {
     e = cudaEventCreateWithFlags(&m->forkEv[i], cudaEventDisableTiming);
     if (!e) e = cudaEventCreateWithFlags(&m->joinEv[i], cudaEventDisableTiming);
