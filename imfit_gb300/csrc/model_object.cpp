@@ -266,6 +266,11 @@ struct imfit_model_s {
   int *hLosFlag = nullptr;  // pinned copy of the "list too short" flag
   double *hPinned = nullptr;  // pinned scratch for small transfers
   size_t hPinnedN = 0;
+  // host-buffer fast evaluations: parameters in, statistics and gradients out
+  // through mapped page-locked memory the kernels read and write directly
+  // (no copy operations around the evaluation)
+  double *hMapped = nullptr, *dMapped = nullptr;
+  size_t hMappedN = 0;
 
   // fast FP32 device state
   bool fastReady = false;
@@ -374,6 +379,7 @@ struct imfit_model_s {
     if (timing)
       for (int i = 0; i < StageTimer::kMax; i++) cudaEventDestroy(timer.ev[i]);
     if (hPinned) cudaFreeHost(hPinned);
+    if (hMapped) cudaFreeHost(hMapped);
     if (hLosFlag) cudaFreeHost(hLosFlag);
     for (int i = 0; i < 2; i++) {
       if (forkEv[i]) cudaEventDestroy(forkEv[i]);
@@ -1654,6 +1660,32 @@ struct imfit_model_s {
     st = ensureFastCap(B);
     if (st) return st;
     const int nP = nParamsTot;
+    const size_t need = (size_t)B * (2 * nP + 1);
+    if (need > hMappedN) {
+      if (hMapped) cudaFreeHost(hMapped);
+      hMapped = dMapped = nullptr;
+      hMappedN = 0;
+      if (cudaHostAlloc(&hMapped, sizeof(double) * need, cudaHostAllocMapped) == cudaSuccess &&
+          cudaHostGetDevicePointer(&dMapped, hMapped, 0) == cudaSuccess) {
+        hMappedN = need;
+      } else {
+        if (hMapped) cudaFreeHost(hMapped);
+        hMapped = dMapped = nullptr;
+        cudaGetLastError();
+      }
+    }
+    if (hMappedN) {  // zero-copy form
+      double *hp = hMapped, *hs = hMapped + (size_t)B * nP, *hg = hs + B;
+      std::copy(params, params + (size_t)B * nP, hp);
+      double *dp = dMapped, *ds = dMapped + (size_t)B * nP, *dg = ds + B;
+      st = enqueueFast(B, dp, ds, grads ? dg : nullptr);
+      if (st) return st;
+      cudaError_t e = cudaStreamSynchronize(stream);
+      if (e) return cuda_fail(e, "fast results");
+      std::copy(hs, hs + B, stats);
+      if (grads) std::copy(hg, hg + (size_t)B * nP, grads);
+      return 0;
+    }
     cudaError_t e = cudaMemcpyAsync(dParams.p, params, sizeof(double) * (size_t)B * nP, cudaMemcpyHostToDevice, stream);
     if (e) return cuda_fail(e, "params upload");
     st = enqueueFast(B, dParams.p, dStat.p, grads ? dGrad.p : nullptr);

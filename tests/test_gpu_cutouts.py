@@ -187,6 +187,10 @@ def test_cutout_set_fits_match_single_fits(gpu, oracle_mod):
     hi = np.array([it["upper"] for it in items])
     rb = m.fit_lm_batch(P, lower=lo, upper=hi, ftol=1e-10)
     assert np.all(rb["status"] > 0), rb["status"]
+    # timing of the batched fit: rounds = evaluations of the most-evaluated cutout
+    t = m.lm_batch_stats()
+    assert t["rounds"] >= 2 and len(items) <= t["evaluations"] <= t["rounds"] * len(items)
+    assert 0.0 < t["eval_s"] <= t["total_s"]
     for i, (d, s, p) in enumerate(imgs):
         g = _single(gpu.ModelObject, d, s, p)
         r1 = g.fit_lm(P[i], lower=lo[i], upper=hi[i], ftol=1e-10)
