@@ -1392,7 +1392,8 @@ __device__ __forceinline__ void deviate_slope(const FastArgs &a, long z, float m
 // order alpha (row-major upper triangle), beta, S.  Warps take 4 x 4 tiles of
 // the triangle over one chunk of the columns (lanes on consecutive columns:
 // conflict-free shared loads, 16 FMAs per 8 loads), reduce each tile entry
-// across the warp, and the chunks' sums are added in a fixed order.
+// across the warp (FP32: at most 32 partial sums), and the chunks' sums are
+// added in a fixed order in double-float, stored as (hi, lo) pairs.
 // Row j of a is at U + ss[j] * uStride (ss[j] < 0: the background row qb),
 // row nP at dv, rows past nP at zero (nc zeros).  red holds jtwj_splits() x Q
 // floats.  All threads of the CTA call it; ends with a barrier.
@@ -1412,7 +1413,7 @@ __host__ __device__ inline int jtwj_aux_floats(int nP, int nc, int threads) {
 template <bool W>
 __device__ __forceinline__ void jtwj_gram(const float *U, long uStride, const int *ss, const float *qb,
                                           const float *dv, const float *zero, const float *cw, int nc, int nP,
-                                          float *red, float *out, long outStride) {
+                                          float *red, float2 *out, long outStride) {
   const int n1 = nP + 1, nt = (n1 + 3) / 4, nTiles = nt * (nt + 1) / 2;
   const int nPair = nP * (nP + 1) / 2, Q = nPair + nP + 1;
   const int nw = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1467,9 +1468,9 @@ __device__ __forceinline__ void jtwj_gram(const float *U, long uStride, const in
   }
   __syncthreads();
   for (int qi = threadIdx.x; qi < Q; qi += blockDim.x) {
-    float t = 0.f;
-    for (int sp = 0; sp < nSplit; sp++) t += red[sp * Q + qi];
-    out[qi * outStride] = t;
+    ffloat t = ff_make(0.f);  // the chunks' warp sums, added in double-float
+    for (int sp = 0; sp < nSplit; sp++) t = ff_add(t, red[sp * Q + qi]);
+    out[qi * outStride] = ff_store(t);
   }
 }
 
@@ -1485,7 +1486,7 @@ __global__ void __launch_bounds__(1024) k_fast_jtwj_rows(FastArgs a, FastGeom g,
                                                         const cplx<float> *__restrict__ dspec,
                                                         const float *__restrict__ regDeriv,
                                                         const int *__restrict__ slot, int nD,
-                                                        float *__restrict__ part, float *__restrict__ jac) {
+                                                        float2 *__restrict__ part, float *__restrict__ jac) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int b = blockIdx.y, row = blockIdx.x;
   const int M = plan.n, ls = M + 1, nP = a.nParams, nc = g.nDataCols;
@@ -1573,7 +1574,7 @@ __global__ void __launch_bounds__(1024) k_fast_jtwj_rows(FastArgs a, FastGeom g,
   }
   __syncthreads();
   const int Q = nP * (nP + 1) / 2 + nP + 1;
-  float *out = part + (long)b * Q * a.partStride + blockIdx.x;
+  float2 *out = part + (long)b * Q * a.partStride + blockIdx.x;
   if (a.count)
     jtwj_gram<true>(Zr, uStride, ss, qb, dv, zero, cw, nc, nP, red, out, a.partStride);
   else
@@ -1581,14 +1582,14 @@ __global__ void __launch_bounds__(1024) k_fast_jtwj_rows(FastArgs a, FastGeom g,
 }
 
 // FP64 sums of the per-row partials: grid (quantity, parameter vector).
-__global__ void __launch_bounds__(256) k_fast_jtwj_reduce(FastArgs a, const float *__restrict__ part, int nRows,
+__global__ void __launch_bounds__(256) k_fast_jtwj_reduce(FastArgs a, const float2 *__restrict__ part, int nRows,
                                                          double *__restrict__ alpha, double *__restrict__ beta,
                                                          double *__restrict__ stat) {
   const int qi = blockIdx.x, b = blockIdx.y, nP = a.nParams;
   const int nPair = nP * (nP + 1) / 2, Q = nPair + nP + 1;
-  const float *p = part + ((long)b * Q + qi) * a.partStride;
+  const float2 *p = part + ((long)b * Q + qi) * a.partStride;
   double t = 0.0;
-  for (int i = threadIdx.x; i < nRows; i += blockDim.x) t += (double)p[i];
+  for (int i = threadIdx.x; i < nRows; i += blockDim.x) t += (double)p[i].x + (double)p[i].y;
   t = block_sum_d(t);
   if (threadIdx.x != 0) return;
   if (qi < nPair) {
@@ -2239,9 +2240,9 @@ __global__ void __launch_bounds__(256) k_rag_jtwj_reduce(FastArgs a, RagArgs r, 
   const int qi = blockIdx.x, k = blockIdx.y, nP = a.nParams;
   const int nPair = nP * (nP + 1) / 2;
   const RagEntry &E = r.ent[r.act[k]];
-  const float *p = r.part + (long)qi * r.totalRows + E.rowOff;
+  const float2 *p = r.part + (long)qi * r.totalRows + E.rowOff;
   double t = 0.0;
-  for (int i = threadIdx.x; i < E.nDataRows; i += blockDim.x) t += (double)p[i];
+  for (int i = threadIdx.x; i < E.nDataRows; i += blockDim.x) t += (double)p[i].x + (double)p[i].y;
   t = block_sum_d(t);
   if (threadIdx.x != 0) return;
   if (qi < nPair) {

@@ -329,7 +329,7 @@ struct JtwjArgs {
   float *regDeriv;   // [B*nD][rRows][rCols] downsampled region derivatives
   const int *slot;   // [nParams]
   int nD;
-  float *part;       // [B][Q][partStride] per-row partials, Q = nP(nP+1)/2 + nP + 1
+  float2 *part;      // [B][Q][partStride] per-row partials (hi, lo), Q = nP(nP+1)/2 + nP + 1
   double *alpha;     // [B][nP][nP]  J^T J
   double *beta;      // [B][nP]      J^T dev
   double *stat;      // [B]          sum dev^2 (the fit statistic)
@@ -374,7 +374,7 @@ struct RagArgs {
   cplx<float> *spec;       // spectra (forward: specOff; derivatives: nD * specOff + j * specSize)
   const cplx<float> *H;    // PSF spectra (hOff)
   float *model;            // FP32 model images (dataOff)
-  float *part;             // per-row partials [Q][totalRows] (rowOff)
+  float2 *part;            // per-row partials (hi, lo) [Q][totalRows] (rowOff)
   long totalRows;
 };
 

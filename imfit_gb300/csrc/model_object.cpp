@@ -1706,7 +1706,7 @@ struct imfit_model_s {
     if (!e && nDeriv) e = dDSpec32.reserve(2 * (size_t)B * nDeriv * g.specBatch);
     if (!e && nDeriv && g.hasRegion) e = dDRSpec32.reserve(2 * (size_t)B * nDeriv * g.rSpecBatch);
     if (!e && nDeriv && g.hasRegion) e = dRegDeriv.reserve((size_t)B * nDeriv * g.rRows * g.rCols);
-    if (!e) e = dJPart.reserve((size_t)B * Q * partStride());
+    if (!e) e = dJPart.reserve(2 * (size_t)B * Q * partStride());  // (hi, lo) pairs
     if (!e) e = dAlpha.reserve((size_t)B * nP * nP);
     if (!e) e = dBeta.reserve((size_t)B * nP);
     if (e) return cuda_fail(e, "JtWJ buffers");
@@ -1748,7 +1748,7 @@ struct imfit_model_s {
     J.regDeriv = dRegDeriv.p;
     J.slot = dSlot.p;
     J.nD = nDeriv;
-    J.part = dJPart.p;
+    J.part = reinterpret_cast<float2 *>(dJPart.p);
     J.alpha = dA;
     J.beta = dBt;
     J.stat = dS;
@@ -1972,7 +1972,7 @@ struct imfit_model_s {
     if (!e) e = dRagSpec.reserve(2 * (size_t)R.totalSpec);
     if (!e && ragNDeriv) e = dRagDSpec.reserve(2 * (size_t)ragNDeriv * R.totalSpec);
     if (!e) e = dRagModel.reserve(R.totalPix);
-    if (!e) e = dRagPart.reserve((size_t)Q * R.totalRows);
+    if (!e) e = dRagPart.reserve(2 * (size_t)Q * R.totalRows);  // (hi, lo) pairs
     if (!e) e = dRagParams.reserve((size_t)nImg * nP);
     if (!e) e = dRagS.reserve(nImg);
     if (!e) e = dRagA.reserve((size_t)nImg * nP * nP);
@@ -2045,7 +2045,7 @@ struct imfit_model_s {
     r.spec = reinterpret_cast<cplx<float> *>(dRagSpec.p);
     r.H = reinterpret_cast<const cplx<float> *>(dRagH.p);
     r.model = dRagModel.p;
-    r.part = dRagPart.p;
+    r.part = reinterpret_cast<float2 *>(dRagPart.p);
     r.totalRows = R.totalRows;
     const int *starts[kRagWorkKinds];
     int totals[kRagWorkKinds];
