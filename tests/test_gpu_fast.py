@@ -157,3 +157,27 @@ def test_no_psf_fast_path(gpu, oracle_mod):
     g = workloads.configure(gpu.ModelObject(), wl)
     o = workloads.configure(oracle_mod.OracleModel(), wl)
     assert relerr(g.fit_statistic_fast(wl.start), o.get_fit_statistic(wl.start)) < 1e-5
+
+
+@pytest.mark.parametrize("k", [2, 3, 4, 5])
+def test_oversampled_region_scales(gpu, oracle_mod, k):
+    """Region scales whose subsample table uses the shared lattice (k = 2, 4,
+    5: k divides the 20 x 20 count) and one that does not (k = 3): fast
+    statistic and model image against the FP64 oracle, and the gradient with
+    subsampling on (the lattice's derivative channels) against a small-step
+    FD of the FP64 statistic."""
+    from imfit_gb300 import workloads
+    wl = workloads.small_case(seed=19, region=True)
+    wl.regions = [(workloads.moffat_psf(15 * k | 1, k * 2.5, 3.0), k, (26, 33, 19, 26))]  # odd side
+    workloads.synthesize(wl, oracle_mod.OracleModel)
+    g = _build(gpu.ModelObject, wl)
+    o = _build(oracle_mod.OracleModel, wl)
+    for p in (wl.truth, wl.start):
+        assert relerr(g.fit_statistic_fast(p), o.get_fit_statistic(p)) < 1e-5
+    o.create_model_image(wl.start)
+    ref = o.get_model_image()
+    assert np.max(np.abs(g.get_fast_model_image(wl.start) - ref)) / np.max(np.abs(ref)) < 2e-6
+    s, grad = g.statistic_and_gradient(wl.start)
+    fd = _central_fd(o, wl.start, rel=1e-6)
+    scale = np.abs(fd) + 1e-2 * np.max(np.abs(fd))
+    assert np.median(np.abs(grad - fd) / scale) < 1e-2, list(zip(g.parameter_names(), grad, fd))
