@@ -12,7 +12,10 @@
 //   cols       column FFT x PSF spectrum x inverse column FFT  (Convolver::ConvolveImage,
 //              k_cols32.cu)
 //   region     oversampled region: same pipeline at k x resolution and a
-//              fused block-average                             (OversampledRegion, DownsampleAndReplace)
+//              fused block-average that also forms the statistic terms and
+//              adjoint seeds of the region's pixels, on a second stream
+//              independent of the main window's until the final reduction
+//                                                              (OversampledRegion, DownsampleAndReplace)
 //   stat_rows  inverse row FFT, statistic terms in FP32 per pixel, summed in
 //              double-float above the warp; the adjoint seed g = dS/dM
 //              written and immediately row-FFT'd                (ChiSquared / CashStatistic)
@@ -645,52 +648,6 @@ __device__ float ps_region(const FastArgs &a, int k, int b, int row, int col, fl
   return v;
 }
 
-// ---------------------------------------- region: c2r + block average
-// (also used for the derivative images of the JtWJ pass: batch index b then
-// runs over (parameter vector, parameter) pairs, no background is added and
-// the output goes to a different buffer)
-// PS: the model has point sources (their code is compiled only into the PS instance)
-template <bool PS>
-__global__ void __launch_bounds__(1024) k_fast_region_down(FastArgs a, FastGeom g, const cplx<float> *__restrict__ rspec,
-                                                          FFTPlan<float> plan, const cplx<float> *__restrict__ twL,
-                                                          float *__restrict__ out, int addBackground) {
-  pdl_wait();
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int b = blockIdx.y, s = blockIdx.x;  // replaced data row within the region
-  const int k = g.rScale;
-  const int M = plan.n, ls = M + 1;
-  cplx<float> *bufX = reinterpret_cast<cplx<float> *>(smem);
-  cplx<float> *bufA = bufX + k * ls;
-  cplx<float> *bufB = bufA + k * ls;
-  const cplx<float> *in = rspec + (long)b * g.rSpecBatch + (long)(s * k) * g.rSpecPitch;
-  const FastDiv byM(M), byM1(M + 1);
-  for (int idx = threadIdx.x; idx < k * (M + 1); idx += blockDim.x) {
-    const int l = byM1.div(idx), kk = idx - l * (M + 1);
-    bufX[l * ls + kk] = in[(long)l * g.rSpecPitch + kk];
-  }
-  __syncthreads();
-  for (int idx = threadIdx.x; idx < k * M; idx += blockDim.x) {
-    const int l = byM.div(idx), kk = idx - l * M;
-    bufA[l * ls + kk] = c2r_pre(bufX + l * ls, kk, M, twL);
-  }
-  __syncthreads();
-  cplx<float> *Z = block_fft(bufA, bufB, plan, k, ls, 1, +1, false);
-  const float inv = 1.f / (float)(k * k);
-  const float bg = addBackground ? a.bgLevel[2 * b + 1] : 0.f;
-  for (int t = threadIdx.x; t < g.rCols; t += blockDim.x) {
-    float acc = 0.f;
-    for (int u = 0; u < k; u++)
-      for (int v = 0; v < k; v++) {
-        const int col = t * k + v;
-        const cplx<float> z = Z[u * ls + (col >> 1)];
-        acc += (col & 1) ? z.y : z.x;
-      }
-    if constexpr (PS)
-      if (addBackground) acc += ps_region(a, k, b, g.ry0 + s, g.rx0 + t, 0.f, nullptr);
-    out[((long)b * g.rRows + s) * g.rCols + t] = acc * inv + bg;
-  }
-}
-
 // ------------------------------------------------------------- reduce
 // Double-float sums of the per-CTA partials of parameter vector b in a fixed
 // order (deterministic), one warp per output quantity: the statistic, the
@@ -817,6 +774,134 @@ __device__ __forceinline__ void stat_term(const FastArgs &a, long z, float m, fl
   }
 }
 
+// CTA partial sums of (S, SG) into slot `slot` of vector b: FP32 over the
+// thread's pixels and the warp, double-float across warps.  Every thread of
+// the CTA calls it.
+__device__ __forceinline__ void stat_partials(const FastArgs &a, int b, int slot, float S, float SG) {
+  __shared__ ffloat red[2][32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  S = warp_sum(S);
+  SG = warp_sum(SG);
+  if (lane == 0) {
+    red[0][wid] = ff_make(S);
+    red[1][wid] = ff_make(SG);
+  }
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = blockDim.x >> 5;
+    ffloat v0 = lane < nw ? red[0][lane] : ffloat{0.f, 0.f};
+    ffloat v1 = lane < nw ? red[1][lane] : ffloat{0.f, 0.f};
+    v0 = ff_warp_sum(v0);
+    v1 = ff_warp_sum(v1);
+    if (lane == 0) {
+      float2 *p = a.statPart + (long)b * 2 * a.partStride + slot;
+      p[0] = ff_store(v0);
+      p[a.partStride] = ff_store(v1);
+    }
+  }
+}
+
+// ---------------------------------------- region: c2r + block average
+// One CTA per replaced data row s of the oversampled region: the inverse row
+// FFTs of its k subpixel rows and the k x k block averages.  mode 0: derivative
+// images of the JtWJ pass (batch index b then runs over (parameter vector,
+// parameter) pairs; no background; averages to `out`).  mode 1: the forward
+// model -- background and point sources added -- and the statistic terms of
+// the region's data pixels (the model image, when kept, gets their values);
+// mode 2 adds their adjoint seeds g = dS/dM (a.regG, for k_fast_region_g_r2c)
+// and the point sources' derivative sums.  The statistic partials take the
+// slots after the main window's (statBase + s); with doneTotal > 0 the last
+// CTA of the evaluation adds them up.  The main window's statistic pass skips
+// the region's pixels, so the two windows' pipelines share no dependency
+// before the final reduction.
+// PS: the model has point sources (their code is compiled only into the PS instance)
+template <bool PS>
+__global__ void __launch_bounds__(1024) k_fast_region_down(FastArgs a, FastGeom g, const cplx<float> *__restrict__ rspec,
+                                                          FFTPlan<float> plan, const cplx<float> *__restrict__ twL,
+                                                          float *__restrict__ out, int mode, int statBase,
+                                                          int doneTotal) {
+  pdl_wait();
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ float psAcc[4 * kMaxPsFast];
+  const int b = blockIdx.y, s = blockIdx.x;  // replaced data row within the region
+  const int k = g.rScale;
+  const int M = plan.n, ls = M + 1;
+  cplx<float> *bufX = reinterpret_cast<cplx<float> *>(smem);
+  cplx<float> *bufA = bufX + k * ls;
+  cplx<float> *bufB = bufA + k * ls;
+  if constexpr (PS)
+    if (mode == 2)
+      for (int i = threadIdx.x; i < 4 * a.nPs; i += blockDim.x) psAcc[i] = 0.f;
+  const cplx<float> *in = rspec + (long)b * g.rSpecBatch + (long)(s * k) * g.rSpecPitch;
+  const FastDiv byM(M), byM1(M + 1);
+  for (int idx = threadIdx.x; idx < k * (M + 1); idx += blockDim.x) {
+    const int l = byM1.div(idx), kk = idx - l * (M + 1);
+    bufX[l * ls + kk] = in[(long)l * g.rSpecPitch + kk];
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < k * M; idx += blockDim.x) {
+    const int l = byM.div(idx), kk = idx - l * M;
+    bufA[l * ls + kk] = c2r_pre(bufX + l * ls, kk, M, twL);
+  }
+  __syncthreads();
+  cplx<float> *Z = block_fft(bufA, bufB, plan, k, ls, 1, +1, false);
+  pdl_trigger();
+  const float inv = 1.f / (float)(k * k);
+  if (mode == 0) {
+    for (int t = threadIdx.x; t < g.rCols; t += blockDim.x) {
+      float acc = 0.f;
+      for (int u = 0; u < k; u++)
+        for (int v = 0; v < k; v++) {
+          const int col = t * k + v;
+          const cplx<float> z = Z[u * ls + (col >> 1)];
+          acc += (col & 1) ? z.y : z.x;
+        }
+      out[((long)b * g.rRows + s) * g.rCols + t] = acc * inv;
+    }
+    return;
+  }
+  if (a.dataStride) {  // image stack: this entry's data and weights
+    const long img = a.entry ? a.entry[b] : b;
+    a.data += img * a.dataStride;
+    a.weight += img * a.dataStride;
+  }
+  if (a.count && a.countStride) a.count += (a.entry ? a.entry[b] : b) * a.countStride;  // batched bootstrap
+  const float bg = a.bgLevel[2 * b + 1];
+  const int row = g.ry0 + s;
+  float S = 0.f, SG = 0.f;
+  for (int t = threadIdx.x; t < g.rCols; t += blockDim.x) {
+    float acc = 0.f;
+    for (int u = 0; u < k; u++)
+      for (int v = 0; v < k; v++) {
+        const int col = t * k + v;
+        const cplx<float> z = Z[u * ls + (col >> 1)];
+        acc += (col & 1) ? z.y : z.x;
+      }
+    const int col = g.rx0 + t;
+    if constexpr (PS) acc += ps_region(a, k, b, row, col, 0.f, nullptr);
+    const float m = acc * inv + bg;
+    const long zi = (long)row * g.nDataCols + col;
+    if (a.modelOut) a.modelOut[(long)b * g.nDataRows * g.nDataCols + zi] = m;
+    float gz;
+    stat_term(a, zi, m, S, gz);
+    SG += gz * a.psfSumOs;
+    if (mode == 2) {
+      if constexpr (PS)
+        if (gz != 0.f) ps_region(a, k, b, row, col, gz * inv, psAcc);
+      a.regG[((long)b * g.rRows + s) * g.rCols + t] = gz;
+    }
+  }
+  stat_partials(a, b, statBase + s, S, SG);
+  if constexpr (PS) {
+    if (mode == 2) {
+      __syncthreads();
+      for (int i = threadIdx.x; i < 4 * a.nPs; i += blockDim.x)
+        a.psPart[((long)b * 4 * a.nPs + i) * a.partStride + statBase + s] = make_float2(psAcc[i], 0.f);
+    }
+  }
+  if (doneTotal > 0) finish_cta(a, b, doneTotal, 0);
+}
+
 template <bool PS>
 __global__ void __launch_bounds__(1024) k_fast_stat_rows(FastArgs a, FastGeom g, FFTPlan<float> plan,
                                                         const cplx<float> *__restrict__ twL, int rpb, int wantGrad,
@@ -828,7 +913,6 @@ __global__ void __launch_bounds__(1024) k_fast_stat_rows(FastArgs a, FastGeom g,
   cplx<float> *bufX = reinterpret_cast<cplx<float> *>(smem);
   cplx<float> *bufA = bufX + rpb * ls;
   cplx<float> *bufB = bufA + rpb * ls;
-  __shared__ ffloat red[2][32];
   __shared__ float psAcc[4 * kMaxPsFast];
   if constexpr (PS)
     for (int i = threadIdx.x; i < 4 * a.nPs; i += blockDim.x) psAcc[i] = 0.f;
@@ -868,35 +952,18 @@ __global__ void __launch_bounds__(1024) k_fast_stat_rows(FastArgs a, FastGeom g,
         const int col = 2 * k + e;
         if (col >= g.nDataCols) continue;
         const long zi = (long)row * g.nDataCols + col;
-        float m = (e ? zz.y : zz.x) + bg;
-        bool inReg = false;
-        long ri = 0;
-        if (g.hasRegion) {
+        if (g.hasRegion) {  // the region's pixels: k_fast_region_down
           const int rr = row - g.ry0, rc = col - g.rx0;
-          if (rr >= 0 && rr < g.rRows && rc >= 0 && rc < g.rCols) {
-            inReg = true;
-            ri = ((long)b * g.rRows + rr) * g.rCols + rc;
-            m = a.regModel[ri];
-          }
+          if (rr >= 0 && rr < g.rRows && rc >= 0 && rc < g.rCols) continue;
         }
-        if constexpr (PS)
-          if (!inReg) m += ps_main(a, b, row, col, 0.f, nullptr);
+        float m = (e ? zz.y : zz.x) + bg;
+        if constexpr (PS) m += ps_main(a, b, row, col, 0.f, nullptr);
         if (a.modelOut) a.modelOut[(long)b * g.nDataRows * g.nDataCols + zi] = m;
         float gz;
         stat_term(a, zi, m, S, gz);
-        SG += gz * (inReg ? a.psfSumOs : a.psfSum);
-        if constexpr (PS) {
-          if (wantGrad && gz != 0.f) {
-            if (inReg)
-              ps_region(a, g.rScale, b, row, col, gz * (1.f / (float)(g.rScale * g.rScale)), psAcc);
-            else
-              ps_main(a, b, row, col, gz, psAcc);
-          }
-        }
-        if (inReg) {
-          if (wantGrad) a.regG[ri] = gz;
-          gz = 0.f;
-        }
+        SG += gz * a.psfSum;
+        if constexpr (PS)
+          if (wantGrad && gz != 0.f) ps_main(a, b, row, col, gz, psAcc);
         gv[e] = gz;
       }
       G[l * ls + k] = {gv[0], gv[1]};
@@ -912,28 +979,7 @@ __global__ void __launch_bounds__(1024) k_fast_stat_rows(FastArgs a, FastGeom g,
     }
   }
   pdl_trigger();
-  // CTA partial sums of (S, SG): FP32 over the thread's pixels and the warp,
-  // double-float across warps
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  S = warp_sum(S);
-  SG = warp_sum(SG);
-  if (lane == 0) {
-    red[0][wid] = ff_make(S);
-    red[1][wid] = ff_make(SG);
-  }
-  __syncthreads();
-  if (wid == 0) {
-    const int nw = blockDim.x >> 5;
-    ffloat v0 = lane < nw ? red[0][lane] : ffloat{0.f, 0.f};
-    ffloat v1 = lane < nw ? red[1][lane] : ffloat{0.f, 0.f};
-    v0 = ff_warp_sum(v0);
-    v1 = ff_warp_sum(v1);
-    if (lane == 0) {
-      float2 *p = a.statPart + (long)b * 2 * a.partStride + blockIdx.x;
-      p[0] = ff_store(v0);
-      p[a.partStride] = ff_store(v1);
-    }
-  }
+  stat_partials(a, b, blockIdx.x, S, SG);
   if constexpr (PS) {
     if (wantGrad) {
       __syncthreads();
@@ -1620,8 +1666,14 @@ static FFTPlan<float> plan32(const FFTLen &L, bool half) {
 }
 
 
-int fast_stat_blocks(const FastGeom &g, const FastTune &t) {
+// CTAs of the main window's statistic pass, and of the whole statistic (the
+// region's block-average CTAs, one per replaced data row, take the slots after)
+static int fast_stat_main_blocks(const FastGeom &g, const FastTune &t) {
   return (g.nDataRows + t.rowRpb - 1) / t.rowRpb;
+}
+
+int fast_stat_blocks(const FastGeom &g, const FastTune &t) {
+  return fast_stat_main_blocks(g, t) + (g.hasRegion ? g.rRows : 0);
 }
 
 static WinDesc main_win(const FastGeom &g, void *spec) {
@@ -1779,7 +1831,8 @@ static cudaError_t launch_los_grad(const FastArgs &a, const WinDesc &w, int nBat
                     doneTotal);
 }
 
-static cudaError_t launch_region_down(const FastPlan &p, const FastArgs &a, int nBatch, cudaStream_t st) {
+static cudaError_t launch_region_down(const FastPlan &p, const FastArgs &a, int nBatch, bool wantGrad,
+                                      cudaStream_t st, int doneTotal) {
   const FastGeom &g = p.g;
   const int M = p.Rx->half.n;
   const size_t sm = sizeof(cplx<float>) * 3 * g.rScale * (M + 1);
@@ -1787,7 +1840,8 @@ static cudaError_t launch_region_down(const FastPlan &p, const FastArgs &a, int 
   ensure_smem(kern, sm);
   return launch_pdl(kern, dim3(g.rRows, nBatch), dim3(line_threads(M * g.rScale / 2)), sm, st, a, g,
                     reinterpret_cast<const cplx<float> *>(a.rspec), plan32(*p.Rx, true),
-                    reinterpret_cast<const cplx<float> *>(p.Rx->twL32), a.regModel, 1);
+                    reinterpret_cast<const cplx<float> *>(p.Rx->twL32), (float *)nullptr, wantGrad ? 2 : 1,
+                    fast_stat_main_blocks(g, p.tune), doneTotal);
 }
 
 static cudaError_t launch_stat(const FastPlan &p, const FastArgs &a, int nBatch, bool wantGrad, cudaStream_t st,
@@ -1814,9 +1868,10 @@ static cudaError_t launch_region_g(const FastPlan &p, const FastArgs &a, int nBa
 
 
 // The whole statistic (+ gradient) evaluation.  With p.side set, the
-// oversampled-region pipeline runs on the side stream, forked after the
-// main-window subsample table and joined before the statistic (forward) and
-// before the final reduction (adjoint).
+// oversampled region's pipeline -- subsample table, model rows, convolution,
+// block average with the region pixels' statistic, and with the gradient its
+// adjoint -- runs on the side stream, forked after the set-up and joined at
+// the end; the last CTA of either window's final pass adds up the partials.
 cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool wantGrad, cudaStream_t st) {
   const FastGeom &g = p.g;
   if (!a.done) return cudaErrorInvalidValue;  // the final reduction needs the completion counters
@@ -1831,6 +1886,7 @@ cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool 
   const int nMain = fast_grad_blocks(g, tu), nReg = fast_reg_grad_blocks(g, tu);
   const int nLos = los ? kLosCtas * (g.hasRegion ? 2 : 1) : 0;
   const int nTot = nMain + nReg + nLos;
+  const int nStat = fast_stat_blocks(g, tu);
   WinDesc mw = main_win(g, a.spec), rw = region_win(g, a.rspec);
   mw.losVal = a.losVal;
   mw.losRt = a.losRt;
@@ -1856,34 +1912,31 @@ cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool 
     STAGE("region_cols_conv", rs,
           launch_cols32(a.rspec, g.rSpecPitch, g.rSpecBatch, p.Rx->L / 2 + 1, g.rWinRows, g.rSubRows, p.Hr,
                              p.hrPitch, *p.Ry, rscale, 1, nBatch, rs, tu.colCpb, 0, 1, nullptr, tu.colThreads));
-    STAGE("region_down", rs, launch_region_down(p, a, nBatch, rs));
+    STAGE("region_down", rs, launch_region_down(p, a, nBatch, wantGrad, rs, wantGrad ? 0 : nStat));
+    if (wantGrad) {
+      STAGE("region_g_r2c", rs, launch_region_g(p, a, nBatch, rs));
+      STAGE("region_cols_adjoint", rs,
+            launch_cols32(a.rspec, g.rSpecPitch, g.rSpecBatch, p.Rx->L / 2 + 1, g.rSubRows, g.rWinRows, p.Hr,
+                          p.hrPitch, *p.Ry, rscale, 2, nBatch, rs, tu.colCpb, 0, 1, nullptr, tu.colThreads));
+      STAGE("region_grad_rows", rs, launch_grad(a, rw, *p.Rx, nBatch, nMain, 1, tu, rs, nTot));
+      if (los) STAGE("region_los_grad", rs, launch_los_grad(a, rw, nBatch, nMain + nReg + kLosCtas, rks, rs, nTot));
+    }
   }
   if (los) STAGE("los_eval", st, launch_los_eval(a, mw, nBatch, mks, st));
   STAGE("eval_r2c", st, launch_eval(a, mw, *p.Lx, nBatch, 0, tu, st));
   STAGE("cols_conv", st,
         launch_cols32(a.spec, g.specPitch, g.specBatch, p.Lx->L / 2 + 1, g.winRows, g.nDataRows, p.H, p.hPitch,
                            *p.Ly, scale, 1, nBatch, st, tu.colCpb, p.hBatch, 1, p.hMap, tu.colThreads));
-  if (fork) {
-    cudaError_t e = cudaEventRecord(p.join0, rs);
-    if (!e) e = cudaStreamWaitEvent(st, p.join0, 0);
-    if (e) return e;
-  }
-  // without the gradient the statistic pass is the last one: its final CTA
-  // per vector adds the partials up; with it, the gradient passes' last CTA does
-  STAGE("stat_rows", st, launch_stat(p, a, nBatch, wantGrad, st, wantGrad ? 0 : fast_stat_blocks(g, tu)));
-  if (!wantGrad) return cudaSuccess;
-  if (fork) {
-    cudaError_t e = cudaEventRecord(p.fork1, st);
-    if (!e) e = cudaStreamWaitEvent(rs, p.fork1, 0);
-    if (e) return e;
-  }
-  if (g.hasRegion) {
-    STAGE("region_g_r2c", rs, launch_region_g(p, a, nBatch, rs));
-    STAGE("region_cols_adjoint", rs,
-          launch_cols32(a.rspec, g.rSpecPitch, g.rSpecBatch, p.Rx->L / 2 + 1, g.rSubRows, g.rWinRows, p.Hr,
-                             p.hrPitch, *p.Ry, rscale, 2, nBatch, rs, tu.colCpb, 0, 1, nullptr, tu.colThreads));
-    STAGE("region_grad_rows", rs, launch_grad(a, rw, *p.Rx, nBatch, nMain, 1, tu, rs, nTot));
-    if (los) STAGE("region_los_grad", rs, launch_los_grad(a, rw, nBatch, nMain + nReg + kLosCtas, rks, rs, nTot));
+  // without the gradient the statistic passes are the last ones: the final
+  // CTA per vector adds the partials up; with it, the gradient passes' last CTA does
+  STAGE("stat_rows", st, launch_stat(p, a, nBatch, wantGrad, st, wantGrad ? 0 : nStat));
+  if (!wantGrad) {
+    if (fork) {
+      cudaError_t e = cudaEventRecord(p.join0, rs);
+      if (!e) e = cudaStreamWaitEvent(st, p.join0, 0);
+      if (e) return e;
+    }
+    return cudaSuccess;
   }
   STAGE("cols_adjoint", st,
         launch_cols32(a.spec, g.specPitch, g.specBatch, p.Lx->L / 2 + 1, g.nDataRows, g.winRows, p.H, p.hPitch,
@@ -1954,7 +2007,7 @@ cudaError_t fast_jtwj(const FastPlan &p, const FastArgs &a, const JtwjArgs &J, i
       stage_begin(p, "jtwj_region_down", st);
       k_fast_region_down<false><<<dim3(g.rRows, nB), line_threads(M * g.rScale / 2), sm, st>>>(
           a, g, reinterpret_cast<const cplx<float> *>(J.drspec), plan32(*p.Rx, true),
-          reinterpret_cast<const cplx<float> *>(p.Rx->twL32), J.regDeriv, 0);
+          reinterpret_cast<const cplx<float> *>(p.Rx->twL32), J.regDeriv, 0, 0, 0);
       if ((e = cudaGetLastError())) return e;
       stage_end(p, "jtwj_region_down", st);
     }

@@ -276,7 +276,7 @@ struct imfit_model_s {
   bool fastReady = false;
   FastGeom fg{};
   FFTLen Fx, Fy, FRx, FRy;
-  DevBuf<float> dH32, dHr32, dData32, dW32, dExtra32, dCount32, dBg, dRegModel, dRegG, dModelOut;
+  DevBuf<float> dH32, dHr32, dData32, dW32, dExtra32, dCount32, dBg, dRegG, dModelOut;
   DevBuf<float> dCountBatch;  // batched bootstrap: [sample][data pixel] multiplicities
   int bootBatch = 0;          // number of samples while a batched bootstrap fit runs
   DevBuf<float> dSpec32, dRSpec32;  // complex
@@ -1303,7 +1303,6 @@ struct imfit_model_s {
     if (!e) e = dBg.reserve((size_t)B * 2);
     if (!e) e = dSpec32.reserve(2 * (size_t)B * g.specBatch);
     if (!e && g.hasRegion) e = dRSpec32.reserve(2 * (size_t)B * g.rSpecBatch);
-    if (!e && g.hasRegion) e = dRegModel.reserve((size_t)B * g.rRows * g.rCols);
     if (!e && g.hasRegion) e = dRegG.reserve((size_t)B * g.rRows * g.rCols);
     if (!e) e = dStatPart.reserve((size_t)B * 2 * stride);
     if (!e) e = dGradPart.reserve((size_t)B * nP * stride);
@@ -1340,9 +1339,11 @@ struct imfit_model_s {
 
   static constexpr int kBoxMain = 24;  // covers radius 10 around a centre, main grid
   // CTA count of the finest launch shape (one row per CTA): bounds every shape
+  // (statistic: main rows and the region's replaced rows; gradient: window rows)
   int partStride() const {
     const int los = hasLos ? kLosCtas * (fg.hasRegion ? 2 : 1) : 0;
-    return std::max(fg.nDataRows, fg.winRows + (fg.hasRegion ? fg.rWinRows : 0) + los);
+    return std::max(fg.nDataRows + (fg.hasRegion ? fg.rRows : 0),
+                    fg.winRows + (fg.hasRegion ? fg.rWinRows : 0) + los);
   }
   int boxReg() const { return fg.hasRegion ? 20 * fg.rScale + 5 : 0; }
   // the region's subsample lattice: pixels within radius 4 of a centre (every
@@ -1406,7 +1407,6 @@ struct imfit_model_s {
     a.psfSumOs = (float)psfSumOsFast;
     a.spec = dSpec32.p;
     a.rspec = dRSpec32.p;
-    a.regModel = dRegModel.p;
     a.regG = dRegG.p;
     a.statPart = dStatPart.p;
     a.gradPart = dGradPart.p;
