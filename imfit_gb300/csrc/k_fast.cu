@@ -47,6 +47,7 @@ struct WinDesc {
   int xOrig, yOrig;  // main: IRAF x = col + xOrig, y = row + yOrig
   int x1, y1, offX, offY, scale;
   float startOff, frac;
+  float invScale;  // 1 / scale, correctly rounded
   int specPitch;
   long specBatch;
   cplx<float> *spec;
@@ -55,10 +56,12 @@ struct WinDesc {
   float *losVal, *losRt;
 };
 
-__device__ __forceinline__ int floordiv(int a, int b) {
-  int q = a / b;
-  if ((a % b != 0) && ((a < 0) != (b < 0))) q--;
-  return q;
+// floor(a / scale) for the window's scale: floor((a + 1/2) * (1/scale)) in
+// FP32 with the correctly rounded reciprocal is exact for |a| < 2^21 and
+// scales 1..128 (checked exhaustively), far beyond any window coordinate;
+// four instructions instead of an integer division.
+__device__ __forceinline__ int floordiv_scale(int a, float invScale) {
+  return (int)floorf(((float)a + 0.5f) * invScale);
 }
 
 __device__ __forceinline__ void win_offsets(const WinDesc &w, const CompF32 &c, int row, int col, float &dx,
@@ -70,7 +73,7 @@ __device__ __forceinline__ void win_offsets(const WinDesc &w, const CompF32 &c, 
     yi = row + w.yOrig;
   } else {
     const int tx = col + w.offX, ty = row + w.offY;
-    const int qx = floordiv(tx, w.scale), qy = floordiv(ty, w.scale);
+    const int qx = floordiv_scale(tx, w.invScale), qy = floordiv_scale(ty, w.invScale);
     xi = w.x1 + qx;
     yi = w.y1 + qy;
     xf = w.startOff + (float)(tx - qx * w.scale) * w.frac;
@@ -808,15 +811,17 @@ __device__ __forceinline__ void stat_partials(const FastArgs &a, int b, int slot
 // parameter) pairs; no background; averages to `out`).  mode 1: the forward
 // model -- background and point sources added -- and the statistic terms of
 // the region's data pixels (the model image, when kept, gets their values);
-// mode 2 adds their adjoint seeds g = dS/dM (a.regG, for k_fast_region_g_r2c)
-// and the point sources' derivative sums.  The statistic partials take the
+// mode 2 adds their adjoint seeds g = dS/dM, spread as g / k^2 over the
+// subpixels and row-transformed into the CTA's k rows of the region spectrum
+// (the input of the adjoint column pass), and the point sources' derivative
+// sums.  The statistic partials take the
 // slots after the main window's (statBase + s); with doneTotal > 0 the last
 // CTA of the evaluation adds them up.  The main window's statistic pass skips
 // the region's pixels, so the two windows' pipelines share no dependency
 // before the final reduction.
 // PS: the model has point sources (their code is compiled only into the PS instance)
 template <bool PS>
-__global__ void __launch_bounds__(1024) k_fast_region_down(FastArgs a, FastGeom g, const cplx<float> *__restrict__ rspec,
+__global__ void __launch_bounds__(1024) k_fast_region_down(FastArgs a, FastGeom g, cplx<float> *__restrict__ rspec,
                                                           FFTPlan<float> plan, const cplx<float> *__restrict__ twL,
                                                           float *__restrict__ out, int mode, int statBase,
                                                           int doneTotal) {
@@ -832,7 +837,7 @@ __global__ void __launch_bounds__(1024) k_fast_region_down(FastArgs a, FastGeom 
   if constexpr (PS)
     if (mode == 2)
       for (int i = threadIdx.x; i < 4 * a.nPs; i += blockDim.x) psAcc[i] = 0.f;
-  const cplx<float> *in = rspec + (long)b * g.rSpecBatch + (long)(s * k) * g.rSpecPitch;
+  cplx<float> *in = rspec + (long)b * g.rSpecBatch + (long)(s * k) * g.rSpecPitch;
   const FastDiv byM(M), byM1(M + 1);
   for (int idx = threadIdx.x; idx < k * (M + 1); idx += blockDim.x) {
     const int l = byM1.div(idx), kk = idx - l * (M + 1);
@@ -868,6 +873,7 @@ __global__ void __launch_bounds__(1024) k_fast_region_down(FastArgs a, FastGeom 
   if (a.count && a.countStride) a.count += (a.entry ? a.entry[b] : b) * a.countStride;  // batched bootstrap
   const float bg = a.bgLevel[2 * b + 1];
   const int row = g.ry0 + s;
+  float *gRow = reinterpret_cast<float *>(bufX);  // the loaded spectrum is consumed
   float S = 0.f, SG = 0.f;
   for (int t = threadIdx.x; t < g.rCols; t += blockDim.x) {
     float acc = 0.f;
@@ -888,10 +894,30 @@ __global__ void __launch_bounds__(1024) k_fast_region_down(FastArgs a, FastGeom 
     if (mode == 2) {
       if constexpr (PS)
         if (gz != 0.f) ps_region(a, k, b, row, col, gz * inv, psAcc);
-      a.regG[((long)b * g.rRows + s) * g.rCols + t] = gz;
+      gRow[t] = gz;
     }
   }
-  stat_partials(a, b, statBase + s, S, SG);
+  stat_partials(a, b, statBase + s, S, SG);  // (its barrier also publishes gRow)
+  if (mode == 2) {
+    // adjoint seed: g / k^2 on each of the row's k x k subpixels.  Its k
+    // subpixel rows are equal, so one r2c serves all k rows of the region
+    // spectrum (those this CTA read above).
+    cplx<float> *G = (Z == bufA) ? bufB : bufA;
+    const float invk = 1.f / (float)k;
+    for (int kk = threadIdx.x; kk < M; kk += blockDim.x) {
+      const int c0 = 2 * kk, c1 = 2 * kk + 1;
+      cplx<float> z;
+      z.x = (c0 < g.rSubCols) ? gRow[floordiv_scale(c0, invk)] * inv : 0.f;
+      z.y = (c1 < g.rSubCols) ? gRow[floordiv_scale(c1, invk)] * inv : 0.f;
+      G[kk] = z;
+    }
+    __syncthreads();
+    cplx<float> *R = block_fft(G, Z, plan, 1, ls, 1, -1, false);
+    for (int kk = threadIdx.x; kk <= M; kk += blockDim.x) {
+      const cplx<float> v = r2c_post(R, kk, M, twL);
+      for (int u = 0; u < k; u++) in[(long)u * g.rSpecPitch + kk] = v;
+    }
+  }
   if constexpr (PS) {
     if (mode == 2) {
       __syncthreads();
@@ -988,31 +1014,6 @@ __global__ void __launch_bounds__(1024) k_fast_stat_rows(FastArgs a, FastGeom g,
     }
   }
   if (doneTotal > 0) finish_cta(a, b, doneTotal, 0);
-}
-
-// --------------------------- region adjoint seed: g/k^2 on subpixels, r2c
-__global__ void __launch_bounds__(1024) k_fast_region_g_r2c(FastArgs a, FastGeom g, cplx<float> *__restrict__ rspec,
-                                                           FFTPlan<float> plan, const cplx<float> *__restrict__ twL) {
-  pdl_wait();
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int b = blockIdx.y, u = blockIdx.x;  // subpixel row
-  const int M = plan.n, ls = M + 1;
-  cplx<float> *bufA = reinterpret_cast<cplx<float> *>(smem);
-  cplx<float> *bufB = bufA + ls;
-  const int k = g.rScale;
-  const float inv = 1.f / (float)(k * k);
-  const float *gr = a.regG + ((long)b * g.rRows + u / k) * g.rCols;
-  for (int kk = threadIdx.x; kk < M; kk += blockDim.x) {
-    const int c0 = 2 * kk, c1 = 2 * kk + 1;
-    cplx<float> z;
-    z.x = (c0 < g.rSubCols) ? gr[c0 / k] * inv : 0.f;
-    z.y = (c1 < g.rSubCols) ? gr[c1 / k] * inv : 0.f;
-    bufA[kk] = z;
-  }
-  __syncthreads();
-  cplx<float> *Z = block_fft(bufA, bufB, plan, 1, ls, 1, -1, false);
-  cplx<float> *out = rspec + (long)b * g.rSpecBatch + (long)u * g.rSpecPitch;
-  for (int kk = threadIdx.x; kk <= M; kk += blockDim.x) out[kk] = r2c_post(Z, kk, M, twL);
 }
 
 // ---------------------------------------- gradient pass over the window
@@ -1699,6 +1700,7 @@ static WinDesc region_win(const FastGeom &g, void *rspec) {
   w.offX = g.rWinOffX;
   w.offY = g.rWinOffY;
   w.scale = g.rScale;
+  w.invScale = 1.f / (float)g.rScale;
   w.startOff = g.rStartOff;
   w.frac = g.rFrac;
   w.specPitch = g.rSpecPitch;
@@ -1839,7 +1841,7 @@ static cudaError_t launch_region_down(const FastPlan &p, const FastArgs &a, int 
   auto kern = a.nPs ? k_fast_region_down<true> : k_fast_region_down<false>;
   ensure_smem(kern, sm);
   return launch_pdl(kern, dim3(g.rRows, nBatch), dim3(line_threads(M * g.rScale / 2)), sm, st, a, g,
-                    reinterpret_cast<const cplx<float> *>(a.rspec), plan32(*p.Rx, true),
+                    reinterpret_cast<cplx<float> *>(a.rspec), plan32(*p.Rx, true),
                     reinterpret_cast<const cplx<float> *>(p.Rx->twL32), (float *)nullptr, wantGrad ? 2 : 1,
                     fast_stat_main_blocks(g, p.tune), doneTotal);
 }
@@ -1857,14 +1859,6 @@ static cudaError_t launch_stat(const FastPlan &p, const FastArgs &a, int nBatch,
                     reinterpret_cast<const cplx<float> *>(p.Lx->twL32), rpb, wantGrad ? 1 : 0, doneTotal);
 }
 
-static cudaError_t launch_region_g(const FastPlan &p, const FastArgs &a, int nBatch, cudaStream_t st) {
-  const FastGeom &g = p.g;
-  const int M = p.Rx->half.n;
-  const size_t sm = sizeof(cplx<float>) * 2 * (M + 1);
-  return launch_pdl(k_fast_region_g_r2c, dim3(g.rSubRows, nBatch), dim3(line_threads(M)), sm, st, a, g,
-                    reinterpret_cast<cplx<float> *>(a.rspec), plan32(*p.Rx, true),
-                    reinterpret_cast<const cplx<float> *>(p.Rx->twL32));
-}
 
 
 // The whole statistic (+ gradient) evaluation.  With p.side set, the
@@ -1914,7 +1908,6 @@ cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool 
                              p.hrPitch, *p.Ry, rscale, 1, nBatch, rs, tu.colCpb, 0, 1, nullptr, tu.colThreads));
     STAGE("region_down", rs, launch_region_down(p, a, nBatch, wantGrad, rs, wantGrad ? 0 : nStat));
     if (wantGrad) {
-      STAGE("region_g_r2c", rs, launch_region_g(p, a, nBatch, rs));
       STAGE("region_cols_adjoint", rs,
             launch_cols32(a.rspec, g.rSpecPitch, g.rSpecBatch, p.Rx->L / 2 + 1, g.rSubRows, g.rWinRows, p.Hr,
                           p.hrPitch, *p.Ry, rscale, 2, nBatch, rs, tu.colCpb, 0, 1, nullptr, tu.colThreads));
@@ -2006,7 +1999,7 @@ cudaError_t fast_jtwj(const FastPlan &p, const FastArgs &a, const JtwjArgs &J, i
       const size_t sm = sizeof(cplx<float>) * 3 * g.rScale * (M + 1);
       stage_begin(p, "jtwj_region_down", st);
       k_fast_region_down<false><<<dim3(g.rRows, nB), line_threads(M * g.rScale / 2), sm, st>>>(
-          a, g, reinterpret_cast<const cplx<float> *>(J.drspec), plan32(*p.Rx, true),
+          a, g, reinterpret_cast<cplx<float> *>(J.drspec), plan32(*p.Rx, true),
           reinterpret_cast<const cplx<float> *>(p.Rx->twL32), J.regDeriv, 0, 0, 0);
       if ((e = cudaGetLastError())) return e;
       stage_end(p, "jtwj_region_down", st);
@@ -2388,7 +2381,6 @@ void fast_prepare_kernels() {
   allow_max_smem((const void *)k_fast_stat_rows<true>);
   allow_max_smem((const void *)k_fast_region_down<false>);
   allow_max_smem((const void *)k_fast_region_down<true>);
-  allow_max_smem((const void *)k_fast_region_g_r2c);
   allow_max_smem((const void *)k_fast_deriv_r2c);
   allow_max_smem((const void *)k_fast_jtwj_rows<false>);
   allow_max_smem((const void *)k_fast_jtwj_rows<true>);

@@ -233,7 +233,6 @@ struct FastArgs {
   // spectra and scratch
   void *spec;            // main half spectrum [B][Ly][specPitch] complex float
   void *rspec;           // region half spectrum
-  float *regG;           // [B][rRows][rCols] dS/dM for region pixels
   // per-CTA partial sums, double-float (hi, lo) pairs: each thread sums its
   // few pixels in FP32 and the warp's 32 thread sums in FP32; every level
   // above (across warps, across CTAs) adds in double-float; the final value
