@@ -64,11 +64,20 @@ __device__ __forceinline__ int floordiv_scale(int a, float invScale) {
   return (int)floorf(((float)a + 0.5f) * invScale);
 }
 
-__device__ __forceinline__ void win_offsets(const WinDesc &w, const CompF32 &c, int row, int col, float &dx,
-                                            float &dy) {
+__device__ __forceinline__ bool subsampling_type(int t) {
+  return t == F_SERSIC || t == F_EXP || t == F_MOFFAT || t == F_GAUSS;
+}
+
+// Offsets (dx, dy) of window pixel (row, col) from component c's centre,
+// the integer parts exact and the fractions added once.  REG: the window is
+// an oversampled region (fixed at compile time in the pixel loops, so the
+// main window's loops carry none of the region's index arithmetic).
+template <bool REG>
+__device__ __forceinline__ void win_offsets_t(const WinDesc &w, const CompF32 &c, int row, int col, float &dx,
+                                              float &dy) {
   int xi, yi;
   float xf = 0.f, yf = 0.f;
-  if (!w.isRegion) {
+  if constexpr (!REG) {
     xi = col + w.xOrig;
     yi = row + w.yOrig;
   } else {
@@ -81,6 +90,21 @@ __device__ __forceinline__ void win_offsets(const WinDesc &w, const CompF32 &c, 
   }
   dx = (float)(xi - c.x0i) + (xf - c.x0r);
   dy = (float)(yi - c.y0i) + (yf - c.y0r);
+}
+
+__device__ __forceinline__ void win_offsets(const WinDesc &w, const CompF32 &c, int row, int col, float &dx,
+                                            float &dy) {
+  if (w.isRegion)
+    win_offsets_t<true>(w, c, row, col, dx, dy);
+  else
+    win_offsets_t<false>(w, c, row, col, dx, dy);
+}
+
+// Rows [r0, r0 + n) meet component c's subsample box (rows [br0, br0 + side))?
+// Only then can a pixel need the subsample table; the pixel loops of the
+// other CTAs are compiled without the test.
+__device__ __forceinline__ bool rows_meet_box(const CompF32 &c, int r0, int n, int br0, int side) {
+  return c.subsample && subsampling_type(c.type) && r0 < br0 + side && br0 < r0 + n;
 }
 
 __device__ __forceinline__ float warp_sum(float v) {
@@ -173,9 +197,6 @@ __device__ __forceinline__ long sub_base(const FastArgs &a, int b, int c, int w)
 // line-of-sight kernels)
 __device__ __forceinline__ bool in_rows(int t) { return t != F_FLATSKY && !is_los(t) && !is_point_source(t); }
 
-__device__ __forceinline__ bool subsampling_type(int t) {
-  return t == F_SERSIC || t == F_EXP || t == F_MOFFAT || t == F_GAUSS;
-}
 
 // Box origin (window col, row) around a component centre.  Every pixel whose
 // centre is within radius 10 of the component centre (the only ones the
@@ -465,7 +486,7 @@ __device__ __forceinline__ float sub_value(const FastArgs &a, const int *box, in
 // Adds component cc's value at every pixel of the CTA's rows to the row
 // buffer (one thread per complex point = two pixels; every pass maps the
 // same points to the same thread, so the passes need no barrier).
-template <int TY>
+template <int TY, bool REG, bool BOX>
 __device__ __forceinline__ void eval_pixels(const CompF32 cc, const WinDesc &w, int row0, int nl, int M, int ls,
                                             const FastDiv &byM, cplx<float> *buf, const float *tab, int side,
                                             int bc0, int br0) {
@@ -478,12 +499,12 @@ __device__ __forceinline__ void eval_pixels(const CompF32 cc, const WinDesc &w, 
       const int col = 2 * k + e;
       if (col >= w.cols) continue;
       float dx, dy;
-      win_offsets(w, cc, row, col, dx, dy);
+      win_offsets_t<REG>(w, cc, row, col, dx, dy);
       if constexpr (TY == F_TILTEDSKY) {
         v[e] = plane32(cc, dx, dy);
       } else {
         const Geo g = geo32(cc, dx, dy);
-        if (subsampling_t<TY>() && cc.subsample && g.r2 < 100.f && n_subsamples32(cc, fast_sqrt(g.r2)) > 1) {
+        if (BOX && subsampling_t<TY>() && g.r2 < 100.f && n_subsamples32(cc, fast_sqrt(g.r2)) > 1) {
           // subsampled pixel: the precomputed table (a direct average outside
           // the box, which the radius bound rules out)
           const int br = row - br0, bc = col - bc0;
@@ -497,6 +518,20 @@ __device__ __forceinline__ void eval_pixels(const CompF32 cc, const WinDesc &w, 
     cplx<float> &z = buf[l * ls + k];
     z.x += v[0];
     z.y += v[1];
+  }
+}
+
+// eval_pixels with the window kind and the box test chosen at run time
+template <int TY>
+__device__ __forceinline__ void eval_pixels_rt(bool reg, bool box, const CompF32 &cc, const WinDesc &w, int row0,
+                                               int nl, int M, int ls, const FastDiv &byM, cplx<float> *buf,
+                                               const float *tab, int side, int bc0, int br0) {
+  if (reg) {
+    if (box) eval_pixels<TY, true, true>(cc, w, row0, nl, M, ls, byM, buf, tab, side, bc0, br0);
+    else eval_pixels<TY, true, false>(cc, w, row0, nl, M, ls, byM, buf, tab, side, bc0, br0);
+  } else {
+    if (box) eval_pixels<TY, false, true>(cc, w, row0, nl, M, ls, byM, buf, tab, side, bc0, br0);
+    else eval_pixels<TY, false, false>(cc, w, row0, nl, M, ls, byM, buf, tab, side, bc0, br0);
   }
 }
 
@@ -532,13 +567,14 @@ __global__ void __launch_bounds__(1024) k_fast_eval_r2c(FastArgs a, WinDesc w, F
     if (!in_rows(cc.type)) continue;
     const float *tab = a.subTab + sub_base(a, b, c, win);
     const int bc0 = boxes[2 * c], br0 = boxes[2 * c + 1];
+    const bool box = rows_meet_box(cc, row0, nl, br0, side);
     switch (cc.type) {
-      case F_SERSIC: eval_pixels<F_SERSIC>(cc, w, row0, nl, M, ls, byM, bufA, tab, side, bc0, br0); break;
-      case F_EXP: eval_pixels<F_EXP>(cc, w, row0, nl, M, ls, byM, bufA, tab, side, bc0, br0); break;
-      case F_GRING: eval_pixels<F_GRING>(cc, w, row0, nl, M, ls, byM, bufA, tab, side, bc0, br0); break;
-      case F_MOFFAT: eval_pixels<F_MOFFAT>(cc, w, row0, nl, M, ls, byM, bufA, tab, side, bc0, br0); break;
-      case F_GAUSS: eval_pixels<F_GAUSS>(cc, w, row0, nl, M, ls, byM, bufA, tab, side, bc0, br0); break;
-      case F_TILTEDSKY: eval_pixels<F_TILTEDSKY>(cc, w, row0, nl, M, ls, byM, bufA, tab, side, bc0, br0); break;
+      case F_SERSIC: eval_pixels_rt<F_SERSIC>(w.isRegion, box, cc, w, row0, nl, M, ls, byM, bufA, tab, side, bc0, br0); break;
+      case F_EXP: eval_pixels_rt<F_EXP>(w.isRegion, box, cc, w, row0, nl, M, ls, byM, bufA, tab, side, bc0, br0); break;
+      case F_GRING: eval_pixels_rt<F_GRING>(w.isRegion, box, cc, w, row0, nl, M, ls, byM, bufA, tab, side, bc0, br0); break;
+      case F_MOFFAT: eval_pixels_rt<F_MOFFAT>(w.isRegion, box, cc, w, row0, nl, M, ls, byM, bufA, tab, side, bc0, br0); break;
+      case F_GAUSS: eval_pixels_rt<F_GAUSS>(w.isRegion, box, cc, w, row0, nl, M, ls, byM, bufA, tab, side, bc0, br0); break;
+      case F_TILTEDSKY: eval_pixels_rt<F_TILTEDSKY>(w.isRegion, box, cc, w, row0, nl, M, ls, byM, bufA, tab, side, bc0, br0); break;
       default: break;
     }
   }
@@ -1019,7 +1055,7 @@ __global__ void __launch_bounds__(1024) k_fast_stat_rows(FastArgs a, FastGeom g,
 // ---------------------------------------- gradient pass over the window
 // acc[0..1+NP] += r~ * dm/dtheta over the CTA's window pixels for component cc
 // (X0, Y0, then its function parameters); subsampled pixels from the table.
-template <int TY>
+template <int TY, bool REG, bool BOX>
 __device__ __forceinline__ void grad_pixels(const CompF32 cc, const WinDesc &w, const float *rt, int ls, int row0,
                                             int npix, const FastDiv &byCols, const float *tab, int side, int bc0,
                                             int br0, float *acc) {
@@ -1030,13 +1066,13 @@ __device__ __forceinline__ void grad_pixels(const CompF32 cc, const WinDesc &w, 
     const int row = row0 + l;
     const float r = rt[2 * l * ls + col];
     float dx, dy;
-    win_offsets(w, cc, row, col, dx, dy);
+    win_offsets_t<REG>(w, cc, row, col, dx, dy);
     if constexpr (TY == F_TILTEDSKY) {
       if (r == 0.f) continue;
       plane_grad32(cc, dx, dy, r, o);
     } else {
       const Geo g = geo32(cc, dx, dy);
-      if (subsampling_t<TY>() && cc.subsample && g.r2 < 100.f) {
+      if (BOX && subsampling_t<TY>() && g.r2 < 100.f) {
         const int ns = n_subsamples32(cc, fast_sqrt(g.r2));
         if (ns > 1) {
           const int br = row - br0, bc = col - bc0;
@@ -1062,6 +1098,19 @@ __device__ __forceinline__ void grad_pixels(const CompF32 cc, const WinDesc &w, 
     }
 #pragma unroll
     for (int q = 0; q < 2 + NP; q++) acc[q] += o[q];
+  }
+}
+
+template <int TY>
+__device__ __forceinline__ void grad_pixels_rt(bool reg, bool box, const CompF32 &cc, const WinDesc &w,
+                                               const float *rt, int ls, int row0, int npix, const FastDiv &byCols,
+                                               const float *tab, int side, int bc0, int br0, float *acc) {
+  if (reg) {
+    if (box) grad_pixels<TY, true, true>(cc, w, rt, ls, row0, npix, byCols, tab, side, bc0, br0, acc);
+    else grad_pixels<TY, true, false>(cc, w, rt, ls, row0, npix, byCols, tab, side, bc0, br0, acc);
+  } else {
+    if (box) grad_pixels<TY, false, true>(cc, w, rt, ls, row0, npix, byCols, tab, side, bc0, br0, acc);
+    else grad_pixels<TY, false, false>(cc, w, rt, ls, row0, npix, byCols, tab, side, bc0, br0, acc);
   }
 }
 
@@ -1118,15 +1167,16 @@ __global__ void __launch_bounds__(1024) k_fast_grad_rows(FastArgs a, WinDesc w, 
       const int side = win ? a.boxReg : a.boxMain;
       const float *tab = a.subTab + sub_base(a, b, c, win);
       const int bc0 = boxes[2 * c], br0 = boxes[2 * c + 1];
+      const bool box = rows_meet_box(cc, row0, nl, br0, side);
       float acc[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
       switch (cc.type) {
-        case F_SERSIC: grad_pixels<F_SERSIC>(cc, w, rt, ls, row0, npix, byCols, tab, side, bc0, br0, acc); break;
-        case F_EXP: grad_pixels<F_EXP>(cc, w, rt, ls, row0, npix, byCols, tab, side, bc0, br0, acc); break;
-        case F_GRING: grad_pixels<F_GRING>(cc, w, rt, ls, row0, npix, byCols, tab, side, bc0, br0, acc); break;
-        case F_MOFFAT: grad_pixels<F_MOFFAT>(cc, w, rt, ls, row0, npix, byCols, tab, side, bc0, br0, acc); break;
-        case F_GAUSS: grad_pixels<F_GAUSS>(cc, w, rt, ls, row0, npix, byCols, tab, side, bc0, br0, acc); break;
+        case F_SERSIC: grad_pixels_rt<F_SERSIC>(w.isRegion, box, cc, w, rt, ls, row0, npix, byCols, tab, side, bc0, br0, acc); break;
+        case F_EXP: grad_pixels_rt<F_EXP>(w.isRegion, box, cc, w, rt, ls, row0, npix, byCols, tab, side, bc0, br0, acc); break;
+        case F_GRING: grad_pixels_rt<F_GRING>(w.isRegion, box, cc, w, rt, ls, row0, npix, byCols, tab, side, bc0, br0, acc); break;
+        case F_MOFFAT: grad_pixels_rt<F_MOFFAT>(w.isRegion, box, cc, w, rt, ls, row0, npix, byCols, tab, side, bc0, br0, acc); break;
+        case F_GAUSS: grad_pixels_rt<F_GAUSS>(w.isRegion, box, cc, w, rt, ls, row0, npix, byCols, tab, side, bc0, br0, acc); break;
         case F_TILTEDSKY:
-          grad_pixels<F_TILTEDSKY>(cc, w, rt, ls, row0, npix, byCols, tab, side, bc0, br0, acc);
+          grad_pixels_rt<F_TILTEDSKY>(w.isRegion, box, cc, w, rt, ls, row0, npix, byCols, tab, side, bc0, br0, acc);
           break;
         default: break;
       }
@@ -1291,19 +1341,19 @@ __device__ __forceinline__ double block_sum_d(double v) {
 // Adds component cc's dm/dtheta at every pixel of window row `row` to the
 // derivative lines sl[q] (q: X0, Y0, then its function parameters; -1 = not
 // a derivative line); each column belongs to one thread.
-template <int TY>
+template <int TY, bool REG, bool BOX>
 __device__ __forceinline__ void deriv_pixels(const CompF32 cc, const WinDesc &w, int row, const int *sl,
                                              float *lines, int ls, const float *tab, int side, int bc0, int br0) {
   constexpr int NP = n_fparams<TY>();
   for (int col = threadIdx.x; col < w.cols; col += blockDim.x) {
     float dx, dy;
-    win_offsets(w, cc, row, col, dx, dy);
+    win_offsets_t<REG>(w, cc, row, col, dx, dy);
     float o[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     if constexpr (TY == F_TILTEDSKY) {
       plane_grad32(cc, dx, dy, 1.f, o);
     } else {
       const Geo g = geo32(cc, dx, dy);
-      const int ns = (subsampling_t<TY>() && cc.subsample && g.r2 < 100.f) ? n_subsamples32(cc, fast_sqrt(g.r2)) : 1;
+      const int ns = (BOX && subsampling_t<TY>() && g.r2 < 100.f) ? n_subsamples32(cc, fast_sqrt(g.r2)) : 1;
       if (ns > 1) {
         const int br = row - br0, bc = col - bc0;
         if (br >= 0 && br < side && bc >= 0 && bc < side) {
@@ -1328,6 +1378,19 @@ __device__ __forceinline__ void deriv_pixels(const CompF32 cc, const WinDesc &w,
 #pragma unroll
     for (int q = 0; q < 2 + NP; q++)
       if (sl[q] >= 0) lines[2 * sl[q] * ls + col] += o[q];
+  }
+}
+
+template <int TY>
+__device__ __forceinline__ void deriv_pixels_rt(bool reg, bool box, const CompF32 &cc, const WinDesc &w, int row,
+                                                const int *sl, float *lines, int ls, const float *tab, int side,
+                                                int bc0, int br0) {
+  if (reg) {
+    if (box) deriv_pixels<TY, true, true>(cc, w, row, sl, lines, ls, tab, side, bc0, br0);
+    else deriv_pixels<TY, true, false>(cc, w, row, sl, lines, ls, tab, side, bc0, br0);
+  } else {
+    if (box) deriv_pixels<TY, false, true>(cc, w, row, sl, lines, ls, tab, side, bc0, br0);
+    else deriv_pixels<TY, false, false>(cc, w, row, sl, lines, ls, tab, side, bc0, br0);
   }
 }
 
@@ -1373,13 +1436,14 @@ __global__ void __launch_bounds__(512) k_fast_deriv_r2c(FastArgs a, WinDesc w, F
     for (int q = 0; q < 5; q++) sl[2 + q] = q < npar[c] ? ss[cc.paramOffset + q] : -1;
     const float *tab = a.subTab + sub_base(a, b, c, win);
     const int bc0 = boxes[2 * c], br0 = boxes[2 * c + 1];
+    const bool box = rows_meet_box(cc, row, 1, br0, side);
     switch (cc.type) {
-      case F_SERSIC: deriv_pixels<F_SERSIC>(cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
-      case F_EXP: deriv_pixels<F_EXP>(cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
-      case F_GRING: deriv_pixels<F_GRING>(cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
-      case F_MOFFAT: deriv_pixels<F_MOFFAT>(cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
-      case F_GAUSS: deriv_pixels<F_GAUSS>(cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
-      case F_TILTEDSKY: deriv_pixels<F_TILTEDSKY>(cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
+      case F_SERSIC: deriv_pixels_rt<F_SERSIC>(w.isRegion, box, cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
+      case F_EXP: deriv_pixels_rt<F_EXP>(w.isRegion, box, cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
+      case F_GRING: deriv_pixels_rt<F_GRING>(w.isRegion, box, cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
+      case F_MOFFAT: deriv_pixels_rt<F_MOFFAT>(w.isRegion, box, cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
+      case F_GAUSS: deriv_pixels_rt<F_GAUSS>(w.isRegion, box, cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
+      case F_TILTEDSKY: deriv_pixels_rt<F_TILTEDSKY>(w.isRegion, box, cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
       default: break;
     }
   }
@@ -2129,13 +2193,14 @@ __global__ void __launch_bounds__(512) k_rag_eval_r2c(FastArgs a, RagArgs r) {
     if (!in_rows(cc.type)) continue;
     const float *tab = a.subTab + sub_base(a, k, c, 0);
     const int bc0 = boxes[2 * c], br0 = boxes[2 * c + 1], side = a.boxMain;
+    const bool box = rows_meet_box(cc, row, 1, br0, side);
     switch (cc.type) {
-      case F_SERSIC: eval_pixels<F_SERSIC>(cc, w, row, 1, M, ls, byM, bufA, tab, side, bc0, br0); break;
-      case F_EXP: eval_pixels<F_EXP>(cc, w, row, 1, M, ls, byM, bufA, tab, side, bc0, br0); break;
-      case F_GRING: eval_pixels<F_GRING>(cc, w, row, 1, M, ls, byM, bufA, tab, side, bc0, br0); break;
-      case F_MOFFAT: eval_pixels<F_MOFFAT>(cc, w, row, 1, M, ls, byM, bufA, tab, side, bc0, br0); break;
-      case F_GAUSS: eval_pixels<F_GAUSS>(cc, w, row, 1, M, ls, byM, bufA, tab, side, bc0, br0); break;
-      case F_TILTEDSKY: eval_pixels<F_TILTEDSKY>(cc, w, row, 1, M, ls, byM, bufA, tab, side, bc0, br0); break;
+      case F_SERSIC: eval_pixels_rt<F_SERSIC>(false, box, cc, w, row, 1, M, ls, byM, bufA, tab, side, bc0, br0); break;
+      case F_EXP: eval_pixels_rt<F_EXP>(false, box, cc, w, row, 1, M, ls, byM, bufA, tab, side, bc0, br0); break;
+      case F_GRING: eval_pixels_rt<F_GRING>(false, box, cc, w, row, 1, M, ls, byM, bufA, tab, side, bc0, br0); break;
+      case F_MOFFAT: eval_pixels_rt<F_MOFFAT>(false, box, cc, w, row, 1, M, ls, byM, bufA, tab, side, bc0, br0); break;
+      case F_GAUSS: eval_pixels_rt<F_GAUSS>(false, box, cc, w, row, 1, M, ls, byM, bufA, tab, side, bc0, br0); break;
+      case F_TILTEDSKY: eval_pixels_rt<F_TILTEDSKY>(false, box, cc, w, row, 1, M, ls, byM, bufA, tab, side, bc0, br0); break;
       default: break;
     }
   }
@@ -2211,13 +2276,14 @@ __global__ void __launch_bounds__(512) k_rag_deriv_r2c(FastArgs a, RagArgs r, co
     for (int q = 0; q < 5; q++) sl[2 + q] = q < npar[c] ? ss[cc.paramOffset + q] : -1;
     const float *tab = a.subTab + sub_base(a, k, c, 0);
     const int bc0 = boxes[2 * c], br0 = boxes[2 * c + 1], side = a.boxMain;
+    const bool box = rows_meet_box(cc, row, 1, br0, side);
     switch (cc.type) {
-      case F_SERSIC: deriv_pixels<F_SERSIC>(cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
-      case F_EXP: deriv_pixels<F_EXP>(cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
-      case F_GRING: deriv_pixels<F_GRING>(cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
-      case F_MOFFAT: deriv_pixels<F_MOFFAT>(cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
-      case F_GAUSS: deriv_pixels<F_GAUSS>(cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
-      case F_TILTEDSKY: deriv_pixels<F_TILTEDSKY>(cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
+      case F_SERSIC: deriv_pixels_rt<F_SERSIC>(false, box, cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
+      case F_EXP: deriv_pixels_rt<F_EXP>(false, box, cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
+      case F_GRING: deriv_pixels_rt<F_GRING>(false, box, cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
+      case F_MOFFAT: deriv_pixels_rt<F_MOFFAT>(false, box, cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
+      case F_GAUSS: deriv_pixels_rt<F_GAUSS>(false, box, cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
+      case F_TILTEDSKY: deriv_pixels_rt<F_TILTEDSKY>(false, box, cc, w, row, sl, lines, ls, tab, side, bc0, br0); break;
       default: break;
     }
   }
