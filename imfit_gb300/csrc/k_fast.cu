@@ -365,6 +365,7 @@ __device__ void subsample_pixels(const WinDesc &w, const CompF32 &cc, int side, 
 // counter for the final reduction.
 __global__ void __launch_bounds__(256) k_fast_setup(FastArgs a, WinDesc mw, WinDesc rw, int hasRegion) {
   pdl_wait();
+  pdl_trigger();  // dependents still wait for this grid to complete
   const int c = blockIdx.x, b = blockIdx.y;
   __shared__ CompF32 rec;
   setup_component(a, c, b, rec, c == 0);
@@ -385,6 +386,7 @@ __global__ void __launch_bounds__(256) k_fast_setup(FastArgs a, WinDesc mw, WinD
 // the function parameters).
 __global__ void __launch_bounds__(256) k_fast_subsample(FastArgs a, WinDesc w) {
   pdl_wait();
+  pdl_trigger();  // dependents still wait for this grid to complete
   const int b = blockIdx.z, c = blockIdx.y;
   const CompF32 cc = a.comps[b * a.nComp + c];
   if (!cc.subsample || !subsampling_type(cc.type)) return;
@@ -430,6 +432,7 @@ __device__ __forceinline__ void lattice_point(const CompF32 &cc, float x, float 
 
 __global__ void __launch_bounds__(256) k_fast_region_lattice(FastArgs a, WinDesc w) {
   pdl_wait();
+  pdl_trigger();  // dependents still wait for this grid to complete
   const int b = blockIdx.z, c = blockIdx.y;
   const CompF32 cc = a.comps[b * a.nComp + c];
   if (!cc.subsample || !subsampling_type(cc.type)) return;
@@ -456,6 +459,7 @@ __global__ void __launch_bounds__(256) k_fast_region_lattice(FastArgs a, WinDesc
 // shared lattice when there is one).
 __global__ void __launch_bounds__(256) k_fast_region_sub(FastArgs a, WinDesc w) {
   pdl_wait();
+  pdl_trigger();  // dependents still wait for this grid to complete
   const int b = blockIdx.z, c = blockIdx.y;
   const CompF32 cc = a.comps[b * a.nComp + c];
   if (!cc.subsample || !subsampling_type(cc.type)) return;
@@ -1812,7 +1816,10 @@ static cudaError_t launch_region_sub(const FastArgs &a, const WinDesc &rw, int n
     e = launch_pdl(k_fast_region_lattice, dim3((pts + 255) / 256, a.nComp, nBatch), dim3(256), 0, st, a, rw);
     if (e) return e;
   }
-  const int cap = std::max(1, 8 * 152 / std::max(a.nComp * nBatch, 1));
+  // about two CTAs per SM: the region's pipeline runs beside the main
+  // window's at a higher stream priority, and a full wave of these CTAs would
+  // hold the SMs the main window's model pass is waiting for
+  const int cap = std::max(1, 2 * 152 / std::max(a.nComp * nBatch, 1));
   const int n = std::max(1, std::min((a.boxReg * a.boxReg + 7) / 8, cap));
   return launch_pdl(k_fast_region_sub, dim3(n, a.nComp, nBatch), dim3(256), 0, st, a, rw);
 }

@@ -1477,7 +1477,8 @@ struct imfit_model_s {
       explicit Freeze(bool &x) : f(x), old(x) { f = true; }
       ~Freeze() { f = old; }
     } freeze(psStateFrozen);
-    auto it = tuned.find(B);
+    const int key = B;
+    auto it = tuned.find(key);
     if (it != tuned.end()) {
       tune = it->second;
       return 0;
@@ -1485,12 +1486,12 @@ struct imfit_model_s {
     if (stack.n && B != stack.n) {  // a subset of a stack: the whole stack's shape
       auto full = tuned.find(stack.n);
       tune = (full != tuned.end()) ? full->second : FastTune{};
-      tuned[B] = tune;
+      tuned[key] = tune;
       return 0;
     }
     if (hasFixedTune || !autotune) {
       tune = hasFixedTune ? fixedTune : FastTune{};
-      tuned[B] = tune;
+      tuned[key] = tune;
       return 0;
     }
     constexpr int kSamples = 4;
@@ -1511,9 +1512,13 @@ struct imfit_model_s {
       if (flush) cudaFree(flush);
       timing = timingWas;
     };
-    // Each candidate runs the way later calls will: replayed from a CUDA
-    // graph when graphs are on (launch costs and the programmatic-dependent
-    // overlap then match), else launched kernel by kernel.  Every timed
+    // Candidates are timed on the statistic + gradient evaluation (the one a
+    // fit repeats) whichever call triggers the tuning; statistic-only calls
+    // use the same plan and shapes, so a parameter vector gets the same
+    // statistic with or without its gradient.  Each candidate runs the way
+    // later calls will: replayed from a CUDA graph when graphs are on (launch
+    // costs and the programmatic-dependent overlap then match), else launched
+    // kernel by kernel.  Every timed
     // evaluation starts from an L2 cache that holds none of its data (a
     // 256 MiB write before it): a single-image step's working set fits in
     // L2, and shapes that win with warm data need not win without it.  Best
@@ -1529,7 +1534,7 @@ struct imfit_model_s {
         cudaGraph_t gr;
         e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
         if (e) return e;
-        cudaError_t e2 = fast_forward(p, a, B, dG != nullptr, stream);
+        cudaError_t e2 = fast_forward(p, a, B, true, stream);
         e = cudaStreamEndCapture(stream, &gr);
         if (e2) return e2;
         if (e) return e;
@@ -1537,7 +1542,7 @@ struct imfit_model_s {
         cudaGraphDestroy(gr);
         if (e) return e;
       }
-      auto run = [&]() { return ex ? cudaGraphLaunch(ex, stream) : fast_forward(p, a, B, dG != nullptr, stream); };
+      auto run = [&]() { return ex ? cudaGraphLaunch(ex, stream) : fast_forward(p, a, B, true, stream); };
       e = run();  // warm
       best = 1e30f;
       for (int trial = 0; trial < 3 && !e; trial++) {
@@ -1666,7 +1671,7 @@ struct imfit_model_s {
     release();
     if (e) return cuda_fail(e, "autotune");
     tune = bestT;
-    tuned[B] = tune;
+    tuned[key] = tune;
     return 0;
   }
 
@@ -1677,10 +1682,8 @@ struct imfit_model_s {
     if (stack.n && B != stack.n) return fail(IMFIT_E_ARG, "an image stack evaluates exactly one parameter vector per image");
     st = ensureFastCap(B);
     if (st) return st;
-    if (tuned.find(B) == tuned.end() || !(graph.exec && graph.nBatch == B)) {
-      st = autotuneFast(B, dP, dS, dG);
-      if (st) return st;
-    }
+    st = autotuneFast(B, dP, dS, dG);  // a lookup once this (B, gradient) pair is tuned
+    if (st) return st;
     const bool wantGrad = dG != nullptr;
     FastArgs a = fastArgs(dP, dS, dG ? dG : dGrad.p, modelOut);
     FastPlan p = fastPlan();
@@ -1787,10 +1790,8 @@ struct imfit_model_s {
     st = ensureFastCap(B);
     if (st) return st;
     if (!dP || !dS || !dA || !dBt) return fail(IMFIT_E_ARG, "JtWJ: null device buffer");
-    if (tuned.find(B) == tuned.end()) {
-      st = autotuneFast(B, dP, dS, nullptr);
-      if (st) return st;
-    }
+    st = autotuneFast(B, dP, dS, nullptr);
+    if (st) return st;
     // after the autotuner: its choice of FFT plan sets the derivative spectra's size
     st = ensureJtwjCap(B);
     if (st) return st;
@@ -2335,7 +2336,11 @@ int imfit_ModelObject_new(int device, imfit_model_t *out) {
   auto *m = new imfit_model_s();
   m->device = device;
   e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
-  if (!e) e = cudaStreamCreateWithFlags(&m->side, cudaStreamNonBlocking);
+  // the oversampled region's pipeline (side stream) finishes last when both
+  // windows' passes share the SMs: its CTAs go first
+  int prioLeast = 0, prioGreatest = 0;
+  if (!e) e = cudaDeviceGetStreamPriorityRange(&prioLeast, &prioGreatest);
+  if (!e) e = cudaStreamCreateWithPriority(&m->side, cudaStreamNonBlocking, prioGreatest);
 
   for (int i = 0; i < 2 && !e; i++) {
     e = cudaEventCreateWithFlags(&m->forkEv[i], cudaEventDisableTiming);
