@@ -1494,8 +1494,8 @@ struct imfit_model_s {
       tuned[key] = tune;
       return 0;
     }
-    constexpr int kSamples = 4;
-    cudaEvent_t ev[2 * kSamples];
+    constexpr int kMaxSamples = 16;
+    cudaEvent_t ev[2 * kMaxSamples];
     for (auto &x : ev)
       if (cudaEventCreate(&x)) return fail(IMFIT_E_CUDA, "autotune events");
     // L2-sized scratch written before each timed evaluation
@@ -1518,12 +1518,14 @@ struct imfit_model_s {
     // statistic with or without its gradient.  Each candidate runs the way
     // later calls will: replayed from a CUDA graph when graphs are on (launch
     // costs and the programmatic-dependent overlap then match), else launched
-    // kernel by kernel.  Every timed
-    // evaluation starts from an L2 cache that holds none of its data (a
-    // 256 MiB write before it): a single-image step's working set fits in
-    // L2, and shapes that win with warm data need not win without it.  Best
-    // of three trials of four such evaluations (the candidates differ by a
-    // few percent, comparable to the run-to-run noise of a single timing).
+    // kernel by kernel.  Every timed evaluation starts from an L2 cache that
+    // holds none of its data (a 256 MiB write before it): a single-image
+    // step's working set fits in L2, and shapes that win with warm data need
+    // not win without it.  A candidate's time is the best of three trials,
+    // each the sum over kSamples such evaluations, kSamples chosen so that a
+    // trial holds about 2 ms of evaluations (4 to 16): the candidates differ
+    // by a few percent, comparable to the noise of a single short evaluation.
+    int kSamples = 4;
     auto measure = [&](const FastTune &t, float &best) -> cudaError_t {
       tune = t;
       FastArgs a = fastArgs(dP, dS, dG ? dG : dGrad.p, nullptr);
@@ -1565,6 +1567,12 @@ struct imfit_model_s {
       return e;
     };
     cudaError_t e = cudaSuccess;
+    {
+      float ms = 0.f;
+      e = measure(FastTune{}, ms);
+      if (!e && ms > 0.f)
+        kSamples = std::min(kMaxSamples, std::max(4, (int)std::ceil(2.0f * (float)kSamples / ms)));
+    }
     // launch shapes for the current plan: row shapes with the automatic
     // column shape, then column shapes with the best row shape
     auto tuneShapes = [&](FastTune &bestT, float &bestMs) -> cudaError_t {
