@@ -31,6 +31,11 @@ _DP = ctypes.POINTER(ctypes.c_double)
 NORMAL_EQ_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
                                 ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), ctypes.c_void_p)
 
+# imfit_normal_eq_batch_fn: (B, X, active, statistics, A, b, user) -> status
+NORMAL_EQ_BATCH_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                      ctypes.POINTER(ctypes.c_ubyte), ctypes.POINTER(ctypes.c_double),
+                                      ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), ctypes.c_void_p)
+
 _SIGS = [
     ("imfit_ModelObject_new", _I, [_I, ctypes.POINTER(_P)]),
     ("imfit_ModelObject_delete", _I, [_P]),
@@ -96,6 +101,8 @@ _SIGS = [
     ("imfit_CutoutsJtWJ", _I, [_P, _I, ctypes.POINTER(_I), _DP, _DP, _DP, _DP]),
     ("imfit_MinimizeNormalEquations", _I, [_I, _DP, ctypes.POINTER(_I), _DP, _DP, _D, _I, NORMAL_EQ_FN, _P, _DP,
                                            ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)]),
+    ("imfit_MinimizeNormalEquationsBatch", _I, [_I, _I, _DP, ctypes.POINTER(_I), _DP, _DP, _D, _I,
+                                                NORMAL_EQ_BATCH_FN, _P, _DP, ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     ("imfit_SetFunctionOptionalParam", _I, [_P, _I, ctypes.c_char_p, ctypes.c_char_p]),
     ("imfit_Synchronize", _I, [_P]),
     ("imfit_GetStream", _I, [_P, ctypes.POINTER(_P)]),
@@ -209,6 +216,49 @@ def minimize_normal_equations(fun, x0, fixed=None, lower=None, upper=None, ftol=
     if rc != 0:
         raise RuntimeError(lib.imfit_LastError(None).decode())
     return dict(params=x, statistic=stat.value, niter=it.value, nev=nev.value, status=st.value)
+
+
+def minimize_normal_equations_batch(fun, X0, fixed=None, lower=None, upper=None, ftol=1e-8, max_iter=0):
+    """imfit_MinimizeNormalEquationsBatch: B independent problems stepped in
+    lockstep.  fun(X, active) -> (S, A, b) for the trial vectors X (B x n) and
+    the mask of running problems: S (B), A (B x n x n), b (B x n); rows of
+    inactive problems are ignored.  lower / upper: (B x n) or None.  Returns a
+    dict of arrays: params, statistic, niter, status."""
+    lib = load_library()
+    X = np.array(X0, dtype=float)
+    B, n = X.shape
+    fx = (_I * n)(*([0] * n if fixed is None else [int(v) for v in fixed]))
+    lo = _f64(np.asarray(lower, dtype=float).reshape(B, n)) if lower is not None else None
+    hi = _f64(np.asarray(upper, dtype=float).reshape(B, n)) if upper is not None else None
+    errors = []
+
+    @NORMAL_EQ_BATCH_FN
+    def cb(bb, xp, ap_, sp, ap, bp, user):
+        try:
+            act = np.ctypeslib.as_array(ap_, shape=(bb,)).astype(bool)
+            S, A, b = fun(np.ctypeslib.as_array(xp, shape=(bb, n)).copy(), act)
+            s_out = np.ctypeslib.as_array(sp, shape=(bb,))
+            a_out = np.ctypeslib.as_array(ap, shape=(bb, n * n))
+            b_out = np.ctypeslib.as_array(bp, shape=(bb, n))
+            s_out[act] = np.asarray(S, dtype=float)[act]
+            a_out[act] = np.asarray(A, dtype=float).reshape(bb, n * n)[act]
+            b_out[act] = np.asarray(b, dtype=float).reshape(bb, n)[act]
+            return 0
+        except Exception as e:  # reported after the driver returns
+            errors.append(e)
+            return -1
+
+    stats = np.zeros(B)
+    it = (_I * B)()
+    st = (_I * B)()
+    rc = lib.imfit_MinimizeNormalEquationsBatch(B, n, _dp(X), fx, _dp(lo) if lo is not None else None,
+                                                _dp(hi) if hi is not None else None, ftol, int(max_iter), cb, None,
+                                                _dp(stats), it, st)
+    if errors:
+        raise errors[0]
+    if rc != 0:
+        raise RuntimeError(lib.imfit_LastError(None).decode())
+    return dict(params=X, statistic=stats, niter=np.array(it[:]), status=np.array(st[:]))
 
 
 def _dp(a):

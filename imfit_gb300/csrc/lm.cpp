@@ -32,6 +32,9 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <condition_variable>
+#include <functional>
+#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -431,25 +434,76 @@ int settle(TrState &q, int n, double *x, const double *t, double St, const doubl
 
 }  // namespace
 
-// f(i) for i in [0, n) on up to 16 host threads (the problems of a batch are
-// independent: each step and acceptance touches only problem i's state);
-// serial for small batches.
-template <typename F>
-static void parallel_for(int n, const F &f) {
-  const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
-  const int nt = std::min(std::min(hw, 16), n / 64);
-  if (nt <= 1) {
-    for (int i = 0; i < n; i++) f(i);
-    return;
+// Host worker threads for the per-problem steps of a batch: created once per
+// batch fit and woken for each phase (two per round), instead of threads
+// created and joined per phase -- C5's 4096-problem fits run ~750 phases.
+// run(n, f) calls f(i) for i in [0, n); the problems of a batch are
+// independent (each step and acceptance touches only problem i's state).
+// Small phases run on the calling thread.
+class WorkPool {
+ public:
+  explicit WorkPool(int workers) {
+    for (int t = 0; t < workers; t++) th_.emplace_back([this]() { work(); });
   }
-  std::atomic<int> next(0);
-  std::vector<std::thread> pool;
-  pool.reserve(nt);
-  for (int t = 0; t < nt; t++)
-    pool.emplace_back([&]() {
-      for (int i = next.fetch_add(1); i < n; i = next.fetch_add(1)) f(i);
-    });
-  for (auto &th : pool) th.join();
+  ~WorkPool() {
+    {
+      std::lock_guard<std::mutex> lk(m_);
+      stop_ = true;
+    }
+    wake_.notify_all();
+    for (auto &t : th_) t.join();
+  }
+  void run(int n, const std::function<void(int)> &f) {
+    if (th_.empty() || n < kMinParallel) {
+      for (int i = 0; i < n; i++) f(i);
+      return;
+    }
+    {
+      std::lock_guard<std::mutex> lk(m_);
+      task_ = &f;
+      n_ = n;
+      next_.store(0);
+      busy_ = (int)th_.size();
+      gen_++;
+    }
+    wake_.notify_all();
+    for (int i = next_.fetch_add(1); i < n; i = next_.fetch_add(1)) f(i);
+    std::unique_lock<std::mutex> lk(m_);
+    idle_.wait(lk, [this]() { return busy_ == 0; });
+    task_ = nullptr;
+  }
+
+ private:
+  static constexpr int kMinParallel = 128;
+  void work() {
+    long seen = 0;
+    for (;;) {
+      std::unique_lock<std::mutex> lk(m_);
+      wake_.wait(lk, [&]() { return stop_ || gen_ != seen; });
+      if (stop_) return;
+      seen = gen_;
+      const std::function<void(int)> *f = task_;
+      const int n = n_;
+      lk.unlock();
+      for (int i = next_.fetch_add(1); i < n; i = next_.fetch_add(1)) (*f)(i);
+      lk.lock();
+      if (--busy_ == 0) idle_.notify_one();
+    }
+  }
+  std::vector<std::thread> th_;
+  std::mutex m_;
+  std::condition_variable wake_, idle_;
+  const std::function<void(int)> *task_ = nullptr;
+  int n_ = 0, busy_ = 0;
+  long gen_ = 0;
+  bool stop_ = false;
+  std::atomic<int> next_{0};
+};
+
+static int pool_workers(int B) {
+  if (B < 128) return 0;
+  const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+  return std::max(0, std::min(hw, 16) - 1);  // the calling thread takes part
 }
 
 int lm_minimize_batch(int B, int n, double *X, const int *fixed, const double *lower, const double *upper,
@@ -486,8 +540,9 @@ int lm_minimize_batch(int B, int n, double *X, const int *fixed, const double *l
   // rounds: one trial per running problem, evaluated together; a rejected
   // trial costs a round but no iteration (as mpfit's inner loop)
   const long maxRounds = 20L * set.maxIter + 100;
+  WorkPool pool(pool_workers(B));
   // the host steps visit only the problems still running (the last rounds of
-  // a large batch have few; below 64 of them parallel_for runs serially)
+  // a large batch have few; small phases run on this thread)
   std::vector<int> run;
   run.reserve(B);
   for (int i = 0; i < B; i++) live[i] = ps[i].done ? 0 : 1;
@@ -497,7 +552,7 @@ int lm_minimize_batch(int B, int n, double *X, const int *fixed, const double *l
       if (!ps[i].done) run.push_back(i);
     if (run.empty()) break;
     const int nr = (int)run.size();
-    parallel_for(nr, [&](int k) {
+    pool.run(nr, [&](int k) {
       const int i = run[k];
       TrState &q = ps[i];
       const int s = propose(q, n, X + (size_t)i * n, T.data() + (size_t)i * n, freeIdx, limits(i), set);
@@ -511,7 +566,7 @@ int lm_minimize_batch(int B, int n, double *X, const int *fixed, const double *l
     if (!any) break;
     st = eval(T.data(), live.data(), S.data(), A.data(), b.data());
     if (st) return st;
-    parallel_for(nr, [&](int k) {
+    pool.run(nr, [&](int k) {
       const int i = run[k];
       TrState &q = ps[i];
       if (!live[i]) return;

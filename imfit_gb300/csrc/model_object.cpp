@@ -2790,6 +2790,33 @@ int imfit_MinimizeNormalEquations(int n, double *params, const int *fixed, const
   return st < 0 ? st : 0;
 }
 
+int imfit_MinimizeNormalEquationsBatch(int B, int n, double *params, const int *fixed, const double *lower,
+                                       const double *upper, double ftol, int maxIter, imfit_normal_eq_batch_fn eval,
+                                       void *user, double *statistics, int *nIter, int *status) {
+  if (B < 1 || n < 1 || !params || !eval) {
+    imfit::set_global_error("MinimizeNormalEquationsBatch: bad arguments");
+    return IMFIT_E_ARG;
+  }
+  if (!(ftol > 0.0)) {
+    imfit::set_global_error("MinimizeNormalEquationsBatch: ftol must be positive");
+    return IMFIT_E_ARG;
+  }
+  LMSettings set;
+  set.ftol = ftol;
+  if (maxIter > 0) set.maxIter = maxIter;
+  std::vector<LMResult> res((size_t)B);
+  JtwjBatchEval ev = [eval, user, B](const double *X, const unsigned char *active, double *S, double *A,
+                                     double *b) { return eval(B, X, active, S, A, b, user); };
+  const int st = lm_minimize_batch(B, n, params, fixed, lower, upper, set, ev, res.data());
+  for (int i = 0; i < B; i++) {
+    if (statistics) statistics[i] = res[i].stat;
+    if (nIter) nIter[i] = res[i].nIter;
+    if (status) status[i] = res[i].status;
+  }
+  if (st < 0) imfit::set_global_error("MinimizeNormalEquationsBatch: the evaluator failed");
+  return st < 0 ? st : 0;
+}
+
 int imfit_BootstrapFitBatch(imfit_model_t m, int nSamples, const double *bestfit, const int *fixed,
                             const double *lower, const double *upper, double ftol, int maxIter, double *params,
                             double *statistics, int *nIter, int *status) {

@@ -247,6 +247,22 @@ typedef int (*imfit_normal_eq_fn)(const double *x, double *statistic, double *A,
 int imfit_MinimizeNormalEquations(int n, double *params, const int *fixed, const double *lower, const double *upper,
                                   double ftol, int maxIter, imfit_normal_eq_fn eval, void *user, double *statistic,
                                   int *nIter, int *nEval, int *status);
+/* The same driver over B independent problems of n parameters, stepped in
+ * lockstep (the form imfit_FitLMBatch uses for cutout batches): each round
+ * calls eval(B, X, active, S, A, b, user) once for the trial vectors X (B x n)
+ * of the problems still running (active[i] = 1; the others' rows must be left
+ * untouched), which fills S[i], A (B x n x n) and b (B x n).  params (B x n)
+ * holds the starts and receives the results; fixed (n) is shared, lower and
+ * upper (B x n) are per problem or NULL; statistics, nIter and status (B) may
+ * be NULL.  The host steps of a large batch run on a pool of worker threads.
+ * No counterpart in the reference (its fits are one at a time:
+ * core/bootstrap_errors.cpp:205-215, core/model_object_multimage.cpp:353,437).
+ * Errors: imfit_LastError(NULL). */
+typedef int (*imfit_normal_eq_batch_fn)(int B, const double *X, const unsigned char *active, double *statistics,
+                                        double *A, double *b, void *user);
+int imfit_MinimizeNormalEquationsBatch(int B, int n, double *params, const int *fixed, const double *lower,
+                                       const double *upper, double ftol, int maxIter, imfit_normal_eq_batch_fn eval,
+                                       void *user, double *statistics, int *nIter, int *status);
 /* Bootstrap refits, replacing the loop of BootstrapErrorsBase
  * (core/bootstrap_errors.cpp:160-240: MakeBootstrapSample, then LevMarFit from
  * the best-fit vector, per iteration): draws the next nSamples samples of the

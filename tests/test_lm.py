@@ -96,3 +96,36 @@ def test_parameter_without_effect_stays_put():
     assert r["params"][3] == 7.25 and r["status"] in (1, 2)
     ref = scipy_opt.least_squares(dev0, [4.0, 0.6, 0.4], jac=jac0, xtol=1e-15, ftol=1e-15, gtol=1e-15)
     assert np.allclose(r["params"][:3], ref.x, rtol=1e-6)
+
+
+def test_batch_matches_one_at_a_time():
+    """imfit_MinimizeNormalEquationsBatch over 256 decay problems (enough to
+    run the host steps on the worker pool; per-problem limits on half of
+    them, the offset held fixed in all) gives each problem exactly the
+    result of its own imfit_MinimizeNormalEquations fit: the problems are
+    stepped independently, only their evaluations are batched."""
+    from imfit_gb300 import minimize_normal_equations_batch
+    B = 256
+    probs = [_decay_problem(seed=100 + i) for i in range(B)]
+    funs = [_normal(dev, jac) for dev, jac, _ in probs]
+    rng = np.random.default_rng(7)
+    X0 = np.column_stack([rng.uniform(1.0, 20.0, B), rng.uniform(0.1, 3.0, B), np.full(B, 0.5)])
+    lo = np.tile([0.0, 0.0, -10.0], (B, 1))
+    hi = np.tile([100.0, 10.0, 10.0], (B, 1))
+    hi[::2, 1] = 0.6  # the rate limit binds for some of these
+    fixed = [0, 0, 1]
+
+    def batch_fun(X, active):
+        S, A, b = np.zeros(B), np.zeros((B, 3, 3)), np.zeros((B, 3))
+        for i in np.flatnonzero(active):
+            S[i], A[i], b[i] = funs[i](X[i])
+        return S, A, b
+
+    rb = minimize_normal_equations_batch(batch_fun, X0, fixed=fixed, lower=lo, upper=hi)
+    for i in range(B):
+        r = _lm()(funs[i], X0[i], fixed=fixed, lower=lo[i], upper=hi[i])
+        assert np.array_equal(rb["params"][i], r["params"]), (i, rb["params"][i], r["params"])
+        assert rb["statistic"][i] == r["statistic"] and rb["status"][i] == r["status"]
+        assert rb["niter"][i] == r["niter"]
+    assert np.all(rb["params"][:, 2] == 0.5)
+    assert np.any(rb["params"][::2, 1] == 0.6)
