@@ -359,10 +359,53 @@ __device__ void subsample_pixels(const WinDesc &w, const CompF32 &cc, int side, 
   }
 }
 
-// First kernel of an evaluation: CTA (c, b) sets up component c of parameter
-// vector b in FP64 and publishes the FP32 record, the subsample boxes of both
-// windows and, for c = 0, the background levels and a zeroed completion
-// counter for the final reduction.
+// First kernel of an evaluation, on grid (x, c, b): every CTA sets up
+// component c of parameter vector b in FP64 (each redundantly, so that no
+// CTA waits for another), CTA x = 0 publishes the FP32 record, the subsample
+// boxes of both windows and, for c = 0, the background levels and a zeroed
+// completion counter for the final reduction; then the CTAs of a subsampling
+// component fill the main window's subsample table, one warp per box pixel
+// (grid-stride over the CTAs of (c, b)): the average over the pixel's ns x ns
+// subsamples of the profile and of its 7 derivatives (X0, Y0, then the
+// function parameters).
+__global__ void __launch_bounds__(256) k_fast_setup_subsample(FastArgs a, WinDesc mw, WinDesc rw, int hasRegion) {
+  pdl_wait();
+  pdl_trigger();  // dependents still wait for this grid to complete
+  const int b = blockIdx.z, c = blockIdx.y;
+  __shared__ CompF32 rec;
+  __shared__ int box[2];
+  setup_component(a, c, b, rec, c == 0 && blockIdx.x == 0);
+  const bool sub = rec.subsample && subsampling_type(rec.type);
+  if (threadIdx.x == 0) {
+    if (sub) box_origin(mw, rec, a.boxMain, box[0], box[1]);
+    if (blockIdx.x == 0) {
+      a.comps[b * a.nComp + c] = rec;
+      if (c == 0 && a.done) a.done[b] = 0u;
+      if (sub) {
+        int *o = a.subBox + ((long)b * a.nComp + c) * 4;
+        o[0] = box[0];
+        o[1] = box[1];
+        if (hasRegion) box_origin(rw, rec, a.boxReg, o[2], o[3]);
+      }
+    }
+  }
+  __syncthreads();
+  if (!sub) return;
+  const CompF32 cc = rec;
+  float *tab = a.subTab + sub_base(a, b, c, 0);
+  const LatView none{nullptr, 0, 0, 0, 0};
+  switch (cc.type) {
+    case F_SERSIC: subsample_pixels<F_SERSIC>(mw, cc, a.boxMain, box[0], box[1], tab, none); break;
+    case F_EXP: subsample_pixels<F_EXP>(mw, cc, a.boxMain, box[0], box[1], tab, none); break;
+    case F_MOFFAT: subsample_pixels<F_MOFFAT>(mw, cc, a.boxMain, box[0], box[1], tab, none); break;
+    default: subsample_pixels<F_GAUSS>(mw, cc, a.boxMain, box[0], box[1], tab, none); break;
+  }
+}
+
+// With an oversampled region the set-up and the main window's table are two
+// kernels, so that the region's pipeline (side stream) can start after the
+// set-up alone: CTA (c, b) sets up component c of parameter vector b in FP64
+// and publishes what k_fast_setup_subsample's CTA x = 0 publishes.
 __global__ void __launch_bounds__(256) k_fast_setup(FastArgs a, WinDesc mw, WinDesc rw, int hasRegion) {
   pdl_wait();
   pdl_trigger();  // dependents still wait for this grid to complete
@@ -1792,6 +1835,17 @@ static void ensure_smem(K kern, size_t bytes) {
   allow_max_smem((const void *)kern);
 }
 
+// Set-up and main-window subsample table: CTAs per (component, vector) chosen
+// so that the grid is about one wave of 8 CTAs per SM, at most one warp per
+// box pixel.
+static cudaError_t launch_setup_subsample(const FastArgs &a, const WinDesc &mw, const WinDesc &rw, bool region,
+                                          int nBatch, cudaStream_t st) {
+  const int cap = std::max(1, 8 * 152 / std::max(a.nComp * nBatch, 1));
+  const int n = std::max(1, std::min((a.boxMain * a.boxMain + 7) / 8, cap));
+  return launch_pdl(k_fast_setup_subsample, dim3(n, a.nComp, nBatch), dim3(256), 0, st, a, mw, rw,
+                    region ? 1 : 0);
+}
+
 // Set-up: one CTA per (component, vector).
 static cudaError_t launch_setup(const FastArgs &a, const WinDesc &mw, const WinDesc &rw, bool region, int nBatch,
                                 cudaStream_t st) {
@@ -1963,14 +2017,20 @@ cudaError_t fast_forward(const FastPlan &p, const FastArgs &a, int nBatch, bool 
   if (!mks.panels) mks.count = nullptr;
   if (!rks.panels) rks.count = nullptr;
 
-  STAGE("setup", st, launch_setup(a, mw, rw, g.hasRegion != 0, nBatch, st));
+  // one kernel for the set-up and the main window's table, unless the
+  // region's pipeline waits to start after the set-up
+  if (g.hasRegion) {
+    STAGE("setup", st, launch_setup(a, mw, rw, true, nBatch, st));
+  } else {
+    STAGE("setup_subsample", st, launch_setup_subsample(a, mw, rw, false, nBatch, st));
+  }
   if (fork) {
     cudaError_t e = cudaEventRecord(p.fork0, st);
     if (!e) e = cudaStreamWaitEvent(rs, p.fork0, 0);
     if (e) return e;
   }
   if (g.hasRegion) STAGE("region_subsample", rs, launch_region_sub(a, rw, nBatch, rs));
-  STAGE("subsample", st, launch_subsample(a, mw, nBatch, st));
+  if (g.hasRegion) STAGE("subsample", st, launch_subsample(a, mw, nBatch, st));
   if (g.hasRegion) {
     if (los) STAGE("region_los_eval", rs, launch_los_eval(a, rw, nBatch, rks, rs));
     STAGE("region_eval_r2c", rs, launch_eval(a, rw, *p.Rx, nBatch, 1, tu, rs));
