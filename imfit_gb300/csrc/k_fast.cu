@@ -1171,11 +1171,12 @@ __global__ void __launch_bounds__(1024) k_fast_grad_rows(FastArgs a, WinDesc w, 
   const int M = plan.n, ls = M + 1;
   CompF32 *sc = reinterpret_cast<CompF32 *>(smem);
   int *boxes = reinterpret_cast<int *>(sc + kMaxComponents);
-  ffloat *gsm = reinterpret_cast<ffloat *>(boxes + 2 * kMaxComponents);
-  cplx<float> *bufX = reinterpret_cast<cplx<float> *>(gsm + kMaxParams);
+  cplx<float> *bufX = reinterpret_cast<cplx<float> *>(boxes + 2 * kMaxComponents);
   cplx<float> *bufA = bufX + rpb * ls;
   cplx<float> *bufB = bufA + rpb * ls;
-  __shared__ ffloat red[32][7];
+  // per-warp double-float sums of every parameter's term over the
+  // components: [warp][parameter]; added across warps once, at the end
+  ffloat *wpart = reinterpret_cast<ffloat *>(bufB + rpb * ls);
   const int nC = a.nComp, nP = a.nParams;
   for (int i = threadIdx.x; i < nC; i += blockDim.x) {
     sc[i] = a.comps[b * nC + i];
@@ -1183,7 +1184,7 @@ __global__ void __launch_bounds__(1024) k_fast_grad_rows(FastArgs a, WinDesc w, 
     boxes[2 * i] = o[0];
     boxes[2 * i + 1] = o[1];
   }
-  for (int i = threadIdx.x; i < nP; i += blockDim.x) gsm[i] = ffloat{0.f, 0.f};
+  for (int i = threadIdx.x; i < (blockDim.x >> 5) * nP; i += blockDim.x) wpart[i] = ffloat{0.f, 0.f};
   const int row0 = blockIdx.x * rpb;
   const int nl = min(rpb, w.rows - row0);
   const cplx<float> *spec = w.spec + (long)b * w.specBatch;
@@ -1201,7 +1202,7 @@ __global__ void __launch_bounds__(1024) k_fast_grad_rows(FastArgs a, WinDesc w, 
     __syncthreads();
     cplx<float> *Z = block_fft(bufA, bufB, plan, nl, ls, 1, +1, false);
     const float *rt = reinterpret_cast<const float *>(Z);  // r~ of (l, col) at rt[2*(l*ls) + col]
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int npix = nl * w.cols;
     if (w.losRt)
       for (int idx = threadIdx.x; idx < npix; idx += blockDim.x) {
@@ -1227,29 +1228,31 @@ __global__ void __launch_bounds__(1024) k_fast_grad_rows(FastArgs a, WinDesc w, 
           break;
         default: break;
       }
-      // CTA reduction of acc[0..6]: FP32 over the warp, double-float across warps
+      // FP32 over the warp, then into the warp's double-float parameter sums
+      // (no barrier: each warp owns its row of wpart)
 #pragma unroll
       for (int q = 0; q < 7; q++) acc[q] = warp_sum(acc[q]);
       if (lane == 0) {
-#pragma unroll
-        for (int q = 0; q < 7; q++) red[wid][q] = ff_make(acc[q]);
-      }
-      __syncthreads();
-      if (threadIdx.x < 7) {
-        ffloat t = {0.f, 0.f};
-        for (int i = 0; i < nw; i++) t = ff_add(t, red[i][threadIdx.x]);
-        const int q = threadIdx.x;
         const int npf = a.desc[c].nParams;
-        const int slot = q == 0 ? cc.x0Index : q == 1 ? cc.x0Index + 1 : (q - 2 < npf ? cc.paramOffset + q - 2 : -1);
-        if (slot >= 0) gsm[slot] = ff_add(gsm[slot], t);
+        ffloat *wp = wpart + wid * nP;
+#pragma unroll
+        for (int q = 0; q < 7; q++) {
+          const int slot = q == 0 ? cc.x0Index : q == 1 ? cc.x0Index + 1 : (q - 2 < npf ? cc.paramOffset + q - 2 : -1);
+          if (slot >= 0) wp[slot] = ff_add(wp[slot], ff_make(acc[q]));
+        }
       }
-      __syncthreads();
     }
   }
   __syncthreads();
   pdl_trigger();
+  // CTA partials: double-float across the warps, in warp order
+  const int nw = blockDim.x >> 5;
   float2 *out = gradPart + (long)b * nP * a.partStride + blockBase + blockIdx.x;
-  for (int i = threadIdx.x; i < nP; i += blockDim.x) out[(long)i * a.partStride] = ff_store(gsm[i]);
+  for (int i = threadIdx.x; i < nP; i += blockDim.x) {
+    ffloat t = {0.f, 0.f};
+    for (int v = 0; v < nw; v++) t = ff_add(t, wpart[v * nP + i]);
+    out[(long)i * a.partStride] = ff_store(t);
+  }
   if (doneTotal > 0) finish_cta(a, b, doneTotal, doneTotal);
 }
 
@@ -1895,7 +1898,7 @@ static cudaError_t launch_grad(const FastArgs &a, const WinDesc &w, const FFTLen
   const int M = L.half.n;
   const int rpb = tu.rowRpb;
   const size_t sm = sizeof(CompF32) * kMaxComponents + sizeof(int) * 2 * kMaxComponents +
-                    sizeof(ffloat) * kMaxParams + sizeof(cplx<float>) * 3 * rpb * (M + 1) + 16;
+                    sizeof(cplx<float>) * 3 * rpb * (M + 1) + sizeof(ffloat) * (tu.rowThreads / 32) * a.nParams + 16;
   ensure_smem(k_fast_grad_rows, sm);
   dim3 grid((w.rows + rpb - 1) / rpb, nBatch);
   return launch_pdl(k_fast_grad_rows, grid, dim3(tu.rowThreads), sm, st, a, w, plan32(L, true),
