@@ -325,10 +325,13 @@ int smooth_size(int n, bool even) {
 }
 
 // Radix orders the fast path's autotuner chooses among (the transform is the
-// same; the pass count, the work per pass and the twiddle traffic differ):
-//   0: 8s, then 4s and 2s, then the odd radices 3, 5, 7;
-//   1: the odd radices 7, 5, 3 first, then 8s, 4s, 2s;
-//   2: 4s (and a final 2) instead of 8s, then 3, 5, 7.
+// same; the pass count, the work per pass and the twiddle traffic differ);
+// each takes the listed radices greedily, as often as they divide:
+//   0: 8, 9, 4, 2, then 3, 5, 7;
+//   1: the odd radices 7, 5, 9, 3 first, then 8, 4, 2;
+//   2: 4 and 2 instead of 8, then 9, 3, 5, 7;
+//   kRadixPlain (the FP64 drop-in's plans): 8, 4, 2, 3, 5, 7 (no radix 9,
+//   whose 3 x 3 butterfly rounds differently from two radix-3 passes).
 int radix_schedule(int n, int *radix, int variant) {
   int np = 0;
   auto take = [&](int p) {

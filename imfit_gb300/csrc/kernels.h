@@ -85,8 +85,8 @@ int line_threads(int points);
 // smallest 7-smooth (2,3,5,7) integer >= n, optionally even
 int smooth_size(int n, bool even);
 
-// radix schedule of order `variant` (0: 8,4,2,3,5,7; 1: 7,5,3,8,4,2;
-// 2: 4,2,3,5,7); returns the number of passes or -1
+// radix schedule of order `variant` (0: 8,9,4,2,3,5,7; 1: 7,5,9,3,8,4,2;
+// 2: 4,2,9,3,5,7; kRadixPlain: 8,4,2,3,5,7); returns the number of passes or -1
 int radix_schedule(int n, int *radix, int variant = 0);
 constexpr int kRadixVariants = 3;
 // the `count` smallest 7-smooth lengths >= n within maxRatio * n; returns how many
@@ -318,10 +318,11 @@ struct FastTune {
 struct FastPlan {
   FastTune tune;
   StageTimer *timer = nullptr;
-  // second stream for the oversampled-region pipeline (null: run serially)
-  // and the events that fork it from / join it back to the main stream
+  // second stream for the oversampled-region pipeline (null: run serially),
+  // the event that forks it from the main stream after the set-up, and those
+  // that join it back at the end (statistic only / with the gradient)
   cudaStream_t side = nullptr;
-  cudaEvent_t fork0 = nullptr, join0 = nullptr, fork1 = nullptr, join1 = nullptr;
+  cudaEvent_t fork0 = nullptr, join0 = nullptr, join1 = nullptr;
   FastGeom g;
   const FFTLen *Lx, *Ly, *Rx, *Ry;  // main and region lengths
   const void *H, *Hr;               // FP32 PSF spectra (main, region)

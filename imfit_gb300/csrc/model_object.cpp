@@ -1447,7 +1447,6 @@ struct imfit_model_s {
     if (concurrent && !(timing && timingStage.empty())) {
       p.side = side;
       p.fork0 = forkEv[0];
-      p.fork1 = forkEv[1];
       p.join0 = joinEv[0];
       p.join1 = joinEv[1];
     }
