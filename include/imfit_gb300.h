@@ -329,9 +329,12 @@ int imfit_SetKernelTimingStage(imfit_model_t m, const char *stage);
 /* Run the oversampled-region pipeline on a second stream concurrently with
  * the main-window pipeline (default on). */
 int imfit_SetConcurrentRegions(imfit_model_t m, int enable);
-/* Autotuning of the fast path's launch shapes (default on): the first fast
- * call for each batch size times a few row/column CTA shapes on that call's
- * parameters and keeps the fastest.  GetLaunchShape reports the choice. */
+/* Autotuning of the fast path (default on): the first fast call for each
+ * batch size times FFT plans (padded lengths x radix orders; again for a batch
+ * four times larger) and row/column CTA shapes on that call's parameters --
+ * graph replays of the statistic + gradient evaluation, each from an empty
+ * L2 -- and keeps the fastest; statistic-only calls use the same choice.
+ * GetLaunchShape and GetFFTPlan report it. */
 int imfit_SetAutotune(imfit_model_t m, int enable);
 int imfit_GetLaunchShape(imfit_model_t m, int *rowsPerCta, int *rowThreads, int *colsPerCta);
 /* Pin the fast path's launch shape instead of autotuning (rowsPerCta < 0
