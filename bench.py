@@ -61,7 +61,23 @@ def parse():
     ap.add_argument("--no-graphs", action="store_true", help="launch kernels one by one (for profilers)")
     ap.add_argument("--jtwj", action="store_true",
                     help="time the forward-mode normal equations (J^T W J, J^T W dev) instead of the gradient")
+    ap.add_argument("--fft-plan", default=None, metavar="CAND,ORDER",
+                    help="pin the FFT plan (padded-length candidate, radix order) instead of autotuning it; "
+                         "profiling runs use the plan a timed run reported (launch_shape.pin)")
+    ap.add_argument("--launch-shape", default=None, metavar="RPB,THREADS,CPB,CTHREADS",
+                    help="pin the launch shape (rows per CTA, row threads, columns per CTA, column threads)")
     return ap.parse_args()
+
+
+def apply_pins(m, args):
+    """Fixed FFT plan / launch shape from the command line (profiling runs:
+    under a profiler the autotuner's timings, and so its choices, differ)."""
+    if args.fft_plan:
+        c, o = (int(v) for v in args.fft_plan.split(","))
+        m.set_fft_plan(c, o)
+    if args.launch_shape:
+        r, t, c, ct = (int(v) for v in args.launch_shape.split(","))
+        m.set_launch_shape(r, t, c, ct)
 
 
 def measured_profile(config, stage):
@@ -459,6 +475,7 @@ def run_gpu(args, rank, local_rank, world):
     wl = workload(args.config, args.batch)
     workloads.synthesize(wl, lambda: imfit_gb300.ModelObject(local_rank))
     m = workloads.configure(imfit_gb300.ModelObject(local_rank), wl)
+    apply_pins(m, args)
     nP = wl.n_params
     stream = torch.cuda.ExternalStream(m.stream(), device=dev)
     p0 = np.array(wl.start, dtype=np.float64)
@@ -823,6 +840,7 @@ def run_jtwj(args, rank, local_rank, world):
     wl = workload(args.config, args.batch)
     workloads.synthesize(wl, lambda: imfit_gb300.ModelObject(local_rank))
     m = workloads.configure(imfit_gb300.ModelObject(local_rank), wl)
+    apply_pins(m, args)
     nP = wl.n_params
     P = np.array(wl.batch if wl.batch is not None else [wl.start], dtype=np.float64)
     B = P.shape[0]

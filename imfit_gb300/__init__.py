@@ -103,6 +103,7 @@ _SIGS = [
                                            ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     ("imfit_MinimizeNormalEquationsBatch", _I, [_I, _I, _DP, ctypes.POINTER(_I), _DP, _DP, _D, _I,
                                                 NORMAL_EQ_BATCH_FN, _P, _DP, ctypes.POINTER(_I), ctypes.POINTER(_I)]),
+    ("imfit_GetTuning", _I, [_P] + [ctypes.POINTER(_I)] * 6),
     ("imfit_SetFunctionOptionalParam", _I, [_P, _I, ctypes.c_char_p, ctypes.c_char_p]),
     ("imfit_Synchronize", _I, [_P]),
     ("imfit_GetStream", _I, [_P, ctypes.POINTER(_P)]),
@@ -664,9 +665,14 @@ class ModelObject:
         a, b, c = _I(), _I(), _I()
         self._ck(self.lib.imfit_GetLaunchShape(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
         lx, ly, order = self.fft_plan()
-        return {"rows_per_cta": a.value, "row_threads": b.value, "cols_per_cta": c.value, "Lx": lx, "Ly": ly,
+        t = [_I() for _ in range(6)]
+        self._ck(self.lib.imfit_GetTuning(self.h, *[ctypes.byref(v) for v in t]))
+        return {"rows_per_cta": a.value, "row_threads": b.value, "cols_per_cta": c.value,
+                "col_threads": t[5].value, "Lx": lx, "Ly": ly, "fft_candidate": t[0].value,
                 "radix_order": order, "row_radices": radix_schedule(lx // 2, order) if lx else [],
-                "col_radices": radix_schedule(ly, order) if ly else []}
+                "col_radices": radix_schedule(ly, order) if ly else [],
+                "pin": {"fft_plan": f"{t[0].value},{t[1].value}",
+                        "launch_shape": f"{t[2].value},{t[3].value},{t[4].value},{t[5].value}"}}
 
     def kernel_times(self):
         """[(kernel name, ms)] of the most recent fast evaluation."""

@@ -2980,6 +2980,18 @@ int imfit_GetFFTPlan(imfit_model_t m, int *Lx, int *Ly, int *radixOrder) {
   return 0;
 }
 
+int imfit_GetTuning(imfit_model_t m, int *fftCandidate, int *radixOrder, int *rowsPerCta, int *rowThreads,
+                    int *colsPerCta, int *colThreads) {
+  GET(m);
+  if (fftCandidate) *fftCandidate = m->fftCand;
+  if (radixOrder) *radixOrder = m->fftVariant;
+  if (rowsPerCta) *rowsPerCta = m->tune.rowRpb;
+  if (rowThreads) *rowThreads = m->tune.rowThreads;
+  if (colsPerCta) *colsPerCta = m->tune.colCpb;
+  if (colThreads) *colThreads = m->tune.colThreads;
+  return 0;
+}
+
 int imfit_GetLaunchShape(imfit_model_t m, int *rowRpb, int *rowThreads, int *colCpb) {
   GET(m);
   if (rowRpb) *rowRpb = m->tune.rowRpb;

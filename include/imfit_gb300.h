@@ -359,6 +359,13 @@ int imfit_MeasureSfuRate(int device, double *opsPerSecond);
  * in use (Lx, Ly of the main window) and the order. */
 int imfit_SetFFTPlan(imfit_model_t m, int candidate, int radixOrder);
 int imfit_GetFFTPlan(imfit_model_t m, int *Lx, int *Ly, int *radixOrder);
+/* Everything the tuning chose, in the arguments SetFFTPlan and SetLaunchShape
+ * take (so that a run can be repeated with the same plan and shape, e.g.
+ * under a profiler): padded-length candidate, radix order, rows per row CTA,
+ * threads per row CTA, columns per column CTA, threads per column CTA (0:
+ * automatic).  Any pointer may be NULL. */
+int imfit_GetTuning(imfit_model_t m, int *fftCandidate, int *radixOrder, int *rowsPerCta, int *rowThreads,
+                    int *colsPerCta, int *colThreads);
 /* Page-locked host memory for the host-buffer entry points (cudaMallocHost). */
 int imfit_HostAlloc(unsigned long bytes, void **ptr);
 int imfit_HostFree(void *ptr);
